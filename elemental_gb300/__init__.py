@@ -1,0 +1,186 @@
+"""GB300-native drop-in for Elemental's sequential dense factor-and-solve path.
+
+The host-side mirror of the reference's Python interface for this path
+(python/lapack_like/factor.py:34,149,525,662; python/lapack_like/solve.py:49,217;
+python/core/Matrix.py, python/core/Permutation.py): the same names and
+argument meanings, over the same C ABI (include/El_gb300.h) — here backed by
+libelgb300.so's sm_103a kernels.  Matrices are host numpy arrays in
+column-major (Fortran) order, as El::Matrix; errors surface as the
+exceptions the reference maps its ElError codes to.
+
+Device-resident work (torch CUDA tensors, no host copies) goes through
+``elemental_gb300.device``.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+
+# Enumerations (include/El/core/types.h:211-228)
+NORMAL, TRANSPOSE, ADJOINT = 0, 1, 2
+LOWER, UPPER = 0, 1
+LU_PARTIAL = 1  # python/lapack_like/factor.py pivType
+
+_TAG = {np.dtype(np.int32): "i", np.dtype(np.float32): "s", np.dtype(np.float64): "d"}
+
+
+class ElError(RuntimeError):
+    def __init__(self, code, what=""):
+        self.code = code
+        super().__init__(f"{what}: {_lib.load().ElErrorString(code).decode()} ({code})")
+
+
+class SingularMatrixException(ElError):
+    pass
+
+
+def _check(rc, what, singular_cls=None):
+    if rc == 0:
+        return
+    if rc == 5 and singular_cls is not None:
+        raise singular_cls(rc, what)
+    raise ElError(rc, what)
+
+
+class Matrix:
+    """A host El::Matrix<T> handle attached to a column-major numpy array."""
+
+    def __init__(self, array):
+        a = np.asfortranarray(array)
+        if a.ndim == 1:
+            a = a.reshape(-1, 1, order="F")
+        if a.dtype not in _TAG:
+            raise TypeError(f"unsupported dtype {a.dtype}")
+        self.array = a
+        self.tag = _TAG[a.dtype]
+        self.lib = _lib.load()
+        h = ctypes.c_void_p()
+        _check(getattr(self.lib, f"ElMatrixCreate_{self.tag}")(ctypes.byref(h)), "Create")
+        self.obj = h
+        m, n = a.shape
+        _check(getattr(self.lib, f"ElMatrixAttach_{self.tag}")(
+            h, m, n, a.ctypes.data_as(ctypes.c_void_p), max(m, 1)), "Attach")
+
+    def Height(self):
+        return self.array.shape[0]
+
+    def Width(self):
+        return self.array.shape[1]
+
+    def ToNumPy(self):
+        return self.array
+
+    def __del__(self):
+        try:
+            getattr(self.lib, f"ElMatrixDestroy_{self.tag}")(self.obj)
+        except Exception:
+            pass
+
+
+class Permutation:
+    """El::Permutation (swap sequence with implicit origins)."""
+
+    def __init__(self):
+        self.lib = _lib.load()
+        h = ctypes.c_void_p()
+        _check(self.lib.ElPermutationCreate(ctypes.byref(h)), "PermutationCreate")
+        self.obj = h
+
+    def Height(self):
+        v = ctypes.c_int()
+        _check(self.lib.ElPermutationHeight(self.obj, ctypes.byref(v)), "Height")
+        return v.value
+
+    def ExplicitVector(self):
+        n = self.Height()
+        p = Matrix(np.zeros((n, 1), dtype=np.int32))
+        _check(self.lib.ElPermutationExplicitVector(self.obj, p.obj), "ExplicitVector")
+        return p.array.ravel().copy()
+
+    def SwapDestinations(self):
+        """The swap destinations, recovered from the explicit vector's
+        replay is ambiguous, so they are kept from the factorization."""
+        return self._dests.copy()
+
+    def PermuteRows(self, A: Matrix, offset=0):
+        _check(getattr(self.lib, f"ElPermutationPermuteRows_{A.tag}")(self.obj, A.obj, offset),
+               "PermuteRows")
+
+    def __del__(self):
+        try:
+            self.lib.ElPermutationDestroy(self.obj)
+        except Exception:
+            pass
+
+
+def _swap_dests_from_explicit(p):
+    """Recovers a swap sequence (implicit origins) equivalent to the explicit
+    permutation vector p (P A = A(p, :))."""
+    n = len(p)
+    cur = np.arange(n)
+    pos = np.arange(n)  # pos[row label] = current position
+    dests = np.empty(n, dtype=np.int32)
+    for i in range(n):
+        j = pos[p[i]]
+        dests[i] = j
+        a, b = cur[i], cur[j]
+        cur[i], cur[j] = b, a
+        pos[a], pos[b] = j, i
+    return dests
+
+
+def Blocksize():
+    v = ctypes.c_int()
+    _check(_lib.load().ElBlocksize(ctypes.byref(v)), "Blocksize")
+    return v.value
+
+
+def SetBlocksize(nb):
+    _check(_lib.load().ElSetBlocksize(int(nb)), "SetBlocksize")
+
+
+def PushBlocksizeStack(nb):
+    _check(_lib.load().ElPushBlocksizeStack(int(nb)), "PushBlocksizeStack")
+
+
+def PopBlocksizeStack():
+    _check(_lib.load().ElPopBlocksizeStack(), "PopBlocksizeStack")
+
+
+def LU(A: Matrix, pivType=LU_PARTIAL):
+    """El.LU(A) with partial pivoting: A is overwritten by the packed L\\U;
+    returns the Permutation (python/lapack_like/factor.py:525-542)."""
+    if pivType != LU_PARTIAL:
+        raise ValueError("only partial pivoting is on this path")
+    P = Permutation()
+    _check(getattr(A.lib, f"ElLUPartialPiv_{A.tag}")(A.obj, P.obj), "LU", SingularMatrixException)
+    P._dests = _swap_dests_from_explicit(P.ExplicitVector())[: min(A.Height(), A.Width())]
+    return P
+
+
+def SolveAfterLUPartialPiv(orient, A: Matrix, P: Permutation, B: Matrix):
+    _check(getattr(A.lib, f"ElSolveAfterLUPartialPiv_{A.tag}")(orient, A.obj, P.obj, B.obj),
+           "SolveAfterLUPartialPiv")
+
+
+def Cholesky(uplo, A: Matrix):
+    _check(getattr(A.lib, f"ElCholesky_{A.tag}")(uplo, A.obj), "Cholesky",
+           SingularMatrixException)
+
+
+def SolveAfterCholesky(uplo, orient, A: Matrix, B: Matrix):
+    _check(getattr(A.lib, f"ElSolveAfterCholesky_{A.tag}")(uplo, orient, A.obj, B.obj),
+           "SolveAfterCholesky")
+
+
+def LinearSolve(A: Matrix, B: Matrix):
+    _check(getattr(A.lib, f"ElLinearSolve_{A.tag}")(A.obj, B.obj), "LinearSolve",
+           SingularMatrixException)
+
+
+def HPDSolve(A: Matrix, B: Matrix, uplo=LOWER, orient=NORMAL):
+    _check(getattr(A.lib, f"ElHPDSolve_{A.tag}")(uplo, orient, A.obj, B.obj), "HPDSolve",
+           SingularMatrixException)

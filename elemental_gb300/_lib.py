@@ -1,0 +1,116 @@
+"""Loads libelgb300.so (built in-tree by elemental_gb300.build) and declares
+the ctypes signatures of its two C interfaces: the Elemental-compatible one
+(include/El_gb300.h) and the device-level one (include/elgb300.h).
+
+There is no fallback: if the library is missing or fails to load, importing
+raises, so nothing silently runs on the CPU.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from .build import LIB
+
+_lib = None
+
+c_int, c_double, c_void_p, c_char_p = ctypes.c_int, ctypes.c_double, ctypes.c_void_p, ctypes.c_char_p
+c_ll = ctypes.c_longlong
+P = ctypes.POINTER
+
+
+def _sig(lib, name, res, *args):
+    f = getattr(lib, name)
+    f.restype = res
+    f.argtypes = list(args)
+
+
+def load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB):
+        raise ImportError(
+            f"libelgb300.so not built ({LIB}); run "
+            "`python -c 'import __graft_entry__ as g; g.build()'` first")
+    lib = ctypes.CDLL(LIB, mode=ctypes.RTLD_GLOBAL)
+    vp = c_void_p
+    # device-level interface
+    _sig(lib, "ElGBCreate", c_int, P(vp), c_int)
+    _sig(lib, "ElGBDestroy", c_int, vp)
+    _sig(lib, "ElGBSetStream", c_int, vp, vp)
+    _sig(lib, "ElGBSynchronize", c_int, vp)
+    _sig(lib, "ElGBStatus", c_int, vp, P(c_int), P(c_int))
+    _sig(lib, "ElGBBlocksize", c_int)
+    _sig(lib, "ElGBSetBlocksize", c_int, c_int)
+    _sig(lib, "ElGBLaunchCount", c_ll, vp)
+    for s in ("d", "s"):
+        _sig(lib, f"ElGBLUPartialPiv_{s}", c_int, vp, c_int, c_int, vp, c_int, vp, c_int)
+        _sig(lib, f"ElGBSolveAfterLUPartialPiv_{s}", c_int, vp, c_int, c_int, vp, c_int, vp,
+             c_int, vp, c_int)
+        _sig(lib, f"ElGBCholesky_{s}", c_int, vp, c_int, c_int, vp, c_int, c_int)
+        _sig(lib, f"ElGBSolveAfterCholesky_{s}", c_int, vp, c_int, c_int, vp, c_int, c_int, vp,
+             c_int)
+        _sig(lib, f"ElGBLinearSolve_{s}", c_int, vp, c_int, vp, c_int, c_int, vp, c_int, c_int)
+        _sig(lib, f"ElGBHPDSolve_{s}", c_int, vp, c_int, c_int, vp, c_int, c_int, vp, c_int,
+             c_int)
+    _sig(lib, "ElGBResidual_d", c_int, vp, c_int, c_int, vp, c_int, vp, c_int, vp, c_int, vp,
+         c_int)
+    _sig(lib, "ElGBBackwardError_d", c_int, vp, c_int, c_int, vp, c_int, vp, c_int, vp, c_int,
+         P(c_double))
+    _sig(lib, "ElGBProbeFP64Peak", c_int, vp, P(c_double))
+    # Elemental-compatible interface
+    for s in ("i", "s", "d"):
+        _sig(lib, f"ElMatrixCreate_{s}", c_int, P(vp))
+        _sig(lib, f"ElMatrixDestroy_{s}", c_int, vp)
+        _sig(lib, f"ElMatrixAttach_{s}", c_int, vp, c_int, c_int, vp, c_int)
+        _sig(lib, f"ElMatrixLockedAttach_{s}", c_int, vp, c_int, c_int, vp, c_int)
+        _sig(lib, f"ElMatrixResize_{s}", c_int, vp, c_int, c_int)
+        _sig(lib, f"ElMatrixHeight_{s}", c_int, vp, P(c_int))
+        _sig(lib, f"ElMatrixWidth_{s}", c_int, vp, P(c_int))
+        _sig(lib, f"ElMatrixLDim_{s}", c_int, vp, P(c_int))
+        _sig(lib, f"ElMatrixBuffer_{s}", c_int, vp, P(vp))
+    _sig(lib, "ElPermutationCreate", c_int, P(vp))
+    _sig(lib, "ElPermutationDestroy", c_int, vp)
+    _sig(lib, "ElPermutationHeight", c_int, vp, P(c_int))
+    _sig(lib, "ElPermutationExplicitVector", c_int, vp, vp)
+    _sig(lib, "ElPermutationPermuteRows_d", c_int, vp, vp, c_int)
+    _sig(lib, "ElPermutationPermuteRows_s", c_int, vp, vp, c_int)
+    _sig(lib, "ElErrorString", c_char_p, c_int)
+    _sig(lib, "ElBlocksize", c_int, P(c_int))
+    _sig(lib, "ElSetBlocksize", c_int, c_int)
+    _sig(lib, "ElPushBlocksizeStack", c_int, c_int)
+    _sig(lib, "ElPopBlocksizeStack", c_int)
+    for s in ("s", "d"):
+        _sig(lib, f"ElLUPartialPiv_{s}", c_int, vp, vp)
+        _sig(lib, f"ElSolveAfterLUPartialPiv_{s}", c_int, c_int, vp, vp, vp)
+        _sig(lib, f"ElCholesky_{s}", c_int, c_int, vp)
+        _sig(lib, f"ElSolveAfterCholesky_{s}", c_int, c_int, c_int, vp, vp)
+        _sig(lib, f"ElLinearSolve_{s}", c_int, vp, vp)
+        _sig(lib, f"ElHPDSolve_{s}", c_int, c_int, c_int, vp, vp)
+    _lib = lib
+    return lib
+
+
+def exported_symbols_from_headers():
+    """Names of every function declared in include/*.h (for export checks)."""
+    import re
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    inc = os.path.join(root, "include")
+    names = set()
+    for f in sorted(os.listdir(inc)):
+        if not f.endswith(".h"):
+            continue
+        txt = open(os.path.join(inc, f)).read()
+        txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+        # expand the per-type macro blocks
+        for m in re.finditer(r"#define (EL_GB_\w+)\(S, T\)(.*?)\n(?=\S)", txt, flags=re.S):
+            body = m.group(2)
+            for use in re.finditer(r"^" + m.group(1) + r"\((\w), [\w ]+\)", txt, flags=re.M):
+                for fn in re.findall(r"(\w+)##S\(", body):
+                    names.add(fn + use.group(1))
+        for fn in re.findall(r"^\s*(?:const\s+)?\w[\w\s\*]*?\b(El\w+)\s*\(", txt, flags=re.M):
+            if "##" not in fn:
+                names.add(fn)
+    return sorted(names)

@@ -1,0 +1,711 @@
+// Host drivers of the GB300 dense factor-and-solve path and the device-level
+// C ABI declared in include/elgb300.h.  The drivers reproduce the blocking
+// and the order of operations of the reference's sequential path (cited per
+// routine) on top of the kernels in lu_kernels.cu.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <vector>
+
+#include "../../include/elgb300.h"
+#include "driver.h"
+#include "kernels.h"
+
+namespace elgb {
+
+static int g_blocksize = 128;  // El's default blocksize (src/core/environment.cpp:183)
+
+int to_el_error(cudaError_t e) { return e == cudaSuccess ? kElSuccess : kElRuntimeError; }
+
+Context::~Context() {
+  if (arena) cudaFree(arena);
+  if (status) cudaFree(status);
+  if (h_status) cudaFreeHost(h_status);
+  if (own_stream) cudaStreamDestroy(own_stream);
+}
+
+cudaError_t Context::ensure(size_t bytes) {
+  if (bytes <= arena_bytes) return cudaSuccess;
+  cudaError_t e = cudaStreamSynchronize(stream);
+  if (e != cudaSuccess) return e;
+  if (arena) cudaFree(arena);
+  arena = nullptr;
+  arena_bytes = 0;
+  size_t want = std::max(bytes, arena_bytes * 2);
+  e = cudaMalloc(&arena, want);
+  if (e != cudaSuccess) {
+    e = cudaMalloc(&arena, bytes);
+    if (e != cudaSuccess) return e;
+    want = bytes;
+  }
+  arena_bytes = want;
+  return cudaSuccess;
+}
+
+cudaError_t Context::begin_call() {
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) return e;
+  return cudaMemsetAsync(status, 0, sizeof(DevStatus), stream);
+}
+
+// Bump allocator over the context arena, reset per call.
+struct Carver {
+  char* base;
+  size_t off = 0, cap;
+  explicit Carver(Context* c) : base(static_cast<char*>(c->arena)), cap(c->arena_bytes) {}
+  template <typename T>
+  T* take(size_t count) {
+    off = (off + 255) & ~size_t(255);
+    T* p = reinterpret_cast<T*>(base + off);
+    off += count * sizeof(T);
+    return off <= cap ? p : nullptr;
+  }
+};
+
+static size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+template <typename T>
+static size_t panel_scratch_bytes(int maxG) {
+  return align256(sizeof(unsigned)) + align256(2 * maxG * sizeof(T)) +
+         align256(2 * maxG * sizeof(int)) + align256(2 * maxG * 32 * sizeof(T)) +
+         align256(2 * 32 * sizeof(T));
+}
+
+template <typename T>
+static PanelScratch<T> carve_panel(Carver& cv, int maxG) {
+  PanelScratch<T> s;
+  s.bar = cv.take<unsigned>(1);
+  s.cand_val = cv.take<T>(2 * maxG);
+  s.cand_row = cv.take<int>(2 * maxG);
+  s.cand_data = cv.take<T>(2 * (size_t)maxG * 32);
+  s.diag_data = cv.take<T>(2 * 32);
+  s.maxG = maxG;
+  return s;
+}
+
+#define ELGB_CHECK(expr, nk)                   \
+  do {                                          \
+    cudaError_t e_ = (expr);                    \
+    if (e_ != cudaSuccess) return e_;           \
+    ctx->launches += (nk);                      \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// LU with partial pivoting
+// ---------------------------------------------------------------------------
+template <typename T>
+struct LuState {
+  Context* ctx;
+  T* A;
+  long lda;
+  int m, n;
+  int* ipiv;           // absolute swap destinations, device
+  PanelScratch<T> ps;
+  int* pairs;          // 4 * pairs_cap ints
+  int* pair_count;
+  int pairs_cap;
+  T* Bc;               // companion block receiving the same row operations
+  long ldbc;           // (RowEchelon's B, src/lapack_like/solve/Linear.cpp:62-71)
+  int nbc;
+};
+
+// Blocked TRSM, left / lower / unit: B := L11^{-1} B with L11 nb x nb (any
+// nb): 128-row diagonal solves plus GEMM updates of the rows below.
+template <typename T>
+static cudaError_t trsm_llnu(Context* ctx, const T* L, long ldl, int nb, T* Bm, long ldb,
+                             int ncols) {
+  for (int i0 = 0; i0 < nb; i0 += 128) {
+    const int ib = std::min(128, nb - i0);
+    ELGB_CHECK(launch_trsm_block<T>(L + i0 + (long)i0 * ldl, ldl, Bm + i0, ldb, ib, ncols,
+                                    true, true, false, false, ctx->stream), 1);
+    const int rest = nb - i0 - ib;
+    if (rest > 0)
+      ELGB_CHECK(launch_gemm_simt<T>(false, false, rest, ncols, ib, T(-1),
+                                     L + (i0 + ib) + (long)i0 * ldl, ldl, Bm + i0, ldb, T(1),
+                                     Bm + i0 + ib, ldb, 0, ctx->stream), 1);
+  }
+  return cudaSuccess;
+}
+
+// Row interchanges of the swaps ipiv[c0 .. c0+w) (rows c0.. of A) applied to
+// the column ranges [a0, a1) and [b0, b1) of A and, if requested, to the
+// companion block.
+template <typename T>
+static cudaError_t apply_swaps(LuState<T>& s, int c0, int w, int a0, int a1, int b0, int b1,
+                               bool companion) {
+  Context* ctx = s.ctx;
+  ELGB_CHECK(launch_build_swap_pairs(s.ipiv + c0, c0, w, s.pairs, s.pair_count, ctx->stream),
+             1);
+  if ((a1 > a0) || (b1 > b0))
+    ELGB_CHECK(launch_apply_swap_pairs<T>(s.A, s.lda, a0, a1, b0, b1, s.pairs, s.pair_count,
+                                          w, ctx->stream), 1);
+  if (companion && s.Bc && s.nbc > 0)
+    ELGB_CHECK(launch_apply_swap_pairs<T>(s.Bc, s.ldbc, 0, s.nbc, 0, 0, s.pairs, s.pair_count,
+                                          w, ctx->stream), 1);
+  return cudaSuccess;
+}
+
+// Recursive panel factorization of columns [c0, c0 + w), rows [c0, m):
+// left half, its swaps / TRSM / GEMM onto the right half, right half, then
+// the right half's swaps back onto the left half.  Leaves of <= 32 columns
+// go to the cooperative getf2 kernel.
+template <typename T>
+static cudaError_t panel_rec(LuState<T>& s, int c0, int w) {
+  Context* ctx = s.ctx;
+  if (w <= 32) {
+    ELGB_CHECK(launch_getf2_panel<T>(s.A + c0 + (long)c0 * s.lda, s.lda, s.m - c0, w,
+                                     s.ipiv + c0, c0, c0, s.ps, ctx->status, ctx->num_sms,
+                                     ctx->stream), 2);
+    return cudaSuccess;
+  }
+  int w1 = (w / 2 + 31) / 32 * 32;
+  if (w1 >= w) w1 = w - 32;
+  const int w2 = w - w1;
+  cudaError_t e = panel_rec(s, c0, w1);
+  if (e != cudaSuccess) return e;
+  e = apply_swaps(s, c0, w1, c0 + w1, c0 + w, 0, 0, false);
+  if (e != cudaSuccess) return e;
+  T* A11 = s.A + c0 + (long)c0 * s.lda;
+  T* A12 = s.A + c0 + (long)(c0 + w1) * s.lda;
+  T* A21 = s.A + (c0 + w1) + (long)c0 * s.lda;
+  T* A22 = s.A + (c0 + w1) + (long)(c0 + w1) * s.lda;
+  e = trsm_llnu<T>(ctx, A11, s.lda, w1, A12, s.lda, w2);
+  if (e != cudaSuccess) return e;
+  ELGB_CHECK(launch_gemm_simt<T>(false, false, s.m - c0 - w1, w2, w1, T(-1), A21, s.lda, A12,
+                                 s.lda, T(1), A22, s.lda, 0, ctx->stream), 1);
+  e = panel_rec(s, c0 + w1, w2);
+  if (e != cudaSuccess) return e;
+  return apply_swaps(s, c0 + w1, w2, c0, c0 + w1, 0, 0, false);
+}
+
+// El::LU(A, P) (src/lapack_like/factor/LU.cpp:104-138), right-looking over
+// blocks of nb columns: panel, PB.PermuteRows on the left and right blocks,
+// Trsm(LEFT, LOWER, NORMAL, UNIT) on A12, Gemm(-1) on A22.
+template <typename T>
+static cudaError_t getrf_run(LuState<T>& s, int nb) {
+  Context* ctx = s.ctx;
+  const int minDim = std::min(s.m, s.n);
+  for (int k = 0; k < minDim; k += nb) {
+    const int jb = std::min(nb, minDim - k);
+    cudaError_t e = panel_rec(s, k, jb);
+    if (e != cudaSuccess) return e;
+    e = apply_swaps(s, k, jb, 0, k, k + jb, s.n, true);
+    if (e != cudaSuccess) return e;
+    const int n2 = s.n - k - jb, m2 = s.m - k - jb;
+    T* A11 = s.A + k + (long)k * s.lda;
+    if (n2 > 0) {
+      e = trsm_llnu<T>(ctx, A11, s.lda, jb, s.A + k + (long)(k + jb) * s.lda, s.lda, n2);
+      if (e != cudaSuccess) return e;
+    }
+    if (s.Bc && s.nbc > 0) {
+      e = trsm_llnu<T>(ctx, A11, s.lda, jb, s.Bc + k, s.ldbc, s.nbc);
+      if (e != cudaSuccess) return e;
+    }
+    if (m2 > 0 && n2 > 0)
+      ELGB_CHECK(launch_gemm_simt<T>(false, false, m2, n2, jb, T(-1),
+                                     s.A + (k + jb) + (long)k * s.lda, s.lda,
+                                     s.A + k + (long)(k + jb) * s.lda, s.lda, T(1),
+                                     s.A + (k + jb) + (long)(k + jb) * s.lda, s.lda, 0,
+                                     ctx->stream), 1);
+    if (m2 > 0 && s.Bc && s.nbc > 0)
+      ELGB_CHECK(launch_gemm_simt<T>(false, false, m2, s.nbc, jb, T(-1),
+                                     s.A + (k + jb) + (long)k * s.lda, s.lda, s.Bc + k,
+                                     s.ldbc, T(1), s.Bc + k + jb, s.ldbc, 0, ctx->stream),
+                 1);
+  }
+  return cudaSuccess;
+}
+
+template <typename T>
+static size_t getrf_scratch_bytes(const Context* ctx, int nb) {
+  const int cap = std::max(nb, 32);
+  return panel_scratch_bytes<T>(ctx->num_sms) + align256(4 * (size_t)cap * sizeof(int)) +
+         align256(sizeof(int));
+}
+
+template <typename T>
+static cudaError_t setup_lu_state(Context* ctx, LuState<T>& s, Carver& cv, int nb) {
+  const int cap = std::max(nb, 32);
+  s.ctx = ctx;
+  s.ps = carve_panel<T>(cv, ctx->num_sms);
+  s.pairs = cv.take<int>(4 * (size_t)cap);
+  s.pair_count = cv.take<int>(1);
+  s.pairs_cap = cap;
+  if (!s.ps.diag_data || !s.pairs || !s.pair_count) return cudaErrorMemoryAllocation;
+  return cudaSuccess;
+}
+
+template <typename T>
+cudaError_t getrf(Context* ctx, int m, int n, T* A, long lda, int* ipiv, int nb) {
+  if (nb <= 0) nb = g_blocksize;
+  cudaError_t e = ctx->begin_call();
+  if (e != cudaSuccess) return e;
+  if (m == 0 || n == 0) return cudaSuccess;
+  e = ctx->ensure(getrf_scratch_bytes<T>(ctx, nb));
+  if (e != cudaSuccess) return e;
+  Carver cv(ctx);
+  LuState<T> s{};
+  e = setup_lu_state(ctx, s, cv, nb);
+  if (e != cudaSuccess) return e;
+  s.A = A;
+  s.lda = lda;
+  s.m = m;
+  s.n = n;
+  s.ipiv = ipiv;
+  return getrf_run(s, nb);
+}
+
+// ---------------------------------------------------------------------------
+// Triangular solves with a few right-hand sides (blocked, 128-row blocks)
+// ---------------------------------------------------------------------------
+// Solves op(A) X = W in place for W n x q (q <= 16), where op(A) is the
+// lower (unit or not) or upper triangle of A, optionally transposed.
+template <typename T>
+static cudaError_t trsv_blocked(Context* ctx, bool lower_of_A, bool trans, bool unit, int n,
+                                const T* A, long lda, T* W, long ldw, int q) {
+  constexpr int bs = 128;
+  // op(A) is lower when (lower_of_A && !trans) || (!lower_of_A && trans).
+  const bool op_lower = lower_of_A != trans;
+  const int nblk = (n + bs - 1) / bs;
+  for (int b = 0; b < nblk; ++b) {
+    const int bi = op_lower ? b : nblk - 1 - b;
+    const int i0 = bi * bs, ib = std::min(bs, n - i0);
+    const T* Aii = A + i0 + (long)i0 * lda;
+    ELGB_CHECK(launch_trsm_block<T>(Aii, lda, W + i0, ldw, ib, q, op_lower, unit, trans,
+                                    false, ctx->stream), 1);
+    if (op_lower) {
+      const int r0 = i0 + ib, rm = n - r0;
+      if (rm > 0) {
+        // rows below: op(A)(r0.., i0..i0+ib)
+        const T* Ab = trans ? A + i0 + (long)r0 * lda : A + r0 + (long)i0 * lda;
+        ELGB_CHECK(launch_gemm_tall_sub<T>(trans, rm, q, ib, Ab, lda, W + i0, ldw, W + r0, ldw,
+                                           ctx->stream), 1);
+      }
+    } else {
+      if (i0 > 0) {
+        // rows above: op(A)(0..i0, i0..i0+ib)
+        const T* Ab = trans ? A + i0 : A + (long)i0 * lda;
+        ELGB_CHECK(launch_gemm_tall_sub<T>(trans, i0, q, ib, Ab, lda, W + i0, ldw, W, ldw,
+                                           ctx->stream), 1);
+      }
+    }
+  }
+  return cudaSuccess;
+}
+
+template <typename T>
+static cudaError_t trsv_any(Context* ctx, bool lower_of_A, bool trans, bool unit, int n,
+                            const T* A, long lda, T* W, long ldw, int nrhs) {
+  for (int c = 0; c < nrhs; c += 16) {
+    cudaError_t e = trsv_blocked<T>(ctx, lower_of_A, trans, unit, n, A, lda,
+                                    W + (long)c * ldw, ldw, std::min(16, nrhs - c));
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+// lu::SolveAfter (src/lapack_like/factor/LU/SolveAfter.hpp:66-92).
+template <typename T>
+cudaError_t getrs(Context* ctx, int orient, int n, const T* A, long lda, const int* ipiv,
+                  int nrhs, T* B, long ldb, const int* perm_in) {
+  cudaError_t e = ctx->begin_call();
+  if (e != cudaSuccess) return e;
+  if (n == 0 || nrhs == 0) return cudaSuccess;
+  e = ctx->ensure(align256((size_t)n * sizeof(int)) + align256((size_t)n * nrhs * sizeof(T)));
+  if (e != cudaSuccess) return e;
+  Carver cv(ctx);
+  int* perm = cv.take<int>(n);
+  T* W = cv.take<T>((size_t)n * nrhs);
+  if (perm_in) {
+    perm = const_cast<int*>(perm_in);
+  } else {
+    ELGB_CHECK(launch_explicit_perm(ipiv, n, n, perm, ctx->stream), 1);
+  }
+  if (orient == 0) {
+    ELGB_CHECK(launch_permute_rows<T>(B, ldb, W, n, n, nrhs, perm, false, ctx->stream), 1);
+    e = trsv_any<T>(ctx, true, false, true, n, A, lda, W, n, nrhs);
+    if (e != cudaSuccess) return e;
+    e = trsv_any<T>(ctx, false, false, false, n, A, lda, W, n, nrhs);
+    if (e != cudaSuccess) return e;
+    e = cudaMemcpy2DAsync(B, ldb * sizeof(T), W, (size_t)n * sizeof(T), (size_t)n * sizeof(T),
+                          nrhs, cudaMemcpyDeviceToDevice, ctx->stream);
+    if (e != cudaSuccess) return e;
+  } else {
+    e = cudaMemcpy2DAsync(W, (size_t)n * sizeof(T), B, ldb * sizeof(T), (size_t)n * sizeof(T),
+                          nrhs, cudaMemcpyDeviceToDevice, ctx->stream);
+    if (e != cudaSuccess) return e;
+    e = trsv_any<T>(ctx, false, true, false, n, A, lda, W, n, nrhs);
+    if (e != cudaSuccess) return e;
+    e = trsv_any<T>(ctx, true, true, true, n, A, lda, W, n, nrhs);
+    if (e != cudaSuccess) return e;
+    ELGB_CHECK(launch_permute_rows<T>(W, n, B, ldb, n, nrhs, perm, true, ctx->stream), 1);
+  }
+  return cudaSuccess;
+}
+
+// ---------------------------------------------------------------------------
+// Cholesky (src/lapack_like/factor/Cholesky.cpp:26-38)
+// ---------------------------------------------------------------------------
+template <typename T>
+cudaError_t potrf(Context* ctx, int uplo, int n, T* A, long lda, int nb) {
+  if (nb <= 0) nb = g_blocksize;
+  if (nb > 128) nb = 128;
+  cudaError_t e = ctx->begin_call();
+  if (e != cudaSuccess) return e;
+  const bool upper = uplo != 0;
+  for (int k = 0; k < n; k += nb) {
+    const int jb = std::min(nb, n - k), n2 = n - k - jb;
+    T* A11 = A + k + (long)k * lda;
+    ELGB_CHECK(launch_potf2_block<T>(A11, lda, jb, upper, k, ctx->status, ctx->stream), 1);
+    if (n2 == 0) continue;
+    if (!upper) {
+      // LowerVariant3Blocked (Cholesky/LowerVariant3.hpp:43-68):
+      // Trsm(RIGHT, LOWER, ADJOINT, NON_UNIT) then Herk(LOWER, NORMAL, -1).
+      T* A21 = A + (k + jb) + (long)k * lda;
+      ELGB_CHECK(launch_trsm_block<T>(A11, lda, A21, lda, jb, n2, true, false, false, true,
+                                      ctx->stream), 1);
+      ELGB_CHECK(launch_gemm_simt<T>(false, true, n2, n2, jb, T(-1), A21, lda, A21, lda, T(1),
+                                     A + (k + jb) + (long)(k + jb) * lda, lda, 1, ctx->stream),
+                 1);
+    } else {
+      // UpperVariant3Blocked (Cholesky/UpperVariant3.hpp:48-73):
+      // Trsm(LEFT, UPPER, ADJOINT, NON_UNIT) then Herk(UPPER, ADJOINT, -1).
+      T* A12 = A + k + (long)(k + jb) * lda;
+      ELGB_CHECK(launch_trsm_block<T>(A11, lda, A12, lda, jb, n2, true, false, true, false,
+                                      ctx->stream), 1);
+      ELGB_CHECK(launch_gemm_simt<T>(true, false, n2, n2, jb, T(-1), A12, lda, A12, lda, T(1),
+                                     A + (k + jb) + (long)(k + jb) * lda, lda, 2, ctx->stream),
+                 1);
+    }
+  }
+  return cudaSuccess;
+}
+
+// cholesky::SolveAfter(uplo, NORMAL) (Cholesky/SolveAfter.hpp:15-43).
+template <typename T>
+cudaError_t potrs(Context* ctx, int uplo, int n, const T* A, long lda, int nrhs, T* B,
+                  long ldb) {
+  cudaError_t e = ctx->begin_call();
+  if (e != cudaSuccess) return e;
+  if (uplo == 0) {
+    e = trsv_any<T>(ctx, true, false, false, n, A, lda, B, ldb, nrhs);
+    if (e != cudaSuccess) return e;
+    return trsv_any<T>(ctx, true, true, false, n, A, lda, B, ldb, nrhs);
+  }
+  e = trsv_any<T>(ctx, false, true, false, n, A, lda, B, ldb, nrhs);
+  if (e != cudaSuccess) return e;
+  return trsv_any<T>(ctx, false, false, false, n, A, lda, B, ldb, nrhs);
+}
+
+// El::LinearSolve (src/lapack_like/solve/Linear.cpp:212-218): copy of A,
+// RowEchelon on [A | B] (:30-77), then Trsm(LEFT, UPPER, NORMAL, NON_UNIT).
+template <typename T>
+cudaError_t linear_solve(Context* ctx, int n, const T* A, long lda, int nrhs, T* B, long ldb,
+                         int nb) {
+  if (nb <= 0) nb = g_blocksize;
+  cudaError_t e = ctx->begin_call();
+  if (e != cudaSuccess) return e;
+  if (n == 0) return cudaSuccess;
+  e = ctx->ensure(getrf_scratch_bytes<T>(ctx, nb) + align256((size_t)n * n * sizeof(T)) +
+                  align256((size_t)n * sizeof(int)));
+  if (e != cudaSuccess) return e;
+  Carver cv(ctx);
+  LuState<T> s{};
+  e = setup_lu_state(ctx, s, cv, nb);
+  if (e != cudaSuccess) return e;
+  T* W = cv.take<T>((size_t)n * n);
+  int* ipiv = cv.take<int>(n);
+  e = cudaMemcpy2DAsync(W, (size_t)n * sizeof(T), A, lda * sizeof(T), (size_t)n * sizeof(T), n,
+                        cudaMemcpyDeviceToDevice, ctx->stream);
+  if (e != cudaSuccess) return e;
+  s.A = W;
+  s.lda = n;
+  s.m = n;
+  s.n = n;
+  s.ipiv = ipiv;
+  s.Bc = nrhs > 0 ? B : nullptr;
+  s.ldbc = ldb;
+  s.nbc = nrhs;
+  e = getrf_run(s, nb);
+  if (e != cudaSuccess) return e;
+  return trsv_any<T>(ctx, false, false, false, n, W, n, B, ldb, nrhs);
+}
+
+// El::HPDSolve (src/lapack_like/solve/HPD.cpp:47-55).
+template <typename T>
+cudaError_t hpd_solve(Context* ctx, int uplo, int n, const T* A, long lda, int nrhs, T* B,
+                      long ldb, int nb) {
+  cudaError_t e = ctx->begin_call();
+  if (e != cudaSuccess) return e;
+  if (n == 0) return cudaSuccess;
+  e = ctx->ensure(align256((size_t)n * n * sizeof(T)));
+  if (e != cudaSuccess) return e;
+  Carver cv(ctx);
+  T* W = cv.take<T>((size_t)n * n);
+  e = cudaMemcpy2DAsync(W, (size_t)n * sizeof(T), A, lda * sizeof(T), (size_t)n * sizeof(T), n,
+                        cudaMemcpyDeviceToDevice, ctx->stream);
+  if (e != cudaSuccess) return e;
+  e = potrf<T>(ctx, uplo, n, W, n, nb);
+  if (e != cudaSuccess) return e;
+  if (uplo == 0) {
+    e = trsv_any<T>(ctx, true, false, false, n, W, n, B, ldb, nrhs);
+    if (e != cudaSuccess) return e;
+    return trsv_any<T>(ctx, true, true, false, n, W, n, B, ldb, nrhs);
+  }
+  e = trsv_any<T>(ctx, false, true, false, n, W, n, B, ldb, nrhs);
+  if (e != cudaSuccess) return e;
+  return trsv_any<T>(ctx, false, false, false, n, W, n, B, ldb, nrhs);
+}
+
+cudaError_t residual(Context* ctx, int n, int q, const double* A, long lda, const double* X,
+                     long ldx, const double* B, long ldb, double* R, long ldr) {
+  if (n == 0 || q == 0) return cudaSuccess;
+  const int nchunks = (n + 4095) / 4096;
+  for (int c = 0; c < q; c += 16) {
+    const int qc = std::min(16, q - c);
+    cudaError_t e = ctx->ensure(align256((size_t)nchunks * n * 16 * sizeof(double)));
+    if (e != cudaSuccess) return e;
+    Carver cv(ctx);
+    double* partial = cv.take<double>((size_t)nchunks * n * 16);
+    ELGB_CHECK(launch_residual_f64(n, qc, A, lda, X + (long)c * ldx, ldx, B + (long)c * ldb,
+                                   ldb, R + (long)c * ldr, ldr, partial, ctx->stream), 2);
+  }
+  return cudaSuccess;
+}
+
+cudaError_t backward_error(Context* ctx, int n, int q, const double* A, long lda,
+                           const double* X, long ldx, const double* B, long ldb,
+                           double* berr) {
+  const size_t need = align256((size_t)n * q * sizeof(double)) +
+                      3 * align256((size_t)(q + 2) * sizeof(double)) +
+                      align256((size_t)64 * (std::max(n, q) + 1) * sizeof(double)) +
+                      align256((size_t)((n + 4095) / 4096) * n * 16 * sizeof(double));
+  cudaError_t e = ctx->ensure(need);
+  if (e != cudaSuccess) return e;
+  Carver cv(ctx);
+  double* R = cv.take<double>((size_t)n * q);
+  double* nA = cv.take<double>(n + 2);
+  double* nX = cv.take<double>(q + 2);
+  double* nR = cv.take<double>(q + 2);
+  double* nB = cv.take<double>(q + 2);
+  double* partial = cv.take<double>((size_t)64 * (std::max(n, q) + 1));
+  double* rpart = cv.take<double>((size_t)((n + 4095) / 4096) * n * 16);
+  for (int c = 0; c < q; c += 16) {
+    const int qc = std::min(16, q - c);
+    ELGB_CHECK(launch_residual_f64(n, qc, A, lda, X + (long)c * ldx, ldx, B + (long)c * ldb,
+                                   ldb, R + (long)c * n, n, rpart, ctx->stream), 2);
+  }
+  ELGB_CHECK(launch_col_sumsq<double>(A, lda, n, n, nA, partial, ctx->stream), 2);
+  ELGB_CHECK(launch_col_sumsq<double>(X, ldx, n, q, nX, partial, ctx->stream), 2);
+  ELGB_CHECK(launch_col_sumsq<double>(B, ldb, n, q, nB, partial, ctx->stream), 2);
+  ELGB_CHECK(launch_col_sumsq<double>(R, n, n, q, nR, partial, ctx->stream), 2);
+  std::vector<double> hx(q + 1), hb(q + 1), hr(q + 1);
+  double hA[1];
+  e = cudaMemcpyAsync(hA, nA + n, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+  if (e != cudaSuccess) return e;
+  e = cudaMemcpyAsync(hx.data(), nX, (q + 1) * sizeof(double), cudaMemcpyDeviceToHost,
+                      ctx->stream);
+  if (e != cudaSuccess) return e;
+  e = cudaMemcpyAsync(hb.data(), nB, (q + 1) * sizeof(double), cudaMemcpyDeviceToHost,
+                      ctx->stream);
+  if (e != cudaSuccess) return e;
+  e = cudaMemcpyAsync(hr.data(), nR, (q + 1) * sizeof(double), cudaMemcpyDeviceToHost,
+                      ctx->stream);
+  if (e != cudaSuccess) return e;
+  e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return e;
+  const double fa = std::sqrt(hA[0]);
+  double worst = 0.0;
+  for (int c = 0; c < q; ++c) {
+    const double den = fa * std::sqrt(hx[c]) + std::sqrt(hb[c]);
+    const double v = den > 0 ? std::sqrt(hr[c]) / den : (hr[c] > 0 ? INFINITY : 0.0);
+    if (!(v <= worst)) worst = v;
+  }
+  *berr = worst;
+  return cudaSuccess;
+}
+
+template cudaError_t getrf<double>(Context*, int, int, double*, long, int*, int);
+template cudaError_t getrf<float>(Context*, int, int, float*, long, int*, int);
+template cudaError_t getrs<double>(Context*, int, int, const double*, long, const int*, int,
+                                   double*, long, const int*);
+template cudaError_t getrs<float>(Context*, int, int, const float*, long, const int*, int,
+                                  float*, long, const int*);
+template cudaError_t potrf<double>(Context*, int, int, double*, long, int);
+template cudaError_t potrf<float>(Context*, int, int, float*, long, int);
+template cudaError_t potrs<double>(Context*, int, int, const double*, long, int, double*,
+                                   long);
+template cudaError_t potrs<float>(Context*, int, int, const float*, long, int, float*, long);
+
+int get_blocksize() { return g_blocksize; }
+void set_blocksize(int nb) { g_blocksize = nb; }
+
+}  // namespace elgb
+
+// ===========================================================================
+// C ABI (include/elgb300.h)
+// ===========================================================================
+using elgb::Context;
+
+struct ElGBContextImpl : public Context {};
+
+static int arg_ok(bool c) { return c ? 0 : elgb::kElArgError; }
+
+extern "C" {
+
+int ElGBCreate(ElGBContext* out, int device) {
+  if (!out) return elgb::kElArgError;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev)
+    return elgb::kElRuntimeError;
+  auto* c = new (std::nothrow) ElGBContextImpl();
+  if (!c) return elgb::kElAllocError;
+  c->device = device;
+  if (cudaSetDevice(device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device) !=
+          cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaMalloc(&c->status, sizeof(elgb::DevStatus)) != cudaSuccess ||
+      cudaMallocHost(&c->h_status, sizeof(elgb::DevStatus)) != cudaSuccess) {
+    delete c;
+    return elgb::kElRuntimeError;
+  }
+  c->stream = c->own_stream;
+  cudaMemset(c->status, 0, sizeof(elgb::DevStatus));
+  *out = c;
+  return 0;
+}
+
+int ElGBDestroy(ElGBContext ctx) {
+  if (!ctx) return elgb::kElArgError;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  delete ctx;
+  return 0;
+}
+
+int ElGBSetStream(ElGBContext ctx, void* stream) {
+  if (!ctx) return elgb::kElArgError;
+  ctx->stream = stream ? static_cast<cudaStream_t>(stream) : ctx->own_stream;
+  return 0;
+}
+
+int ElGBSynchronize(ElGBContext ctx) {
+  if (!ctx) return elgb::kElArgError;
+  return elgb::to_el_error(cudaStreamSynchronize(ctx->stream));
+}
+
+int ElGBStatus(ElGBContext ctx, int* info, int* err) {
+  if (!ctx) return elgb::kElArgError;
+  cudaError_t e = cudaMemcpyAsync(ctx->h_status, ctx->status, sizeof(elgb::DevStatus),
+                                  cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return elgb::kElRuntimeError;
+  if (info) *info = ctx->h_status->info;
+  if (err) *err = ctx->h_status->err;
+  return 0;
+}
+
+int ElGBBlocksize(void) { return elgb::get_blocksize(); }
+int ElGBSetBlocksize(int nb) {
+  if (nb < 1) return elgb::kElArgError;
+  elgb::set_blocksize(nb);
+  return 0;
+}
+long long ElGBLaunchCount(ElGBContext ctx) { return ctx ? ctx->launches : -1; }
+
+#define ELGB_LU(S, T)                                                                      \
+  int ElGBLUPartialPiv_##S(ElGBContext ctx, int m, int n, T* A, int lda, int* swapDests,   \
+                           int nb) {                                                       \
+    if (int r = arg_ok(ctx && m >= 0 && n >= 0 && lda >= std::max(m, 1) &&                 \
+                       (m * n == 0 || (A && swapDests))))                                 \
+      return r;                                                                            \
+    return elgb::to_el_error(elgb::getrf<T>(ctx, m, n, A, lda, swapDests, nb));            \
+  }                                                                                        \
+  int ElGBSolveAfterLUPartialPiv_##S(ElGBContext ctx, int orientation, int n, const T* A,  \
+                                     int lda, const int* swapDests, int nrhs, T* B,        \
+                                     int ldb) {                                            \
+    if (int r = arg_ok(ctx && n >= 0 && nrhs >= 0 && lda >= std::max(n, 1) &&              \
+                       ldb >= std::max(n, 1) && orientation >= 0 && orientation <= 2))      \
+      return r;                                                                            \
+    return elgb::to_el_error(                                                              \
+        elgb::getrs<T>(ctx, orientation, n, A, lda, swapDests, nrhs, B, ldb, nullptr));    \
+  }                                                                                        \
+  int ElGBCholesky_##S(ElGBContext ctx, int uplo, int n, T* A, int lda, int nb) {          \
+    if (int r = arg_ok(ctx && n >= 0 && lda >= std::max(n, 1) && (uplo == 0 || uplo == 1))) \
+      return r;                                                                            \
+    return elgb::to_el_error(elgb::potrf<T>(ctx, uplo, n, A, lda, nb));                    \
+  }                                                                                        \
+  int ElGBSolveAfterCholesky_##S(ElGBContext ctx, int uplo, int n, const T* A, int lda,    \
+                                 int nrhs, T* B, int ldb) {                                \
+    if (int r = arg_ok(ctx && n >= 0 && nrhs >= 0 && lda >= std::max(n, 1) &&              \
+                       ldb >= std::max(n, 1) && (uplo == 0 || uplo == 1)))                 \
+      return r;                                                                            \
+    return elgb::to_el_error(elgb::potrs<T>(ctx, uplo, n, A, lda, nrhs, B, ldb));          \
+  }                                                                                        \
+  int ElGBLinearSolve_##S(ElGBContext ctx, int n, const T* A, int lda, int nrhs, T* B,     \
+                          int ldb, int nb) {                                               \
+    if (int r = arg_ok(ctx && n >= 0 && nrhs >= 0 && lda >= std::max(n, 1) &&              \
+                       ldb >= std::max(n, 1)))                                             \
+      return r;                                                                            \
+    return elgb::to_el_error(elgb::linear_solve<T>(ctx, n, A, lda, nrhs, B, ldb, nb));     \
+  }                                                                                        \
+  int ElGBHPDSolve_##S(ElGBContext ctx, int uplo, int n, const T* A, int lda, int nrhs,    \
+                       T* B, int ldb, int nb) {                                            \
+    if (int r = arg_ok(ctx && n >= 0 && nrhs >= 0 && lda >= std::max(n, 1) &&              \
+                       ldb >= std::max(n, 1) && (uplo == 0 || uplo == 1)))                 \
+      return r;                                                                            \
+    return elgb::to_el_error(elgb::hpd_solve<T>(ctx, uplo, n, A, lda, nrhs, B, ldb, nb));  \
+  }
+
+ELGB_LU(d, double)
+ELGB_LU(s, float)
+
+int ElGBResidual_d(ElGBContext ctx, int n, int nrhs, const double* A, int lda, const double* X,
+                   int ldx, const double* B, int ldb, double* R, int ldr) {
+  if (int r = arg_ok(ctx && n >= 0 && nrhs >= 0 && lda >= std::max(n, 1) &&
+                     ldx >= std::max(n, 1) && ldb >= std::max(n, 1) && ldr >= std::max(n, 1)))
+    return r;
+  return elgb::to_el_error(elgb::residual(ctx, n, nrhs, A, lda, X, ldx, B, ldb, R, ldr));
+}
+
+int ElGBBackwardError_d(ElGBContext ctx, int n, int nrhs, const double* A, int lda,
+                        const double* X, int ldx, const double* B, int ldb, double* berr) {
+  if (int r = arg_ok(ctx && berr && n > 0 && nrhs > 0 && lda >= n && ldx >= n && ldb >= n))
+    return r;
+  return elgb::to_el_error(elgb::backward_error(ctx, n, nrhs, A, lda, X, ldx, B, ldb, berr));
+}
+
+int ElGBProbeFP64Peak(ElGBContext ctx, double* tflops) {
+  if (!ctx || !tflops) return elgb::kElArgError;
+  cudaSetDevice(ctx->device);
+  double* out = nullptr;
+  if (cudaMalloc(&out, sizeof(double)) != cudaSuccess) return elgb::kElAllocError;
+  const int blocks = ctx->num_sms * 8, threads = 256, iters = 4096;
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  elgb::launch_fp64_fma_probe(out, blocks, threads, iters, ctx->stream);  // warm-up
+  cudaEventRecord(a, ctx->stream);
+  for (int r = 0; r < 5; ++r) elgb::launch_fp64_fma_probe(out, blocks, threads, iters, ctx->stream);
+  cudaEventRecord(b, ctx->stream);
+  cudaError_t e = cudaEventSynchronize(b);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(out);
+  ctx->launches += 6;
+  if (e != cudaSuccess) return elgb::kElRuntimeError;
+  const double flops = 5.0 * blocks * threads * (double)iters * 8 * 2;
+  *tflops = flops / (ms * 1e-3) / 1e12;
+  return 0;
+}
+
+}  // extern "C"

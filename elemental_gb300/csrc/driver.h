@@ -1,0 +1,63 @@
+// Host-side context and driver entry points shared by the C ABIs.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace elgb {
+
+// Elemental's ElError codes (include/El/core/types.h:45-54 of the reference).
+enum ElErrorCode : int {
+  kElSuccess = 0,
+  kElAllocError = 1,
+  kElOutOfBoundsError = 2,
+  kElArgError = 3,
+  kElLogicError = 4,
+  kElRuntimeError = 5,
+  kElError = -1,
+};
+
+struct Context {
+  int device = 0;
+  int num_sms = 1;
+  cudaStream_t stream = nullptr;
+  cudaStream_t own_stream = nullptr;
+  void* arena = nullptr;  // growable device scratch, reused across calls
+  size_t arena_bytes = 0;
+  DevStatus* status = nullptr;    // device status word of the last call
+  DevStatus* h_status = nullptr;  // pinned host mirror
+  long long launches = 0;         // kernels enqueued by this context
+
+  ~Context();
+  cudaError_t ensure(size_t bytes);  // grows the arena (synchronizes first)
+  cudaError_t begin_call();          // selects the device, clears the status word
+};
+
+int to_el_error(cudaError_t e);
+int get_blocksize();
+void set_blocksize(int nb);
+
+template <typename T>
+cudaError_t getrf(Context* ctx, int m, int n, T* A, long lda, int* ipiv, int nb);
+template <typename T>
+cudaError_t getrs(Context* ctx, int orient, int n, const T* A, long lda, const int* ipiv,
+                  int nrhs, T* B, long ldb, const int* perm);
+template <typename T>
+cudaError_t potrf(Context* ctx, int uplo, int n, T* A, long lda, int nb);
+template <typename T>
+cudaError_t potrs(Context* ctx, int uplo, int n, const T* A, long lda, int nrhs, T* B,
+                  long ldb);
+template <typename T>
+cudaError_t linear_solve(Context* ctx, int n, const T* A, long lda, int nrhs, T* B, long ldb,
+                         int nb);
+template <typename T>
+cudaError_t hpd_solve(Context* ctx, int uplo, int n, const T* A, long lda, int nrhs, T* B,
+                      long ldb, int nb);
+cudaError_t residual(Context* ctx, int n, int q, const double* A, long lda, const double* X,
+                     long ldx, const double* B, long ldb, double* R, long ldr);
+cudaError_t backward_error(Context* ctx, int n, int q, const double* A, long lda,
+                           const double* X, long ldx, const double* B, long ldb,
+                           double* berr);
+
+}  // namespace elgb

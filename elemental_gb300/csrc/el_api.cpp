@@ -1,0 +1,674 @@
+// El-compatible host layer (include/El_gb300.hpp) and the Elemental C ABI
+// subset (include/El_gb300.h).  Host matrices are staged into device memory,
+// the device path of include/elgb300.h runs, results come back; the numerical
+// failures become the reference's exceptions, and the C entry points map
+// exceptions to ElError exactly as the reference's EL_TRY does
+// (include/El/core/CReflect.hpp:12-26).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <mutex>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/El_gb300.h"
+#include "../../include/El_gb300.hpp"
+#include "../../include/elgb300.h"
+
+namespace El {
+
+// ---------------------------------------------------------------------------
+// Matrix<T>
+// ---------------------------------------------------------------------------
+template <typename T>
+Matrix<T>& Matrix<T>::operator=(const Matrix<T>& A) {
+  if (this == &A) return *this;
+  Resize(A.Height(), A.Width());
+  for (Int j = 0; j < width_; ++j)
+    for (Int i = 0; i < height_; ++i) buf_[i + (long)j * ldim_] = A.Get(i, j);
+  return *this;
+}
+
+template <typename T>
+void Matrix<T>::Empty() {
+  height_ = width_ = 0;
+  ldim_ = 1;
+  buf_ = nullptr;
+  cbuf_ = nullptr;
+  viewing_ = locked_ = false;
+  mem_.clear();
+  mem_.shrink_to_fit();
+}
+
+template <typename T>
+void Matrix<T>::Resize(Int height, Int width) {
+  Resize(height, width, std::max(height, 1));
+}
+
+template <typename T>
+void Matrix<T>::Resize(Int height, Int width, Int ldim) {
+  if (height < 0 || width < 0 || ldim < std::max(height, 1))
+    throw std::logic_error("Matrix::Resize: invalid dimensions");
+  if (viewing_ && (height > height_ || width > width_ || ldim != ldim_))
+    throw std::logic_error("Cannot increase the size of a view");
+  height_ = height;
+  width_ = width;
+  if (viewing_) return;
+  ldim_ = ldim;
+  mem_.assign((size_t)ldim * std::max(width, 0), T(0));
+  buf_ = mem_.data();
+  cbuf_ = buf_;
+}
+
+template <typename T>
+void Matrix<T>::Attach(Int height, Int width, T* buffer, Int ldim) {
+  if (height < 0 || width < 0 || ldim < std::max(height, 1))
+    throw std::logic_error("Matrix::Attach: invalid dimensions");
+  mem_.clear();
+  height_ = height;
+  width_ = width;
+  ldim_ = ldim;
+  buf_ = buffer;
+  cbuf_ = buffer;
+  viewing_ = true;
+  locked_ = false;
+}
+
+template <typename T>
+void Matrix<T>::LockedAttach(Int height, Int width, const T* buffer, Int ldim) {
+  if (height < 0 || width < 0 || ldim < std::max(height, 1))
+    throw std::logic_error("Matrix::LockedAttach: invalid dimensions");
+  mem_.clear();
+  height_ = height;
+  width_ = width;
+  ldim_ = ldim;
+  buf_ = nullptr;
+  cbuf_ = buffer;
+  viewing_ = true;
+  locked_ = true;
+}
+
+template <typename T>
+T* Matrix<T>::Buffer() {
+  if (locked_) throw std::logic_error("Cannot return non-const buffer of locked Matrix");
+  return buf_;
+}
+
+template class Matrix<Int>;
+template class Matrix<float>;
+template class Matrix<double>;
+
+// ---------------------------------------------------------------------------
+// Permutation (swap sequence with implicit origins 0, 1, 2, ...;
+// src/lapack_like/perm/Permutation.cpp:166-250, 544-631, 731-745)
+// ---------------------------------------------------------------------------
+void Permutation::Empty() {
+  size_ = 0;
+  numSwaps_ = 0;
+  dests_.clear();
+}
+
+void Permutation::MakeIdentity(Int size) {
+  size_ = size;
+  numSwaps_ = 0;
+}
+
+void Permutation::ReserveSwaps(Int maxSwaps) {
+  if ((Int)dests_.size() < maxSwaps) dests_.resize(maxSwaps);
+}
+
+void Permutation::Swap(Int origin, Int dest) {
+  if (origin < 0 || origin >= size_ || dest < 0 || dest >= size_)
+    throw std::logic_error("Permutation::Swap: index out of range");
+  if (origin != numSwaps_)
+    throw std::logic_error("Permutation::Swap: only implicit-origin swap sequences");
+  if ((Int)dests_.size() <= numSwaps_) dests_.resize(numSwaps_ + 1);
+  dests_[numSwaps_++] = dest;
+}
+
+bool Permutation::Parity() const {
+  bool p = false;
+  for (Int j = 0; j < numSwaps_; ++j)
+    if (dests_[j] != j) p = !p;
+  return p;
+}
+
+const Matrix<Int> Permutation::SwapDestinations() const {
+  Matrix<Int> d(numSwaps_, 1);
+  for (Int j = 0; j < numSwaps_; ++j) d(j, 0) = dests_[j];
+  return d;
+}
+
+template <typename T>
+static void RowSwapHost(Matrix<T>& A, Int to, Int from) {
+  if (to == from) return;
+  T* b = A.Buffer();
+  const Int ld = A.LDim();
+  for (Int j = 0; j < A.Width(); ++j) std::swap(b[to + (long)j * ld], b[from + (long)j * ld]);
+}
+
+template <typename T>
+void Permutation::PermuteRows(Matrix<T>& A, Int offset) const {
+  if (A.Height() == 0 || A.Width() == 0) return;
+  for (Int j = 0; j < numSwaps_; ++j) RowSwapHost(A, j + offset, dests_[j] + offset);
+}
+
+template <typename T>
+void Permutation::InversePermuteRows(Matrix<T>& A, Int offset) const {
+  if (A.Height() == 0 || A.Width() == 0) return;
+  for (Int j = numSwaps_ - 1; j >= 0; --j) RowSwapHost(A, j + offset, dests_[j] + offset);
+}
+
+void Permutation::ExplicitVector(Matrix<Int>& p) const {
+  p.Resize(size_, 1);
+  for (Int i = 0; i < size_; ++i) p(i, 0) = i;
+  PermuteRows(p);
+}
+
+void Permutation::SetSwapSequence(Int size, const Int* dests, Int numSwaps) {
+  size_ = size;
+  numSwaps_ = numSwaps;
+  dests_.assign(dests, dests + numSwaps);
+}
+
+template void Permutation::PermuteRows<Int>(Matrix<Int>&, Int) const;
+template void Permutation::PermuteRows<float>(Matrix<float>&, Int) const;
+template void Permutation::PermuteRows<double>(Matrix<double>&, Int) const;
+template void Permutation::InversePermuteRows<Int>(Matrix<Int>&, Int) const;
+template void Permutation::InversePermuteRows<float>(Matrix<float>&, Int) const;
+template void Permutation::InversePermuteRows<double>(Matrix<double>&, Int) const;
+
+// ---------------------------------------------------------------------------
+// Blocksize stack (src/blas_like/blocksizes.cpp:37-60)
+// ---------------------------------------------------------------------------
+namespace {
+std::vector<Int>& BlocksizeStack() {
+  static std::vector<Int> s{128};
+  return s;
+}
+}  // namespace
+
+Int Blocksize() { return BlocksizeStack().back(); }
+void SetBlocksize(Int blocksize) {
+  BlocksizeStack().back() = blocksize;
+  ElGBSetBlocksize(blocksize);
+}
+void PushBlocksizeStack(Int blocksize) {
+  BlocksizeStack().push_back(blocksize);
+  ElGBSetBlocksize(blocksize);
+}
+void PopBlocksizeStack() {
+  if (BlocksizeStack().size() > 1) BlocksizeStack().pop_back();
+  ElGBSetBlocksize(BlocksizeStack().back());
+}
+
+// ---------------------------------------------------------------------------
+// Device staging shared by the host-matrix entry points
+// ---------------------------------------------------------------------------
+namespace {
+
+struct Staging {
+  std::mutex mu;
+  ElGBContext ctx = nullptr;
+  int device = -1;
+  void* buf = nullptr;
+  size_t bytes = 0;
+};
+
+Staging& St() {
+  static Staging s;
+  return s;
+}
+
+void Check(cudaError_t e, const char* what) {
+  if (e != cudaSuccess)
+    throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+ElGBContext Ctx() {
+  Staging& s = St();
+  int dev = 0;
+  Check(cudaGetDevice(&dev), "cudaGetDevice");
+  if (s.ctx && s.device != dev) {
+    ElGBDestroy(s.ctx);
+    s.ctx = nullptr;
+    if (s.buf) cudaFree(s.buf);
+    s.buf = nullptr;
+    s.bytes = 0;
+  }
+  if (!s.ctx) {
+    if (ElGBCreate(&s.ctx, dev) != 0) throw std::runtime_error("no usable CUDA device");
+    s.device = dev;
+  }
+  return s.ctx;
+}
+
+char* Dev(size_t bytes) {
+  Staging& s = St();
+  if (bytes > s.bytes) {
+    if (s.buf) cudaFree(s.buf);
+    s.buf = nullptr;
+    s.bytes = 0;
+    Check(cudaMalloc(&s.buf, bytes), "cudaMalloc");
+    s.bytes = bytes;
+  }
+  return static_cast<char*>(s.buf);
+}
+
+size_t Al(size_t b) { return (b + 255) & ~size_t(255); }
+
+template <typename T>
+void Upload(ElGBContext ctx, T* d, const Matrix<T>& A) {
+  if (A.Height() == 0 || A.Width() == 0) return;
+  void* stream = nullptr;
+  (void)stream;
+  Check(cudaMemcpy2D(d, sizeof(T) * A.Height(), A.LockedBuffer(), sizeof(T) * A.LDim(),
+                     sizeof(T) * A.Height(), A.Width(), cudaMemcpyHostToDevice),
+        "upload");
+  (void)ctx;
+}
+
+template <typename T>
+void Download(Matrix<T>& A, const T* d) {
+  if (A.Height() == 0 || A.Width() == 0) return;
+  Check(cudaMemcpy2D(A.Buffer(), sizeof(T) * A.LDim(), d, sizeof(T) * A.Height(),
+                     sizeof(T) * A.Height(), A.Width(), cudaMemcpyDeviceToHost),
+        "download");
+}
+
+void CheckStatus(ElGBContext ctx, bool cholesky) {
+  int info = 0, err = 0;
+  if (ElGBStatus(ctx, &info, &err) != 0) throw std::runtime_error("CUDA failure");
+  if (err) throw std::runtime_error("device-side wait timed out");
+  if (info) {
+    if (cholesky) throw NonHPDMatrixException("A was not numerically HPD");
+    throw SingularMatrixException();
+  }
+}
+
+void CheckRc(int rc) {
+  if (rc == 3) throw std::invalid_argument("invalid argument");
+  if (rc != 0) throw std::runtime_error("GB300 factor-and-solve call failed");
+}
+
+template <typename F>
+struct Dispatch;
+template <>
+struct Dispatch<double> {
+  static int lu(ElGBContext c, int m, int n, double* A, int lda, int* p, int nb) {
+    return ElGBLUPartialPiv_d(c, m, n, A, lda, p, nb);
+  }
+  static int lus(ElGBContext c, int o, int n, const double* A, int lda, const int* p, int q,
+                 double* B, int ldb) {
+    return ElGBSolveAfterLUPartialPiv_d(c, o, n, A, lda, p, q, B, ldb);
+  }
+  static int chol(ElGBContext c, int u, int n, double* A, int lda, int nb) {
+    return ElGBCholesky_d(c, u, n, A, lda, nb);
+  }
+  static int chols(ElGBContext c, int u, int n, const double* A, int lda, int q, double* B,
+                   int ldb) {
+    return ElGBSolveAfterCholesky_d(c, u, n, A, lda, q, B, ldb);
+  }
+  static int lin(ElGBContext c, int n, const double* A, int lda, int q, double* B, int ldb,
+                 int nb) {
+    return ElGBLinearSolve_d(c, n, A, lda, q, B, ldb, nb);
+  }
+  static int hpd(ElGBContext c, int u, int n, const double* A, int lda, int q, double* B,
+                 int ldb, int nb) {
+    return ElGBHPDSolve_d(c, u, n, A, lda, q, B, ldb, nb);
+  }
+};
+template <>
+struct Dispatch<float> {
+  static int lu(ElGBContext c, int m, int n, float* A, int lda, int* p, int nb) {
+    return ElGBLUPartialPiv_s(c, m, n, A, lda, p, nb);
+  }
+  static int lus(ElGBContext c, int o, int n, const float* A, int lda, const int* p, int q,
+                 float* B, int ldb) {
+    return ElGBSolveAfterLUPartialPiv_s(c, o, n, A, lda, p, q, B, ldb);
+  }
+  static int chol(ElGBContext c, int u, int n, float* A, int lda, int nb) {
+    return ElGBCholesky_s(c, u, n, A, lda, nb);
+  }
+  static int chols(ElGBContext c, int u, int n, const float* A, int lda, int q, float* B,
+                   int ldb) {
+    return ElGBSolveAfterCholesky_s(c, u, n, A, lda, q, B, ldb);
+  }
+  static int lin(ElGBContext c, int n, const float* A, int lda, int q, float* B, int ldb,
+                 int nb) {
+    return ElGBLinearSolve_s(c, n, A, lda, q, B, ldb, nb);
+  }
+  static int hpd(ElGBContext c, int u, int n, const float* A, int lda, int q, float* B,
+                 int ldb, int nb) {
+    return ElGBHPDSolve_s(c, u, n, A, lda, q, B, ldb, nb);
+  }
+};
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// The path: El::LU, lu::SolveAfter, El::Cholesky, cholesky::SolveAfter,
+// El::LinearSolve, El::HPDSolve
+// ---------------------------------------------------------------------------
+template <typename F>
+void LU(Matrix<F>& A, Permutation& P) {
+  std::lock_guard<std::mutex> lk(St().mu);
+  const Int m = A.Height(), n = A.Width(), minDim = std::min(m, n);
+  P.MakeIdentity(m);
+  P.ReserveSwaps(minDim);
+  if (minDim == 0) {
+    P.SetSwapSequence(m, nullptr, 0);
+    return;
+  }
+  ElGBContext ctx = Ctx();
+  char* base = Dev(Al(sizeof(F) * (size_t)m * n) + Al(sizeof(int) * minDim));
+  F* dA = reinterpret_cast<F*>(base);
+  int* dP = reinterpret_cast<int*>(base + Al(sizeof(F) * (size_t)m * n));
+  Upload(ctx, dA, A);
+  CheckRc(Dispatch<F>::lu(ctx, m, n, dA, m, dP, Blocksize()));
+  int info = 0, err = 0;
+  if (ElGBStatus(ctx, &info, &err) != 0) throw std::runtime_error("CUDA failure");
+  Download(A, dA);
+  std::vector<Int> piv(minDim);
+  Check(cudaMemcpy(piv.data(), dP, sizeof(int) * minDim, cudaMemcpyDeviceToHost), "pivots");
+  if (err) throw std::runtime_error("device-side wait timed out");
+  if (info) {
+    // The reference stops at the failing column (LU/Panel.hpp:51-52) with
+    // the swaps recorded up to and including it.
+    P.SetSwapSequence(m, piv.data(), std::min<Int>(info, minDim));
+    throw SingularMatrixException();
+  }
+  P.SetSwapSequence(m, piv.data(), minDim);
+}
+
+namespace lu {
+template <typename F>
+void SolveAfter(Orientation orientation, const Matrix<F>& A, const Permutation& P,
+                Matrix<F>& B) {
+  if (A.Height() != A.Width()) throw std::logic_error("A must be square");
+  if (A.Height() != B.Height()) throw std::logic_error("A and B must be the same height");
+  std::lock_guard<std::mutex> lk(St().mu);
+  const Int n = A.Height(), q = B.Width();
+  if (n == 0 || q == 0) return;
+  ElGBContext ctx = Ctx();
+  const size_t sa = Al(sizeof(F) * (size_t)n * n), sb = Al(sizeof(F) * (size_t)n * q);
+  char* base = Dev(sa + sb + Al(sizeof(int) * n));
+  F* dA = reinterpret_cast<F*>(base);
+  F* dB = reinterpret_cast<F*>(base + sa);
+  int* dP = reinterpret_cast<int*>(base + sa + sb);
+  std::vector<int> piv(n);
+  for (Int i = 0; i < n; ++i) piv[i] = i < P.NumSwaps() ? P.SwapDestBuffer()[i] : i;
+  Check(cudaMemcpy(dP, piv.data(), sizeof(int) * n, cudaMemcpyHostToDevice), "pivots");
+  Upload(ctx, dA, A);
+  Upload(ctx, dB, B);
+  CheckRc(Dispatch<F>::lus(ctx, orientation == NORMAL ? 0 : 1, n, dA, n, dP, q, dB, n));
+  CheckStatus(ctx, false);
+  Download(B, dB);
+}
+}  // namespace lu
+
+template <typename F>
+void Cholesky(UpperOrLower uplo, Matrix<F>& A) {
+  if (A.Height() != A.Width()) throw std::logic_error("A must be square");
+  std::lock_guard<std::mutex> lk(St().mu);
+  const Int n = A.Height();
+  if (n == 0) return;
+  ElGBContext ctx = Ctx();
+  F* dA = reinterpret_cast<F*>(Dev(Al(sizeof(F) * (size_t)n * n)));
+  Upload(ctx, dA, A);
+  CheckRc(Dispatch<F>::chol(ctx, uplo == UPPER ? 1 : 0, n, dA, n, Blocksize()));
+  int info = 0, err = 0;
+  if (ElGBStatus(ctx, &info, &err) != 0) throw std::runtime_error("CUDA failure");
+  Download(A, dA);
+  if (err) throw std::runtime_error("device-side wait timed out");
+  if (info) throw NonHPDMatrixException("A was not numerically HPD");
+}
+
+namespace cholesky {
+template <typename F>
+void SolveAfter(UpperOrLower uplo, Orientation orientation, const Matrix<F>& A, Matrix<F>& B) {
+  (void)orientation;  // real scalars: Conjugate(B) is the identity
+  if (A.Height() != A.Width()) throw std::logic_error("A must be square");
+  if (A.Height() != B.Height()) throw std::logic_error("A and B must be the same height");
+  std::lock_guard<std::mutex> lk(St().mu);
+  const Int n = A.Height(), q = B.Width();
+  if (n == 0 || q == 0) return;
+  ElGBContext ctx = Ctx();
+  const size_t sa = Al(sizeof(F) * (size_t)n * n);
+  char* base = Dev(sa + Al(sizeof(F) * (size_t)n * q));
+  F* dA = reinterpret_cast<F*>(base);
+  F* dB = reinterpret_cast<F*>(base + sa);
+  Upload(ctx, dA, A);
+  Upload(ctx, dB, B);
+  CheckRc(Dispatch<F>::chols(ctx, uplo == UPPER ? 1 : 0, n, dA, n, q, dB, n));
+  CheckStatus(ctx, true);
+  Download(B, dB);
+}
+}  // namespace cholesky
+
+template <typename F>
+void LinearSolve(const Matrix<F>& A, Matrix<F>& B) {
+  if (A.Height() != A.Width()) throw std::logic_error("A must be square");
+  if (A.Height() != B.Height()) throw std::logic_error("A and B must be the same height");
+  std::lock_guard<std::mutex> lk(St().mu);
+  const Int n = A.Height(), q = B.Width();
+  if (n == 0) return;
+  ElGBContext ctx = Ctx();
+  const size_t sa = Al(sizeof(F) * (size_t)n * n);
+  char* base = Dev(sa + Al(sizeof(F) * (size_t)n * std::max(q, 1)));
+  F* dA = reinterpret_cast<F*>(base);
+  F* dB = reinterpret_cast<F*>(base + sa);
+  Upload(ctx, dA, A);
+  Upload(ctx, dB, B);
+  CheckRc(Dispatch<F>::lin(ctx, n, dA, n, q, dB, n, Blocksize()));
+  CheckStatus(ctx, false);
+  Download(B, dB);
+}
+
+template <typename F>
+void HPDSolve(UpperOrLower uplo, Orientation orientation, const Matrix<F>& A, Matrix<F>& B) {
+  (void)orientation;
+  if (A.Height() != A.Width()) throw std::logic_error("A must be square");
+  if (A.Height() != B.Height()) throw std::logic_error("A and B must be the same height");
+  std::lock_guard<std::mutex> lk(St().mu);
+  const Int n = A.Height(), q = B.Width();
+  if (n == 0) return;
+  ElGBContext ctx = Ctx();
+  const size_t sa = Al(sizeof(F) * (size_t)n * n);
+  char* base = Dev(sa + Al(sizeof(F) * (size_t)n * std::max(q, 1)));
+  F* dA = reinterpret_cast<F*>(base);
+  F* dB = reinterpret_cast<F*>(base + sa);
+  Upload(ctx, dA, A);
+  Upload(ctx, dB, B);
+  CheckRc(Dispatch<F>::hpd(ctx, uplo == UPPER ? 1 : 0, n, dA, n, q, dB, n, Blocksize()));
+  CheckStatus(ctx, true);
+  Download(B, dB);
+}
+
+#define EL_GB_PROTO(F)                                                                  \
+  template void LU<F>(Matrix<F>&, Permutation&);                                        \
+  template void lu::SolveAfter<F>(Orientation, const Matrix<F>&, const Permutation&,    \
+                                  Matrix<F>&);                                          \
+  template void Cholesky<F>(UpperOrLower, Matrix<F>&);                                  \
+  template void cholesky::SolveAfter<F>(UpperOrLower, Orientation, const Matrix<F>&,    \
+                                        Matrix<F>&);                                    \
+  template void LinearSolve<F>(const Matrix<F>&, Matrix<F>&);                           \
+  template void HPDSolve<F>(UpperOrLower, Orientation, const Matrix<F>&, Matrix<F>&);
+EL_GB_PROTO(float)
+EL_GB_PROTO(double)
+
+}  // namespace El
+
+// ===========================================================================
+// C ABI (include/El_gb300.h), EL_TRY semantics
+// ===========================================================================
+#define EL_GB_TRY(payload)                                   \
+  try {                                                      \
+    payload;                                                 \
+  } catch (std::bad_alloc&) {                                \
+    return EL_ALLOC_ERROR;                                   \
+  } catch (std::invalid_argument&) {                         \
+    return EL_ARG_ERROR;                                     \
+  } catch (std::logic_error&) {                              \
+    return EL_LOGIC_ERROR;                                   \
+  } catch (std::runtime_error&) {                            \
+    return EL_RUNTIME_ERROR;                                 \
+  } catch (std::exception&) {                                \
+    return EL_ERROR;                                         \
+  }                                                          \
+  return EL_SUCCESS;
+
+template <typename T>
+static El::Matrix<T>* M(void* p) {
+  return reinterpret_cast<El::Matrix<T>*>(p);
+}
+template <typename T>
+static const El::Matrix<T>* CM(const void* p) {
+  return reinterpret_cast<const El::Matrix<T>*>(p);
+}
+static El::Permutation* PP(void* p) { return reinterpret_cast<El::Permutation*>(p); }
+static const El::Permutation* CP(const void* p) {
+  return reinterpret_cast<const El::Permutation*>(p);
+}
+
+extern "C" {
+
+const char* ElErrorString(ElError error) {
+  switch (error) {
+    case EL_SUCCESS: return "EL_SUCCESS";
+    case EL_ALLOC_ERROR: return "EL_ALLOC_ERROR";
+    case EL_OUT_OF_BOUNDS_ERROR: return "EL_OUT_OF_BOUNDS_ERROR";
+    case EL_ARG_ERROR: return "EL_ARG_ERROR";
+    case EL_LOGIC_ERROR: return "EL_LOGIC_ERROR";
+    case EL_RUNTIME_ERROR: return "EL_RUNTIME_ERROR";
+    default: return "EL_ERROR";
+  }
+}
+
+#define EL_GB_MATRIX_IMPL(S, T)                                                          \
+  ElError ElMatrixCreate_##S(ElMatrix_##S* A) {                                          \
+    EL_GB_TRY(*A = reinterpret_cast<ElMatrix_##S>(new El::Matrix<T>()))                   \
+  }                                                                                      \
+  ElError ElMatrixDestroy_##S(ElConstMatrix_##S A) { EL_GB_TRY(delete CM<T>(A)) }        \
+  ElError ElMatrixEmpty_##S(ElMatrix_##S A) { EL_GB_TRY(M<T>(A)->Empty()) }              \
+  ElError ElMatrixResize_##S(ElMatrix_##S A, ElInt h, ElInt w) {                         \
+    EL_GB_TRY(M<T>(A)->Resize(h, w))                                                     \
+  }                                                                                      \
+  ElError ElMatrixResizeWithLDim_##S(ElMatrix_##S A, ElInt h, ElInt w, ElInt ld) {       \
+    EL_GB_TRY(M<T>(A)->Resize(h, w, ld))                                                 \
+  }                                                                                      \
+  ElError ElMatrixAttach_##S(ElMatrix_##S A, ElInt h, ElInt w, T* buf, ElInt ld) {       \
+    EL_GB_TRY(M<T>(A)->Attach(h, w, buf, ld))                                            \
+  }                                                                                      \
+  ElError ElMatrixLockedAttach_##S(ElMatrix_##S A, ElInt h, ElInt w, const T* buf,       \
+                                   ElInt ld) {                                           \
+    EL_GB_TRY(M<T>(A)->LockedAttach(h, w, buf, ld))                                      \
+  }                                                                                      \
+  ElError ElMatrixHeight_##S(ElConstMatrix_##S A, ElInt* h) {                            \
+    EL_GB_TRY(*h = CM<T>(A)->Height())                                                   \
+  }                                                                                      \
+  ElError ElMatrixWidth_##S(ElConstMatrix_##S A, ElInt* w) {                             \
+    EL_GB_TRY(*w = CM<T>(A)->Width())                                                    \
+  }                                                                                      \
+  ElError ElMatrixLDim_##S(ElConstMatrix_##S A, ElInt* ld) {                             \
+    EL_GB_TRY(*ld = CM<T>(A)->LDim())                                                    \
+  }                                                                                      \
+  ElError ElMatrixBuffer_##S(ElMatrix_##S A, T** buf) { EL_GB_TRY(*buf = M<T>(A)->Buffer()) } \
+  ElError ElMatrixLockedBuffer_##S(ElConstMatrix_##S A, const T** buf) {                 \
+    EL_GB_TRY(*buf = CM<T>(A)->LockedBuffer())                                           \
+  }                                                                                      \
+  ElError ElMatrixGet_##S(ElConstMatrix_##S A, ElInt i, ElInt j, T* val) {               \
+    EL_GB_TRY(*val = CM<T>(A)->Get(i, j))                                                \
+  }                                                                                      \
+  ElError ElMatrixSet_##S(ElMatrix_##S A, ElInt i, ElInt j, T val) {                     \
+    EL_GB_TRY(M<T>(A)->Set(i, j, val))                                                   \
+  }
+EL_GB_MATRIX_IMPL(i, ElInt)
+EL_GB_MATRIX_IMPL(s, float)
+EL_GB_MATRIX_IMPL(d, double)
+
+ElError ElPermutationCreate(ElPermutation* P) {
+  EL_GB_TRY(*P = reinterpret_cast<ElPermutation>(new El::Permutation()))
+}
+ElError ElPermutationDestroy(ElConstPermutation P) { EL_GB_TRY(delete CP(P)) }
+ElError ElPermutationEmpty(ElPermutation P) { EL_GB_TRY(PP(P)->Empty()) }
+ElError ElPermutationMakeIdentity(ElPermutation P, ElInt size) {
+  EL_GB_TRY(PP(P)->MakeIdentity(size))
+}
+ElError ElPermutationReserveSwaps(ElPermutation P, ElInt maxSwaps) {
+  EL_GB_TRY(PP(P)->ReserveSwaps(maxSwaps))
+}
+ElError ElPermutationSwap(ElPermutation P, ElInt origin, ElInt dest) {
+  EL_GB_TRY(PP(P)->Swap(origin, dest))
+}
+ElError ElPermutationHeight(ElConstPermutation P, ElInt* h) { EL_GB_TRY(*h = CP(P)->Height()) }
+ElError ElPermutationWidth(ElConstPermutation P, ElInt* w) { EL_GB_TRY(*w = CP(P)->Width()) }
+ElError ElPermutationParity(ElConstPermutation P, bool* parity) {
+  EL_GB_TRY(*parity = CP(P)->Parity())
+}
+ElError ElPermutationIsSwapSequence(ElConstPermutation P, bool* isSwap) {
+  EL_GB_TRY(*isSwap = CP(P)->IsSwapSequence())
+}
+ElError ElPermutationIsImplicitSwapSequence(ElConstPermutation P, bool* isImplicit) {
+  EL_GB_TRY(*isImplicit = CP(P)->IsImplicitSwapSequence())
+}
+ElError ElPermutationPermuteRows_s(ElConstPermutation P, ElMatrix_s A, ElInt offset) {
+  EL_GB_TRY(CP(P)->PermuteRows(*M<float>(A), offset))
+}
+ElError ElPermutationPermuteRows_d(ElConstPermutation P, ElMatrix_d A, ElInt offset) {
+  EL_GB_TRY(CP(P)->PermuteRows(*M<double>(A), offset))
+}
+ElError ElPermutationExplicitVector(ElConstPermutation P, ElMatrix_i pVec) {
+  EL_GB_TRY(CP(P)->ExplicitVector(*M<El::Int>(pVec)))
+}
+
+ElError ElBlocksize(ElInt* blocksize) { EL_GB_TRY(*blocksize = El::Blocksize()) }
+ElError ElSetBlocksize(ElInt blocksize) { EL_GB_TRY(El::SetBlocksize(blocksize)) }
+ElError ElPushBlocksizeStack(ElInt blocksize) { EL_GB_TRY(El::PushBlocksizeStack(blocksize)) }
+ElError ElPopBlocksizeStack(void) { EL_GB_TRY(El::PopBlocksizeStack()) }
+
+static El::Orientation Or(ElOrientation o) {
+  return o == EL_NORMAL ? El::NORMAL : (o == EL_TRANSPOSE ? El::TRANSPOSE : El::ADJOINT);
+}
+static El::UpperOrLower Ul(ElUpperOrLower u) { return u == EL_UPPER ? El::UPPER : El::LOWER; }
+
+ElError ElLUPartialPiv_s(ElMatrix_s A, ElPermutation P) { EL_GB_TRY(El::LU(*M<float>(A), *PP(P))) }
+ElError ElLUPartialPiv_d(ElMatrix_d A, ElPermutation P) {
+  EL_GB_TRY(El::LU(*M<double>(A), *PP(P)))
+}
+ElError ElSolveAfterLUPartialPiv_s(ElOrientation o, ElConstMatrix_s A, ElConstPermutation P,
+                                   ElMatrix_s B) {
+  EL_GB_TRY(El::lu::SolveAfter(Or(o), *CM<float>(A), *CP(P), *M<float>(B)))
+}
+ElError ElSolveAfterLUPartialPiv_d(ElOrientation o, ElConstMatrix_d A, ElConstPermutation P,
+                                   ElMatrix_d B) {
+  EL_GB_TRY(El::lu::SolveAfter(Or(o), *CM<double>(A), *CP(P), *M<double>(B)))
+}
+ElError ElCholesky_s(ElUpperOrLower u, ElMatrix_s A) { EL_GB_TRY(El::Cholesky(Ul(u), *M<float>(A))) }
+ElError ElCholesky_d(ElUpperOrLower u, ElMatrix_d A) {
+  EL_GB_TRY(El::Cholesky(Ul(u), *M<double>(A)))
+}
+ElError ElSolveAfterCholesky_s(ElUpperOrLower u, ElOrientation o, ElConstMatrix_s A,
+                               ElMatrix_s B) {
+  EL_GB_TRY(El::cholesky::SolveAfter(Ul(u), Or(o), *CM<float>(A), *M<float>(B)))
+}
+ElError ElSolveAfterCholesky_d(ElUpperOrLower u, ElOrientation o, ElConstMatrix_d A,
+                               ElMatrix_d B) {
+  EL_GB_TRY(El::cholesky::SolveAfter(Ul(u), Or(o), *CM<double>(A), *M<double>(B)))
+}
+ElError ElLinearSolve_s(ElConstMatrix_s A, ElMatrix_s B) {
+  EL_GB_TRY(El::LinearSolve(*CM<float>(A), *M<float>(B)))
+}
+ElError ElLinearSolve_d(ElConstMatrix_d A, ElMatrix_d B) {
+  EL_GB_TRY(El::LinearSolve(*CM<double>(A), *M<double>(B)))
+}
+ElError ElHPDSolve_s(ElUpperOrLower u, ElOrientation o, ElConstMatrix_s A, ElMatrix_s B) {
+  EL_GB_TRY(El::HPDSolve(Ul(u), Or(o), *CM<float>(A), *M<float>(B)))
+}
+ElError ElHPDSolve_d(ElUpperOrLower u, ElOrientation o, ElConstMatrix_d A, ElMatrix_d B) {
+  EL_GB_TRY(El::HPDSolve(Ul(u), Or(o), *CM<double>(A), *M<double>(B)))
+}
+
+}  // extern "C"

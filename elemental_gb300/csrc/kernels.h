@@ -1,0 +1,118 @@
+// Launch wrappers for the GB300 dense factor-and-solve kernels (host side).
+// All matrices are column-major: element (i, j) of a matrix with leading
+// dimension ld sits at ptr[i + j * ld], the layout of El::Matrix
+// (include/El/core/Matrix/decl.hpp:17-241).  Every wrapper enqueues work on
+// `stream` and returns a cudaError_t from the launch.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace elgb {
+
+// Device scratch used by one factorization call.  Sized by the driver.
+template <typename T>
+struct PanelScratch {
+  unsigned* bar;      // grid-barrier counter (zeroed before each panel launch)
+  T* cand_val;        // [2][maxG]   |candidate|
+  int* cand_row;      // [2][maxG]   candidate row (panel-relative), -1 = none
+  T* cand_data;       // [2][maxG][32] candidate rows
+  T* diag_data;       // [2][32]     current diagonal row
+  int maxG;
+};
+
+// getf2 on a w-wide panel (w <= 32): El's lu::Panel
+// (src/lapack_like/factor/LU/Panel.hpp:15-59) as one cooperative launch.
+// `A` points at the panel's top-left element, `mp` rows, `w` columns.
+// ipiv[c] receives the absolute pivot row (row_base + panel row).  A zero
+// pivot records info = info_base + c + 1 (first one wins) in st.
+template <typename T>
+cudaError_t launch_getf2_panel(T* A, long lda, int mp, int w, int* ipiv,
+                               int row_base, int info_base,
+                               const PanelScratch<T>& s, DevStatus* st,
+                               int num_sms, cudaStream_t stream);
+
+// Converts the swap sequence ipiv[0..nb) (absolute destinations for rows
+// k..k+nb) into an explicit list of (dst, src) row moves.  pairs must hold
+// 4*nb ints ([dst..., src...] as 2*nb each); count receives the number of
+// moves.
+cudaError_t launch_build_swap_pairs(const int* ipiv, int k, int nb,
+                                    int* pairs, int* count,
+                                    cudaStream_t stream);
+
+// Applies the row moves from launch_build_swap_pairs to columns
+// [c0a, c1a) and [c0b, c1b) of A (the laswp of El's PB.PermuteRows,
+// src/lapack_like/factor/LU.cpp:130-131).
+template <typename T>
+cudaError_t launch_apply_swap_pairs(T* A, long lda, int c0a, int c1a,
+                                    int c0b, int c1b, const int* pairs,
+                                    const int* count, int nb,
+                                    cudaStream_t stream);
+
+// Explicit permutation vector from a whole swap sequence:
+// perm[i] = the original row that ends up at row i
+// (Permutation::ExplicitVector, src/lapack_like/perm/Permutation.cpp:731-745).
+cudaError_t launch_explicit_perm(const int* ipiv, int nswaps, int n,
+                                 int* perm, cudaStream_t stream);
+
+// Y(i, :) = X(perm[i], :) (inverse = false) or Y(perm[i], :) = X(i, :).
+template <typename T>
+cudaError_t launch_permute_rows(const T* X, long ldx, T* Y, long ldy, int n,
+                                int ncols, const int* perm, bool inverse,
+                                cudaStream_t stream);
+
+// Small dense triangular solve on one diagonal block (nb <= 128):
+//   op(A11) X = B   with B nb x ncols, solved in place.
+// lower/upper and unit/non-unit refer to op(A11); trans_a loads A11
+// transposed; trans_b means B is stored transposed (B^T is ncols x nb at
+// Bm with leading dimension ldb).
+template <typename T>
+cudaError_t launch_trsm_block(const T* A11, long lda, T* Bm, long ldb, int nb,
+                              int ncols, bool lower, bool unit, bool trans_a,
+                              bool trans_b, cudaStream_t stream);
+
+// C = alpha * op(A) * op(B) + beta * C on CUDA cores (SIMT FMA).
+// uplo: 0 full, 1 lower triangle only (i >= j), 2 upper only (i <= j).
+template <typename T>
+cudaError_t launch_gemm_simt(bool ta, bool tb, int m, int n, int k, T alpha,
+                             const T* A, long lda, const T* Bm, long ldb,
+                             T beta, T* C, long ldc, int uplo,
+                             cudaStream_t stream);
+
+// Tall-skinny update C[m x q] -= op(A)[m x K] * X[K x q], K <= 256, q <= 16.
+template <typename T>
+cudaError_t launch_gemm_tall_sub(bool ta, int m, int q, int K, const T* A,
+                                 long lda, const T* X, long ldx, T* C,
+                                 long ldc, cudaStream_t stream);
+
+// Cholesky of one diagonal block (nb <= 128) in place, El's
+// LowerVariant3Unblocked / UpperVariant3Unblocked
+// (src/lapack_like/factor/Cholesky/LowerVariant3.hpp:15-41).  A
+// non-positive pivot records info = info_base + j + 1.
+template <typename T>
+cudaError_t launch_potf2_block(T* A, long lda, int nb, bool upper,
+                               int info_base, DevStatus* st,
+                               cudaStream_t stream);
+
+// Residual R = B - A X in FP64 with a deterministic two-stage reduction.
+// partial must hold nchunks * n * q doubles, nchunks = ceil(n / 4096).
+cudaError_t launch_residual_f64(int n, int q, const double* A, long lda,
+                                const double* X, long ldx, const double* B,
+                                long ldb, double* R, long ldr, double* partial,
+                                cudaStream_t stream);
+
+// Sum of squares of each column (out[j]) and of all entries (out[ncols]) of
+// an m x ncols matrix, deterministic.  partial holds 64 * (ncols + 1) doubles.
+template <typename T>
+cudaError_t launch_col_sumsq(const T* A, long lda, int m, int ncols,
+                             double* out, double* partial,
+                             cudaStream_t stream);
+
+// Measures the device's FP64 FMA rate: `iters` dependent-chain FMAs per
+// thread over the given grid; out receives a checksum.
+cudaError_t launch_fp64_fma_probe(double* out, int blocks, int threads,
+                                  int iters, cudaStream_t stream);
+
+}  // namespace elgb

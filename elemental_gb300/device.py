@@ -1,0 +1,191 @@
+"""Device-level Python access to libelgb300.so for torch CUDA tensors.
+
+Matrices are column-major, as El::Matrix: an m x n matrix is a torch tensor of
+shape (m, n) with strides (1, ld), ld >= m — e.g. ``colmajor(m, n)`` or
+``torch.empty(n, m).t()``.  Every call runs on torch's current CUDA stream of
+the tensor's device, so it orders with surrounding torch work.  torch here is
+only device memory and streams; the arithmetic is the library's kernels.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import torch
+
+from . import _lib
+
+_DT = {torch.float64: "d", torch.float32: "s"}
+
+
+class ElGBError(RuntimeError):
+    pass
+
+
+class SingularMatrixError(ElGBError):
+    """The device path found an exact zero pivot (the reference throws
+    SingularMatrixException, src/lapack_like/factor/LU/Panel.hpp:51-52)."""
+
+
+class NonHPDMatrixError(ElGBError):
+    """A non-positive Cholesky pivot (the reference throws
+    NonHPDMatrixException, src/lapack_like/factor/Cholesky/LowerVariant3.hpp:29-30)."""
+
+
+def colmajor(m, n, dtype=torch.float64, device="cuda", ld=None):
+    ld = max(m, 1) if ld is None else ld
+    return torch.empty((n, ld), dtype=dtype, device=device).t()[:m]
+
+
+def to_colmajor(x):
+    """Column-major copy of a 2-D tensor (or a view of it if already so)."""
+    if x.dim() == 1:
+        x = x.reshape(-1, 1)
+    if x.stride(0) == 1 and (x.shape[1] <= 1 or x.stride(1) >= max(x.shape[0], 1)):
+        return x
+    return x.t().contiguous().t()
+
+
+def _ld(x):
+    if x.stride(0) != 1 and x.shape[0] > 1:
+        raise ValueError("matrix must be column-major (stride(0) == 1)")
+    return max(x.stride(1) if x.shape[1] > 1 else x.shape[0], 1)
+
+
+def _ptr(x):
+    return ctypes.c_void_p(x.data_ptr())
+
+
+class Context:
+    """One GPU, one stream binding, one scratch arena (ElGBContext)."""
+
+    def __init__(self, device=None):
+        self.lib = _lib.load()
+        dev = torch.device("cuda", torch.cuda.current_device() if device is None else device)
+        self.device = dev
+        h = ctypes.c_void_p()
+        rc = self.lib.ElGBCreate(ctypes.byref(h), dev.index)
+        if rc != 0:
+            raise ElGBError(f"ElGBCreate failed ({rc})")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.ElGBDestroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _bind(self):
+        s = torch.cuda.current_stream(self.device).cuda_stream
+        self.lib.ElGBSetStream(self.h, ctypes.c_void_p(s))
+
+    def _rc(self, rc, what):
+        if rc != 0:
+            raise ElGBError(f"{what} returned ElError {rc}")
+
+    def status(self):
+        """(info, err) of the last call; synchronizes the stream."""
+        info, err = ctypes.c_int(), ctypes.c_int()
+        self._rc(self.lib.ElGBStatus(self.h, ctypes.byref(info), ctypes.byref(err)), "status")
+        return info.value, err.value
+
+    def check(self, cholesky=False):
+        info, err = self.status()
+        if err:
+            raise ElGBError(f"device-side bounded wait gave up (code {err})")
+        if info:
+            raise (NonHPDMatrixError if cholesky else SingularMatrixError)(
+                f"info = {info}")
+
+    def launches(self):
+        return int(self.lib.ElGBLaunchCount(self.h))
+
+    # -- the path -----------------------------------------------------------
+    def lu(self, A, piv=None, nb=0):
+        """El::LU(A, P) in place; returns the int32 swap destinations."""
+        m, n = A.shape
+        if piv is None:
+            piv = torch.empty(min(m, n), dtype=torch.int32, device=A.device)
+        self._bind()
+        s = _DT[A.dtype]
+        self._rc(getattr(self.lib, f"ElGBLUPartialPiv_{s}")(self.h, m, n, _ptr(A), _ld(A),
+                                                            _ptr(piv), nb), "LU")
+        return piv
+
+    def lu_solve_after(self, A, piv, B, orientation=0):
+        n = A.shape[0]
+        self._bind()
+        s = _DT[A.dtype]
+        self._rc(getattr(self.lib, f"ElGBSolveAfterLUPartialPiv_{s}")(
+            self.h, orientation, n, _ptr(A), _ld(A), _ptr(piv), B.shape[1], _ptr(B), _ld(B)),
+            "SolveAfterLU")
+        return B
+
+    def cholesky(self, A, uplo=0, nb=0):
+        self._bind()
+        s = _DT[A.dtype]
+        self._rc(getattr(self.lib, f"ElGBCholesky_{s}")(self.h, uplo, A.shape[0], _ptr(A),
+                                                        _ld(A), nb), "Cholesky")
+        return A
+
+    def cholesky_solve_after(self, A, B, uplo=0):
+        self._bind()
+        s = _DT[A.dtype]
+        self._rc(getattr(self.lib, f"ElGBSolveAfterCholesky_{s}")(
+            self.h, uplo, A.shape[0], _ptr(A), _ld(A), B.shape[1], _ptr(B), _ld(B)),
+            "SolveAfterCholesky")
+        return B
+
+    def linear_solve(self, A, B, nb=0):
+        self._bind()
+        s = _DT[A.dtype]
+        self._rc(getattr(self.lib, f"ElGBLinearSolve_{s}")(
+            self.h, A.shape[0], _ptr(A), _ld(A), B.shape[1], _ptr(B), _ld(B), nb),
+            "LinearSolve")
+        return B
+
+    def hpd_solve(self, A, B, uplo=0, nb=0):
+        self._bind()
+        s = _DT[A.dtype]
+        self._rc(getattr(self.lib, f"ElGBHPDSolve_{s}")(
+            self.h, uplo, A.shape[0], _ptr(A), _ld(A), B.shape[1], _ptr(B), _ld(B), nb),
+            "HPDSolve")
+        return B
+
+    def residual(self, A, X, B, R=None):
+        n, q = B.shape
+        if R is None:
+            R = colmajor(n, q, torch.float64, A.device)
+        self._bind()
+        self._rc(self.lib.ElGBResidual_d(self.h, n, q, _ptr(A), _ld(A), _ptr(X), _ld(X),
+                                         _ptr(B), _ld(B), _ptr(R), _ld(R)), "Residual")
+        return R
+
+    def backward_error(self, A, X, B):
+        n, q = B.shape
+        out = ctypes.c_double()
+        self._bind()
+        self._rc(self.lib.ElGBBackwardError_d(self.h, n, q, _ptr(A), _ld(A), _ptr(X), _ld(X),
+                                              _ptr(B), _ld(B), ctypes.byref(out)),
+                 "BackwardError")
+        return out.value
+
+    def fp64_peak_tflops(self):
+        out = ctypes.c_double()
+        self._bind()
+        self._rc(self.lib.ElGBProbeFP64Peak(self.h, ctypes.byref(out)), "probe")
+        return out.value
+
+
+_default = {}
+
+
+def context(device=None) -> Context:
+    idx = torch.cuda.current_device() if device is None else device
+    if idx not in _default:
+        _default[idx] = Context(idx)
+    return _default[idx]

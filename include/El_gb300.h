@@ -1,0 +1,131 @@
+/*
+ * El_gb300.h — the subset of Elemental's C interface that the dense
+ * factor-and-solve path binds, exported by libelgb300.so with the same names,
+ * handle types and error codes, so that a C caller or the reference's ctypes
+ * layer (python/lapack_like/factor.py:525-560, python/lapack_like/solve.py)
+ * can load this library in place of libEl for that path.
+ *
+ * Each declaration cites the reference declaration it replaces.  Handles are
+ * opaque pointers to the El::Matrix<T> / El::Permutation of El_gb300.hpp;
+ * matrices are host memory, column-major, 32-bit ElInt.
+ */
+#ifndef EL_GB300_C_H
+#define EL_GB300_C_H
+
+#include <stdbool.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int ElInt; /* include/El/core/types.h (EL_USE_64BIT_INTS off) */
+
+/* include/El/core/types.h:45-54 */
+typedef enum {
+  EL_SUCCESS,
+  EL_ALLOC_ERROR,
+  EL_OUT_OF_BOUNDS_ERROR,
+  EL_ARG_ERROR,
+  EL_LOGIC_ERROR,
+  EL_RUNTIME_ERROR,
+  EL_ERROR = -1
+} ElError;
+/* include/El/core/types.h:55 */
+const char* ElErrorString(ElError error);
+
+/* include/El/core/types.h:211-228 */
+typedef enum { EL_NORMAL, EL_TRANSPOSE, EL_ADJOINT } ElOrientation;
+typedef enum { EL_LOWER, EL_UPPER } ElUpperOrLower;
+
+/* include/El/core/Matrix.h:20-31 */
+typedef struct ElMatrix_iDummy* ElMatrix_i;
+typedef struct ElMatrix_sDummy* ElMatrix_s;
+typedef struct ElMatrix_dDummy* ElMatrix_d;
+typedef const struct ElMatrix_iDummy* ElConstMatrix_i;
+typedef const struct ElMatrix_sDummy* ElConstMatrix_s;
+typedef const struct ElMatrix_dDummy* ElConstMatrix_d;
+
+/* include/El/core/Permutation.h:50-54 */
+typedef struct ElPermutationDummy* ElPermutation;
+typedef const struct ElPermutationDummy* ElConstPermutation;
+
+/* Matrix<T> (include/El/core/Matrix.h:36-260) */
+#define EL_GB_MATRIX_DECLS(S, T)                                              \
+  ElError ElMatrixCreate_##S(ElMatrix_##S* A);                                \
+  ElError ElMatrixDestroy_##S(ElConstMatrix_##S A);                           \
+  ElError ElMatrixEmpty_##S(ElMatrix_##S A);                                  \
+  ElError ElMatrixResize_##S(ElMatrix_##S A, ElInt height, ElInt width);      \
+  ElError ElMatrixResizeWithLDim_##S(ElMatrix_##S A, ElInt height,            \
+                                     ElInt width, ElInt ldim);                \
+  ElError ElMatrixAttach_##S(ElMatrix_##S A, ElInt height, ElInt width,       \
+                             T* buffer, ElInt ldim);                          \
+  ElError ElMatrixLockedAttach_##S(ElMatrix_##S A, ElInt height, ElInt width, \
+                                   const T* buffer, ElInt ldim);              \
+  ElError ElMatrixHeight_##S(ElConstMatrix_##S A, ElInt* height);             \
+  ElError ElMatrixWidth_##S(ElConstMatrix_##S A, ElInt* width);               \
+  ElError ElMatrixLDim_##S(ElConstMatrix_##S A, ElInt* ldim);                 \
+  ElError ElMatrixBuffer_##S(ElMatrix_##S A, T** buffer);                     \
+  ElError ElMatrixLockedBuffer_##S(ElConstMatrix_##S A, const T** buffer);    \
+  ElError ElMatrixGet_##S(ElConstMatrix_##S A, ElInt i, ElInt j, T* val);     \
+  ElError ElMatrixSet_##S(ElMatrix_##S A, ElInt i, ElInt j, T val);
+EL_GB_MATRIX_DECLS(i, ElInt)
+EL_GB_MATRIX_DECLS(s, float)
+EL_GB_MATRIX_DECLS(d, double)
+#undef EL_GB_MATRIX_DECLS
+
+/* Permutation (include/El/core/Permutation.h:55-199) */
+ElError ElPermutationCreate(ElPermutation* P);
+ElError ElPermutationDestroy(ElConstPermutation P);
+ElError ElPermutationEmpty(ElPermutation P);
+ElError ElPermutationMakeIdentity(ElPermutation P, ElInt size);
+ElError ElPermutationReserveSwaps(ElPermutation P, ElInt maxSwaps);
+ElError ElPermutationSwap(ElPermutation P, ElInt origin, ElInt dest);
+ElError ElPermutationHeight(ElConstPermutation P, ElInt* height);
+ElError ElPermutationWidth(ElConstPermutation P, ElInt* width);
+ElError ElPermutationParity(ElConstPermutation P, bool* parity);
+ElError ElPermutationIsSwapSequence(ElConstPermutation P, bool* isSwap);
+ElError ElPermutationIsImplicitSwapSequence(ElConstPermutation P,
+                                            bool* isImplicit);
+ElError ElPermutationPermuteRows_s(ElConstPermutation P, ElMatrix_s A,
+                                   ElInt offset);
+ElError ElPermutationPermuteRows_d(ElConstPermutation P, ElMatrix_d A,
+                                   ElInt offset);
+ElError ElPermutationExplicitVector(ElConstPermutation P, ElMatrix_i pVec);
+
+/* Blocksize (include/El/core/environment.h:48-52) */
+ElError ElBlocksize(ElInt* blocksize);
+ElError ElSetBlocksize(ElInt blocksize);
+ElError ElPushBlocksizeStack(ElInt blocksize);
+ElError ElPopBlocksizeStack(void);
+
+/* LU with partial pivoting (include/El/lapack_like/factor.h:500-516) */
+ElError ElLUPartialPiv_s(ElMatrix_s A, ElPermutation P);
+ElError ElLUPartialPiv_d(ElMatrix_d A, ElPermutation P);
+ElError ElSolveAfterLUPartialPiv_s(ElOrientation orientation,
+                                   ElConstMatrix_s A, ElConstPermutation P,
+                                   ElMatrix_s B);
+ElError ElSolveAfterLUPartialPiv_d(ElOrientation orientation,
+                                   ElConstMatrix_d A, ElConstPermutation P,
+                                   ElMatrix_d B);
+
+/* Cholesky (include/El/lapack_like/factor.h:24-41) */
+ElError ElCholesky_s(ElUpperOrLower uplo, ElMatrix_s A);
+ElError ElCholesky_d(ElUpperOrLower uplo, ElMatrix_d A);
+ElError ElSolveAfterCholesky_s(ElUpperOrLower uplo, ElOrientation orientation,
+                               ElConstMatrix_s A, ElMatrix_s B);
+ElError ElSolveAfterCholesky_d(ElUpperOrLower uplo, ElOrientation orientation,
+                               ElConstMatrix_d A, ElMatrix_d B);
+
+/* Dense solves (include/El/lapack_like/solve.h:21-22, 151-156) */
+ElError ElLinearSolve_s(ElConstMatrix_s A, ElMatrix_s B);
+ElError ElLinearSolve_d(ElConstMatrix_d A, ElMatrix_d B);
+ElError ElHPDSolve_s(ElUpperOrLower uplo, ElOrientation orientation,
+                     ElConstMatrix_s A, ElMatrix_s B);
+ElError ElHPDSolve_d(ElUpperOrLower uplo, ElOrientation orientation,
+                     ElConstMatrix_d A, ElMatrix_d B);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* EL_GB300_C_H */

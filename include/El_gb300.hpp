@@ -1,0 +1,147 @@
+/*
+ * El_gb300.hpp — C++ drop-in for Elemental's sequential dense
+ * factor-and-solve path, backed by the GB300 kernels of libelgb300.so.
+ *
+ * Same names, signatures, layouts and exceptions as the reference:
+ *   El::Matrix<T>            include/El/core/Matrix/decl.hpp:17-241
+ *   El::Permutation          include/El/core/Permutation.hpp:14-126
+ *   El::LU(A, P)             include/El/lapack_like/factor.hpp:376
+ *   El::lu::SolveAfter       include/El/lapack_like/factor.hpp:434
+ *   El::Cholesky(uplo, A)    include/El/lapack_like/factor.hpp:22
+ *   El::cholesky::SolveAfter include/El/lapack_like/factor.hpp:63
+ *   El::LinearSolve(A, B)    include/El/lapack_like/solve.hpp:20
+ *   El::HPDSolve             include/El/lapack_like/solve.hpp:190
+ *   El::Blocksize / SetBlocksize / PushBlocksizeStack / PopBlocksizeStack
+ *                            src/blas_like/blocksizes.cpp:37-60
+ * Matrices live in host memory (as El::Matrix does); each call moves them to
+ * the GPU, runs the device path and moves the results back.  Pinned host
+ * buffers (Attach to cudaMallocHost memory) make those copies fast.
+ */
+#ifndef EL_GB300_HPP
+#define EL_GB300_HPP
+
+#include <stdexcept>
+#include <vector>
+
+namespace El {
+
+typedef int Int;
+
+enum UpperOrLower { LOWER, UPPER };
+enum Orientation { NORMAL, TRANSPOSE, ADJOINT };
+
+// Exception types of the reference (include/El/core/environment/decl.hpp:209-231).
+class SingularMatrixException : public std::runtime_error {
+ public:
+  SingularMatrixException(const char* msg = "Matrix was singular")
+      : std::runtime_error(msg) {}
+};
+class NonHPDMatrixException : public std::runtime_error {
+ public:
+  NonHPDMatrixException(const char* msg = "Matrix was not HPD")
+      : std::runtime_error(msg) {}
+};
+
+template <typename T>
+class Matrix {
+ public:
+  Matrix() {}
+  Matrix(Int height, Int width) { Resize(height, width); }
+  Matrix(Int height, Int width, Int ldim) { Resize(height, width, ldim); }
+  Matrix(const Matrix<T>& A) { *this = A; }
+  Matrix<T>& operator=(const Matrix<T>& A);
+
+  void Empty();
+  void Resize(Int height, Int width);
+  void Resize(Int height, Int width, Int ldim);
+  void Attach(Int height, Int width, T* buffer, Int ldim);
+  void LockedAttach(Int height, Int width, const T* buffer, Int ldim);
+
+  Int Height() const { return height_; }
+  Int Width() const { return width_; }
+  Int LDim() const { return ldim_; }
+  bool Viewing() const { return viewing_; }
+  bool Locked() const { return locked_; }
+
+  T* Buffer();
+  T* Buffer(Int i, Int j) { return Buffer() + i + (long)j * ldim_; }
+  const T* LockedBuffer() const { return cbuf_; }
+  const T* LockedBuffer(Int i, Int j) const { return cbuf_ + i + (long)j * ldim_; }
+
+  T Get(Int i, Int j) const { return cbuf_[i + (long)j * ldim_]; }
+  void Set(Int i, Int j, T alpha) { Buffer()[i + (long)j * ldim_] = alpha; }
+  T& operator()(Int i, Int j) { return Buffer()[i + (long)j * ldim_]; }
+  const T& operator()(Int i, Int j) const { return cbuf_[i + (long)j * ldim_]; }
+
+ private:
+  Int height_ = 0, width_ = 0, ldim_ = 1;
+  T* buf_ = nullptr;
+  const T* cbuf_ = nullptr;
+  bool viewing_ = false, locked_ = false;
+  std::vector<T> mem_;
+};
+
+class Permutation {
+ public:
+  void Empty();
+  void MakeIdentity(Int size);
+  void ReserveSwaps(Int maxSwaps);
+  void Swap(Int origin, Int dest);
+
+  Int Height() const { return size_; }
+  Int Width() const { return size_; }
+  bool Parity() const;
+  bool IsSwapSequence() const { return true; }
+  bool IsImplicitSwapSequence() const { return true; }
+
+  const Matrix<Int> SwapDestinations() const;
+  template <typename T>
+  void PermuteRows(Matrix<T>& A, Int offset = 0) const;
+  template <typename T>
+  void InversePermuteRows(Matrix<T>& A, Int offset = 0) const;
+  void ExplicitVector(Matrix<Int>& p) const;
+
+  // Number of swaps recorded and direct access to their destinations.
+  Int NumSwaps() const { return numSwaps_; }
+  const Int* SwapDestBuffer() const { return dests_.data(); }
+  // Replaces the swap sequence by `numSwaps` destinations (origins 0..).
+  void SetSwapSequence(Int size, const Int* dests, Int numSwaps);
+
+ private:
+  Int size_ = 0;
+  Int numSwaps_ = 0;
+  std::vector<Int> dests_;
+};
+
+Int Blocksize();
+void SetBlocksize(Int blocksize);
+void PushBlocksizeStack(Int blocksize);
+void PopBlocksizeStack();
+
+template <typename F>
+void LU(Matrix<F>& A, Permutation& P);
+
+namespace lu {
+template <typename F>
+void SolveAfter(Orientation orientation, const Matrix<F>& A, const Permutation& P,
+                Matrix<F>& B);
+}  // namespace lu
+
+template <typename F>
+void Cholesky(UpperOrLower uplo, Matrix<F>& A);
+
+namespace cholesky {
+template <typename F>
+void SolveAfter(UpperOrLower uplo, Orientation orientation, const Matrix<F>& A,
+                Matrix<F>& B);
+}  // namespace cholesky
+
+template <typename F>
+void LinearSolve(const Matrix<F>& A, Matrix<F>& B);
+
+template <typename F>
+void HPDSolve(UpperOrLower uplo, Orientation orientation, const Matrix<F>& A, Matrix<F>& B);
+
+}  // namespace El
+
+#endif  // EL_GB300_HPP

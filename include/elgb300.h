@@ -1,0 +1,124 @@
+/*
+ * elgb300.h — device-level C ABI of the GB300 dense factor-and-solve library
+ * (libelgb300.so).  Plain pointers and sizes only.
+ *
+ * Every routine here works on DEVICE memory of the context's GPU and is
+ * enqueued on the context's stream; none of them synchronizes unless it says
+ * so.  Matrices are column-major with a leading dimension, as El::Matrix
+ * (reference include/El/core/Matrix/decl.hpp:17-241): element (i, j) of A is
+ * A[i + j*lda].  Pivots are Elemental's swap destinations, 0-based, 32-bit
+ * (Permutation::SwapDestinations, reference
+ * src/lapack_like/perm/Permutation.cpp:205-250; equal to LAPACK ipiv - 1).
+ *
+ * Return codes are Elemental's ElError values (reference
+ * include/El/core/types.h:45-54): 0 EL_SUCCESS, 1 EL_ALLOC_ERROR,
+ * 3 EL_ARG_ERROR, 4 EL_LOGIC_ERROR, 5 EL_RUNTIME_ERROR (singular / not HPD /
+ * CUDA failure), -1 EL_ERROR.
+ *
+ * Numerical failures are reported through the context's status word (see
+ * ElGBStatus): info = first zero pivot (LU) or first non-positive diagonal
+ * (Cholesky), 1-based, 0 if none — the conditions under which the reference
+ * throws SingularMatrixException (src/lapack_like/factor/LU/Panel.hpp:51-52)
+ * and NonHPDMatrixException
+ * (src/lapack_like/factor/Cholesky/LowerVariant3.hpp:29-30).
+ */
+#ifndef ELGB300_H
+#define ELGB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct ElGBContextImpl* ElGBContext;
+
+/* Context: one GPU, one stream, one growable scratch arena. */
+int ElGBCreate(ElGBContext* ctx, int device);
+int ElGBDestroy(ElGBContext ctx);
+/* Use `stream` (a cudaStream_t) for subsequent calls; NULL restores the
+ * context's own stream. */
+int ElGBSetStream(ElGBContext ctx, void* stream);
+int ElGBSynchronize(ElGBContext ctx);
+/* Synchronizes, then reads the status word of the last call:
+ * info (see above) and err (nonzero if a bounded device-side wait gave up). */
+int ElGBStatus(ElGBContext ctx, int* info, int* err);
+/* Algorithmic blocksize, El::Blocksize() / El::SetBlocksize()
+ * (reference src/blas_like/blocksizes.cpp:37-60); default 128. */
+int ElGBBlocksize(void);
+int ElGBSetBlocksize(int nb);
+/* Number of kernel launches this context has issued so far. */
+long long ElGBLaunchCount(ElGBContext ctx);
+
+/* El::LU(A, P) with partial pivoting (reference
+ * src/lapack_like/factor/LU.cpp:104-138): A (m x n) is overwritten by the
+ * packed unit-lower L and upper U; swapDests (min(m,n) ints, device) receives
+ * P's swap destinations.  nb <= 0 uses ElGBBlocksize(). */
+int ElGBLUPartialPiv_d(ElGBContext ctx, int m, int n, double* A, int lda,
+                       int* swapDests, int nb);
+int ElGBLUPartialPiv_s(ElGBContext ctx, int m, int n, float* A, int lda,
+                       int* swapDests, int nb);
+
+/* lu::SolveAfter(orientation, A, P, B) (reference
+ * src/lapack_like/factor/LU/SolveAfter.hpp:66-92): orientation 0 NORMAL,
+ * 1 TRANSPOSE, 2 ADJOINT (= TRANSPOSE for real data).  B is n x nrhs. */
+int ElGBSolveAfterLUPartialPiv_d(ElGBContext ctx, int orientation, int n,
+                                 const double* A, int lda,
+                                 const int* swapDests, int nrhs, double* B,
+                                 int ldb);
+int ElGBSolveAfterLUPartialPiv_s(ElGBContext ctx, int orientation, int n,
+                                 const float* A, int lda, const int* swapDests,
+                                 int nrhs, float* B, int ldb);
+
+/* El::Cholesky(uplo, A) (reference src/lapack_like/factor/Cholesky.cpp:26-38):
+ * uplo 0 LOWER, 1 UPPER; only that triangle is read and written. */
+int ElGBCholesky_d(ElGBContext ctx, int uplo, int n, double* A, int lda,
+                   int nb);
+int ElGBCholesky_s(ElGBContext ctx, int uplo, int n, float* A, int lda,
+                   int nb);
+
+/* cholesky::SolveAfter(uplo, NORMAL, A, B) (reference
+ * src/lapack_like/factor/Cholesky/SolveAfter.hpp:15-43). */
+int ElGBSolveAfterCholesky_d(ElGBContext ctx, int uplo, int n,
+                             const double* A, int lda, int nrhs, double* B,
+                             int ldb);
+int ElGBSolveAfterCholesky_s(ElGBContext ctx, int uplo, int n,
+                             const float* A, int lda, int nrhs, float* B,
+                             int ldb);
+
+/* El::LinearSolve(A, B) (reference src/lapack_like/solve/Linear.cpp:212-218):
+ * A is left untouched (the reference copies it); B is overwritten by X.
+ * Gaussian elimination on [A | B] as RowEchelon (Linear.cpp:30-77), then
+ * the upper-triangular solve. */
+int ElGBLinearSolve_d(ElGBContext ctx, int n, const double* A, int lda,
+                      int nrhs, double* B, int ldb, int nb);
+int ElGBLinearSolve_s(ElGBContext ctx, int n, const float* A, int lda,
+                      int nrhs, float* B, int ldb, int nb);
+
+/* El::HPDSolve(uplo, NORMAL, A, B) (reference src/lapack_like/solve/HPD.cpp:47-55). */
+int ElGBHPDSolve_d(ElGBContext ctx, int uplo, int n, const double* A, int lda,
+                   int nrhs, double* B, int ldb, int nb);
+int ElGBHPDSolve_s(ElGBContext ctx, int uplo, int n, const float* A, int lda,
+                   int nrhs, float* B, int ldb, int nb);
+
+/* FP64 residual R = B - A X (n x nrhs, nrhs <= 16), deterministic order;
+ * the residual of the refinement loop of reference
+ * include/El/lapack_like/solve/Refined.hpp:70-73. */
+int ElGBResidual_d(ElGBContext ctx, int n, int nrhs, const double* A,
+                   int lda, const double* X, int ldx, const double* B,
+                   int ldb, double* R, int ldr);
+
+/* Normwise backward error max_j ||b_j - A x_j||_2 /
+ * (||A||_F ||x_j||_2 + ||b_j||_2), computed in FP64 on the device;
+ * synchronizes and writes the value to *berr (host). */
+int ElGBBackwardError_d(ElGBContext ctx, int n, int nrhs, const double* A,
+                        int lda, const double* X, int ldx, const double* B,
+                        int ldb, double* berr);
+
+/* Measures the device FP64 FMA rate (TFLOP/s) with a dependent-chain probe;
+ * synchronizes. */
+int ElGBProbeFP64Peak(ElGBContext ctx, double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ELGB300_H */

@@ -1,0 +1,110 @@
+"""Generates the golden fixtures in this folder by running the REFERENCE's own
+sequential path (Elemental's El::LU, lu::SolveAfter, El::Cholesky,
+cholesky::SolveAfter, El::LinearSolve, El::HPDSolve), compiled from its
+sources into oracle/_ref/elref by oracle/build_ref.sh.
+
+Run (where the reference tree is present):
+    oracle/build_ref.sh && python tests/golden/gen_golden.py
+
+Each fixture is an .npz with the inputs (or, for the large config-1 case, the
+seed plus a SHA-256 of the regenerated input), the blocksize, the
+reference's outputs and its exit status.  The reference has no golden vectors
+of its own (its tests check residual ratios only), so these pin the parity of
+the oracle restatement and of the GPU path.
+"""
+import hashlib
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from elemental_gb300 import matrices as mats  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+
+F64, I32 = np.float64, np.int32
+
+
+def sha(a):
+    return hashlib.sha256(np.asfortranarray(a).tobytes(order="F")).hexdigest()
+
+
+def save(name, **kw):
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **kw)
+    print("wrote", name)
+
+
+def lu_case(name, A, nb, dtype=F64, store_input=True):
+    st, out = O.ref_run("lu", nb=nb, dtype=dtype, inputs=[A], out_dtypes=[dtype, I32])
+    kw = dict(op="lu", nb=nb, status=st, dtype=np.dtype(dtype).name)
+    if store_input:
+        kw["A"] = A.astype(dtype)
+    if st == 0:
+        kw["LU"], kw["piv"] = out[0], out[1].ravel()
+    save(name, **kw)
+
+
+def main():
+    if not O.have_reference():
+        sys.exit("oracle/_ref/elref missing: run oracle/build_ref.sh first")
+    s = mats.BASE_SEED
+    # LU (tests/lapack_like/LU.cpp defaults: --height 100 --nb 96)
+    lu_case("lu_100_nb96", mats.gaussian(100, 100, s + 100), 96)
+    lu_case("lu_gepp_growth_100_nb96", mats.gepp_growth(100), 96)
+    lu_case("lu_129_nb32", mats.gaussian(129, 129, s + 129), 32)
+    lu_case("lu_150x100_nb32", mats.gaussian(150, 100, s + 150), 32)
+    lu_case("lu_100x150_nb32", mats.gaussian(100, 150, s + 151), 32)
+    lu_case("lu_33_nb32", mats.gaussian(33, 33, s + 33), 32)
+    lu_case("lu_1_nb128", mats.gaussian(1, 1, s + 1), 128)
+    Z = mats.gaussian(50, 50, s + 50)
+    Z[:, 17] = 0.0
+    lu_case("lu_singular_50_nb16", Z, 16)
+    lu_case("lu_s_100_nb96", mats.gaussian(100, 100, s + 101), 96, dtype=np.float32)
+
+    # lu::SolveAfter NORMAL / TRANSPOSE
+    for o in ("N", "T"):
+        A = mats.gaussian(120, 120, s + 201)
+        B = mats.gaussian(120, 3, s + 202)
+        st, out = O.ref_run("lusolve", o, nb=32, inputs=[A, B], out_dtypes=[F64, I32, F64])
+        save(f"lusolve_{o}_120_nb32", op="lusolve", orient=o, nb=32, status=st, A=A, B=B,
+             LU=out[0], piv=out[1].ravel(), X=out[2])
+
+    # Cholesky (tests/lapack_like/Cholesky.cpp: HermitianUniformSpectrum(m,1e-9,10), m 100, nb 96)
+    H = mats.hermitian_uniform_spectrum(100, 1e-9, 10.0, s + 400)
+    S = mats.spd(120, s + 401)
+    for u in ("L", "U"):
+        st, out = O.ref_run("chol", u, nb=96, inputs=[H], out_dtypes=[F64])
+        save(f"chol_{u}_hus100_nb96", op="chol", uplo=u, nb=96, status=st, A=H, C=out[0])
+        B = mats.gaussian(120, 4, s + 402)
+        st, out = O.ref_run("cholsolve", u, nb=32, inputs=[S, B], out_dtypes=[F64, F64])
+        save(f"cholsolve_{u}_spd120_nb32", op="cholsolve", uplo=u, nb=32, status=st, A=S, B=B,
+             C=out[0], X=out[1])
+        st, out = O.ref_run("hpdsolve", u, nb=32, inputs=[S, B], out_dtypes=[F64])
+        save(f"hpdsolve_{u}_spd120_nb32", op="hpdsolve", uplo=u, nb=32, status=st, A=S, B=B,
+             X=out[0])
+    G = mats.gaussian(60, 60, s + 403)
+    st, _ = O.ref_run("chol", "L", nb=16, inputs=[G], out_dtypes=[F64])
+    save("chol_nonhpd_60_nb16", op="chol", uplo="L", nb=16, status=st, A=G)
+
+    # El::LinearSolve
+    A = mats.gaussian(120, 120, s + 500)
+    B = mats.gaussian(120, 5, s + 501)
+    st, out = O.ref_run("linsolve", nb=32, inputs=[A, B], out_dtypes=[F64])
+    save("linsolve_120_nb32", op="linsolve", nb=32, status=st, A=A, B=B, X=out[0])
+
+    # Config 1: n = 1024, 1 RHS, iid N(0,1), nb = 128 (the default blocksize)
+    n = 1024
+    A = mats.gaussian(n, n, s + 1)
+    b = mats.gaussian(n, 1, s + 1001)
+    st, out = O.ref_run("lusolve", "N", nb=128, inputs=[A, b], out_dtypes=[F64, I32, F64])
+    berr = O.backward_error(A, out[2], b)
+    save("cfg1_lusolve_1024_nb128", op="lusolve", orient="N", nb=128, status=st, n=n,
+         seed_A=s + 1, seed_b=s + 1001, sha_A=sha(A), sha_b=sha(b), piv=out[1].ravel(),
+         X=out[2], berr=berr, LU_fro=np.linalg.norm(out[0]), LU_diag=np.diag(out[0]).copy())
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,98 @@
+"""The CPU oracle (oracle/el_oracle.c) against golden fixtures produced by the
+reference itself (tests/golden/gen_golden.py).  Pivots must match exactly;
+values match bit-for-bit on the BLAS the fixtures were made with and to
+rounding on any other BLAS build."""
+import glob
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+from elemental_gb300 import matrices as mats
+from oracle import oracle as O
+
+GOLD = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+RTOL = 1e-11
+
+
+def close(a, b, scale=1.0):
+    a, b = np.asarray(a), np.asarray(b)
+    assert a.shape == b.shape
+    tol = RTOL * max(scale, np.abs(b).max() if b.size else 0.0, 1.0)
+    assert np.abs(a - b).max(initial=0.0) <= tol, np.abs(a - b).max()
+
+
+def _name(p):
+    return os.path.basename(p)[:-4]
+
+
+@pytest.mark.parametrize("path", [p for p in GOLD if not _name(p).startswith("cfg1")],
+                         ids=[_name(p) for p in GOLD if not _name(p).startswith("cfg1")])
+def test_oracle_matches_reference_fixture(path):
+    g = np.load(path)
+    op = str(g["op"])
+    st = int(g["status"])
+    nb = int(g["nb"])
+    if op == "lu":
+        dt = np.float32 if str(g["dtype"]) == "float32" else np.float64
+        if st != 0:
+            with pytest.raises(O.OracleError) as e:
+                O.lu(g["A"], nb=nb, dtype=dt)
+            assert e.value.status == st
+            return
+        LU, piv = O.lu(g["A"], nb=nb, dtype=dt)
+        assert np.array_equal(piv, g["piv"])
+        if dt == np.float32:
+            assert np.abs(LU - g["LU"]).max() <= 1e-4 * max(1.0, np.abs(g["LU"]).max())
+        else:
+            close(LU, g["LU"])
+    elif op == "lusolve":
+        LU, piv = O.lu(g["A"], nb=nb)
+        assert np.array_equal(piv, g["piv"])
+        X = O.lu_solve_after(LU, piv, g["B"], 0 if str(g["orient"]) == "N" else 1)
+        close(X, g["X"])
+    elif op == "chol":
+        if st != 0:
+            with pytest.raises(O.OracleError) as e:
+                O.cholesky(g["A"], str(g["uplo"]), nb=nb)
+            assert e.value.status == st
+            return
+        C = O.cholesky(g["A"], str(g["uplo"]), nb=nb)
+        close(C, g["C"])
+    elif op == "cholsolve":
+        C = O.cholesky(g["A"], str(g["uplo"]), nb=nb)
+        close(C, g["C"])
+        close(O.cholesky_solve_after(C, g["B"], str(g["uplo"])), g["X"])
+    elif op == "hpdsolve":
+        close(O.hpd_solve(g["A"], g["B"], str(g["uplo"]), nb=nb), g["X"])
+    elif op == "linsolve":
+        close(O.linear_solve(g["A"], g["B"], nb=nb), g["X"])
+    else:
+        pytest.fail(op)
+
+
+def test_oracle_config1_against_reference():
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "cfg1_lusolve_1024_nb128.npz"))
+    n = int(g["n"])
+    A = mats.gaussian(n, n, int(g["seed_A"]))
+    b = mats.gaussian(n, 1, int(g["seed_b"]))
+    assert hashlib.sha256(A.tobytes(order="F")).hexdigest() == str(g["sha_A"]), \
+        "input generator is not reproducible on this platform"
+    assert hashlib.sha256(b.tobytes(order="F")).hexdigest() == str(g["sha_b"])
+    LU, piv = O.lu(A, nb=128)
+    assert np.array_equal(piv, g["piv"])
+    X = O.lu_solve_after(LU, piv, b)
+    close(X, g["X"], scale=1e3)
+    berr = O.backward_error(A, X, b)
+    assert berr <= 4 * n * np.finfo(np.float64).eps
+    assert abs(berr - float(g["berr"])) <= 4 * n * np.finfo(np.float64).eps
+
+
+def test_backward_error_metric():
+    A = np.eye(3)
+    X = np.ones((3, 1))
+    assert O.backward_error(A, X, A @ X) == 0.0
+    B = A @ X + np.array([[1e-3], [0], [0]])
+    be = O.backward_error(A, X, B)
+    assert abs(be - 1e-3 / (np.sqrt(3) * np.sqrt(3) + np.linalg.norm(B))) < 1e-15
