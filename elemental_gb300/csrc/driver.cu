@@ -321,6 +321,7 @@ cudaError_t getrs(Context* ctx, int orient, int n, const T* A, long lda, const i
   Carver cv(ctx);
   int* perm = cv.take<int>(n);
   T* W = cv.take<T>((size_t)n * nrhs);
+  if (!perm || !W) return cudaErrorMemoryAllocation;
   if (perm_in) {
     perm = const_cast<int*>(perm_in);
   } else {
@@ -420,6 +421,7 @@ cudaError_t linear_solve(Context* ctx, int n, const T* A, long lda, int nrhs, T*
   if (e != cudaSuccess) return e;
   T* W = cv.take<T>((size_t)n * n);
   int* ipiv = cv.take<int>(n);
+  if (!W || !ipiv) return cudaErrorMemoryAllocation;
   e = cudaMemcpy2DAsync(W, (size_t)n * sizeof(T), A, lda * sizeof(T), (size_t)n * sizeof(T), n,
                         cudaMemcpyDeviceToDevice, ctx->stream);
   if (e != cudaSuccess) return e;
@@ -447,6 +449,7 @@ cudaError_t hpd_solve(Context* ctx, int uplo, int n, const T* A, long lda, int n
   if (e != cudaSuccess) return e;
   Carver cv(ctx);
   T* W = cv.take<T>((size_t)n * n);
+  if (!W) return cudaErrorMemoryAllocation;
   e = cudaMemcpy2DAsync(W, (size_t)n * sizeof(T), A, lda * sizeof(T), (size_t)n * sizeof(T), n,
                         cudaMemcpyDeviceToDevice, ctx->stream);
   if (e != cudaSuccess) return e;
@@ -472,6 +475,7 @@ cudaError_t residual(Context* ctx, int n, int q, const double* A, long lda, cons
     if (e != cudaSuccess) return e;
     Carver cv(ctx);
     double* partial = cv.take<double>((size_t)nchunks * n * 16);
+    if (!partial) return cudaErrorMemoryAllocation;
     ELGB_CHECK(launch_residual_f64(n, qc, A, lda, X + (long)c * ldx, ldx, B + (long)c * ldb,
                                    ldb, R + (long)c * ldr, ldr, partial, ctx->stream), 2);
   }
@@ -482,6 +486,7 @@ cudaError_t backward_error(Context* ctx, int n, int q, const double* A, long lda
                            const double* X, long ldx, const double* B, long ldb,
                            double* berr) {
   const size_t need = align256((size_t)n * q * sizeof(double)) +
+                      align256((size_t)(n + 2) * sizeof(double)) +
                       3 * align256((size_t)(q + 2) * sizeof(double)) +
                       align256((size_t)64 * (std::max(n, q) + 1) * sizeof(double)) +
                       align256((size_t)((n + 4095) / 4096) * n * 16 * sizeof(double));
@@ -495,6 +500,7 @@ cudaError_t backward_error(Context* ctx, int n, int q, const double* A, long lda
   double* nB = cv.take<double>(q + 2);
   double* partial = cv.take<double>((size_t)64 * (std::max(n, q) + 1));
   double* rpart = cv.take<double>((size_t)((n + 4095) / 4096) * n * 16);
+  if (!R || !nA || !nX || !nR || !nB || !partial || !rpart) return cudaErrorMemoryAllocation;
   for (int c = 0; c < q; c += 16) {
     const int qc = std::min(16, q - c);
     ELGB_CHECK(launch_residual_f64(n, qc, A, lda, X + (long)c * ldx, ldx, B + (long)c * ldb,
@@ -592,7 +598,7 @@ int ElGBDestroy(ElGBContext ctx) {
 
 int ElGBSetStream(ElGBContext ctx, void* stream) {
   if (!ctx) return elgb::kElArgError;
-  ctx->stream = stream ? static_cast<cudaStream_t>(stream) : ctx->own_stream;
+  ctx->stream = static_cast<cudaStream_t>(stream);  // NULL: the legacy default stream
   return 0;
 }
 

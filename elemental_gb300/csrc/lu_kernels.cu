@@ -118,8 +118,8 @@ getf2_panel_kernel(PanelParams<T> p) {
       T v = T(-1);
       int r = -1;
       for (int g = lane; g < G; g += 32) {
-        const T gv = p.s.cand_val[par * maxG + g];
-        const int gr = p.s.cand_row[par * maxG + g];
+        const T gv = __ldcg(p.s.cand_val + par * maxG + g);
+        const int gr = __ldcg(p.s.cand_row + par * maxG + g);
         if (argmax_better(gv, gr, v, r)) {
           v = gv;
           r = gr;
@@ -131,10 +131,11 @@ getf2_panel_kernel(PanelParams<T> p) {
     __syncthreads();
     const int piv = s_piv;
     if (tid < w) {
-      const T d = p.s.diag_data[par * W + tid];
+      // cross-CTA data: read at L2 (never a stale L1 line)
+      const T d = __ldcg(p.s.diag_data + par * W + tid);
       s_d[tid] = d;
       s_u[tid] = (piv == j) ? d
-                            : p.s.cand_data[((long)par * maxG + piv / R) * W + tid];
+                            : __ldcg(p.s.cand_data + ((long)par * maxG + piv / R) * W + tid);
     }
     __syncthreads();
     if (b == 0 && tid == 0) p.ipiv[j] = p.row_base + piv;

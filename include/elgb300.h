@@ -34,8 +34,8 @@ typedef struct ElGBContextImpl* ElGBContext;
 /* Context: one GPU, one stream, one growable scratch arena. */
 int ElGBCreate(ElGBContext* ctx, int device);
 int ElGBDestroy(ElGBContext ctx);
-/* Use `stream` (a cudaStream_t) for subsequent calls; NULL restores the
- * context's own stream. */
+/* Use `stream` (a cudaStream_t) for subsequent calls; NULL selects the
+ * legacy default stream.  A new context uses a stream of its own. */
 int ElGBSetStream(ElGBContext ctx, void* stream);
 int ElGBSynchronize(ElGBContext ctx);
 /* Synchronizes, then reads the status word of the last call:
