@@ -1,0 +1,27 @@
+// Tensor-core (tcgen05) GEMM update used by the low-precision factorizations.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace elgb {
+
+// Operand precision of the tensor-core products (accumulation is FP32).
+enum TcKind : int {
+  kTcBF16 = 0,  // tcgen05.mma kind::f16 with BF16 operands
+  kTcTF32 = 1,  // tcgen05.mma kind::tf32
+  kTcTF32x3 = 2,  // kind::tf32, operands split hi + lo, three products (~FP32)
+};
+
+// Bytes of device workspace launch_tc_gemm_sub needs for its packed operands.
+size_t tc_gemm_workspace_bytes(int kind, int m, int n, int K);
+
+// C[m x n] -= A[m x K] * B[K x n]; A, B, C FP32 column-major.  Packs A and B
+// into `ws` (tc_gemm_workspace_bytes) in the operand precision, then runs the
+// tcgen05 kernel.  *nlaunch receives the number of kernels enqueued.
+cudaError_t launch_tc_gemm_sub(int kind, int m, int n, int K, const float* A, long lda,
+                               const float* B, long ldb, float* C, long ldc, void* ws,
+                               DevStatus* st, cudaStream_t stream, int* nlaunch);
+
+}  // namespace elgb
