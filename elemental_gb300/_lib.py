@@ -54,6 +54,9 @@ def load():
         _sig(lib, f"ElGBLinearSolve_{s}", c_int, vp, c_int, vp, c_int, c_int, vp, c_int, c_int)
         _sig(lib, f"ElGBHPDSolve_{s}", c_int, vp, c_int, c_int, vp, c_int, c_int, vp, c_int,
              c_int)
+    _sig(lib, "ElGBLUPartialPivMixed_s", c_int, vp, c_int, c_int, vp, c_int, vp, c_int, c_int)
+    _sig(lib, "ElGBGemmSubTC", c_int, vp, c_int, c_int, c_int, c_int, vp, c_int, vp, c_int, vp,
+         c_int)
     _sig(lib, "ElGBResidual_d", c_int, vp, c_int, c_int, vp, c_int, vp, c_int, vp, c_int, vp,
          c_int)
     _sig(lib, "ElGBBackwardError_d", c_int, vp, c_int, c_int, vp, c_int, vp, c_int, vp, c_int,

@@ -15,6 +15,7 @@
 #include "../../include/elgb300.h"
 #include "driver.h"
 #include "kernels.h"
+#include "tc_gemm.h"
 
 namespace elgb {
 
@@ -98,9 +99,38 @@ static PanelScratch<T> carve_panel(Carver& cv, int maxG) {
 // ---------------------------------------------------------------------------
 // LU with partial pivoting
 // ---------------------------------------------------------------------------
+// How the float path's contractions run: SIMT FP32 FMA (tc_kind < 0) or on
+// the tensor cores (tc_gemm.cu) with `ws` holding the packed operands.
+struct GemmCfg {
+  int tc_kind = -1;
+  void* ws = nullptr;
+};
+
+static cudaError_t gemm_sub(Context* ctx, const GemmCfg&, int m, int n, int k, const double* A,
+                            long lda, const double* B, long ldb, double* C, long ldc) {
+  ELGB_CHECK(launch_gemm_simt<double>(false, false, m, n, k, -1.0, A, lda, B, ldb, 1.0, C, ldc,
+                                      0, ctx->stream), 1);
+  return cudaSuccess;
+}
+
+static cudaError_t gemm_sub(Context* ctx, const GemmCfg& g, int m, int n, int k, const float* A,
+                            long lda, const float* B, long ldb, float* C, long ldc) {
+  if (g.tc_kind >= 0 && m >= 64 && n >= 64 && k >= 16) {
+    int nl = 0;
+    cudaError_t e = launch_tc_gemm_sub(g.tc_kind, m, n, k, A, lda, B, ldb, C, ldc, g.ws,
+                                       ctx->status, ctx->stream, &nl);
+    ctx->launches += nl;
+    return e;
+  }
+  ELGB_CHECK(launch_gemm_simt<float>(false, false, m, n, k, -1.f, A, lda, B, ldb, 1.f, C, ldc,
+                                     0, ctx->stream), 1);
+  return cudaSuccess;
+}
+
 template <typename T>
 struct LuState {
   Context* ctx;
+  GemmCfg gemm;
   T* A;
   long lda;
   int m, n;
@@ -117,17 +147,18 @@ struct LuState {
 // Blocked TRSM, left / lower / unit: B := L11^{-1} B with L11 nb x nb (any
 // nb): 128-row diagonal solves plus GEMM updates of the rows below.
 template <typename T>
-static cudaError_t trsm_llnu(Context* ctx, const T* L, long ldl, int nb, T* Bm, long ldb,
-                             int ncols) {
+static cudaError_t trsm_llnu(Context* ctx, const GemmCfg& g, const T* L, long ldl, int nb,
+                             T* Bm, long ldb, int ncols) {
   for (int i0 = 0; i0 < nb; i0 += 128) {
     const int ib = std::min(128, nb - i0);
     ELGB_CHECK(launch_trsm_block<T>(L + i0 + (long)i0 * ldl, ldl, Bm + i0, ldb, ib, ncols,
                                     true, true, false, false, ctx->stream), 1);
     const int rest = nb - i0 - ib;
-    if (rest > 0)
-      ELGB_CHECK(launch_gemm_simt<T>(false, false, rest, ncols, ib, T(-1),
-                                     L + (i0 + ib) + (long)i0 * ldl, ldl, Bm + i0, ldb, T(1),
-                                     Bm + i0 + ib, ldb, 0, ctx->stream), 1);
+    if (rest > 0) {
+      cudaError_t e = gemm_sub(ctx, g, rest, ncols, ib, L + (i0 + ib) + (long)i0 * ldl, ldl,
+                               Bm + i0, ldb, Bm + i0 + ib, ldb);
+      if (e != cudaSuccess) return e;
+    }
   }
   return cudaSuccess;
 }
@@ -174,10 +205,10 @@ static cudaError_t panel_rec(LuState<T>& s, int c0, int w) {
   T* A12 = s.A + c0 + (long)(c0 + w1) * s.lda;
   T* A21 = s.A + (c0 + w1) + (long)c0 * s.lda;
   T* A22 = s.A + (c0 + w1) + (long)(c0 + w1) * s.lda;
-  e = trsm_llnu<T>(ctx, A11, s.lda, w1, A12, s.lda, w2);
+  e = trsm_llnu<T>(ctx, s.gemm, A11, s.lda, w1, A12, s.lda, w2);
   if (e != cudaSuccess) return e;
-  ELGB_CHECK(launch_gemm_simt<T>(false, false, s.m - c0 - w1, w2, w1, T(-1), A21, s.lda, A12,
-                                 s.lda, T(1), A22, s.lda, 0, ctx->stream), 1);
+  e = gemm_sub(ctx, s.gemm, s.m - c0 - w1, w2, w1, A21, s.lda, A12, s.lda, A22, s.lda);
+  if (e != cudaSuccess) return e;
   e = panel_rec(s, c0 + w1, w2);
   if (e != cudaSuccess) return e;
   return apply_swaps(s, c0 + w1, w2, c0, c0 + w1, 0, 0, false);
@@ -199,24 +230,25 @@ static cudaError_t getrf_run(LuState<T>& s, int nb) {
     const int n2 = s.n - k - jb, m2 = s.m - k - jb;
     T* A11 = s.A + k + (long)k * s.lda;
     if (n2 > 0) {
-      e = trsm_llnu<T>(ctx, A11, s.lda, jb, s.A + k + (long)(k + jb) * s.lda, s.lda, n2);
+      e = trsm_llnu<T>(ctx, s.gemm, A11, s.lda, jb, s.A + k + (long)(k + jb) * s.lda, s.lda,
+                       n2);
       if (e != cudaSuccess) return e;
     }
     if (s.Bc && s.nbc > 0) {
-      e = trsm_llnu<T>(ctx, A11, s.lda, jb, s.Bc + k, s.ldbc, s.nbc);
+      e = trsm_llnu<T>(ctx, s.gemm, A11, s.lda, jb, s.Bc + k, s.ldbc, s.nbc);
       if (e != cudaSuccess) return e;
     }
-    if (m2 > 0 && n2 > 0)
-      ELGB_CHECK(launch_gemm_simt<T>(false, false, m2, n2, jb, T(-1),
-                                     s.A + (k + jb) + (long)k * s.lda, s.lda,
-                                     s.A + k + (long)(k + jb) * s.lda, s.lda, T(1),
-                                     s.A + (k + jb) + (long)(k + jb) * s.lda, s.lda, 0,
-                                     ctx->stream), 1);
-    if (m2 > 0 && s.Bc && s.nbc > 0)
-      ELGB_CHECK(launch_gemm_simt<T>(false, false, m2, s.nbc, jb, T(-1),
-                                     s.A + (k + jb) + (long)k * s.lda, s.lda, s.Bc + k,
-                                     s.ldbc, T(1), s.Bc + k + jb, s.ldbc, 0, ctx->stream),
-                 1);
+    if (m2 > 0 && n2 > 0) {
+      e = gemm_sub(ctx, s.gemm, m2, n2, jb, s.A + (k + jb) + (long)k * s.lda, s.lda,
+                   s.A + k + (long)(k + jb) * s.lda, s.lda,
+                   s.A + (k + jb) + (long)(k + jb) * s.lda, s.lda);
+      if (e != cudaSuccess) return e;
+    }
+    if (m2 > 0 && s.Bc && s.nbc > 0) {
+      e = gemm_sub(ctx, s.gemm, m2, s.nbc, jb, s.A + (k + jb) + (long)k * s.lda, s.lda,
+                   s.Bc + k, s.ldbc, s.Bc + k + jb, s.ldbc);
+      if (e != cudaSuccess) return e;
+    }
   }
   return cudaSuccess;
 }
@@ -241,17 +273,24 @@ static cudaError_t setup_lu_state(Context* ctx, LuState<T>& s, Carver& cv, int n
 }
 
 template <typename T>
-cudaError_t getrf(Context* ctx, int m, int n, T* A, long lda, int* ipiv, int nb) {
+cudaError_t getrf(Context* ctx, int m, int n, T* A, long lda, int* ipiv, int nb, int tc_kind) {
   if (nb <= 0) nb = g_blocksize;
   cudaError_t e = ctx->begin_call();
   if (e != cudaSuccess) return e;
   if (m == 0 || n == 0) return cudaSuccess;
-  e = ctx->ensure(getrf_scratch_bytes<T>(ctx, nb));
+  const bool tc = sizeof(T) == 4 && tc_kind >= 0;
+  const size_t tcb = tc ? tc_gemm_workspace_bytes(tc_kind, m, std::max(n, nb), nb) : 0;
+  e = ctx->ensure(getrf_scratch_bytes<T>(ctx, nb) + align256(tcb));
   if (e != cudaSuccess) return e;
   Carver cv(ctx);
   LuState<T> s{};
   e = setup_lu_state(ctx, s, cv, nb);
   if (e != cudaSuccess) return e;
+  if (tc) {
+    s.gemm.tc_kind = tc_kind;
+    s.gemm.ws = cv.take<char>(tcb);
+    if (!s.gemm.ws) return cudaErrorMemoryAllocation;
+  }
   s.A = A;
   s.lda = lda;
   s.m = m;
@@ -536,8 +575,8 @@ cudaError_t backward_error(Context* ctx, int n, int q, const double* A, long lda
   return cudaSuccess;
 }
 
-template cudaError_t getrf<double>(Context*, int, int, double*, long, int*, int);
-template cudaError_t getrf<float>(Context*, int, int, float*, long, int*, int);
+template cudaError_t getrf<double>(Context*, int, int, double*, long, int*, int, int);
+template cudaError_t getrf<float>(Context*, int, int, float*, long, int*, int, int);
 template cudaError_t getrs<double>(Context*, int, int, const double*, long, const int*, int,
                                    double*, long, const int*);
 template cudaError_t getrs<float>(Context*, int, int, const float*, long, const int*, int,
@@ -632,7 +671,7 @@ long long ElGBLaunchCount(ElGBContext ctx) { return ctx ? ctx->launches : -1; }
     if (int r = arg_ok(ctx && m >= 0 && n >= 0 && lda >= std::max(m, 1) &&                 \
                        (m * n == 0 || (A && swapDests))))                                 \
       return r;                                                                            \
-    return elgb::to_el_error(elgb::getrf<T>(ctx, m, n, A, lda, swapDests, nb));            \
+    return elgb::to_el_error(elgb::getrf<T>(ctx, m, n, A, lda, swapDests, nb, -1));        \
   }                                                                                        \
   int ElGBSolveAfterLUPartialPiv_##S(ElGBContext ctx, int orientation, int n, const T* A,  \
                                      int lda, const int* swapDests, int nrhs, T* B,        \
@@ -672,6 +711,30 @@ long long ElGBLaunchCount(ElGBContext ctx) { return ctx ? ctx->launches : -1; }
 
 ELGB_LU(d, double)
 ELGB_LU(s, float)
+
+int ElGBLUPartialPivMixed_s(ElGBContext ctx, int m, int n, float* A, int lda, int* swapDests,
+                            int nb, int gemm_kind) {
+  if (int r = arg_ok(ctx && m >= 0 && n >= 0 && lda >= std::max(m, 1) &&
+                     gemm_kind >= -1 && gemm_kind <= 2 && (m * n == 0 || (A && swapDests))))
+    return r;
+  if (nb <= 0) nb = 512;
+  return elgb::to_el_error(elgb::getrf<float>(ctx, m, n, A, lda, swapDests, nb, gemm_kind));
+}
+
+int ElGBGemmSubTC(ElGBContext ctx, int gemm_kind, int m, int n, int k, const float* A, int lda,
+                  const float* B, int ldb, float* C, int ldc) {
+  if (int r = arg_ok(ctx && gemm_kind >= 0 && gemm_kind <= 2 && m >= 0 && n >= 0 && k >= 0 &&
+                     lda >= std::max(m, 1) && ldb >= std::max(k, 1) && ldc >= std::max(m, 1)))
+    return r;
+  cudaError_t e = ctx->begin_call();
+  if (e == cudaSuccess) e = ctx->ensure(elgb::tc_gemm_workspace_bytes(gemm_kind, m, n, k));
+  if (e != cudaSuccess) return elgb::kElRuntimeError;
+  int nl = 0;
+  e = elgb::launch_tc_gemm_sub(gemm_kind, m, n, k, A, lda, B, ldb, C, ldc, ctx->arena,
+                               ctx->status, ctx->stream, &nl);
+  ctx->launches += nl;
+  return elgb::to_el_error(e);
+}
 
 int ElGBResidual_d(ElGBContext ctx, int n, int nrhs, const double* A, int lda, const double* X,
                    int ldx, const double* B, int ldb, double* R, int ldr) {

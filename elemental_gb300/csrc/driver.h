@@ -39,7 +39,8 @@ int get_blocksize();
 void set_blocksize(int nb);
 
 template <typename T>
-cudaError_t getrf(Context* ctx, int m, int n, T* A, long lda, int* ipiv, int nb);
+cudaError_t getrf(Context* ctx, int m, int n, T* A, long lda, int* ipiv, int nb,
+                  int tc_kind = -1);
 template <typename T>
 cudaError_t getrs(Context* ctx, int orient, int n, const T* A, long lda, const int* ipiv,
                   int nrhs, T* B, long ldb, const int* perm);

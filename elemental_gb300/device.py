@@ -116,6 +116,27 @@ class Context:
                                                             _ptr(piv), nb), "LU")
         return piv
 
+    def lu_mixed(self, A, gemm_kind=2, piv=None, nb=0):
+        """El::LU on an FP32 matrix with tensor-core updates (gemm_kind:
+        -1 SIMT FP32, 0 BF16, 1 TF32, 2 TF32x3)."""
+        m, n = A.shape
+        assert A.dtype == torch.float32
+        if piv is None:
+            piv = torch.empty(min(m, n), dtype=torch.int32, device=A.device)
+        self._bind()
+        self._rc(self.lib.ElGBLUPartialPivMixed_s(self.h, m, n, _ptr(A), _ld(A), _ptr(piv), nb,
+                                                  gemm_kind), "LUMixed")
+        return piv
+
+    def gemm_sub_tc(self, A, B, C, gemm_kind=0):
+        """C -= A @ B on the tensor cores (FP32 column-major tensors)."""
+        m, k = A.shape
+        n = B.shape[1]
+        self._bind()
+        self._rc(self.lib.ElGBGemmSubTC(self.h, gemm_kind, m, n, k, _ptr(A), _ld(A), _ptr(B),
+                                        _ld(B), _ptr(C), _ld(C)), "GemmSubTC")
+        return C
+
     def lu_solve_after(self, A, piv, B, orientation=0):
         n = A.shape[0]
         self._bind()

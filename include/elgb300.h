@@ -57,6 +57,33 @@ int ElGBLUPartialPiv_d(ElGBContext ctx, int m, int n, double* A, int lda,
 int ElGBLUPartialPiv_s(ElGBContext ctx, int m, int n, float* A, int lda,
                        int* swapDests, int nb);
 
+/* Operand precision of the tensor-core products used by the low-precision
+ * factorization (accumulation is always FP32):
+ *   ELGB_GEMM_SIMT_FP32  FP32 FMA on the CUDA cores (no tensor cores)
+ *   ELGB_GEMM_BF16       tcgen05.mma kind::f16, BF16 operands
+ *   ELGB_GEMM_TF32       tcgen05.mma kind::tf32
+ *   ELGB_GEMM_TF32X3     kind::tf32 on hi + lo operand splits, three products
+ *                        (close to FP32 accuracy) */
+enum {
+  ELGB_GEMM_SIMT_FP32 = -1,
+  ELGB_GEMM_BF16 = 0,
+  ELGB_GEMM_TF32 = 1,
+  ELGB_GEMM_TF32X3 = 2
+};
+
+/* El::LU(A, P) on an FP32 matrix whose trailing updates, blocked-TRSM updates
+ * and panel-internal updates run on the tensor cores in `gemm_kind`
+ * precision; same output layout as ElGBLUPartialPiv_s.  nb <= 0 selects 512. */
+int ElGBLUPartialPivMixed_s(ElGBContext ctx, int m, int n, float* A, int lda,
+                            int* swapDests, int nb, int gemm_kind);
+
+/* C -= A B on the tensor cores (FP32 in and out, column-major, device):
+ * the Gemm(NORMAL, NORMAL, -1, A, B, 1, C) of reference
+ * src/blas_like/level3/Gemm.cpp:19-71 in `gemm_kind` operand precision. */
+int ElGBGemmSubTC(ElGBContext ctx, int gemm_kind, int m, int n, int k,
+                  const float* A, int lda, const float* B, int ldb, float* C,
+                  int ldc);
+
 /* lu::SolveAfter(orientation, A, P, B) (reference
  * src/lapack_like/factor/LU/SolveAfter.hpp:66-92): orientation 0 NORMAL,
  * 1 TRANSPOSE, 2 ADJOINT (= TRANSPOSE for real data).  B is n x nrhs. */
