@@ -283,7 +283,8 @@ tc_gemm_sub_kernel(const __grid_constant__ CUtensorMap tmA,
       cv[j] = (row_ok && col < n) ? crow[(long)col * ldc] : 0.f;
     }
     if (!ready) {
-      ready = mbar_wait(&accum_bar, 0, st, 12);
+      // warp-uniform decision: tcgen05.ld below is a whole-warp instruction
+      ready = __all_sync(0xffffffffu, mbar_wait(&accum_bar, 0, st, 12));
       tc_fence_after();
       if (!ready) break;
     }
