@@ -19,6 +19,18 @@ c_ll = ctypes.c_longlong
 P = ctypes.POINTER
 
 
+class RefineCtrl(ctypes.Structure):
+    """ElGBRefineCtrl (include/elgb300.h)."""
+    _fields_ = [("precision", c_int), ("method", c_int), ("tol", c_double),
+                ("max_iters", c_int), ("restart", c_int), ("fallback", c_int), ("nb", c_int)]
+
+
+class RefineInfo(ctypes.Structure):
+    """ElGBRefineInfo (include/elgb300.h)."""
+    _fields_ = [("iterations", c_int), ("converged", c_int), ("fell_back", c_int),
+                ("precision", c_int), ("backward_error", c_double)]
+
+
 def _sig(lib, name, res, *args):
     f = getattr(lib, name)
     f.restype = res
@@ -57,6 +69,8 @@ def load():
     _sig(lib, "ElGBLUPartialPivMixed_s", c_int, vp, c_int, c_int, vp, c_int, vp, c_int, c_int)
     _sig(lib, "ElGBGemmSubTC", c_int, vp, c_int, c_int, c_int, c_int, vp, c_int, vp, c_int, vp,
          c_int)
+    _sig(lib, "ElGBRefinedSolve_d", c_int, vp, c_int, vp, c_int, c_int, vp, c_int, vp, c_int,
+         P(RefineCtrl), P(RefineInfo))
     _sig(lib, "ElGBResidual_d", c_int, vp, c_int, c_int, vp, c_int, vp, c_int, vp, c_int, vp,
          c_int)
     _sig(lib, "ElGBBackwardError_d", c_int, vp, c_int, c_int, vp, c_int, vp, c_int, vp, c_int,

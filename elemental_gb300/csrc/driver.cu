@@ -25,6 +25,7 @@ int to_el_error(cudaError_t e) { return e == cudaSuccess ? kElSuccess : kElRunti
 
 Context::~Context() {
   if (arena) cudaFree(arena);
+  if (arena2) cudaFree(arena2);
   if (status) cudaFree(status);
   if (h_status) cudaFreeHost(h_status);
   if (own_stream) cudaStreamDestroy(own_stream);
@@ -45,6 +46,19 @@ cudaError_t Context::ensure(size_t bytes) {
     want = bytes;
   }
   arena_bytes = want;
+  return cudaSuccess;
+}
+
+cudaError_t Context::ensure2(size_t bytes) {
+  if (bytes <= arena2_bytes) return cudaSuccess;
+  cudaError_t e = cudaStreamSynchronize(stream);
+  if (e != cudaSuccess) return e;
+  if (arena2) cudaFree(arena2);
+  arena2 = nullptr;
+  arena2_bytes = 0;
+  e = cudaMalloc(&arena2, bytes);
+  if (e != cudaSuccess) return e;
+  arena2_bytes = bytes;
   return cudaSuccess;
 }
 
@@ -596,8 +610,6 @@ void set_blocksize(int nb) { g_blocksize = nb; }
 // C ABI (include/elgb300.h)
 // ===========================================================================
 using elgb::Context;
-
-struct ElGBContextImpl : public Context {};
 
 static int arg_ok(bool c) { return c ? 0 : elgb::kElArgError; }
 

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include "common.cuh"
+#include "../../include/elgb300.h"
 
 namespace elgb {
 
@@ -28,9 +29,12 @@ struct Context {
   DevStatus* status = nullptr;    // device status word of the last call
   DevStatus* h_status = nullptr;  // pinned host mirror
   long long launches = 0;         // kernels enqueued by this context
+  void* arena2 = nullptr;  // second arena for drivers that call the ones above
+  size_t arena2_bytes = 0;
 
   ~Context();
-  cudaError_t ensure(size_t bytes);  // grows the arena (synchronizes first)
+  cudaError_t ensure(size_t bytes);   // grows the arena (synchronizes first)
+  cudaError_t ensure2(size_t bytes);  // grows arena2 (synchronizes first)
   cudaError_t begin_call();          // selects the device, clears the status word
 };
 
@@ -60,5 +64,10 @@ cudaError_t residual(Context* ctx, int n, int q, const double* A, long lda, cons
 cudaError_t backward_error(Context* ctx, int n, int q, const double* A, long lda,
                            const double* X, long ldx, const double* B, long ldb,
                            double* berr);
+cudaError_t refined_solve(Context* ctx, int n, const double* A, long lda, int nrhs,
+                          const double* B, long ldb, double* X, long ldx,
+                          const ElGBRefineCtrl& c, ElGBRefineInfo* info);
 
 }  // namespace elgb
+
+struct ElGBContextImpl : public elgb::Context {};

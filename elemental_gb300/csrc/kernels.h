@@ -96,7 +96,8 @@ cudaError_t launch_potf2_block(T* A, long lda, int nb, bool upper,
                                int info_base, DevStatus* st,
                                cudaStream_t stream);
 
-// Residual R = B - A X in FP64 with a deterministic two-stage reduction.
+// Residual R = B - A X in FP64 with a deterministic two-stage reduction
+// (B == nullptr gives the product R = A X).
 // partial must hold nchunks * n * q doubles, nchunks = ceil(n / 4096).
 cudaError_t launch_residual_f64(int n, int q, const double* A, long lda,
                                 const double* X, long ldx, const double* B,

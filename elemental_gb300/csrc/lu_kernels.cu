@@ -871,7 +871,7 @@ __global__ void residual_finish_kernel(int n, int q, int nchunks,
   if (i >= n) return;
   double s = 0.0;
   for (int ch = 0; ch < nchunks; ++ch) s += partial[((long)ch * q + c) * n + i];
-  R[i + (long)c * ldr] = B[i + (long)c * ldb] - s;
+  R[i + (long)c * ldr] = B ? B[i + (long)c * ldb] - s : s;  // B == nullptr: R = A X
 }
 
 cudaError_t launch_residual_f64(int n, int q, const double* A, long lda, const double* X,

@@ -16,6 +16,11 @@ from . import _lib
 
 _DT = {torch.float64: "d", torch.float32: "s"}
 
+# ElGB precision / method codes (include/elgb300.h)
+PRECISIONS = {"fp64": 0, "fp32": 1, "tf32": 2, "bf16": 3}
+PRECISION_NAMES = {v: k for k, v in PRECISIONS.items()}
+METHODS = {"lu-ir": 0, "gmres-ir": 1}
+
 
 class ElGBError(RuntimeError):
     pass
@@ -136,6 +141,26 @@ class Context:
         self._rc(self.lib.ElGBGemmSubTC(self.h, gemm_kind, m, n, k, _ptr(A), _ld(A), _ptr(B),
                                         _ld(B), _ptr(C), _ld(C)), "GemmSubTC")
         return C
+
+    def refined_solve(self, A, B, X=None, precision="fp32", method="lu-ir", tol=0.0,
+                      max_iters=0, restart=0, fallback=True, nb=0):
+        """Mixed-precision solve A X = B (FP64 in/out): low-precision LU on the
+        tensor cores + LU-IR or GMRES-IR with an FP64 residual, FP64 LU as the
+        fallback.  Returns (X, info dict)."""
+        n, q = B.shape
+        if X is None:
+            X = colmajor(n, q, torch.float64, A.device)
+        ctrl = _lib.RefineCtrl(PRECISIONS[precision], METHODS[method], float(tol),
+                               int(max_iters), int(restart), 1 if fallback else 0, int(nb))
+        inf = _lib.RefineInfo()
+        self._bind()
+        self._rc(self.lib.ElGBRefinedSolve_d(self.h, n, _ptr(A), _ld(A), q, _ptr(B), _ld(B),
+                                             _ptr(X), _ld(X), ctypes.byref(ctrl),
+                                             ctypes.byref(inf)), "RefinedSolve")
+        return X, dict(iterations=inf.iterations, converged=bool(inf.converged),
+                       fell_back=bool(inf.fell_back),
+                       precision=PRECISION_NAMES[inf.precision],
+                       backward_error=inf.backward_error)
 
     def lu_solve_after(self, A, piv, B, orientation=0):
         n = A.shape[0]

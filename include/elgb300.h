@@ -84,6 +84,42 @@ int ElGBGemmSubTC(ElGBContext ctx, int gemm_kind, int m, int n, int k,
                   const float* A, int lda, const float* B, int ldb, float* C,
                   int ldc);
 
+/* Factorization precision of the mixed-precision solve. */
+enum {
+  ELGB_PREC_FP64 = 0, /* plain FP64 getrf + getrs (no refinement)           */
+  ELGB_PREC_FP32 = 1, /* FP32 storage, TF32x3 tensor-core products (~FP32)  */
+  ELGB_PREC_TF32 = 2, /* FP32 storage, TF32 tensor-core products            */
+  ELGB_PREC_BF16 = 3  /* FP32 storage, BF16 tensor-core products            */
+};
+
+typedef struct {
+  int precision;  /* ELGB_PREC_*                                            */
+  int method;     /* 0 LU-IR, 1 GMRES-IR                                    */
+  double tol;     /* target normwise backward error; <= 0: n * eps64         */
+  int max_iters;  /* refinement steps (LU-IR) / GMRES iterations; <= 0: 30   */
+  int restart;    /* GMRES restart length; <= 0: 20                          */
+  int fallback;   /* nonzero: FP64 LU when the low-precision factor is
+                     singular or refinement stalls                           */
+  int nb;         /* blocksize of the low-precision factorization; <= 0: 512 */
+} ElGBRefineCtrl;
+
+typedef struct {
+  int iterations;        /* refinement steps / GMRES iterations taken        */
+  int converged;         /* 1 if every column reached tol                   */
+  int fell_back;         /* 1 if the FP64 LU produced the answer             */
+  int precision;         /* precision of the factorization that answered     */
+  double backward_error; /* achieved max-over-columns normwise backward error */
+} ElGBRefineInfo;
+
+/* Mixed-precision solve A X = B (A n x n, B and X n x nrhs, FP64, device):
+ * low-precision LU on the tensor cores + LU-IR or GMRES-IR with an FP64
+ * residual (semantics of reference include/El/lapack_like/solve/Refined.hpp:44-119
+ * and FGMRES.hpp:37-315), FP64 LU as the fallback.  A and B are not modified.
+ * Synchronizes (the stopping test runs on the host). */
+int ElGBRefinedSolve_d(ElGBContext ctx, int n, const double* A, int lda,
+                       int nrhs, const double* B, int ldb, double* X, int ldx,
+                       const ElGBRefineCtrl* ctrl, ElGBRefineInfo* info);
+
 /* lu::SolveAfter(orientation, A, P, B) (reference
  * src/lapack_like/factor/LU/SolveAfter.hpp:66-92): orientation 0 NORMAL,
  * 1 TRANSPOSE, 2 ADJOINT (= TRANSPOSE for real data).  B is n x nrhs. */
