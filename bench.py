@@ -1,0 +1,397 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 dense factor-and-solve path.
+
+Headline workload (default): mixed-precision solve of A X = B, A n x n and B
+n x 16 iid N(0,1) in FP64 (n = 32768, the largest single-GPU size of the
+plain-FP64 configuration), by FP32 factors (TF32x3 tcgen05 trailing updates)
+and LU-IR with an FP64 residual, to a normwise backward error <= n eps64.
+One step = one full solve (factor + refine) of the system.  Beside it the
+plain FP64 GPU LU (getrf + getrs) is timed once on the same system, and the
+reference's CPU algorithm (the oracle restatement of El::LU +
+lu::SolveAfter over OpenBLAS, all host threads) on a bounded sample.
+
+  value  solves/s with A, B resident in HBM (CUDA events, max over ranks)
+  e2e    the same solve through the Elemental-style C ABI on pinned host
+         buffers (ElLinearSolveMixed_d): H2D of A and B, D2H of X per step
+
+`--impl reference` times the CPU reference arm alone.  Under torchrun each
+rank solves its own system (replicas; the factorization does not shard).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "solves/s & TFLOP/s-eq at FP64 backward err: mixed-prec IR vs plain FP64 LU"
+EPS64 = 2.220446049250313e-16
+
+
+def flops_per_solve(n, q):
+    return 2.0 / 3.0 * n ** 3 + 2.0 * n * n * q
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--n", type=int, default=32768)
+    p.add_argument("--nrhs", type=int, default=16)
+    p.add_argument("--precision", default="fp32", choices=["fp32", "tf32", "bf16", "fp64"])
+    p.add_argument("--method", default="lu-ir", choices=["lu-ir", "gmres-ir"])
+    p.add_argument("--nb", type=int, default=0)
+    p.add_argument("--fp64-compare", default="on", choices=["on", "off"])
+    p.add_argument("--e2e", default="on", choices=["on", "off"])
+    p.add_argument("--cpu-baseline", default="on", choices=["on", "off"])
+    p.add_argument("--cpu-n", type=int, default=8192)
+    p.add_argument("--seed", type=int, default=20261204 + 1)
+    return p.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.dev = device_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons, power = [], None, set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+                power.append(float(f[3]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm),
+                "power_w_max": max(power) if power else None}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return d, "measured"
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, \
+            "fallback"
+
+
+# ---------------------------------------------------------------------------
+# CPU reference arm: the oracle's restatement of El::LU + lu::SolveAfter
+# ---------------------------------------------------------------------------
+def cpu_sample(n_sample, q, seed, reps=1):
+    import numpy as np
+
+    from oracle import oracle as O
+
+    threads = os.cpu_count() or 1
+    O.lib(threads)
+    rng = np.random.default_rng(seed)
+    A = np.asfortranarray(rng.standard_normal((n_sample, n_sample)))
+    B = np.asfortranarray(rng.standard_normal((n_sample, q)))
+    best = None
+    berr = None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        LU, piv = O.lu(A, nb=128)
+        X = O.lu_solve_after(LU, piv, B)
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+        berr = O.backward_error(A, X, B)
+    return best, threads, berr
+
+
+def reference_arm(args, rank):
+    if rank != 0:
+        return 0
+    n, q = args.n, args.nrhs
+    ns = min(args.cpu_n, n)
+    scale = flops_per_solve(n, q) / flops_per_solve(ns, q)
+    for _ in range(max(args.warmup, 0)):
+        cpu_sample(ns, q, args.seed)
+    times = []
+    for _ in range(args.steps):
+        t, threads, berr = cpu_sample(ns, q, args.seed)
+        times.append(t)
+    tot = sum(times)
+    value = args.steps / (tot * scale)
+    sample = (f"El::LU + lu::SolveAfter restatement (oracle/el_oracle.c over OpenBLAS), "
+              f"N(0,1) n={ns}, {q} RHS, FP64, nb=128; each step one sample solve, value "
+              f"scaled to n={n} by the flop count (x{scale:.1f})")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic: seeded iid N(0,1)",
+        "config": {"workload": f"FP64 LU + solve, n={n}, {q} RHS, N(0,1) (CPU sample n={ns})",
+                   "n": n, "nrhs": q, "parallelism": "cpu"},
+        "tflops_eq": value * flops_per_solve(n, q) / 1e12,
+        "backward_error_sample": berr,
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def gpu_arm(args, rank, world, local_rank):
+    import numpy as np
+    import torch
+
+    import elemental_gb300 as El
+    from elemental_gb300 import device as D
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    n, q = args.n, args.nrhs
+    ctx = D.context(local_rank)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(args.seed + 7919 * rank)
+    A = D.colmajor(n, n)
+    A.copy_(torch.randn(n, n, generator=g, device="cuda", dtype=torch.float64).t())
+    B = D.colmajor(n, q)
+    B.copy_(torch.randn(q, n, generator=g, device="cuda", dtype=torch.float64).t())
+    X = D.colmajor(n, q)
+    torch.cuda.synchronize()
+
+    def solve():
+        return ctx.refined_solve(A, B, X, precision=args.precision, method=args.method,
+                                 nb=args.nb)
+
+    info = None
+    for _ in range(max(args.warmup, 0)):
+        _, info = solve()
+    barrier()
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    l0 = ctx.launches()
+    ctx.profile_start()
+    stream = torch.cuda.current_stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    infos = []
+    e0.record(stream)
+    for _ in range(args.steps):
+        _, info = solve()
+        infos.append(info)
+    e1.record(stream)
+    e1.synchronize()
+    barrier()
+    prof = ctx.profile_stop()
+    launches = ctx.launches() - l0
+    clk = clocks.stop()
+    t = e0.elapsed_time(e1) / 1e3
+    tmax = t
+    if dist is not None:
+        tt = torch.tensor([t], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        tmax = float(tt.item())
+    value = args.steps * world / tmax
+    berr = max(i["backward_error"] for i in infos)
+    iters = max(i["iterations"] for i in infos)
+
+    # plain FP64 GPU LU on the same system (one step; warm-up on a small case)
+    fp64 = None
+    if args.fp64_compare == "on" and rank == 0:
+        As = D.colmajor(512, 512)
+        As.copy_(torch.randn(512, 512, device="cuda", dtype=torch.float64))
+        Bs = D.colmajor(512, q)
+        Bs.copy_(torch.randn(512, q, device="cuda", dtype=torch.float64))
+        ctx.refined_solve(As, Bs, precision="fp64")
+        torch.cuda.synchronize()
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        _, finfo = ctx.refined_solve(A, B, X, precision="fp64")
+        f1.record(stream)
+        f1.synchronize()
+        tf = f0.elapsed_time(f1) / 1e3
+        fp64 = {"ms": tf * 1e3, "solves_per_s": 1.0 / tf,
+                "tflops_eq": flops_per_solve(n, q) / tf / 1e12,
+                "backward_error": finfo["backward_error"],
+                "fp64_fma_peak_tflops_probe": ctx.fp64_peak_tflops(),
+                "speedup_mixed_vs_fp64": tf / (tmax / args.steps)}
+
+    # end to end through the Elemental-style C ABI on pinned host buffers
+    e2e = None
+    if args.e2e == "on":
+        Ah = torch.empty((n, n), dtype=torch.float64, pin_memory=True)
+        Ah.copy_(A.t())  # row-major (n, n) of A^T = column-major A
+        B0 = torch.empty((q, n), dtype=torch.float64, pin_memory=True)
+        B0.copy_(B.t())
+        Bh = torch.empty((q, n), dtype=torch.float64, pin_memory=True)
+        Am = El.Matrix(Ah.numpy().T)
+        assert Am.array.ctypes.data == Ah.data_ptr()
+        Bh.copy_(B0)
+        Bm = El.Matrix(Bh.numpy().T)
+        assert Bm.array.ctypes.data == Bh.data_ptr()
+        El.LinearSolveMixed(Am, Bm, precision=args.precision, method=args.method, nb=args.nb)
+        tot = 0.0
+        for _ in range(args.steps):
+            Bh.copy_(B0)
+            barrier()
+            t0 = time.perf_counter()
+            El.LinearSolveMixed(Am, Bm, precision=args.precision, method=args.method,
+                                nb=args.nb)
+            tot += time.perf_counter() - t0
+        te = tot
+        if dist is not None:
+            tt = torch.tensor([te], device="cuda")
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            te = float(tt.item())
+        Xh = torch.from_numpy(Bm.array.T.copy())
+        err = float((Xh.cuda() - X.t()).abs().max())
+        e2e = {"value": args.steps * world / te, "unit": "solves/s",
+               "h2d_bytes_per_step": 8 * n * n + 8 * n * q, "d2h_bytes_per_step": 8 * n * q,
+               "api": "ElLinearSolveMixed_d (El::Matrix handles on pinned host memory)",
+               "max_abs_diff_vs_device_run": err}
+        del Ah, B0, Bh, Am, Bm
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return 0
+
+    peaks, peak_kind = measured_peaks()
+    tf_achieved = prof["flops"] / (prof["ms"] * 1e-3) / 1e12 if prof["ms"] > 0 else None
+    peak = peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops"))
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "tc_gemm_traffic.json")
+    if os.path.exists(tpath) and prof["launches"]:
+        with open(tpath) as f:
+            tj = json.load(f)
+        # DRAM bytes per algorithmic byte from one ncu capture, applied to the
+        # average launch of this run
+        traffic = tj["dram_bytes_per_algorithmic_byte"] * prof["bytes"] / prof["launches"]
+    roofline = {
+        "kernel": "tc_gemm_sub_kernel (tcgen05 trailing update, "
+                  f"{ {'fp32': 'TF32x3', 'tf32': 'TF32', 'bf16': 'BF16', 'fp64': 'n/a'}[args.precision] } operands)",
+        "bound": "tensor", "achieved": tf_achieved, "peak": peak, "unit": "TFLOP/s",
+        "frac": (tf_achieved / peak) if tf_achieved else None,
+        "peak_source": f"{peak_kind} bf16 dense (sustained): the kernel is timed inside a long step",
+        "traffic": traffic,
+        "launches": prof["launches"], "kernel_ms_total": prof["ms"],
+        "algorithmic_flops_per_launch": prof["flops"] / max(prof["launches"], 1),
+        "algorithmic_bytes_per_launch": prof["bytes"] / max(prof["launches"], 1),
+        "achieved_gbs": prof["bytes"] / (prof["ms"] * 1e-3) / 1e9 if prof["ms"] > 0 else None,
+        "share_of_step_time": prof["ms"] * 1e-3 / tmax if tmax > 0 else None,
+    }
+    cpu = None
+    if args.cpu_baseline == "on":
+        ns = min(args.cpu_n, n)
+        tcpu, threads, cberr = cpu_sample(ns, q, args.seed)
+        scale = flops_per_solve(n, q) / flops_per_solve(ns, q)
+        cpu = {"value": 1.0 / (tcpu * scale), "unit": "solves/s", "cores": threads,
+               "kind": "port",
+               "sample": f"El::LU + lu::SolveAfter restatement over OpenBLAS, N(0,1) n={ns}, "
+                         f"{q} RHS, {threads} threads: {tcpu:.3f} s, scaled to n={n} by flops "
+                         f"(x{scale:.1f})",
+               "backward_error_sample": cberr}
+    prec_desc = {"fp32": "FP32 factors via TF32x3 tcgen05 updates",
+                 "tf32": "FP32 storage, TF32 tcgen05 updates",
+                 "bf16": "FP32 storage, BF16 tcgen05 updates",
+                 "fp64": "plain FP64 getrf + getrs"}[args.precision]
+    line = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tmax / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": {"fp32": "f64+tf32x3", "tf32": "f64+tf32", "bf16": "f64+bf16",
+                  "fp64": "f64"}[args.precision],
+        "data": "synthetic: seeded iid N(0,1) FP64 (device Philox generator)",
+        "config": {"workload": f"mixed-precision {args.method.upper()} ({prec_desc}, FP64 "
+                               f"residual) of A X = B, n={n}, {q} RHS, A,B iid N(0,1), to "
+                               f"backward error <= n*eps64",
+                   "n": n, "nrhs": q, "precision": args.precision, "method": args.method,
+                   "nb": args.nb or 512, "l2": "inputs larger than L2 (A is 8 GiB)",
+                   "parallelism": f"replicas x{world}"},
+        "tflops_eq": value * flops_per_solve(n, q) / 1e12,
+        "backward_error": berr, "backward_error_bound": n * EPS64, "iterations": iters,
+        "fell_back": any(i["fell_back"] for i in infos),
+        "fp64_gpu": fp64,
+        "e2e": e2e,
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "gpu_launches": launches,
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return reference_arm(args, rank)
+    return gpu_arm(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

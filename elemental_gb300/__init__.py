@@ -184,3 +184,19 @@ def LinearSolve(A: Matrix, B: Matrix):
 def HPDSolve(A: Matrix, B: Matrix, uplo=LOWER, orient=NORMAL):
     _check(getattr(A.lib, f"ElHPDSolve_{A.tag}")(uplo, orient, A.obj, B.obj), "HPDSolve",
            SingularMatrixException)
+
+
+def LinearSolveMixed(A: Matrix, B: Matrix, precision="fp32", method="lu-ir", tol=0.0,
+                     max_iters=0, restart=0, fallback=True, nb=0):
+    """Added form: El.LinearSolve on host matrices through the mixed-precision
+    path (ElLinearSolveMixed_d); returns the refinement info as a dict."""
+    from .device import METHODS, PRECISION_NAMES, PRECISIONS
+
+    ctrl = _lib.RefineCtrl(PRECISIONS[precision], METHODS[method], float(tol), int(max_iters),
+                           int(restart), 1 if fallback else 0, int(nb))
+    inf = _lib.RefineInfo()
+    _check(A.lib.ElLinearSolveMixed_d(A.obj, B.obj, ctypes.byref(ctrl), ctypes.byref(inf)),
+           "LinearSolveMixed", SingularMatrixException)
+    return dict(iterations=inf.iterations, converged=bool(inf.converged),
+                fell_back=bool(inf.fell_back), precision=PRECISION_NAMES[inf.precision],
+                backward_error=inf.backward_error)

@@ -56,6 +56,8 @@ def load():
     _sig(lib, "ElGBBlocksize", c_int)
     _sig(lib, "ElGBSetBlocksize", c_int, c_int)
     _sig(lib, "ElGBLaunchCount", c_ll, vp)
+    _sig(lib, "ElGBProfileStart", c_int, vp)
+    _sig(lib, "ElGBProfileStop", c_int, vp, P(c_ll), P(c_double), P(c_double), P(c_double))
     for s in ("d", "s"):
         _sig(lib, f"ElGBLUPartialPiv_{s}", c_int, vp, c_int, c_int, vp, c_int, vp, c_int)
         _sig(lib, f"ElGBSolveAfterLUPartialPiv_{s}", c_int, vp, c_int, c_int, vp, c_int, vp,
@@ -105,6 +107,7 @@ def load():
         _sig(lib, f"ElSolveAfterCholesky_{s}", c_int, c_int, c_int, vp, vp)
         _sig(lib, f"ElLinearSolve_{s}", c_int, vp, vp)
         _sig(lib, f"ElHPDSolve_{s}", c_int, c_int, c_int, vp, vp)
+    _sig(lib, "ElLinearSolveMixed_d", c_int, vp, vp, P(RefineCtrl), P(RefineInfo))
     _lib = lib
     return lib
 

@@ -23,7 +23,17 @@ static int g_blocksize = 128;  // El's default blocksize (src/core/environment.c
 
 int to_el_error(cudaError_t e) { return e == cudaSuccess ? kElSuccess : kElRuntimeError; }
 
+cudaEvent_t Context::next_event() {
+  if (ev_used == ev_pool.size()) {
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+    ev_pool.push_back(e);
+  }
+  return ev_pool[ev_used++];
+}
+
 Context::~Context() {
+  for (cudaEvent_t e : ev_pool) cudaEventDestroy(e);
   if (arena) cudaFree(arena);
   if (arena2) cudaFree(arena2);
   if (status) cudaFree(status);
@@ -131,9 +141,20 @@ static cudaError_t gemm_sub(Context* ctx, const GemmCfg& g, int m, int n, int k,
                             long lda, const float* B, long ldb, float* C, long ldc) {
   if (g.tc_kind >= 0 && m >= 64 && n >= 64 && k >= 16) {
     int nl = 0;
+    cudaEvent_t a = nullptr, b = nullptr;
+    if (ctx->prof_on) {
+      a = ctx->next_event();
+      b = ctx->next_event();
+    }
     cudaError_t e = launch_tc_gemm_sub(g.tc_kind, m, n, k, A, lda, B, ldb, C, ldc, g.ws,
-                                       ctx->status, ctx->stream, &nl);
+                                       ctx->status, ctx->stream, &nl, a, b);
     ctx->launches += nl;
+    if (a && b) {
+      const double esz = g.tc_kind == kTcBF16 ? 2.0 : 4.0;
+      const double copies = g.tc_kind == kTcTF32x3 ? 2.0 : 1.0;
+      ctx->prof.push_back({a, b, 2.0 * m * n * (double)k,
+                           8.0 * m * n + copies * esz * (double)k * (m + n)});
+    }
     return e;
   }
   ELGB_CHECK(launch_gemm_simt<float>(false, false, m, n, k, -1.f, A, lda, B, ldb, 1.f, C, ldc,
@@ -666,6 +687,34 @@ int ElGBStatus(ElGBContext ctx, int* info, int* err) {
   if (e != cudaSuccess) return elgb::kElRuntimeError;
   if (info) *info = ctx->h_status->info;
   if (err) *err = ctx->h_status->err;
+  return 0;
+}
+
+int ElGBProfileStart(ElGBContext ctx) {
+  if (!ctx) return elgb::kElArgError;
+  ctx->prof.clear();
+  ctx->ev_used = 0;
+  ctx->prof_on = true;
+  return 0;
+}
+
+int ElGBProfileStop(ElGBContext ctx, long long* launches, double* ms, double* flops,
+                    double* bytes) {
+  if (!ctx) return elgb::kElArgError;
+  ctx->prof_on = false;
+  if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return elgb::kElRuntimeError;
+  double t = 0, f = 0, b = 0;
+  for (auto& r : ctx->prof) {
+    float x = 0;
+    if (cudaEventElapsedTime(&x, r.a, r.b) != cudaSuccess) return elgb::kElRuntimeError;
+    t += x;
+    f += r.flops;
+    b += r.bytes;
+  }
+  if (launches) *launches = (long long)ctx->prof.size();
+  if (ms) *ms = t;
+  if (flops) *flops = f;
+  if (bytes) *bytes = b;
   return 0;
 }
 

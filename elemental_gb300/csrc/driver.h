@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include "common.cuh"
 #include "../../include/elgb300.h"
 
@@ -31,6 +33,19 @@ struct Context {
   long long launches = 0;         // kernels enqueued by this context
   void* arena2 = nullptr;  // second arena for drivers that call the ones above
   size_t arena2_bytes = 0;
+
+  // Live per-kernel timing (ElGBProfile*): CUDA event pairs recorded on the
+  // launching stream around the tensor-core GEMM kernel, with its algorithmic
+  // flops and bytes.
+  struct ProfRec {
+    cudaEvent_t a, b;
+    double flops, bytes;
+  };
+  bool prof_on = false;
+  std::vector<ProfRec> prof;        // records of the current window
+  std::vector<cudaEvent_t> ev_pool;  // reusable events
+  size_t ev_used = 0;
+  cudaEvent_t next_event();
 
   ~Context();
   cudaError_t ensure(size_t bytes);   // grows the arena (synchronizes first)

@@ -487,6 +487,27 @@ void HPDSolve(UpperOrLower uplo, Orientation orientation, const Matrix<F>& A, Ma
   Download(B, dB);
 }
 
+// Mixed-precision El::LinearSolve on host matrices (added form).
+void LinearSolveMixed(const Matrix<double>& A, Matrix<double>& B, const ElGBRefineCtrl* ctrl,
+                      ElGBRefineInfo* info) {
+  if (A.Height() != A.Width()) throw std::logic_error("A must be square");
+  if (A.Height() != B.Height()) throw std::logic_error("A and B must be the same height");
+  std::lock_guard<std::mutex> lk(St().mu);
+  const Int n = A.Height(), q = B.Width();
+  if (n == 0 || q == 0) return;
+  ElGBContext ctx = Ctx();
+  const size_t sa = Al(sizeof(double) * (size_t)n * n), sb = Al(sizeof(double) * (size_t)n * q);
+  char* base = Dev(sa + 2 * sb);
+  double* dA = reinterpret_cast<double*>(base);
+  double* dB = reinterpret_cast<double*>(base + sa);
+  double* dX = reinterpret_cast<double*>(base + sa + sb);
+  Upload(ctx, dA, A);
+  Upload(ctx, dB, B);
+  CheckRc(ElGBRefinedSolve_d(ctx, n, dA, n, q, dB, n, dX, n, ctrl, info));
+  Check(cudaDeviceSynchronize(), "mixed solve");
+  Download(B, dX);
+}
+
 #define EL_GB_PROTO(F)                                                                  \
   template void LU<F>(Matrix<F>&, Permutation&);                                        \
   template void lu::SolveAfter<F>(Orientation, const Matrix<F>&, const Permutation&,    \
@@ -663,6 +684,10 @@ ElError ElLinearSolve_s(ElConstMatrix_s A, ElMatrix_s B) {
 }
 ElError ElLinearSolve_d(ElConstMatrix_d A, ElMatrix_d B) {
   EL_GB_TRY(El::LinearSolve(*CM<double>(A), *M<double>(B)))
+}
+ElError ElLinearSolveMixed_d(ElConstMatrix_d A, ElMatrix_d B, const ElGBRefineCtrl* ctrl,
+                             ElGBRefineInfo* info) {
+  EL_GB_TRY(El::LinearSolveMixed(*CM<double>(A), *M<double>(B), ctrl, info))
 }
 ElError ElHPDSolve_s(ElUpperOrLower u, ElOrientation o, ElConstMatrix_s A, ElMatrix_s B) {
   EL_GB_TRY(El::HPDSolve(Ul(u), Or(o), *CM<float>(A), *M<float>(B)))

@@ -399,7 +399,8 @@ size_t tc_gemm_workspace_bytes(int kind, int m, int n, int K) {
 
 cudaError_t launch_tc_gemm_sub(int kind, int m, int n, int K, const float* A, long lda,
                                const float* B, long ldb, float* C, long ldc, void* ws,
-                               DevStatus* st, cudaStream_t stream, int* nlaunch) {
+                               DevStatus* st, cudaStream_t stream, int* nlaunch,
+                               cudaEvent_t ev0, cudaEvent_t ev1) {
   if (nlaunch) *nlaunch = 0;
   if (m <= 0 || n <= 0 || K <= 0) return cudaSuccess;
   const bool split = kind == kTcTF32x3;
@@ -439,6 +440,7 @@ cudaError_t launch_tc_gemm_sub(int kind, int m, int n, int K, const float* A, lo
   dim3 grid((m + kBM - 1) / kBM, (n + kBN - 1) / kBN);
   const int num_kb = Kp / kbe;
   const int passes = split ? 3 : 1;
+  if (ev0) cudaEventRecord(ev0, stream);
   if (kind == kTcBF16) {
     auto kern = tc_gemm_sub_kernel<kTcBF16>;
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -452,6 +454,7 @@ cudaError_t launch_tc_gemm_sub(int kind, int m, int n, int K, const float* A, lo
     kern<<<grid, kGemmThreads, smem, stream>>>(tmA, tmB, tmAlo, tmBlo, C, ldc, m, n, num_kb,
                                                passes, st);
   }
+  if (ev1) cudaEventRecord(ev1, stream);
   if (nlaunch) *nlaunch = 3;
   return cudaGetLastError();
 }

@@ -20,8 +20,11 @@ size_t tc_gemm_workspace_bytes(int kind, int m, int n, int K);
 // C[m x n] -= A[m x K] * B[K x n]; A, B, C FP32 column-major.  Packs A and B
 // into `ws` (tc_gemm_workspace_bytes) in the operand precision, then runs the
 // tcgen05 kernel.  *nlaunch receives the number of kernels enqueued.
+// If ev0/ev1 are given they are recorded immediately before and after the
+// tensor-core kernel itself (not the packing), for live per-kernel timing.
 cudaError_t launch_tc_gemm_sub(int kind, int m, int n, int K, const float* A, long lda,
                                const float* B, long ldb, float* C, long ldc, void* ws,
-                               DevStatus* st, cudaStream_t stream, int* nlaunch);
+                               DevStatus* st, cudaStream_t stream, int* nlaunch,
+                               cudaEvent_t ev0 = nullptr, cudaEvent_t ev1 = nullptr);
 
 }  // namespace elgb

@@ -109,6 +109,17 @@ class Context:
     def launches(self):
         return int(self.lib.ElGBLaunchCount(self.h))
 
+    def profile_start(self):
+        self._rc(self.lib.ElGBProfileStart(self.h), "ProfileStart")
+
+    def profile_stop(self):
+        """Summed event timing of the tensor-core GEMM launches since
+        profile_start: dict(launches, ms, flops, bytes)."""
+        n, ms, fl, by = ctypes.c_longlong(), ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        self._rc(self.lib.ElGBProfileStop(self.h, ctypes.byref(n), ctypes.byref(ms),
+                                          ctypes.byref(fl), ctypes.byref(by)), "ProfileStop")
+        return dict(launches=n.value, ms=ms.value, flops=fl.value, bytes=by.value)
+
     # -- the path -----------------------------------------------------------
     def lu(self, A, piv=None, nb=0):
         """El::LU(A, P) in place; returns the int32 swap destinations."""

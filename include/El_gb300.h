@@ -14,6 +14,8 @@
 
 #include <stdbool.h>
 
+#include "elgb300.h"
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -123,6 +125,14 @@ ElError ElHPDSolve_s(ElUpperOrLower uplo, ElOrientation orientation,
                      ElConstMatrix_s A, ElMatrix_s B);
 ElError ElHPDSolve_d(ElUpperOrLower uplo, ElOrientation orientation,
                      ElConstMatrix_d A, ElMatrix_d B);
+
+/* Added form, no counterpart in the reference's C interface: El::LinearSolve
+ * on host matrices through the mixed-precision path of this library
+ * (low-precision tensor-core LU + LU-IR / GMRES-IR with an FP64 residual,
+ * FP64 LU fallback; see ElGBRefinedSolve_d).  A is left untouched, B is
+ * overwritten by X; ctrl may be NULL (FP32 factors, LU-IR, fallback on). */
+ElError ElLinearSolveMixed_d(ElConstMatrix_d A, ElMatrix_d B,
+                             const ElGBRefineCtrl* ctrl, ElGBRefineInfo* info);
 
 #ifdef __cplusplus
 }

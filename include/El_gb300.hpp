@@ -144,4 +144,16 @@ void HPDSolve(UpperOrLower uplo, Orientation orientation, const Matrix<F>& A, Ma
 
 }  // namespace El
 
+#include "elgb300.h"
+
+namespace El {
+
+// Added form (no counterpart in the reference): LinearSolve through the
+// mixed-precision path (tensor-core low-precision LU + LU-IR / GMRES-IR with
+// an FP64 residual, FP64 LU fallback).  ctrl may be null.
+void LinearSolveMixed(const Matrix<double>& A, Matrix<double>& B,
+                      const ElGBRefineCtrl* ctrl = nullptr, ElGBRefineInfo* info = nullptr);
+
+}  // namespace El
+
 #endif  // EL_GB300_HPP

@@ -47,6 +47,14 @@ int ElGBBlocksize(void);
 int ElGBSetBlocksize(int nb);
 /* Number of kernel launches this context has issued so far. */
 long long ElGBLaunchCount(ElGBContext ctx);
+/* Live timing of the dominant kernel (the tensor-core trailing-update GEMM):
+ * between Start and Stop every launch of it is bracketed by CUDA events on
+ * its stream; Stop synchronizes and returns the number of launches, their
+ * summed device time (ms) and their algorithmic flops (2 m n k) and bytes
+ * (C read + write, packed operands read). */
+int ElGBProfileStart(ElGBContext ctx);
+int ElGBProfileStop(ElGBContext ctx, long long* launches, double* ms,
+                    double* flops, double* bytes);
 
 /* El::LU(A, P) with partial pivoting (reference
  * src/lapack_like/factor/LU.cpp:104-138): A (m x n) is overwritten by the
