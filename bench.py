@@ -339,6 +339,8 @@ def gpu_arm(args, rank, world, local_rank):
         "achieved_gbs": prof["bytes"] / (prof["ms"] * 1e-3) / 1e9 if prof["ms"] > 0 else None,
         "share_of_step_time": prof["ms"] * 1e-3 / tmax if tmax > 0 else None,
     }
+    breakdown = {k: {"launches": v["launches"], "ms_per_step": v["ms"] / args.steps}
+                 for k, v in prof["by_kernel"].items()}
     cpu = None
     if args.cpu_baseline == "on":
         ns = min(args.cpu_n, n)
@@ -375,6 +377,7 @@ def gpu_arm(args, rank, world, local_rank):
         "roofline": roofline,
         "cpu_baseline": cpu,
         "gpu_launches": launches,
+        "kernel_time_breakdown": breakdown,
         "clocks": clk,
     }
     print(json.dumps(line), flush=True)

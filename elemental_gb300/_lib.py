@@ -58,6 +58,8 @@ def load():
     _sig(lib, "ElGBLaunchCount", c_ll, vp)
     _sig(lib, "ElGBProfileStart", c_int, vp)
     _sig(lib, "ElGBProfileStop", c_int, vp, P(c_ll), P(c_double), P(c_double), P(c_double))
+    _sig(lib, "ElGBProfileTag", c_int, vp, c_int, P(c_ll), P(c_double), P(c_double),
+         P(c_double))
     for s in ("d", "s"):
         _sig(lib, f"ElGBLUPartialPiv_{s}", c_int, vp, c_int, c_int, vp, c_int, vp, c_int)
         _sig(lib, f"ElGBSolveAfterLUPartialPiv_{s}", c_int, vp, c_int, c_int, vp, c_int, vp,

@@ -32,8 +32,31 @@ cudaEvent_t Context::next_event() {
   return ev_pool[ev_used++];
 }
 
+int Context::prof_begin(cudaStream_t st) {
+  if (!prof_on) return -1;
+  cudaEvent_t a = next_event();
+  if (!a) return -1;
+  cudaEventRecord(a, st);
+  prof.push_back({a, nullptr, 0, 0, -1});
+  return (int)prof.size() - 1;
+}
+
+void Context::prof_end(int idx, cudaStream_t st, int tag, double flops, double bytes) {
+  if (idx < 0 || !prof_on) return;
+  cudaEvent_t b = next_event();
+  if (!b) return;
+  cudaEventRecord(b, st);
+  prof[idx].b = b;
+  prof[idx].tag = tag;
+  prof[idx].flops = flops;
+  prof[idx].bytes = bytes;
+}
+
 Context::~Context() {
   for (cudaEvent_t e : ev_pool) cudaEventDestroy(e);
+  if (ev_fork) cudaEventDestroy(ev_fork);
+  if (ev_join) cudaEventDestroy(ev_join);
+  if (side_stream) cudaStreamDestroy(side_stream);
   if (arena) cudaFree(arena);
   if (arena2) cudaFree(arena2);
   if (status) cudaFree(status);
@@ -130,15 +153,34 @@ struct GemmCfg {
   void* ws = nullptr;
 };
 
-static cudaError_t gemm_sub(Context* ctx, const GemmCfg&, int m, int n, int k, const double* A,
+// One stream of the factorization with the scratch only it touches, so two
+// lanes (the trailing update and the look-ahead panel) can run concurrently.
+struct LuLane {
+  cudaStream_t st = nullptr;
+  int* pairs = nullptr;  // 4 * cap ints
+  int* pair_count = nullptr;
+  GemmCfg gemm;
+};
+
+#define LANE_CHECK(expr, nk)                   \
+  do {                                          \
+    cudaError_t e_ = (expr);                    \
+    if (e_ != cudaSuccess) return e_;           \
+    ctx->launches += (nk);                      \
+  } while (0)
+
+static cudaError_t gemm_sub(Context* ctx, const LuLane& L, int m, int n, int k, const double* A,
                             long lda, const double* B, long ldb, double* C, long ldc) {
-  ELGB_CHECK(launch_gemm_simt<double>(false, false, m, n, k, -1.0, A, lda, B, ldb, 1.0, C, ldc,
-                                      0, ctx->stream), 1);
+  const int pi = ctx->prof_begin(L.st);
+  LANE_CHECK(launch_gemm_simt<double>(false, false, m, n, k, -1.0, A, lda, B, ldb, 1.0, C, ldc,
+                                      0, L.st), 1);
+  ctx->prof_end(pi, L.st, ELGB_PROF_GEMM_SIMT, 2.0 * m * n * (double)k, 24.0 * m * n);
   return cudaSuccess;
 }
 
-static cudaError_t gemm_sub(Context* ctx, const GemmCfg& g, int m, int n, int k, const float* A,
+static cudaError_t gemm_sub(Context* ctx, const LuLane& L, int m, int n, int k, const float* A,
                             long lda, const float* B, long ldb, float* C, long ldc) {
+  const GemmCfg& g = L.gemm;
   if (g.tc_kind >= 0 && m >= 64 && n >= 64 && k >= 16) {
     int nl = 0;
     cudaEvent_t a = nullptr, b = nullptr;
@@ -147,33 +189,33 @@ static cudaError_t gemm_sub(Context* ctx, const GemmCfg& g, int m, int n, int k,
       b = ctx->next_event();
     }
     cudaError_t e = launch_tc_gemm_sub(g.tc_kind, m, n, k, A, lda, B, ldb, C, ldc, g.ws,
-                                       ctx->status, ctx->stream, &nl, a, b);
+                                       ctx->status, L.st, &nl, a, b);
     ctx->launches += nl;
     if (a && b) {
       const double esz = g.tc_kind == kTcBF16 ? 2.0 : 4.0;
       const double copies = g.tc_kind == kTcTF32x3 ? 2.0 : 1.0;
       ctx->prof.push_back({a, b, 2.0 * m * n * (double)k,
-                           8.0 * m * n + copies * esz * (double)k * (m + n)});
+                           8.0 * m * n + copies * esz * (double)k * (m + n), ELGB_PROF_TC_GEMM});
     }
     return e;
   }
-  ELGB_CHECK(launch_gemm_simt<float>(false, false, m, n, k, -1.f, A, lda, B, ldb, 1.f, C, ldc,
-                                     0, ctx->stream), 1);
+  const int pi = ctx->prof_begin(L.st);
+  LANE_CHECK(launch_gemm_simt<float>(false, false, m, n, k, -1.f, A, lda, B, ldb, 1.f, C, ldc,
+                                     0, L.st), 1);
+  ctx->prof_end(pi, L.st, ELGB_PROF_GEMM_SIMT, 2.0 * m * n * (double)k, 12.0 * m * n);
   return cudaSuccess;
 }
 
 template <typename T>
 struct LuState {
   Context* ctx;
-  GemmCfg gemm;
   T* A;
   long lda;
   int m, n;
   int* ipiv;           // absolute swap destinations, device
-  PanelScratch<T> ps;
-  int* pairs;          // 4 * pairs_cap ints
-  int* pair_count;
-  int pairs_cap;
+  PanelScratch<T> ps;  // used by whichever lane factors panels
+  int panel_ctas;      // CTAs of a panel launch (fewer when it overlaps the update)
+  LuLane main, side;   // side.st == nullptr: no look-ahead
   T* Bc;               // companion block receiving the same row operations
   long ldbc;           // (RowEchelon's B, src/lapack_like/solve/Linear.cpp:62-71)
   int nbc;
@@ -182,15 +224,19 @@ struct LuState {
 // Blocked TRSM, left / lower / unit: B := L11^{-1} B with L11 nb x nb (any
 // nb): 128-row diagonal solves plus GEMM updates of the rows below.
 template <typename T>
-static cudaError_t trsm_llnu(Context* ctx, const GemmCfg& g, const T* L, long ldl, int nb,
+static cudaError_t trsm_llnu(Context* ctx, const LuLane& L, const T* Lm, long ldl, int nb,
                              T* Bm, long ldb, int ncols) {
+  if (ncols <= 0) return cudaSuccess;
   for (int i0 = 0; i0 < nb; i0 += 128) {
     const int ib = std::min(128, nb - i0);
-    ELGB_CHECK(launch_trsm_block<T>(L + i0 + (long)i0 * ldl, ldl, Bm + i0, ldb, ib, ncols,
-                                    true, true, false, false, ctx->stream), 1);
+    const int pi = ctx->prof_begin(L.st);
+    LANE_CHECK(launch_trsm_block<T>(Lm + i0 + (long)i0 * ldl, ldl, Bm + i0, ldb, ib, ncols,
+                                    true, true, false, false, L.st), 1);
+    ctx->prof_end(pi, L.st, ELGB_PROF_TRSM, (double)ib * ib * ncols,
+                  2.0 * sizeof(T) * ib * (double)ncols);
     const int rest = nb - i0 - ib;
     if (rest > 0) {
-      cudaError_t e = gemm_sub(ctx, g, rest, ncols, ib, L + (i0 + ib) + (long)i0 * ldl, ldl,
+      cudaError_t e = gemm_sub(ctx, L, rest, ncols, ib, Lm + (i0 + ib) + (long)i0 * ldl, ldl,
                                Bm + i0, ldb, Bm + i0 + ib, ldb);
       if (e != cudaSuccess) return e;
     }
@@ -202,17 +248,19 @@ static cudaError_t trsm_llnu(Context* ctx, const GemmCfg& g, const T* L, long ld
 // the column ranges [a0, a1) and [b0, b1) of A and, if requested, to the
 // companion block.
 template <typename T>
-static cudaError_t apply_swaps(LuState<T>& s, int c0, int w, int a0, int a1, int b0, int b1,
-                               bool companion) {
+static cudaError_t apply_swaps(LuState<T>& s, const LuLane& L, int c0, int w, int a0, int a1,
+                               int b0, int b1, bool companion) {
   Context* ctx = s.ctx;
-  ELGB_CHECK(launch_build_swap_pairs(s.ipiv + c0, c0, w, s.pairs, s.pair_count, ctx->stream),
-             1);
+  const int pi = ctx->prof_begin(L.st);
+  LANE_CHECK(launch_build_swap_pairs(s.ipiv + c0, c0, w, L.pairs, L.pair_count, L.st), 1);
   if ((a1 > a0) || (b1 > b0))
-    ELGB_CHECK(launch_apply_swap_pairs<T>(s.A, s.lda, a0, a1, b0, b1, s.pairs, s.pair_count,
-                                          w, ctx->stream), 1);
+    LANE_CHECK(launch_apply_swap_pairs<T>(s.A, s.lda, a0, a1, b0, b1, L.pairs, L.pair_count, w,
+                                          L.st), 1);
+  ctx->prof_end(pi, L.st, ELGB_PROF_SWAP, 0.0,
+                4.0 * sizeof(T) * w * (double)(std::max(a1 - a0, 0) + std::max(b1 - b0, 0)));
   if (companion && s.Bc && s.nbc > 0)
-    ELGB_CHECK(launch_apply_swap_pairs<T>(s.Bc, s.ldbc, 0, s.nbc, 0, 0, s.pairs, s.pair_count,
-                                          w, ctx->stream), 1);
+    LANE_CHECK(launch_apply_swap_pairs<T>(s.Bc, s.ldbc, 0, s.nbc, 0, 0, L.pairs, L.pair_count,
+                                          w, L.st), 1);
   return cudaSuccess;
 }
 
@@ -221,67 +269,113 @@ static cudaError_t apply_swaps(LuState<T>& s, int c0, int w, int a0, int a1, int
 // the right half's swaps back onto the left half.  Leaves of <= 32 columns
 // go to the cooperative getf2 kernel.
 template <typename T>
-static cudaError_t panel_rec(LuState<T>& s, int c0, int w) {
+static cudaError_t panel_rec(LuState<T>& s, const LuLane& L, int c0, int w) {
   Context* ctx = s.ctx;
   if (w <= 32) {
-    ELGB_CHECK(launch_getf2_panel<T>(s.A + c0 + (long)c0 * s.lda, s.lda, s.m - c0, w,
-                                     s.ipiv + c0, c0, c0, s.ps, ctx->status, ctx->num_sms,
-                                     ctx->stream), 2);
+    const int pi = ctx->prof_begin(L.st);
+    LANE_CHECK(launch_getf2_panel<T>(s.A + c0 + (long)c0 * s.lda, s.lda, s.m - c0, w,
+                                     s.ipiv + c0, c0, c0, s.ps, ctx->status, s.panel_ctas,
+                                     L.st), 2);
+    ctx->prof_end(pi, L.st, ELGB_PROF_PANEL, (double)(s.m - c0) * w * w,
+                  2.0 * sizeof(T) * (s.m - c0) * (double)w);
     return cudaSuccess;
   }
   int w1 = (w / 2 + 31) / 32 * 32;
   if (w1 >= w) w1 = w - 32;
   const int w2 = w - w1;
-  cudaError_t e = panel_rec(s, c0, w1);
+  cudaError_t e = panel_rec(s, L, c0, w1);
   if (e != cudaSuccess) return e;
-  e = apply_swaps(s, c0, w1, c0 + w1, c0 + w, 0, 0, false);
+  e = apply_swaps(s, L, c0, w1, c0 + w1, c0 + w, 0, 0, false);
   if (e != cudaSuccess) return e;
   T* A11 = s.A + c0 + (long)c0 * s.lda;
   T* A12 = s.A + c0 + (long)(c0 + w1) * s.lda;
   T* A21 = s.A + (c0 + w1) + (long)c0 * s.lda;
   T* A22 = s.A + (c0 + w1) + (long)(c0 + w1) * s.lda;
-  e = trsm_llnu<T>(ctx, s.gemm, A11, s.lda, w1, A12, s.lda, w2);
+  e = trsm_llnu<T>(ctx, L, A11, s.lda, w1, A12, s.lda, w2);
   if (e != cudaSuccess) return e;
-  e = gemm_sub(ctx, s.gemm, s.m - c0 - w1, w2, w1, A21, s.lda, A12, s.lda, A22, s.lda);
+  e = gemm_sub(ctx, L, s.m - c0 - w1, w2, w1, A21, s.lda, A12, s.lda, A22, s.lda);
   if (e != cudaSuccess) return e;
-  e = panel_rec(s, c0 + w1, w2);
+  e = panel_rec(s, L, c0 + w1, w2);
   if (e != cudaSuccess) return e;
-  return apply_swaps(s, c0 + w1, w2, c0, c0 + w1, 0, 0, false);
+  return apply_swaps(s, L, c0 + w1, w2, c0, c0 + w1, 0, 0, false);
+}
+
+// Trailing update of block k (columns [c_begin, c_end) of the right part):
+// Trsm(LEFT, LOWER, NORMAL, UNIT) on A12 then Gemm(-1) on A22.
+template <typename T>
+static cudaError_t update_cols(LuState<T>& s, const LuLane& L, int k, int jb, int c_begin,
+                               int c_end) {
+  if (c_end <= c_begin) return cudaSuccess;
+  Context* ctx = s.ctx;
+  const int m2 = s.m - k - jb;
+  T* A11 = s.A + k + (long)k * s.lda;
+  cudaError_t e = trsm_llnu<T>(ctx, L, A11, s.lda, jb, s.A + k + (long)c_begin * s.lda, s.lda,
+                               c_end - c_begin);
+  if (e != cudaSuccess) return e;
+  if (m2 > 0)
+    e = gemm_sub(ctx, L, m2, c_end - c_begin, jb, s.A + (k + jb) + (long)k * s.lda, s.lda,
+                 s.A + k + (long)c_begin * s.lda, s.lda,
+                 s.A + (k + jb) + (long)c_begin * s.lda, s.lda);
+  return e;
+}
+
+template <typename T>
+static cudaError_t update_companion(LuState<T>& s, const LuLane& L, int k, int jb) {
+  if (!s.Bc || s.nbc <= 0) return cudaSuccess;
+  Context* ctx = s.ctx;
+  const int m2 = s.m - k - jb;
+  T* A11 = s.A + k + (long)k * s.lda;
+  cudaError_t e = trsm_llnu<T>(ctx, L, A11, s.lda, jb, s.Bc + k, s.ldbc, s.nbc);
+  if (e != cudaSuccess || m2 <= 0) return e;
+  return gemm_sub(ctx, L, m2, s.nbc, jb, s.A + (k + jb) + (long)k * s.lda, s.lda, s.Bc + k,
+                  s.ldbc, s.Bc + k + jb, s.ldbc);
 }
 
 // El::LU(A, P) (src/lapack_like/factor/LU.cpp:104-138), right-looking over
 // blocks of nb columns: panel, PB.PermuteRows on the left and right blocks,
 // Trsm(LEFT, LOWER, NORMAL, UNIT) on A12, Gemm(-1) on A22.
+//
+// With a side lane the schedule has a look-ahead of one panel: after block
+// k's swaps, the block column of panel k+1 is updated first, panel k+1 is
+// factored on the side stream while the main stream updates the remaining
+// columns, and the two meet before block k+1's swaps.  Every element sees the
+// same operations in the same order as without look-ahead.
 template <typename T>
 static cudaError_t getrf_run(LuState<T>& s, int nb) {
   Context* ctx = s.ctx;
   const int minDim = std::min(s.m, s.n);
+  const bool la = s.side.st != nullptr;
+  cudaError_t e = cudaSuccess;
+  if (minDim == 0) return e;
+  e = panel_rec(s, s.main, 0, std::min(nb, minDim));
+  if (e != cudaSuccess) return e;
   for (int k = 0; k < minDim; k += nb) {
     const int jb = std::min(nb, minDim - k);
-    cudaError_t e = panel_rec(s, k, jb);
+    const int kn = k + jb;
+    const int jb2 = std::min(nb, std::max(minDim - kn, 0));
+    e = apply_swaps(s, s.main, k, jb, 0, k, kn, s.n, true);
     if (e != cudaSuccess) return e;
-    e = apply_swaps(s, k, jb, 0, k, k + jb, s.n, true);
+    if (jb2 > 0) {
+      // the next panel's block column first
+      e = update_cols(s, s.main, k, jb, kn, kn + jb2);
+      if (e != cudaSuccess) return e;
+      if (la) {
+        e = cudaEventRecord(ctx->ev_fork, s.main.st);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s.side.st, ctx->ev_fork, 0);
+        if (e == cudaSuccess) e = panel_rec(s, s.side, kn, jb2);
+        if (e == cudaSuccess) e = cudaEventRecord(ctx->ev_join, s.side.st);
+        if (e != cudaSuccess) return e;
+      }
+    }
+    e = update_cols(s, s.main, k, jb, kn + jb2, s.n);
     if (e != cudaSuccess) return e;
-    const int n2 = s.n - k - jb, m2 = s.m - k - jb;
-    T* A11 = s.A + k + (long)k * s.lda;
-    if (n2 > 0) {
-      e = trsm_llnu<T>(ctx, s.gemm, A11, s.lda, jb, s.A + k + (long)(k + jb) * s.lda, s.lda,
-                       n2);
-      if (e != cudaSuccess) return e;
-    }
-    if (s.Bc && s.nbc > 0) {
-      e = trsm_llnu<T>(ctx, s.gemm, A11, s.lda, jb, s.Bc + k, s.ldbc, s.nbc);
-      if (e != cudaSuccess) return e;
-    }
-    if (m2 > 0 && n2 > 0) {
-      e = gemm_sub(ctx, s.gemm, m2, n2, jb, s.A + (k + jb) + (long)k * s.lda, s.lda,
-                   s.A + k + (long)(k + jb) * s.lda, s.lda,
-                   s.A + (k + jb) + (long)(k + jb) * s.lda, s.lda);
-      if (e != cudaSuccess) return e;
-    }
-    if (m2 > 0 && s.Bc && s.nbc > 0) {
-      e = gemm_sub(ctx, s.gemm, m2, s.nbc, jb, s.A + (k + jb) + (long)k * s.lda, s.lda,
-                   s.Bc + k, s.ldbc, s.Bc + k + jb, s.ldbc);
+    e = update_companion(s, s.main, k, jb);
+    if (e != cudaSuccess) return e;
+    if (jb2 > 0) {
+      if (la)
+        e = cudaStreamWaitEvent(s.main.st, ctx->ev_join, 0);
+      else
+        e = panel_rec(s, s.main, kn, jb2);
       if (e != cudaSuccess) return e;
     }
   }
@@ -291,8 +385,8 @@ static cudaError_t getrf_run(LuState<T>& s, int nb) {
 template <typename T>
 static size_t getrf_scratch_bytes(const Context* ctx, int nb) {
   const int cap = std::max(nb, 32);
-  return panel_scratch_bytes<T>(ctx->num_sms) + align256(4 * (size_t)cap * sizeof(int)) +
-         align256(sizeof(int));
+  return panel_scratch_bytes<T>(ctx->num_sms) + 2 * align256(4 * (size_t)cap * sizeof(int)) +
+         2 * align256(sizeof(int));
 }
 
 template <typename T>
@@ -300,12 +394,18 @@ static cudaError_t setup_lu_state(Context* ctx, LuState<T>& s, Carver& cv, int n
   const int cap = std::max(nb, 32);
   s.ctx = ctx;
   s.ps = carve_panel<T>(cv, ctx->num_sms);
-  s.pairs = cv.take<int>(4 * (size_t)cap);
-  s.pair_count = cv.take<int>(1);
-  s.pairs_cap = cap;
-  if (!s.ps.diag_data || !s.pairs || !s.pair_count) return cudaErrorMemoryAllocation;
+  s.panel_ctas = ctx->num_sms;
+  s.main.st = ctx->stream;
+  s.main.pairs = cv.take<int>(4 * (size_t)cap);
+  s.main.pair_count = cv.take<int>(1);
+  s.side.pairs = cv.take<int>(4 * (size_t)cap);
+  s.side.pair_count = cv.take<int>(1);
+  if (!s.ps.diag_data || !s.side.pair_count) return cudaErrorMemoryAllocation;
   return cudaSuccess;
 }
+
+// Look-ahead pays once the trailing update is large enough to hide a panel.
+static bool use_lookahead(int m, int n, int nb) { return std::min(m, n) >= 4 * nb && n >= 2048; }
 
 template <typename T>
 cudaError_t getrf(Context* ctx, int m, int n, T* A, long lda, int* ipiv, int nb, int tc_kind) {
@@ -314,17 +414,32 @@ cudaError_t getrf(Context* ctx, int m, int n, T* A, long lda, int* ipiv, int nb,
   if (e != cudaSuccess) return e;
   if (m == 0 || n == 0) return cudaSuccess;
   const bool tc = sizeof(T) == 4 && tc_kind >= 0;
+  const bool la = use_lookahead(m, n, nb) && ctx->side_stream;
   const size_t tcb = tc ? tc_gemm_workspace_bytes(tc_kind, m, std::max(n, nb), nb) : 0;
-  e = ctx->ensure(getrf_scratch_bytes<T>(ctx, nb) + align256(tcb));
+  const size_t tcs = (tc && la) ? tc_gemm_workspace_bytes(tc_kind, m, nb, nb) : 0;
+  e = ctx->ensure(getrf_scratch_bytes<T>(ctx, nb) + align256(tcb) + align256(tcs));
   if (e != cudaSuccess) return e;
   Carver cv(ctx);
   LuState<T> s{};
   e = setup_lu_state(ctx, s, cv, nb);
   if (e != cudaSuccess) return e;
   if (tc) {
-    s.gemm.tc_kind = tc_kind;
-    s.gemm.ws = cv.take<char>(tcb);
-    if (!s.gemm.ws) return cudaErrorMemoryAllocation;
+    s.main.gemm.tc_kind = tc_kind;
+    s.main.gemm.ws = cv.take<char>(tcb);
+    if (!s.main.gemm.ws) return cudaErrorMemoryAllocation;
+  }
+  if (la) {
+    s.side.st = ctx->side_stream;
+    s.side.gemm.tc_kind = tc ? tc_kind : -1;
+    if (tc) {
+      s.side.gemm.ws = cv.take<char>(tcs);
+      if (!s.side.gemm.ws) return cudaErrorMemoryAllocation;
+    }
+    // leave most SMs to the concurrent trailing update: ~1024 rows per CTA,
+    // within the panel kernel's shared-memory budget
+    const int rows_cap = (int)((200 * 1024) / (32 * sizeof(T)));
+    int g = std::max((m + 1023) / 1024, (m + rows_cap - 1) / rows_cap);
+    s.panel_ctas = std::max(1, std::min(g, ctx->num_sms));
   }
   s.A = A;
   s.lda = lda;
@@ -649,6 +764,9 @@ int ElGBCreate(ElGBContext* out, int device) {
       cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device) !=
           cudaSuccess ||
       cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->side_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
       cudaMalloc(&c->status, sizeof(elgb::DevStatus)) != cudaSuccess ||
       cudaMallocHost(&c->h_status, sizeof(elgb::DevStatus)) != cudaSuccess) {
     delete c;
@@ -703,18 +821,34 @@ int ElGBProfileStop(ElGBContext ctx, long long* launches, double* ms, double* fl
   if (!ctx) return elgb::kElArgError;
   ctx->prof_on = false;
   if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return elgb::kElRuntimeError;
-  double t = 0, f = 0, b = 0;
+  for (auto& ps : ctx->prof_sum) ps = Context::ProfSum();
   for (auto& r : ctx->prof) {
+    if (!r.b || r.tag < 0 || r.tag >= 16) continue;
     float x = 0;
     if (cudaEventElapsedTime(&x, r.a, r.b) != cudaSuccess) return elgb::kElRuntimeError;
-    t += x;
-    f += r.flops;
-    b += r.bytes;
+    auto& ps = ctx->prof_sum[r.tag];
+    ps.launches += 1;
+    ps.ms += x;
+    ps.flops += r.flops;
+    ps.bytes += r.bytes;
   }
-  if (launches) *launches = (long long)ctx->prof.size();
+  const auto& g = ctx->prof_sum[ELGB_PROF_TC_GEMM];
+  const double t = g.ms, f = g.flops, b = g.bytes;
+  if (launches) *launches = g.launches;
   if (ms) *ms = t;
   if (flops) *flops = f;
   if (bytes) *bytes = b;
+  return 0;
+}
+
+int ElGBProfileTag(ElGBContext ctx, int tag, long long* launches, double* ms, double* flops,
+                   double* bytes) {
+  if (!ctx || tag < 0 || tag >= 16) return elgb::kElArgError;
+  const auto& g = ctx->prof_sum[tag];
+  if (launches) *launches = g.launches;
+  if (ms) *ms = g.ms;
+  if (flops) *flops = g.flops;
+  if (bytes) *bytes = g.bytes;
   return 0;
 }
 

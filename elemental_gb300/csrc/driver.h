@@ -26,6 +26,8 @@ struct Context {
   int num_sms = 1;
   cudaStream_t stream = nullptr;
   cudaStream_t own_stream = nullptr;
+  cudaStream_t side_stream = nullptr;  // look-ahead panels run here
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   void* arena = nullptr;  // growable device scratch, reused across calls
   size_t arena_bytes = 0;
   DevStatus* status = nullptr;    // device status word of the last call
@@ -40,7 +42,17 @@ struct Context {
   struct ProfRec {
     cudaEvent_t a, b;
     double flops, bytes;
+    int tag;  // ELGB_PROF_*
   };
+  struct ProfSum {
+    long long launches = 0;
+    double ms = 0, flops = 0, bytes = 0;
+  };
+  ProfSum prof_sum[16];
+  // Brackets the launches issued between begin and end on `st` when
+  // profiling is on; returns -1 when off.
+  int prof_begin(cudaStream_t st);
+  void prof_end(int idx, cudaStream_t st, int tag, double flops, double bytes);
   bool prof_on = false;
   std::vector<ProfRec> prof;        // records of the current window
   std::vector<cudaEvent_t> ev_pool;  // reusable events

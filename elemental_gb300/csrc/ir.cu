@@ -219,7 +219,10 @@ static cudaError_t lowprec_solve(Context* ctx, int n, int q, const Ws& w, const 
   scale_to_f32_kernel<<<g, 256, 0, ctx->stream>>>(R, rcs, n, scale ? w.scale : nullptr, w.Rf, n);
   ctx->launches += 1;
   IR_CHECK(cudaGetLastError());
+  const int pi = ctx->prof_begin(ctx->stream);
   IR_CHECK(getrs<float>(ctx, 0, n, w.Af, n, w.ipiv, q, w.Rf, n, w.perm));
+  ctx->prof_end(pi, ctx->stream, ELGB_PROF_SOLVE, 2.0 * n * (double)n * q,
+                4.0 * n * (double)n);
   f32_axpy_kernel<<<g, 256, 0, ctx->stream>>>(X, xcs, n, w.Rf, n, scale ? w.scale : nullptr,
                                               accumulate ? 1 : 0);
   ctx->launches += 1;
@@ -334,8 +337,11 @@ cudaError_t refined_solve(Context* ctx, int n, const double* A, long lda, int nr
         int it = 0;
         bool conv = false;
         while (true) {
+          const int pr = ctx->prof_begin(ctx->stream);
           IR_CHECK(launch_residual_f64(n, q, A, lda, Xc, ldx, Bc, ldb, w.R, n, w.rpart,
                                        ctx->stream));
+          ctx->prof_end(pr, ctx->stream, ELGB_PROF_RESIDUAL, 2.0 * n * (double)n * q,
+                        8.0 * n * (double)n);
           ctx->launches += 2;
           IR_CHECK(colnorm2(ctx, w.R, n, n, q, w.sums, w.part, nr));
           IR_CHECK(colnorm2(ctx, Xc, ldx, n, q, w.sums + 17, w.part, nx));
@@ -395,8 +401,11 @@ cudaError_t refined_solve(Context* ctx, int n, const double* A, long lda, int nr
             IR_CHECK(lowprec_solve(ctx, n, q, w, w.V + (long)j * n, vcs, w.Z + (long)j * n, zcs,
                                    false, false));
             // W = A Z(:, j)
+            const int pg = ctx->prof_begin(ctx->stream);
             IR_CHECK(launch_residual_f64(n, q, A, lda, w.Z + (long)j * n, zcs, nullptr, 0, w.W,
                                          n, w.rpart, ctx->stream));
+            ctx->prof_end(pg, ctx->stream, ELGB_PROF_RESIDUAL, 2.0 * n * (double)n * q,
+                          8.0 * n * (double)n);
             ctx->launches += 2;
             // classical Gram-Schmidt, twice
             for (int pass = 0; pass < 2; ++pass) {

@@ -20,6 +20,8 @@ _DT = {torch.float64: "d", torch.float32: "s"}
 PRECISIONS = {"fp64": 0, "fp32": 1, "tf32": 2, "bf16": 3}
 PRECISION_NAMES = {v: k for k, v in PRECISIONS.items()}
 METHODS = {"lu-ir": 0, "gmres-ir": 1}
+PROFILE_TAGS = {"tc_gemm": 0, "panel": 1, "swap": 2, "trsm": 3, "gemm_simt": 4,
+                "residual": 5, "lowprec_solve": 6}
 
 
 class ElGBError(RuntimeError):
@@ -118,7 +120,14 @@ class Context:
         n, ms, fl, by = ctypes.c_longlong(), ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
         self._rc(self.lib.ElGBProfileStop(self.h, ctypes.byref(n), ctypes.byref(ms),
                                           ctypes.byref(fl), ctypes.byref(by)), "ProfileStop")
-        return dict(launches=n.value, ms=ms.value, flops=fl.value, bytes=by.value)
+        out = dict(launches=n.value, ms=ms.value, flops=fl.value, bytes=by.value)
+        tags = {}
+        for name, tag in PROFILE_TAGS.items():
+            self._rc(self.lib.ElGBProfileTag(self.h, tag, ctypes.byref(n), ctypes.byref(ms),
+                                             ctypes.byref(fl), ctypes.byref(by)), "ProfileTag")
+            tags[name] = dict(launches=n.value, ms=ms.value)
+        out["by_kernel"] = tags
+        return out
 
     # -- the path -----------------------------------------------------------
     def lu(self, A, piv=None, nb=0):

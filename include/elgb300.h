@@ -55,6 +55,20 @@ long long ElGBLaunchCount(ElGBContext ctx);
 int ElGBProfileStart(ElGBContext ctx);
 int ElGBProfileStop(ElGBContext ctx, long long* launches, double* ms,
                     double* flops, double* bytes);
+/* After ElGBProfileStop: the same sums for one kernel family (event-bracketed
+ * launch groups; with look-ahead two streams overlap, so the sums can exceed
+ * wall time). */
+enum {
+  ELGB_PROF_TC_GEMM = 0,   /* tcgen05 trailing / TRSM / panel updates        */
+  ELGB_PROF_PANEL = 1,     /* cooperative getf2 leaf panels                  */
+  ELGB_PROF_SWAP = 2,      /* row-interchange pair build + apply             */
+  ELGB_PROF_TRSM = 3,      /* diagonal-block triangular solves (factorization) */
+  ELGB_PROF_GEMM_SIMT = 4, /* CUDA-core GEMM (FP64 path, small FP32 updates) */
+  ELGB_PROF_RESIDUAL = 5,  /* FP64 residual b - A x                          */
+  ELGB_PROF_SOLVE = 6      /* low-precision triangular solves of refinement  */
+};
+int ElGBProfileTag(ElGBContext ctx, int tag, long long* launches, double* ms,
+                   double* flops, double* bytes);
 
 /* El::LU(A, P) with partial pivoting (reference
  * src/lapack_like/factor/LU.cpp:104-138): A (m x n) is overwritten by the
