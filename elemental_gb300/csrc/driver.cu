@@ -119,19 +119,13 @@ static size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
 template <typename T>
 static size_t panel_scratch_bytes(int maxG) {
-  return align256(sizeof(unsigned)) + align256(2 * maxG * sizeof(T)) +
-         align256(2 * maxG * sizeof(int)) + align256(2 * maxG * 32 * sizeof(T)) +
-         align256(2 * 32 * sizeof(T));
+  return align256(2 * (size_t)maxG * sizeof(PanelSlot<T>));
 }
 
 template <typename T>
 static PanelScratch<T> carve_panel(Carver& cv, int maxG) {
   PanelScratch<T> s;
-  s.bar = cv.take<unsigned>(1);
-  s.cand_val = cv.take<T>(2 * maxG);
-  s.cand_row = cv.take<int>(2 * maxG);
-  s.cand_data = cv.take<T>(2 * (size_t)maxG * 32);
-  s.diag_data = cv.take<T>(2 * 32);
+  s.slots = cv.take<PanelSlot<T>>(2 * (size_t)maxG);
   s.maxG = maxG;
   return s;
 }
@@ -215,6 +209,7 @@ struct LuState {
   int* ipiv;           // absolute swap destinations, device
   PanelScratch<T> ps;  // used by whichever lane factors panels
   int panel_ctas;      // CTAs of a panel launch (fewer when it overlaps the update)
+  int panel_epoch;     // panel columns published so far (slot epochs)
   LuLane main, side;   // side.st == nullptr: no look-ahead
   T* Bc;               // companion block receiving the same row operations
   long ldbc;           // (RowEchelon's B, src/lapack_like/solve/Linear.cpp:62-71)
@@ -274,8 +269,9 @@ static cudaError_t panel_rec(LuState<T>& s, const LuLane& L, int c0, int w) {
   if (w <= 32) {
     const int pi = ctx->prof_begin(L.st);
     LANE_CHECK(launch_getf2_panel<T>(s.A + c0 + (long)c0 * s.lda, s.lda, s.m - c0, w,
-                                     s.ipiv + c0, c0, c0, s.ps, ctx->status, s.panel_ctas,
-                                     L.st), 2);
+                                     s.ipiv + c0, c0, c0, s.panel_epoch, s.ps, ctx->status,
+                                     s.panel_ctas, L.st), 1);
+    s.panel_epoch += w;
     ctx->prof_end(pi, L.st, ELGB_PROF_PANEL, (double)(s.m - c0) * w * w,
                   2.0 * sizeof(T) * (s.m - c0) * (double)w);
     return cudaSuccess;
@@ -395,12 +391,17 @@ static cudaError_t setup_lu_state(Context* ctx, LuState<T>& s, Carver& cv, int n
   s.ctx = ctx;
   s.ps = carve_panel<T>(cv, ctx->num_sms);
   s.panel_ctas = ctx->num_sms;
+  s.panel_epoch = 0;
+  if (!s.ps.slots) return cudaErrorMemoryAllocation;
+  cudaError_t e = cudaMemsetAsync(s.ps.slots, 0, 2 * (size_t)ctx->num_sms * sizeof(PanelSlot<T>),
+                                  ctx->stream);
+  if (e != cudaSuccess) return e;
   s.main.st = ctx->stream;
   s.main.pairs = cv.take<int>(4 * (size_t)cap);
   s.main.pair_count = cv.take<int>(1);
   s.side.pairs = cv.take<int>(4 * (size_t)cap);
   s.side.pair_count = cv.take<int>(1);
-  if (!s.ps.diag_data || !s.side.pair_count) return cudaErrorMemoryAllocation;
+  if (!s.side.pair_count) return cudaErrorMemoryAllocation;
   return cudaSuccess;
 }
 
@@ -677,7 +678,7 @@ cudaError_t backward_error(Context* ctx, int n, int q, const double* A, long lda
   const size_t need = align256((size_t)n * q * sizeof(double)) +
                       align256((size_t)(n + 2) * sizeof(double)) +
                       3 * align256((size_t)(q + 2) * sizeof(double)) +
-                      align256((size_t)64 * (std::max(n, q) + 1) * sizeof(double)) +
+                      align256(((size_t)64 * (std::max(n, q) + 1) + 8) * sizeof(double)) +
                       align256((size_t)((n + 4095) / 4096) * n * 16 * sizeof(double));
   cudaError_t e = ctx->ensure(need);
   if (e != cudaSuccess) return e;
@@ -687,7 +688,7 @@ cudaError_t backward_error(Context* ctx, int n, int q, const double* A, long lda
   double* nX = cv.take<double>(q + 2);
   double* nR = cv.take<double>(q + 2);
   double* nB = cv.take<double>(q + 2);
-  double* partial = cv.take<double>((size_t)64 * (std::max(n, q) + 1));
+  double* partial = cv.take<double>((size_t)64 * (std::max(n, q) + 1) + 8);
   double* rpart = cv.take<double>((size_t)((n + 4095) / 4096) * n * 16);
   if (!R || !nA || !nX || !nR || !nB || !partial || !rpart) return cudaErrorMemoryAllocation;
   for (int c = 0; c < q; c += 16) {

@@ -28,6 +28,7 @@
 #include "driver.h"
 #include "kernels.h"
 #include "tc_gemm.h"
+#include "trsv.h"
 
 namespace elgb {
 
@@ -66,6 +67,19 @@ __global__ void col_absmax_finish_kernel(const double* __restrict__ partial, int
   double v = 0.0;
   for (int ch = 0; ch < nch; ++ch) v = fmax(v, partial[(long)c * nch + ch]);
   scale[c] = (v > 0.0 && v < INFINITY) ? v : 1.0;
+}
+
+// Rf(i, c) = R(perm[i], c) / scale[c]  (row permutation P R fused with the
+// FP64 -> FP32 scaling)
+__global__ void scale_perm_to_f32_kernel(const double* __restrict__ R, long cstride, int n,
+                                         const int* __restrict__ perm,
+                                         const double* __restrict__ scale,
+                                         float* __restrict__ Rf, long ldf) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = blockIdx.y;
+  if (i < n)
+    Rf[i + (long)c * ldf] =
+        (float)(R[perm[i] + (long)c * cstride] / (scale ? scale[c] : 1.0));
 }
 
 // Rf(:, c) = R(:, c) / scale[c]  (FP64 -> FP32); column c of R starts at
@@ -177,6 +191,11 @@ struct Ws {
   double* W;
   double* H;         // device [q][restart + 1]
   double* dpart;
+  float* Dl;         // inverted 64 x 64 diagonal blocks of L (unit lower)
+  float* Du;         // ... and of U
+  int* flags;        // block-row done flags of the one-launch triangular solves
+  unsigned* ticket;
+  int epoch;
 };
 
 size_t al(size_t b) { return (b + 255) & ~size_t(255); }
@@ -207,7 +226,7 @@ static cudaError_t colnorm2(Context* ctx, const double* X, long ld, int n, int q
 // The low-precision preconditioner application: D = (P^T L U)^{-1} R in
 // FP32 (columns scaled by their max-abs to stay in range), D into X either
 // added (accumulate) or stored.
-static cudaError_t lowprec_solve(Context* ctx, int n, int q, const Ws& w, const double* R,
+static cudaError_t lowprec_solve(Context* ctx, int n, int q, Ws& w, const double* R,
                                  long rcs, double* X, long xcs, bool accumulate, bool scale) {
   dim3 g((n + 255) / 256, q);
   const int nch = (n + kRowChunk - 1) / kRowChunk;
@@ -216,11 +235,18 @@ static cudaError_t lowprec_solve(Context* ctx, int n, int q, const Ws& w, const 
     col_absmax_finish_kernel<<<1, 32, 0, ctx->stream>>>(w.part, nch, q, w.scale);
     ctx->launches += 2;
   }
-  scale_to_f32_kernel<<<g, 256, 0, ctx->stream>>>(R, rcs, n, scale ? w.scale : nullptr, w.Rf, n);
+  scale_perm_to_f32_kernel<<<g, 256, 0, ctx->stream>>>(R, rcs, n, w.perm,
+                                                       scale ? w.scale : nullptr, w.Rf, n);
   ctx->launches += 1;
   IR_CHECK(cudaGetLastError());
+  // (P^T L U)^{-1}: L then U, each one launch
   const int pi = ctx->prof_begin(ctx->stream);
-  IR_CHECK(getrs<float>(ctx, 0, n, w.Af, n, w.ipiv, q, w.Rf, n, w.perm));
+  IR_CHECK(launch_trsv_persistent<float>(w.Af, n, w.Dl, w.Rf, n, n, q, true, w.ticket, w.flags,
+                                         ++w.epoch, ctx->status, ctx->num_sms, ctx->stream));
+  IR_CHECK(launch_trsv_persistent<float>(w.Af, n, w.Du, w.Rf, n, n, q, false, w.ticket,
+                                         w.flags, ++w.epoch, ctx->status, ctx->num_sms,
+                                         ctx->stream));
+  ctx->launches += 2;
   ctx->prof_end(pi, ctx->stream, ELGB_PROF_SOLVE, 2.0 * n * (double)n * q,
                 4.0 * n * (double)n);
   f32_axpy_kernel<<<g, 256, 0, ctx->stream>>>(X, xcs, n, w.Rf, n, scale ? w.scale : nullptr,
@@ -266,9 +292,12 @@ cudaError_t refined_solve(Context* ctx, int n, const double* A, long lda, int nr
   const int kb = c.restart + 1;
   size_t need = al((size_t)n * n * sizeof(float)) + 2 * al((size_t)n * sizeof(int)) +
                 2 * al((size_t)n * Q * sizeof(double)) + al((size_t)n * Q * sizeof(float)) +
-                al(Q * sizeof(double)) + al((size_t)64 * (n + 1) * sizeof(double)) +
+                al(Q * sizeof(double)) + al(((size_t)64 * (n + 1) + 8) * sizeof(double)) +
                 al((size_t)rch * n * 16 * sizeof(double)) + al(4 * (Q + 1) * sizeof(double)) +
                 al((size_t)(n + 1) * sizeof(double));
+  const int nblk = trsv_blocks(n);
+  need += 2 * al((size_t)nblk * 4096 * sizeof(float)) + al((size_t)nblk * sizeof(int)) +
+          al(sizeof(unsigned));
   if (gm)
     need += al((size_t)Q * kb * n * sizeof(double)) + al((size_t)Q * c.restart * n * sizeof(double)) +
             al((size_t)n * Q * sizeof(double)) + al((size_t)Q * kb * sizeof(double)) +
@@ -291,10 +320,16 @@ cudaError_t refined_solve(Context* ctx, int n, const double* A, long lda, int nr
     w.Xprev = (double*)take((size_t)n * Q * sizeof(double));
     w.Rf = (float*)take((size_t)n * Q * sizeof(float));
     w.scale = (double*)take(Q * sizeof(double));
-    w.part = (double*)take((size_t)64 * (n + 1) * sizeof(double));
+    w.part = (double*)take(((size_t)64 * (n + 1) + 8) * sizeof(double));
     w.rpart = (double*)take((size_t)rch * n * 16 * sizeof(double));
     w.sums = (double*)take(4 * (Q + 1) * sizeof(double));
     w.colout = (double*)take((size_t)(n + 1) * sizeof(double));
+    w.Dl = (float*)take((size_t)nblk * 4096 * sizeof(float));
+    w.Du = (float*)take((size_t)nblk * 4096 * sizeof(float));
+    w.flags = (int*)take((size_t)nblk * sizeof(int));
+    w.ticket = (unsigned*)take(sizeof(unsigned));
+    w.epoch = 0;
+    IR_CHECK(cudaMemsetAsync(w.flags, 0, (size_t)nblk * sizeof(int), ctx->stream));
     if (gm) {
       w.V = (double*)take((size_t)Q * kb * n * sizeof(double));
       w.Z = (double*)take((size_t)Q * c.restart * n * sizeof(double));
@@ -314,7 +349,9 @@ cudaError_t refined_solve(Context* ctx, int n, const double* A, long lda, int nr
     if (ferr) return cudaErrorLaunchTimeout;
     if (finfo == 0) {
       IR_CHECK(launch_explicit_perm(w.ipiv, n, n, w.perm, ctx->stream));
-      ctx->launches += 1;
+      IR_CHECK(launch_trtri_diag<float>(w.Af, n, n, true, true, w.Dl, ctx->stream));
+      IR_CHECK(launch_trtri_diag<float>(w.Af, n, n, false, false, w.Du, ctx->stream));
+      ctx->launches += 3;
       // ||A||_F
       IR_CHECK(launch_col_sumsq<double>(A, lda, n, n, w.colout, w.part, ctx->stream));
       ctx->launches += 2;

@@ -12,14 +12,21 @@
 
 namespace elgb {
 
-// Device scratch used by one factorization call.  Sized by the driver.
+// One CTA's published state for one panel column (see getf2_panel_kernel).
+template <typename T>
+struct alignas(16) PanelSlot {
+  T val;        // |candidate|
+  int row;      // candidate row (panel-relative), -1 = none
+  int epoch;    // written last, with release semantics
+  T cand[32];   // the candidate row
+  T diag[32];   // row j (written by its owner only)
+};
+
+// Device scratch of the panel factorization: slots [2][maxG] (column
+// parity x CTA), zeroed once per factorization.
 template <typename T>
 struct PanelScratch {
-  unsigned* bar;      // grid-barrier counter (zeroed before each panel launch)
-  T* cand_val;        // [2][maxG]   |candidate|
-  int* cand_row;      // [2][maxG]   candidate row (panel-relative), -1 = none
-  T* cand_data;       // [2][maxG][32] candidate rows
-  T* diag_data;       // [2][32]     current diagonal row
+  PanelSlot<T>* slots;
   int maxG;
 };
 
@@ -28,9 +35,11 @@ struct PanelScratch {
 // `A` points at the panel's top-left element, `mp` rows, `w` columns.
 // ipiv[c] receives the absolute pivot row (row_base + panel row).  A zero
 // pivot records info = info_base + c + 1 (first one wins) in st.
+// epoch_base: columns published so far in this factorization (the slot
+// epochs must keep growing across launches).
 template <typename T>
 cudaError_t launch_getf2_panel(T* A, long lda, int mp, int w, int* ipiv,
-                               int row_base, int info_base,
+                               int row_base, int info_base, int epoch_base,
                                const PanelScratch<T>& s, DevStatus* st,
                                int num_sms, cudaStream_t stream);
 
@@ -105,7 +114,8 @@ cudaError_t launch_residual_f64(int n, int q, const double* A, long lda,
                                 cudaStream_t stream);
 
 // Sum of squares of each column (out[j]) and of all entries (out[ncols]) of
-// an m x ncols matrix, deterministic.  partial holds 64 * (ncols + 1) doubles.
+// an m x ncols matrix, deterministic.  partial holds 64 * (ncols + 1) doubles
+// followed by one zero-initialised unsigned counter (left zero on return).
 template <typename T>
 cudaError_t launch_col_sumsq(const T* A, long lda, int m, int ncols,
                              double* out, double* partial,

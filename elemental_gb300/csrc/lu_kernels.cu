@@ -44,16 +44,21 @@ __device__ __forceinline__ void block_argmax(T& v, int& r, T* s_v, int* s_r) {
 // One cooperative launch factors a w-column panel (w <= W = 32).  CTA b owns
 // panel rows [b*R, b*R + R) and keeps them in shared memory for the whole
 // panel (column-major slab, slab[c * R + r]).  Per column j:
-//   1. each CTA publishes its best candidate (|a|, row, whole row) for column
-//      j, found while it applied the previous column's update;
-//   2. one grid barrier;
-//   3. every CTA reduces the G candidates (ties -> lowest row, idamax's
-//      rule), swaps the pivot row and row j inside its slab if it owns them,
+//   1. each CTA writes its slot: its best candidate (|a|, row) for column j
+//      with that row, and (the owner of row j only) row j itself, then
+//      publishes the slot with a release store of the column's epoch;
+//   2. threads 0..G-1 poll the G slot epochs (acquire): seeing all of them is
+//      the grid barrier, and the candidate headers arrive with it;
+//   3. warp 0 reduces the candidates (ties -> lowest row, idamax's rule);
+//      the winner's row and row j are read from their slots;
+//   4. the CTA swaps the pivot row and row j inside its slab if it owns them,
 //      scales by the reciprocal of the pivot (El scales by alpha11Inv,
 //      Panel.hpp:53-55) and applies the rank-1 update to its rows while
 //      computing its candidate for column j+1.
-// Candidate slots are double-buffered by column parity, so one barrier per
-// column suffices.
+// Slots are double-buffered by column parity: a CTA can only rewrite a slot
+// after every CTA has published the next column, i.e. finished reading this
+// one.  Epochs grow across the launches of one factorization, so slots never
+// need clearing between panels.
 template <typename T>
 struct PanelParams {
   T* A;
@@ -61,12 +66,22 @@ struct PanelParams {
   int mp, w, R;
   int* ipiv;
   int row_base, info_base;
+  int epoch_base;  // column j of this launch publishes epoch_base + j + 1
   PanelScratch<T> s;
   DevStatus* st;
 };
 
 constexpr int kPanelW = 32;
 constexpr int kPanelThreads = 256;
+
+__device__ __forceinline__ void st_release_s32(int* p, int v) {
+  asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ int ld_acquire_s32(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
 
 template <typename T, int W>
 __global__ void __launch_bounds__(kPanelThreads)
@@ -77,7 +92,9 @@ getf2_panel_kernel(PanelParams<T> p) {
   __shared__ T s_d[W];
   __shared__ T s_rv[33];
   __shared__ int s_rr[33];
-  __shared__ int s_piv;
+  __shared__ T s_gv[kPanelThreads];
+  __shared__ int s_gr[kPanelThreads];
+  __shared__ int s_piv, s_abort;
 
   const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
@@ -89,6 +106,7 @@ getf2_panel_kernel(PanelParams<T> p) {
   for (int c = 0; c < w; ++c)
     for (int r = tid; r < nr; r += blockDim.x)
       slab[c * R + r] = p.A[(long)(rb + r) + (long)c * p.lda];
+  if (tid == 0) s_abort = 0;
   __syncthreads();
 
   T bv = T(-1);
@@ -103,26 +121,48 @@ getf2_panel_kernel(PanelParams<T> p) {
   block_argmax(bv, br, s_rv, s_rr);
 
   for (int j = 0; j < w; ++j) {
-    const int par = j & 1;
-    T* my_cand = p.s.cand_data + ((long)par * maxG + b) * W;
+    const int epoch = p.epoch_base + j + 1;
+    const int par = epoch & 1;
+    PanelSlot<T>* my = p.s.slots + (long)par * maxG + b;
+    // 1. publish
+    if (br >= 0 && tid < w) my->cand[tid] = slab[tid * R + (br - rb)];
+    if (j >= rb && j < re && tid < w) my->diag[tid] = slab[tid * R + (j - rb)];
     if (tid == 0) {
-      p.s.cand_val[par * maxG + b] = bv;
-      p.s.cand_row[par * maxG + b] = br;
+      my->val = bv;
+      my->row = br;
     }
-    if (br >= 0 && tid < w) my_cand[tid] = slab[tid * R + (br - rb)];
-    if (j >= rb && j < re && tid < w)
-      p.s.diag_data[par * W + tid] = slab[tid * R + (j - rb)];
-    if (!grid_barrier(p.s.bar, (unsigned)(j + 1), (unsigned)G, p.st, 1)) return;
-
+    __syncthreads();
+    if (tid == 0) {
+      __threadfence();
+      st_release_s32(&my->epoch, epoch);
+    }
+    // 2. the barrier: every slot carries this epoch
+    if (tid < G) {
+      const PanelSlot<T>* sl = p.s.slots + (long)par * maxG + tid;
+      if (ld_acquire_s32(&sl->epoch) != epoch) {
+        const unsigned long long t0 = globaltimer_ns();
+        while (ld_acquire_s32(&sl->epoch) != epoch) {
+          if (*(volatile int*)&p.st->err != 0 || globaltimer_ns() - t0 > kSpinLimitNs) {
+            atomicCAS(&p.st->err, 0, (int)kErrBarrierTimeout);
+            p.st->err_where = 1;
+            s_abort = 1;
+            break;
+          }
+        }
+      }
+      s_gv[tid] = __ldcg(&sl->val);
+      s_gr[tid] = __ldcg(&sl->row);
+    }
+    __syncthreads();
+    if (s_abort) return;
+    // 3. reduce
     if (warp == 0) {
       T v = T(-1);
       int r = -1;
       for (int g = lane; g < G; g += 32) {
-        const T gv = __ldcg(p.s.cand_val + par * maxG + g);
-        const int gr = __ldcg(p.s.cand_row + par * maxG + g);
-        if (argmax_better(gv, gr, v, r)) {
-          v = gv;
-          r = gr;
+        if (argmax_better(s_gv[g], s_gr[g], v, r)) {
+          v = s_gv[g];
+          r = s_gr[g];
         }
       }
       warp_argmax(v, r);
@@ -131,13 +171,13 @@ getf2_panel_kernel(PanelParams<T> p) {
     __syncthreads();
     const int piv = s_piv;
     if (tid < w) {
-      // cross-CTA data: read at L2 (never a stale L1 line)
-      const T d = __ldcg(p.s.diag_data + par * W + tid);
+      const PanelSlot<T>* own = p.s.slots + (long)par * maxG + j / R;
+      const T d = __ldcg(&own->diag[tid]);
       s_d[tid] = d;
-      s_u[tid] = (piv == j) ? d
-                            : __ldcg(p.s.cand_data + ((long)par * maxG + piv / R) * W + tid);
+      s_u[tid] = (piv == j) ? d : __ldcg(&p.s.slots[(long)par * maxG + piv / R].cand[tid]);
     }
     __syncthreads();
+    // 4. swap, scale, update, next candidate
     if (b == 0 && tid == 0) p.ipiv[j] = p.row_base + piv;
     if (piv != j && tid < w) {
       if (j >= rb && j < re) slab[tid * R + (j - rb)] = s_u[tid];
@@ -174,93 +214,96 @@ getf2_panel_kernel(PanelParams<T> p) {
 }
 
 template <typename T>
-cudaError_t launch_getf2_panel(T* A, long lda, int mp, int w, int* ipiv,
-                               int row_base, int info_base,
-                               const PanelScratch<T>& s, DevStatus* st,
-                               int num_sms, cudaStream_t stream) {
+cudaError_t launch_getf2_panel(T* A, long lda, int mp, int w, int* ipiv, int row_base,
+                               int info_base, int epoch_base, const PanelScratch<T>& s,
+                               DevStatus* st, int num_sms, cudaStream_t stream) {
   if (w <= 0 || mp <= 0) return cudaSuccess;
   if (w > kPanelW || mp < w) return cudaErrorInvalidValue;
   constexpr int kMaxSmem = 200 * 1024;
   int G = ceil_div(mp, 128);
   if (G > num_sms) G = num_sms;
   if (G > s.maxG) G = s.maxG;
+  if (G > kPanelThreads) G = kPanelThreads;
   if (G < 1) G = 1;
   int R = ceil_div(mp, G);
+  G = ceil_div(mp, R);  // no CTA without rows
   size_t smem = (size_t)R * kPanelW * sizeof(T);
   if (smem > (size_t)kMaxSmem) return cudaErrorInvalidValue;
   auto kern = getf2_panel_kernel<T, kPanelW>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        kMaxSmem);
   if (e != cudaSuccess) return e;
-  e = cudaMemsetAsync(s.bar, 0, sizeof(unsigned), stream);
-  if (e != cudaSuccess) return e;
-  PanelParams<T> prm{A, lda, mp, w, R, ipiv, row_base, info_base, s, st};
+  PanelParams<T> prm{A, lda, mp, w, R, ipiv, row_base, info_base, epoch_base, s, st};
   void* args[] = {&prm};
   return cudaLaunchCooperativeKernel((const void*)kern, dim3(G), dim3(kPanelThreads),
                                      args, smem, stream);
 }
 
-template cudaError_t launch_getf2_panel<double>(double*, long, int, int, int*, int, int,
+template cudaError_t launch_getf2_panel<double>(double*, long, int, int, int*, int, int, int,
                                                 const PanelScratch<double>&, DevStatus*,
                                                 int, cudaStream_t);
-template cudaError_t launch_getf2_panel<float>(float*, long, int, int, int*, int, int,
+template cudaError_t launch_getf2_panel<float>(float*, long, int, int, int*, int, int, int,
                                                const PanelScratch<float>&, DevStatus*,
                                                int, cudaStream_t);
 
 // ---------------------------------------------------------------------------
 // K2: row interchanges (PB.PermuteRows, src/lapack_like/factor/LU.cpp:130-131)
 // ---------------------------------------------------------------------------
-// The nb swaps (k+i <-> ipiv[i]) are replayed once, by one warp, on row
-// labels only; the result is the list of rows whose contents change and the
-// row each one receives.  Applying that list touches every affected element
-// once (read all, then write all) instead of replaying nb dependent swaps.
-__global__ void build_swap_pairs_kernel(const int* __restrict__ ipiv, int k, int nb,
+// The nb swaps (k+i <-> ipiv[i]) are replayed once, on row labels only, by
+// one thread with an open-addressing hash table in shared memory for the rows
+// below the block; the result is the list of rows whose contents change and
+// the row each one receives.  Applying that list touches every affected
+// element once (read all, then write all) instead of replaying nb dependent
+// swaps.
+__device__ __forceinline__ int swap_hash(int row, int mask) {
+  return (int)(((unsigned)row * 2654435761u) >> 7) & mask;
+}
+
+__global__ void build_swap_pairs_kernel(const int* __restrict__ ipiv, int k, int nb, int tbits,
                                         int* __restrict__ pairs, int* __restrict__ count) {
   extern __shared__ int sh[];
-  int* top = sh;            // top[i]: original row now at row k+i
-  int* keys = sh + nb;      // rows >= k+nb that were touched
-  int* vals = sh + 2 * nb;  // original row now at keys[i]
-  __shared__ int s_nkeys;
-  const int lane = threadIdx.x;
-  for (int i = lane; i < nb; i += 32) top[i] = k + i;
-  if (lane == 0) s_nkeys = 0;
-  __syncwarp();
-  for (int i = 0; i < nb; ++i) {
-    const int piv = ipiv[i];
-    if (piv < k + nb) {
-      if (lane == 0 && piv != k + i) {
+  const int tsize = 1 << tbits, mask = tsize - 1;
+  int* top = sh;                  // top[i]: original row now at row k+i
+  int* piv = sh + nb;             // the pivots, staged
+  int* order = sh + 2 * nb;       // table slots in insertion order
+  int* keys = sh + 3 * nb;        // rows >= k+nb that were touched (-1 = empty)
+  int* vals = keys + tsize;       // original row now at keys[slot]
+  __shared__ int s_nk;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+    top[i] = k + i;
+    piv[i] = ipiv[i];
+  }
+  for (int i = threadIdx.x; i < tsize; i += blockDim.x) keys[i] = -1;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int nk = 0;
+    for (int i = 0; i < nb; ++i) {
+      const int p = piv[i];
+      if (p < k + nb) {
         const int t = top[i];
-        top[i] = top[piv - k];
-        top[piv - k] = t;
-      }
-    } else {
-      const int nk = s_nkeys;
-      int found = -1;
-      for (int base = 0; base < nk; base += 32) {
-        const int idx = base + lane;
-        const bool hit = idx < nk && keys[idx] == piv;
-        const unsigned bal = __ballot_sync(0xffffffffu, hit);
-        if (bal) {
-          found = base + __ffs(bal) - 1;
-          break;
-        }
-      }
-      if (lane == 0) {
-        if (found >= 0) {
-          const int t = vals[found];
-          vals[found] = top[i];
+        top[i] = top[p - k];
+        top[p - k] = t;
+      } else {
+        int h = swap_hash(p, mask);
+        while (keys[h] != -1 && keys[h] != p) h = (h + 1) & mask;
+        if (keys[h] == p) {
+          const int t = vals[h];
+          vals[h] = top[i];
           top[i] = t;
         } else {
-          keys[nk] = piv;
-          vals[nk] = top[i];
-          top[i] = piv;
-          s_nkeys = nk + 1;
+          keys[h] = p;
+          vals[h] = top[i];
+          top[i] = p;
+          order[nk++] = h;
         }
       }
     }
-    __syncwarp();
+    s_nk = nk;
   }
-  if (lane == 0) {
+  __syncthreads();
+  // emit (dst, src) for changed rows; lane-parallel with a block-wide scan
+  // kept simple: thread 0 compacts (at most 2 nb entries)
+  if (threadIdx.x == 0) {
     int* dst = pairs;
     int* src = pairs + 2 * nb;
     int c = 0;
@@ -270,28 +313,31 @@ __global__ void build_swap_pairs_kernel(const int* __restrict__ ipiv, int k, int
         src[c] = top[i];
         ++c;
       }
-    const int nk = s_nkeys;
-    for (int i = 0; i < nk; ++i)
-      if (vals[i] != keys[i]) {
-        dst[c] = keys[i];
-        src[c] = vals[i];
+    for (int t = 0; t < s_nk; ++t) {
+      const int h = order[t];
+      if (vals[h] != keys[h]) {
+        dst[c] = keys[h];
+        src[c] = vals[h];
         ++c;
       }
+    }
     *count = c;
   }
 }
 
-cudaError_t launch_build_swap_pairs(const int* ipiv, int k, int nb, int* pairs,
-                                    int* count, cudaStream_t stream) {
+cudaError_t launch_build_swap_pairs(const int* ipiv, int k, int nb, int* pairs, int* count,
+                                    cudaStream_t stream) {
   if (nb <= 0) return cudaMemsetAsync(count, 0, sizeof(int), stream);
-  const size_t smem = 3 * (size_t)nb * sizeof(int);
+  int tbits = 5;
+  while ((1 << tbits) < 4 * nb) ++tbits;
+  const size_t smem = (3 * (size_t)nb + 2 * ((size_t)1 << tbits)) * sizeof(int);
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(build_swap_pairs_kernel,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
   }
-  build_swap_pairs_kernel<<<1, 32, smem, stream>>>(ipiv, k, nb, pairs, count);
+  build_swap_pairs_kernel<<<1, 128, smem, stream>>>(ipiv, k, nb, tbits, pairs, count);
   return cudaGetLastError();
 }
 
@@ -915,17 +961,41 @@ col_sumsq_partial_kernel(const T* __restrict__ A, long lda, int m, int ncols,
   if (threadIdx.x == 0) partial[(long)c * kSumsqChunks + ch] = s[0];
 }
 
+// Per-column sums (one warp per column, fixed shuffle order), then the total
+// over columns by the last block to finish (fixed order, deterministic).
 __global__ void col_sumsq_finish_kernel(int ncols, const double* __restrict__ partial,
-                                        double* __restrict__ out) {
-  if (threadIdx.x != 0) return;
-  double tot = 0.0;
-  for (int c = 0; c < ncols; ++c) {
-    double s = 0.0;
-    for (int ch = 0; ch < kSumsqChunks; ++ch) s += partial[(long)c * kSumsqChunks + ch];
-    out[c] = s;
-    tot += s;
+                                        double* __restrict__ out, unsigned* __restrict__ done) {
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31;
+  const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (c < ncols) {
+    double s = partial[(long)c * kSumsqChunks + lane] + partial[(long)c * kSumsqChunks + 32 + lane];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) out[c] = s;
   }
-  out[ncols] = tot;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(done, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  __shared__ double red[256];
+  double t = 0.0;
+  const int per = (ncols + blockDim.x - 1) / blockDim.x;
+  for (int i = 0; i < per; ++i) {
+    const int cc = threadIdx.x * per + i;
+    if (cc < ncols) t += __ldcg(out + cc);
+  }
+  red[threadIdx.x] = t;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out[ncols] = red[0];
+    *done = 0;  // ready for the next call
+  }
 }
 
 template <typename T>
@@ -935,7 +1005,11 @@ cudaError_t launch_col_sumsq(const T* A, long lda, int m, int ncols, double* out
   if (m <= 0) return cudaMemsetAsync(out, 0, sizeof(double) * (ncols + 1), stream);
   col_sumsq_partial_kernel<T><<<dim3(ncols, kSumsqChunks), 256, 0, stream>>>(A, lda, m,
                                                                              ncols, partial);
-  col_sumsq_finish_kernel<<<1, 32, 0, stream>>>(ncols, partial, out);
+  // the completion counter lives right after the partial sums
+  unsigned* done = reinterpret_cast<unsigned*>(partial + (long)kSumsqChunks * (ncols + 1));
+  cudaError_t e = cudaMemsetAsync(done, 0, sizeof(unsigned), stream);
+  if (e != cudaSuccess) return e;
+  col_sumsq_finish_kernel<<<(ncols + 7) / 8, 256, 0, stream>>>(ncols, partial, out, done);
   return cudaGetLastError();
 }
 template cudaError_t launch_col_sumsq<double>(const double*, long, int, int, double*,
