@@ -31,6 +31,12 @@ class RefineInfo(ctypes.Structure):
                 ("precision", c_int), ("backward_error", c_double)]
 
 
+class BatchResult(ctypes.Structure):
+    """ElGBBatchResult (include/elgb300.h)."""
+    _fields_ = [("iterations", c_int), ("converged", c_int), ("fell_back", c_int),
+                ("info", c_int), ("backward_error", c_double)]
+
+
 def _sig(lib, name, res, *args):
     f = getattr(lib, name)
     f.restype = res
@@ -56,6 +62,7 @@ def load():
     _sig(lib, "ElGBBlocksize", c_int)
     _sig(lib, "ElGBSetBlocksize", c_int, c_int)
     _sig(lib, "ElGBLaunchCount", c_ll, vp)
+    _sig(lib, "ElGBSetOption", c_int, vp, c_int, c_int)
     _sig(lib, "ElGBProfileStart", c_int, vp)
     _sig(lib, "ElGBProfileStop", c_int, vp, P(c_ll), P(c_double), P(c_double), P(c_double))
     _sig(lib, "ElGBProfileTag", c_int, vp, c_int, P(c_ll), P(c_double), P(c_double),
@@ -77,6 +84,12 @@ def load():
          P(RefineCtrl), P(RefineInfo))
     _sig(lib, "ElGBResidual_d", c_int, vp, c_int, c_int, vp, c_int, vp, c_int, vp, c_int, vp,
          c_int)
+    _sig(lib, "ElGBBatchedPlanCreate", c_int, vp, c_int, vp, vp, vp, c_int, vp, vp, vp, vp,
+         c_int, c_double, c_int, P(vp))
+    _sig(lib, "ElGBBatchedExecute", c_int, vp)
+    _sig(lib, "ElGBBatchedResults", c_int, vp, vp)
+    _sig(lib, "ElGBBatchedFlops", c_double, vp)
+    _sig(lib, "ElGBBatchedPlanDestroy", c_int, vp)
     _sig(lib, "ElGBBackwardError_d", c_int, vp, c_int, c_int, vp, c_int, vp, c_int, vp, c_int,
          P(c_double))
     _sig(lib, "ElGBProbeFP64Peak", c_int, vp, P(c_double))

@@ -1,0 +1,97 @@
+"""Batched uneven-size solves (added form 2) from Python: packs a list of
+systems into the device layout of ElGBBatchedPlanCreate (include/elgb300.h),
+keeps the plan (descriptors, workspaces, CUDA graph) and replays it."""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from .device import Context, context
+
+KIND = {"lu": 0, "chol": 1}
+PREC = {"fp64": 0, "fp32": 1}
+
+
+class BatchedSolver:
+    """Solve A_i X_i = B_i for many small systems in one persistent launch.
+
+    systems: list of (A_i (n_i x n_i), B_i (n_i x q)) numpy FP64 arrays, or
+    pre-packed device tensors via from_packed().  kinds / precisions: lists of
+    "lu" / "chol" and "fp32" / "fp64".
+    """
+
+    def __init__(self, ns, q, A_packed, B_packed, kinds=None, precisions=None, nb_table=None,
+                 ctas_per_sm=1, tol=1e-13, max_iters=10, ctx: Context | None = None):
+        self.ctx = ctx or context()
+        self.lib = _lib.load()
+        self.ns = np.ascontiguousarray(ns, dtype=np.int32)
+        self.count = len(self.ns)
+        self.q = q
+        self.A = A_packed
+        self.B = B_packed
+        self.X = torch.empty_like(B_packed)
+        k = np.ascontiguousarray([KIND[x] for x in kinds] if kinds is not None
+                                 else np.zeros(self.count), dtype=np.int32)
+        pr = np.ascontiguousarray([PREC[x] for x in precisions] if precisions is not None
+                                  else np.ones(self.count), dtype=np.int32)
+        self.kinds, self.precs = k, pr
+        nbt = None
+        if nb_table is not None:
+            nbt = np.ascontiguousarray(nb_table, dtype=np.int32)
+        h = ctypes.c_void_p()
+        vp = ctypes.c_void_p
+        rc = self.lib.ElGBBatchedPlanCreate(
+            self.ctx.h, self.count, self.ns.ctypes.data_as(vp), k.ctypes.data_as(vp),
+            pr.ctypes.data_as(vp), q, vp(self.A.data_ptr()), vp(self.B.data_ptr()),
+            vp(self.X.data_ptr()), nbt.ctypes.data_as(vp) if nbt is not None else None,
+            ctas_per_sm, float(tol), int(max_iters), ctypes.byref(h))
+        if rc != 0:
+            raise RuntimeError(f"ElGBBatchedPlanCreate returned {rc}")
+        self.h = h
+
+    @staticmethod
+    def pack(systems, q, device="cuda"):
+        """systems: list of (A, B) numpy arrays -> (ns, A_packed, B_packed)."""
+        ns = [a.shape[0] for a, _ in systems]
+        A = np.concatenate([np.asfortranarray(a).ravel(order="F") for a, _ in systems])
+        B = np.concatenate([np.asfortranarray(b.reshape(b.shape[0], q)).ravel(order="F")
+                            for _, b in systems])
+        return ns, torch.from_numpy(A).to(device), torch.from_numpy(B).to(device)
+
+    def run(self):
+        """Enqueue one replay of the captured launch on the context stream."""
+        self.ctx._bind()
+        rc = self.lib.ElGBBatchedExecute(self.h)
+        if rc != 0:
+            raise RuntimeError(f"ElGBBatchedExecute returned {rc}")
+
+    def results(self):
+        out = (_lib.BatchResult * self.count)()
+        rc = self.lib.ElGBBatchedResults(self.h, out)
+        if rc != 0:
+            raise RuntimeError(f"ElGBBatchedResults returned {rc}")
+        return [dict(iterations=r.iterations, converged=bool(r.converged),
+                     fell_back=bool(r.fell_back), info=r.info,
+                     backward_error=r.backward_error) for r in out]
+
+    def solution(self, i):
+        off = int(np.sum(self.ns[:i].astype(np.int64))) * self.q
+        n = int(self.ns[i])
+        return self.X[off:off + n * self.q].reshape(self.q, n).t().cpu().numpy()
+
+    def flops(self):
+        return float(self.lib.ElGBBatchedFlops(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ElGBBatchedPlanDestroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

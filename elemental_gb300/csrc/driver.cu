@@ -415,7 +415,7 @@ cudaError_t getrf(Context* ctx, int m, int n, T* A, long lda, int* ipiv, int nb,
   if (e != cudaSuccess) return e;
   if (m == 0 || n == 0) return cudaSuccess;
   const bool tc = sizeof(T) == 4 && tc_kind >= 0;
-  const bool la = use_lookahead(m, n, nb) && ctx->side_stream;
+  const bool la = use_lookahead(m, n, nb) && ctx->side_stream && ctx->opt_lookahead;
   const size_t tcb = tc ? tc_gemm_workspace_bytes(tc_kind, m, std::max(n, nb), nb) : 0;
   const size_t tcs = (tc && la) ? tc_gemm_workspace_bytes(tc_kind, m, nb, nb) : 0;
   e = ctx->ensure(getrf_scratch_bytes<T>(ctx, nb) + align256(tcb) + align256(tcs));
@@ -442,6 +442,7 @@ cudaError_t getrf(Context* ctx, int m, int n, T* A, long lda, int* ipiv, int nb,
     int g = std::max((m + 1023) / 1024, (m + rows_cap - 1) / rows_cap);
     s.panel_ctas = std::max(1, std::min(g, ctx->num_sms));
   }
+  if (ctx->opt_panel_ctas > 0) s.panel_ctas = std::min(ctx->opt_panel_ctas, ctx->num_sms);
   s.A = A;
   s.lda = lda;
   s.m = m;
@@ -851,6 +852,21 @@ int ElGBProfileTag(ElGBContext ctx, int tag, long long* launches, double* ms, do
   if (flops) *flops = g.flops;
   if (bytes) *bytes = g.bytes;
   return 0;
+}
+
+int ElGBSetOption(ElGBContext ctx, int option, int value) {
+  if (!ctx) return elgb::kElArgError;
+  switch (option) {
+    case ELGB_OPT_LOOKAHEAD:
+      ctx->opt_lookahead = value ? 1 : 0;
+      return 0;
+    case ELGB_OPT_PANEL_CTAS:
+      if (value < 0) return elgb::kElArgError;
+      ctx->opt_panel_ctas = value;
+      return 0;
+    default:
+      return elgb::kElArgError;
+  }
 }
 
 int ElGBBlocksize(void) { return elgb::get_blocksize(); }

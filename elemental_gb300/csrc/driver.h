@@ -33,6 +33,8 @@ struct Context {
   DevStatus* status = nullptr;    // device status word of the last call
   DevStatus* h_status = nullptr;  // pinned host mirror
   long long launches = 0;         // kernels enqueued by this context
+  int opt_lookahead = 1;          // ElGBSetOption(ELGB_OPT_LOOKAHEAD)
+  int opt_panel_ctas = 0;         // ElGBSetOption(ELGB_OPT_PANEL_CTAS), 0 = automatic
   void* arena2 = nullptr;  // second arena for drivers that call the ones above
   size_t arena2_bytes = 0;
 

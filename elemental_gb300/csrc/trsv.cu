@@ -71,16 +71,24 @@ trtri_diag_kernel(const T* __restrict__ A, long lda, int n, int lower, int unit,
   }
 }
 
+// Thread t owns row r = t % 64 of its block row and the k-slice
+// [16 g, 16 g + 16) of every 64 x 64 tile (g = t / 64), with all q columns
+// in registers; the four slices are summed once at the end.  The A tile of
+// the next dependency is loaded before waiting for its flag, and the block
+// row's inverted diagonal block sits in shared memory from the start, so a
+// link of the dependency chain is: flag -> X_j tile -> 256 FMAs -> done.
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
 trsv_persistent_kernel(const T* __restrict__ A, long lda, const T* __restrict__ Dinv,
                        T* __restrict__ X, long ldx, int n, int q, int lower,
                        unsigned* __restrict__ ticket, int* __restrict__ flags, int epoch,
                        DevStatus* st) {
-  __shared__ T xs[kB][kQ + 1];
+  __shared__ T sD[kB * kB];
+  __shared__ T xs[2][kB][kQ + 1];
+  __shared__ T red[4][kB][kQ + 1];
   __shared__ int s_blk, s_abort;
   const int nblk = (n + kB - 1) / kB;
-  const int tid = threadIdx.x, r = tid & (kB - 1), cg = tid >> 6;  // 4 groups x 4 columns
+  const int tid = threadIdx.x, r = tid & (kB - 1), g = tid >> 6;
   while (true) {
     __syncthreads();
     if (tid == 0) {
@@ -92,15 +100,24 @@ trsv_persistent_kernel(const T* __restrict__ A, long lda, const T* __restrict__ 
     if (t >= nblk) break;
     const int bi = lower ? t : nblk - 1 - t;
     const int i0 = bi * kB, nbi = min(kB, n - i0);
-    T acc[4];
+    for (int idx = tid; idx < kB * kB; idx += blockDim.x) sD[idx] = Dinv[(long)bi * kB * kB + idx];
+    T acc[kQ];
 #pragma unroll
-    for (int c4 = 0; c4 < 4; ++c4) {
-      const int c = cg * 4 + c4;
-      acc[c4] = (r < nbi && c < q) ? X[(i0 + r) + (long)c * ldx] : T(0);
-    }
+    for (int c = 0; c < kQ; ++c) acc[c] = T(0);
+    T a[16];
+    auto load_tile = [&](int s) {
+      const int bj = lower ? s : nblk - 1 - s;
+      const int j0 = bj * kB, nbj = min(kB, n - j0);
+      const T* ap = A + (i0 + r) + (long)(j0 + 16 * g) * lda;
+#pragma unroll
+      for (int u = 0; u < 16; ++u)
+        a[u] = (r < nbi && 16 * g + u < nbj) ? ap[(long)u * lda] : T(0);
+    };
+    if (t > 0) load_tile(0);
     for (int s = 0; s < t; ++s) {
       const int bj = lower ? s : nblk - 1 - s;
       const int j0 = bj * kB, nbj = min(kB, n - j0);
+      const int buf = s & 1;
       if (tid == 0) {
         if (ld_acquire_gpu_s32(flags + bj) != epoch) {
           const unsigned long long t0 = globaltimer_ns();
@@ -122,34 +139,40 @@ trsv_persistent_kernel(const T* __restrict__ A, long lda, const T* __restrict__ 
       if (s_abort) break;
       for (int idx = tid; idx < kB * kQ; idx += blockDim.x) {
         const int rr = idx % kB, cc = idx / kB;
-        xs[rr][cc] = (rr < nbj && cc < q) ? __ldcg(X + (j0 + rr) + (long)cc * ldx) : T(0);
+        xs[buf][rr][cc] = (rr < nbj && cc < q) ? __ldcg(X + (j0 + rr) + (long)cc * ldx) : T(0);
       }
       __syncthreads();
-      if (r < nbi) {
-        const T* ap = A + (i0 + r) + (long)j0 * lda;
-        for (int kk = 0; kk < nbj; ++kk) {
-          const T a = ap[(long)kk * lda];
+      T cur[16];
 #pragma unroll
-          for (int c4 = 0; c4 < 4; ++c4) acc[c4] = fma(-a, xs[kk][cg * 4 + c4], acc[c4]);
-        }
+      for (int u = 0; u < 16; ++u) cur[u] = a[u];
+      if (s + 1 < t) load_tile(s + 1);  // next tile in flight during the FMAs
+#pragma unroll
+      for (int u = 0; u < 16; ++u) {
+        const T av = cur[u];
+#pragma unroll
+        for (int c = 0; c < kQ; ++c) acc[c] = fma(-av, xs[buf][16 * g + u][c], acc[c]);
       }
-      __syncthreads();
     }
     if (s_abort) break;
-    // X_bi = inv(D_bi) * acc
+    // sum the four k-slices, add the right-hand side, apply inv(D_bi)
 #pragma unroll
-    for (int c4 = 0; c4 < 4; ++c4) xs[r][cg * 4 + c4] = acc[c4];
+    for (int c = 0; c < kQ; ++c) red[g][r][c] = acc[c];
+    __syncthreads();
+    for (int idx = tid; idx < kB * kQ; idx += blockDim.x) {
+      const int rr = idx % kB, cc = idx / kB;
+      const T b = (rr < nbi && cc < q) ? X[(i0 + rr) + (long)cc * ldx] : T(0);
+      xs[0][rr][cc] = b + red[0][rr][cc] + red[1][rr][cc] + red[2][rr][cc] + red[3][rr][cc];
+    }
     __syncthreads();
     T out[4] = {T(0), T(0), T(0), T(0)};
-    const T* dp = Dinv + (long)bi * kB * kB + r;
     for (int kk = 0; kk < kB; ++kk) {
-      const T d = dp[kk * kB];
+      const T d = sD[r + kk * kB];
 #pragma unroll
-      for (int c4 = 0; c4 < 4; ++c4) out[c4] = fma(d, xs[kk][cg * 4 + c4], out[c4]);
+      for (int c4 = 0; c4 < 4; ++c4) out[c4] = fma(d, xs[0][kk][g * 4 + c4], out[c4]);
     }
 #pragma unroll
     for (int c4 = 0; c4 < 4; ++c4) {
-      const int c = cg * 4 + c4;
+      const int c = g * 4 + c4;
       if (r < nbi && c < q) X[(i0 + r) + (long)c * ldx] = out[c4];
     }
     __threadfence();
@@ -189,13 +212,8 @@ cudaError_t launch_trsv_persistent(const T* A, long lda, const T* Dinv, T* X, lo
 
 template cudaError_t launch_trtri_diag<float>(const float*, long, int, bool, bool, float*,
                                               cudaStream_t);
-template cudaError_t launch_trtri_diag<double>(const double*, long, int, bool, bool, double*,
-                                               cudaStream_t);
 template cudaError_t launch_trsv_persistent<float>(const float*, long, const float*, float*, long,
                                                    int, int, bool, unsigned*, int*, int,
                                                    DevStatus*, int, cudaStream_t);
-template cudaError_t launch_trsv_persistent<double>(const double*, long, const double*, double*,
-                                                    long, int, int, bool, unsigned*, int*, int,
-                                                    DevStatus*, int, cudaStream_t);
 
 }  // namespace elgb

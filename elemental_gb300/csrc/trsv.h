@@ -1,4 +1,5 @@
-// One-launch blocked triangular solves (trsv.cu).
+// One-launch blocked triangular solves (trsv.cu); instantiated for float
+// (the refinement loop's low-precision factors).
 #pragma once
 
 #include <cuda_runtime.h>

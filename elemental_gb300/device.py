@@ -108,6 +108,11 @@ class Context:
             raise (NonHPDMatrixError if cholesky else SingularMatrixError)(
                 f"info = {info}")
 
+    def set_option(self, option, value):
+        """ElGBSetOption: option "lookahead" (0/1) or "panel_ctas" (0 = auto)."""
+        code = {"lookahead": 1, "panel_ctas": 2}[option]
+        self._rc(self.lib.ElGBSetOption(self.h, code, int(value)), "SetOption")
+
     def launches(self):
         return int(self.lib.ElGBLaunchCount(self.h))
 

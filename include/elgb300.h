@@ -45,6 +45,13 @@ int ElGBStatus(ElGBContext ctx, int* info, int* err);
  * (reference src/blas_like/blocksizes.cpp:37-60); default 128. */
 int ElGBBlocksize(void);
 int ElGBSetBlocksize(int nb);
+/* Tuning switches of a context:
+ *   ELGB_OPT_LOOKAHEAD  1 (default): factor the next panel on a second
+ *                       stream while the trailing update runs; 0: in order
+ *   ELGB_OPT_PANEL_CTAS CTAs of a panel launch, 0 (default) = automatic */
+enum { ELGB_OPT_LOOKAHEAD = 1, ELGB_OPT_PANEL_CTAS = 2 };
+int ElGBSetOption(ElGBContext ctx, int option, int value);
+
 /* Number of kernel launches this context has issued so far. */
 long long ElGBLaunchCount(ElGBContext ctx);
 /* Live timing of the dominant kernel (the tensor-core trailing-update GEMM):
@@ -141,6 +148,33 @@ typedef struct {
 int ElGBRefinedSolve_d(ElGBContext ctx, int n, const double* A, int lda,
                        int nrhs, const double* B, int ldb, double* X, int ldx,
                        const ElGBRefineCtrl* ctrl, ElGBRefineInfo* info);
+
+/* Batched uneven-size solves (added form): `count` independent systems
+ * A_i X_i = B_i, packed column-major on the device (A_i n_i x n_i, then the
+ * next; B_i and X_i n_i x nrhs, nrhs <= 8), solved by ONE persistent launch
+ * replayed from a CUDA graph.  kind[i]: 0 LU with partial pivoting (El::LU +
+ * lu::SolveAfter), 1 lower Cholesky (El::Cholesky + cholesky::SolveAfter);
+ * precision[i]: 0 FP64 factors, 1 FP32 factors + FP64 refinement with an
+ * FP64 refactorization on stall (NULL arrays: all LU / all FP32).  nb_table
+ * (8 ints or NULL): panel width per size bucket n <= 32, 64, 128, 256, 512,
+ * 1024, 2048, larger (the autotuner's output).  tol: target backward error
+ * (<= 0: 1e-13).  The plan keeps the device pointers; Execute enqueues the
+ * graph on the context's stream, Results synchronizes and copies one
+ * ElGBBatchResult per system. */
+typedef struct ElGBBatchPlanImpl* ElGBBatchPlan;
+typedef struct {
+  int iterations, converged, fell_back, info;
+  double backward_error;
+} ElGBBatchResult;
+int ElGBBatchedPlanCreate(ElGBContext ctx, int count, const int* n,
+                          const int* kind, const int* precision, int nrhs,
+                          const double* A, const double* B, double* X,
+                          const int* nb_table, int ctas_per_sm, double tol,
+                          int max_iters, ElGBBatchPlan* plan);
+int ElGBBatchedExecute(ElGBBatchPlan plan);
+int ElGBBatchedResults(ElGBBatchPlan plan, ElGBBatchResult* out);
+double ElGBBatchedFlops(ElGBBatchPlan plan);
+int ElGBBatchedPlanDestroy(ElGBBatchPlan plan);
 
 /* lu::SolveAfter(orientation, A, P, B) (reference
  * src/lapack_like/factor/LU/SolveAfter.hpp:66-92): orientation 0 NORMAL,
