@@ -90,6 +90,8 @@ def load():
     _sig(lib, "ElGBBatchedResults", c_int, vp, vp)
     _sig(lib, "ElGBBatchedFlops", c_double, vp)
     _sig(lib, "ElGBBatchedPlanDestroy", c_int, vp)
+    _sig(lib, "ElGBResidualNoAlloc_d", c_int, c_int, c_int, vp, c_int, vp, c_int, vp, c_int, vp,
+         c_int, vp)
     _sig(lib, "ElGBBackwardError_d", c_int, vp, c_int, c_int, vp, c_int, vp, c_int, vp, c_int,
          P(c_double))
     _sig(lib, "ElGBProbeFP64Peak", c_int, vp, P(c_double))

@@ -225,6 +225,22 @@ int ElGBResidual_d(ElGBContext ctx, int n, int nrhs, const double* A,
                    int lda, const double* X, int ldx, const double* B,
                    int ldb, double* R, int ldr);
 
+/* The residual of ElGBResidual_d for callers that cannot allocate device
+ * memory (stream capture without allocation nodes, budgeted or externally
+ * owned device memory).  No counterpart in the reference.  It calls no
+ * cudaMalloc / cudaFree and needs no context: its scratch is a fixed 8 MiB
+ * device array that the library holds on every GPU it is loaded on, so it
+ * accepts only n * min(nrhs, 16) * ceil(n / 4096) <= 1048576 (e.g. n <= 16384
+ * with 16 right-hand sides, n <= 32768 with 4) and returns EL_ARG_ERROR (3)
+ * beyond that, before touching any memory.  Runs on `stream` (a cudaStream_t,
+ * NULL = legacy default stream) of the current device.  The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress); make
+ * that first call before any stream capture.  All calls share the array:
+ * calls that overlap on the GPU race on it, calls on one stream do not. */
+int ElGBResidualNoAlloc_d(int n, int nrhs, const double* A, int lda,
+                          const double* X, int ldx, const double* B, int ldb,
+                          double* R, int ldr, void* stream);
+
 /* Normwise backward error max_j ||b_j - A x_j||_2 /
  * (||A||_F ||x_j||_2 + ||b_j||_2), computed in FP64 on the device;
  * synchronizes and writes the value to *berr (host). */
