@@ -84,6 +84,11 @@ def load():
          P(RefineCtrl), P(RefineInfo))
     _sig(lib, "ElGBResidual_d", c_int, vp, c_int, c_int, vp, c_int, vp, c_int, vp, c_int, vp,
          c_int)
+    _sig(lib, "ElGBMLPParamCount", c_int)
+    _sig(lib, "ElGBMLPForward", c_int, vp, vp, vp, c_int, vp, vp)
+    _sig(lib, "ElGBMLPGradient", c_int, vp, vp, vp, vp, c_int, vp, P(ctypes.c_float))
+    _sig(lib, "ElGBMLPAdamStep", c_int, vp, vp, vp, vp, vp, ctypes.c_float, ctypes.c_float,
+         ctypes.c_float, ctypes.c_float, ctypes.c_float, c_int)
     _sig(lib, "ElGBBatchedPlanCreate", c_int, vp, c_int, vp, vp, vp, c_int, vp, vp, vp, vp,
          c_int, c_double, c_int, P(vp))
     _sig(lib, "ElGBBatchedExecute", c_int, vp)

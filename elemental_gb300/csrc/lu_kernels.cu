@@ -94,6 +94,7 @@ getf2_panel_kernel(PanelParams<T> p) {
   __shared__ int s_rr[33];
   __shared__ T s_gv[kPanelThreads];
   __shared__ int s_gr[kPanelThreads];
+  T* s_rows = slab + (size_t)p.R * W;  // [G][W] candidate rows (dynamic smem)
   __shared__ int s_piv, s_abort;
 
   const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x;
@@ -136,7 +137,9 @@ getf2_panel_kernel(PanelParams<T> p) {
       __threadfence();
       st_release_s32(&my->epoch, epoch);
     }
-    // 2. the barrier: every slot carries this epoch
+    // 2. the barrier: every slot carries this epoch.  The thread that polled
+    // slot g copies g's candidate row (and, for the owner of row j, row j)
+    // right away, so the winner's row is already on chip after the barrier.
     if (tid < G) {
       const PanelSlot<T>* sl = p.s.slots + (long)par * maxG + tid;
       if (ld_acquire_s32(&sl->epoch) != epoch) {
@@ -150,8 +153,13 @@ getf2_panel_kernel(PanelParams<T> p) {
           }
         }
       }
+      const int gr = __ldcg(&sl->row);
       s_gv[tid] = __ldcg(&sl->val);
-      s_gr[tid] = __ldcg(&sl->row);
+      s_gr[tid] = gr;
+      if (gr >= 0)
+        for (int c = 0; c < w; ++c) s_rows[tid * W + c] = __ldcg(&sl->cand[c]);
+      if (tid == j / R)
+        for (int c = 0; c < w; ++c) s_d[c] = __ldcg(&sl->diag[c]);
     }
     __syncthreads();
     if (s_abort) return;
@@ -170,12 +178,7 @@ getf2_panel_kernel(PanelParams<T> p) {
     }
     __syncthreads();
     const int piv = s_piv;
-    if (tid < w) {
-      const PanelSlot<T>* own = p.s.slots + (long)par * maxG + j / R;
-      const T d = __ldcg(&own->diag[tid]);
-      s_d[tid] = d;
-      s_u[tid] = (piv == j) ? d : __ldcg(&p.s.slots[(long)par * maxG + piv / R].cand[tid]);
-    }
+    if (tid < w) s_u[tid] = (piv == j) ? s_d[tid] : s_rows[(piv / R) * W + tid];
     __syncthreads();
     // 4. swap, scale, update, next candidate
     if (b == 0 && tid == 0) p.ipiv[j] = p.row_base + piv;
@@ -227,7 +230,7 @@ cudaError_t launch_getf2_panel(T* A, long lda, int mp, int w, int* ipiv, int row
   if (G < 1) G = 1;
   int R = ceil_div(mp, G);
   G = ceil_div(mp, R);  // no CTA without rows
-  size_t smem = (size_t)R * kPanelW * sizeof(T);
+  size_t smem = ((size_t)R + G) * kPanelW * sizeof(T);  // slab + candidate rows
   if (smem > (size_t)kMaxSmem) return cudaErrorInvalidValue;
   auto kern = getf2_panel_kernel<T, kPanelW>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -367,8 +370,10 @@ apply_swap_pairs_kernel(T* __restrict__ A, long lda, int c0a, int c1a, int c0b, 
   for (int q = gw; q < ncols; q += nw) {
     const int col = q < na ? c0a + q : c0b + (q - na);
     T* colp = A + (long)col * lda;
+#pragma unroll 8
     for (int e = lane; e < cnt; e += 32) wbuf[e] = colp[s_src[e]];
     __syncwarp();
+#pragma unroll 8
     for (int e = lane; e < cnt; e += 32) colp[s_dst[e]] = wbuf[e];
     __syncwarp();
   }

@@ -176,6 +176,23 @@ int ElGBBatchedResults(ElGBBatchPlan plan, ElGBBatchResult* out);
 double ElGBBatchedFlops(ElGBBatchPlan plan);
 int ElGBBatchedPlanDestroy(ElGBBatchPlan plan);
 
+/* Learned precision selector (added form): a 16 -> 64 -> 64 -> 3 FP32 MLP
+ * (ReLU, softmax cross-entropy; classes 0 FP64, 1 FP32, 2 BF16) with
+ * hand-written kernels.  Parameters are one flat FP32 device vector of
+ * ElGBMLPParamCount() entries: W1[16][64] b1[64] W2[64][64] b2[64] W3[64][3]
+ * b3[3] (row-major, input x output).  X is B x 16 row-major (device).
+ * Forward: probs (B x 3) and/or argmax (B) may be NULL.  Gradient: the mean
+ * cross-entropy gradient into grad (deterministic order), loss (host, may
+ * be NULL; synchronizes when given).  AdamStep: one Adam update (step >= 1). */
+int ElGBMLPParamCount(void);
+int ElGBMLPForward(ElGBContext ctx, const float* params, const float* X, int B,
+                   float* probs, int* argmax);
+int ElGBMLPGradient(ElGBContext ctx, const float* params, const float* X,
+                    const int* labels, int B, float* grad, float* loss);
+int ElGBMLPAdamStep(ElGBContext ctx, float* params, const float* grad, float* m,
+                    float* v, float lr, float beta1, float beta2, float eps,
+                    float weight_decay, int step);
+
 /* lu::SolveAfter(orientation, A, P, B) (reference
  * src/lapack_like/factor/LU/SolveAfter.hpp:66-92): orientation 0 NORMAL,
  * 1 TRANSPOSE, 2 ADJOINT (= TRANSPOSE for real data).  B is n x nrhs. */
