@@ -37,6 +37,13 @@ class BatchResult(ctypes.Structure):
                 ("info", c_int), ("backward_error", c_double)]
 
 
+class BatchOptions(ctypes.Structure):
+    """ElGBBatchOptions (include/elgb300.h)."""
+    _fields_ = [("kind", c_void_p), ("precision", c_void_p), ("nb_table", c_void_p),
+                ("ctas_per_sm", c_int), ("tol", c_double), ("max_iters", c_int),
+                ("no_fallback", c_int), ("features_only", c_int), ("features", c_void_p)]
+
+
 def _sig(lib, name, res, *args):
     f = getattr(lib, name)
     f.restype = res
@@ -89,8 +96,8 @@ def load():
     _sig(lib, "ElGBMLPGradient", c_int, vp, vp, vp, vp, c_int, vp, P(ctypes.c_float))
     _sig(lib, "ElGBMLPAdamStep", c_int, vp, vp, vp, vp, vp, ctypes.c_float, ctypes.c_float,
          ctypes.c_float, ctypes.c_float, ctypes.c_float, c_int)
-    _sig(lib, "ElGBBatchedPlanCreate", c_int, vp, c_int, vp, vp, vp, c_int, vp, vp, vp, vp,
-         c_int, c_double, c_int, P(vp))
+    _sig(lib, "ElGBBatchedPlanCreate", c_int, vp, c_int, vp, c_int, vp, vp, vp,
+         P(BatchOptions), P(vp))
     _sig(lib, "ElGBBatchedExecute", c_int, vp)
     _sig(lib, "ElGBBatchedResults", c_int, vp, vp)
     _sig(lib, "ElGBBatchedFlops", c_double, vp)

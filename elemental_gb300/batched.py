@@ -12,7 +12,7 @@ from . import _lib
 from .device import Context, context
 
 KIND = {"lu": 0, "chol": 1}
-PREC = {"fp64": 0, "fp32": 1}
+PREC = {"fp64": 0, "fp32": 1, "bf16": 2}
 
 
 class BatchedSolver:
@@ -24,7 +24,8 @@ class BatchedSolver:
     """
 
     def __init__(self, ns, q, A_packed, B_packed, kinds=None, precisions=None, nb_table=None,
-                 ctas_per_sm=1, tol=1e-13, max_iters=10, ctx: Context | None = None):
+                 ctas_per_sm=1, tol=1e-13, max_iters=10, fallback=True, features_only=False,
+                 ctx: Context | None = None):
         self.ctx = ctx or context()
         self.lib = _lib.load()
         self.ns = np.ascontiguousarray(ns, dtype=np.int32)
@@ -33,6 +34,8 @@ class BatchedSolver:
         self.A = A_packed
         self.B = B_packed
         self.X = torch.empty_like(B_packed)
+        self.features = (torch.empty(len(ns), 16, dtype=torch.float32, device=A_packed.device)
+                         if features_only else None)
         k = np.ascontiguousarray([KIND[x] for x in kinds] if kinds is not None
                                  else np.zeros(self.count), dtype=np.int32)
         pr = np.ascontiguousarray([PREC[x] for x in precisions] if precisions is not None
@@ -43,11 +46,15 @@ class BatchedSolver:
             nbt = np.ascontiguousarray(nb_table, dtype=np.int32)
         h = ctypes.c_void_p()
         vp = ctypes.c_void_p
+        opt = _lib.BatchOptions(
+            k.ctypes.data_as(vp).value, pr.ctypes.data_as(vp).value,
+            nbt.ctypes.data_as(vp).value if nbt is not None else None, int(ctas_per_sm),
+            float(tol), int(max_iters), 0 if fallback else 1, 1 if features_only else 0,
+            self.features.data_ptr() if features_only else None)
+        self._keep = (k, pr, nbt)
         rc = self.lib.ElGBBatchedPlanCreate(
-            self.ctx.h, self.count, self.ns.ctypes.data_as(vp), k.ctypes.data_as(vp),
-            pr.ctypes.data_as(vp), q, vp(self.A.data_ptr()), vp(self.B.data_ptr()),
-            vp(self.X.data_ptr()), nbt.ctypes.data_as(vp) if nbt is not None else None,
-            ctas_per_sm, float(tol), int(max_iters), ctypes.byref(h))
+            self.ctx.h, self.count, self.ns.ctypes.data_as(vp), q, vp(self.A.data_ptr()),
+            vp(self.B.data_ptr()), vp(self.X.data_ptr()), ctypes.byref(opt), ctypes.byref(h))
         if rc != 0:
             raise RuntimeError(f"ElGBBatchedPlanCreate returned {rc}")
         self.h = h

@@ -19,6 +19,7 @@
 // staged in shared memory, the trailing update is register-tiled FMA with
 // both operands staged in shared memory.  nb is per system (autotuned per
 // size bucket, capped so the panel fits in shared memory).
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -57,6 +58,13 @@ struct Shared {
 
 template <typename T>
 __device__ __forceinline__ T tabs(T x) { return x < T(0) ? -x : x; }
+
+// Operand rounding of the BF16 factorization: products of BF16-rounded
+// operands accumulated in FP32 (what a BF16 tensor-core update computes).
+__device__ __forceinline__ float rnd(float x, bool lowp) {
+  return lowp ? __bfloat162float(__float2bfloat16_rn(x)) : x;
+}
+__device__ __forceinline__ double rnd(double x, bool) { return x; }
 
 // ---- block reductions ------------------------------------------------------
 __device__ __forceinline__ void block_argmax_abs(float& v, int& r, Shared& sh, float* fv,
@@ -213,14 +221,14 @@ __device__ void cta_apply_swaps(T* W, int n, int ld, int k, int jb, Shared& sh, 
 template <typename T>
 __device__ void cta_gemm_update(const T* P, int ldp, const T* Q, int ldq, T* C, int ldc, int m,
                                 int nc, int jb, T* qs, bool lower_only, int row_base,
-                                int col_base) {
+                                int col_base, bool lowp) {
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
   for (int c0 = 0; c0 < nc; c0 += 64) {
     const int cw = min(64, nc - c0);
     __syncthreads();
     for (int idx = threadIdx.x; idx < jb * 64; idx += kBT) {
       const int kk = idx % jb, cc = idx / jb;
-      qs[kk + cc * jb] = cc < cw ? Q[kk + (long)(c0 + cc) * ldq] : T(0);
+      qs[kk + cc * jb] = cc < cw ? rnd(Q[kk + (long)(c0 + cc) * ldq], lowp) : T(0);
     }
     __syncthreads();
     for (int r0 = 0; r0 < m; r0 += 64) {
@@ -235,7 +243,7 @@ __device__ void cta_gemm_update(const T* P, int ldp, const T* Q, int ldq, T* C, 
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
           const int r = r0 + tx + 16 * i;
-          a[i] = r < m ? P[r + kk * ldp] : T(0);
+          a[i] = r < m ? rnd(P[r + kk * ldp], lowp) : T(0);
         }
 #pragma unroll
         for (int j = 0; j < 4; ++j) b[j] = qs[kk + (ty + 16 * j) * jb];
@@ -267,7 +275,7 @@ __device__ void cta_gemm_update(const T* P, int ldp, const T* Q, int ldq, T* C, 
 // the first zero pivot).
 template <typename T>
 __device__ int cta_lu(T* W, int n, int ld, int nb, int* piv_out, Shared& sh, T* smem,
-                      int smem_elems) {
+                      int smem_elems, bool lowp) {
   __shared__ T fv[9];
   __shared__ int fr[9];
   int info = 0;
@@ -308,7 +316,9 @@ __device__ int cta_lu(T* W, int n, int ld, int nb, int* piv_out, Shared& sh, T* 
         for (int r = j + 1 + threadIdx.x; r < mp; r += kBT) {
           const T l = panel[r + j * mp] * inv;
           panel[r + j * mp] = l;
-          for (int c = j + 1; c < jb; ++c) panel[r + c * mp] = fma(-l, panel[j + c * mp], panel[r + c * mp]);
+          const T lr = rnd(l, lowp);
+          for (int c = j + 1; c < jb; ++c)
+            panel[r + c * mp] = fma(-lr, rnd(panel[j + c * mp], lowp), panel[r + c * mp]);
         }
       }
       __syncthreads();
@@ -328,7 +338,7 @@ __device__ int cta_lu(T* W, int n, int ld, int nb, int* piv_out, Shared& sh, T* 
         T* col = W + k + (long)(k + jb + c) * ld;
         for (int i = 1; i < jb; ++i) {
           T s = col[i];
-          for (int l = 0; l < i; ++l) s = fma(-panel[i + l * mp], col[l], s);
+          for (int l = 0; l < i; ++l) s = fma(-rnd(panel[i + l * mp], lowp), rnd(col[l], lowp), s);
           col[i] = s;
         }
       }
@@ -336,7 +346,7 @@ __device__ int cta_lu(T* W, int n, int ld, int nb, int* piv_out, Shared& sh, T* 
       // A22 -= A21 U12, A21 = panel rows jb.. (still in shared memory)
       cta_gemm_update<T>(panel + jb, mp, W + k + (long)(k + jb) * ld, ld,
                          W + (k + jb) + (long)(k + jb) * ld, ld, n2, n2, jb,
-                         smem + mp * jb, false, 0, 0);
+                         smem + mp * jb, false, 0, 0, lowp);
     }
     __syncthreads();
   }
@@ -345,7 +355,7 @@ __device__ int cta_lu(T* W, int n, int ld, int nb, int* piv_out, Shared& sh, T* 
 
 // In-CTA lower Cholesky of W; returns info (j+1 at the first non-positive pivot).
 template <typename T>
-__device__ int cta_chol(T* W, int n, int ld, int nb, T* smem) {
+__device__ int cta_chol(T* W, int n, int ld, int nb, T* smem, bool lowp) {
   __shared__ int s_bad;
   if (threadIdx.x == 0) s_bad = 0;
   __syncthreads();
@@ -373,9 +383,9 @@ __device__ int cta_chol(T* W, int n, int ld, int nb, T* smem) {
       __syncthreads();
       // rank-1 update of the panel's trailing columns (rows >= column)
       for (int r = j + 1 + threadIdx.x; r < mp; r += kBT) {
-        const T l = panel[r + j * mp];
+        const T l = rnd(panel[r + j * mp], lowp);
         for (int c = j + 1; c < jb && c <= r; ++c)
-          panel[r + c * mp] = fma(-l, panel[c + j * mp], panel[r + c * mp]);
+          panel[r + c * mp] = fma(-l, rnd(panel[c + j * mp], lowp), panel[r + c * mp]);
       }
       __syncthreads();
     }
@@ -404,12 +414,12 @@ __device__ int cta_chol(T* W, int n, int ld, int nb, T* smem) {
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
               const int r = r0 + tx + 16 * i;
-              av[i] = r < n2 ? panel[jb + r + kk * mp] : T(0);
+              av[i] = r < n2 ? rnd(panel[jb + r + kk * mp], lowp) : T(0);
             }
 #pragma unroll
             for (int jj = 0; jj < 4; ++jj) {
               const int cc = c0 + ty + 16 * jj;
-              bv[jj] = cc < n2 ? panel[jb + cc + kk * mp] : T(0);
+              bv[jj] = cc < n2 ? rnd(panel[jb + cc + kk * mp], lowp) : T(0);
             }
 #pragma unroll
             for (int i = 0; i < 4; ++i)
@@ -564,6 +574,9 @@ struct BatchParams {
   int max_iters;
   unsigned* ticket;
   BatchResult* out;
+  int mode;          // 0 solve, 1 features only
+  int fallback;      // FP64 refactorization when refinement does not converge
+  float* feat;       // mode 1: count x 16 features
 };
 
 __device__ double sys_berr(const double* A, int n, const double* X, const double* B, double* R,
@@ -605,11 +618,235 @@ __device__ double sys_berr(const double* A, int n, const double* X, const double
   return worst;
 }
 
+// x := (L U)^{-T} x for one vector: U^T (lower, diag u_jj) forward, then
+// L^T (upper; unit diagonal for LU, l_jj for Cholesky) backward, both read
+// transposed from W.
+template <typename T>
+__device__ void cta_solve_t(const T* W, int n, int ld, bool unit_lower, T* x) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int j0 = 0; j0 < n; j0 += 32) {
+    const int jb = min(32, n - j0);
+    if (warp == 0) {
+      T v = lane < jb ? x[j0 + lane] : T(0);
+      for (int jj = 0; jj < jb; ++jj) {
+        if (lane == jj) v = v / W[(j0 + jj) + (long)(j0 + jj) * ld];
+        const T xj = __shfl_sync(0xffffffffu, v, jj);
+        if (lane > jj && lane < jb) v = fma(-W[(j0 + jj) + (long)(j0 + lane) * ld], xj, v);
+      }
+      if (lane < jb) x[j0 + lane] = v;
+    }
+    __syncthreads();
+    for (int r = j0 + jb + threadIdx.x; r < n; r += kBT) {
+      T acc = x[r];
+      for (int jj = 0; jj < jb; ++jj) acc = fma(-W[(j0 + jj) + (long)r * ld], x[j0 + jj], acc);
+      x[r] = acc;
+    }
+    __syncthreads();
+  }
+  for (int j0 = ((n - 1) / 32) * 32; j0 >= 0; j0 -= 32) {
+    const int jb = min(32, n - j0);
+    if (warp == 0) {
+      T v = lane < jb ? x[j0 + lane] : T(0);
+      for (int jj = jb - 1; jj >= 0; --jj) {
+        if (!unit_lower && lane == jj) v = v / W[(j0 + jj) + (long)(j0 + jj) * ld];
+        const T xj = __shfl_sync(0xffffffffu, v, jj);
+        if (lane < jj) v = fma(-W[(j0 + jj) + (long)(j0 + lane) * ld], xj, v);
+      }
+      if (lane < jb) x[j0 + lane] = v;
+    }
+    __syncthreads();
+    for (int r = threadIdx.x; r < j0; r += kBT) {
+      T acc = x[r];
+      for (int jj = 0; jj < jb; ++jj) acc = fma(-W[(j0 + jj) + (long)r * ld], x[j0 + jj], acc);
+      x[r] = acc;
+    }
+    __syncthreads();
+  }
+}
+
+// Block-wide sum and max of f(i), i < n (double).
+template <typename F>
+__device__ void block_sum_max(int n, F f, Shared& sh, double* out_sum, double* out_max) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  double sm = 0.0, mx = 0.0;
+  for (int i = threadIdx.x; i < n; i += kBT) {
+    const double v = f(i);
+    sm += v;
+    mx = fmax(mx, v);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    sm += __shfl_xor_sync(0xffffffffu, sm, o);
+    mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  }
+  if (lane == 0) {
+    sh.red[warp][0] = sm;
+    sh.red[warp][1] = mx;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int w = 0; w < kBT / 32; ++w) {
+      a += sh.red[w][0];
+      b = fmax(b, sh.red[w][1]);
+    }
+    sh.colv[0] = a;
+    sh.colv[1] = b;
+  }
+  __syncthreads();
+  *out_sum = sh.colv[0];
+  *out_max = sh.colv[1];
+  __syncthreads();
+}
+
 template <typename T>
 __device__ int factor_sys(T* W, int n, int kind, int nb, int* piv, Shared& sh, T* smem,
-                          int smem_elems) {
-  return kind == 0 ? cta_lu<T>(W, n, n, nb, piv, sh, smem, smem_elems)
-                   : cta_chol<T>(W, n, n, nb, smem);
+                          int smem_elems, bool lowp) {
+  return kind == 0 ? cta_lu<T>(W, n, n, nb, piv, sh, smem, smem_elems, lowp)
+                   : cta_chol<T>(W, n, n, nb, smem, lowp);
+}
+
+// The selector's 16 features of one system (written to p.feat[s * 16 ..]):
+// norm ratios of A, an FP32 LU's growth and pivot spread, and a Hager /
+// Higham 1-norm estimate of ||A^{-1}||_1 (LAPACK xLACON's iteration plus
+// Higham's alternating vector) computed with that FP32 LU.
+__device__ void compute_features(const BatchParams& p, const SysDesc& d, int s, const double* A,
+                                 int n, double nA, float* Wf, int* piv, int* perm, float* v,
+                                 Shared& sh, float* smf) {
+  __shared__ float s_fv[16];
+  double sum, mx, colmax = 0.0, rowmax = 0.0, amax = 0.0, dsum = 0.0;
+  // column sums (||A||_1), row sums (||A||_inf), max |a|, diagonal weight
+  block_sum_max(n, [&](int j) {
+    double c = 0.0;
+    for (int i = 0; i < n; ++i) c += fabs(A[i + (long)j * n]);
+    return c;
+  }, sh, &sum, &colmax);
+  block_sum_max(n, [&](int i) {
+    double r = 0.0;
+    for (int j = 0; j < n; ++j) r += fabs(A[i + (long)j * n]);
+    return r;
+  }, sh, &sum, &rowmax);
+  block_sum_max(n, [&](int j) {
+    double m = 0.0;
+    for (int i = 0; i < n; ++i) m = fmax(m, fabs(A[i + (long)j * n]));
+    return m;
+  }, sh, &sum, &amax);
+  block_sum_max(n, [&](int i) { return fabs(A[i + (long)i * n]); }, sh, &dsum, &mx);
+  // FP32 factorization
+  for (long i = threadIdx.x; i < (long)n * n; i += kBT) Wf[i] = (float)A[i];
+  __syncthreads();
+  const int info = factor_sys<float>(Wf, n, d.kind, d.nb, piv, sh, smf,
+                                     kSmemPanel / (int)sizeof(float), false);
+  double umax = 0.0, dmin = 0.0, dmax = 0.0;
+  block_sum_max(n, [&](int j) {
+    double m = 0.0;
+    const int top = d.kind == 0 ? j : n - 1;  // U (LU) or L (Cholesky) column j
+    const int i0 = d.kind == 0 ? 0 : j;
+    for (int i = i0; i <= top; ++i) m = fmax(m, fabs((double)Wf[i + (long)j * n]));
+    return m;
+  }, sh, &sum, &umax);
+  block_sum_max(n, [&](int j) { return fabs((double)Wf[j + (long)j * n]); }, sh, &sum, &dmax);
+  block_sum_max(n, [&](int j) { return 1.0 / fmax(fabs((double)Wf[j + (long)j * n]), 1e-300); },
+                sh, &sum, &dmin);
+  dmin = 1.0 / dmin;
+  double est = 0.0, est2 = 0.0;
+  int iters = 0;
+  if (info == 0) {
+    if (d.kind == 0)
+      cta_perm_from_swaps(piv, n, perm, reinterpret_cast<int*>(smf), kSmemPanel / (int)sizeof(int));
+    else
+      cta_mirror_lower(Wf, n, n);
+    float* y = v;
+    float* z = v + n;
+    // Hager: x = 1/n
+    int jlast = -1;
+    for (int it = 0; it < 5; ++it) {
+      ++iters;
+      for (int i = threadIdx.x; i < n; i += kBT) {
+        const float xi = it == 0 ? 1.f / n : (i == jlast ? 1.f : 0.f);
+        z[i] = xi;
+      }
+      __syncthreads();
+      for (int i = threadIdx.x; i < n; i += kBT) y[i] = z[d.kind == 0 ? perm[i] : i];
+      __syncthreads();
+      cta_solve<float>(Wf, n, n, d.kind == 0, y, 1);  // y = A^{-1} x
+      double ny, dum;
+      block_sum_max(n, [&](int i) { return fabs((double)y[i]); }, sh, &ny, &dum);
+      if (it > 0 && ny <= est) break;
+      est = ny;
+      // z = A^{-T} sign(y)
+      for (int i = threadIdx.x; i < n; i += kBT) z[i] = y[i] >= 0.f ? 1.f : -1.f;
+      __syncthreads();
+      cta_solve_t<float>(Wf, n, n, d.kind == 0, z);
+      if (d.kind == 0) {  // inverse permutation: P^T z
+        for (int i = threadIdx.x; i < n; i += kBT) y[perm[i]] = z[i];
+        __syncthreads();
+        for (int i = threadIdx.x; i < n; i += kBT) z[i] = y[i];
+        __syncthreads();
+      }
+      // j = argmax |z|, and z^T x
+      __shared__ float s_zx;
+      __shared__ int s_j;
+      if (threadIdx.x == 0) {
+        int jb = 0;
+        float zb = -1.f, zx = 0.f;
+        for (int i = 0; i < n; ++i) {
+          const float a = fabsf(z[i]);
+          if (a > zb) {
+            zb = a;
+            jb = i;
+          }
+          zx += z[i] * (it == 0 ? 1.f / n : (i == jlast ? 1.f : 0.f));
+        }
+        s_j = jb;
+        s_zx = (fabsf(z[jb]) <= zx) ? 1.f : 0.f;
+      }
+      __syncthreads();
+      if (it > 0 && s_zx > 0.f) break;
+      if (s_j == jlast) break;
+      jlast = s_j;
+    }
+    // Higham's alternating vector: x_i = (-1)^i (1 + i / (n - 1))
+    for (int i = threadIdx.x; i < n; i += kBT) {
+      const int src = d.kind == 0 ? perm[i] : i;
+      y[i] = (src & 1 ? -1.f : 1.f) * (1.f + (n > 1 ? (float)src / (n - 1) : 0.f));
+    }
+    __syncthreads();
+    cta_solve<float>(Wf, n, n, d.kind == 0, y, 1);
+    double ny, dum;
+    block_sum_max(n, [&](int i) { return fabs((double)y[i]); }, sh, &ny, &dum);
+    est2 = 2.0 * ny / (3.0 * n);
+  }
+  if (threadIdx.x == 0) {
+    const double tiny = 1e-300;
+    const double e = fmax(est, est2);
+    const double fro = fmax(nA, tiny);
+    s_fv[0] = (float)log2((double)n);
+    s_fv[1] = (float)log10(fmax(colmax * e, 1.0));
+    s_fv[2] = (float)log10(fmax(colmax, tiny) / fro);
+    s_fv[3] = (float)log10(fmax(rowmax, tiny) / fro);
+    s_fv[4] = (float)log10(fmax(amax, tiny) / fro);
+    s_fv[5] = (float)log10(fmax(umax, tiny) / fmax(amax, tiny));
+    s_fv[6] = (float)log10(fmax(dmin, tiny) / fmax(dmax, tiny));
+    s_fv[7] = (float)log10(fmax(dsum / (n * fmax(amax, tiny)), 1e-30));
+    s_fv[8] = (float)d.kind;
+    s_fv[9] = (float)log10(fro);
+    s_fv[10] = (float)log10(fmax(e, tiny));
+    s_fv[11] = (float)log10(fmax(dmin, tiny));
+    s_fv[12] = (float)log10(fmax(dmax, tiny));
+    s_fv[13] = (float)iters;
+    s_fv[14] = info != 0 ? 1.f : 0.f;
+    s_fv[15] = (float)log10(fmax(est2, tiny) / fmax(est, tiny));
+    for (int k = 0; k < 16; ++k) {
+      float f = s_fv[k];
+      if (!(f == f) || f > 1e30f || f < -1e30f) f = 0.f;  // keep features finite
+      p.feat[(long)s * 16 + k] = f;
+    }
+    BatchResult r{};
+    r.info = info;
+    r.berr = colmax * fmax(est, est2);  // the kappa_1 estimate
+    p.out[s] = r;
+  }
+  __syncthreads();
 }
 
 __global__ void __launch_bounds__(kBT)
@@ -656,13 +893,18 @@ batched_solve_kernel(BatchParams p) {
     }
     const double nA = s_na;
     bool done = false;
-    if (d.prec == 1) {
-      // FP32 factors + FP64 refinement
+    if (p.mode == 1) {
+      compute_features(p, d, s, A, n, nA, Wf, piv, perm, reinterpret_cast<float*>(V), sh,
+                       reinterpret_cast<float*>(smem_raw));
+      continue;
+    }
+    if (d.prec >= 1) {
+      // FP32 factors (BF16 operand products for prec 2) + FP64 refinement
       float* smf = reinterpret_cast<float*>(smem_raw);
       for (long i = threadIdx.x; i < (long)n * n; i += kBT) Wf[i] = (float)A[i];
       __syncthreads();
       const int info = factor_sys<float>(Wf, n, d.kind, d.nb, piv, sh, smf,
-                                         kSmemPanel / (int)sizeof(float));
+                                         kSmemPanel / (int)sizeof(float), d.prec == 2);
       res.info = info;
       if (info == 0) {
         if (d.kind == 0)
@@ -695,15 +937,15 @@ batched_solve_kernel(BatchParams p) {
         }
       }
     }
-    if (!done) {
+    if (!done && (p.fallback || d.prec == 0)) {
       // FP64 factors: the plain path, or the fallback
-      res.fell_back = d.prec == 1 ? 1 : 0;
+      res.fell_back = d.prec >= 1 ? 1 : 0;
       double* smd = reinterpret_cast<double*>(smem_raw);
       for (long i = threadIdx.x; i < (long)n * n; i += kBT) Wd[i] = A[i];
       __syncthreads();
       const int nb64 = max(1, min(d.nb, (kSmemPanel / 8 - 64 * 64) / max(n, 1)));
       const int info = factor_sys<double>(Wd, n, d.kind, nb64, piv, sh, smd,
-                                          kSmemPanel / (int)sizeof(double));
+                                          kSmemPanel / (int)sizeof(double), false);
       res.info = info;
       if (info == 0) {
         if (d.kind == 0)
@@ -762,7 +1004,7 @@ static int pick_nb(int n, int prec, const int* nb_table) {
 cudaError_t batched_plan(Context* ctx, int count, const int* h_n, const int* h_kind,
                          const int* h_prec, int q, const double* A, const double* B, double* X,
                          const int* nb_table, int ctas_per_sm, double tol, int max_iters,
-                         BatchPlan** out) {
+                         int fallback, int mode, float* feat, BatchPlan** out) {
   *out = nullptr;
   if (q < 1 || q > kBQ) return cudaErrorInvalidValue;
   auto* P = new BatchPlan();
@@ -790,8 +1032,8 @@ cudaError_t batched_plan(Context* ctx, int count, const int* h_n, const int* h_k
   std::vector<int> order(count);
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-    const double ca = (double)desc[a].n * desc[a].n * desc[a].n * (desc[a].prec == 0 ? 8 : 1);
-    const double cb = (double)desc[b].n * desc[b].n * desc[b].n * (desc[b].prec == 0 ? 8 : 1);
+    const double ca = (double)desc[a].n * desc[a].n * desc[a].n * (desc[a].prec == 0 ? 16 : 1);
+    const double cb = (double)desc[b].n * desc[b].n * desc[b].n * (desc[b].prec == 0 ? 16 : 1);
     return ca > cb;
   });
   P->grid = std::max(1, std::min(count, ctx->num_sms * std::max(1, ctas_per_sm)));
@@ -831,6 +1073,9 @@ cudaError_t batched_plan(Context* ctx, int count, const int* h_n, const int* h_k
   prm.max_iters = max_iters > 0 ? max_iters : 10;
   prm.ticket = P->d_ticket;
   prm.out = P->d_out;
+  prm.mode = mode;
+  prm.fallback = fallback;
+  prm.feat = feat;
   e = cudaFuncSetAttribute(batched_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            kSmemPanel);
   if (e != cudaSuccess) {
@@ -899,21 +1144,24 @@ struct ElGBBatchPlanImpl {
 
 extern "C" {
 
-int ElGBBatchedPlanCreate(ElGBContext ctx, int count, const int* n, const int* kind,
-                          const int* precision, int nrhs, const double* A, const double* B,
-                          double* X, const int* nb_table, int ctas_per_sm, double tol,
-                          int max_iters, ElGBBatchPlan* plan) {
-  if (!ctx || !plan || count < 0 || !n || nrhs < 1 || nrhs > 8 || (count > 0 && (!A || !B || !X)))
+int ElGBBatchedPlanCreate(ElGBContext ctx, int count, const int* n, int nrhs, const double* A,
+                          const double* B, double* X, const ElGBBatchOptions* opt,
+                          ElGBBatchPlan* plan) {
+  ElGBBatchOptions o{};
+  if (opt) o = *opt;
+  if (!ctx || !plan || count <= 0 || !n || nrhs < 1 || nrhs > 8 || !A ||
+      (!o.features_only && (!B || !X)) || (o.features_only && !o.features))
     return elgb::kElArgError;
   for (int i = 0; i < count; ++i)
-    if (n[i] < 1 || (kind && (kind[i] < 0 || kind[i] > 1)) ||
-        (precision && (precision[i] < 0 || precision[i] > 1)))
+    if (n[i] < 1 || (o.kind && (o.kind[i] < 0 || o.kind[i] > 1)) ||
+        (o.precision && (o.precision[i] < 0 || o.precision[i] > 2)))
       return elgb::kElArgError;
   *plan = nullptr;
-  if (count == 0) return elgb::kElArgError;
   elgb::BatchPlan* p = nullptr;
-  cudaError_t e = elgb::batched_plan(static_cast<elgb::Context*>(ctx), count, n, kind, precision,
-                                     nrhs, A, B, X, nb_table, ctas_per_sm, tol, max_iters, &p);
+  cudaError_t e = elgb::batched_plan(static_cast<elgb::Context*>(ctx), count, n, o.kind,
+                                     o.precision, nrhs, A, B, X, o.nb_table, o.ctas_per_sm, o.tol,
+                                     o.max_iters, o.no_fallback ? 0 : 1,
+                                     o.features_only ? 1 : 0, o.features, &p);
   if (e != cudaSuccess) return e == cudaErrorMemoryAllocation ? elgb::kElAllocError
                                                                : elgb::kElRuntimeError;
   *plan = new ElGBBatchPlanImpl{p};

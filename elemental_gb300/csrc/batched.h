@@ -17,13 +17,16 @@ struct BatchPlan;
 // Builds descriptors (largest-first order), per-CTA workspaces and a CUDA
 // graph holding the persistent launch.  A, B, X: packed column-major
 // systems (A_i n_i x n_i, B_i / X_i n_i x q, consecutive).  kind: 0 LU,
-// 1 Cholesky; prec: 0 FP64 factors, 1 FP32 factors + FP64 refinement
-// (nullptr: all LU / all FP32).  nb_table: panel width per size bucket
+// 1 Cholesky; prec: 0 FP64 factors, 1 FP32 factors + FP64 refinement, 2 the
+// same with BF16 operand products (nullptr: all LU / all FP32).  nb_table: panel width per size bucket
 // (n <= 32, 64, ..., 2048, larger), nullptr for 32 everywhere.
+// fallback: FP64 refactorization when refinement does not converge; mode 1
+// computes the selector's 16 features per system into feat instead of
+// solving.
 cudaError_t batched_plan(Context* ctx, int count, const int* h_n, const int* h_kind,
                          const int* h_prec, int q, const double* A, const double* B, double* X,
                          const int* nb_table, int ctas_per_sm, double tol, int max_iters,
-                         BatchPlan** out);
+                         int fallback, int mode, float* feat, BatchPlan** out);
 cudaError_t batched_execute(BatchPlan* P);
 cudaError_t batched_results(BatchPlan* P, BatchResult* h_out);
 void batched_destroy(BatchPlan* P);

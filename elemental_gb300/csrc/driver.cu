@@ -436,11 +436,6 @@ cudaError_t getrf(Context* ctx, int m, int n, T* A, long lda, int* ipiv, int nb,
       s.side.gemm.ws = cv.take<char>(tcs);
       if (!s.side.gemm.ws) return cudaErrorMemoryAllocation;
     }
-    // leave most SMs to the concurrent trailing update: ~1024 rows per CTA,
-    // within the panel kernel's shared-memory budget
-    const int rows_cap = (int)((200 * 1024) / (32 * sizeof(T))) - ctx->num_sms;
-    int g = std::max((m + 1023) / 1024, (m + rows_cap - 1) / rows_cap);
-    s.panel_ctas = std::max(1, std::min(g, ctx->num_sms));
   }
   if (ctx->opt_panel_ctas > 0) s.panel_ctas = std::min(ctx->opt_panel_ctas, ctx->num_sms);
   s.A = A;

@@ -5,6 +5,8 @@
 // residual and norms.  The tensor-core contractions live in tc_gemm.cu.
 #include <cooperative_groups.h>
 
+#include <algorithm>
+
 #include "kernels.h"
 
 namespace elgb {
@@ -153,13 +155,23 @@ getf2_panel_kernel(PanelParams<T> p) {
           }
         }
       }
+      // all loads of the slot issued together (one round trip)
       const int gr = __ldcg(&sl->row);
-      s_gv[tid] = __ldcg(&sl->val);
+      const T gv = __ldcg(&sl->val);
+      const bool own = tid == j / R;
+      T cr[W], dr[W];
+#pragma unroll
+      for (int c = 0; c < W; ++c) {
+        cr[c] = c < w ? __ldcg(&sl->cand[c]) : T(0);
+        dr[c] = (own && c < w) ? __ldcg(&sl->diag[c]) : T(0);
+      }
+      s_gv[tid] = gv;
       s_gr[tid] = gr;
-      if (gr >= 0)
-        for (int c = 0; c < w; ++c) s_rows[tid * W + c] = __ldcg(&sl->cand[c]);
-      if (tid == j / R)
-        for (int c = 0; c < w; ++c) s_d[c] = __ldcg(&sl->diag[c]);
+#pragma unroll
+      for (int c = 0; c < W; ++c) s_rows[tid * W + c] = cr[c];
+      if (own)
+#pragma unroll
+        for (int c = 0; c < W; ++c) s_d[c] = dr[c];
     }
     __syncthreads();
     if (s_abort) return;
@@ -223,7 +235,11 @@ cudaError_t launch_getf2_panel(T* A, long lda, int mp, int w, int* ipiv, int row
   if (w <= 0 || mp <= 0) return cudaSuccess;
   if (w > kPanelW || mp < w) return cudaErrorInvalidValue;
   constexpr int kMaxSmem = 200 * 1024;
-  int G = ceil_div(mp, 128);
+  // About 1024 rows per CTA: fewer CTAs make the per-column exchange cheap
+  // (every CTA copies every candidate row), more only where shared memory
+  // forces it.
+  const int rows_cap = (int)(kMaxSmem / (kPanelW * sizeof(T))) - 64;
+  int G = std::max(ceil_div(mp, 1024), ceil_div(mp, rows_cap));
   if (G > num_sms) G = num_sms;
   if (G > s.maxG) G = s.maxG;
   if (G > kPanelThreads) G = kPanelThreads;

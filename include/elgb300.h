@@ -152,46 +152,47 @@ int ElGBRefinedSolve_d(ElGBContext ctx, int n, const double* A, int lda,
 /* Batched uneven-size solves (added form): `count` independent systems
  * A_i X_i = B_i, packed column-major on the device (A_i n_i x n_i, then the
  * next; B_i and X_i n_i x nrhs, nrhs <= 8), solved by ONE persistent launch
- * replayed from a CUDA graph.  kind[i]: 0 LU with partial pivoting (El::LU +
- * lu::SolveAfter), 1 lower Cholesky (El::Cholesky + cholesky::SolveAfter);
- * precision[i]: 0 FP64 factors, 1 FP32 factors + FP64 refinement with an
- * FP64 refactorization on stall (NULL arrays: all LU / all FP32).  nb_table
- * (8 ints or NULL): panel width per size bucket n <= 32, 64, 128, 256, 512,
- * 1024, 2048, larger (the autotuner's output).  tol: target backward error
- * (<= 0: 1e-13).  The plan keeps the device pointers; Execute enqueues the
- * graph on the context's stream, Results synchronizes and copies one
- * ElGBBatchResult per system. */
+ * replayed from a CUDA graph.  Options (zero-initialised = defaults):
+ *   kind[i]       0 LU with partial pivoting (El::LU + lu::SolveAfter),
+ *                 1 lower Cholesky (El::Cholesky + cholesky::SolveAfter);
+ *                 NULL: all LU
+ *   precision[i]  0 FP64 factors, 1 FP32 factors, 2 FP32 storage with BF16
+ *                 operand products; 1 and 2 refine with an FP64 residual;
+ *                 NULL: all FP32
+ *   nb_table      8 panel widths for n <= 32, 64, ..., 2048, larger (the
+ *                 autotuner's output); NULL: 32
+ *   ctas_per_sm   persistent CTAs per SM (<= 0: 1)
+ *   tol           target normwise backward error (<= 0: 1e-13)
+ *   max_iters     refinement steps (<= 0: 10)
+ *   no_fallback   1: report non-convergence instead of refactoring in FP64
+ *   features_only 1: write the selector's 16 features per system to
+ *                 `features` (count x 16 floats, device) instead of solving
+ * Execute enqueues the graph on the context's stream; Results synchronizes
+ * and copies one ElGBBatchResult per system (features_only: backward_error
+ * holds the 1-norm condition estimate). */
 typedef struct ElGBBatchPlanImpl* ElGBBatchPlan;
 typedef struct {
   int iterations, converged, fell_back, info;
   double backward_error;
 } ElGBBatchResult;
-int ElGBBatchedPlanCreate(ElGBContext ctx, int count, const int* n,
-                          const int* kind, const int* precision, int nrhs,
+typedef struct {
+  const int* kind;
+  const int* precision;
+  const int* nb_table;
+  int ctas_per_sm;
+  double tol;
+  int max_iters;
+  int no_fallback;
+  int features_only;
+  float* features;
+} ElGBBatchOptions;
+int ElGBBatchedPlanCreate(ElGBContext ctx, int count, const int* n, int nrhs,
                           const double* A, const double* B, double* X,
-                          const int* nb_table, int ctas_per_sm, double tol,
-                          int max_iters, ElGBBatchPlan* plan);
+                          const ElGBBatchOptions* options, ElGBBatchPlan* plan);
 int ElGBBatchedExecute(ElGBBatchPlan plan);
 int ElGBBatchedResults(ElGBBatchPlan plan, ElGBBatchResult* out);
 double ElGBBatchedFlops(ElGBBatchPlan plan);
 int ElGBBatchedPlanDestroy(ElGBBatchPlan plan);
-
-/* Learned precision selector (added form): a 16 -> 64 -> 64 -> 3 FP32 MLP
- * (ReLU, softmax cross-entropy; classes 0 FP64, 1 FP32, 2 BF16) with
- * hand-written kernels.  Parameters are one flat FP32 device vector of
- * ElGBMLPParamCount() entries: W1[16][64] b1[64] W2[64][64] b2[64] W3[64][3]
- * b3[3] (row-major, input x output).  X is B x 16 row-major (device).
- * Forward: probs (B x 3) and/or argmax (B) may be NULL.  Gradient: the mean
- * cross-entropy gradient into grad (deterministic order), loss (host, may
- * be NULL; synchronizes when given).  AdamStep: one Adam update (step >= 1). */
-int ElGBMLPParamCount(void);
-int ElGBMLPForward(ElGBContext ctx, const float* params, const float* X, int B,
-                   float* probs, int* argmax);
-int ElGBMLPGradient(ElGBContext ctx, const float* params, const float* X,
-                    const int* labels, int B, float* grad, float* loss);
-int ElGBMLPAdamStep(ElGBContext ctx, float* params, const float* grad, float* m,
-                    float* v, float lr, float beta1, float beta2, float eps,
-                    float weight_decay, int step);
 
 /* lu::SolveAfter(orientation, A, P, B) (reference
  * src/lapack_like/factor/LU/SolveAfter.hpp:66-92): orientation 0 NORMAL,

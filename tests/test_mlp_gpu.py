@@ -55,12 +55,14 @@ def test_forward_and_gradient_match_oracle(ctx, B):
     gg = grad.cpu().numpy().astype(np.float64)
     rel = np.linalg.norm(gg - g) / max(np.linalg.norm(g), 1e-30)
     assert rel < 1e-4, rel
-    # and the gradient is the gradient: central finite difference of the
-    # oracle loss along a random direction
+    # and the oracle gradient is the gradient: central finite difference of
+    # the oracle loss along a random direction (ReLU kinks crossed within
+    # +-h make this approximate, hence the looser bound)
     d = rng.standard_normal(MO.NPARAM)
-    h = 1e-5
-    fd = (MO.loss_and_grad(theta + h * d, X, y)[0] - MO.loss_and_grad(theta - h * d, X, y)[0]) / (2 * h)
-    assert abs(fd - g @ d) <= 1e-4 * max(1.0, abs(fd))
+    h = 1e-6
+    th64 = theta.astype(np.float64)
+    fd = (MO.loss_and_grad(th64 + h * d, X, y)[0] - MO.loss_and_grad(th64 - h * d, X, y)[0]) / (2 * h)
+    assert abs(fd - g @ d) <= 2e-3 * max(1.0, abs(fd))
 
 
 def test_adam_training_lowers_loss(ctx):
