@@ -323,9 +323,10 @@ def gpu_arm(args, rank, world, local_rank):
     if os.path.exists(tpath) and prof["launches"]:
         with open(tpath) as f:
             tj = json.load(f)
-        # DRAM bytes per algorithmic byte from one ncu capture, applied to the
+        # DRAM bytes per GEMM flop from one ncu capture of the same LU at a
+        # smaller n (all tc_gemm launches of one step), applied to the
         # average launch of this run
-        traffic = tj["dram_bytes_per_algorithmic_byte"] * prof["bytes"] / prof["launches"]
+        traffic = tj["dram_bytes_per_flop"] * prof["flops"] / prof["launches"]
     roofline = {
         "kernel": "tc_gemm_sub_kernel (tcgen05 trailing update, "
                   f"{ {'fp32': 'TF32x3', 'tf32': 'TF32', 'bf16': 'BF16', 'fp64': 'n/a'}[args.precision] } operands)",
@@ -333,6 +334,10 @@ def gpu_arm(args, rank, world, local_rank):
         "frac": (tf_achieved / peak) if tf_achieved else None,
         "peak_source": f"{peak_kind} bf16 dense (sustained): the kernel is timed inside a long step",
         "traffic": traffic,
+        "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum over every "
+                           "tc_gemm_sub_kernel launch of an n=8192 step, per GEMM flop, scaled "
+                           "to this run's average launch (profiles/tc_gemm_traffic.json)")
+        if traffic is not None else None,
         "launches": prof["launches"], "kernel_ms_total": prof["ms"],
         "algorithmic_flops_per_launch": prof["flops"] / max(prof["launches"], 1),
         "algorithmic_bytes_per_launch": prof["bytes"] / max(prof["launches"], 1),

@@ -1,0 +1,117 @@
+"""Single-kernel cases of the factor-and-solve path, for timing and for
+profiler captures (one warm-up call, then one measured call, so a profiler
+can skip the first launch of the kernel it targets).
+
+    python -m elemental_gb300.kernel_cases tc_gemm --m 16384 --n 16384 --k 512 --kind 2
+    python -m elemental_gb300.kernel_cases lu --n 8192 --kind 2
+    python -m elemental_gb300.kernel_cases refine --n 8192 --nrhs 16
+    python -m elemental_gb300.kernel_cases lu64 --n 4096
+
+Each prints one JSON line with the event-timed duration of the measured
+call and its algorithmic work.  Inputs are seeded N(0, 1), generated on the
+device.
+"""
+import argparse
+import json
+
+import torch
+
+from . import device as D
+
+KIND_NAMES = {-1: "simt-fp32", 0: "bf16", 1: "tf32", 2: "tf32x3"}
+
+
+def _timed(fn):
+    torch.cuda.synchronize()
+    s = torch.cuda.Event(enable_timing=True)
+    e = torch.cuda.Event(enable_timing=True)
+    s.record()
+    fn()
+    e.record()
+    e.synchronize()
+    return s.elapsed_time(e)
+
+
+def case_tc_gemm(ctx, a):
+    """C (m x n) -= A (m x k) B (k x n) on the tensor cores: the trailing
+    update of El::LU (src/lapack_like/factor/LU.cpp:131-133)."""
+    g = torch.Generator(device="cuda").manual_seed(a.seed)
+    A = D.colmajor(a.m, a.k, torch.float32)
+    B = D.colmajor(a.k, a.n, torch.float32)
+    C = D.colmajor(a.m, a.n, torch.float32)
+    A.copy_(torch.randn(a.m, a.k, device="cuda", generator=g))
+    B.copy_(torch.randn(a.k, a.n, device="cuda", generator=g))
+    C.zero_()
+    ctx.gemm_sub_tc(A, B, C, a.kind)
+    ms = _timed(lambda: ctx.gemm_sub_tc(A, B, C, a.kind))
+    flops = 2.0 * a.m * a.n * a.k
+    return dict(case="tc_gemm", m=a.m, n=a.n, k=a.k, kind=KIND_NAMES[a.kind], ms=ms,
+                tflops=flops / (ms * 1e-3) / 1e12,
+                algorithmic_bytes=4.0 * (a.m * a.k + a.k * a.n + 2 * a.m * a.n))
+
+
+def case_lu(ctx, a):
+    """El::LU on an FP32 matrix with tensor-core updates (the low-precision
+    factorization of the refinement)."""
+    g = torch.Generator(device="cuda").manual_seed(a.seed)
+    A0 = torch.randn(a.n, a.n, device="cuda", generator=g).t()
+    A = A0.clone()
+    ctx.lu_mixed(A, gemm_kind=a.kind, nb=a.nb)
+    A.copy_(A0)
+    ms = _timed(lambda: ctx.lu_mixed(A, gemm_kind=a.kind, nb=a.nb))
+    flops = 2.0 / 3.0 * a.n ** 3
+    return dict(case="lu", n=a.n, kind=KIND_NAMES[a.kind], ms=ms,
+                tflops=flops / (ms * 1e-3) / 1e12)
+
+
+def case_lu64(ctx, a):
+    """El::LU in FP64 (the plain path)."""
+    g = torch.Generator(device="cuda").manual_seed(a.seed)
+    A0 = torch.randn(a.n, a.n, device="cuda", generator=g, dtype=torch.float64).t()
+    A = A0.clone()
+    ctx.lu(A, nb=a.nb)
+    A.copy_(A0)
+    ms = _timed(lambda: ctx.lu(A, nb=a.nb))
+    flops = 2.0 / 3.0 * a.n ** 3
+    return dict(case="lu64", n=a.n, ms=ms, tflops=flops / (ms * 1e-3) / 1e12)
+
+
+def case_refine(ctx, a):
+    """Mixed-precision LU-IR (FP32 factors, FP64 residual)."""
+    g = torch.Generator(device="cuda").manual_seed(a.seed)
+    A = D.colmajor(a.n, a.n)
+    B = D.colmajor(a.n, a.nrhs)
+    A.copy_(torch.randn(a.n, a.n, device="cuda", generator=g, dtype=torch.float64))
+    B.copy_(torch.randn(a.n, a.nrhs, device="cuda", generator=g, dtype=torch.float64))
+    ctx.refined_solve(A, B, precision="fp32", method=a.method)
+    info = {}
+
+    def run():
+        info.update(ctx.refined_solve(A, B, precision="fp32", method=a.method)[1])
+
+    ms = _timed(run)
+    return dict(case="refine", n=a.n, nrhs=a.nrhs, method=a.method, ms=ms, **info)
+
+
+CASES = {"tc_gemm": case_tc_gemm, "lu": case_lu, "lu64": case_lu64, "refine": case_refine}
+
+
+def main(argv=None):
+    p = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    p.add_argument("case", choices=sorted(CASES))
+    p.add_argument("--m", type=int, default=16384)
+    p.add_argument("--n", type=int, default=8192)
+    p.add_argument("--k", type=int, default=512)
+    p.add_argument("--kind", type=int, default=2, choices=sorted(KIND_NAMES))
+    p.add_argument("--nb", type=int, default=0)
+    p.add_argument("--nrhs", type=int, default=16)
+    p.add_argument("--method", default="lu-ir", choices=["lu-ir", "gmres-ir"])
+    p.add_argument("--seed", type=int, default=20261204)
+    a = p.parse_args(argv)
+    ctx = D.context(0)
+    out = CASES[a.case](ctx, a)
+    print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()
