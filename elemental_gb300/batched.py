@@ -13,6 +13,9 @@ from .device import Context, context
 
 KIND = {"lu": 0, "chol": 1}
 PREC = {"fp64": 0, "fp32": 1, "bf16": 2}
+# refinement of low-precision factors: LU-IR then flexible GMRES-IR when it
+# stalls ("auto"), LU-IR only, or FGMRES-IR only
+METHOD = {"auto": 0, "lu-ir": 1, "gmres-ir": 2}
 
 
 class BatchedSolver:
@@ -25,7 +28,8 @@ class BatchedSolver:
 
     def __init__(self, ns, q, A_packed, B_packed, kinds=None, precisions=None, nb_table=None,
                  ctas_per_sm=1, tol=1e-13, max_iters=10, fallback=True, features_only=False,
-                 ctx: Context | None = None):
+                 method="auto", gmres_restart=0, gmres_max_iters=0, precision_device=None,
+                 phases=False, ctx: Context | None = None):
         self.ctx = ctx or context()
         self.lib = _lib.load()
         self.ns = np.ascontiguousarray(ns, dtype=np.int32)
@@ -50,7 +54,16 @@ class BatchedSolver:
             k.ctypes.data_as(vp).value, pr.ctypes.data_as(vp).value,
             nbt.ctypes.data_as(vp).value if nbt is not None else None, int(ctas_per_sm),
             float(tol), int(max_iters), 0 if fallback else 1, 1 if features_only else 0,
-            self.features.data_ptr() if features_only else None)
+            self.features.data_ptr() if features_only else None, METHOD[method],
+            int(gmres_restart), int(gmres_max_iters),
+            precision_device.data_ptr() if precision_device is not None else None,
+            None)
+        self.precision_device = precision_device
+        self.phase_ns = None
+        if phases:
+            self.phase_ns = torch.zeros(self.count, 8, dtype=torch.int64,
+                                        device=A_packed.device)
+            opt.phase_ns = self.phase_ns.data_ptr()
         self._keep = (k, pr, nbt)
         rc = self.lib.ElGBBatchedPlanCreate(
             self.ctx.h, self.count, self.ns.ctypes.data_as(vp), q, vp(self.A.data_ptr()),
@@ -82,7 +95,17 @@ class BatchedSolver:
             raise RuntimeError(f"ElGBBatchedResults returned {rc}")
         return [dict(iterations=r.iterations, converged=bool(r.converged),
                      fell_back=bool(r.fell_back), info=r.info,
-                     backward_error=r.backward_error) for r in out]
+                     backward_error=r.backward_error, gmres_iterations=r.gmres_iterations,
+                     precision=r.precision, device_ms=r.device_ns * 1e-6) for r in out]
+
+    PHASES = ("panel", "swaps", "u12_solve", "trailing_update", "lu_ir", "fgmres_ir",
+              "fp64_path", "features")
+
+    def phase_ms(self):
+        """Per-system device time by phase (requires phases=True): dict of
+        numpy arrays in ms."""
+        ph = self.phase_ns.cpu().numpy() * 1e-6
+        return {k: ph[:, i] for i, k in enumerate(self.PHASES)}
 
     def solution(self, i):
         off = int(np.sum(self.ns[:i].astype(np.int64))) * self.q

@@ -45,6 +45,10 @@ struct SysDesc {
 };
 
 struct Shared {
+  // per-system device time by phase (thread 0 accumulates, globaltimer ns):
+  // 0 panel, 1 row swaps, 2 U12 solve, 3 trailing update, 4 LU-IR,
+  // 5 FGMRES-IR, 6 FP64 path, 7 features
+  unsigned long long ph[8];
   double red[kBT / 32][kBQ + 1];
   double colv[kBQ + 1];
   int ival[4];
@@ -200,12 +204,14 @@ __device__ void cta_apply_swaps(T* W, int n, int ld, int k, int jb, Shared& sh, 
   const int chunk = max(1, stage_elems / cnt);
   for (int c0 = 0; c0 < ncols_out; c0 += chunk) {
     const int cw = min(chunk, ncols_out - c0);
+#pragma unroll 8
     for (int idx = threadIdx.x; idx < cw * cnt; idx += kBT) {
       const int e = idx % cnt, cc = c0 + idx / cnt;
       const int col = cc < k ? cc : cc + jb;
       stage[idx] = W[sh.pairs[128 + e] + (long)col * ld];
     }
     __syncthreads();
+#pragma unroll 8
     for (int idx = threadIdx.x; idx < cw * cnt; idx += kBT) {
       const int e = idx % cnt, cc = c0 + idx / cnt;
       const int col = cc < k ? cc : cc + jb;
@@ -216,56 +222,132 @@ __device__ void cta_apply_swaps(T* W, int n, int ld, int k, int jb, Shared& sh, 
 }
 
 // C[m x nc] -= P[m x jb] * Q[jb x nc]: P in shared memory (ld = ldp), Q in
-// global (ld = ldq, staged in 64-column chunks into `qs`), C in global.
-// 64 x 64 tiles, each thread a 4 x 4 block (rows tx + 16 i, cols ty + 16 j).
+// global (ld = ldq, staged in kGC-column chunks into `qs`), C in global.
+// Tiles of 128 x kGC: lane l of warp w owns rows r0 + l + 32 i (i < 4) and
+// columns c0 + w + 8 j (j < kGC / 8), so a warp's C accesses are 128-byte
+// rows of one column and its Q reads are shared-memory broadcasts.  The C
+// tile is loaded into registers before the k loop (the loads are in flight
+// during the FMAs).
 template <typename T>
-__device__ void cta_gemm_update(const T* P, int ldp, const T* Q, int ldq, T* C, int ldc, int m,
-                                int nc, int jb, T* qs, bool lower_only, int row_base,
-                                int col_base, bool lowp) {
-  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  for (int c0 = 0; c0 < nc; c0 += 64) {
-    const int cw = min(64, nc - c0);
+struct GemmShape {
+  static constexpr int kGC = 64;  // FP32: 4 x 8 per thread
+};
+template <>
+struct GemmShape<double> {
+  static constexpr int kGC = 32;  // FP64: 4 x 4 per thread
+};
+
+template <typename T>
+__device__ __forceinline__ void gemm_tile_load(const T* C, int ldc, int m, int cw, int r0,
+                                               int lane, int w, T (&v)[4][GemmShape<T>::kGC / 8]) {
+  constexpr int kTC = GemmShape<T>::kGC / 8;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int r = r0 + lane + 32 * i;
+#pragma unroll
+    for (int j = 0; j < kTC; ++j) {
+      const int cc = w + 8 * j;
+      v[i][j] = (r < m && cc < cw) ? C[r + (long)cc * ldc] : T(0);
+    }
+  }
+}
+
+template <typename T>
+__device__ __noinline__ void cta_gemm_update(const T* P, int ldp, const T* Q, int ldq, T* C,
+                                             int ldc, int m, int nc, int jb, T* qs, bool lowp) {
+  constexpr int kGC = GemmShape<T>::kGC, kTC = kGC / 8;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int c0 = 0; c0 < nc; c0 += kGC) {
+    const int cw = min(kGC, nc - c0);
+    T* Cc = C + (long)c0 * ldc;
     __syncthreads();
-    for (int idx = threadIdx.x; idx < jb * 64; idx += kBT) {
+    for (int idx = threadIdx.x; idx < jb * kGC; idx += kBT) {
       const int kk = idx % jb, cc = idx / jb;
       qs[kk + cc * jb] = cc < cw ? rnd(Q[kk + (long)(c0 + cc) * ldq], lowp) : T(0);
     }
     __syncthreads();
-    for (int r0 = 0; r0 < m; r0 += 64) {
-      if (lower_only && row_base + r0 + 63 < col_base + c0) continue;
-      T acc[4][4];
+    // software pipeline over the 128-row tiles: the next tile's C is loaded
+    // while this tile's FMAs run
+    T cv[4][kTC], cn[4][kTC];
+    gemm_tile_load<T>(Cc, ldc, m, cw, 0, lane, w, cv);
+    for (int r0 = 0; r0 < m; r0 += 128) {
+      if (r0 + 128 < m) gemm_tile_load<T>(Cc, ldc, m, cw, r0 + 128, lane, w, cn);
+      T acc[4][kTC];
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
+        for (int j = 0; j < kTC; ++j) acc[i][j] = T(0);
+#pragma unroll 4
       for (int kk = 0; kk < jb; ++kk) {
-        T a[4], b[4];
+        T a[4], b[kTC];
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-          const int r = r0 + tx + 16 * i;
+          const int r = r0 + lane + 32 * i;
           a[i] = r < m ? rnd(P[r + kk * ldp], lowp) : T(0);
         }
 #pragma unroll
-        for (int j = 0; j < 4; ++j) b[j] = qs[kk + (ty + 16 * j) * jb];
+        for (int j = 0; j < kTC; ++j) b[j] = qs[kk + (w + 8 * j) * jb];
 #pragma unroll
         for (int i = 0; i < 4; ++i)
 #pragma unroll
-          for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+          for (int j = 0; j < kTC; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
       }
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
-        const int r = r0 + tx + 16 * i;
-        if (r >= m) continue;
+        const int r = r0 + lane + 32 * i;
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const int cc = ty + 16 * j;
-          if (cc >= cw) continue;
-          if (lower_only && row_base + r < col_base + c0 + cc) continue;
-          T* cp = C + r + (long)(c0 + cc) * ldc;
-          *cp -= acc[i][j];
+        for (int j = 0; j < kTC; ++j) {
+          const int cc = w + 8 * j;
+          if (r < m && cc < cw) Cc[r + (long)cc * ldc] = cv[i][j] - acc[i][j];
+          cv[i][j] = cn[i][j];
         }
       }
     }
+  }
+  __syncthreads();
+}
+
+// U12 := L11^{-1} U12 (L11 unit lower, jb x jb in the shared panel, ld mp),
+// one thread per column with the column held in registers.
+template <typename T, int JB>
+__device__ __noinline__ void cta_trsm_cols(const T* L, int mp, T* W0, int ld, int n2, bool lowp) {
+  for (int c = threadIdx.x; c < n2; c += kBT) {
+    T* col = W0 + (long)c * ld;
+    T x[JB];
+#pragma unroll
+    for (int i = 0; i < JB; ++i) x[i] = col[i];
+#pragma unroll
+    for (int i = 1; i < JB; ++i) {
+      T s = x[i];
+#pragma unroll
+      for (int l = 0; l < i; ++l) s = fma(-rnd(L[i + l * mp], lowp), rnd(x[l], lowp), s);
+      x[i] = s;
+    }
+#pragma unroll
+    for (int i = 1; i < JB; ++i) col[i] = x[i];
+  }
+}
+
+template <typename T>
+__device__ void cta_trsm_u12(const T* L, int mp, T* W0, int ld, int jb, int n2, bool lowp) {
+  switch (jb) {
+    case 8: cta_trsm_cols<T, 8>(L, mp, W0, ld, n2, lowp); break;
+    case 16: cta_trsm_cols<T, 16>(L, mp, W0, ld, n2, lowp); break;
+    case 32:
+      if (sizeof(T) == 4) {  // 32 doubles per thread would spill
+        cta_trsm_cols<T, 32>(L, mp, W0, ld, n2, lowp);
+        break;
+      }
+      [[fallthrough]];
+    default:
+      for (int c = threadIdx.x; c < n2; c += kBT) {
+        T* col = W0 + (long)c * ld;
+        for (int i = 1; i < jb; ++i) {
+          T s = col[i];
+          for (int l = 0; l < i; ++l) s = fma(-rnd(L[i + l * mp], lowp), rnd(col[l], lowp), s);
+          col[i] = s;
+        }
+      }
   }
   __syncthreads();
 }
@@ -274,11 +356,19 @@ __device__ void cta_gemm_update(const T* P, int ldp, const T* Q, int ldq, T* C, 
 // piv_out[0..n) receives the swap destinations; returns info (0 ok, j+1 at
 // the first zero pivot).
 template <typename T>
-__device__ int cta_lu(T* W, int n, int ld, int nb, int* piv_out, Shared& sh, T* smem,
+__device__ __noinline__ int cta_lu(T* W, int n, int ld, int nb, int* piv_out, Shared& sh, T* smem,
                       int smem_elems, bool lowp) {
   __shared__ T fv[9];
   __shared__ int fr[9];
   int info = 0;
+  unsigned long long t0 = threadIdx.x == 0 ? globaltimer_ns() : 0ull;
+  auto phase = [&](int i) {  // closes phase i (after a block barrier)
+    if (threadIdx.x == 0) {
+      const unsigned long long t = globaltimer_ns();
+      sh.ph[i] += t - t0;
+      t0 = t;
+    }
+  };
   for (int k = 0; k < n; k += nb) {
     const int jb = min(nb, n - k);
     const int mp = n - k;
@@ -329,33 +419,29 @@ __device__ int cta_lu(T* W, int n, int ld, int nb, int* piv_out, Shared& sh, T* 
     }
     for (int j = threadIdx.x; j < jb; j += kBT) piv_out[k + j] = sh.piv[j];
     __syncthreads();
+    phase(0);
     // swaps on the other columns (staging space after the panel)
     cta_apply_swaps(W, n, ld, k, jb, sh, smem + mp * jb, smem_elems - mp * jb);
+    phase(1);
     const int n2 = n - k - jb;
     if (n2 > 0) {
       // U12 = L11^{-1} A12 (one thread per column, L11 from the panel)
-      for (int c = threadIdx.x; c < n2; c += kBT) {
-        T* col = W + k + (long)(k + jb + c) * ld;
-        for (int i = 1; i < jb; ++i) {
-          T s = col[i];
-          for (int l = 0; l < i; ++l) s = fma(-rnd(panel[i + l * mp], lowp), rnd(col[l], lowp), s);
-          col[i] = s;
-        }
-      }
-      __syncthreads();
+      cta_trsm_u12<T>(panel, mp, W + k + (long)(k + jb) * ld, ld, jb, n2, lowp);
+      phase(2);
       // A22 -= A21 U12, A21 = panel rows jb.. (still in shared memory)
       cta_gemm_update<T>(panel + jb, mp, W + k + (long)(k + jb) * ld, ld,
                          W + (k + jb) + (long)(k + jb) * ld, ld, n2, n2, jb,
-                         smem + mp * jb, false, 0, 0, lowp);
+                         smem + mp * jb, lowp);
     }
     __syncthreads();
+    phase(3);
   }
   return info;
 }
 
 // In-CTA lower Cholesky of W; returns info (j+1 at the first non-positive pivot).
 template <typename T>
-__device__ int cta_chol(T* W, int n, int ld, int nb, T* smem, bool lowp) {
+__device__ __noinline__ int cta_chol(T* W, int n, int ld, int nb, T* smem, bool lowp) {
   __shared__ int s_bad;
   if (threadIdx.x == 0) s_bad = 0;
   __syncthreads();
@@ -469,50 +555,67 @@ __device__ void cta_perm_from_swaps(const int* piv, int n, int* perm, int* lab_s
 
 // x := U^{-1} L^{-1} x for n x q x (ld n): L lower (unit or not), U upper
 // (non-unit) both in W (for Cholesky U = L^T has been written to the upper
-// triangle).  32-row diagonal blocks are solved by one warp per column in
-// registers; the rows after (before) a block are updated by all threads.
-template <typename T>
-__device__ void cta_solve(const T* W, int n, int ld, bool unit_lower, T* x, int q) {
+// triangle).  Factors stored as S, arithmetic in T (T = double with S =
+// float applies FP32 factors exactly, as a fixed FP64 operator).  Each
+// 32 x 32 diagonal block is first staged in shared memory by all threads,
+// then solved by one warp per column in registers; the rows after (before)
+// the block are updated by all threads.
+template <typename S, typename T>
+__device__ __noinline__ void cta_solve(const S* W, int n, int ld, bool unit_lower, T* x, int q) {
+  __shared__ T sdg[32][33];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  auto stage = [&](int j0, int jb) {
+    for (int idx = threadIdx.x; idx < 32 * 32; idx += kBT) {
+      const int r = idx & 31, c = idx >> 5;
+      sdg[r][c] = (r < jb && c < jb) ? (T)W[(j0 + r) + (long)(j0 + c) * ld] : T(0);
+    }
+    __syncthreads();
+  };
   for (int j0 = 0; j0 < n; j0 += 32) {
     const int jb = min(32, n - j0);
+    stage(j0, jb);
     if (warp < q) {
       T* xc = x + (long)warp * n;
       T v = lane < jb ? xc[j0 + lane] : T(0);
       for (int jj = 0; jj < jb; ++jj) {
-        if (!unit_lower && lane == jj) v = v / W[(j0 + jj) + (long)(j0 + jj) * ld];
+        if (!unit_lower && lane == jj) v = v / sdg[jj][jj];
         const T xj = __shfl_sync(0xffffffffu, v, jj);
-        if (lane > jj && lane < jb) v = fma(-W[(j0 + lane) + (long)(j0 + jj) * ld], xj, v);
+        if (lane > jj && lane < jb) v = fma(-sdg[lane][jj], xj, v);
       }
       if (lane < jb) xc[j0 + lane] = v;
     }
     __syncthreads();
     for (int idx = threadIdx.x; idx < (n - j0 - jb) * q; idx += kBT) {
       const int r = j0 + jb + idx % (n - j0 - jb), c = idx / (n - j0 - jb);
-      T s = x[r + (long)c * n];
-      for (int jj = 0; jj < jb; ++jj) s = fma(-W[r + (long)(j0 + jj) * ld], x[j0 + jj + (long)c * n], s);
-      x[r + (long)c * n] = s;
+      T acc = x[r + (long)c * n];
+      const T* xb = x + j0 + (long)c * n;
+#pragma unroll 8
+      for (int jj = 0; jj < jb; ++jj) acc = fma(-(T)W[r + (long)(j0 + jj) * ld], xb[jj], acc);
+      x[r + (long)c * n] = acc;
     }
     __syncthreads();
   }
   for (int j0 = ((n - 1) / 32) * 32; j0 >= 0; j0 -= 32) {
     const int jb = min(32, n - j0);
+    stage(j0, jb);
     if (warp < q) {
       T* xc = x + (long)warp * n;
       T v = lane < jb ? xc[j0 + lane] : T(0);
       for (int jj = jb - 1; jj >= 0; --jj) {
-        if (lane == jj) v = v / W[(j0 + jj) + (long)(j0 + jj) * ld];
+        if (lane == jj) v = v / sdg[jj][jj];
         const T xj = __shfl_sync(0xffffffffu, v, jj);
-        if (lane < jj) v = fma(-W[(j0 + lane) + (long)(j0 + jj) * ld], xj, v);
+        if (lane < jj) v = fma(-sdg[lane][jj], xj, v);
       }
       if (lane < jb) xc[j0 + lane] = v;
     }
     __syncthreads();
     for (int idx = threadIdx.x; idx < j0 * q; idx += kBT) {
       const int r = idx % j0, c = idx / j0;
-      T s = x[r + (long)c * n];
-      for (int jj = 0; jj < jb; ++jj) s = fma(-W[r + (long)(j0 + jj) * ld], x[j0 + jj + (long)c * n], s);
-      x[r + (long)c * n] = s;
+      T acc = x[r + (long)c * n];
+      const T* xb = x + j0 + (long)c * n;
+#pragma unroll 8
+      for (int jj = 0; jj < jb; ++jj) acc = fma(-(T)W[r + (long)(j0 + jj) * ld], xb[jj], acc);
+      x[r + (long)c * n] = acc;
     }
     __syncthreads();
   }
@@ -536,10 +639,14 @@ __device__ void cta_apply_inverse(const T* W, int n, int kind, const int* perm, 
                                   double* x, T* xt, T* tmp, int q, bool accumulate,
                                   double* scale) {
   __syncthreads();
-  if (threadIdx.x < q) {
-    double m = 0.0;
-    for (int r = 0; r < n; ++r) m = fmax(m, fabs(rhs[r + (long)threadIdx.x * n]));
-    scale[threadIdx.x] = (m > 0 && m < INFINITY) ? m : 1.0;
+  {  // per-column max |rhs| (one warp per column)
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int c = warp; c < q; c += kBT / 32) {
+      double m = 0.0;
+      for (int r = lane; r < n; r += 32) m = fmax(m, fabs(rhs[r + (long)c * n]));
+      for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+      if (lane == 0) scale[c] = (m > 0 && m < INFINITY) ? m : 1.0;
+    }
   }
   __syncthreads();
   for (int i = threadIdx.x; i < n * q; i += kBT) {
@@ -548,7 +655,7 @@ __device__ void cta_apply_inverse(const T* W, int n, int kind, const int* perm, 
     xt[i] = (T)(rhs[src + (long)c * n] / scale[c]);
   }
   __syncthreads();
-  cta_solve<T>(W, n, n, kind == 0, xt, q);
+  cta_solve<T, T>(W, n, n, kind == 0, xt, q);
   for (int i = threadIdx.x; i < n * q; i += kBT) {
     const double v = (double)xt[i] * scale[i / n];
     x[i] = accumulate ? x[i] + v : v;
@@ -577,26 +684,74 @@ struct BatchParams {
   int mode;          // 0 solve, 1 features only
   int fallback;      // FP64 refactorization when refinement does not converge
   float* feat;       // mode 1: count x 16 features
+  int method;        // 0 LU-IR then FGMRES-IR on stall, 1 LU-IR only, 2 FGMRES-IR only
+  int kry_m;         // FGMRES restart length (<= kKryMax)
+  int kry_max;       // FGMRES inner iterations per right-hand side
+  double* kry;       // per CTA: (2 kry_m + 2) x n_max doubles (V, Z, scratch)
+  const int* prec_dev;  // per-system precision read at run time (or null)
+  unsigned long long* phase_ns;  // count x 8 phase times (or null)
 };
+
+// Y = B - A X (B != null) or Y = A X (B == null) for the n x q block X (all
+// ld n), FP64.  Thread t owns rows t + kBT g (g < RG) of each 8-row-group
+// sweep, so every j step has RG independent coalesced loads of A in flight
+// (the product is latency-bound otherwise: one SM, 8 warps).
+template <int RG, int QM>
+__device__ void cta_gemv_rows(const double* __restrict__ A, int n, const double* X, int q,
+                              const double* B, double* Y) {
+  for (int r0 = 0; r0 < n; r0 += RG * kBT) {
+    double acc[RG][QM];
+#pragma unroll
+    for (int g = 0; g < RG; ++g)
+#pragma unroll
+      for (int c = 0; c < QM; ++c) acc[g][c] = 0.0;
+    int rr[RG];
+#pragma unroll
+    for (int g = 0; g < RG; ++g) {
+      const int r = r0 + threadIdx.x + g * kBT;
+      rr[g] = r < n ? r : n - 1;  // clamped: loads stay in bounds, results unused
+    }
+#pragma unroll 2
+    for (int j = 0; j < n; ++j) {
+      double a[RG];
+#pragma unroll
+      for (int g = 0; g < RG; ++g) a[g] = A[rr[g] + (long)j * n];
+      double x[QM];
+#pragma unroll
+      for (int c = 0; c < QM; ++c) x[c] = c < q ? X[j + (long)c * n] : 0.0;
+#pragma unroll
+      for (int g = 0; g < RG; ++g)
+#pragma unroll
+        for (int c = 0; c < QM; ++c) acc[g][c] = fma(a[g], x[c], acc[g][c]);
+    }
+#pragma unroll
+    for (int g = 0; g < RG; ++g) {
+      const int r = r0 + threadIdx.x + g * kBT;
+      if (r >= n) continue;
+#pragma unroll
+      for (int c = 0; c < QM; ++c)
+        if (c < q) Y[r + (long)c * n] = B ? B[r + (long)c * n] - acc[g][c] : acc[g][c];
+    }
+  }
+}
+
+__device__ __noinline__ void cta_gemv(const double* A, int n, const double* X, int q,
+                                      const double* B, double* Y) {
+  if (q == 1)
+    cta_gemv_rows<8, 1>(A, n, X, q, B, Y);
+  else if (q == 2)
+    cta_gemv_rows<8, 2>(A, n, X, q, B, Y);
+  else if (q <= 4)
+    cta_gemv_rows<4, 4>(A, n, X, q, B, Y);
+  else
+    cta_gemv_rows<4, kBQ>(A, n, X, q, B, Y);
+  __syncthreads();
+}
 
 __device__ double sys_berr(const double* A, int n, const double* X, const double* B, double* R,
                            int q, Shared& sh, double nA) {
   // R = B - A X (FP64), berr = max_c ||R_c|| / (nA ||X_c|| + ||B_c||)
-  for (int r = threadIdx.x; r < n; r += kBT) {
-    double acc[kBQ];
-#pragma unroll
-    for (int c = 0; c < kBQ; ++c) acc[c] = 0.0;
-    for (int j = 0; j < n; ++j) {
-      const double a = A[r + (long)j * n];
-#pragma unroll
-      for (int c = 0; c < kBQ; ++c)
-        if (c < q) acc[c] = fma(a, X[j + (long)c * n], acc[c]);
-    }
-#pragma unroll
-    for (int c = 0; c < kBQ; ++c)
-      if (c < q) R[r + (long)c * n] = B[r + (long)c * n] - acc[c];
-  }
-  __syncthreads();
+  cta_gemv(A, n, X, q, B, R);
   double nr[kBQ], nx[kBQ], nb[kBQ];
   __shared__ double s_n[3][kBQ];
   block_colsum(n, q, [&](int r, int c) { const double v = R[r + (long)c * n]; return v * v; }, sh,
@@ -698,6 +853,145 @@ __device__ void block_sum_max(int n, F f, Shared& sh, double* out_sum, double* o
   __syncthreads();
 }
 
+// ---- FGMRES-IR ------------------------------------------------------------
+// Flexible right-preconditioned restarted GMRES on A x = b in FP64, the
+// preconditioner being the low-precision factors (El's FGMRES,
+// include/El/lapack_like/solve/FGMRES.hpp:37-290: z_j = M^{-1} v_j kept,
+// w = A z_j, Givens-updated least squares, x = x0 + Z y, explicit residual
+// at every restart).  The orthogonalization is classical Gram-Schmidt
+// applied twice (each pass one warp per basis vector) instead of the
+// reference's modified Gram-Schmidt: same subspace, fewer block barriers.
+constexpr int kKryMax = 32;
+
+struct KryShared {
+  double H[kKryMax + 1][kKryMax];
+  double cs[kKryMax], sn[kKryMax], g[kKryMax + 1], y[kKryMax], h[kKryMax + 1];
+  int stop;
+};
+
+// h[i] = <w, V_i>, i < cnt (one warp per basis vector).
+__device__ void cta_multi_dot(const double* Vk, long ldv, int cnt, const double* w, int n,
+                              double* h) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int i = warp; i < cnt; i += kBT / 32) {
+    const double* v = Vk + (long)i * ldv;
+    double acc = 0.0;
+    for (int r = lane; r < n; r += 32) acc = fma(w[r], v[r], acc);
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) h[i] = acc;
+  }
+  __syncthreads();
+}
+
+// y = A v (FP64), one thread per row.
+__device__ void cta_matvec(const double* A, int n, const double* v, double* y) {
+  cta_gemv(A, n, v, 1, nullptr, y);
+}
+
+// z = M^{-1} v with the low-precision factors applied in FP64 arithmetic:
+// M = L U exactly (a fixed linear operator), the GMRES-IR preconditioner of
+// Carson and Higham (the factors' precision limits M's quality, not the
+// solve's rounding).  z may alias nothing else; perm maps rows for LU.
+template <typename T>
+__device__ void cta_precond(const T* W, int n, int kind, const int* perm, const double* v,
+                            double* z) {
+  for (int r = threadIdx.x; r < n; r += kBT) z[r] = v[kind == 0 ? perm[r] : r];
+  __syncthreads();
+  cta_solve<T, double>(W, n, n, kind == 0, z, 1);
+}
+
+// One right-hand side: improves x in place until its normwise backward
+// error ||b - A x|| / (nA ||x|| + ||b||) <= tol or max_inner iterations are
+// spent.  Returns the inner iterations used; *berr gets the last explicit
+// backward error.
+template <typename T>
+__device__ __noinline__ int cta_fgmres(const double* A, int n, double nA, const T* W, int kind,
+                          const int* perm, const double* b, double* x, double* kry, int m,
+                          int max_inner, double tol, T* vt, Shared& sh, KryShared& ks,
+                          double* berr) {
+  double* Vk = kry;                       // V_0 .. V_m
+  double* Zk = kry + (long)(m + 1) * n;   // Z_0 .. Z_{m-1}
+  double* tmp = Zk + (long)m * n;
+  int total = 0;
+  double sum, mx;
+  block_sum_max(n, [&](int i) { return b[i] * b[i]; }, sh, &sum, &mx);
+  const double nb = sqrt(sum);
+  while (true) {
+    cta_matvec(A, n, x, tmp);
+    for (int r = threadIdx.x; r < n; r += kBT) Vk[r] = b[r] - tmp[r];
+    __syncthreads();
+    block_sum_max(n, [&](int i) { return Vk[i] * Vk[i]; }, sh, &sum, &mx);
+    const double beta = sqrt(sum);
+    block_sum_max(n, [&](int i) { return x[i] * x[i]; }, sh, &sum, &mx);
+    const double den = nA * sqrt(sum) + nb;
+    const double be = den > 0 ? beta / den : (beta > 0 ? INFINITY : 0.0);
+    *berr = be;
+    if (be <= tol || total >= max_inner || !(be == be) || beta == 0.0) return total;
+    for (int r = threadIdx.x; r < n; r += kBT) Vk[r] /= beta;
+    if (threadIdx.x == 0) {
+      ks.g[0] = beta;
+      for (int k = 1; k <= kKryMax; ++k) ks.g[k] = 0.0;
+    }
+    __syncthreads();
+    int jd = 0;
+    for (int j = 0; j < m && total < max_inner; ++j) {
+      double* zj = Zk + (long)j * n;
+      double* w = Vk + (long)(j + 1) * n;
+      cta_precond<T>(W, n, kind, perm, Vk + (long)j * n, zj);
+      cta_matvec(A, n, zj, w);
+      for (int pass = 0; pass < 2; ++pass) {
+        cta_multi_dot(Vk, n, j + 1, w, n, ks.h);
+        for (int r = threadIdx.x; r < n; r += kBT) {
+          double acc = w[r];
+          for (int i = 0; i <= j; ++i) acc = fma(-ks.h[i], Vk[(long)i * n + r], acc);
+          w[r] = acc;
+        }
+        if (threadIdx.x == 0)
+          for (int i = 0; i <= j; ++i) ks.H[i][j] = (pass ? ks.H[i][j] : 0.0) + ks.h[i];
+        __syncthreads();
+      }
+      block_sum_max(n, [&](int i) { return w[i] * w[i]; }, sh, &sum, &mx);
+      const double hn = sqrt(sum);
+      for (int r = threadIdx.x; r < n; r += kBT) w[r] = hn > 0 ? w[r] / hn : 0.0;
+      if (threadIdx.x == 0) {
+        for (int i = 0; i < j; ++i) {  // previous rotations
+          const double t = ks.cs[i] * ks.H[i][j] + ks.sn[i] * ks.H[i + 1][j];
+          ks.H[i + 1][j] = -ks.sn[i] * ks.H[i][j] + ks.cs[i] * ks.H[i + 1][j];
+          ks.H[i][j] = t;
+        }
+        const double a = ks.H[j][j];
+        const double rr = hypot(a, hn);
+        const double c = rr > 0 ? a / rr : 1.0, sv = rr > 0 ? hn / rr : 0.0;
+        ks.cs[j] = c;
+        ks.sn[j] = sv;
+        ks.H[j][j] = rr;
+        ks.g[j + 1] = -sv * ks.g[j];
+        ks.g[j] = c * ks.g[j];
+        // the least-squares residual estimate is |g_{j+1}|
+        ks.stop = (fabs(ks.g[j + 1]) <= 0.25 * tol * den || hn == 0.0) ? 1 : 0;
+      }
+      __syncthreads();
+      ++total;
+      jd = j + 1;
+      if (ks.stop) break;
+    }
+    if (threadIdx.x == 0) {
+      for (int i = jd - 1; i >= 0; --i) {
+        double acc = ks.g[i];
+        for (int k = i + 1; k < jd; ++k) acc -= ks.H[i][k] * ks.y[k];
+        ks.y[i] = ks.H[i][i] != 0.0 ? acc / ks.H[i][i] : 0.0;
+      }
+    }
+    __syncthreads();
+    for (int r = threadIdx.x; r < n; r += kBT) {
+      double acc = x[r];
+      for (int i = 0; i < jd; ++i) acc = fma(ks.y[i], Zk[(long)i * n + r], acc);
+      x[r] = acc;
+    }
+    __syncthreads();
+  }
+}
+
 template <typename T>
 __device__ int factor_sys(T* W, int n, int kind, int nb, int* piv, Shared& sh, T* smem,
                           int smem_elems, bool lowp) {
@@ -709,27 +1003,73 @@ __device__ int factor_sys(T* W, int n, int kind, int nb, int* piv, Shared& sh, T
 // norm ratios of A, an FP32 LU's growth and pivot spread, and a Hager /
 // Higham 1-norm estimate of ||A^{-1}||_1 (LAPACK xLACON's iteration plus
 // Higham's alternating vector) computed with that FP32 LU.
-__device__ void compute_features(const BatchParams& p, const SysDesc& d, int s, const double* A,
+__device__ __noinline__ void compute_features(const BatchParams& p, const SysDesc& d, int s, const double* A,
                                  int n, double nA, float* Wf, int* piv, int* perm, float* v,
                                  Shared& sh, float* smf) {
   __shared__ float s_fv[16];
   double sum, mx, colmax = 0.0, rowmax = 0.0, amax = 0.0, dsum = 0.0;
-  // column sums (||A||_1), row sums (||A||_inf), max |a|, diagonal weight
-  block_sum_max(n, [&](int j) {
-    double c = 0.0;
-    for (int i = 0; i < n; ++i) c += fabs(A[i + (long)j * n]);
-    return c;
-  }, sh, &sum, &colmax);
-  block_sum_max(n, [&](int i) {
-    double r = 0.0;
-    for (int j = 0; j < n; ++j) r += fabs(A[i + (long)j * n]);
-    return r;
-  }, sh, &sum, &rowmax);
-  block_sum_max(n, [&](int j) {
-    double m = 0.0;
-    for (int i = 0; i < n; ++i) m = fmax(m, fabs(A[i + (long)j * n]));
-    return m;
-  }, sh, &sum, &amax);
+  // column sums (||A||_1) and max |a|: one warp per column (coalesced)
+  {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    double cmax = 0.0, am = 0.0;
+    for (int j = warp; j < n; j += kBT / 32) {
+      double c = 0.0, m = 0.0;
+#pragma unroll 4
+      for (int i = lane; i < n; i += 32) {
+        const double v = fabs(A[i + (long)j * n]);
+        c += v;
+        m = fmax(m, v);
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        c += __shfl_xor_sync(0xffffffffu, c, o);
+        m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+      }
+      cmax = fmax(cmax, c);
+      am = fmax(am, m);
+    }
+    // every lane of warp w holds (cmax, am) of its columns: reduce over warps
+    if (lane == 0) {
+      sh.red[warp][0] = cmax;
+      sh.red[warp][1] = am;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double a = 0.0, b = 0.0;
+      for (int w = 0; w < kBT / 32; ++w) {
+        a = fmax(a, sh.red[w][0]);
+        b = fmax(b, sh.red[w][1]);
+      }
+      sh.colv[0] = a;
+      sh.colv[1] = b;
+    }
+    __syncthreads();
+    colmax = sh.colv[0];
+    amax = sh.colv[1];
+    __syncthreads();
+  }
+  // row sums (||A||_inf): |A| 1 with the GEMV's row blocking
+  {
+    double rmax = 0.0;
+    for (int r0 = 0; r0 < n; r0 += 8 * kBT) {
+      double acc[8];
+      int rr[8];
+#pragma unroll
+      for (int g = 0; g < 8; ++g) {
+        acc[g] = 0.0;
+        const int r = r0 + threadIdx.x + g * kBT;
+        rr[g] = r < n ? r : n - 1;
+      }
+#pragma unroll 2
+      for (int j = 0; j < n; ++j)
+#pragma unroll
+        for (int g = 0; g < 8; ++g) acc[g] += fabs(A[rr[g] + (long)j * n]);
+#pragma unroll
+      for (int g = 0; g < 8; ++g)
+        if (r0 + threadIdx.x + g * kBT < n) rmax = fmax(rmax, acc[g]);
+    }
+    block_sum_max(kBT, [&](int t) { return t == (int)threadIdx.x ? rmax : 0.0; }, sh, &sum,
+                  &rowmax);
+  }
   block_sum_max(n, [&](int i) { return fabs(A[i + (long)i * n]); }, sh, &dsum, &mx);
   // FP32 factorization
   for (long i = threadIdx.x; i < (long)n * n; i += kBT) Wf[i] = (float)A[i];
@@ -768,7 +1108,7 @@ __device__ void compute_features(const BatchParams& p, const SysDesc& d, int s, 
       __syncthreads();
       for (int i = threadIdx.x; i < n; i += kBT) y[i] = z[d.kind == 0 ? perm[i] : i];
       __syncthreads();
-      cta_solve<float>(Wf, n, n, d.kind == 0, y, 1);  // y = A^{-1} x
+      cta_solve<float, float>(Wf, n, n, d.kind == 0, y, 1);  // y = A^{-1} x
       double ny, dum;
       block_sum_max(n, [&](int i) { return fabs((double)y[i]); }, sh, &ny, &dum);
       if (it > 0 && ny <= est) break;
@@ -811,7 +1151,7 @@ __device__ void compute_features(const BatchParams& p, const SysDesc& d, int s, 
       y[i] = (src & 1 ? -1.f : 1.f) * (1.f + (n > 1 ? (float)src / (n - 1) : 0.f));
     }
     __syncthreads();
-    cta_solve<float>(Wf, n, n, d.kind == 0, y, 1);
+    cta_solve<float, float>(Wf, n, n, d.kind == 0, y, 1);
     double ny, dum;
     block_sum_max(n, [&](int i) { return fabs((double)y[i]); }, sh, &ny, &dum);
     est2 = 2.0 * ny / (3.0 * n);
@@ -849,7 +1189,7 @@ __device__ void compute_features(const BatchParams& p, const SysDesc& d, int s, 
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(kBT)
+__global__ void __launch_bounds__(kBT, 1)
 batched_solve_kernel(BatchParams p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ Shared sh;
@@ -864,6 +1204,8 @@ batched_solve_kernel(BatchParams p) {
   double* R = p.vec + cta * (long)p.nmax * p.q * 3;
   double* Xprev = R + (long)p.nmax * p.q;
   double* V = Xprev + (long)p.nmax * p.q;  // solve vector, as float or double
+  double* kry = p.kry + cta * (long)(2 * p.kry_m + 2) * p.nmax;
+  __shared__ KryShared ks;
   const int q = p.q;
   while (true) {
     __syncthreads();
@@ -878,6 +1220,11 @@ batched_solve_kernel(BatchParams p) {
     const double* B = p.B + d.b_off;
     double* X = p.X + d.b_off;
     BatchResult res{};
+    const unsigned long long t_begin = globaltimer_ns();
+    if (threadIdx.x < 8) sh.ph[threadIdx.x] = 0ull;
+    auto mark = [&](int i, unsigned long long since) {  // thread 0, after a barrier
+      if (threadIdx.x == 0) sh.ph[i] += globaltimer_ns() - since;
+    };
     {  // ||A||_F
       double acc = 0.0;
       for (long i = threadIdx.x; i < (long)n * n; i += kBT) acc = fma(A[i], A[i], acc);
@@ -896,15 +1243,24 @@ batched_solve_kernel(BatchParams p) {
     if (p.mode == 1) {
       compute_features(p, d, s, A, n, nA, Wf, piv, perm, reinterpret_cast<float*>(V), sh,
                        reinterpret_cast<float*>(smem_raw));
+      __syncthreads();
+      mark(7, t_begin);
+      if (p.phase_ns && threadIdx.x < 8) p.phase_ns[(long)s * 8 + threadIdx.x] = sh.ph[threadIdx.x];
       continue;
     }
-    if (d.prec >= 1) {
-      // FP32 factors (BF16 operand products for prec 2) + FP64 refinement
+    // precision chosen at run time (the selector's output) or at plan time
+    int prec = d.prec;
+    if (p.prec_dev) prec = min(max(p.prec_dev[s], 0), 2);
+    res.prec = prec;  // becomes the precision the result came from
+    // low-precision attempts: BF16 (if chosen), then FP32 when falling back
+    for (int pr = prec; pr >= 1 && !done; --pr) {
+      if (pr != prec && !p.fallback) break;
+      // FP32 factors (BF16 operand products for pr 2) + FP64 refinement
       float* smf = reinterpret_cast<float*>(smem_raw);
       for (long i = threadIdx.x; i < (long)n * n; i += kBT) Wf[i] = (float)A[i];
       __syncthreads();
       const int info = factor_sys<float>(Wf, n, d.kind, d.nb, piv, sh, smf,
-                                         kSmemPanel / (int)sizeof(float), d.prec == 2);
+                                         kSmemPanel / (int)sizeof(float), pr == 2);
       res.info = info;
       if (info == 0) {
         if (d.kind == 0)
@@ -913,7 +1269,9 @@ batched_solve_kernel(BatchParams p) {
         else
           cta_mirror_lower(Wf, n, n);
         float* vf = reinterpret_cast<float*>(V);
+        const unsigned long long t_ir = globaltimer_ns();
         cta_apply_inverse<float>(Wf, n, d.kind, perm, B, X, vf, nullptr, q, false, s_sc);
+        const int lu_its = p.method == 2 ? 0 : p.max_iters;
         double prev = INFINITY;
         for (int it = 0;; ++it) {
           const double be = sys_berr(A, n, X, B, R, q, sh, nA);
@@ -928,22 +1286,56 @@ batched_solve_kernel(BatchParams p) {
           res.iters = it;
           if (be <= p.tol) {
             done = true;
+            res.prec = pr;
             break;
           }
-          if (it >= p.max_iters) break;
+          if (it >= lu_its) break;
           prev = be;
           for (int i = threadIdx.x; i < n * q; i += kBT) Xprev[i] = X[i];
           cta_apply_inverse<float>(Wf, n, d.kind, perm, R, X, vf, nullptr, q, true, s_sc);
         }
+        __syncthreads();
+        mark(4, t_ir);
+        const int kry_budget = p.kry_max > 0 ? p.kry_max : max(p.kry_m, n / 6);
+        if (!done && p.method != 1) {
+          const unsigned long long t_kr = globaltimer_ns();
+          // LU-IR stalled (or was skipped): FGMRES-IR per right-hand side
+          // from the best iterate, kept only if it lowers the backward error
+          for (int i = threadIdx.x; i < n * q; i += kBT) Xprev[i] = X[i];
+          __syncthreads();
+          int used = 0;
+          for (int c = 0; c < q; ++c) {
+            double bc;
+            used += cta_fgmres<float>(A, n, nA, Wf, d.kind, perm, B + (long)c * n,
+                                      X + (long)c * n, kry, p.kry_m, kry_budget, p.tol, vf, sh,
+                                      ks, &bc);
+          }
+          res.gmres_iters = used;
+          const double be = sys_berr(A, n, X, B, R, q, sh, nA);
+          if (be < res.berr) {
+            res.berr = be;
+            done = be <= p.tol;
+            if (done) res.prec = pr;
+          } else {
+            for (int i = threadIdx.x; i < n * q; i += kBT) X[i] = Xprev[i];
+            __syncthreads();
+          }
+          __syncthreads();
+          mark(5, t_kr);
+        }
       }
     }
-    if (!done && (p.fallback || d.prec == 0)) {
+    if (!done && (p.fallback || prec == 0)) {
       // FP64 factors: the plain path, or the fallback
-      res.fell_back = d.prec >= 1 ? 1 : 0;
+      res.prec = 0;
+      const unsigned long long t_64 = globaltimer_ns();
+      unsigned long long keep[4];
+      for (int i = 0; i < 4; ++i) keep[i] = sh.ph[i];  // the FP64 LU's phases go to 6
       double* smd = reinterpret_cast<double*>(smem_raw);
       for (long i = threadIdx.x; i < (long)n * n; i += kBT) Wd[i] = A[i];
       __syncthreads();
-      const int nb64 = max(1, min(d.nb, (kSmemPanel / 8 - 64 * 64) / max(n, 1)));
+      int nb64 = max(1, min(d.nb, (kSmemPanel / 8 - 64 * 64) / max(n, 1)));
+      if (nb64 > 8) nb64 = nb64 / 8 * 8;
       const int info = factor_sys<double>(Wd, n, d.kind, nb64, piv, sh, smd,
                                           kSmemPanel / (int)sizeof(double), false);
       res.info = info;
@@ -957,9 +1349,17 @@ batched_solve_kernel(BatchParams p) {
       }
       res.berr = sys_berr(A, n, X, B, R, q, sh, nA);
       done = res.berr <= p.tol;
+      __syncthreads();
+      if (threadIdx.x == 0)
+        for (int i = 0; i < 4; ++i) sh.ph[i] = keep[i];
+      mark(6, t_64);
     }
     res.converged = done ? 1 : 0;
+    res.fell_back = (res.prec != prec) ? 1 : 0;
+    res.ns = (long long)(globaltimer_ns() - t_begin);
     if (threadIdx.x == 0) p.out[s] = res;
+    __syncthreads();
+    if (p.phase_ns && threadIdx.x < 8) p.phase_ns[(long)s * 8 + threadIdx.x] = sh.ph[threadIdx.x];
   }
 }
 
@@ -977,6 +1377,7 @@ struct BatchPlan {
   double* d_wsd = nullptr;
   int* d_piv = nullptr;
   double* d_vec = nullptr;
+  double* d_kry = nullptr;
   unsigned* d_ticket = nullptr;
   BatchResult* d_out = nullptr;
   int grid = 0;
@@ -993,20 +1394,28 @@ static int pick_nb(int n, int prec, const int* nb_table) {
   for (int lim = 32; b < 7 && n > lim; lim *= 2) ++b;
   int nb = nb_table ? nb_table[b] : 32;
   if (nb <= 0) nb = 32;
-  const int es = prec == 1 ? 4 : 8;
+  const int es = prec == 0 ? 8 : 4;  // the FP64 path re-caps nb for itself
   // panel (n x nb) plus a 64-column staging tile within the budget
   const int cap = (kSmemPanel / es - 64 * 64) / std::max(n, 1);
   nb = std::min(nb, std::max(cap, 1));
   nb = std::max(1, std::min(nb, 64));
+  if (nb > 8) nb = nb / 8 * 8;  // the register-resident U12 solves take 8 / 16 / 32
   return nb;
 }
 
 cudaError_t batched_plan(Context* ctx, int count, const int* h_n, const int* h_kind,
                          const int* h_prec, int q, const double* A, const double* B, double* X,
                          const int* nb_table, int ctas_per_sm, double tol, int max_iters,
-                         int fallback, int mode, float* feat, BatchPlan** out) {
+                         int fallback, int mode, float* feat, int method, int kry_m,
+                         int kry_max, const int* prec_dev, unsigned long long* phase_ns,
+                         BatchPlan** out) {
   *out = nullptr;
   if (q < 1 || q > kBQ) return cudaErrorInvalidValue;
+  kry_m = kry_m > 0 ? std::min(kry_m, kKryMax) : 30;
+  // <= 0: per-system budget max(kry_m, n / 6) inner iterations, which keeps
+  // FGMRES's FP64 work (2 n^2 per iteration) under half an FP64 LU's
+  kry_max = kry_max > 0 ? kry_max : -1;
+  if (method == 1) kry_m = 1;  // no Krylov workspace beyond a token
   auto* P = new BatchPlan();
   P->ctx = ctx;
   P->count = count;
@@ -1031,11 +1440,13 @@ cudaError_t batched_plan(Context* ctx, int count, const int* h_n, const int* h_k
   P->nmax = nmax;
   std::vector<int> order(count);
   std::iota(order.begin(), order.end(), 0);
-  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-    const double ca = (double)desc[a].n * desc[a].n * desc[a].n * (desc[a].prec == 0 ? 16 : 1);
-    const double cb = (double)desc[b].n * desc[b].n * desc[b].n * (desc[b].prec == 0 ? 16 : 1);
-    return ca > cb;
-  });
+  // largest expected cost first; FP64 arithmetic runs at ~1/60 of the FP32
+  // rate on this GPU (a run-time precision is not known here: n^3 alone)
+  auto cost = [&](const SysDesc& x) {
+    return (double)x.n * x.n * x.n * ((!prec_dev && x.prec == 0) ? 48.0 : 1.0);
+  };
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int a, int b) { return cost(desc[a]) > cost(desc[b]); });
   P->grid = std::max(1, std::min(count, ctx->num_sms * std::max(1, ctas_per_sm)));
   P->ws_elems = (long)nmax * nmax;
   cudaError_t e = cudaSetDevice(ctx->device);
@@ -1045,6 +1456,8 @@ cudaError_t batched_plan(Context* ctx, int count, const int* h_n, const int* h_k
   if (e == cudaSuccess) e = cudaMalloc(&P->d_wsd, sizeof(double) * P->ws_elems * P->grid);
   if (e == cudaSuccess) e = cudaMalloc(&P->d_piv, sizeof(int) * 2 * (long)nmax * P->grid);
   if (e == cudaSuccess) e = cudaMalloc(&P->d_vec, sizeof(double) * 3 * (long)nmax * q * P->grid);
+  if (e == cudaSuccess)
+    e = cudaMalloc(&P->d_kry, sizeof(double) * (2 * (long)kry_m + 2) * nmax * P->grid);
   if (e == cudaSuccess) e = cudaMalloc(&P->d_ticket, sizeof(unsigned));
   if (e == cudaSuccess) e = cudaMalloc(&P->d_out, sizeof(BatchResult) * count);
   if (e == cudaSuccess)
@@ -1076,6 +1489,12 @@ cudaError_t batched_plan(Context* ctx, int count, const int* h_n, const int* h_k
   prm.mode = mode;
   prm.fallback = fallback;
   prm.feat = feat;
+  prm.method = method;
+  prm.kry_m = kry_m;
+  prm.kry_max = kry_max;
+  prm.kry = P->d_kry;
+  prm.prec_dev = prec_dev;
+  prm.phase_ns = phase_ns;
   e = cudaFuncSetAttribute(batched_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            kSmemPanel);
   if (e != cudaSuccess) {
@@ -1126,6 +1545,7 @@ void batched_destroy(BatchPlan* P) {
   cudaFree(P->d_wsd);
   cudaFree(P->d_piv);
   cudaFree(P->d_vec);
+  cudaFree(P->d_kry);
   cudaFree(P->d_ticket);
   cudaFree(P->d_out);
   delete P;
@@ -1156,12 +1576,17 @@ int ElGBBatchedPlanCreate(ElGBContext ctx, int count, const int* n, int nrhs, co
     if (n[i] < 1 || (o.kind && (o.kind[i] < 0 || o.kind[i] > 1)) ||
         (o.precision && (o.precision[i] < 0 || o.precision[i] > 2)))
       return elgb::kElArgError;
+  if (o.method < 0 || o.method > 2 || o.gmres_restart < 0 || o.gmres_restart > 32 ||
+      o.gmres_max_iters < 0)
+    return elgb::kElArgError;
   *plan = nullptr;
   elgb::BatchPlan* p = nullptr;
   cudaError_t e = elgb::batched_plan(static_cast<elgb::Context*>(ctx), count, n, o.kind,
                                      o.precision, nrhs, A, B, X, o.nb_table, o.ctas_per_sm, o.tol,
                                      o.max_iters, o.no_fallback ? 0 : 1,
-                                     o.features_only ? 1 : 0, o.features, &p);
+                                     o.features_only ? 1 : 0, o.features, o.method,
+                                     o.gmres_restart, o.gmres_max_iters, o.precision_device,
+                                     reinterpret_cast<unsigned long long*>(o.phase_ns), &p);
   if (e != cudaSuccess) return e == cudaErrorMemoryAllocation ? elgb::kElAllocError
                                                                : elgb::kElRuntimeError;
   *plan = new ElGBBatchPlanImpl{p};

@@ -10,6 +10,8 @@ namespace elgb {
 struct BatchResult {
   int iters, converged, fell_back, info;
   double berr;
+  int gmres_iters, prec;  // FGMRES iterations; the precision the result came from
+  long long ns;  // device time spent on the system (globaltimer)
 };
 
 struct BatchPlan;
@@ -22,11 +24,19 @@ struct BatchPlan;
 // (n <= 32, 64, ..., 2048, larger), nullptr for 32 everywhere.
 // fallback: FP64 refactorization when refinement does not converge; mode 1
 // computes the selector's 16 features per system into feat instead of
-// solving.
+// solving.  method: 0 LU-IR, then FGMRES-IR (restart kry_m, at most kry_max
+// inner iterations per right-hand side, <= 0: max(kry_m, n / 6)) when LU-IR stalls; 1 LU-IR only;
+// 2 FGMRES-IR only.  prec_dev (device, may be null): per-system precision
+// read when the graph runs, overriding h_prec (the selector's output).
+// phase_ns (device, may be null): count x 8 device times per system: panel,
+// row swaps, U12 solve, trailing update (low-precision factorization),
+// LU-IR, FGMRES-IR, FP64 path, features.
 cudaError_t batched_plan(Context* ctx, int count, const int* h_n, const int* h_kind,
                          const int* h_prec, int q, const double* A, const double* B, double* X,
                          const int* nb_table, int ctas_per_sm, double tol, int max_iters,
-                         int fallback, int mode, float* feat, BatchPlan** out);
+                         int fallback, int mode, float* feat, int method, int kry_m,
+                         int kry_max, const int* prec_dev, unsigned long long* phase_ns,
+                         BatchPlan** out);
 cudaError_t batched_execute(BatchPlan* P);
 cudaError_t batched_results(BatchPlan* P, BatchResult* h_out);
 void batched_destroy(BatchPlan* P);

@@ -6,6 +6,7 @@ can skip the first launch of the kernel it targets).
     python -m elemental_gb300.kernel_cases lu --n 8192 --kind 2
     python -m elemental_gb300.kernel_cases refine --n 8192 --nrhs 16
     python -m elemental_gb300.kernel_cases lu64 --n 4096
+    python -m elemental_gb300.kernel_cases batched --n 1024 --count 152 --precision fp32
 
 Each prints one JSON line with the event-timed duration of the measured
 call and its algorithmic work.  Inputs are seeded N(0, 1), generated on the
@@ -93,7 +94,33 @@ def case_refine(ctx, a):
     return dict(case="refine", n=a.n, nrhs=a.nrhs, method=a.method, ms=ms, **info)
 
 
-CASES = {"tc_gemm": case_tc_gemm, "lu": case_lu, "lu64": case_lu64, "refine": case_refine}
+def case_batched(ctx, a):
+    """`count` N(0, 1) LU systems of order n, one persistent batched launch
+    (warm-up replay, then the measured replay)."""
+    from .batched import BatchedSolver
+    g = torch.Generator(device="cuda").manual_seed(a.seed)
+    A = torch.randn(a.count * a.n * a.n, device="cuda", generator=g, dtype=torch.float64)
+    B = torch.randn(a.count * a.n * a.nrhs, device="cuda", generator=g, dtype=torch.float64)
+    bs = BatchedSolver([a.n] * a.count, a.nrhs, A, B, precisions=[a.precision] * a.count,
+                       fallback=False, method="lu-ir", ctx=ctx, phases=True,
+                       nb_table=[a.nb] * 8 if a.nb else None)
+    bs.run()
+    ms = _timed(bs.run)
+    res = bs.results()
+    dev = [r["device_ms"] for r in res]
+    flops = a.count * 2.0 / 3.0 * a.n ** 3
+    out = dict(case="batched", n=a.n, count=a.count, nrhs=a.nrhs, precision=a.precision, ms=ms,
+               tflops=flops / (ms * 1e-3) / 1e12, converged=sum(r["converged"] for r in res),
+               device_ms_mean=sum(dev) / len(dev), device_ms_max=max(dev),
+               gflops_per_system_cta=2.0 / 3.0 * a.n ** 3 / (sum(dev) / len(dev) * 1e-3) / 1e9,
+               iterations_mean=sum(r["iterations"] for r in res) / len(res),
+               phase_ms_mean={k: round(float(v.mean()), 3) for k, v in bs.phase_ms().items()})
+    bs.close()
+    return out
+
+
+CASES = {"tc_gemm": case_tc_gemm, "lu": case_lu, "lu64": case_lu64, "refine": case_refine,
+         "batched": case_batched}
 
 
 def main(argv=None):
@@ -106,6 +133,8 @@ def main(argv=None):
     p.add_argument("--nb", type=int, default=0)
     p.add_argument("--nrhs", type=int, default=16)
     p.add_argument("--method", default="lu-ir", choices=["lu-ir", "gmres-ir"])
+    p.add_argument("--count", type=int, default=152)
+    p.add_argument("--precision", default="fp32", choices=["fp64", "fp32", "bf16"])
     p.add_argument("--seed", type=int, default=20261204)
     a = p.parse_args(argv)
     ctx = D.context(0)

@@ -157,7 +157,8 @@ int ElGBRefinedSolve_d(ElGBContext ctx, int n, const double* A, int lda,
  *                 1 lower Cholesky (El::Cholesky + cholesky::SolveAfter);
  *                 NULL: all LU
  *   precision[i]  0 FP64 factors, 1 FP32 factors, 2 FP32 storage with BF16
- *                 operand products; 1 and 2 refine with an FP64 residual;
+ *                 operand products; 1 and 2 refine with an FP64 residual
+ *                 and, unless no_fallback, fall back BF16 -> FP32 -> FP64;
  *                 NULL: all FP32
  *   nb_table      8 panel widths for n <= 32, 64, ..., 2048, larger (the
  *                 autotuner's output); NULL: 32
@@ -167,6 +168,10 @@ int ElGBRefinedSolve_d(ElGBContext ctx, int n, const double* A, int lda,
  *   no_fallback   1: report non-convergence instead of refactoring in FP64
  *   features_only 1: write the selector's 16 features per system to
  *                 `features` (count x 16 floats, device) instead of solving
+ *   method        refinement of precision 1/2 factors: 0 LU-IR and, when it
+ *                 stalls, flexible GMRES-IR (FP64 Arnoldi, the factors as
+ *                 preconditioner, El's FGMRES semantics); 1 LU-IR only;
+ *                 2 FGMRES-IR only
  * Execute enqueues the graph on the context's stream; Results synchronizes
  * and copies one ElGBBatchResult per system (features_only: backward_error
  * holds the 1-norm condition estimate). */
@@ -174,6 +179,11 @@ typedef struct ElGBBatchPlanImpl* ElGBBatchPlan;
 typedef struct {
   int iterations, converged, fell_back, info;
   double backward_error;
+  int gmres_iterations;
+  int precision;       /* precision whose factors produced the result (0 FP64,
+                          1 FP32, 2 BF16); fell_back = it differs from the
+                          precision asked for */
+  long long device_ns; /* device time the persistent CTA spent on the system */
 } ElGBBatchResult;
 typedef struct {
   const int* kind;
@@ -185,6 +195,17 @@ typedef struct {
   int no_fallback;
   int features_only;
   float* features;
+  int method;          /* 0 LU-IR then FGMRES-IR on stall, 1 LU-IR, 2 FGMRES-IR */
+  int gmres_restart;   /* FGMRES restart length, <= 32 (0: 30) */
+  int gmres_max_iters; /* FGMRES iterations per right-hand side (0: max(restart,
+                          n / 6), under half the FP64 work of an FP64 LU) */
+  const int* precision_device; /* device int per system, read at each Execute
+                                  (overrides precision; e.g. the selector's
+                                  ElGBMLPForward argmax), or NULL */
+  long long* phase_ns; /* device, count x 8, or NULL: per-system device time of
+                          the low-precision LU's panel, row swaps, U12 solve,
+                          trailing update, then LU-IR, FGMRES-IR, the FP64
+                          path and the feature pass (ns) */
 } ElGBBatchOptions;
 int ElGBBatchedPlanCreate(ElGBContext ctx, int count, const int* n, int nrhs,
                           const double* A, const double* B, double* X,

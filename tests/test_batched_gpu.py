@@ -73,3 +73,93 @@ def test_batched_singular_reports_info(ctx):
     res = bs.results()
     assert res[0]["info"] > 0 and not res[0]["converged"]
     assert res[1]["converged"]
+
+
+def test_batched_fgmres_ir_reaches_target_where_lu_ir_stalls(ctx):
+    """kappa = 1e8 with FP32 factors: kappa * u_fp32 > 1, so LU-IR stalls on
+    some systems; flexible GMRES-IR (FP64 Arnoldi, the FP32 factors as
+    preconditioner) reaches 1e-13 on more of them, fallback switched off."""
+    q = 1
+    systems, kinds = make(12, 64, 200, q, 21, spd_every=1000, kappa=1e8)
+    ns, A, B = BatchedSolver.pack(systems, q)
+    lu_only = BatchedSolver(ns, q, A, B, kinds=kinds, fallback=False, method="lu-ir", ctx=ctx)
+    lu_only.run()
+    n_lu = sum(r["converged"] for r in lu_only.results())
+    lu_only.close()
+    assert n_lu < len(ns)
+    bs = BatchedSolver(ns, q, A, B, kinds=kinds, fallback=False, method="auto", ctx=ctx)
+    bs.run()
+    res = bs.results()
+    assert sum(r["converged"] for r in res) > n_lu
+    for i, ((Ai, Bi), r) in enumerate(zip(systems, res)):
+        assert not r["fell_back"]
+        be = O.backward_error(Ai, bs.solution(i), Bi)
+        assert abs(be - r["backward_error"]) <= 0.05 * be + 1e-18, (i, be, r)
+        if r["converged"]:
+            assert be <= 1e-13, (i, r)
+    assert sum(r["gmres_iterations"] for r in res) > 0
+
+
+def test_batched_fgmres_only_method(ctx):
+    q = 2
+    systems, kinds = make(6, 30, 150, q, 23, spd_every=3, kappa=1e6)
+    ns, A, B = BatchedSolver.pack(systems, q)
+    bs = BatchedSolver(ns, q, A, B, kinds=kinds, fallback=False, method="gmres-ir", ctx=ctx)
+    bs.run()
+    for i, ((Ai, Bi), r) in enumerate(zip(systems, bs.results())):
+        assert r["converged"], (i, r)
+        assert r["iterations"] == 0 and (r["gmres_iterations"] > 0 or r["backward_error"] <= 1e-13)
+        assert O.backward_error(Ai, bs.solution(i), Bi) <= 1e-13
+
+
+def test_batched_runtime_precision_and_cascade(ctx):
+    """Per-system precision read from device memory at run time (the
+    selector's output); with two LU-IR steps allowed, BF16 choices on
+    kappa = 1e13 systems cascade to FP32 and FP64 and still meet the
+    target; `precision` reports the factors the result came from."""
+    import torch
+    q = 1
+    systems, kinds = make(9, 40, 160, q, 25, spd_every=1000, kappa=1e13)
+    ns, A, B = BatchedSolver.pack(systems, q)
+    asked = [0, 1, 2] * 3
+    codes = torch.tensor(asked, dtype=torch.int32, device="cuda")
+    bs = BatchedSolver(ns, q, A, B, kinds=kinds, precision_device=codes, method="lu-ir",
+                       max_iters=2, ctx=ctx)
+    bs.run()
+    res = bs.results()
+    for i, ((Ai, Bi), r) in enumerate(zip(systems, res)):
+        assert r["converged"], (i, r)
+        assert O.backward_error(Ai, bs.solution(i), Bi) <= 1e-13
+        assert r["precision"] <= asked[i]
+        assert r["fell_back"] == (r["precision"] != asked[i])
+    assert any(r["fell_back"] for i, r in enumerate(res) if asked[i] == 2)
+    # a second replay reads the array again
+    codes.fill_(0)
+    bs.run()
+    assert all(r["precision"] == 0 and not r["fell_back"] for r in bs.results())
+
+
+def test_batched_features(ctx):
+    """The selector's features: finite, log2 n exact, and the Hager/Higham
+    estimate of kappa_1 within a small factor of numpy's exact kappa_1 for
+    matrices an FP32 LU resolves."""
+    q = 1
+    rng = np.random.default_rng(3)
+    systems, kinds, kap = [], [], []
+    for i in range(8):
+        n = int(rng.integers(32, 300))
+        k = [1e2, 1e4, 1e5, 1e3][i % 4]
+        systems.append((mats.conditioned(n, k, 500 + i), mats.gaussian(n, q, 600 + i)))
+        kinds.append("lu")
+        kap.append(np.linalg.cond(systems[-1][0], 1))
+    ns, A, B = BatchedSolver.pack(systems, q)
+    bs = BatchedSolver(ns, q, A, B, kinds=kinds, features_only=True, ctx=ctx)
+    bs.run()
+    res = bs.results()
+    F = bs.features.cpu().numpy()
+    assert np.isfinite(F).all()
+    assert np.allclose(F[:, 0], np.log2(ns), atol=1e-5)
+    for i, r in enumerate(res):
+        ratio = r["backward_error"] / kap[i]
+        assert 0.1 <= ratio <= 1.01, (i, ratio)
+        assert abs(F[i, 1] - np.log10(r["backward_error"])) < 1e-3
