@@ -35,7 +35,8 @@ class BatchResult(ctypes.Structure):
     """ElGBBatchResult (include/elgb300.h)."""
     _fields_ = [("iterations", c_int), ("converged", c_int), ("fell_back", c_int),
                 ("info", c_int), ("backward_error", c_double), ("gmres_iterations", c_int),
-                ("precision", c_int), ("device_ns", ctypes.c_longlong)]
+                ("precision", c_int), ("device_ns", ctypes.c_longlong),
+                ("selector_choice", c_int), ("reserved", c_int)]
 
 
 class BatchOptions(ctypes.Structure):
@@ -44,7 +45,8 @@ class BatchOptions(ctypes.Structure):
                 ("ctas_per_sm", c_int), ("tol", c_double), ("max_iters", c_int),
                 ("no_fallback", c_int), ("features_only", c_int), ("features", c_void_p),
                 ("method", c_int), ("gmres_restart", c_int), ("gmres_max_iters", c_int),
-                ("precision_device", c_void_p), ("phase_ns", c_void_p)]
+                ("precision_device", c_void_p), ("phase_ns", c_void_p),
+                ("selector_params", c_void_p)]
 
 
 def _sig(lib, name, res, *args):

@@ -29,7 +29,7 @@ class BatchedSolver:
     def __init__(self, ns, q, A_packed, B_packed, kinds=None, precisions=None, nb_table=None,
                  ctas_per_sm=1, tol=1e-13, max_iters=10, fallback=True, features_only=False,
                  method="auto", gmres_restart=0, gmres_max_iters=0, precision_device=None,
-                 phases=False, ctx: Context | None = None):
+                 phases=False, selector_params=None, ctx: Context | None = None):
         self.ctx = ctx or context()
         self.lib = _lib.load()
         self.ns = np.ascontiguousarray(ns, dtype=np.int32)
@@ -39,7 +39,8 @@ class BatchedSolver:
         self.B = B_packed
         self.X = torch.empty_like(B_packed)
         self.features = (torch.empty(len(ns), 16, dtype=torch.float32, device=A_packed.device)
-                         if features_only else None)
+                         if features_only or selector_params is not None else None)
+        self.selector_params = selector_params
         k = np.ascontiguousarray([KIND[x] for x in kinds] if kinds is not None
                                  else np.zeros(self.count), dtype=np.int32)
         pr = np.ascontiguousarray([PREC[x] for x in precisions] if precisions is not None
@@ -54,7 +55,7 @@ class BatchedSolver:
             k.ctypes.data_as(vp).value, pr.ctypes.data_as(vp).value,
             nbt.ctypes.data_as(vp).value if nbt is not None else None, int(ctas_per_sm),
             float(tol), int(max_iters), 0 if fallback else 1, 1 if features_only else 0,
-            self.features.data_ptr() if features_only else None, METHOD[method],
+            self.features.data_ptr() if self.features is not None else None, METHOD[method],
             int(gmres_restart), int(gmres_max_iters),
             precision_device.data_ptr() if precision_device is not None else None,
             None)
@@ -64,6 +65,8 @@ class BatchedSolver:
             self.phase_ns = torch.zeros(self.count, 8, dtype=torch.int64,
                                         device=A_packed.device)
             opt.phase_ns = self.phase_ns.data_ptr()
+        if selector_params is not None:
+            opt.selector_params = selector_params.data_ptr()
         self._keep = (k, pr, nbt)
         rc = self.lib.ElGBBatchedPlanCreate(
             self.ctx.h, self.count, self.ns.ctypes.data_as(vp), q, vp(self.A.data_ptr()),
@@ -96,7 +99,8 @@ class BatchedSolver:
         return [dict(iterations=r.iterations, converged=bool(r.converged),
                      fell_back=bool(r.fell_back), info=r.info,
                      backward_error=r.backward_error, gmres_iterations=r.gmres_iterations,
-                     precision=r.precision, device_ms=r.device_ns * 1e-6) for r in out]
+                     precision=r.precision, device_ms=r.device_ns * 1e-6,
+                     selector_choice=r.selector_choice) for r in out]
 
     PHASES = ("panel", "swaps", "u12_solve", "trailing_update", "lu_ir", "fgmres_ir",
               "fp64_path", "features")

@@ -30,6 +30,7 @@
 #include "../../include/elgb300.h"
 #include "batched.h"
 #include "driver.h"
+#include "mlp_device.cuh"
 
 namespace elgb {
 
@@ -49,6 +50,8 @@ struct Shared {
   // 0 panel, 1 row swaps, 2 U12 solve, 3 trailing update, 4 LU-IR,
   // 5 FGMRES-IR, 6 FP64 path, 7 features
   unsigned long long ph[8];
+  float feat[16];                     // the selector's features of the system
+  float h1[64], h2[64], lg[4];        // the selector network's activations
   double red[kBT / 32][kBQ + 1];
   double colv[kBQ + 1];
   int ival[4];
@@ -681,7 +684,7 @@ struct BatchParams {
   int max_iters;
   unsigned* ticket;
   BatchResult* out;
-  int mode;          // 0 solve, 1 features only
+  int mode;          // 0 solve, 1 features only, 2 features -> selector -> solve
   int fallback;      // FP64 refactorization when refinement does not converge
   float* feat;       // mode 1: count x 16 features
   int method;        // 0 LU-IR then FGMRES-IR on stall, 1 LU-IR only, 2 FGMRES-IR only
@@ -690,6 +693,7 @@ struct BatchParams {
   double* kry;       // per CTA: (2 kry_m + 2) x n_max doubles (V, Z, scratch)
   const int* prec_dev;  // per-system precision read at run time (or null)
   unsigned long long* phase_ns;  // count x 8 phase times (or null)
+  const float* mlp;  // mode 2: the selector network's parameters
 };
 
 // Y = B - A X (B != null) or Y = A X (B == null) for the n x q block X (all
@@ -1003,7 +1007,7 @@ __device__ int factor_sys(T* W, int n, int kind, int nb, int* piv, Shared& sh, T
 // norm ratios of A, an FP32 LU's growth and pivot spread, and a Hager /
 // Higham 1-norm estimate of ||A^{-1}||_1 (LAPACK xLACON's iteration plus
 // Higham's alternating vector) computed with that FP32 LU.
-__device__ __noinline__ void compute_features(const BatchParams& p, const SysDesc& d, int s, const double* A,
+__device__ __noinline__ int compute_features(const BatchParams& p, const SysDesc& d, int s, const double* A,
                                  int n, double nA, float* Wf, int* piv, int* perm, float* v,
                                  Shared& sh, float* smf) {
   __shared__ float s_fv[16];
@@ -1179,7 +1183,8 @@ __device__ __noinline__ void compute_features(const BatchParams& p, const SysDes
     for (int k = 0; k < 16; ++k) {
       float f = s_fv[k];
       if (!(f == f) || f > 1e30f || f < -1e30f) f = 0.f;  // keep features finite
-      p.feat[(long)s * 16 + k] = f;
+      sh.feat[k] = f;
+      if (p.feat) p.feat[(long)s * 16 + k] = f;
     }
     BatchResult r{};
     r.info = info;
@@ -1187,6 +1192,7 @@ __device__ __noinline__ void compute_features(const BatchParams& p, const SysDes
     p.out[s] = r;
   }
   __syncthreads();
+  return info;
 }
 
 __global__ void __launch_bounds__(kBT, 1)
@@ -1251,23 +1257,43 @@ batched_solve_kernel(BatchParams p) {
     // precision chosen at run time (the selector's output) or at plan time
     int prec = d.prec;
     if (p.prec_dev) prec = min(max(p.prec_dev[s], 0), 2);
+    bool have32 = false;  // FP32 factors of this system already in Wf
+    if (p.mode == 2) {
+      // fused selection: features from an FP32 LU (kept), the network's
+      // choice, then the solve -- a low-precision choice refines with the
+      // FP32 factors just computed (they are at least as good as BF16's)
+      const int finfo = compute_features(p, d, s, A, n, nA, Wf, piv, perm,
+                                         reinterpret_cast<float*>(V), sh,
+                                         reinterpret_cast<float*>(smem_raw));
+      __syncthreads();
+      mark(7, t_begin);
+      prec = mlpd::block_argmax(p.mlp, sh.feat, sh.h1, sh.h2, sh.lg);
+      res.choice = prec;
+      have32 = finfo == 0;
+    }
     res.prec = prec;  // becomes the precision the result came from
     // low-precision attempts: BF16 (if chosen), then FP32 when falling back
     for (int pr = prec; pr >= 1 && !done; --pr) {
       if (pr != prec && !p.fallback) break;
+      if (have32 && pr != prec) break;  // the kept FP32 factors were the attempt
       // FP32 factors (BF16 operand products for pr 2) + FP64 refinement
       float* smf = reinterpret_cast<float*>(smem_raw);
-      for (long i = threadIdx.x; i < (long)n * n; i += kBT) Wf[i] = (float)A[i];
-      __syncthreads();
-      const int info = factor_sys<float>(Wf, n, d.kind, d.nb, piv, sh, smf,
-                                         kSmemPanel / (int)sizeof(float), pr == 2);
+      int info = 0;
+      if (!have32) {
+        for (long i = threadIdx.x; i < (long)n * n; i += kBT) Wf[i] = (float)A[i];
+        __syncthreads();
+        info = factor_sys<float>(Wf, n, d.kind, d.nb, piv, sh, smf,
+                                 kSmemPanel / (int)sizeof(float), pr == 2);
+        if (info == 0) {
+          if (d.kind == 0)
+            cta_perm_from_swaps(piv, n, perm, reinterpret_cast<int*>(smem_raw),
+                                kSmemPanel / (int)sizeof(int));
+          else
+            cta_mirror_lower(Wf, n, n);
+        }
+      }
       res.info = info;
       if (info == 0) {
-        if (d.kind == 0)
-          cta_perm_from_swaps(piv, n, perm, reinterpret_cast<int*>(smem_raw),
-                              kSmemPanel / (int)sizeof(int));
-        else
-          cta_mirror_lower(Wf, n, n);
         float* vf = reinterpret_cast<float*>(V);
         const unsigned long long t_ir = globaltimer_ns();
         cta_apply_inverse<float>(Wf, n, d.kind, perm, B, X, vf, nullptr, q, false, s_sc);
@@ -1408,7 +1434,7 @@ cudaError_t batched_plan(Context* ctx, int count, const int* h_n, const int* h_k
                          const int* nb_table, int ctas_per_sm, double tol, int max_iters,
                          int fallback, int mode, float* feat, int method, int kry_m,
                          int kry_max, const int* prec_dev, unsigned long long* phase_ns,
-                         BatchPlan** out) {
+                         const float* mlp, BatchPlan** out) {
   *out = nullptr;
   if (q < 1 || q > kBQ) return cudaErrorInvalidValue;
   kry_m = kry_m > 0 ? std::min(kry_m, kKryMax) : 30;
@@ -1486,7 +1512,8 @@ cudaError_t batched_plan(Context* ctx, int count, const int* h_n, const int* h_k
   prm.max_iters = max_iters > 0 ? max_iters : 10;
   prm.ticket = P->d_ticket;
   prm.out = P->d_out;
-  prm.mode = mode;
+  prm.mode = (mode == 0 && mlp) ? 2 : mode;
+  prm.mlp = mlp;
   prm.fallback = fallback;
   prm.feat = feat;
   prm.method = method;
@@ -1586,7 +1613,8 @@ int ElGBBatchedPlanCreate(ElGBContext ctx, int count, const int* n, int nrhs, co
                                      o.max_iters, o.no_fallback ? 0 : 1,
                                      o.features_only ? 1 : 0, o.features, o.method,
                                      o.gmres_restart, o.gmres_max_iters, o.precision_device,
-                                     reinterpret_cast<unsigned long long*>(o.phase_ns), &p);
+                                     reinterpret_cast<unsigned long long*>(o.phase_ns),
+                                     o.selector_params, &p);
   if (e != cudaSuccess) return e == cudaErrorMemoryAllocation ? elgb::kElAllocError
                                                                : elgb::kElRuntimeError;
   *plan = new ElGBBatchPlanImpl{p};

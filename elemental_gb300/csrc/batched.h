@@ -12,6 +12,7 @@ struct BatchResult {
   double berr;
   int gmres_iters, prec;  // FGMRES iterations; the precision the result came from
   long long ns;  // device time spent on the system (globaltimer)
+  int choice, pad2;  // fused selection: the network's class (else 0)
 };
 
 struct BatchPlan;
@@ -30,13 +31,15 @@ struct BatchPlan;
 // read when the graph runs, overriding h_prec (the selector's output).
 // phase_ns (device, may be null): count x 8 device times per system: panel,
 // row swaps, U12 solve, trailing update (low-precision factorization),
-// LU-IR, FGMRES-IR, FP64 path, features.
+// LU-IR, FGMRES-IR, FP64 path, features.  mlp (device, may be null): with
+// mode 0, fused selection -- each system's features (FP32 LU kept), the
+// network's class, then the solve with that precision.
 cudaError_t batched_plan(Context* ctx, int count, const int* h_n, const int* h_kind,
                          const int* h_prec, int q, const double* A, const double* B, double* X,
                          const int* nb_table, int ctas_per_sm, double tol, int max_iters,
                          int fallback, int mode, float* feat, int method, int kry_m,
                          int kry_max, const int* prec_dev, unsigned long long* phase_ns,
-                         BatchPlan** out);
+                         const float* mlp, BatchPlan** out);
 cudaError_t batched_execute(BatchPlan* P);
 cudaError_t batched_results(BatchPlan* P, BatchResult* h_out);
 void batched_destroy(BatchPlan* P);

@@ -306,6 +306,41 @@ def kappa_rule(log10_kappa, t_bf16, t_fp32):
 THEORY_THRESHOLDS = (1.0 / UNIT_ROUNDOFF["bf16"], 1.0 / UNIT_ROUNDOFF["fp32"])
 
 
+def rule_network(t_bf16, t_fp32, slope=1e4, device="cuda"):
+    """The kappa-threshold rule written as parameters of the same 16-64-64-3
+    network, so that it runs through the identical fused select-and-solve
+    launch: with f = features[1] = log10 kappa_est, a = log10 t_bf16,
+    b = log10 t_fp32, h0 = relu(f - a), h1 = relu(f - b) and logits
+    (FP64, FP32, BF16) = (-2 + 2 M h1, -1, -M h0).  The argmax is BF16 for
+    f < a, FP32 for a < f < b and FP64 for f > b, exactly except within
+    1/M decades of a threshold."""
+    a, b = float(np.log10(t_bf16)), float(np.log10(t_fp32))
+    W1 = np.zeros((16, 64)); b1 = np.zeros(64)
+    W1[LOG10_KAPPA_FEATURE, 0] = 1.0; b1[0] = -a
+    W1[LOG10_KAPPA_FEATURE, 1] = 1.0; b1[1] = -b
+    W2 = np.zeros((64, 64)); b2 = np.zeros(64)
+    W2[0, 0] = 1.0; W2[1, 1] = 1.0
+    W3 = np.zeros((64, 3)); b3 = np.array([-2.0, -1.0, 0.0])
+    W3[1, 0] = 2.0 * slope
+    W3[0, 2] = -slope
+    th = np.concatenate([W1.ravel(), b1, W2.ravel(), b2, W3.ravel(), b3]).astype(np.float32)
+    return torch.from_numpy(th).to(device)
+
+
+def solve_selected(systems, params, ctx=None, nb_table=None, tol=1e-13, phases=False):
+    """The fused select-and-solve launch: per system, features from an FP32
+    LU (kept), the network `params`' class, then the solve in that
+    precision (BF16 / FP32 classes refine with the kept FP32 factors, FP64
+    refactors; refinement that stalls falls back to FP64).  Returns
+    (results, ms, solver) -- close() the solver when done."""
+    ctx = ctx or context()
+    solver = BatchedSolver(systems["ns"], systems["nrhs"], systems["A"], systems["B"],
+                           selector_params=params, nb_table=nb_table, tol=tol, phases=phases,
+                           ctx=ctx)
+    ms = _timed(ctx, solver.run)
+    return solver.results(), ms, solver
+
+
 def fit_kappa_rule(log10_kappa, labels):
     """Best fixed thresholds (label accuracy) on training data, over a grid
     of 0.25-decade steps."""

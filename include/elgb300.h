@@ -184,6 +184,9 @@ typedef struct {
                           1 FP32, 2 BF16); fell_back = it differs from the
                           precision asked for */
   long long device_ns; /* device time the persistent CTA spent on the system */
+  int selector_choice; /* fused selection: the network's class (0 FP64, 1 FP32,
+                          2 BF16); otherwise 0 */
+  int reserved;
 } ElGBBatchResult;
 typedef struct {
   const int* kind;
@@ -206,6 +209,13 @@ typedef struct {
                           the low-precision LU's panel, row swaps, U12 solve,
                           trailing update, then LU-IR, FGMRES-IR, the FP64
                           path and the feature pass (ns) */
+  const float* selector_params; /* device, ElGBMLPParamCount() floats, or NULL:
+                          fused selection in the same launch -- each
+                          system's features (FP32 LU, kept), the network's
+                          class (ElGBMLPForward's argmax), then the solve in
+                          that precision; a low-precision class refines with
+                          the kept FP32 factors.  `features` (if set) also
+                          receives the features */
 } ElGBBatchOptions;
 int ElGBBatchedPlanCreate(ElGBContext ctx, int count, const int* n, int nrhs,
                           const double* A, const double* B, double* X,
