@@ -46,7 +46,7 @@ class BatchOptions(ctypes.Structure):
                 ("no_fallback", c_int), ("features_only", c_int), ("features", c_void_p),
                 ("method", c_int), ("gmres_restart", c_int), ("gmres_max_iters", c_int),
                 ("precision_device", c_void_p), ("phase_ns", c_void_p),
-                ("selector_params", c_void_p)]
+                ("selector_params", c_void_p), ("simt_update", c_int)]
 
 
 def _sig(lib, name, res, *args):

@@ -29,7 +29,8 @@ class BatchedSolver:
     def __init__(self, ns, q, A_packed, B_packed, kinds=None, precisions=None, nb_table=None,
                  ctas_per_sm=1, tol=1e-13, max_iters=10, fallback=True, features_only=False,
                  method="auto", gmres_restart=0, gmres_max_iters=0, precision_device=None,
-                 phases=False, selector_params=None, ctx: Context | None = None):
+                 phases=False, selector_params=None, simt_update=False,
+                 ctx: Context | None = None):
         self.ctx = ctx or context()
         self.lib = _lib.load()
         self.ns = np.ascontiguousarray(ns, dtype=np.int32)
@@ -62,11 +63,12 @@ class BatchedSolver:
         self.precision_device = precision_device
         self.phase_ns = None
         if phases:
-            self.phase_ns = torch.zeros(self.count, 8, dtype=torch.int64,
+            self.phase_ns = torch.zeros(self.count, len(self.PHASES), dtype=torch.int64,
                                         device=A_packed.device)
             opt.phase_ns = self.phase_ns.data_ptr()
         if selector_params is not None:
             opt.selector_params = selector_params.data_ptr()
+        opt.simt_update = 1 if simt_update else 0
         self._keep = (k, pr, nbt)
         rc = self.lib.ElGBBatchedPlanCreate(
             self.ctx.h, self.count, self.ns.ctypes.data_as(vp), q, vp(self.A.data_ptr()),
@@ -103,7 +105,7 @@ class BatchedSolver:
                      selector_choice=r.selector_choice) for r in out]
 
     PHASES = ("panel", "swaps", "u12_solve", "trailing_update", "lu_ir", "fgmres_ir",
-              "fp64_path", "features")
+              "fp64_path", "features", "ir_residual", "ir_lowprec_solve")
 
     def phase_ms(self):
         """Per-system device time by phase (requires phases=True): dict of

@@ -31,6 +31,7 @@
 #include "batched.h"
 #include "driver.h"
 #include "mlp_device.cuh"
+#include "tcgen05.cuh"
 
 namespace elgb {
 
@@ -38,7 +39,16 @@ namespace {
 
 constexpr int kBT = 256;               // threads per CTA
 constexpr int kBQ = 8;                 // max right-hand sides
-constexpr int kSmemPanel = 160 * 1024; // panel staging budget (bytes)
+constexpr int kPhases = 10;            // per-system timing slots
+constexpr int kSmemPanel = 144 * 1024; // panel staging budget (bytes)
+// tensor-core trailing update (FP32 / BF16 factors): operand tiles after the
+// panel budget, 1024-byte aligned for the 128-byte swizzle
+constexpr int kTcM = 128, kTcN = 128;             // C tile per MMA round
+constexpr int kTcTileA = kTcM * 128;              // one 128-byte K row per M row
+constexpr int kTcTileB = kTcN * 128;
+constexpr int kTcSmem = 2 * kTcTileA + 2 * kTcTileB;  // hi and lo of each: 64 KB
+constexpr int kTcCols = 128;                      // TMEM columns (FP32 accumulator)
+constexpr int kDynSmem = kSmemPanel + kTcSmem + 1024;
 
 struct SysDesc {
   int n, kind, nb, prec;  // kind 0 LU, 1 Cholesky; prec 0 FP64, 1 FP32 + IR
@@ -48,9 +58,14 @@ struct SysDesc {
 struct Shared {
   // per-system device time by phase (thread 0 accumulates, globaltimer ns):
   // 0 panel, 1 row swaps, 2 U12 solve, 3 trailing update, 4 LU-IR,
-  // 5 FGMRES-IR, 6 FP64 path, 7 features
-  unsigned long long ph[8];
+  // 5 FGMRES-IR, 6 FP64 path, 7 features; within 4-5: 8 FP64 residuals and
+  // products, 9 low-precision triangular solves
+  unsigned long long ph[kPhases];
   float feat[16];                     // the selector's features of the system
+  unsigned long long mma_bar;         // tcgen05 commit barrier
+  unsigned mma_phase;                 // its next parity
+  unsigned tmem;                      // TMEM accumulator base
+  int tc_err;                         // a tensor-core wait timed out
   float h1[64], h2[64], lg[4];        // the selector network's activations
   double red[kBT / 32][kBQ + 1];
   double colv[kBQ + 1];
@@ -151,12 +166,12 @@ __device__ __forceinline__ void block_colsum(int n, int q, F f, Shared& sh, doub
 }
 
 // ---- LU --------------------------------------------------------------------
-// Row interchanges of the panel's swaps (rows k+i <-> piv[i], i < jb) on the
-// columns outside [k, k+jb), via the (dst, src) list of changed rows, staged
-// through shared memory in column chunks.
-template <typename T>
-__device__ void cta_apply_swaps(T* W, int n, int ld, int k, int jb, Shared& sh, T* stage,
-                                int stage_elems) {
+// (dst, src) list of the rows changed by the panel's interchanges (rows
+// k + i <-> sh.piv[i], i < jb, in order): after them row dst holds what row
+// src held.  Label replay by thread 0 on the top rows plus a small hash
+// table of the outside rows; cnt in sh.ival[0], dst in sh.pairs[0..),
+// src in sh.pairs[128..).
+__device__ void cta_build_pairs(int k, int jb, Shared& sh) {
   if (threadIdx.x == 0) {
     // replay on labels (top rows + up to jb outside rows in a small table)
     int nk = 0;
@@ -201,23 +216,32 @@ __device__ void cta_apply_swaps(T* W, int n, int ld, int k, int jb, Shared& sh, 
     sh.ival[0] = c;
   }
   __syncthreads();
+}
+
+// The panel's interchanges on the columns right of it ([k + jb, n)); the
+// columns left of it get every later panel's interchanges at once when the
+// factorization ends (cta_lu).
+template <typename T>
+__device__ void cta_apply_swaps(T* W, int n, int ld, int k, int jb, Shared& sh, T* stage,
+                                int stage_elems) {
+  cta_build_pairs(k, jb, sh);
   const int cnt = sh.ival[0];
   if (cnt == 0) return;
-  const int ncols_out = n - jb;
+  const int ncols_out = n - k - jb;
   const int chunk = max(1, stage_elems / cnt);
   for (int c0 = 0; c0 < ncols_out; c0 += chunk) {
     const int cw = min(chunk, ncols_out - c0);
 #pragma unroll 8
     for (int idx = threadIdx.x; idx < cw * cnt; idx += kBT) {
       const int e = idx % cnt, cc = c0 + idx / cnt;
-      const int col = cc < k ? cc : cc + jb;
+      const int col = k + jb + cc;
       stage[idx] = W[sh.pairs[128 + e] + (long)col * ld];
     }
     __syncthreads();
 #pragma unroll 8
     for (int idx = threadIdx.x; idx < cw * cnt; idx += kBT) {
       const int e = idx % cnt, cc = c0 + idx / cnt;
-      const int col = cc < k ? cc : cc + jb;
+      const int col = k + jb + cc;
       W[sh.pairs[e] + (long)col * ld] = stage[idx];
     }
     __syncthreads();
@@ -355,12 +379,168 @@ __device__ void cta_trsm_u12(const T* L, int mp, T* W0, int ld, int jb, int n2, 
   __syncthreads();
 }
 
+// ---- tensor-core trailing update ----------------------------------------------
+// C[m x nc] -= P[m x jb] * Q[jb x nc] on the 5th-generation tensor cores,
+// inside one CTA: P is the panel's A21 in shared memory (ld ldp), Q = U12 and
+// C = A22 in the CTA's global workspace (ld ldq / ldc).  For each 128 x 64
+// C tile the CTA writes the operands into 128-byte-swizzled K-major tiles
+// (the layout TMA's SWIZZLE_128B produces: 8-row groups of 1024 bytes, the
+// 16-byte chunk c of row r stored at chunk c ^ (r & 7)), thread 0 issues
+// tcgen05.mma into a 128 x 64 FP32 accumulator in TMEM and commits to an
+// mbarrier, and all 8 warps read the accumulator back (tcgen05.ld, warp w
+// owns TMEM lanes 32 (w % 4).. and column half w / 4) and subtract it from
+// C, whose loads were issued before the wait.
+//   FP32 factors: TF32 split, C -= Ahi Bhi + Ahi Blo + Alo Bhi (~FP32);
+//   BF16 factors: one kind::f16 pass on BF16 operands (FP32 accumulation).
+// K = jb <= 32 (TF32) or <= 64 (BF16): one 128-byte K row per operand row.
+__device__ __forceinline__ int sw128(int r, int chunk) {
+  return (r >> 3) * 1024 + (r & 7) * 128 + ((chunk ^ (r & 7)) << 4);
+}
+
+__device__ __forceinline__ float tf32_rna(float v) {
+  uint32_t t;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(t) : "f"(v));
+  return __uint_as_float(t);
+}
+
+// 16 bytes of K for operand row r: 4 FP32 (TF32 hi / lo) or 8 BF16 values
+// taken from get(k), zero past jb.
+template <typename G>
+__device__ __forceinline__ void tc_put_chunk(unsigned char* hi, unsigned char* lo, int r,
+                                             int c, int jb, bool bf16, G get) {
+  const int off = sw128(r, c);
+  if (bf16) {
+    __nv_bfloat162 h[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int k = 8 * c + 2 * e;
+      h[e] = __floats2bfloat162_rn(k < jb ? get(k) : 0.f, k + 1 < jb ? get(k + 1) : 0.f);
+    }
+    *reinterpret_cast<uint4*>(hi + off) = *reinterpret_cast<uint4*>(h);
+  } else {
+    float4 vh, vl;
+    float* ph = &vh.x;
+    float* pl = &vl.x;
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int k = 4 * c + e;
+      const float v = k < jb ? get(k) : 0.f;
+      ph[e] = tf32_rna(v);
+      pl[e] = tf32_rna(v - ph[e]);
+    }
+    *reinterpret_cast<float4*>(hi + off) = vh;
+    *reinterpret_cast<float4*>(lo + off) = vl;
+  }
+}
+
+__device__ __noinline__ void cta_gemm_update_tc(const float* P, int ldp, const float* Q,
+                                                int ldq, float* C, int ldc, int m, int nc,
+                                                int jb, bool bf16, Shared& sh,
+                                                unsigned char* tiles) {
+  unsigned char* sAh = tiles;
+  unsigned char* sAl = tiles + kTcTileA;
+  unsigned char* sBh = tiles + 2 * kTcTileA;
+  unsigned char* sBl = sBh + kTcTileB;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int wl = warp & 3, half = warp >> 2;
+  const int kstep = bf16 ? 16 : 8;
+  const int nk = (jb + kstep - 1) / kstep;     // MMAs per pass (32 bytes of K each)
+  const int nchunk = bf16 ? (jb + 7) / 8 : (jb + 3) / 4;
+  const uint32_t idesc = (1u << 4) | ((bf16 ? 1u : 2u) << 7) | ((bf16 ? 1u : 2u) << 10) |
+                         ((uint32_t)(kTcN >> 3) << 17) | ((uint32_t)(kTcM >> 4) << 24);
+  uint32_t phase = sh.mma_phase;
+  const uint32_t tmem = sh.tmem;
+  for (int r0 = 0; r0 < m && !sh.tc_err; r0 += kTcM) {
+    // A tile: rows r0.. of P
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < kTcM * 8; idx += kBT) {
+      const int r = idx >> 3, c = idx & 7;
+      const bool ok = r0 + r < m && c < nchunk;
+      const float* pr = P + r0 + r;
+      tc_put_chunk(sAh, sAl, r, c, ok ? jb : 0, bf16, [&](int k) { return pr[k * ldp]; });
+    }
+    for (int c0 = 0; c0 < nc && !sh.tc_err; c0 += kTcN) {
+      // B tile: columns c0.. of Q (each column's jb values are contiguous)
+      for (int idx = threadIdx.x; idx < kTcN * 8; idx += kBT) {
+        const int j = idx >> 3, c = idx & 7;
+        const bool ok = c0 + j < nc && c < nchunk;
+        const float* qc = Q + (long)(c0 + j) * ldq;
+        tc_put_chunk(sBh, sBl, j, c, ok ? jb : 0, bf16, [&](int k) { return qc[k]; });
+      }
+      // the 2 x 32 C values this thread updates, loaded before the MMAs complete
+      const int row = r0 + 32 * wl + lane;
+      const bool row_ok = row < m;
+      const int cb = c0 + 64 * half;
+      float cv[64];
+#pragma unroll
+      for (int j = 0; j < 64; ++j)
+        cv[j] = (row_ok && cb + j < nc) ? C[row + (long)(cb + j) * ldc] : 0.f;
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      tc::tc_fence_before();
+      __syncthreads();
+      tc::tc_fence_after();
+      if (threadIdx.x == 0) {
+        const uint64_t ah = tc::sdesc_sw128(tc::smem_u32(sAh));
+        const uint64_t al = tc::sdesc_sw128(tc::smem_u32(sAl));
+        const uint64_t bh = tc::sdesc_sw128(tc::smem_u32(sBh));
+        const uint64_t bl = tc::sdesc_sw128(tc::smem_u32(sBl));
+        const int passes = bf16 ? 1 : 3;
+        uint32_t acc = 0;
+        for (int ps = 0; ps < passes; ++ps) {
+          const uint64_t ad = ps == 2 ? al : ah;
+          const uint64_t bd = ps == 1 ? bl : bh;
+          for (int kk = 0; kk < nk; ++kk) {
+            if (bf16)
+              tc::umma<kTcBF16>(tmem, ad + 2 * kk, bd + 2 * kk, idesc, acc);
+            else
+              tc::umma<kTcTF32>(tmem, ad + 2 * kk, bd + 2 * kk, idesc, acc);
+            acc = 1;
+          }
+        }
+        tc::umma_commit(reinterpret_cast<uint64_t*>(&sh.mma_bar));
+      }
+      __syncwarp();
+      // warp-uniform: tcgen05.ld is a whole-warp instruction
+      bool ok = tc::mbar_try_wait(reinterpret_cast<uint64_t*>(&sh.mma_bar), phase);
+      if (!__all_sync(0xffffffffu, ok)) {
+        const unsigned long long t0 = globaltimer_ns();
+        while (true) {
+          ok = tc::mbar_try_wait(reinterpret_cast<uint64_t*>(&sh.mma_bar), phase);
+          if (__all_sync(0xffffffffu, ok)) break;
+          if (globaltimer_ns() - t0 > kSpinLimitNs) {
+            sh.tc_err = 1;
+            break;
+          }
+        }
+      }
+      phase ^= 1u;
+      tc::tc_fence_after();
+      if (__all_sync(0xffffffffu, ok)) {
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          uint32_t a[32];
+          tc::tmem_ld32(tmem + ((uint32_t)(32 * wl) << 16) + (uint32_t)(64 * half + 32 * h), a);
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const int col = cb + 32 * h + j;
+            if (row_ok && col < nc) C[row + (long)col * ldc] = cv[32 * h + j] - __uint_as_float(a[j]);
+          }
+        }
+      }
+      tc::tc_fence_before();
+      __syncthreads();
+    }
+  }
+  if (threadIdx.x == 0) sh.mma_phase = phase;
+  __syncthreads();
+}
+
 // In-CTA LU with partial pivoting of the n x n matrix W (ld), blocked by nb.
 // piv_out[0..n) receives the swap destinations; returns info (0 ok, j+1 at
 // the first zero pivot).
 template <typename T>
 __device__ __noinline__ int cta_lu(T* W, int n, int ld, int nb, int* piv_out, Shared& sh, T* smem,
-                      int smem_elems, bool lowp) {
+                      int smem_elems, bool lowp, unsigned char* tc_tiles) {
   __shared__ T fv[9];
   __shared__ int fr[9];
   int info = 0;
@@ -432,13 +612,79 @@ __device__ __noinline__ int cta_lu(T* W, int n, int ld, int nb, int* piv_out, Sh
       cta_trsm_u12<T>(panel, mp, W + k + (long)(k + jb) * ld, ld, jb, n2, lowp);
       phase(2);
       // A22 -= A21 U12, A21 = panel rows jb.. (still in shared memory)
-      cta_gemm_update<T>(panel + jb, mp, W + k + (long)(k + jb) * ld, ld,
-                         W + (k + jb) + (long)(k + jb) * ld, ld, n2, n2, jb,
-                         smem + mp * jb, lowp);
+      bool done_tc = false;
+      if constexpr (sizeof(T) == 4) {
+        if (tc_tiles && n2 >= 32 && jb <= (lowp ? 64 : 32)) {
+          cta_gemm_update_tc(panel + jb, mp, W + k + (long)(k + jb) * ld, ld,
+                             W + (k + jb) + (long)(k + jb) * ld, ld, n2, n2, jb, lowp, sh,
+                             tc_tiles);
+          done_tc = true;
+        }
+      }
+      if (!done_tc)
+        cta_gemm_update<T>(panel + jb, mp, W + k + (long)(k + jb) * ld, ld,
+                           W + (k + jb) + (long)(k + jb) * ld, ld, n2, n2, jb,
+                           smem + mp * jb, lowp);
     }
     __syncthreads();
     phase(3);
   }
+  // Left columns: each block column b = [kb, kb + jbb) takes the
+  // interchanges of every later panel, composed into one row relabelling
+  // lab (rows >= kb + jbb; the content of row i comes from row lab[i]) and
+  // applied as a gather through shared memory -- coalesced reads and writes
+  // instead of per-panel scattered row swaps.  lab is built from the last
+  // panel backwards: lab <- lambda_b o lab, lambda_b the relabelling of
+  // panel b's own interchanges.
+  {
+    int* lab = reinterpret_cast<int*>(smem);
+    int* pmap = lab + n;
+    T* buf = reinterpret_cast<T*>(pmap + n);  // 2n ints: 8-byte aligned
+    const int cap = (int)((smem_elems * (long)sizeof(T) - 2 * (long)n * sizeof(int)) /
+                          (long)sizeof(T));
+    for (int i = threadIdx.x; i < n; i += kBT) {
+      lab[i] = i;
+      pmap[i] = -1;
+    }
+    __syncthreads();
+    const int last = ((n - 1) / nb) * nb;
+    for (int kb = last; kb >= 0; kb -= nb) {
+      const int jbb = min(nb, n - kb), kn = kb + jbb, rows = n - kn;
+      if (rows > 0 && kb < kn) {
+        const int cw_max = max(1, min(jbb, cap / rows));
+        for (int c0 = kb; c0 < kn; c0 += cw_max) {
+          const int cw = min(cw_max, kn - c0);
+          for (int idx = threadIdx.x; idx < cw * rows; idx += kBT) {
+            const int i = idx % rows, c = idx / rows;
+            buf[idx] = W[(kn + i) + (long)(c0 + c) * ld];
+          }
+          __syncthreads();
+          for (int idx = threadIdx.x; idx < cw * rows; idx += kBT) {
+            const int i = idx % rows, c = idx / rows;
+            const int src = lab[kn + i] - kn;
+            if (src != i) W[(kn + i) + (long)(c0 + c) * ld] = buf[src + c * rows];
+          }
+          __syncthreads();
+        }
+      }
+      // fold panel b's interchanges into lab
+      for (int j = threadIdx.x; j < jbb; j += kBT) sh.piv[j] = piv_out[kb + j];
+      __syncthreads();
+      cta_build_pairs(kb, jbb, sh);
+      const int cnt = sh.ival[0];
+      for (int e = threadIdx.x; e < cnt; e += kBT) pmap[sh.pairs[e]] = e;
+      __syncthreads();
+      for (int i = threadIdx.x; i < n; i += kBT) {
+        const int x = lab[i];
+        const int e = pmap[x];
+        if (e >= 0) lab[i] = sh.pairs[128 + e];
+      }
+      __syncthreads();
+      for (int e = threadIdx.x; e < cnt; e += kBT) pmap[sh.pairs[e]] = -1;
+      __syncthreads();
+    }
+  }
+  phase(1);
   return info;
 }
 
@@ -556,6 +802,57 @@ __device__ void cta_perm_from_swaps(const int* piv, int n, int* perm, int* lab_s
   __syncthreads();
 }
 
+// x[r, c] -= sum_{jj < jb} W[r, j0 + jj] x[j0 + jj, c] for rows r in
+// [r_lo, r_hi): eight rows per thread at a time, so every jj step has eight
+// independent coalesced loads of W in flight.
+template <int RG, typename S, typename T>
+__device__ __forceinline__ void cta_solve_rows_g(const S* W, int ld, T* x, int n, int q, int j0,
+                                                 int jb, int r_lo, int r_hi) {
+  const int rows = r_hi - r_lo;
+  if (rows <= 0) return;
+  for (int c = 0; c < q; ++c) {
+    T* xc = x + (long)c * n;
+    const T* xb = xc + j0;
+    for (int b0 = 0; b0 < rows; b0 += RG * kBT) {
+      T acc[RG];
+      int rr[RG];
+#pragma unroll
+      for (int g = 0; g < RG; ++g) {
+        const int i = b0 + threadIdx.x + g * kBT;
+        rr[g] = r_lo + (i < rows ? i : rows - 1);  // clamped: loads stay in bounds
+        acc[g] = T(0);
+      }
+#pragma unroll 4
+      for (int jj = 0; jj < jb; ++jj) {
+        const T xv = xb[jj];
+        const S* wc = W + (long)(j0 + jj) * ld;
+#pragma unroll
+        for (int g = 0; g < RG; ++g) acc[g] = fma(-(T)wc[rr[g]], xv, acc[g]);
+      }
+#pragma unroll
+      for (int g = 0; g < RG; ++g) {
+        const int i = b0 + threadIdx.x + g * kBT;
+        if (i < rows) xc[r_lo + i] += acc[g];
+      }
+    }
+  }
+}
+
+// RG matched to the row count: no idle duplicate loads on short columns.
+template <typename S, typename T>
+__device__ __forceinline__ void cta_solve_rows(const S* W, int ld, T* x, int n, int q, int j0,
+                                               int jb, int r_lo, int r_hi) {
+  const int rows = r_hi - r_lo;
+  if (rows <= kBT)
+    cta_solve_rows_g<1>(W, ld, x, n, q, j0, jb, r_lo, r_hi);
+  else if (rows <= 2 * kBT)
+    cta_solve_rows_g<2>(W, ld, x, n, q, j0, jb, r_lo, r_hi);
+  else if (rows <= 4 * kBT)
+    cta_solve_rows_g<4>(W, ld, x, n, q, j0, jb, r_lo, r_hi);
+  else
+    cta_solve_rows_g<8>(W, ld, x, n, q, j0, jb, r_lo, r_hi);
+}
+
 // x := U^{-1} L^{-1} x for n x q x (ld n): L lower (unit or not), U upper
 // (non-unit) both in W (for Cholesky U = L^T has been written to the upper
 // triangle).  Factors stored as S, arithmetic in T (T = double with S =
@@ -565,9 +862,13 @@ __device__ void cta_perm_from_swaps(const int* piv, int n, int* perm, int* lab_s
 // the block are updated by all threads.
 template <typename S, typename T>
 __device__ __noinline__ void cta_solve(const S* W, int n, int ld, bool unit_lower, T* x, int q) {
-  __shared__ T sdg[32][33];
+  // the 32 x 32 diagonal block, staged at the start of the dynamic shared
+  // memory (the panel region, unused once a factorization is done)
+  extern __shared__ __align__(16) unsigned char smem_dyn[];
+  T(*sdg)[33] = reinterpret_cast<T(*)[33]>(smem_dyn);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   auto stage = [&](int j0, int jb) {
+    __syncthreads();  // the previous block's readers are done
     for (int idx = threadIdx.x; idx < 32 * 32; idx += kBT) {
       const int r = idx & 31, c = idx >> 5;
       sdg[r][c] = (r < jb && c < jb) ? (T)W[(j0 + r) + (long)(j0 + c) * ld] : T(0);
@@ -588,14 +889,7 @@ __device__ __noinline__ void cta_solve(const S* W, int n, int ld, bool unit_lowe
       if (lane < jb) xc[j0 + lane] = v;
     }
     __syncthreads();
-    for (int idx = threadIdx.x; idx < (n - j0 - jb) * q; idx += kBT) {
-      const int r = j0 + jb + idx % (n - j0 - jb), c = idx / (n - j0 - jb);
-      T acc = x[r + (long)c * n];
-      const T* xb = x + j0 + (long)c * n;
-#pragma unroll 8
-      for (int jj = 0; jj < jb; ++jj) acc = fma(-(T)W[r + (long)(j0 + jj) * ld], xb[jj], acc);
-      x[r + (long)c * n] = acc;
-    }
+    cta_solve_rows(W, ld, x, n, q, j0, jb, j0 + jb, n);
     __syncthreads();
   }
   for (int j0 = ((n - 1) / 32) * 32; j0 >= 0; j0 -= 32) {
@@ -612,14 +906,7 @@ __device__ __noinline__ void cta_solve(const S* W, int n, int ld, bool unit_lowe
       if (lane < jb) xc[j0 + lane] = v;
     }
     __syncthreads();
-    for (int idx = threadIdx.x; idx < j0 * q; idx += kBT) {
-      const int r = idx % j0, c = idx / j0;
-      T acc = x[r + (long)c * n];
-      const T* xb = x + j0 + (long)c * n;
-#pragma unroll 8
-      for (int jj = 0; jj < jb; ++jj) acc = fma(-(T)W[r + (long)(j0 + jj) * ld], xb[jj], acc);
-      x[r + (long)c * n] = acc;
-    }
+    cta_solve_rows(W, ld, x, n, q, j0, jb, 0, j0);
     __syncthreads();
   }
 }
@@ -692,8 +979,10 @@ struct BatchParams {
   int kry_max;       // FGMRES inner iterations per right-hand side
   double* kry;       // per CTA: (2 kry_m + 2) x n_max doubles (V, Z, scratch)
   const int* prec_dev;  // per-system precision read at run time (or null)
-  unsigned long long* phase_ns;  // count x 8 phase times (or null)
+  unsigned long long* phase_ns;  // count x kPhases phase times (or null)
   const float* mlp;  // mode 2: the selector network's parameters
+  int tc;            // 1: FP32 / BF16 trailing updates on the tensor cores
+  int* err;          // set when a tensor-core wait timed out
 };
 
 // Y = B - A X (B != null) or Y = A X (B == null) for the n x q block X (all
@@ -998,8 +1287,9 @@ __device__ __noinline__ int cta_fgmres(const double* A, int n, double nA, const 
 
 template <typename T>
 __device__ int factor_sys(T* W, int n, int kind, int nb, int* piv, Shared& sh, T* smem,
+                          unsigned char* tc_tiles,
                           int smem_elems, bool lowp) {
-  return kind == 0 ? cta_lu<T>(W, n, n, nb, piv, sh, smem, smem_elems, lowp)
+  return kind == 0 ? cta_lu<T>(W, n, n, nb, piv, sh, smem, smem_elems, lowp, tc_tiles)
                    : cta_chol<T>(W, n, n, nb, smem, lowp);
 }
 
@@ -1009,7 +1299,7 @@ __device__ int factor_sys(T* W, int n, int kind, int nb, int* piv, Shared& sh, T
 // Higham's alternating vector) computed with that FP32 LU.
 __device__ __noinline__ int compute_features(const BatchParams& p, const SysDesc& d, int s, const double* A,
                                  int n, double nA, float* Wf, int* piv, int* perm, float* v,
-                                 Shared& sh, float* smf) {
+                                 Shared& sh, float* smf, unsigned char* tc_tiles) {
   __shared__ float s_fv[16];
   double sum, mx, colmax = 0.0, rowmax = 0.0, amax = 0.0, dsum = 0.0;
   // column sums (||A||_1) and max |a|: one warp per column (coalesced)
@@ -1078,7 +1368,7 @@ __device__ __noinline__ int compute_features(const BatchParams& p, const SysDesc
   // FP32 factorization
   for (long i = threadIdx.x; i < (long)n * n; i += kBT) Wf[i] = (float)A[i];
   __syncthreads();
-  const int info = factor_sys<float>(Wf, n, d.kind, d.nb, piv, sh, smf,
+  const int info = factor_sys<float>(Wf, n, d.kind, d.nb, piv, sh, smf, p.tc ? tc_tiles : nullptr,
                                      kSmemPanel / (int)sizeof(float), false);
   double umax = 0.0, dmin = 0.0, dmax = 0.0;
   block_sum_max(n, [&](int j) {
@@ -1213,6 +1503,20 @@ batched_solve_kernel(BatchParams p) {
   double* kry = p.kry + cta * (long)(2 * p.kry_m + 2) * p.nmax;
   __shared__ KryShared ks;
   const int q = p.q;
+  // tensor-core update state: operand tiles after the panel budget (1024-
+  // byte aligned), the commit barrier, a 64-column TMEM accumulator
+  unsigned char* tc_tiles = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + kSmemPanel + 1023) & ~uintptr_t(1023));
+  if (threadIdx.x == 0) {
+    tc::mbar_init(reinterpret_cast<uint64_t*>(&sh.mma_bar), 1);
+    tc::fence_mbar_init();
+    sh.mma_phase = 0;
+    sh.tc_err = 0;
+  }
+  if (threadIdx.x < 32) tc::tmem_alloc(&sh.tmem, kTcCols);
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
   while (true) {
     __syncthreads();
     if (threadIdx.x == 0) s_sys = (int)atomicAdd(p.ticket, 1u);
@@ -1227,7 +1531,7 @@ batched_solve_kernel(BatchParams p) {
     double* X = p.X + d.b_off;
     BatchResult res{};
     const unsigned long long t_begin = globaltimer_ns();
-    if (threadIdx.x < 8) sh.ph[threadIdx.x] = 0ull;
+    if (threadIdx.x < kPhases) sh.ph[threadIdx.x] = 0ull;
     auto mark = [&](int i, unsigned long long since) {  // thread 0, after a barrier
       if (threadIdx.x == 0) sh.ph[i] += globaltimer_ns() - since;
     };
@@ -1248,10 +1552,11 @@ batched_solve_kernel(BatchParams p) {
     bool done = false;
     if (p.mode == 1) {
       compute_features(p, d, s, A, n, nA, Wf, piv, perm, reinterpret_cast<float*>(V), sh,
-                       reinterpret_cast<float*>(smem_raw));
+                       reinterpret_cast<float*>(smem_raw), tc_tiles);
       __syncthreads();
       mark(7, t_begin);
-      if (p.phase_ns && threadIdx.x < 8) p.phase_ns[(long)s * 8 + threadIdx.x] = sh.ph[threadIdx.x];
+      if (p.phase_ns && threadIdx.x < kPhases)
+        p.phase_ns[(long)s * kPhases + threadIdx.x] = sh.ph[threadIdx.x];
       continue;
     }
     // precision chosen at run time (the selector's output) or at plan time
@@ -1264,7 +1569,7 @@ batched_solve_kernel(BatchParams p) {
       // FP32 factors just computed (they are at least as good as BF16's)
       const int finfo = compute_features(p, d, s, A, n, nA, Wf, piv, perm,
                                          reinterpret_cast<float*>(V), sh,
-                                         reinterpret_cast<float*>(smem_raw));
+                                         reinterpret_cast<float*>(smem_raw), tc_tiles);
       __syncthreads();
       mark(7, t_begin);
       prec = mlpd::block_argmax(p.mlp, sh.feat, sh.h1, sh.h2, sh.lg);
@@ -1282,7 +1587,7 @@ batched_solve_kernel(BatchParams p) {
       if (!have32) {
         for (long i = threadIdx.x; i < (long)n * n; i += kBT) Wf[i] = (float)A[i];
         __syncthreads();
-        info = factor_sys<float>(Wf, n, d.kind, d.nb, piv, sh, smf,
+        info = factor_sys<float>(Wf, n, d.kind, d.nb, piv, sh, smf, p.tc ? tc_tiles : nullptr,
                                  kSmemPanel / (int)sizeof(float), pr == 2);
         if (info == 0) {
           if (d.kind == 0)
@@ -1296,11 +1601,15 @@ batched_solve_kernel(BatchParams p) {
       if (info == 0) {
         float* vf = reinterpret_cast<float*>(V);
         const unsigned long long t_ir = globaltimer_ns();
+        unsigned long long t_sub = t_ir;
         cta_apply_inverse<float>(Wf, n, d.kind, perm, B, X, vf, nullptr, q, false, s_sc);
+        mark(9, t_sub);
         const int lu_its = p.method == 2 ? 0 : p.max_iters;
         double prev = INFINITY;
         for (int it = 0;; ++it) {
+          t_sub = globaltimer_ns();
           const double be = sys_berr(A, n, X, B, R, q, sh, nA);
+          mark(8, t_sub);
           if (it > 0 && !(be < prev)) {
             // Refined.hpp keeps an update only if it lowers the residual
             for (int i = threadIdx.x; i < n * q; i += kBT) X[i] = Xprev[i];
@@ -1318,7 +1627,9 @@ batched_solve_kernel(BatchParams p) {
           if (it >= lu_its) break;
           prev = be;
           for (int i = threadIdx.x; i < n * q; i += kBT) Xprev[i] = X[i];
+          t_sub = globaltimer_ns();
           cta_apply_inverse<float>(Wf, n, d.kind, perm, R, X, vf, nullptr, q, true, s_sc);
+          mark(9, t_sub);
         }
         __syncthreads();
         mark(4, t_ir);
@@ -1362,7 +1673,7 @@ batched_solve_kernel(BatchParams p) {
       __syncthreads();
       int nb64 = max(1, min(d.nb, (kSmemPanel / 8 - 64 * 64) / max(n, 1)));
       if (nb64 > 8) nb64 = nb64 / 8 * 8;
-      const int info = factor_sys<double>(Wd, n, d.kind, nb64, piv, sh, smd,
+      const int info = factor_sys<double>(Wd, n, d.kind, nb64, piv, sh, smd, nullptr,
                                           kSmemPanel / (int)sizeof(double), false);
       res.info = info;
       if (info == 0) {
@@ -1383,9 +1694,26 @@ batched_solve_kernel(BatchParams p) {
     res.converged = done ? 1 : 0;
     res.fell_back = (res.prec != prec) ? 1 : 0;
     res.ns = (long long)(globaltimer_ns() - t_begin);
+    if (sh.tc_err) res.info = -1;  // a tensor-core wait timed out: result invalid
     if (threadIdx.x == 0) p.out[s] = res;
     __syncthreads();
-    if (p.phase_ns && threadIdx.x < 8) p.phase_ns[(long)s * 8 + threadIdx.x] = sh.ph[threadIdx.x];
+    if (p.phase_ns && threadIdx.x < kPhases)
+        p.phase_ns[(long)s * kPhases + threadIdx.x] = sh.ph[threadIdx.x];
+  }
+  __syncthreads();
+  if (sh.tc_err) {
+    if (threadIdx.x == 0) atomicExch(p.err, 1);
+    // let an MMA that outlived the wait finish before the TMEM goes (bounded)
+    const unsigned long long t0 = globaltimer_ns();
+    while (!tc::mbar_try_wait(reinterpret_cast<uint64_t*>(&sh.mma_bar), sh.mma_phase) &&
+           globaltimer_ns() - t0 < kSpinLimitNs) {
+    }
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    tc::tc_fence_after();
+    tc::tmem_dealloc(sh.tmem, kTcCols);
   }
 }
 
@@ -1405,6 +1733,7 @@ struct BatchPlan {
   double* d_vec = nullptr;
   double* d_kry = nullptr;
   unsigned* d_ticket = nullptr;
+  int* d_err = nullptr;
   BatchResult* d_out = nullptr;
   int grid = 0;
   long ws_elems = 0;
@@ -1434,7 +1763,7 @@ cudaError_t batched_plan(Context* ctx, int count, const int* h_n, const int* h_k
                          const int* nb_table, int ctas_per_sm, double tol, int max_iters,
                          int fallback, int mode, float* feat, int method, int kry_m,
                          int kry_max, const int* prec_dev, unsigned long long* phase_ns,
-                         const float* mlp, BatchPlan** out) {
+                         const float* mlp, int tc, BatchPlan** out) {
   *out = nullptr;
   if (q < 1 || q > kBQ) return cudaErrorInvalidValue;
   kry_m = kry_m > 0 ? std::min(kry_m, kKryMax) : 30;
@@ -1485,6 +1814,8 @@ cudaError_t batched_plan(Context* ctx, int count, const int* h_n, const int* h_k
   if (e == cudaSuccess)
     e = cudaMalloc(&P->d_kry, sizeof(double) * (2 * (long)kry_m + 2) * nmax * P->grid);
   if (e == cudaSuccess) e = cudaMalloc(&P->d_ticket, sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMalloc(&P->d_err, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(P->d_err, 0, sizeof(int));
   if (e == cudaSuccess) e = cudaMalloc(&P->d_out, sizeof(BatchResult) * count);
   if (e == cudaSuccess)
     e = cudaMemcpy(P->d_desc, desc.data(), sizeof(SysDesc) * count, cudaMemcpyHostToDevice);
@@ -1514,6 +1845,8 @@ cudaError_t batched_plan(Context* ctx, int count, const int* h_n, const int* h_k
   prm.out = P->d_out;
   prm.mode = (mode == 0 && mlp) ? 2 : mode;
   prm.mlp = mlp;
+  prm.tc = tc ? 1 : 0;
+  prm.err = P->d_err;
   prm.fallback = fallback;
   prm.feat = feat;
   prm.method = method;
@@ -1523,7 +1856,7 @@ cudaError_t batched_plan(Context* ctx, int count, const int* h_n, const int* h_k
   prm.prec_dev = prec_dev;
   prm.phase_ns = phase_ns;
   e = cudaFuncSetAttribute(batched_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           kSmemPanel);
+                           kDynSmem);
   if (e != cudaSuccess) {
     batched_destroy(P);
     return e;
@@ -1534,7 +1867,7 @@ cudaError_t batched_plan(Context* ctx, int count, const int* h_n, const int* h_k
   if (e == cudaSuccess) e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
     cudaMemsetAsync(P->d_ticket, 0, sizeof(unsigned), cs);
-    batched_solve_kernel<<<P->grid, kBT, kSmemPanel, cs>>>(prm);
+    batched_solve_kernel<<<P->grid, kBT, kDynSmem, cs>>>(prm);
     e = cudaStreamEndCapture(cs, &P->graph);
   }
   if (e == cudaSuccess) e = cudaGraphInstantiate(&P->exec, P->graph, 0);
@@ -1558,8 +1891,13 @@ cudaError_t batched_execute(BatchPlan* P) {
 cudaError_t batched_results(BatchPlan* P, BatchResult* h_out) {
   cudaError_t e = cudaMemcpyAsync(h_out, P->d_out, sizeof(BatchResult) * P->count,
                                   cudaMemcpyDeviceToHost, P->ctx->stream);
+  int err = 0;
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&err, P->d_err, sizeof(int), cudaMemcpyDeviceToHost, P->ctx->stream);
   if (e != cudaSuccess) return e;
-  return cudaStreamSynchronize(P->ctx->stream);
+  e = cudaStreamSynchronize(P->ctx->stream);
+  if (e == cudaSuccess && err) return cudaErrorLaunchTimeout;  // a bounded wait expired
+  return e;
 }
 
 void batched_destroy(BatchPlan* P) {
@@ -1574,6 +1912,7 @@ void batched_destroy(BatchPlan* P) {
   cudaFree(P->d_vec);
   cudaFree(P->d_kry);
   cudaFree(P->d_ticket);
+  cudaFree(P->d_err);
   cudaFree(P->d_out);
   delete P;
 }
@@ -1614,7 +1953,7 @@ int ElGBBatchedPlanCreate(ElGBContext ctx, int count, const int* n, int nrhs, co
                                      o.features_only ? 1 : 0, o.features, o.method,
                                      o.gmres_restart, o.gmres_max_iters, o.precision_device,
                                      reinterpret_cast<unsigned long long*>(o.phase_ns),
-                                     o.selector_params, &p);
+                                     o.selector_params, o.simt_update ? 0 : 1, &p);
   if (e != cudaSuccess) return e == cudaErrorMemoryAllocation ? elgb::kElAllocError
                                                                : elgb::kElRuntimeError;
   *plan = new ElGBBatchPlanImpl{p};

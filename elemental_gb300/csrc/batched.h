@@ -29,17 +29,19 @@ struct BatchPlan;
 // inner iterations per right-hand side, <= 0: max(kry_m, n / 6)) when LU-IR stalls; 1 LU-IR only;
 // 2 FGMRES-IR only.  prec_dev (device, may be null): per-system precision
 // read when the graph runs, overriding h_prec (the selector's output).
-// phase_ns (device, may be null): count x 8 device times per system: panel,
+// phase_ns (device, may be null): count x 10 device times per system: panel,
 // row swaps, U12 solve, trailing update (low-precision factorization),
-// LU-IR, FGMRES-IR, FP64 path, features.  mlp (device, may be null): with
+// LU-IR, FGMRES-IR, FP64 path, features, and within LU-IR the FP64
+// residuals and the low-precision solves.  mlp (device, may be null): with
 // mode 0, fused selection -- each system's features (FP32 LU kept), the
-// network's class, then the solve with that precision.
+// network's class, then the solve with that precision.  tc: FP32 / BF16
+// trailing updates on the tensor cores (tcgen05), else SIMT FMAs.
 cudaError_t batched_plan(Context* ctx, int count, const int* h_n, const int* h_kind,
                          const int* h_prec, int q, const double* A, const double* B, double* X,
                          const int* nb_table, int ctas_per_sm, double tol, int max_iters,
                          int fallback, int mode, float* feat, int method, int kry_m,
                          int kry_max, const int* prec_dev, unsigned long long* phase_ns,
-                         const float* mlp, BatchPlan** out);
+                         const float* mlp, int tc, BatchPlan** out);
 cudaError_t batched_execute(BatchPlan* P);
 cudaError_t batched_results(BatchPlan* P, BatchResult* h_out);
 void batched_destroy(BatchPlan* P);

@@ -103,13 +103,15 @@ def case_batched(ctx, a):
     B = torch.randn(a.count * a.n * a.nrhs, device="cuda", generator=g, dtype=torch.float64)
     bs = BatchedSolver([a.n] * a.count, a.nrhs, A, B, precisions=[a.precision] * a.count,
                        fallback=False, method="lu-ir", ctx=ctx, phases=True,
+                       simt_update=a.simt,
                        nb_table=[a.nb] * 8 if a.nb else None)
     bs.run()
     ms = _timed(bs.run)
     res = bs.results()
     dev = [r["device_ms"] for r in res]
     flops = a.count * 2.0 / 3.0 * a.n ** 3
-    out = dict(case="batched", n=a.n, count=a.count, nrhs=a.nrhs, precision=a.precision, ms=ms,
+    out = dict(case="batched", n=a.n, count=a.count, nrhs=a.nrhs, precision=a.precision,
+               update="simt" if a.simt else "tcgen05", ms=ms,
                tflops=flops / (ms * 1e-3) / 1e12, converged=sum(r["converged"] for r in res),
                device_ms_mean=sum(dev) / len(dev), device_ms_max=max(dev),
                gflops_per_system_cta=2.0 / 3.0 * a.n ** 3 / (sum(dev) / len(dev) * 1e-3) / 1e9,
@@ -134,6 +136,7 @@ def main(argv=None):
     p.add_argument("--nrhs", type=int, default=16)
     p.add_argument("--method", default="lu-ir", choices=["lu-ir", "gmres-ir"])
     p.add_argument("--count", type=int, default=152)
+    p.add_argument("--simt", action="store_true", help="batched: SIMT trailing updates")
     p.add_argument("--precision", default="fp32", choices=["fp64", "fp32", "bf16"])
     p.add_argument("--seed", type=int, default=20261204)
     a = p.parse_args(argv)

@@ -205,10 +205,11 @@ typedef struct {
   const int* precision_device; /* device int per system, read at each Execute
                                   (overrides precision; e.g. the selector's
                                   ElGBMLPForward argmax), or NULL */
-  long long* phase_ns; /* device, count x 8, or NULL: per-system device time of
-                          the low-precision LU's panel, row swaps, U12 solve,
-                          trailing update, then LU-IR, FGMRES-IR, the FP64
-                          path and the feature pass (ns) */
+  long long* phase_ns; /* device, count x 10, or NULL: per-system device time
+                          of the low-precision LU's panel, row swaps, U12
+                          solve, trailing update, then LU-IR, FGMRES-IR, the
+                          FP64 path, the feature pass, and within LU-IR the
+                          FP64 residuals and the low-precision solves (ns) */
   const float* selector_params; /* device, ElGBMLPParamCount() floats, or NULL:
                           fused selection in the same launch -- each
                           system's features (FP32 LU, kept), the network's
@@ -216,6 +217,8 @@ typedef struct {
                           that precision; a low-precision class refines with
                           the kept FP32 factors.  `features` (if set) also
                           receives the features */
+  int simt_update;     /* 1: FP32 / BF16 trailing updates on SIMT FMAs instead
+                          of the tensor cores (tcgen05) */
 } ElGBBatchOptions;
 int ElGBBatchedPlanCreate(ElGBContext ctx, int count, const int* n, int nrhs,
                           const double* A, const double* B, double* X,
