@@ -47,7 +47,8 @@ def parse():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--n", type=int, default=32768)
     p.add_argument("--nrhs", type=int, default=16)
-    p.add_argument("--precision", default="fp32", choices=["fp32", "tf32", "bf16", "fp64"])
+    p.add_argument("--precision", default="fp32",
+                   choices=["fp32", "tf32", "bf16", "fp8", "fp64"])
     p.add_argument("--method", default="lu-ir", choices=["lu-ir", "gmres-ir"])
     p.add_argument("--nb", type=int, default=0)
     p.add_argument("--fp64-compare", default="on", choices=["on", "off"])
@@ -335,7 +336,7 @@ def gpu_arm(args, rank, world, local_rank):
         traffic = tj["dram_bytes_per_flop"] * prof["flops"] / prof["launches"]
     roofline = {
         "kernel": "tc_gemm_sub_kernel (tcgen05 trailing update, "
-                  f"{ {'fp32': 'TF32x3', 'tf32': 'TF32', 'bf16': 'BF16', 'fp64': 'n/a'}[args.precision] } operands)",
+                  f"{ {'fp32': 'TF32x3', 'tf32': 'TF32', 'bf16': 'BF16', 'fp8': 'E4M3', 'fp64': 'n/a'}[args.precision] } operands)",
         "bound": "tensor", "achieved": tf_achieved, "peak": peak, "unit": "TFLOP/s",
         "frac": (tf_achieved / peak) if tf_achieved else None,
         "peak_source": f"{peak_kind} bf16 dense (sustained): the kernel is timed inside a long step",
@@ -366,12 +367,13 @@ def gpu_arm(args, rank, world, local_rank):
     prec_desc = {"fp32": "FP32 factors via TF32x3 tcgen05 updates",
                  "tf32": "FP32 storage, TF32 tcgen05 updates",
                  "bf16": "FP32 storage, BF16 tcgen05 updates",
+                 "fp8": "FP32 storage, FP8 E4M3 tcgen05 trailing updates, per-panel scales",
                  "fp64": "plain FP64 getrf + getrs"}[args.precision]
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tmax / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": {"fp32": "f64+tf32x3", "tf32": "f64+tf32", "bf16": "f64+bf16",
+        "dtype": {"fp32": "f64+tf32x3", "tf32": "f64+tf32", "bf16": "f64+bf16", "fp8": "f64+e4m3",
                   "fp64": "f64"}[args.precision],
         "data": "synthetic: seeded iid N(0,1) FP64 (device Philox generator)",
         "config": {"workload": f"mixed-precision {args.method.upper()} ({prec_desc}, FP64 "

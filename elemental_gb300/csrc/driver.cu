@@ -143,7 +143,8 @@ static PanelScratch<T> carve_panel(Carver& cv, int maxG) {
 // How the float path's contractions run: SIMT FP32 FMA (tc_kind < 0) or on
 // the tensor cores (tc_gemm.cu) with `ws` holding the packed operands.
 struct GemmCfg {
-  int tc_kind = -1;
+  int tc_kind = -1;     // panel-internal and TRSM GEMMs
+  int trail_kind = -1;  // the trailing-matrix update (>= 0: overrides tc_kind)
   void* ws = nullptr;
 };
 
@@ -164,7 +165,9 @@ struct LuLane {
   } while (0)
 
 static cudaError_t gemm_sub(Context* ctx, const LuLane& L, int m, int n, int k, const double* A,
-                            long lda, const double* B, long ldb, double* C, long ldc) {
+                            long lda, const double* B, long ldb, double* C, long ldc,
+                            bool trailing = false) {
+  (void)trailing;
   const int pi = ctx->prof_begin(L.st);
   LANE_CHECK(launch_gemm_simt<double>(false, false, m, n, k, -1.0, A, lda, B, ldb, 1.0, C, ldc,
                                       0, L.st), 1);
@@ -173,21 +176,23 @@ static cudaError_t gemm_sub(Context* ctx, const LuLane& L, int m, int n, int k, 
 }
 
 static cudaError_t gemm_sub(Context* ctx, const LuLane& L, int m, int n, int k, const float* A,
-                            long lda, const float* B, long ldb, float* C, long ldc) {
+                            long lda, const float* B, long ldb, float* C, long ldc,
+                            bool trailing = false) {
   const GemmCfg& g = L.gemm;
-  if (g.tc_kind >= 0 && m >= 64 && n >= 64 && k >= 16) {
+  const int kind = (trailing && g.trail_kind >= 0) ? g.trail_kind : g.tc_kind;
+  if (kind >= 0 && m >= 64 && n >= 64 && k >= 16) {
     int nl = 0;
     cudaEvent_t a = nullptr, b = nullptr;
     if (ctx->prof_on) {
       a = ctx->next_event();
       b = ctx->next_event();
     }
-    cudaError_t e = launch_tc_gemm_sub(g.tc_kind, m, n, k, A, lda, B, ldb, C, ldc, g.ws,
+    cudaError_t e = launch_tc_gemm_sub(kind, m, n, k, A, lda, B, ldb, C, ldc, g.ws,
                                        ctx->status, L.st, &nl, a, b);
     ctx->launches += nl;
     if (a && b) {
-      const double esz = g.tc_kind == kTcBF16 ? 2.0 : 4.0;
-      const double copies = g.tc_kind == kTcTF32x3 ? 2.0 : 1.0;
+      const double esz = kind == kTcBF16 ? 2.0 : kind == kTcFP8 ? 1.0 : 4.0;
+      const double copies = kind == kTcTF32x3 ? 2.0 : 1.0;
       ctx->prof.push_back({a, b, 2.0 * m * n * (double)k,
                            8.0 * m * n + copies * esz * (double)k * (m + n), ELGB_PROF_TC_GEMM});
     }
@@ -311,7 +316,7 @@ static cudaError_t update_cols(LuState<T>& s, const LuLane& L, int k, int jb, in
   if (m2 > 0)
     e = gemm_sub(ctx, L, m2, c_end - c_begin, jb, s.A + (k + jb) + (long)k * s.lda, s.lda,
                  s.A + k + (long)c_begin * s.lda, s.lda,
-                 s.A + (k + jb) + (long)c_begin * s.lda, s.lda);
+                 s.A + (k + jb) + (long)c_begin * s.lda, s.lda, true);
   return e;
 }
 
@@ -415,9 +420,15 @@ cudaError_t getrf(Context* ctx, int m, int n, T* A, long lda, int* ipiv, int nb,
   if (e != cudaSuccess) return e;
   if (m == 0 || n == 0) return cudaSuccess;
   const bool tc = sizeof(T) == 4 && tc_kind >= 0;
+  // FP8 serves the trailing update only; the panel's and the TRSM's
+  // contractions keep TF32x3 (their operands are the pivoted panel itself)
+  const int inner_kind = tc_kind == kTcFP8 ? kTcTF32x3 : tc_kind;
   const bool la = use_lookahead(m, n, nb) && ctx->side_stream && ctx->opt_lookahead;
-  const size_t tcb = tc ? tc_gemm_workspace_bytes(tc_kind, m, std::max(n, nb), nb) : 0;
-  const size_t tcs = (tc && la) ? tc_gemm_workspace_bytes(tc_kind, m, nb, nb) : 0;
+  const size_t tcb =
+      tc ? std::max(tc_gemm_workspace_bytes(tc_kind, m, std::max(n, nb), nb),
+                    tc_gemm_workspace_bytes(inner_kind, m, std::max(n, nb), nb))
+         : 0;
+  const size_t tcs = (tc && la) ? tc_gemm_workspace_bytes(inner_kind, m, nb, nb) : 0;
   e = ctx->ensure(getrf_scratch_bytes<T>(ctx, nb) + align256(tcb) + align256(tcs));
   if (e != cudaSuccess) return e;
   Carver cv(ctx);
@@ -425,13 +436,14 @@ cudaError_t getrf(Context* ctx, int m, int n, T* A, long lda, int* ipiv, int nb,
   e = setup_lu_state(ctx, s, cv, nb);
   if (e != cudaSuccess) return e;
   if (tc) {
-    s.main.gemm.tc_kind = tc_kind;
+    s.main.gemm.tc_kind = inner_kind;
+    s.main.gemm.trail_kind = tc_kind;
     s.main.gemm.ws = cv.take<char>(tcb);
     if (!s.main.gemm.ws) return cudaErrorMemoryAllocation;
   }
   if (la) {
     s.side.st = ctx->side_stream;
-    s.side.gemm.tc_kind = tc ? tc_kind : -1;
+    s.side.gemm.tc_kind = tc ? inner_kind : -1;
     if (tc) {
       s.side.gemm.ws = cv.take<char>(tcs);
       if (!s.side.gemm.ws) return cudaErrorMemoryAllocation;
@@ -922,7 +934,7 @@ ELGB_LU(s, float)
 int ElGBLUPartialPivMixed_s(ElGBContext ctx, int m, int n, float* A, int lda, int* swapDests,
                             int nb, int gemm_kind) {
   if (int r = arg_ok(ctx && m >= 0 && n >= 0 && lda >= std::max(m, 1) &&
-                     gemm_kind >= -1 && gemm_kind <= 2 && (m * n == 0 || (A && swapDests))))
+                     gemm_kind >= -1 && gemm_kind <= 3 && (m * n == 0 || (A && swapDests))))
     return r;
   if (nb <= 0) nb = 512;
   return elgb::to_el_error(elgb::getrf<float>(ctx, m, n, A, lda, swapDests, nb, gemm_kind));
@@ -930,7 +942,7 @@ int ElGBLUPartialPivMixed_s(ElGBContext ctx, int m, int n, float* A, int lda, in
 
 int ElGBGemmSubTC(ElGBContext ctx, int gemm_kind, int m, int n, int k, const float* A, int lda,
                   const float* B, int ldb, float* C, int ldc) {
-  if (int r = arg_ok(ctx && gemm_kind >= 0 && gemm_kind <= 2 && m >= 0 && n >= 0 && k >= 0 &&
+  if (int r = arg_ok(ctx && gemm_kind >= 0 && gemm_kind <= 3 && m >= 0 && n >= 0 && k >= 0 &&
                      lda >= std::max(m, 1) && ldb >= std::max(k, 1) && ldc >= std::max(m, 1)))
     return r;
   cudaError_t e = ctx->begin_call();

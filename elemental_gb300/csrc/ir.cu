@@ -284,6 +284,7 @@ cudaError_t refined_solve(Context* ctx, int n, const double* A, long lda, int nr
   }
   const int tc_kind = c.precision == ELGB_PREC_BF16   ? kTcBF16
                       : c.precision == ELGB_PREC_TF32 ? kTcTF32
+                      : c.precision == ELGB_PREC_FP8  ? kTcFP8
                                                       : kTcTF32x3;
   const bool gm = c.method == 1;
   const int Q = std::min(nrhs, 16);
@@ -581,7 +582,7 @@ extern "C" int ElGBRefinedSolve_d(ElGBContext ctx, int n, const double* A, int l
     c.precision = ELGB_PREC_FP32;
     c.fallback = 1;
   }
-  if (c.precision < ELGB_PREC_FP64 || c.precision > ELGB_PREC_BF16 || c.method < 0 ||
+  if (c.precision < ELGB_PREC_FP64 || c.precision > ELGB_PREC_FP8 || c.method < 0 ||
       c.method > 1)
     return elgb::kElArgError;
   auto* cx = static_cast<elgb::Context*>(ctx);

@@ -22,6 +22,7 @@
 // its TMEM.
 #include <cuda.h>
 #include <cuda_bf16.h>
+#include <cuda_fp8.h>
 #include <cudaTypedefs.h>
 
 #include "kernels.h"
@@ -56,8 +57,17 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, u
 // K-major, M = 128, N = 256.
 template <int KIND>
 __host__ __device__ constexpr uint32_t idesc_m128n256() {
-  return (1u << 4) | ((KIND == kTcBF16 ? 1u : 2u) << 7) | ((KIND == kTcBF16 ? 1u : 2u) << 10) |
-         ((uint32_t)(kBN >> 3) << 17) | ((uint32_t)(kBM >> 4) << 24);
+  // operand formats: kind::f16 BF16 = 1, kind::tf32 TF32 = 2, kind::f8f6f4 E4M3 = 0
+  constexpr uint32_t fmt = KIND == kTcBF16 ? 1u : KIND == kTcFP8 ? 0u : 2u;
+  return (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(kBN >> 3) << 17) |
+         ((uint32_t)(kBM >> 4) << 24);
+}
+
+// Power-of-two scale mapping an operand whose largest magnitude is amax to
+// at most the E4M3 maximum 448 (1 for an all-zero operand).
+__host__ __device__ __forceinline__ float fp8_scale(float amax) {
+  if (!(amax > 0.f) || !(amax < 3.0e38f)) return 1.f;
+  return ldexpf(1.f, ilogbf(448.f / amax));
 }
 
 // passes = 1: C -= A B.  passes = 3 (TF32 split, ~FP32 accuracy):
@@ -69,7 +79,8 @@ tc_gemm_sub_kernel(const __grid_constant__ CUtensorMap tmA,
                    const __grid_constant__ CUtensorMap tmB,
                    const __grid_constant__ CUtensorMap tmAlo,
                    const __grid_constant__ CUtensorMap tmBlo, float* __restrict__ C, long ldc,
-                   int m, int n, int num_kb, int passes, DevStatus* st) {
+                   int m, int n, int num_kb, int passes, const float* __restrict__ amax,
+                   DevStatus* st) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   // 1024-byte alignment for the swizzled tiles
   unsigned char* base = reinterpret_cast<unsigned char*>(
@@ -113,7 +124,7 @@ tc_gemm_sub_kernel(const __grid_constant__ CUtensorMap tmA,
       }
       const int pass = kb / num_kb;
       mbar_arrive_expect_tx(&full_bar[s], kStageA + kStageB);
-      const int xk = (kb - pass * num_kb) * (kBKBytes / (KIND == kTcBF16 ? 2 : 4));
+      const int xk = (kb - pass * num_kb) * (kBKBytes / (KIND == kTcBF16 ? 2 : KIND == kTcFP8 ? 1 : 4));
       tma_load_2d(sA + s * kStageA, pass == 2 ? &tmAlo : &tmA, &full_bar[s], xk, m0);
       tma_load_2d(sB + s * kStageB, pass == 1 ? &tmBlo : &tmB, &full_bar[s], xk, n0);
     }
@@ -146,6 +157,8 @@ tc_gemm_sub_kernel(const __grid_constant__ CUtensorMap tmA,
   const int row = m0 + 32 * wl + lane;
   const bool row_ok = row < m;
   float* crow = C + row;
+  // FP8: the products carry the operands' scales (exact powers of two)
+  const float unscale = KIND == kTcFP8 ? 1.f / (fp8_scale(amax[0]) * fp8_scale(amax[1])) : 1.f;
   bool ready = false;
   for (int cc = 0; cc < 4; ++cc) {
     const int cbase = half * 128 + cc * 32;
@@ -166,7 +179,7 @@ tc_gemm_sub_kernel(const __grid_constant__ CUtensorMap tmA,
 #pragma unroll
     for (int j = 0; j < 32; ++j) {
       const int col = n0 + cbase + j;
-      if (row_ok && col < n) crow[(long)col * ldc] = cv[j] - __uint_as_float(acc[j]);
+      if (row_ok && col < n) crow[(long)col * ldc] = cv[j] - __uint_as_float(acc[j]) * unscale;
     }
   }
   tc_fence_before();
@@ -189,8 +202,11 @@ __device__ __forceinline__ float to_tf32(float v) {
 // Writes the operand value (and, for the split form, the TF32 remainder
 // v - tf32(v) to `lo`).
 template <int KIND>
-__device__ __forceinline__ void store_op(void* out, void* lo, size_t idx, float v) {
-  if (KIND == kTcBF16) {
+__device__ __forceinline__ void store_op(void* out, void* lo, size_t idx, float v, float scale) {
+  if (KIND == kTcFP8) {
+    reinterpret_cast<__nv_fp8_storage_t*>(out)[idx] =
+        __nv_cvt_float_to_fp8(v * scale, __NV_SATFINITE, __NV_E4M3);
+  } else if (KIND == kTcBF16) {
     reinterpret_cast<__nv_bfloat16*>(out)[idx] = __float2bfloat16_rn(v);
   } else {
     const float hi = to_tf32(v);
@@ -203,8 +219,10 @@ __device__ __forceinline__ void store_op(void* out, void* lo, size_t idx, float 
 // memory so both the read and the write are coalesced.
 template <int KIND>
 __global__ void pack_a_kernel(const float* __restrict__ A, long lda, int m, int K, int Kp,
-                              void* __restrict__ out, void* __restrict__ lo) {
+                              void* __restrict__ out, void* __restrict__ lo,
+                              const float* __restrict__ amax) {
   __shared__ float t[32][33];
+  const float scale = KIND == kTcFP8 ? fp8_scale(amax[0]) : 1.f;
   const int i0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
   const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
   for (int q = 0; q < 32; q += 8) {
@@ -214,17 +232,41 @@ __global__ void pack_a_kernel(const float* __restrict__ A, long lda, int m, int 
   __syncthreads();
   for (int q = 0; q < 32; q += 8) {
     const int i = i0 + ty + q, k = k0 + tx;
-    if (i < m && k < Kp) store_op<KIND>(out, lo, (size_t)i * Kp + k, t[tx][ty + q]);
+    if (i < m && k < Kp) store_op<KIND>(out, lo, (size_t)i * Kp + k, t[tx][ty + q], scale);
   }
 }
 
 // B (K x n, column-major) -> out[j * Kp + k]: already K-contiguous.
 template <int KIND>
 __global__ void pack_b_kernel(const float* __restrict__ B, long ldb, int K, int n, int Kp,
-                              void* __restrict__ out, void* __restrict__ lo) {
+                              void* __restrict__ out, void* __restrict__ lo,
+                              const float* __restrict__ amax) {
+  const float scale = KIND == kTcFP8 ? fp8_scale(amax[1]) : 1.f;
   const int j = blockIdx.y;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < Kp; k += gridDim.x * blockDim.x)
-    store_op<KIND>(out, lo, (size_t)j * Kp + k, k < K ? B[k + (long)j * ldb] : 0.f);
+    store_op<KIND>(out, lo, (size_t)j * Kp + k, k < K ? B[k + (long)j * ldb] : 0.f, scale);
+}
+
+// amax[0] = max |A| (m x K), amax[1] = max |B| (K x n), both column-major;
+// amax zeroed beforehand.  Non-negative floats order as their bit patterns.
+__global__ void absmax_kernel(const float* __restrict__ A, long lda, int m, int K,
+                              const float* __restrict__ B, long ldb, int n,
+                              float* __restrict__ amax) {
+  float a = 0.f, b = 0.f;
+  const long na = (long)m * K, nb = (long)K * n;
+  const long stride = (long)gridDim.x * blockDim.x;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < na; i += stride)
+    a = fmaxf(a, fabsf(A[(i % m) + (i / m) * lda]));
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < nb; i += stride)
+    b = fmaxf(b, fabsf(B[(i % K) + (i / K) * ldb]));
+  for (int o = 16; o > 0; o >>= 1) {
+    a = fmaxf(a, __shfl_xor_sync(0xffffffffu, a, o));
+    b = fmaxf(b, __shfl_xor_sync(0xffffffffu, b, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(reinterpret_cast<int*>(amax), __float_as_int(a));
+    atomicMax(reinterpret_cast<int*>(amax) + 1, __float_as_int(b));
+  }
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
@@ -245,13 +287,14 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 bool make_operand_map(CUtensorMap* map, void* gptr, int kind, int Kp, int rows, int box_rows) {
   auto fn = encode_fn();
   if (!fn) return false;
-  const int esz = kind == kTcBF16 ? 2 : 4;
+  const int esz = kind == kTcBF16 ? 2 : kind == kTcFP8 ? 1 : 4;
   cuuint64_t dims[2] = {(cuuint64_t)Kp, (cuuint64_t)rows};
   cuuint64_t strides[1] = {(cuuint64_t)Kp * esz};
   cuuint32_t box[2] = {(cuuint32_t)(kBKBytes / esz), (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1, 1};
-  CUresult r = fn(map, kind == kTcBF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16
-                                       : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+  CUresult r = fn(map, kind == kTcBF16  ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16
+                       : kind == kTcFP8 ? CU_TENSOR_MAP_DATA_TYPE_UINT8
+                                        : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
                   2, gptr, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                   CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
@@ -262,12 +305,14 @@ bool make_operand_map(CUtensorMap* map, void* gptr, int kind, int Kp, int rows, 
 
 static size_t rup1k(size_t b) { return (b + 1023) / 1024 * 1024; }
 
+static int op_esz(int kind) { return kind == kTcBF16 ? 2 : kind == kTcFP8 ? 1 : 4; }
+
 size_t tc_gemm_workspace_bytes(int kind, int m, int n, int K) {
-  const int esz = kind == kTcBF16 ? 2 : 4;
+  const int esz = op_esz(kind);
   const int kbe = kBKBytes / esz;
   const size_t Kp = (size_t)((K + kbe - 1) / kbe) * kbe;
   const size_t copies = kind == kTcTF32x3 ? 2 : 1;
-  return copies * (rup1k((size_t)m * Kp * esz) + rup1k((size_t)n * Kp * esz));
+  return copies * (rup1k((size_t)m * Kp * esz) + rup1k((size_t)n * Kp * esz)) + 1024;
 }
 
 cudaError_t launch_tc_gemm_sub(int kind, int m, int n, int K, const float* A, long lda,
@@ -277,26 +322,39 @@ cudaError_t launch_tc_gemm_sub(int kind, int m, int n, int K, const float* A, lo
   if (nlaunch) *nlaunch = 0;
   if (m <= 0 || n <= 0 || K <= 0) return cudaSuccess;
   const bool split = kind == kTcTF32x3;
-  const int esz = kind == kTcBF16 ? 2 : 4;
+  const int esz = op_esz(kind);
   const int kbe = kBKBytes / esz;
   const int Kp = (K + kbe - 1) / kbe * kbe;
   char* Abuf = static_cast<char*>(ws);
   char* Bbuf = Abuf + rup1k((size_t)m * Kp * esz);
   char* Alo = split ? Bbuf + rup1k((size_t)n * Kp * esz) : nullptr;
   char* Blo = split ? Alo + rup1k((size_t)m * Kp * esz) : nullptr;
+  // FP8 operand maxima (per call, i.e. per panel) after the packed operands
+  float* amax = reinterpret_cast<float*>(
+      Abuf + (split ? 2 : 1) * (rup1k((size_t)m * Kp * esz) + rup1k((size_t)n * Kp * esz)));
   dim3 pg((m + 31) / 32, (Kp + 31) / 32);
-  if (kind == kTcBF16) {
-    pack_a_kernel<kTcBF16><<<pg, dim3(32, 8), 0, stream>>>(A, lda, m, K, Kp, Abuf, nullptr);
+  int nl = 2;
+  if (kind == kTcFP8) {
+    cudaError_t e0 = cudaMemsetAsync(amax, 0, 2 * sizeof(float), stream);
+    if (e0 != cudaSuccess) return e0;
+    absmax_kernel<<<1024, 256, 0, stream>>>(A, lda, m, K, B, ldb, n, amax);
+    pack_a_kernel<kTcFP8><<<pg, dim3(32, 8), 0, stream>>>(A, lda, m, K, Kp, Abuf, nullptr, amax);
+    pack_b_kernel<kTcFP8><<<dim3((Kp + 255) / 256, n), 256, 0, stream>>>(B, ldb, K, n, Kp,
+                                                                        Bbuf, nullptr, amax);
+    nl = 3;
+  } else if (kind == kTcBF16) {
+    pack_a_kernel<kTcBF16><<<pg, dim3(32, 8), 0, stream>>>(A, lda, m, K, Kp, Abuf, nullptr,
+                                                           amax);
     pack_b_kernel<kTcBF16><<<dim3((Kp + 255) / 256, n), 256, 0, stream>>>(B, ldb, K, n, Kp,
-                                                                         Bbuf, nullptr);
+                                                                         Bbuf, nullptr, amax);
   } else {
-    pack_a_kernel<kTcTF32><<<pg, dim3(32, 8), 0, stream>>>(A, lda, m, K, Kp, Abuf, Alo);
+    pack_a_kernel<kTcTF32><<<pg, dim3(32, 8), 0, stream>>>(A, lda, m, K, Kp, Abuf, Alo, amax);
     pack_b_kernel<kTcTF32><<<dim3((Kp + 255) / 256, n), 256, 0, stream>>>(B, ldb, K, n, Kp,
-                                                                         Bbuf, Blo);
+                                                                         Bbuf, Blo, amax);
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  const int mk = kind == kTcBF16 ? kTcBF16 : kTcTF32;
+  const int mk = kind == kTcTF32x3 ? kTcTF32 : kind;
   CUtensorMap tmA, tmB, tmAlo, tmBlo;
   if (!make_operand_map(&tmA, Abuf, mk, Kp, m, kBM) ||
       !make_operand_map(&tmB, Bbuf, mk, Kp, n, kBN))
@@ -314,21 +372,15 @@ cudaError_t launch_tc_gemm_sub(int kind, int m, int n, int K, const float* A, lo
   const int num_kb = Kp / kbe;
   const int passes = split ? 3 : 1;
   if (ev0) cudaEventRecord(ev0, stream);
-  if (kind == kTcBF16) {
-    auto kern = tc_gemm_sub_kernel<kTcBF16>;
-    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    kern<<<grid, kGemmThreads, smem, stream>>>(tmA, tmB, tmAlo, tmBlo, C, ldc, m, n, num_kb,
-                                               passes, st);
-  } else {
-    auto kern = tc_gemm_sub_kernel<kTcTF32>;
-    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    kern<<<grid, kGemmThreads, smem, stream>>>(tmA, tmB, tmAlo, tmBlo, C, ldc, m, n, num_kb,
-                                               passes, st);
-  }
+  auto kern = kind == kTcBF16  ? tc_gemm_sub_kernel<kTcBF16>
+              : kind == kTcFP8 ? tc_gemm_sub_kernel<kTcFP8>
+                               : tc_gemm_sub_kernel<kTcTF32>;
+  e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  kern<<<grid, kGemmThreads, smem, stream>>>(tmA, tmB, tmAlo, tmBlo, C, ldc, m, n, num_kb,
+                                             passes, amax, st);
   if (ev1) cudaEventRecord(ev1, stream);
-  if (nlaunch) *nlaunch = 3;
+  if (nlaunch) *nlaunch = nl + 1;
   return cudaGetLastError();
 }
 

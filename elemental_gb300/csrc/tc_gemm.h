@@ -12,6 +12,10 @@ enum TcKind : int {
   kTcBF16 = 0,  // tcgen05.mma kind::f16 with BF16 operands
   kTcTF32 = 1,  // tcgen05.mma kind::tf32
   kTcTF32x3 = 2,  // kind::tf32, operands split hi + lo, three products (~FP32)
+  kTcFP8 = 3,     // kind::f8f6f4 with E4M3 operands, each operand scaled per
+                  // call (per panel) by a power of two that maps its largest
+                  // magnitude near the E4M3 maximum 448; the scales are
+                  // divided out in the epilogue
 };
 
 // Bytes of device workspace launch_tc_gemm_sub needs for its packed operands.

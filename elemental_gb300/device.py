@@ -17,7 +17,7 @@ from . import _lib
 _DT = {torch.float64: "d", torch.float32: "s"}
 
 # ElGB precision / method codes (include/elgb300.h)
-PRECISIONS = {"fp64": 0, "fp32": 1, "tf32": 2, "bf16": 3}
+PRECISIONS = {"fp64": 0, "fp32": 1, "tf32": 2, "bf16": 3, "fp8": 4}
 PRECISION_NAMES = {v: k for k, v in PRECISIONS.items()}
 METHODS = {"lu-ir": 0, "gmres-ir": 1}
 PROFILE_TAGS = {"tc_gemm": 0, "panel": 1, "swap": 2, "trsm": 3, "gemm_simt": 4,
@@ -148,7 +148,8 @@ class Context:
 
     def lu_mixed(self, A, gemm_kind=2, piv=None, nb=0):
         """El::LU on an FP32 matrix with tensor-core updates (gemm_kind:
-        -1 SIMT FP32, 0 BF16, 1 TF32, 2 TF32x3)."""
+        -1 SIMT FP32, 0 BF16, 1 TF32, 2 TF32x3, 3 FP8 E4M3 trailing updates
+        with per-panel scales)."""
         m, n = A.shape
         assert A.dtype == torch.float32
         if piv is None:

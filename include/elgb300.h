@@ -92,12 +92,17 @@ int ElGBLUPartialPiv_s(ElGBContext ctx, int m, int n, float* A, int lda,
  *   ELGB_GEMM_BF16       tcgen05.mma kind::f16, BF16 operands
  *   ELGB_GEMM_TF32       tcgen05.mma kind::tf32
  *   ELGB_GEMM_TF32X3     kind::tf32 on hi + lo operand splits, three products
- *                        (close to FP32 accuracy) */
+ *                        (close to FP32 accuracy)
+ *   ELGB_GEMM_FP8        kind::f8f6f4 on E4M3 operands, each scaled per panel
+ *                        (per call) by a power of two mapping its largest
+ *                        magnitude near 448; in the LU only the trailing
+ *                        update uses it, the panel and TRSM keep TF32X3 */
 enum {
   ELGB_GEMM_SIMT_FP32 = -1,
   ELGB_GEMM_BF16 = 0,
   ELGB_GEMM_TF32 = 1,
-  ELGB_GEMM_TF32X3 = 2
+  ELGB_GEMM_TF32X3 = 2,
+  ELGB_GEMM_FP8 = 3
 };
 
 /* El::LU(A, P) on an FP32 matrix whose trailing updates, blocked-TRSM updates
@@ -118,7 +123,9 @@ enum {
   ELGB_PREC_FP64 = 0, /* plain FP64 getrf + getrs (no refinement)           */
   ELGB_PREC_FP32 = 1, /* FP32 storage, TF32x3 tensor-core products (~FP32)  */
   ELGB_PREC_TF32 = 2, /* FP32 storage, TF32 tensor-core products            */
-  ELGB_PREC_BF16 = 3  /* FP32 storage, BF16 tensor-core products            */
+  ELGB_PREC_BF16 = 3, /* FP32 storage, BF16 tensor-core products            */
+  ELGB_PREC_FP8 = 4   /* FP32 storage, E4M3 trailing updates with per-panel
+                         power-of-two scales (TF32x3 panel / TRSM)          */
 };
 
 typedef struct {
