@@ -53,6 +53,7 @@ constexpr int kDynSmem = kSmemPanel + kTcSmem + 1024;
 struct SysDesc {
   int n, kind, nb, prec;  // kind 0 LU, 1 Cholesky; prec 0 FP64, 1 FP32 + IR
   long a_off, b_off;      // into A (FP64, ld n) and B / X (FP64, ld n)
+  int ib, pad;            // inner panel width (the shared-memory panel), <= nb
 };
 
 struct Shared {
@@ -218,30 +219,27 @@ __device__ void cta_build_pairs(int k, int jb, Shared& sh) {
   __syncthreads();
 }
 
-// The panel's interchanges on the columns right of it ([k + jb, n)); the
-// columns left of it get every later panel's interchanges at once when the
-// factorization ends (cta_lu).
+// The row interchanges listed by cta_build_pairs on the columns [c_lo, c_hi).
 template <typename T>
-__device__ void cta_apply_swaps(T* W, int n, int ld, int k, int jb, Shared& sh, T* stage,
-                                int stage_elems) {
-  cta_build_pairs(k, jb, sh);
+__device__ void cta_swap_cols(T* W, int ld, Shared& sh, T* stage, int stage_elems, int c_lo,
+                              int c_hi) {
   const int cnt = sh.ival[0];
-  if (cnt == 0) return;
-  const int ncols_out = n - k - jb;
+  if (cnt == 0 || c_hi <= c_lo) return;
+  const int ncols_out = c_hi - c_lo;
   const int chunk = max(1, stage_elems / cnt);
   for (int c0 = 0; c0 < ncols_out; c0 += chunk) {
     const int cw = min(chunk, ncols_out - c0);
 #pragma unroll 8
     for (int idx = threadIdx.x; idx < cw * cnt; idx += kBT) {
       const int e = idx % cnt, cc = c0 + idx / cnt;
-      const int col = k + jb + cc;
+      const int col = c_lo + cc;
       stage[idx] = W[sh.pairs[128 + e] + (long)col * ld];
     }
     __syncthreads();
 #pragma unroll 8
     for (int idx = threadIdx.x; idx < cw * cnt; idx += kBT) {
       const int e = idx % cnt, cc = c0 + idx / cnt;
-      const int col = k + jb + cc;
+      const int col = c_lo + cc;
       W[sh.pairs[e] + (long)col * ld] = stage[idx];
     }
     __syncthreads();
@@ -539,8 +537,9 @@ __device__ __noinline__ void cta_gemm_update_tc(const float* P, int ldp, const f
 // piv_out[0..n) receives the swap destinations; returns info (0 ok, j+1 at
 // the first zero pivot).
 template <typename T>
-__device__ __noinline__ int cta_lu(T* W, int n, int ld, int nb, int* piv_out, Shared& sh, T* smem,
-                      int smem_elems, bool lowp, unsigned char* tc_tiles) {
+__device__ __noinline__ int cta_lu(T* W, int n, int ld, int nb, int ib, int* piv_out, Shared& sh,
+                                   T* smem, int smem_elems, bool lowp,
+                                   unsigned char* tc_tiles) {
   __shared__ T fv[9];
   __shared__ int fr[9];
   int info = 0;
@@ -552,79 +551,117 @@ __device__ __noinline__ int cta_lu(T* W, int n, int ld, int nb, int* piv_out, Sh
       t0 = t;
     }
   };
+  // Two levels when the shared-memory panel is narrower than the block:
+  // sub-panels of ib columns are factored in shared memory and update only
+  // the rest of their nb-column block; the block then updates the trailing
+  // matrix once with K = nb (half the trailing traffic of K = ib).
+  ib = max(1, min(ib, nb));
+  const bool one_level = ib == nb;
   for (int k = 0; k < n; k += nb) {
-    const int jb = min(nb, n - k);
-    const int mp = n - k;
-    T* panel = smem;  // mp x jb, ld mp
-    for (int idx = threadIdx.x; idx < mp * jb; idx += kBT) {
-      const int r = idx % mp, c = idx / mp;
-      panel[idx] = W[(k + r) + (long)(k + c) * ld];
-    }
-    __syncthreads();
-    for (int j = 0; j < jb; ++j) {
-      T bv = T(-1);
-      int br = -1;
-      for (int r = j + threadIdx.x; r < mp; r += kBT) {
-        const T v = tabs(panel[r + j * mp]);
-        if (argmax_better(v, r, bv, br)) {
-          bv = v;
-          br = r;
-        }
-      }
-      block_argmax_abs(bv, br, sh, fv, fr);
-      const int p = br < 0 ? j : br;
-      if (threadIdx.x == 0) sh.piv[j] = k + p;
-      if (p != j)
-        for (int c = threadIdx.x; c < jb; c += kBT) {
-          const T t = panel[j + c * mp];
-          panel[j + c * mp] = panel[p + c * mp];
-          panel[p + c * mp] = t;
-        }
-      __syncthreads();
-      const T alpha = panel[j + j * mp];
-      if (alpha == T(0)) {
-        if (info == 0) info = k + j + 1;
-      } else {
-        const T inv = T(1) / alpha;
-        for (int r = j + 1 + threadIdx.x; r < mp; r += kBT) {
-          const T l = panel[r + j * mp] * inv;
-          panel[r + j * mp] = l;
-          const T lr = rnd(l, lowp);
-          for (int c = j + 1; c < jb; ++c)
-            panel[r + c * mp] = fma(-lr, rnd(panel[j + c * mp], lowp), panel[r + c * mp]);
-        }
+    const int nbk = min(nb, n - k);
+    T* panel = smem;
+    int mp = n - k, jb = nbk;
+    for (int ks = k; ks < k + nbk; ks += ib) {
+      jb = min(ib, k + nbk - ks);
+      mp = n - ks;
+      panel = smem;  // mp x jb, ld mp
+      for (int idx = threadIdx.x; idx < mp * jb; idx += kBT) {
+        const int r = idx % mp, c = idx / mp;
+        panel[idx] = W[(ks + r) + (long)(ks + c) * ld];
       }
       __syncthreads();
+      for (int j = 0; j < jb; ++j) {
+        T bv = T(-1);
+        int br = -1;
+        for (int r = j + threadIdx.x; r < mp; r += kBT) {
+          const T v = tabs(panel[r + j * mp]);
+          if (argmax_better(v, r, bv, br)) {
+            bv = v;
+            br = r;
+          }
+        }
+        block_argmax_abs(bv, br, sh, fv, fr);
+        const int p = br < 0 ? j : br;
+        if (threadIdx.x == 0) sh.piv[j] = ks + p;
+        if (p != j)
+          for (int c = threadIdx.x; c < jb; c += kBT) {
+            const T t = panel[j + c * mp];
+            panel[j + c * mp] = panel[p + c * mp];
+            panel[p + c * mp] = t;
+          }
+        __syncthreads();
+        const T alpha = panel[j + j * mp];
+        if (alpha == T(0)) {
+          if (info == 0) info = ks + j + 1;
+        } else {
+          const T inv = T(1) / alpha;
+          for (int r = j + 1 + threadIdx.x; r < mp; r += kBT) {
+            const T l = panel[r + j * mp] * inv;
+            panel[r + j * mp] = l;
+            const T lr = rnd(l, lowp);
+            for (int c = j + 1; c < jb; ++c)
+              panel[r + c * mp] = fma(-lr, rnd(panel[j + c * mp], lowp), panel[r + c * mp]);
+          }
+        }
+        __syncthreads();
+      }
+      for (int idx = threadIdx.x; idx < mp * jb; idx += kBT) {
+        const int r = idx % mp, c = idx / mp;
+        W[(ks + r) + (long)(ks + c) * ld] = panel[idx];
+      }
+      for (int j = threadIdx.x; j < jb; j += kBT) piv_out[ks + j] = sh.piv[j];
+      __syncthreads();
+      phase(0);
+      const int nin = k + nbk - ks - jb;  // block columns right of the sub-panel
+      if (!one_level) {
+        // the sub-panel's interchanges on the rest of its block (left and
+        // right of it), so the block's L and U12 are consistently permuted
+        cta_build_pairs(ks, jb, sh);
+        cta_swap_cols(W, ld, sh, smem + mp * jb, smem_elems - mp * jb, k, ks);
+        cta_swap_cols(W, ld, sh, smem + mp * jb, smem_elems - mp * jb, ks + jb, k + nbk);
+        phase(1);
+      }
+      if (nin > 0) {
+        cta_trsm_u12<T>(panel, mp, W + ks + (long)(ks + jb) * ld, ld, jb, nin, lowp);
+        phase(2);
+        cta_gemm_update<T>(panel + jb, mp, W + ks + (long)(ks + jb) * ld, ld,
+                           W + (ks + jb) + (long)(ks + jb) * ld, ld, mp - jb, nin, jb,
+                           smem + mp * jb, lowp);
+        phase(3);
+      }
     }
-    for (int idx = threadIdx.x; idx < mp * jb; idx += kBT) {
-      const int r = idx % mp, c = idx / mp;
-      W[(k + r) + (long)(k + c) * ld] = panel[idx];
-    }
-    for (int j = threadIdx.x; j < jb; j += kBT) piv_out[k + j] = sh.piv[j];
-    __syncthreads();
-    phase(0);
-    // swaps on the other columns (staging space after the panel)
-    cta_apply_swaps(W, n, ld, k, jb, sh, smem + mp * jb, smem_elems - mp * jb);
-    phase(1);
-    const int n2 = n - k - jb;
+    // the block's interchanges on the trailing columns, U12, A22 update
+    const int n2 = n - k - nbk;
     if (n2 > 0) {
-      // U12 = L11^{-1} A12 (one thread per column, L11 from the panel)
-      cta_trsm_u12<T>(panel, mp, W + k + (long)(k + jb) * ld, ld, jb, n2, lowp);
+      T* stage = one_level ? smem + mp * jb : smem;
+      const int stage_elems = one_level ? smem_elems - mp * jb : smem_elems;
+      if (!one_level) {
+        for (int j = threadIdx.x; j < nbk; j += kBT) sh.piv[j] = piv_out[k + j];
+        __syncthreads();
+      }
+      // right of the block at once; left of it deferred to the end
+      cta_build_pairs(k, nbk, sh);
+      cta_swap_cols(W, ld, sh, stage, stage_elems, k + nbk, n);
+      phase(1);
+      // one level: L11 and A21 still in the shared panel; two: from W
+      const T* L11 = one_level ? panel : W + k + (long)k * ld;
+      const int ldl = one_level ? mp : ld;
+      const T* A21 = one_level ? panel + nbk : W + (k + nbk) + (long)k * ld;
+      cta_trsm_u12<T>(L11, ldl, W + k + (long)(k + nbk) * ld, ld, nbk, n2, lowp);
       phase(2);
-      // A22 -= A21 U12, A21 = panel rows jb.. (still in shared memory)
       bool done_tc = false;
       if constexpr (sizeof(T) == 4) {
-        if (tc_tiles && n2 >= 32 && jb <= (lowp ? 64 : 32)) {
-          cta_gemm_update_tc(panel + jb, mp, W + k + (long)(k + jb) * ld, ld,
-                             W + (k + jb) + (long)(k + jb) * ld, ld, n2, n2, jb, lowp, sh,
+        if (tc_tiles && n2 >= 32 && nbk <= (lowp ? 64 : 32)) {
+          cta_gemm_update_tc(A21, ldl, W + k + (long)(k + nbk) * ld, ld,
+                             W + (k + nbk) + (long)(k + nbk) * ld, ld, n2, n2, nbk, lowp, sh,
                              tc_tiles);
           done_tc = true;
         }
       }
       if (!done_tc)
-        cta_gemm_update<T>(panel + jb, mp, W + k + (long)(k + jb) * ld, ld,
-                           W + (k + jb) + (long)(k + jb) * ld, ld, n2, n2, jb,
-                           smem + mp * jb, lowp);
+        cta_gemm_update<T>(A21, ldl, W + k + (long)(k + nbk) * ld, ld,
+                           W + (k + nbk) + (long)(k + nbk) * ld, ld, n2, n2, nbk,
+                           stage, lowp);
     }
     __syncthreads();
     phase(3);
@@ -647,8 +684,7 @@ __device__ __noinline__ int cta_lu(T* W, int n, int ld, int nb, int* piv_out, Sh
       pmap[i] = -1;
     }
     __syncthreads();
-    const int last = ((n - 1) / nb) * nb;
-    for (int kb = last; kb >= 0; kb -= nb) {
+    for (int kb = ((n - 1) / nb) * nb; kb >= 0; kb -= nb) {
       const int jbb = min(nb, n - kb), kn = kb + jbb, rows = n - kn;
       if (rows > 0 && kb < kn) {
         const int cw_max = max(1, min(jbb, cap / rows));
@@ -1286,11 +1322,11 @@ __device__ __noinline__ int cta_fgmres(const double* A, int n, double nA, const 
 }
 
 template <typename T>
-__device__ int factor_sys(T* W, int n, int kind, int nb, int* piv, Shared& sh, T* smem,
+__device__ int factor_sys(T* W, int n, int kind, int nb, int ib, int* piv, Shared& sh, T* smem,
                           unsigned char* tc_tiles,
                           int smem_elems, bool lowp) {
-  return kind == 0 ? cta_lu<T>(W, n, n, nb, piv, sh, smem, smem_elems, lowp, tc_tiles)
-                   : cta_chol<T>(W, n, n, nb, smem, lowp);
+  return kind == 0 ? cta_lu<T>(W, n, n, nb, ib, piv, sh, smem, smem_elems, lowp, tc_tiles)
+                   : cta_chol<T>(W, n, n, ib, smem, lowp);
 }
 
 // The selector's 16 features of one system (written to p.feat[s * 16 ..]):
@@ -1368,7 +1404,7 @@ __device__ __noinline__ int compute_features(const BatchParams& p, const SysDesc
   // FP32 factorization
   for (long i = threadIdx.x; i < (long)n * n; i += kBT) Wf[i] = (float)A[i];
   __syncthreads();
-  const int info = factor_sys<float>(Wf, n, d.kind, d.nb, piv, sh, smf, p.tc ? tc_tiles : nullptr,
+  const int info = factor_sys<float>(Wf, n, d.kind, d.nb, d.ib, piv, sh, smf, p.tc ? tc_tiles : nullptr,
                                      kSmemPanel / (int)sizeof(float), false);
   double umax = 0.0, dmin = 0.0, dmax = 0.0;
   block_sum_max(n, [&](int j) {
@@ -1587,7 +1623,7 @@ batched_solve_kernel(BatchParams p) {
       if (!have32) {
         for (long i = threadIdx.x; i < (long)n * n; i += kBT) Wf[i] = (float)A[i];
         __syncthreads();
-        info = factor_sys<float>(Wf, n, d.kind, d.nb, piv, sh, smf, p.tc ? tc_tiles : nullptr,
+        info = factor_sys<float>(Wf, n, d.kind, d.nb, d.ib, piv, sh, smf, p.tc ? tc_tiles : nullptr,
                                  kSmemPanel / (int)sizeof(float), pr == 2);
         if (info == 0) {
           if (d.kind == 0)
@@ -1633,7 +1669,7 @@ batched_solve_kernel(BatchParams p) {
         }
         __syncthreads();
         mark(4, t_ir);
-        const int kry_budget = p.kry_max > 0 ? p.kry_max : max(p.kry_m, n / 6);
+        const int kry_budget = p.kry_max > 0 ? p.kry_max : max(16, n / -p.kry_max);
         if (!done && p.method != 1) {
           const unsigned long long t_kr = globaltimer_ns();
           // LU-IR stalled (or was skipped): FGMRES-IR per right-hand side
@@ -1673,7 +1709,7 @@ batched_solve_kernel(BatchParams p) {
       __syncthreads();
       int nb64 = max(1, min(d.nb, (kSmemPanel / 8 - 64 * 64) / max(n, 1)));
       if (nb64 > 8) nb64 = nb64 / 8 * 8;
-      const int info = factor_sys<double>(Wd, n, d.kind, nb64, piv, sh, smd, nullptr,
+      const int info = factor_sys<double>(Wd, n, d.kind, nb64, nb64, piv, sh, smd, nullptr,
                                           kSmemPanel / (int)sizeof(double), false);
       res.info = info;
       if (info == 0) {
@@ -1743,19 +1779,23 @@ struct BatchPlan {
   double flops = 0;
 };
 
-static int pick_nb(int n, int prec, const int* nb_table) {
+// Block width nb (from the tuned table, <= 64) and the shared-memory panel
+// width ib <= nb: the panel (n x ib) plus a 64-column staging tile fit the
+// budget.  Multiples of 8 (the register-resident U12 solves take 8 / 16 / 32).
+static void pick_nb(int n, int prec, const int* nb_table, int* nb_out, int* ib_out) {
   // size buckets: <=32, <=64, <=128, <=256, <=512, <=1024, <=2048, larger
   int b = 0;
   for (int lim = 32; b < 7 && n > lim; lim *= 2) ++b;
   int nb = nb_table ? nb_table[b] : 32;
   if (nb <= 0) nb = 32;
-  const int es = prec == 0 ? 8 : 4;  // the FP64 path re-caps nb for itself
-  // panel (n x nb) plus a 64-column staging tile within the budget
-  const int cap = (kSmemPanel / es - 64 * 64) / std::max(n, 1);
-  nb = std::min(nb, std::max(cap, 1));
   nb = std::max(1, std::min(nb, 64));
-  if (nb > 8) nb = nb / 8 * 8;  // the register-resident U12 solves take 8 / 16 / 32
-  return nb;
+  if (nb > 8) nb = nb / 8 * 8;
+  const int es = prec == 0 ? 8 : 4;  // the FP64 path re-caps for itself
+  const int cap = (kSmemPanel / es - 64 * 64) / std::max(n, 1);
+  int ib = std::min(nb, std::max(cap, 1));
+  if (ib > 8) ib = ib / 8 * 8;
+  *nb_out = nb;
+  *ib_out = ib;
 }
 
 cudaError_t batched_plan(Context* ctx, int count, const int* h_n, const int* h_kind,
@@ -1767,9 +1807,11 @@ cudaError_t batched_plan(Context* ctx, int count, const int* h_n, const int* h_k
   *out = nullptr;
   if (q < 1 || q > kBQ) return cudaErrorInvalidValue;
   kry_m = kry_m > 0 ? std::min(kry_m, kKryMax) : 30;
-  // <= 0: per-system budget max(kry_m, n / 6) inner iterations, which keeps
-  // FGMRES's FP64 work (2 n^2 per iteration) under half an FP64 LU's
-  kry_max = kry_max > 0 ? kry_max : -1;
+  // <= 0: per-system budget max(16, n / 24) inner iterations: an iteration
+  // (FP64 matrix-vector product + FP64-arithmetic triangular solves, both
+  // bandwidth-bound in one CTA) costs ~12 / n of an FP64 LU, so FGMRES stays
+  // under ~half of the factorization it would save
+  kry_max = kry_max > 0 ? kry_max : (kry_max < 0 ? kry_max : -24);
   if (method == 1) kry_m = 1;  // no Krylov workspace beyond a token
   auto* P = new BatchPlan();
   P->ctx = ctx;
@@ -1783,7 +1825,7 @@ cudaError_t batched_plan(Context* ctx, int count, const int* h_n, const int* h_k
     s.n = h_n[i];
     s.kind = h_kind ? h_kind[i] : 0;
     s.prec = h_prec ? h_prec[i] : 1;
-    s.nb = pick_nb(s.n, s.prec, nb_table);
+    pick_nb(s.n, s.prec, nb_table, &s.nb, &s.ib);
     s.a_off = aoff;
     s.b_off = boff;
     aoff += (long)s.n * s.n;
@@ -1943,7 +1985,7 @@ int ElGBBatchedPlanCreate(ElGBContext ctx, int count, const int* n, int nrhs, co
         (o.precision && (o.precision[i] < 0 || o.precision[i] > 2)))
       return elgb::kElArgError;
   if (o.method < 0 || o.method > 2 || o.gmres_restart < 0 || o.gmres_restart > 32 ||
-      o.gmres_max_iters < 0)
+      o.gmres_max_iters < -4096)
     return elgb::kElArgError;
   *plan = nullptr;
   elgb::BatchPlan* p = nullptr;

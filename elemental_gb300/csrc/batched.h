@@ -26,7 +26,7 @@ struct BatchPlan;
 // fallback: FP64 refactorization when refinement does not converge; mode 1
 // computes the selector's 16 features per system into feat instead of
 // solving.  method: 0 LU-IR, then FGMRES-IR (restart kry_m, at most kry_max
-// inner iterations per right-hand side, <= 0: max(kry_m, n / 6)) when LU-IR stalls; 1 LU-IR only;
+// inner iterations per right-hand side; 0: max(16, n / 24), -d: max(16, n / d)) when LU-IR stalls; 1 LU-IR only;
 // 2 FGMRES-IR only.  prec_dev (device, may be null): per-system precision
 // read when the graph runs, overriding h_prec (the selector's output).
 // phase_ns (device, may be null): count x 10 device times per system: panel,

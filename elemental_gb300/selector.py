@@ -113,14 +113,14 @@ def extract_features(systems, ctx=None, nb_table=None):
 
 
 def solve_with(systems, precisions, fallback=True, method="auto", ctx=None, nb_table=None,
-               tol=1e-13, precision_device=None):
+               tol=1e-13, precision_device=None, gmres_max_iters=0):
     """Solve every system with the given per-system precision names (or a
     device int32 array of codes); returns (results, ms, X)."""
     ctx = ctx or context()
     solver = BatchedSolver(systems["ns"], systems["nrhs"], systems["A"], systems["B"],
                            precisions=precisions, fallback=fallback, method=method,
                            nb_table=nb_table, tol=tol, precision_device=precision_device,
-                           ctx=ctx)
+                           gmres_max_iters=gmres_max_iters, ctx=ctx)
     try:
         ms = _timed(ctx, solver.run)
         return solver.results(), ms, solver.X
@@ -128,7 +128,7 @@ def solve_with(systems, precisions, fallback=True, method="auto", ctx=None, nb_t
         solver.close()
 
 
-def outcome_labels(systems, ctx=None, nb_table=None, tol=1e-13):
+def outcome_labels(systems, ctx=None, nb_table=None, tol=1e-13, gmres_max_iters=0):
     """Label of each system: the lowest precision (highest class code) whose
     refinement reached `tol` with the fallback switched off."""
     count = len(systems["ns"])
@@ -136,7 +136,7 @@ def outcome_labels(systems, ctx=None, nb_table=None, tol=1e-13):
     info = {}
     for code in (1, 2):
         res, ms, _ = solve_with(systems, [CLASSES[code]] * count, fallback=False, ctx=ctx,
-                                nb_table=nb_table, tol=tol)
+                                nb_table=nb_table, tol=tol, gmres_max_iters=gmres_max_iters)
         ok = np.array([r["converged"] for r in res])
         labels[ok] = code
         info[CLASSES[code]] = dict(ms=ms, converged=int(ok.sum()))
@@ -327,7 +327,8 @@ def rule_network(t_bf16, t_fp32, slope=1e4, device="cuda"):
     return torch.from_numpy(th).to(device)
 
 
-def solve_selected(systems, params, ctx=None, nb_table=None, tol=1e-13, phases=False):
+def solve_selected(systems, params, ctx=None, nb_table=None, tol=1e-13, phases=False,
+                   gmres_max_iters=0):
     """The fused select-and-solve launch: per system, features from an FP32
     LU (kept), the network `params`' class, then the solve in that
     precision (BF16 / FP32 classes refine with the kept FP32 factors, FP64
@@ -336,7 +337,7 @@ def solve_selected(systems, params, ctx=None, nb_table=None, tol=1e-13, phases=F
     ctx = ctx or context()
     solver = BatchedSolver(systems["ns"], systems["nrhs"], systems["A"], systems["B"],
                            selector_params=params, nb_table=nb_table, tol=tol, phases=phases,
-                           ctx=ctx)
+                           gmres_max_iters=gmres_max_iters, ctx=ctx)
     ms = _timed(ctx, solver.run)
     return solver.results(), ms, solver
 

@@ -207,8 +207,9 @@ typedef struct {
   float* features;
   int method;          /* 0 LU-IR then FGMRES-IR on stall, 1 LU-IR, 2 FGMRES-IR */
   int gmres_restart;   /* FGMRES restart length, <= 32 (0: 30) */
-  int gmres_max_iters; /* FGMRES iterations per right-hand side (0: max(restart,
-                          n / 6), under half the FP64 work of an FP64 LU) */
+  int gmres_max_iters; /* FGMRES iterations per right-hand side; 0: max(16,
+                          n / 24) (under ~half the time of an FP64 LU);
+                          negative -d: max(16, n / d) */
   const int* precision_device; /* device int per system, read at each Execute
                                   (overrides precision; e.g. the selector's
                                   ElGBMLPForward argmax), or NULL */

@@ -163,3 +163,24 @@ def test_batched_features(ctx):
         ratio = r["backward_error"] / kap[i]
         assert 0.1 <= ratio <= 1.01, (i, ratio)
         assert abs(F[i, 1] - np.log10(r["backward_error"])) < 1e-3
+
+
+@pytest.mark.parametrize("prec", ["fp32", "bf16"])
+def test_batched_two_level_blocking(ctx, prec):
+    """n ~ 1300 with a 32-column block but a shared-memory panel of at most 24
+    columns: sub-panels update only their block, the block updates the
+    trailing matrix with K = 32 (tensor cores).  The factorization must be
+    as good as a one-level one: LU-IR converges in a few steps, no fallback."""
+    q = 1
+    systems, kinds = make(3, 1250, 1350, q, 31, spd_every=1000)
+    ns, A, B = BatchedSolver.pack(systems, q)
+    # BF16 factors need FGMRES-IR at this size (kappa * u_bf16 > 1)
+    bs = BatchedSolver(ns, q, A, B, kinds=kinds, precisions=[prec] * len(ns),
+                       nb_table=[32] * 8, fallback=False,
+                       method="lu-ir" if prec == "fp32" else "auto", ctx=ctx)
+    bs.run()
+    for i, ((Ai, Bi), r) in enumerate(zip(systems, bs.results())):
+        assert r["converged"] and not r["fell_back"], (i, r)
+        if prec == "fp32":
+            assert r["iterations"] <= 4, (i, r)
+        assert O.backward_error(Ai, bs.solution(i), Bi) <= 1e-13
