@@ -22,7 +22,8 @@ P = ctypes.POINTER
 class RefineCtrl(ctypes.Structure):
     """ElGBRefineCtrl (include/elgb300.h)."""
     _fields_ = [("precision", c_int), ("method", c_int), ("tol", c_double),
-                ("max_iters", c_int), ("restart", c_int), ("fallback", c_int), ("nb", c_int)]
+                ("max_iters", c_int), ("restart", c_int), ("fallback", c_int), ("nb", c_int),
+                ("pivoting", c_int)]
 
 
 class RefineInfo(ctypes.Structure):

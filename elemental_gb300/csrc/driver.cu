@@ -119,14 +119,15 @@ static size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
 template <typename T>
 static size_t panel_scratch_bytes(int maxG) {
-  return align256(2 * (size_t)maxG * sizeof(PanelSlot<T>));
+  return align256(2 * (size_t)maxG * sizeof(PanelSlot<T>)) +
+         align256(calu_scratch_ints(maxG) * sizeof(int));
 }
-
 template <typename T>
 static PanelScratch<T> carve_panel(Carver& cv, int maxG) {
   PanelScratch<T> s;
   s.slots = cv.take<PanelSlot<T>>(2 * (size_t)maxG);
   s.maxG = maxG;
+  s.cand = cv.take<int>(calu_scratch_ints(maxG));
   return s;
 }
 
@@ -219,6 +220,9 @@ struct LuState {
   T* Bc;               // companion block receiving the same row operations
   long ldbc;           // (RowEchelon's B, src/lapack_like/solve/Linear.cpp:62-71)
   int nbc;
+  int* dlab;           // deferred left interchanges: labels per block column
+  T* dtmp;             //   and the gather's scratch
+  bool tournament;     // FP32 leaf panels by tournament pivoting
 };
 
 // Blocked TRSM, left / lower / unit: B := L11^{-1} B with L11 nb x nb (any
@@ -273,10 +277,24 @@ static cudaError_t panel_rec(LuState<T>& s, const LuLane& L, int c0, int w) {
   Context* ctx = s.ctx;
   if (w <= 32) {
     const int pi = ctx->prof_begin(L.st);
-    LANE_CHECK(launch_getf2_panel<T>(s.A + c0 + (long)c0 * s.lda, s.lda, s.m - c0, w,
-                                     s.ipiv + c0, c0, c0, s.panel_epoch, s.ps, ctx->status,
-                                     s.panel_ctas, L.st), 1);
-    s.panel_epoch += w;
+    bool done = false;
+    if constexpr (sizeof(T) == 4) {
+      if (s.tournament) {
+        int nl = 0;
+        const cudaError_t e = launch_calu_panel(
+            reinterpret_cast<float*>(s.A) + c0 + (long)c0 * s.lda, s.lda, s.m - c0, w,
+            s.ipiv + c0, c0, c0, s.ps.cand, s.ps.maxG, ctx->status, s.panel_ctas, L.st, &nl);
+        ctx->launches += nl;
+        if (e == cudaSuccess) done = true;
+        else if (e != cudaErrorNotSupported) return e;
+      }
+    }
+    if (!done) {
+      LANE_CHECK(launch_getf2_panel<T>(s.A + c0 + (long)c0 * s.lda, s.lda, s.m - c0, w,
+                                       s.ipiv + c0, c0, c0, s.panel_epoch, s.ps, ctx->status,
+                                       s.panel_ctas, L.st), 1);
+      s.panel_epoch += w;
+    }
     ctx->prof_end(pi, L.st, ELGB_PROF_PANEL, (double)(s.m - c0) * w * w,
                   2.0 * sizeof(T) * (s.m - c0) * (double)w);
     return cudaSuccess;
@@ -354,7 +372,8 @@ static cudaError_t getrf_run(LuState<T>& s, int nb) {
     const int jb = std::min(nb, minDim - k);
     const int kn = k + jb;
     const int jb2 = std::min(nb, std::max(minDim - kn, 0));
-    e = apply_swaps(s, s.main, k, jb, 0, k, kn, s.n, true);
+    // right of the panel now; left of it (earlier L columns) deferred
+    e = apply_swaps(s, s.main, k, jb, 0, 0, kn, s.n, true);
     if (e != cudaSuccess) return e;
     if (jb2 > 0) {
       // the next panel's block column first
@@ -380,19 +399,32 @@ static cudaError_t getrf_run(LuState<T>& s, int nb) {
       if (e != cudaSuccess) return e;
     }
   }
+  // every block column of L takes the later panels' interchanges at once
+  const int pi = ctx->prof_begin(s.main.st);
+  LANE_CHECK(launch_defer_labels(s.ipiv, s.m, minDim, nb, s.dlab, s.main.st), 1);
+  LANE_CHECK(launch_defer_gather<T>(s.A, s.lda, s.m, minDim, nb, s.dlab, s.dtmp,
+                                    defer_gather_grid(ctx->num_sms), s.main.st), 1);
+  ctx->prof_end(pi, s.main.st, ELGB_PROF_SWAP, 0.0,
+                8.0 * sizeof(T) * 0.5 * (double)s.m * minDim);
   return cudaSuccess;
 }
 
 template <typename T>
-static size_t getrf_scratch_bytes(const Context* ctx, int nb) {
+static size_t getrf_scratch_bytes(const Context* ctx, int nb, int m, int n) {
   const int cap = std::max(nb, 32);
+  const size_t nblk = (size_t)(std::min(m, n) + nb - 1) / std::max(nb, 1);
   return panel_scratch_bytes<T>(ctx->num_sms) + 2 * align256(4 * (size_t)cap * sizeof(int)) +
-         2 * align256(sizeof(int));
+         2 * align256(sizeof(int)) + align256(nblk * (size_t)m * sizeof(int)) +
+         align256((size_t)defer_gather_grid(ctx->num_sms) * m * sizeof(T));
 }
 
 template <typename T>
-static cudaError_t setup_lu_state(Context* ctx, LuState<T>& s, Carver& cv, int nb) {
+static cudaError_t setup_lu_state(Context* ctx, LuState<T>& s, Carver& cv, int nb, int m, int n) {
   const int cap = std::max(nb, 32);
+  const size_t nblk = (size_t)(std::min(m, n) + nb - 1) / std::max(nb, 1);
+  s.dlab = cv.take<int>(nblk * (size_t)m);
+  s.dtmp = cv.take<T>((size_t)defer_gather_grid(ctx->num_sms) * m);
+  if (!s.dtmp) return cudaErrorMemoryAllocation;
   s.ctx = ctx;
   s.ps = carve_panel<T>(cv, ctx->num_sms);
   s.panel_ctas = ctx->num_sms;
@@ -414,7 +446,8 @@ static cudaError_t setup_lu_state(Context* ctx, LuState<T>& s, Carver& cv, int n
 static bool use_lookahead(int m, int n, int nb) { return std::min(m, n) >= 4 * nb && n >= 2048; }
 
 template <typename T>
-cudaError_t getrf(Context* ctx, int m, int n, T* A, long lda, int* ipiv, int nb, int tc_kind) {
+cudaError_t getrf(Context* ctx, int m, int n, T* A, long lda, int* ipiv, int nb, int tc_kind,
+                  bool tournament) {
   if (nb <= 0) nb = g_blocksize;
   cudaError_t e = ctx->begin_call();
   if (e != cudaSuccess) return e;
@@ -429,11 +462,11 @@ cudaError_t getrf(Context* ctx, int m, int n, T* A, long lda, int* ipiv, int nb,
                     tc_gemm_workspace_bytes(inner_kind, m, std::max(n, nb), nb))
          : 0;
   const size_t tcs = (tc && la) ? tc_gemm_workspace_bytes(inner_kind, m, nb, nb) : 0;
-  e = ctx->ensure(getrf_scratch_bytes<T>(ctx, nb) + align256(tcb) + align256(tcs));
+  e = ctx->ensure(getrf_scratch_bytes<T>(ctx, nb, m, n) + align256(tcb) + align256(tcs));
   if (e != cudaSuccess) return e;
   Carver cv(ctx);
   LuState<T> s{};
-  e = setup_lu_state(ctx, s, cv, nb);
+  e = setup_lu_state(ctx, s, cv, nb, m, n);
   if (e != cudaSuccess) return e;
   if (tc) {
     s.main.gemm.tc_kind = inner_kind;
@@ -450,6 +483,7 @@ cudaError_t getrf(Context* ctx, int m, int n, T* A, long lda, int* ipiv, int nb,
     }
   }
   if (ctx->opt_panel_ctas > 0) s.panel_ctas = std::min(ctx->opt_panel_ctas, ctx->num_sms);
+  s.tournament = tournament && sizeof(T) == 4;
   s.A = A;
   s.lda = lda;
   s.m = m;
@@ -610,12 +644,12 @@ cudaError_t linear_solve(Context* ctx, int n, const T* A, long lda, int nrhs, T*
   cudaError_t e = ctx->begin_call();
   if (e != cudaSuccess) return e;
   if (n == 0) return cudaSuccess;
-  e = ctx->ensure(getrf_scratch_bytes<T>(ctx, nb) + align256((size_t)n * n * sizeof(T)) +
+  e = ctx->ensure(getrf_scratch_bytes<T>(ctx, nb, n, n) + align256((size_t)n * n * sizeof(T)) +
                   align256((size_t)n * sizeof(int)));
   if (e != cudaSuccess) return e;
   Carver cv(ctx);
   LuState<T> s{};
-  e = setup_lu_state(ctx, s, cv, nb);
+  e = setup_lu_state(ctx, s, cv, nb, n, n);
   if (e != cudaSuccess) return e;
   T* W = cv.take<T>((size_t)n * n);
   int* ipiv = cv.take<int>(n);
@@ -734,8 +768,8 @@ cudaError_t backward_error(Context* ctx, int n, int q, const double* A, long lda
   return cudaSuccess;
 }
 
-template cudaError_t getrf<double>(Context*, int, int, double*, long, int*, int, int);
-template cudaError_t getrf<float>(Context*, int, int, float*, long, int*, int, int);
+template cudaError_t getrf<double>(Context*, int, int, double*, long, int*, int, int, bool);
+template cudaError_t getrf<float>(Context*, int, int, float*, long, int*, int, int, bool);
 template cudaError_t getrs<double>(Context*, int, int, const double*, long, const int*, int,
                                    double*, long, const int*);
 template cudaError_t getrs<float>(Context*, int, int, const float*, long, const int*, int,
@@ -871,6 +905,9 @@ int ElGBSetOption(ElGBContext ctx, int option, int value) {
       if (value < 0) return elgb::kElArgError;
       ctx->opt_panel_ctas = value;
       return 0;
+    case ELGB_OPT_TOURNAMENT:
+      ctx->opt_tournament = value ? 1 : 0;
+      return 0;
     default:
       return elgb::kElArgError;
   }
@@ -937,7 +974,8 @@ int ElGBLUPartialPivMixed_s(ElGBContext ctx, int m, int n, float* A, int lda, in
                      gemm_kind >= -1 && gemm_kind <= 3 && (m * n == 0 || (A && swapDests))))
     return r;
   if (nb <= 0) nb = 512;
-  return elgb::to_el_error(elgb::getrf<float>(ctx, m, n, A, lda, swapDests, nb, gemm_kind));
+  return elgb::to_el_error(elgb::getrf<float>(ctx, m, n, A, lda, swapDests, nb, gemm_kind,
+                                              ctx->opt_tournament != 0));
 }
 
 int ElGBGemmSubTC(ElGBContext ctx, int gemm_kind, int m, int n, int k, const float* A, int lda,

@@ -35,6 +35,7 @@ struct Context {
   long long launches = 0;         // kernels enqueued by this context
   int opt_lookahead = 1;          // ElGBSetOption(ELGB_OPT_LOOKAHEAD)
   int opt_panel_ctas = 0;         // ElGBSetOption(ELGB_OPT_PANEL_CTAS), 0 = automatic
+  int opt_tournament = 0;         // ElGBSetOption(ELGB_OPT_TOURNAMENT)
   void* arena2 = nullptr;  // second arena for drivers that call the ones above
   size_t arena2_bytes = 0;
 
@@ -73,7 +74,7 @@ void set_blocksize(int nb);
 
 template <typename T>
 cudaError_t getrf(Context* ctx, int m, int n, T* A, long lda, int* ipiv, int nb,
-                  int tc_kind = -1);
+                  int tc_kind = -1, bool tournament = false);
 template <typename T>
 cudaError_t getrs(Context* ctx, int orient, int n, const T* A, long lda, const int* ipiv,
                   int nrhs, T* B, long ldb, const int* perm);

@@ -342,7 +342,7 @@ cudaError_t refined_solve(Context* ctx, int n, const double* A, long lda, int nr
     cvt_f64_f32_kernel<<<dim3((n + 255) / 256, n), 256, 0, ctx->stream>>>(A, lda, n, n, w.Af, n);
     ctx->launches += 1;
     IR_CHECK(cudaGetLastError());
-    IR_CHECK(getrf<float>(ctx, n, n, w.Af, n, w.ipiv, c.nb, tc_kind));
+    IR_CHECK(getrf<float>(ctx, n, n, w.Af, n, w.ipiv, c.nb, tc_kind, c.pivoting == 1));
     IR_CHECK(cudaMemcpyAsync(ctx->h_status, ctx->status, sizeof(DevStatus),
                              cudaMemcpyDeviceToHost, ctx->stream));
     IR_CHECK(cudaStreamSynchronize(ctx->stream));
@@ -582,7 +582,8 @@ extern "C" int ElGBRefinedSolve_d(ElGBContext ctx, int n, const double* A, int l
     c.precision = ELGB_PREC_FP32;
     c.fallback = 1;
   }
-  if (c.precision < ELGB_PREC_FP64 || c.precision > ELGB_PREC_FP8 || c.method < 0 ||
+  if (c.pivoting < 0 || c.pivoting > 1 || c.precision < ELGB_PREC_FP64 ||
+      c.precision > ELGB_PREC_FP8 || c.method < 0 ||
       c.method > 1)
     return elgb::kElArgError;
   auto* cx = static_cast<elgb::Context*>(ctx);

@@ -28,7 +28,17 @@ template <typename T>
 struct PanelScratch {
   PanelSlot<T>* slots;
   int maxG;
+  int* cand;  // tournament pivoting: maxG x 33 candidate lists
 };
+
+// Tournament-pivoted leaf panel of the FP32 (preconditioner) LU, w <= 32
+// (calu.cu): same outputs as launch_getf2_panel (ipiv, the factored panel,
+// info), pivots chosen by a reduction tree.  cudaErrorNotSupported when the
+// candidate set does not fit in shared memory (the caller then uses getf2).
+size_t calu_scratch_ints(int max_ctas);
+cudaError_t launch_calu_panel(float* A, long lda, int mp, int w, int* ipiv, int row_base,
+                              int info_base, int* cand, int max_ctas, DevStatus* st,
+                              int num_sms, cudaStream_t stream, int* nlaunch);
 
 // getf2 on a w-wide panel (w <= 32): El's lu::Panel
 // (src/lapack_like/factor/LU/Panel.hpp:15-59) as one cooperative launch.
@@ -59,6 +69,20 @@ cudaError_t launch_apply_swap_pairs(T* A, long lda, int c0a, int c1a,
                                     int c0b, int c1b, const int* pairs,
                                     const int* count, int nb,
                                     cudaStream_t stream);
+
+// Deferred interchanges of the blocked LU's left columns.  Block column b
+// (columns [b nb, (b+1) nb)) must end up with every later panel's row
+// interchanges applied; instead of swapping those rows after each panel,
+// lab[b m + r] (r >= (b+1) nb) receives the original row whose content ends
+// at row r after the interchanges ipiv[(b+1) nb .. mn), and the gather
+// A(r, c) <- A(lab[r], c) applies them once per column (coalesced writes,
+// L2-resident reads).  tmp: gridDim x m elements of scratch.
+cudaError_t launch_defer_labels(const int* ipiv, int m, int mn, int nb, int* lab,
+                                cudaStream_t stream);
+template <typename T>
+cudaError_t launch_defer_gather(T* A, long lda, int m, int mn, int nb, const int* lab, T* tmp,
+                                int grid, cudaStream_t stream);
+int defer_gather_grid(int num_sms);
 
 // Explicit permutation vector from a whole swap sequence:
 // perm[i] = the original row that ends up at row i

@@ -424,6 +424,88 @@ template cudaError_t launch_apply_swap_pairs<float>(float*, long, int, int, int,
                                                     const int*, const int*, int,
                                                     cudaStream_t);
 
+// ---- deferred left interchanges ----------------------------------------------
+// One CTA per block column b: replay the interchanges of every later panel
+// on row labels (shared memory when they fit, else in place in global
+// memory), serially in one thread -- the replay is inherently ordered.
+__global__ void defer_labels_kernel(const int* __restrict__ ipiv, int m, int mn, int nb,
+                                    int* __restrict__ lab, int use_smem) {
+  extern __shared__ int sl[];
+  const int b = blockIdx.x;
+  const int base = (b + 1) * nb;
+  if (base >= m || base >= mn) return;
+  const int rows = m - base;
+  int* L = use_smem ? sl : lab + (long)b * m + base;
+  for (int i = threadIdx.x; i < rows; i += blockDim.x) L[i] = base + i;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int t = base; t < mn; ++t) {
+      const int p = ipiv[t];  // partial pivoting: p >= t >= base
+      if (p != t) {
+        const int a = L[t - base];
+        L[t - base] = L[p - base];
+        L[p - base] = a;
+      }
+    }
+  }
+  __syncthreads();
+  if (use_smem)
+    for (int i = threadIdx.x; i < rows; i += blockDim.x) lab[(long)b * m + base + i] = L[i];
+}
+
+// Columns c < (last block start): A(r, c) <- A(lab_b[r], c) for r >= base_b,
+// through the CTA's own m-element slice of tmp.
+template <typename T>
+__global__ void __launch_bounds__(256)
+defer_gather_kernel(T* __restrict__ A, long lda, int m, int mn, int nb,
+                    const int* __restrict__ lab, T* __restrict__ tmp) {
+  const int nblk = (mn + nb - 1) / nb;
+  const int ncols = (nblk - 1) * nb;  // the last block column has no later panel
+  T* t = tmp + (long)blockIdx.x * m;
+  for (int c = blockIdx.x; c < ncols; c += gridDim.x) {
+    const int b = c / nb, base = (b + 1) * nb;
+    if (base >= m) continue;
+    const int* lb = lab + (long)b * m;
+    T* col = A + (long)c * lda;
+    for (int r = base + threadIdx.x; r < m; r += blockDim.x) t[r] = col[lb[r]];
+    __syncthreads();
+    for (int r = base + threadIdx.x; r < m; r += blockDim.x) col[r] = t[r];
+    __syncthreads();
+  }
+}
+
+int defer_gather_grid(int num_sms) { return 2 * num_sms; }
+
+cudaError_t launch_defer_labels(const int* ipiv, int m, int mn, int nb, int* lab,
+                                cudaStream_t stream) {
+  const int nblk = (mn + nb - 1) / nb;
+  if (nblk <= 1) return cudaSuccess;
+  const size_t smem = (size_t)m * sizeof(int);
+  const bool use_smem = smem <= 200 * 1024;
+  if (use_smem && smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(defer_labels_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  defer_labels_kernel<<<nblk - 1, 256, use_smem ? smem : 0, stream>>>(ipiv, m, mn, nb, lab,
+                                                                      use_smem ? 1 : 0);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_defer_gather(T* A, long lda, int m, int mn, int nb, const int* lab, T* tmp,
+                                int grid, cudaStream_t stream) {
+  const int nblk = (mn + nb - 1) / nb;
+  if (nblk <= 1) return cudaSuccess;
+  defer_gather_kernel<T><<<grid, 256, 0, stream>>>(A, lda, m, mn, nb, lab, tmp);
+  return cudaGetLastError();
+}
+
+template cudaError_t launch_defer_gather<double>(double*, long, int, int, int, const int*, double*,
+                                                 int, cudaStream_t);
+template cudaError_t launch_defer_gather<float>(float*, long, int, int, int, const int*, float*,
+                                                int, cudaStream_t);
+
 // Explicit permutation vector of a whole swap sequence (one thread; the
 // labels live in shared memory when they fit).
 __global__ void explicit_perm_kernel(const int* __restrict__ ipiv, int nswaps, int n,

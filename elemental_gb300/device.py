@@ -109,8 +109,9 @@ class Context:
                 f"info = {info}")
 
     def set_option(self, option, value):
-        """ElGBSetOption: option "lookahead" (0/1) or "panel_ctas" (0 = auto)."""
-        code = {"lookahead": 1, "panel_ctas": 2}[option]
+        """ElGBSetOption: "lookahead" (0/1), "panel_ctas" (0 = auto) or
+        "tournament" (0/1: tournament pivoting in lu_mixed's leaf panels)."""
+        code = {"lookahead": 1, "panel_ctas": 2, "tournament": 3}[option]
         self._rc(self.lib.ElGBSetOption(self.h, code, int(value)), "SetOption")
 
     def launches(self):
@@ -169,15 +170,17 @@ class Context:
         return C
 
     def refined_solve(self, A, B, X=None, precision="fp32", method="lu-ir", tol=0.0,
-                      max_iters=0, restart=0, fallback=True, nb=0):
+                      max_iters=0, restart=0, fallback=True, nb=0, pivoting="partial"):
         """Mixed-precision solve A X = B (FP64 in/out): low-precision LU on the
-        tensor cores + LU-IR or GMRES-IR with an FP64 residual, FP64 LU as the
-        fallback.  Returns (X, info dict)."""
+        tensor cores (partial pivoting as El::LU, or "tournament" pivoting of
+        the leaf panels) + LU-IR or GMRES-IR with an FP64 residual, FP64 LU
+        as the fallback.  Returns (X, info dict)."""
         n, q = B.shape
         if X is None:
             X = colmajor(n, q, torch.float64, A.device)
         ctrl = _lib.RefineCtrl(PRECISIONS[precision], METHODS[method], float(tol),
-                               int(max_iters), int(restart), 1 if fallback else 0, int(nb))
+                               int(max_iters), int(restart), 1 if fallback else 0, int(nb),
+                               {"partial": 0, "tournament": 1}[pivoting])
         inf = _lib.RefineInfo()
         self._bind()
         self._rc(self.lib.ElGBRefinedSolve_d(self.h, n, _ptr(A), _ld(A), q, _ptr(B), _ld(B),

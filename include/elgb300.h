@@ -48,8 +48,11 @@ int ElGBSetBlocksize(int nb);
 /* Tuning switches of a context:
  *   ELGB_OPT_LOOKAHEAD  1 (default): factor the next panel on a second
  *                       stream while the trailing update runs; 0: in order
- *   ELGB_OPT_PANEL_CTAS CTAs of a panel launch, 0 (default) = automatic */
-enum { ELGB_OPT_LOOKAHEAD = 1, ELGB_OPT_PANEL_CTAS = 2 };
+ *   ELGB_OPT_PANEL_CTAS CTAs of a panel launch, 0 (default) = automatic
+ *   ELGB_OPT_TOURNAMENT 1: ElGBLUPartialPivMixed_s picks its leaf panels'
+ *                       pivots by tournament (CALU); 0 (default): partial
+ *                       pivoting, El::LU's pivot sequence */
+enum { ELGB_OPT_LOOKAHEAD = 1, ELGB_OPT_PANEL_CTAS = 2, ELGB_OPT_TOURNAMENT = 3 };
 int ElGBSetOption(ElGBContext ctx, int option, int value);
 
 /* Number of kernel launches this context has issued so far. */
@@ -137,6 +140,10 @@ typedef struct {
   int fallback;   /* nonzero: FP64 LU when the low-precision factor is
                      singular or refinement stalls                           */
   int nb;         /* blocksize of the low-precision factorization; <= 0: 512 */
+  int pivoting;   /* low-precision LU's pivoting: 0 partial pivoting
+                     (El::LU's; default), 1 tournament (CALU: the leaf
+                     panel's pivots by a reduction tree of small partial-
+                     pivoting eliminations, no per-column grid exchange) */
 } ElGBRefineCtrl;
 
 typedef struct {
