@@ -372,8 +372,12 @@ static cudaError_t getrf_run(LuState<T>& s, int nb) {
     const int jb = std::min(nb, minDim - k);
     const int kn = k + jb;
     const int jb2 = std::min(nb, std::max(minDim - kn, 0));
-    // right of the panel now; left of it (earlier L columns) deferred
-    e = apply_swaps(s, s.main, k, jb, 0, 0, kn, s.n, true);
+    // interchanges right of the panel (left of it, earlier L columns, are
+    // deferred to the end); with look-ahead the next panel's block column
+    // goes first, so only its share of the swap sits on the critical path
+    const bool split = la && jb2 > 0;
+    e = split ? apply_swaps(s, s.main, k, jb, kn, kn + jb2, 0, 0, false)
+              : apply_swaps(s, s.main, k, jb, 0, 0, kn, s.n, true);
     if (e != cudaSuccess) return e;
     if (jb2 > 0) {
       // the next panel's block column first
@@ -386,6 +390,10 @@ static cudaError_t getrf_run(LuState<T>& s, int nb) {
         if (e == cudaSuccess) e = cudaEventRecord(ctx->ev_join, s.side.st);
         if (e != cudaSuccess) return e;
       }
+    }
+    if (split) {
+      e = apply_swaps(s, s.main, k, jb, kn + jb2, s.n, 0, 0, true);
+      if (e != cudaSuccess) return e;
     }
     e = update_cols(s, s.main, k, jb, kn + jb2, s.n);
     if (e != cudaSuccess) return e;

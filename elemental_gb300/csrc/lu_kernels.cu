@@ -40,6 +40,26 @@ __device__ __forceinline__ void block_argmax(T& v, int& r, T* s_v, int* s_r) {
   r = s_r[32];
 }
 
+// The same without the leading barrier, for callers whose previous readers of
+// s_v / s_r are already behind a barrier.
+template <typename T>
+__device__ __forceinline__ void block_argmax_nolead(T& v, int& r, T* s_v, int* s_r) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nwarps = blockDim.x >> 5;
+  warp_argmax(v, r);
+  if (lane == 0) {
+    s_v[warp] = v;
+    s_r[warp] = r;
+  }
+  __syncthreads();
+  // every warp reduces the per-warp results (no second broadcast barrier)
+  T wv = lane < nwarps ? s_v[lane] : T(-1);
+  int wr = lane < nwarps ? s_r[lane] : -1;
+  warp_argmax(wv, wr);
+  v = wv;
+  r = wr;
+}
+
 // ---------------------------------------------------------------------------
 // K1 + K3: panel factorization (lu::Panel, src/lapack_like/factor/LU/Panel.hpp:15-59)
 // ---------------------------------------------------------------------------
@@ -51,12 +71,14 @@ __device__ __forceinline__ void block_argmax(T& v, int& r, T* s_v, int* s_r) {
 //      publishes the slot with a release store of the column's epoch;
 //   2. threads 0..G-1 poll the G slot epochs (acquire): seeing all of them is
 //      the grid barrier, and the candidate headers arrive with it;
-//   3. warp 0 reduces the candidates (ties -> lowest row, idamax's rule);
-//      the winner's row and row j are read from their slots;
-//   4. the CTA swaps the pivot row and row j inside its slab if it owns them,
-//      scales by the reciprocal of the pivot (El scales by alpha11Inv,
-//      Panel.hpp:53-55) and applies the rank-1 update to its rows while
-//      computing its candidate for column j+1.
+//   3. every warp reduces the candidates itself (ties -> lowest row,
+//      idamax's rule); the winner's row and row j are already on chip;
+//   4. the CTA writes the pivot row into row j if it owns row j, updates its
+//      rows (the pivot row's position, if it owns it, starting from old row
+//      j), scaling by the reciprocal of the pivot (El scales by alpha11Inv,
+//      Panel.hpp:53-55) and applying the rank-1 update while computing its
+//      candidate for column j+1.
+// Four barriers per column: publish, exchange, and two in the argmax.
 // Slots are double-buffered by column parity: a CTA can only rewrite a slot
 // after every CTA has published the next column, i.e. finished reading this
 // one.  Epochs grow across the launches of one factorization, so slots never
@@ -90,17 +112,16 @@ __global__ void __launch_bounds__(kPanelThreads)
 getf2_panel_kernel(PanelParams<T> p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* slab = reinterpret_cast<T*>(smem_raw);
-  __shared__ T s_u[W];
   __shared__ T s_d[W];
   __shared__ T s_rv[33];
   __shared__ int s_rr[33];
   __shared__ T s_gv[kPanelThreads];
   __shared__ int s_gr[kPanelThreads];
   T* s_rows = slab + (size_t)p.R * W;  // [G][W] candidate rows (dynamic smem)
-  __shared__ int s_piv, s_abort;
+  __shared__ int s_abort;
 
   const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x;
-  const int lane = tid & 31, warp = tid >> 5;
+  const int lane = tid & 31;
   const int R = p.R, w = p.w, maxG = p.s.maxG;
   const int rb = b * R;
   const int re = min(rb + R, p.mp);
@@ -127,7 +148,8 @@ getf2_panel_kernel(PanelParams<T> p) {
     const int epoch = p.epoch_base + j + 1;
     const int par = epoch & 1;
     PanelSlot<T>* my = p.s.slots + (long)par * maxG + b;
-    // 1. publish
+    // 1. publish (the release store orders the CTA's slot writes, which
+    // the barrier makes visible to the publishing thread)
     if (br >= 0 && tid < w) my->cand[tid] = slab[tid * R + (br - rb)];
     if (j >= rb && j < re && tid < w) my->diag[tid] = slab[tid * R + (j - rb)];
     if (tid == 0) {
@@ -135,10 +157,7 @@ getf2_panel_kernel(PanelParams<T> p) {
       my->row = br;
     }
     __syncthreads();
-    if (tid == 0) {
-      __threadfence();
-      st_release_s32(&my->epoch, epoch);
-    }
+    if (tid == 0) st_release_s32(&my->epoch, epoch);
     // 2. the barrier: every slot carries this epoch.  The thread that polled
     // slot g copies g's candidate row (and, for the owner of row j, row j)
     // right away, so the winner's row is already on chip after the barrier.
@@ -175,8 +194,9 @@ getf2_panel_kernel(PanelParams<T> p) {
     }
     __syncthreads();
     if (s_abort) return;
-    // 3. reduce
-    if (warp == 0) {
+    // 3. reduce (every warp, identical result)
+    int piv;
+    {
       T v = T(-1);
       int r = -1;
       for (int g = lane; g < G; g += 32) {
@@ -186,32 +206,31 @@ getf2_panel_kernel(PanelParams<T> p) {
         }
       }
       warp_argmax(v, r);
-      if (lane == 0) s_piv = (r < 0) ? j : r;
+      piv = (r < 0) ? j : r;
     }
-    __syncthreads();
-    const int piv = s_piv;
-    if (tid < w) s_u[tid] = (piv == j) ? s_d[tid] : s_rows[(piv / R) * W + tid];
-    __syncthreads();
-    // 4. swap, scale, update, next candidate
+    const T* urow = (piv == j) ? s_d : s_rows + (piv / R) * W;  // the pivot row
     if (b == 0 && tid == 0) p.ipiv[j] = p.row_base + piv;
-    if (piv != j && tid < w) {
-      if (j >= rb && j < re) slab[tid * R + (j - rb)] = s_u[tid];
-      if (piv >= rb && piv < re) slab[tid * R + (piv - rb)] = s_d[tid];
-    }
-    __syncthreads();
-
-    const T alpha = s_u[j];
+    const T alpha = urow[j];
     const bool singular = (alpha == T(0));
     if (singular && b == 0 && tid == 0) atomicCAS(&p.st->info, 0, p.info_base + j + 1);
     const T inv = singular ? T(1) : T(1) / alpha;
+    // 4. row j takes the pivot row (row j is not updated below); the pivot
+    // row's position takes old row j, updated from s_d
+    if (piv != j && tid < w && j >= rb && j < re) slab[tid * R + (j - rb)] = urow[tid];
     bv = T(-1);
     br = -1;
     const int r0 = max(j + 1 - rb, 0);
+    const int pl = (piv != j && piv >= rb && piv < re) ? piv - rb : -1;
+    // the pivot row's position: old row j's multipliers of the earlier
+    // columns move with it (columns j.. come from the update below)
+    if (pl >= 0 && tid < j) slab[tid * R + pl] = s_d[tid];
     for (int r = r0 + tid; r < nr; r += blockDim.x) {
-      T l = slab[j * R + r];
+      const bool pr = r == pl;
+      T l = pr ? s_d[j] : slab[j * R + r];
       if (!singular) l *= inv;
       slab[j * R + r] = l;
-      for (int c = j + 1; c < w; ++c) slab[c * R + r] = fma(-l, s_u[c], slab[c * R + r]);
+      for (int c = j + 1; c < w; ++c)
+        slab[c * R + r] = fma(-l, urow[c], pr ? s_d[c] : slab[c * R + r]);
       if (j + 1 < w) {
         const T v = absv(slab[(j + 1) * R + r]);
         if (argmax_better(v, rb + r, bv, br)) {
@@ -220,7 +239,7 @@ getf2_panel_kernel(PanelParams<T> p) {
         }
       }
     }
-    block_argmax(bv, br, s_rv, s_rr);
+    block_argmax_nolead(bv, br, s_rv, s_rr);
   }
   __syncthreads();
   for (int c = 0; c < w; ++c)
