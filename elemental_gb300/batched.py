@@ -86,6 +86,17 @@ class BatchedSolver:
                             for _, b in systems])
         return ns, torch.from_numpy(A).to(device), torch.from_numpy(B).to(device)
 
+    @staticmethod
+    def subset(ns, q, A_packed, B_packed, idx):
+        """The systems `idx` (sorted indices) of a packed batch, repacked:
+        (ns, A, B) for a rank's share (elemental_gb300.shard)."""
+        ns = np.asarray(ns, dtype=np.int64)
+        aoff = np.concatenate([[0], np.cumsum(ns ** 2)])
+        boff = np.concatenate([[0], np.cumsum(ns * q)])
+        A = torch.cat([A_packed[aoff[i]:aoff[i + 1]] for i in idx]) if len(idx) else A_packed[:0]
+        B = torch.cat([B_packed[boff[i]:boff[i + 1]] for i in idx]) if len(idx) else B_packed[:0]
+        return ns[idx].astype(np.int32), A, B
+
     def run(self):
         """Enqueue one replay of the captured launch on the context stream."""
         self.ctx._bind()
