@@ -47,8 +47,9 @@ constexpr int kTcM = 128, kTcN = 128;             // C tile per MMA round
 constexpr int kTcTileA = kTcM * 128;              // one 128-byte K row per M row
 constexpr int kTcTileB = kTcN * 128;
 constexpr int kTcSmem = 2 * kTcTileA + 2 * kTcTileB;  // hi and lo of each: 64 KB
-constexpr int kTcCols = 128;                      // TMEM columns (FP32 accumulator)
+constexpr int kTcCols = 256;                      // TMEM columns (2 FP32 accumulators)
 constexpr int kDynSmem = kSmemPanel + kTcSmem + 1024;
+static_assert(kSmemPanel >= 2 * kTcM * kTcN * 4, "C staging of the tensor-core update");
 
 struct SysDesc {
   int n, kind, nb, prec;  // kind 0 LU, 1 Cholesky; prec 0 FP64, 1 FP32 + IR
@@ -431,10 +432,33 @@ __device__ __forceinline__ void tc_put_chunk(unsigned char* hi, unsigned char* l
   }
 }
 
+__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(tc::smem_u32(dst)), "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// Software-pipelined over the 128 x 128 C tiles t (row blocks outer):
+//   * C(t+1) streams into a shared-memory buffer by cp.async (no registers
+//     held) while tile t's epilogue runs, so ~64 KB of C is always in flight;
+//   * the accumulator is double-buffered in TMEM (2 x 128 columns): the MMAs
+//     of tile t+1 run while the epilogue of tile t reads tile t's columns;
+//   * tile t+1's U12 values are loaded into registers before waiting for
+//     tile t's MMAs and converted into the operand tile after it.
+// cs: 2 x 128 x 128 floats of shared memory (the panel's staging area, free
+// during the trailing update).  A thread copies and updates the same C
+// elements (row 32 (w % 4) + lane, columns 64 (w / 4) + j), so its own
+// cp.async.wait_group is the only wait the C buffer needs.
 __device__ __noinline__ void cta_gemm_update_tc(const float* P, int ldp, const float* Q,
                                                 int ldq, float* C, int ldc, int m, int nc,
                                                 int jb, bool bf16, Shared& sh,
-                                                unsigned char* tiles) {
+                                                unsigned char* tiles, float* cs) {
   unsigned char* sAh = tiles;
   unsigned char* sAl = tiles + kTcTileA;
   unsigned char* sBh = tiles + 2 * kTcTileA;
@@ -444,91 +468,172 @@ __device__ __noinline__ void cta_gemm_update_tc(const float* P, int ldp, const f
   const int kstep = bf16 ? 16 : 8;
   const int nk = (jb + kstep - 1) / kstep;     // MMAs per pass (32 bytes of K each)
   const int nchunk = bf16 ? (jb + 7) / 8 : (jb + 3) / 4;
+  const int per = bf16 ? 8 : 4;                // K values per 16-byte chunk
   const uint32_t idesc = (1u << 4) | ((bf16 ? 1u : 2u) << 7) | ((bf16 ? 1u : 2u) << 10) |
                          ((uint32_t)(kTcN >> 3) << 17) | ((uint32_t)(kTcM >> 4) << 24);
+  const int nct = (nc + kTcN - 1) / kTcN;
+  const int T = ((m + kTcM - 1) / kTcM) * nct;
   uint32_t phase = sh.mma_phase;
   const uint32_t tmem = sh.tmem;
-  for (int r0 = 0; r0 < m && !sh.tc_err; r0 += kTcM) {
-    // A tile: rows r0.. of P
-    __syncthreads();
+  constexpr int kItems = kTcN * 8 / kBT;       // (column, chunk) items per thread
+  static_assert(kItems * kBT == kTcN * 8 && kTcM * 8 == kItems * kBT, "tile items");
+
+  auto load_c = [&](int t) {  // C(t) -> cs[t & 1]; one commit group per call
+    if (t < T) {
+      const int r0 = (t / nct) * kTcM, c0 = (t % nct) * kTcN;
+      const int row = r0 + 32 * wl + lane;
+      const int cb = c0 + 64 * half;
+      if (row < m) {
+        float* dst = cs + (t & 1) * (kTcM * kTcN) + (64 * half) * kTcM + 32 * wl + lane;
+        const float* src = C + row + (long)cb * ldc;
+        const int ncol = min(64, nc - cb);
+#pragma unroll 8
+        for (int j = 0; j < ncol; ++j) cp_async4(dst + j * kTcM, src + (long)j * ldc);
+      }
+    }
+    cp_async_commit();
+  };
+  float qv[kItems][8];
+  auto fetch_b = [&](int t) {  // tile t's U12 values into registers
+    const int c0 = (t % nct) * kTcN;
+#pragma unroll
+    for (int it = 0; it < kItems; ++it) {
+      const int idx = threadIdx.x + it * kBT;
+      const int j = idx >> 3, c = idx & 7;
+      const bool ok = c0 + j < nc && c < nchunk;
+      const float* qc = Q + (long)(c0 + j) * ldq;
+#pragma unroll
+      for (int e = 0; e < 8; ++e) {
+        const int k = per * c + e;
+        qv[it][e] = (ok && e < per && k < jb) ? qc[k] : 0.f;
+      }
+    }
+  };
+  auto put_b = [&]() {  // qv is zero past jb and outside the tile
+#pragma unroll
+    for (int it = 0; it < kItems; ++it) {
+      const int idx = threadIdx.x + it * kBT;
+      const int off = sw128(idx >> 3, idx & 7);
+      if (bf16) {
+        __nv_bfloat162 h[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) h[e] = __floats2bfloat162_rn(qv[it][2 * e], qv[it][2 * e + 1]);
+        *reinterpret_cast<uint4*>(sBh + off) = *reinterpret_cast<uint4*>(h);
+      } else {
+        float4 vh, vl;
+        float* ph = &vh.x;
+        float* pl = &vl.x;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          ph[e] = tf32_rna(qv[it][e]);
+          pl[e] = tf32_rna(qv[it][e] - ph[e]);
+        }
+        *reinterpret_cast<float4*>(sBh + off) = vh;
+        *reinterpret_cast<float4*>(sBl + off) = vl;
+      }
+    }
+  };
+  auto build_a = [&](int t) {  // rows r0.. of P
+    const int r0 = (t / nct) * kTcM;
     for (int idx = threadIdx.x; idx < kTcM * 8; idx += kBT) {
       const int r = idx >> 3, c = idx & 7;
       const bool ok = r0 + r < m && c < nchunk;
       const float* pr = P + r0 + r;
-      tc_put_chunk(sAh, sAl, r, c, ok ? jb : 0, bf16, [&](int k) { return pr[k * ldp]; });
+      tc_put_chunk(sAh, sAl, r, c, ok ? jb : 0, bf16, [&](int k) { return pr[(long)k * ldp]; });
     }
-    for (int c0 = 0; c0 < nc && !sh.tc_err; c0 += kTcN) {
-      // B tile: columns c0.. of Q (each column's jb values are contiguous)
-      for (int idx = threadIdx.x; idx < kTcN * 8; idx += kBT) {
-        const int j = idx >> 3, c = idx & 7;
-        const bool ok = c0 + j < nc && c < nchunk;
-        const float* qc = Q + (long)(c0 + j) * ldq;
-        tc_put_chunk(sBh, sBl, j, c, ok ? jb : 0, bf16, [&](int k) { return qc[k]; });
+  };
+  auto issue = [&](int t) {  // thread 0: tile t's MMAs into TMEM buffer t & 1
+    const uint64_t ah = tc::sdesc_sw128(tc::smem_u32(sAh));
+    const uint64_t al = tc::sdesc_sw128(tc::smem_u32(sAl));
+    const uint64_t bh = tc::sdesc_sw128(tc::smem_u32(sBh));
+    const uint64_t bl = tc::sdesc_sw128(tc::smem_u32(sBl));
+    const uint32_t d = tmem + (uint32_t)((t & 1) * kTcN);
+    const int passes = bf16 ? 1 : 3;
+    uint32_t acc = 0;
+    for (int ps = 0; ps < passes; ++ps) {
+      const uint64_t ad = ps == 2 ? al : ah;
+      const uint64_t bd = ps == 1 ? bl : bh;
+      for (int kk = 0; kk < nk; ++kk) {
+        if (bf16)
+          tc::umma<kTcBF16>(d, ad + 2 * kk, bd + 2 * kk, idesc, acc);
+        else
+          tc::umma<kTcTF32>(d, ad + 2 * kk, bd + 2 * kk, idesc, acc);
+        acc = 1;
       }
-      // the 2 x 32 C values this thread updates, loaded before the MMAs complete
-      const int row = r0 + 32 * wl + lane;
-      const bool row_ok = row < m;
-      const int cb = c0 + 64 * half;
-      float cv[64];
-#pragma unroll
-      for (int j = 0; j < 64; ++j)
-        cv[j] = (row_ok && cb + j < nc) ? C[row + (long)(cb + j) * ldc] : 0.f;
+    }
+    tc::umma_commit(reinterpret_cast<uint64_t*>(&sh.mma_bar));
+  };
+
+  __syncthreads();  // the callers' use of cs and the operand tiles is over
+  if (sh.tc_err || T == 0) {
+    __syncthreads();
+    return;
+  }
+  load_c(0);
+  fetch_b(0);
+  build_a(0);
+  put_b();
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  if (threadIdx.x == 0) issue(0);
+  for (int t = 0; t < T; ++t) {
+    load_c(t + 1);
+    const bool more = t + 1 < T;
+    if (more) fetch_b(t + 1);
+    // tile t's MMAs done: its TMEM buffer is final and the operand tiles free
+    bool ok = tc::mbar_try_wait(reinterpret_cast<uint64_t*>(&sh.mma_bar), phase);
+    if (!__all_sync(0xffffffffu, ok)) {
+      const unsigned long long t0 = globaltimer_ns();
+      while (true) {
+        ok = tc::mbar_try_wait(reinterpret_cast<uint64_t*>(&sh.mma_bar), phase);
+        if (__all_sync(0xffffffffu, ok)) break;
+        if (globaltimer_ns() - t0 > kSpinLimitNs) {
+          if (lane == 0) sh.tc_err = 1;
+          break;
+        }
+      }
+    }
+    phase ^= 1u;
+    tc::tc_fence_after();
+    if (more) {
+      if ((t + 1) % nct == 0) build_a(t + 1);
+      put_b();
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      tc::tc_fence_before();
-      __syncthreads();
-      tc::tc_fence_after();
-      if (threadIdx.x == 0) {
-        const uint64_t ah = tc::sdesc_sw128(tc::smem_u32(sAh));
-        const uint64_t al = tc::sdesc_sw128(tc::smem_u32(sAl));
-        const uint64_t bh = tc::sdesc_sw128(tc::smem_u32(sBh));
-        const uint64_t bl = tc::sdesc_sw128(tc::smem_u32(sBl));
-        const int passes = bf16 ? 1 : 3;
-        uint32_t acc = 0;
-        for (int ps = 0; ps < passes; ++ps) {
-          const uint64_t ad = ps == 2 ? al : ah;
-          const uint64_t bd = ps == 1 ? bl : bh;
-          for (int kk = 0; kk < nk; ++kk) {
-            if (bf16)
-              tc::umma<kTcBF16>(tmem, ad + 2 * kk, bd + 2 * kk, idesc, acc);
-            else
-              tc::umma<kTcTF32>(tmem, ad + 2 * kk, bd + 2 * kk, idesc, acc);
-            acc = 1;
-          }
-        }
-        tc::umma_commit(reinterpret_cast<uint64_t*>(&sh.mma_bar));
-      }
-      __syncwarp();
-      // warp-uniform: tcgen05.ld is a whole-warp instruction
-      bool ok = tc::mbar_try_wait(reinterpret_cast<uint64_t*>(&sh.mma_bar), phase);
-      if (!__all_sync(0xffffffffu, ok)) {
-        const unsigned long long t0 = globaltimer_ns();
-        while (true) {
-          ok = tc::mbar_try_wait(reinterpret_cast<uint64_t*>(&sh.mma_bar), phase);
-          if (__all_sync(0xffffffffu, ok)) break;
-          if (globaltimer_ns() - t0 > kSpinLimitNs) {
-            sh.tc_err = 1;
-            break;
-          }
-        }
-      }
-      phase ^= 1u;
-      tc::tc_fence_after();
-      if (__all_sync(0xffffffffu, ok)) {
+    }
+    cp_async_wait<1>();  // this thread's copies of C(t) have landed
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    const bool err = sh.tc_err != 0;  // uniform: written only before the barrier
+    if (!err) {
+      if (more && threadIdx.x == 0) issue(t + 1);
+      const int r0 = (t / nct) * kTcM, c0 = (t % nct) * kTcN;
+      const int row = r0 + 32 * wl + lane;
+      const int cb = c0 + 64 * half;
+      const float* src = cs + (t & 1) * (kTcM * kTcN) + (64 * half) * kTcM + 32 * wl + lane;
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          uint32_t a[32];
-          tc::tmem_ld32(tmem + ((uint32_t)(32 * wl) << 16) + (uint32_t)(64 * half + 32 * h), a);
+      for (int h = 0; h < 2; ++h) {
+        uint32_t a[32];
+        tc::tmem_ld32(tmem + ((uint32_t)(32 * wl) << 16) +
+                          (uint32_t)((t & 1) * kTcN + 64 * half + 32 * h),
+                      a);
+        if (row < m) {
 #pragma unroll
           for (int j = 0; j < 32; ++j) {
             const int col = cb + 32 * h + j;
-            if (row_ok && col < nc) C[row + (long)col * ldc] = cv[32 * h + j] - __uint_as_float(a[j]);
+            if (col < nc)
+              C[row + (long)col * ldc] = src[(32 * h + j) * kTcM] - __uint_as_float(a[j]);
           }
         }
       }
-      tc::tc_fence_before();
-      __syncthreads();
     }
+    tc::tc_fence_before();
+    __syncthreads();
+    if (err) break;
   }
+  cp_async_wait<0>();
   if (threadIdx.x == 0) sh.mma_phase = phase;
   __syncthreads();
 }
@@ -652,9 +757,11 @@ __device__ __noinline__ int cta_lu(T* W, int n, int ld, int nb, int ib, int* piv
       bool done_tc = false;
       if constexpr (sizeof(T) == 4) {
         if (tc_tiles && n2 >= 32 && nbk <= (lowp ? 64 : 32)) {
-          cta_gemm_update_tc(A21, ldl, W + k + (long)(k + nbk) * ld, ld,
+          // A21 from W (written back with the panel): the panel's shared
+          // memory stages C
+          cta_gemm_update_tc(W + (k + nbk) + (long)k * ld, ld, W + k + (long)(k + nbk) * ld, ld,
                              W + (k + nbk) + (long)(k + nbk) * ld, ld, n2, n2, nbk, lowp, sh,
-                             tc_tiles);
+                             tc_tiles, reinterpret_cast<float*>(smem));
           done_tc = true;
         }
       }
@@ -1025,7 +1132,7 @@ struct BatchParams {
 // ld n), FP64.  Thread t owns rows t + kBT g (g < RG) of each 8-row-group
 // sweep, so every j step has RG independent coalesced loads of A in flight
 // (the product is latency-bound otherwise: one SM, 8 warps).
-template <int RG, int QM>
+template <int RG, int QM, int U>
 __device__ void cta_gemv_rows(const double* __restrict__ A, int n, const double* X, int q,
                               const double* B, double* Y) {
   for (int r0 = 0; r0 < n; r0 += RG * kBT) {
@@ -1040,18 +1147,27 @@ __device__ void cta_gemv_rows(const double* __restrict__ A, int n, const double*
       const int r = r0 + threadIdx.x + g * kBT;
       rr[g] = r < n ? r : n - 1;  // clamped: loads stay in bounds, results unused
     }
-#pragma unroll 2
-    for (int j = 0; j < n; ++j) {
-      double a[RG];
+    // U columns' loads issued together: RG * U independent coalesced loads
+    // in flight per thread (one CTA per SM is latency-bound otherwise)
+    for (int j0 = 0; j0 < n; j0 += U) {
+      double a[U][RG];
 #pragma unroll
-      for (int g = 0; g < RG; ++g) a[g] = A[rr[g] + (long)j * n];
-      double x[QM];
+      for (int u = 0; u < U; ++u) {
+        const long col = (long)min(j0 + u, n - 1) * n;
 #pragma unroll
-      for (int c = 0; c < QM; ++c) x[c] = c < q ? X[j + (long)c * n] : 0.0;
+        for (int g = 0; g < RG; ++g) a[u][g] = A[rr[g] + col];
+      }
 #pragma unroll
-      for (int g = 0; g < RG; ++g)
+      for (int u = 0; u < U; ++u) {
+        if (j0 + u >= n) break;
+        double x[QM];
 #pragma unroll
-        for (int c = 0; c < QM; ++c) acc[g][c] = fma(a[g], x[c], acc[g][c]);
+        for (int c = 0; c < QM; ++c) x[c] = c < q ? X[j0 + u + (long)c * n] : 0.0;
+#pragma unroll
+        for (int g = 0; g < RG; ++g)
+#pragma unroll
+          for (int c = 0; c < QM; ++c) acc[g][c] = fma(a[u][g], x[c], acc[g][c]);
+      }
     }
 #pragma unroll
     for (int g = 0; g < RG; ++g) {
@@ -1066,14 +1182,27 @@ __device__ void cta_gemv_rows(const double* __restrict__ A, int n, const double*
 
 __device__ __noinline__ void cta_gemv(const double* A, int n, const double* X, int q,
                                       const double* B, double* Y) {
-  if (q == 1)
-    cta_gemv_rows<8, 1>(A, n, X, q, B, Y);
-  else if (q == 2)
-    cta_gemv_rows<8, 2>(A, n, X, q, B, Y);
-  else if (q <= 4)
-    cta_gemv_rows<4, 4>(A, n, X, q, B, Y);
-  else
-    cta_gemv_rows<4, kBQ>(A, n, X, q, B, Y);
+  // row groups matched to n (no clamped duplicate rows), the rest of the
+  // loads in flight taken from more columns
+  if (q == 1) {
+    if (n <= kBT) cta_gemv_rows<1, 1, 16>(A, n, X, q, B, Y);
+    else if (n <= 2 * kBT) cta_gemv_rows<2, 1, 8>(A, n, X, q, B, Y);
+    else if (n <= 4 * kBT) cta_gemv_rows<4, 1, 8>(A, n, X, q, B, Y);
+    else cta_gemv_rows<8, 1, 4>(A, n, X, q, B, Y);
+  } else if (q == 2) {
+    if (n <= kBT) cta_gemv_rows<1, 2, 16>(A, n, X, q, B, Y);
+    else if (n <= 2 * kBT) cta_gemv_rows<2, 2, 8>(A, n, X, q, B, Y);
+    else if (n <= 4 * kBT) cta_gemv_rows<4, 2, 4>(A, n, X, q, B, Y);
+    else cta_gemv_rows<8, 2, 4>(A, n, X, q, B, Y);
+  } else if (q <= 4) {
+    if (n <= kBT) cta_gemv_rows<1, 4, 16>(A, n, X, q, B, Y);
+    else if (n <= 2 * kBT) cta_gemv_rows<2, 4, 8>(A, n, X, q, B, Y);
+    else cta_gemv_rows<4, 4, 4>(A, n, X, q, B, Y);
+  } else {
+    if (n <= kBT) cta_gemv_rows<1, kBQ, 8>(A, n, X, q, B, Y);
+    else if (n <= 2 * kBT) cta_gemv_rows<2, kBQ, 4>(A, n, X, q, B, Y);
+    else cta_gemv_rows<4, kBQ, 2>(A, n, X, q, B, Y);
+  }
   __syncthreads();
 }
 
@@ -1104,48 +1233,71 @@ __device__ double sys_berr(const double* A, int n, const double* X, const double
 
 // x := (L U)^{-T} x for one vector: U^T (lower, diag u_jj) forward, then
 // L^T (upper; unit diagonal for LU, l_jj for Cholesky) backward, both read
-// transposed from W.
+// transposed from W.  Each 32 x 32 diagonal block is staged in shared memory
+// (the panel region) before one warp solves it in registers; the other rows
+// take the block's update with the block's 32 loads of their column segment
+// issued together.
 template <typename T>
 __device__ void cta_solve_t(const T* W, int n, int ld, bool unit_lower, T* x) {
+  extern __shared__ __align__(16) unsigned char smem_dyn[];
+  T(*sdg)[33] = reinterpret_cast<T(*)[33]>(smem_dyn);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  auto stage = [&](int j0, int jb) {
+    __syncthreads();  // the previous block's readers are done
+    for (int idx = threadIdx.x; idx < 32 * 32; idx += kBT) {
+      const int r = idx & 31, c = idx >> 5;
+      sdg[r][c] = (r < jb && c < jb) ? W[(j0 + r) + (long)(j0 + c) * ld] : T(0);
+    }
+    __syncthreads();
+  };
+  // x[r] -= sum_jj W[j0 + jj, r] x[j0 + jj] for r in [r_lo, r_hi)
+  auto update = [&](int j0, int jb, int r_lo, int r_hi) {
+    for (int r = r_lo + threadIdx.x; r < r_hi; r += kBT) {
+      const T* wr = W + j0 + (long)r * ld;
+      T acc = x[r];
+      if (jb == 32) {
+        T w[32];
+#pragma unroll
+        for (int jj = 0; jj < 32; ++jj) w[jj] = wr[jj];
+#pragma unroll
+        for (int jj = 0; jj < 32; ++jj) acc = fma(-w[jj], x[j0 + jj], acc);
+      } else {
+        for (int jj = 0; jj < jb; ++jj) acc = fma(-wr[jj], x[j0 + jj], acc);
+      }
+      x[r] = acc;
+    }
+  };
   for (int j0 = 0; j0 < n; j0 += 32) {
     const int jb = min(32, n - j0);
+    stage(j0, jb);
     if (warp == 0) {
       T v = lane < jb ? x[j0 + lane] : T(0);
       for (int jj = 0; jj < jb; ++jj) {
-        if (lane == jj) v = v / W[(j0 + jj) + (long)(j0 + jj) * ld];
+        if (lane == jj) v = v / sdg[jj][jj];
         const T xj = __shfl_sync(0xffffffffu, v, jj);
-        if (lane > jj && lane < jb) v = fma(-W[(j0 + jj) + (long)(j0 + lane) * ld], xj, v);
+        if (lane > jj && lane < jb) v = fma(-sdg[jj][lane], xj, v);
       }
       if (lane < jb) x[j0 + lane] = v;
     }
     __syncthreads();
-    for (int r = j0 + jb + threadIdx.x; r < n; r += kBT) {
-      T acc = x[r];
-      for (int jj = 0; jj < jb; ++jj) acc = fma(-W[(j0 + jj) + (long)r * ld], x[j0 + jj], acc);
-      x[r] = acc;
-    }
-    __syncthreads();
+    update(j0, jb, j0 + jb, n);
   }
   for (int j0 = ((n - 1) / 32) * 32; j0 >= 0; j0 -= 32) {
     const int jb = min(32, n - j0);
+    stage(j0, jb);
     if (warp == 0) {
       T v = lane < jb ? x[j0 + lane] : T(0);
       for (int jj = jb - 1; jj >= 0; --jj) {
-        if (!unit_lower && lane == jj) v = v / W[(j0 + jj) + (long)(j0 + jj) * ld];
+        if (!unit_lower && lane == jj) v = v / sdg[jj][jj];
         const T xj = __shfl_sync(0xffffffffu, v, jj);
-        if (lane < jj) v = fma(-W[(j0 + jj) + (long)(j0 + lane) * ld], xj, v);
+        if (lane < jj) v = fma(-sdg[jj][lane], xj, v);
       }
       if (lane < jb) x[j0 + lane] = v;
     }
     __syncthreads();
-    for (int r = threadIdx.x; r < j0; r += kBT) {
-      T acc = x[r];
-      for (int jj = 0; jj < jb; ++jj) acc = fma(-W[(j0 + jj) + (long)r * ld], x[j0 + jj], acc);
-      x[r] = acc;
-    }
-    __syncthreads();
+    update(j0, jb, 0, j0);
   }
+  __syncthreads();
 }
 
 // Block-wide sum and max of f(i), i < n (double).
@@ -1329,81 +1481,125 @@ __device__ int factor_sys(T* W, int n, int kind, int nb, int ib, int* piv, Share
                    : cta_chol<T>(W, n, n, ib, smem, lowp);
 }
 
+// W = (T) A over nn elements, 8 loads in flight per thread.
+template <typename T>
+__device__ __forceinline__ void cta_copy_cast(const double* A, T* W, long nn) {
+  long i = threadIdx.x;
+  for (; i + 7L * kBT < nn; i += 8L * kBT) {
+    double v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) v[u] = A[i + (long)u * kBT];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) W[i + (long)u * kBT] = (T)v[u];
+  }
+  for (; i < nn; i += kBT) W[i] = (T)A[i];
+}
+
+// One pass over the FP64 matrix (column-major n x n) for the selector's
+// norm features: the sum of squares (||A||_F^2), the largest column sum
+// (||A||_1), max |a_ij|, sum |a_ii|, the row sums of |A| accumulated in
+// shared memory (rowacc, n doubles; ||A||_inf), and the FP32 copy Wf that
+// the feature LU factors.  One warp per column with 16 loads in flight per
+// lane, so A is read once instead of once per quantity.
+struct MatScan {
+  double fro2, col1, amax, rowinf, dsum;
+};
+
+__device__ __noinline__ void cta_scan_matrix(const double* A, int n, float* Wf, double* rowacc,
+                                             Shared& sh, MatScan* out) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int i = threadIdx.x; i < n; i += kBT) rowacc[i] = 0.0;
+  __syncthreads();
+  constexpr int V = 16;
+  double fro = 0.0, cmax = 0.0, am = 0.0, ds = 0.0;
+  for (int j = warp; j < n; j += kBT / 32) {
+    const double* col = A + (long)j * n;
+    float* wcol = Wf + (long)j * n;
+    double c = 0.0, m = 0.0;
+    for (int i0 = 0; i0 < n; i0 += 32 * V) {
+      double v[V];
+#pragma unroll
+      for (int u = 0; u < V; ++u) {
+        const int i = i0 + lane + 32 * u;
+        v[u] = i < n ? col[i] : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < V; ++u) {
+        const int i = i0 + lane + 32 * u;
+        if (i < n) {
+          const double a = fabs(v[u]);
+          c += a;
+          m = fmax(m, a);
+          fro = fma(v[u], v[u], fro);
+          atomicAdd(&rowacc[i], a);
+          wcol[i] = (float)v[u];
+          if (i == j) ds += a;
+        }
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      c += __shfl_xor_sync(0xffffffffu, c, o);
+      m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    }
+    cmax = fmax(cmax, c);
+    am = fmax(am, m);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    fro += __shfl_xor_sync(0xffffffffu, fro, o);
+    ds += __shfl_xor_sync(0xffffffffu, ds, o);
+  }
+  __syncthreads();  // row sums complete
+  double rmax = 0.0;
+  for (int i = threadIdx.x; i < n; i += kBT) rmax = fmax(rmax, rowacc[i]);
+  for (int o = 16; o > 0; o >>= 1) rmax = fmax(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+  if (lane == 0) {
+    sh.red[warp][0] = fro;
+    sh.red[warp][1] = cmax;
+    sh.red[warp][2] = am;
+    sh.red[warp][3] = ds;
+    sh.red[warp][4] = rmax;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    MatScan r{0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int w = 0; w < kBT / 32; ++w) {
+      r.fro2 += sh.red[w][0];
+      r.col1 = fmax(r.col1, sh.red[w][1]);
+      r.amax = fmax(r.amax, sh.red[w][2]);
+      r.dsum += sh.red[w][3];
+      r.rowinf = fmax(r.rowinf, sh.red[w][4]);
+    }
+    sh.colv[0] = r.fro2;
+    sh.colv[1] = r.col1;
+    sh.colv[2] = r.amax;
+    sh.colv[3] = r.dsum;
+    sh.colv[4] = r.rowinf;
+  }
+  __syncthreads();
+  *out = MatScan{sh.colv[0], sh.colv[1], sh.colv[2], sh.colv[4], sh.colv[3]};
+  __syncthreads();
+}
+
 // The selector's 16 features of one system (written to p.feat[s * 16 ..]):
 // norm ratios of A, an FP32 LU's growth and pivot spread, and a Hager /
 // Higham 1-norm estimate of ||A^{-1}||_1 (LAPACK xLACON's iteration plus
 // Higham's alternating vector) computed with that FP32 LU.
 __device__ __noinline__ int compute_features(const BatchParams& p, const SysDesc& d, int s, const double* A,
-                                 int n, double nA, float* Wf, int* piv, int* perm, float* v,
+                                 int n, double* na_out, float* Wf, int* piv, int* perm, float* v,
                                  Shared& sh, float* smf, unsigned char* tc_tiles) {
   __shared__ float s_fv[16];
-  double sum, mx, colmax = 0.0, rowmax = 0.0, amax = 0.0, dsum = 0.0;
-  // column sums (||A||_1) and max |a|: one warp per column (coalesced)
-  {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    double cmax = 0.0, am = 0.0;
-    for (int j = warp; j < n; j += kBT / 32) {
-      double c = 0.0, m = 0.0;
-#pragma unroll 4
-      for (int i = lane; i < n; i += 32) {
-        const double v = fabs(A[i + (long)j * n]);
-        c += v;
-        m = fmax(m, v);
-      }
-      for (int o = 16; o > 0; o >>= 1) {
-        c += __shfl_xor_sync(0xffffffffu, c, o);
-        m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-      }
-      cmax = fmax(cmax, c);
-      am = fmax(am, m);
-    }
-    // every lane of warp w holds (cmax, am) of its columns: reduce over warps
-    if (lane == 0) {
-      sh.red[warp][0] = cmax;
-      sh.red[warp][1] = am;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double a = 0.0, b = 0.0;
-      for (int w = 0; w < kBT / 32; ++w) {
-        a = fmax(a, sh.red[w][0]);
-        b = fmax(b, sh.red[w][1]);
-      }
-      sh.colv[0] = a;
-      sh.colv[1] = b;
-    }
-    __syncthreads();
-    colmax = sh.colv[0];
-    amax = sh.colv[1];
-    __syncthreads();
-  }
-  // row sums (||A||_inf): |A| 1 with the GEMV's row blocking
-  {
-    double rmax = 0.0;
-    for (int r0 = 0; r0 < n; r0 += 8 * kBT) {
-      double acc[8];
-      int rr[8];
-#pragma unroll
-      for (int g = 0; g < 8; ++g) {
-        acc[g] = 0.0;
-        const int r = r0 + threadIdx.x + g * kBT;
-        rr[g] = r < n ? r : n - 1;
-      }
-#pragma unroll 2
-      for (int j = 0; j < n; ++j)
-#pragma unroll
-        for (int g = 0; g < 8; ++g) acc[g] += fabs(A[rr[g] + (long)j * n]);
-#pragma unroll
-      for (int g = 0; g < 8; ++g)
-        if (r0 + threadIdx.x + g * kBT < n) rmax = fmax(rmax, acc[g]);
-    }
-    block_sum_max(kBT, [&](int t) { return t == (int)threadIdx.x ? rmax : 0.0; }, sh, &sum,
-                  &rowmax);
-  }
-  block_sum_max(n, [&](int i) { return fabs(A[i + (long)i * n]); }, sh, &dsum, &mx);
-  // FP32 factorization
-  for (long i = threadIdx.x; i < (long)n * n; i += kBT) Wf[i] = (float)A[i];
-  __syncthreads();
+  double sum;
+  // one pass over A: norms, row sums (in the panel's shared memory), FP32 copy
+  MatScan ms;
+  // (row sums in the vector workspace -- n doubles -- past the panel's size)
+  cta_scan_matrix(A, n, Wf,
+                  (long)n * 8 <= kSmemPanel ? reinterpret_cast<double*>(smf)
+                                            : reinterpret_cast<double*>(v),
+                  sh, &ms);
+  const double colmax = ms.col1, rowmax = ms.rowinf, amax = ms.amax, dsum = ms.dsum;
+  const double nA = sqrt(ms.fro2);
+  if (threadIdx.x == 0) *na_out = nA;
+  // FP32 factorization (Wf holds the FP32 copy)
   const int info = factor_sys<float>(Wf, n, d.kind, d.nb, d.ib, piv, sh, smf, p.tc ? tc_tiles : nullptr,
                                      kSmemPanel / (int)sizeof(float), false);
   double umax = 0.0, dmin = 0.0, dmax = 0.0;
@@ -1571,11 +1767,31 @@ batched_solve_kernel(BatchParams p) {
     auto mark = [&](int i, unsigned long long since) {  // thread 0, after a barrier
       if (threadIdx.x == 0) sh.ph[i] += globaltimer_ns() - since;
     };
-    {  // ||A||_F
-      double acc = 0.0;
-      for (long i = threadIdx.x; i < (long)n * n; i += kBT) acc = fma(A[i], A[i], acc);
-      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-      if ((threadIdx.x & 31) == 0) sh.red[threadIdx.x >> 5][0] = acc;
+    bool done = false;
+    if (p.mode == 1) {
+      compute_features(p, d, s, A, n, &s_na, Wf, piv, perm, reinterpret_cast<float*>(V), sh,
+                       reinterpret_cast<float*>(smem_raw), tc_tiles);
+      __syncthreads();
+      mark(7, t_begin);
+      if (p.phase_ns && threadIdx.x < kPhases)
+        p.phase_ns[(long)s * kPhases + threadIdx.x] = sh.ph[threadIdx.x];
+      continue;
+    }
+    if (p.mode == 0) {  // ||A||_F (the feature pass computes it in mode 2)
+      const long nn = (long)n * n;
+      double acc[4] = {0.0, 0.0, 0.0, 0.0};
+      long i = threadIdx.x;
+      for (; i + 7L * kBT < nn; i += 8L * kBT) {  // 8 loads in flight
+        double v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = A[i + (long)u * kBT];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) acc[u & 3] = fma(v[u], v[u], acc[u & 3]);
+      }
+      for (; i < nn; i += kBT) acc[0] = fma(A[i], A[i], acc[0]);
+      double a = (acc[0] + acc[1]) + (acc[2] + acc[3]);
+      for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+      if ((threadIdx.x & 31) == 0) sh.red[threadIdx.x >> 5][0] = a;
       __syncthreads();
       if (threadIdx.x == 0) {
         double v = 0.0;
@@ -1583,17 +1799,6 @@ batched_solve_kernel(BatchParams p) {
         s_na = sqrt(v);
       }
       __syncthreads();
-    }
-    const double nA = s_na;
-    bool done = false;
-    if (p.mode == 1) {
-      compute_features(p, d, s, A, n, nA, Wf, piv, perm, reinterpret_cast<float*>(V), sh,
-                       reinterpret_cast<float*>(smem_raw), tc_tiles);
-      __syncthreads();
-      mark(7, t_begin);
-      if (p.phase_ns && threadIdx.x < kPhases)
-        p.phase_ns[(long)s * kPhases + threadIdx.x] = sh.ph[threadIdx.x];
-      continue;
     }
     // precision chosen at run time (the selector's output) or at plan time
     int prec = d.prec;
@@ -1603,7 +1808,7 @@ batched_solve_kernel(BatchParams p) {
       // fused selection: features from an FP32 LU (kept), the network's
       // choice, then the solve -- a low-precision choice refines with the
       // FP32 factors just computed (they are at least as good as BF16's)
-      const int finfo = compute_features(p, d, s, A, n, nA, Wf, piv, perm,
+      const int finfo = compute_features(p, d, s, A, n, &s_na, Wf, piv, perm,
                                          reinterpret_cast<float*>(V), sh,
                                          reinterpret_cast<float*>(smem_raw), tc_tiles);
       __syncthreads();
@@ -1612,6 +1817,7 @@ batched_solve_kernel(BatchParams p) {
       res.choice = prec;
       have32 = finfo == 0;
     }
+    const double nA = s_na;
     res.prec = prec;  // becomes the precision the result came from
     // low-precision attempts: BF16 (if chosen), then FP32 when falling back
     for (int pr = prec; pr >= 1 && !done; --pr) {
@@ -1621,7 +1827,7 @@ batched_solve_kernel(BatchParams p) {
       float* smf = reinterpret_cast<float*>(smem_raw);
       int info = 0;
       if (!have32) {
-        for (long i = threadIdx.x; i < (long)n * n; i += kBT) Wf[i] = (float)A[i];
+        cta_copy_cast(A, Wf, (long)n * n);
         __syncthreads();
         info = factor_sys<float>(Wf, n, d.kind, d.nb, d.ib, piv, sh, smf, p.tc ? tc_tiles : nullptr,
                                  kSmemPanel / (int)sizeof(float), pr == 2);
@@ -1705,7 +1911,7 @@ batched_solve_kernel(BatchParams p) {
       unsigned long long keep[4];
       for (int i = 0; i < 4; ++i) keep[i] = sh.ph[i];  // the FP64 LU's phases go to 6
       double* smd = reinterpret_cast<double*>(smem_raw);
-      for (long i = threadIdx.x; i < (long)n * n; i += kBT) Wd[i] = A[i];
+      cta_copy_cast(A, Wd, (long)n * n);
       __syncthreads();
       int nb64 = max(1, min(d.nb, (kSmemPanel / 8 - 64 * 64) / max(n, 1)));
       if (nb64 > 8) nb64 = nb64 / 8 * 8;

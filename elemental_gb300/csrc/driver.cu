@@ -916,6 +916,14 @@ int ElGBSetOption(ElGBContext ctx, int option, int value) {
     case ELGB_OPT_TOURNAMENT:
       ctx->opt_tournament = value ? 1 : 0;
       return 0;
+    case ELGB_OPT_PANEL_CLUSTER:
+      if (value != 1 && value != 2 && value != 4 && value != 8 && value != 16)
+        return elgb::kElArgError;
+      elgb::g_panel_cluster = value;
+      return 0;
+    case ELGB_OPT_PANEL_REGS:
+      elgb::g_panel_regs = value ? 1 : 0;
+      return 0;
     default:
       return elgb::kElArgError;
   }

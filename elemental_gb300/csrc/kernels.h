@@ -40,6 +40,12 @@ cudaError_t launch_calu_panel(float* A, long lda, int mp, int w, int* ipiv, int 
                               int info_base, int* cand, int max_ctas, DevStatus* st,
                               int num_sms, cudaStream_t stream, int* nlaunch);
 
+// Largest thread-block cluster the panel kernel may use (1: the cooperative
+// kernel only); process-wide, ElGBSetOption(ELGB_OPT_PANEL_CLUSTER).
+extern int g_panel_cluster;
+// FP32 panels with the rows in registers (1, default) or in shared memory.
+extern int g_panel_regs;
+
 // getf2 on a w-wide panel (w <= 32): El's lu::Panel
 // (src/lapack_like/factor/LU/Panel.hpp:15-59) as one cooperative launch.
 // `A` points at the panel's top-left element, `mp` rows, `w` columns.

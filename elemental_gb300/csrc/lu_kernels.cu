@@ -11,6 +11,12 @@
 
 namespace elgb {
 
+// Largest thread-block cluster the panel may use (1: the cooperative kernel
+// only); set by ElGBSetOption(ELGB_OPT_PANEL_CLUSTER).
+int g_panel_cluster = 16;
+// FP32 panels with the rows in registers (ElGBSetOption(ELGB_OPT_PANEL_REGS)).
+int g_panel_regs = 0;
+
 template <typename T>
 __device__ __forceinline__ T absv(T x) { return x < T(0) ? -x : x; }
 
@@ -106,6 +112,30 @@ __device__ __forceinline__ int ld_acquire_s32(const int* p) {
   asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
+__device__ __forceinline__ int ld_relaxed_s32(const int* p) {
+  int v;
+  asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+// Spin (relaxed loads, bounded) until *flag == epoch, then one acquire
+// fence orders the caller's later loads after the flag.  Returns false on a
+// timeout or another CTA's error (recorded in st).
+__device__ __forceinline__ bool wait_epoch(const int* flag, int epoch, DevStatus* st, int where) {
+  bool ok = true;
+  if (ld_relaxed_s32(flag) != epoch) {
+    const unsigned long long t0 = globaltimer_ns();
+    while (ld_relaxed_s32(flag) != epoch) {
+      if (*(volatile int*)&st->err != 0 || globaltimer_ns() - t0 > kSpinLimitNs) {
+        atomicCAS(&st->err, 0, (int)kErrBarrierTimeout);
+        st->err_where = where;
+        ok = false;
+        break;
+      }
+    }
+  }
+  asm volatile("fence.acq_rel.gpu;" ::: "memory");
+  return ok;
+}
 
 template <typename T, int W>
 __global__ void __launch_bounds__(kPanelThreads)
@@ -163,17 +193,7 @@ getf2_panel_kernel(PanelParams<T> p) {
     // right away, so the winner's row is already on chip after the barrier.
     if (tid < G) {
       const PanelSlot<T>* sl = p.s.slots + (long)par * maxG + tid;
-      if (ld_acquire_s32(&sl->epoch) != epoch) {
-        const unsigned long long t0 = globaltimer_ns();
-        while (ld_acquire_s32(&sl->epoch) != epoch) {
-          if (*(volatile int*)&p.st->err != 0 || globaltimer_ns() - t0 > kSpinLimitNs) {
-            atomicCAS(&p.st->err, 0, (int)kErrBarrierTimeout);
-            p.st->err_where = 1;
-            s_abort = 1;
-            break;
-          }
-        }
-      }
+      if (!wait_epoch(&sl->epoch, epoch, p.st, 1)) s_abort = 1;
       // all loads of the slot issued together (one round trip)
       const int gr = __ldcg(&sl->row);
       const T gv = __ldcg(&sl->val);
@@ -247,12 +267,420 @@ getf2_panel_kernel(PanelParams<T> p) {
       p.A[(long)(rb + r) + (long)c * p.lda] = slab[c * R + r];
 }
 
+// ---------------------------------------------------------------------------
+// FP32 panel with the rows in registers.  512 threads per CTA, thread t owns
+// panel rows rb + t and rb + t + 512 with all w values in registers, so the
+// rank-1 update of a column is register FMAs (no shared-memory traffic) and
+// the per-column time is the exchange.  The exchange, slots, epochs, pivot
+// choice and arithmetic order are those of getf2_panel_kernel: same pivots,
+// same results.
+constexpr int kRegThreads = 512, kRegRows = 2;
+
+template <int W>
+__global__ void __launch_bounds__(kRegThreads, 1)
+getf2_panel_reg_kernel(PanelParams<float> p) {
+  __shared__ float s_d[W];
+  __shared__ float s_rv[33];
+  __shared__ int s_rr[33];
+  __shared__ float s_gv[kRegThreads];
+  __shared__ int s_gr[kRegThreads];
+  __shared__ float s_rows[kRegThreads / 2][W];  // candidate rows of up to 256 CTAs
+  __shared__ int s_abort;
+
+  const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x;
+  const int lane = tid & 31;
+  const int R = p.R, w = p.w, maxG = p.s.maxG;
+  const int rb = b * R;
+  const int re = min(rb + R, p.mp);
+  const int nr = max(re - rb, 0);
+
+  float a[kRegRows][W];
+  int lr[kRegRows];  // local rows (or -1)
+#pragma unroll
+  for (int i = 0; i < kRegRows; ++i) {
+    const int r = tid + i * kRegThreads;
+    lr[i] = r < nr ? r : -1;
+#pragma unroll
+    for (int c = 0; c < W; ++c)
+      a[i][c] = (lr[i] >= 0 && c < w) ? p.A[(long)(rb + r) + (long)c * p.lda] : 0.f;
+  }
+  if (tid == 0) s_abort = 0;
+
+  auto col = [&](int i, int j) {  // a[i][j] for a run-time j
+    float v = 0.f;
+#pragma unroll
+    for (int c = 0; c < W; ++c)
+      if (c == j) v = a[i][c];
+    return v;
+  };
+
+  float bv = -1.f;
+  int br = -1;
+#pragma unroll
+  for (int i = 0; i < kRegRows; ++i)
+    if (lr[i] >= 0) {
+      const float v = fabsf(a[i][0]);
+      if (argmax_better(v, rb + lr[i], bv, br)) {
+        bv = v;
+        br = rb + lr[i];
+      }
+    }
+  block_argmax(bv, br, s_rv, s_rr);
+
+  for (int j = 0; j < w; ++j) {
+    const int epoch = p.epoch_base + j + 1;
+    const int par = epoch & 1;
+    PanelSlot<float>* my = p.s.slots + (long)par * maxG + b;
+    // 1. publish: the owners of the candidate row and of row j write them
+#pragma unroll
+    for (int i = 0; i < kRegRows; ++i) {
+      if (lr[i] >= 0 && rb + lr[i] == br)
+#pragma unroll
+        for (int c = 0; c < W; ++c)
+          if (c < w) my->cand[c] = a[i][c];
+      if (lr[i] >= 0 && rb + lr[i] == j)
+#pragma unroll
+        for (int c = 0; c < W; ++c)
+          if (c < w) my->diag[c] = a[i][c];
+    }
+    if (tid == 0) {
+      my->val = bv;
+      my->row = br;
+    }
+    __syncthreads();
+    if (tid == 0) st_release_s32(&my->epoch, epoch);
+    // 2. the barrier and the candidates (as getf2_panel_kernel)
+    if (tid < G) {
+      const PanelSlot<float>* sl = p.s.slots + (long)par * maxG + tid;
+      if (!wait_epoch(&sl->epoch, epoch, p.st, 3)) s_abort = 1;
+      const int gr = __ldcg(&sl->row);
+      const float gv = __ldcg(&sl->val);
+      const bool own = tid == j / R;
+      float cr[W], dr[W];
+#pragma unroll
+      for (int c = 0; c < W; ++c) {
+        cr[c] = c < w ? __ldcg(&sl->cand[c]) : 0.f;
+        dr[c] = (own && c < w) ? __ldcg(&sl->diag[c]) : 0.f;
+      }
+      s_gv[tid] = gv;
+      s_gr[tid] = gr;
+#pragma unroll
+      for (int c = 0; c < W; ++c) s_rows[tid][c] = cr[c];
+      if (own)
+#pragma unroll
+        for (int c = 0; c < W; ++c) s_d[c] = dr[c];
+    }
+    __syncthreads();
+    if (s_abort) break;  // uniform: read after the barrier
+    // 3. reduce (every warp)
+    int piv;
+    {
+      float v = -1.f;
+      int r = -1;
+      for (int g = lane; g < G; g += 32)
+        if (argmax_better(s_gv[g], s_gr[g], v, r)) {
+          v = s_gv[g];
+          r = s_gr[g];
+        }
+      warp_argmax(v, r);
+      piv = (r < 0) ? j : r;
+    }
+    const float* urow = (piv == j) ? s_d : s_rows[piv / R];
+    if (b == 0 && tid == 0) p.ipiv[j] = p.row_base + piv;
+    const float alpha = urow[j];
+    const bool singular = (alpha == 0.f);
+    if (singular && b == 0 && tid == 0) atomicCAS(&p.st->info, 0, p.info_base + j + 1);
+    const float inv = singular ? 1.f : 1.f / alpha;
+    // 4. interchange: row j takes the pivot row, the pivot row's position
+    // takes old row j; then the update of the rows after j
+    bv = -1.f;
+    br = -1;
+#pragma unroll
+    for (int i = 0; i < kRegRows; ++i) {
+      if (lr[i] < 0) continue;
+      const int row = rb + lr[i];
+      if (piv != j && row == j) {
+#pragma unroll
+        for (int c = 0; c < W; ++c) a[i][c] = urow[c];
+        continue;  // row j is not updated
+      }
+      if (piv != j && row == piv)
+#pragma unroll
+        for (int c = 0; c < W; ++c) a[i][c] = s_d[c];
+      if (row <= j) continue;
+      float l = col(i, j);
+      if (!singular) l *= inv;
+#pragma unroll
+      for (int c = 0; c < W; ++c) {
+        if (c == j) a[i][c] = l;
+        if (c > j && c < w) a[i][c] = fmaf(-l, urow[c], a[i][c]);
+      }
+      if (j + 1 < w) {
+        const float v = fabsf(col(i, j + 1));
+        if (argmax_better(v, row, bv, br)) {
+          bv = v;
+          br = row;
+        }
+      }
+    }
+    block_argmax_nolead(bv, br, s_rv, s_rr);
+  }
+#pragma unroll
+  for (int i = 0; i < kRegRows; ++i)
+    if (lr[i] >= 0)
+#pragma unroll
+      for (int c = 0; c < W; ++c)
+        if (c < w) p.A[(long)(rb + lr[i]) + (long)c * p.lda] = a[i][c];
+}
+
+// ---------------------------------------------------------------------------
+// The same panel on one thread-block cluster: the per-column exchange goes
+// through distributed shared memory and the cluster's hardware barrier
+// instead of global-memory slots and polling.  CTA b of the cluster keeps
+// rows [b R, b R + R) in its shared memory as above; per column j it writes
+// its candidate (|a|, row, the row's w values, and row j if it owns it) to
+// its own shared slot, all threads arrive at the cluster barrier (release /
+// acquire), and thread g < C reads CTA g's slot with ld.shared::cluster.
+// Slots are double-buffered by column parity: a CTA rewrites a slot only
+// after the next column's barrier, which every CTA reaches after its reads.
+// Same arithmetic, in the same order, as getf2_panel_kernel.
+template <typename T>
+struct ClusterSlot {
+  T val;
+  int row;
+  T cand[kPanelW];
+  T diag[kPanelW];
+};
+
+__device__ __forceinline__ void cluster_barrier() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n"
+               "barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ uint32_t cluster_map(const void* local, unsigned rank) {
+  uint32_t a = static_cast<uint32_t>(__cvta_generic_to_shared(local)), r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+  return r;
+}
+
+__device__ __forceinline__ float ld_cluster(uint32_t addr, float*) {
+  float v;
+  asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(addr) : "memory");
+  return v;
+}
+__device__ __forceinline__ double ld_cluster(uint32_t addr, double*) {
+  double v;
+  asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(addr) : "memory");
+  return v;
+}
+__device__ __forceinline__ int ld_cluster_s32(uint32_t addr) {
+  int v;
+  asm volatile("ld.shared::cluster.s32 %0, [%1];" : "=r"(v) : "r"(addr) : "memory");
+  return v;
+}
+
+template <typename T, int W>
+__global__ void __launch_bounds__(kPanelThreads)
+getf2_panel_cluster_kernel(PanelParams<T> p) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* slab = reinterpret_cast<T*>(smem_raw);
+  __shared__ ClusterSlot<T> slots[2];
+  __shared__ T s_d[W];
+  __shared__ T s_rv[33];
+  __shared__ int s_rr[33];
+  __shared__ T s_gv[32];
+  __shared__ int s_gr[32];
+  T* s_rows = slab + (size_t)p.R * W;  // [C][W] candidate rows
+
+  const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x;
+  const int lane = tid & 31;
+  const int R = p.R, w = p.w;
+  const int rb = b * R;
+  const int re = min(rb + R, p.mp);
+  const int nr = max(re - rb, 0);
+
+  for (int c = 0; c < w; ++c)
+    for (int r = tid; r < nr; r += blockDim.x)
+      slab[c * R + r] = p.A[(long)(rb + r) + (long)c * p.lda];
+  __syncthreads();
+
+  T bv = T(-1);
+  int br = -1;
+  for (int r = tid; r < nr; r += blockDim.x) {
+    const T v = absv(slab[r]);
+    if (argmax_better(v, rb + r, bv, br)) {
+      bv = v;
+      br = rb + r;
+    }
+  }
+  block_argmax(bv, br, s_rv, s_rr);
+  cluster_barrier();  // every CTA of the cluster is running
+
+  for (int j = 0; j < w; ++j) {
+    ClusterSlot<T>* my = &slots[j & 1];
+    // 1. publish in this CTA's shared memory
+    if (br >= 0 && tid < w) my->cand[tid] = slab[tid * R + (br - rb)];
+    if (j >= rb && j < re && tid < w) my->diag[tid] = slab[tid * R + (j - rb)];
+    if (tid == 0) {
+      my->val = bv;
+      my->row = br;
+    }
+    cluster_barrier();
+    // 2. thread g < C reads CTA g's slot
+    if (tid < G) {
+      const uint32_t base = cluster_map(my, (unsigned)tid);
+      const uint32_t o_val = (uint32_t)offsetof(ClusterSlot<T>, val);
+      const uint32_t o_row = (uint32_t)offsetof(ClusterSlot<T>, row);
+      const uint32_t o_cand = (uint32_t)offsetof(ClusterSlot<T>, cand);
+      const uint32_t o_diag = (uint32_t)offsetof(ClusterSlot<T>, diag);
+      const bool own = tid == j / R;
+      T cr[W], dr[W];
+      const T gv = ld_cluster(base + o_val, (T*)nullptr);
+      const int gr = ld_cluster_s32(base + o_row);
+#pragma unroll
+      for (int c = 0; c < W; ++c) {
+        cr[c] = c < w ? ld_cluster(base + o_cand + c * (uint32_t)sizeof(T), (T*)nullptr) : T(0);
+        dr[c] = (own && c < w) ? ld_cluster(base + o_diag + c * (uint32_t)sizeof(T), (T*)nullptr)
+                               : T(0);
+      }
+      s_gv[tid] = gv;
+      s_gr[tid] = gr;
+#pragma unroll
+      for (int c = 0; c < W; ++c) s_rows[tid * W + c] = cr[c];
+      if (own)
+#pragma unroll
+        for (int c = 0; c < W; ++c) s_d[c] = dr[c];
+    }
+    __syncthreads();
+    // 3. reduce (every warp, identical result)
+    int piv;
+    {
+      T v = T(-1);
+      int r = -1;
+      if (lane < G && argmax_better(s_gv[lane], s_gr[lane], v, r)) {
+        v = s_gv[lane];
+        r = s_gr[lane];
+      }
+      warp_argmax(v, r);
+      piv = (r < 0) ? j : r;
+    }
+    const T* urow = (piv == j) ? s_d : s_rows + (piv / R) * W;
+    if (b == 0 && tid == 0) p.ipiv[j] = p.row_base + piv;
+    const T alpha = urow[j];
+    const bool singular = (alpha == T(0));
+    if (singular && b == 0 && tid == 0) atomicCAS(&p.st->info, 0, p.info_base + j + 1);
+    const T inv = singular ? T(1) : T(1) / alpha;
+    // 4. swap, update, next candidate (as getf2_panel_kernel)
+    if (piv != j && tid < w && j >= rb && j < re) slab[tid * R + (j - rb)] = urow[tid];
+    bv = T(-1);
+    br = -1;
+    const int r0 = max(j + 1 - rb, 0);
+    const int pl = (piv != j && piv >= rb && piv < re) ? piv - rb : -1;
+    if (pl >= 0 && tid < j) slab[tid * R + pl] = s_d[tid];
+    for (int r = r0 + tid; r < nr; r += blockDim.x) {
+      const bool pr = r == pl;
+      T l = pr ? s_d[j] : slab[j * R + r];
+      if (!singular) l *= inv;
+      slab[j * R + r] = l;
+      for (int c = j + 1; c < w; ++c)
+        slab[c * R + r] = fma(-l, urow[c], pr ? s_d[c] : slab[c * R + r]);
+      if (j + 1 < w) {
+        const T v = absv(slab[(j + 1) * R + r]);
+        if (argmax_better(v, rb + r, bv, br)) {
+          bv = v;
+          br = rb + r;
+        }
+      }
+    }
+    block_argmax_nolead(bv, br, s_rv, s_rr);
+  }
+  __syncthreads();
+  for (int c = 0; c < w; ++c)
+    for (int r = tid; r < nr; r += blockDim.x)
+      p.A[(long)(rb + r) + (long)c * p.lda] = slab[c * R + r];
+  cluster_barrier();  // no CTA leaves while another may still read its slots
+}
+
+// Cluster size for a panel of mp rows: the power of two giving ~1024 rows
+// per CTA (at least 2 CTAs, at most max_cluster), or 0 when one cluster
+// cannot hold the panel in shared memory or the panel is too small for one
+// (the caller then uses the cooperative kernel).
+template <typename T>
+static int cluster_ctas(int mp, int max_cluster) {
+  constexpr int kMaxSmem = 200 * 1024;
+  const int rows_cap = (int)(kMaxSmem / (kPanelW * sizeof(T))) - 32;
+  if (mp < 128) return 0;
+  int C = 2;
+  while (C < max_cluster && (mp + C - 1) / C > 1024) C *= 2;
+  if (C > max_cluster || (mp + C - 1) / C > rows_cap) return 0;
+  return C;
+}
+
+template <typename T>
+static cudaError_t launch_getf2_panel_cluster(T* A, long lda, int mp, int w, int* ipiv,
+                                              int row_base, int info_base, DevStatus* st,
+                                              int C, cudaStream_t stream) {
+  const int R = ceil_div(mp, C);
+  const size_t smem = ((size_t)R + C) * kPanelW * sizeof(T);
+  auto kern = getf2_panel_cluster_kernel<T, kPanelW>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e == cudaSuccess && C > 8)
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(C);
+  cfg.blockDim = dim3(kPanelThreads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = C;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int nclusters = 0;
+  e = cudaOccupancyMaxActiveClusters(&nclusters, (void*)kern, &cfg);
+  if (e != cudaSuccess || nclusters < 1) {
+    cudaGetLastError();
+    return cudaErrorNotSupported;
+  }
+  PanelParams<T> prm{A, lda, mp, w, R, ipiv, row_base, info_base, 0, PanelScratch<T>{}, st};
+  return cudaLaunchKernelEx(&cfg, kern, prm);
+}
+
 template <typename T>
 cudaError_t launch_getf2_panel(T* A, long lda, int mp, int w, int* ipiv, int row_base,
                                int info_base, int epoch_base, const PanelScratch<T>& s,
                                DevStatus* st, int num_sms, cudaStream_t stream) {
   if (w <= 0 || mp <= 0) return cudaSuccess;
   if (w > kPanelW || mp < w) return cudaErrorInvalidValue;
+  if constexpr (sizeof(T) == 4) {
+    if (g_panel_regs) {
+      // ~1024 rows per CTA (512 threads x 2 rows in registers)
+      const int Rr = kRegThreads * kRegRows;
+      int G = ceil_div(mp, Rr);
+      if (G <= std::min({num_sms, s.maxG, kRegThreads / 2})) {
+        PanelParams<float> prm{reinterpret_cast<float*>(A), lda, mp, w, Rr, ipiv, row_base,
+                               info_base, epoch_base,
+                               PanelScratch<float>{reinterpret_cast<PanelSlot<float>*>(s.slots),
+                                                   s.maxG, s.cand},
+                               st};
+        void* args[] = {&prm};
+        return cudaLaunchCooperativeKernel((const void*)getf2_panel_reg_kernel<kPanelW>, dim3(G),
+                                           dim3(kRegThreads), args, 0, stream);
+      }
+    }
+  }
+  if (g_panel_cluster > 1) {
+    const int C = cluster_ctas<T>(mp, g_panel_cluster);
+    if (C > 0) {
+      const cudaError_t e =
+          launch_getf2_panel_cluster<T>(A, lda, mp, w, ipiv, row_base, info_base, st, C, stream);
+      if (e != cudaErrorNotSupported) return e;
+    }
+  }
   constexpr int kMaxSmem = 200 * 1024;
   // About 1024 rows per CTA: fewer CTAs make the per-column exchange cheap
   // (every CTA copies every candidate row), more only where shared memory

@@ -111,7 +111,8 @@ class Context:
     def set_option(self, option, value):
         """ElGBSetOption: "lookahead" (0/1), "panel_ctas" (0 = auto) or
         "tournament" (0/1: tournament pivoting in lu_mixed's leaf panels)."""
-        code = {"lookahead": 1, "panel_ctas": 2, "tournament": 3}[option]
+        code = {"lookahead": 1, "panel_ctas": 2, "tournament": 3, "panel_cluster": 4,
+                "panel_regs": 5}[option]
         self._rc(self.lib.ElGBSetOption(self.h, code, int(value)), "SetOption")
 
     def launches(self):

@@ -51,8 +51,23 @@ int ElGBSetBlocksize(int nb);
  *   ELGB_OPT_PANEL_CTAS CTAs of a panel launch, 0 (default) = automatic
  *   ELGB_OPT_TOURNAMENT 1: ElGBLUPartialPivMixed_s picks its leaf panels'
  *                       pivots by tournament (CALU); 0 (default): partial
- *                       pivoting, El::LU's pivot sequence */
-enum { ELGB_OPT_LOOKAHEAD = 1, ELGB_OPT_PANEL_CTAS = 2, ELGB_OPT_TOURNAMENT = 3 };
+ *                       pivoting, El::LU's pivot sequence
+ *   ELGB_OPT_PANEL_CLUSTER largest thread-block cluster (1, 2, 4, 8 or 16;
+ *                       default 16) for panels that fit one cluster's
+ *                       shared memory: the per-column exchange then runs
+ *                       through distributed shared memory and the cluster
+ *                       barrier; 1: always the cooperative kernel.
+ *                       Process-wide (every context).
+ *   ELGB_OPT_PANEL_REGS 1 (default): FP32 panels keep their rows in
+ *                       registers (512 threads x 2 rows per CTA); 0: in
+ *                       shared memory.  Process-wide. */
+enum {
+  ELGB_OPT_LOOKAHEAD = 1,
+  ELGB_OPT_PANEL_CTAS = 2,
+  ELGB_OPT_TOURNAMENT = 3,
+  ELGB_OPT_PANEL_CLUSTER = 4,
+  ELGB_OPT_PANEL_REGS = 5
+};
 int ElGBSetOption(ElGBContext ctx, int option, int value);
 
 /* Number of kernel launches this context has issued so far. */

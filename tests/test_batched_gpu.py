@@ -165,6 +165,31 @@ def test_batched_features(ctx):
         assert abs(F[i, 1] - np.log10(r["backward_error"])) < 1e-3
 
 
+def test_batched_norm_features_match_numpy(ctx):
+    """The one-pass scan of A behind the norm features (||A||_1, ||A||_inf,
+    max |a|, sum |a_ii| over ||A||_F, and ||A||_F itself) against numpy on
+    uneven sizes from 1 to 2400 (ragged final row chunks of a column)."""
+    q = 1
+    rng = np.random.default_rng(11)
+    sizes = [1, 17, 100, 257, 640, 2400]
+    systems = [(rng.standard_normal((n, n)) * rng.uniform(0.1, 10.0),
+                mats.gaussian(n, q, 700 + i)) for i, n in enumerate(sizes)]
+    ns, A, B = BatchedSolver.pack(systems, q)
+    bs = BatchedSolver(ns, q, A, B, features_only=True, ctx=ctx)
+    bs.run()
+    F = bs.features.cpu().numpy().astype(np.float64)
+    for i, (Ai, _) in enumerate(systems):
+        fro = np.linalg.norm(Ai)
+        amax = np.abs(Ai).max()
+        exp = {2: np.log10(np.abs(Ai).sum(0).max() / fro),
+               3: np.log10(np.abs(Ai).sum(1).max() / fro),
+               4: np.log10(amax / fro),
+               7: np.log10(max(np.abs(np.diag(Ai)).sum() / (len(Ai) * amax), 1e-30)),
+               9: np.log10(fro)}
+        for k, v in exp.items():
+            assert abs(F[i, k] - v) < 2e-6 * max(1.0, abs(v)), (sizes[i], k, F[i, k], v)
+
+
 @pytest.mark.parametrize("prec", ["fp32", "bf16"])
 def test_batched_two_level_blocking(ctx, prec):
     """n ~ 1300 with a 32-column block but a shared-memory panel of at most 24
