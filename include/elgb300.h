@@ -178,6 +178,29 @@ int ElGBRefinedSolve_d(ElGBContext ctx, int n, const double* A, int lda,
                        int nrhs, const double* B, int ldb, double* X, int ldx,
                        const ElGBRefineCtrl* ctrl, ElGBRefineInfo* info);
 
+/* The learned precision selector (added form): a 16 -> 64 -> 64 -> 3 FP32
+ * MLP (ReLU, softmax) over the batched solver's 16 per-system features,
+ * classes 0 FP64, 1 FP32, 2 BF16 factors.  Parameters are one flat FP32
+ * device vector of ElGBMLPParamCount() floats:
+ *   W1[16][64] b1[64] W2[64][64] b2[64] W3[64][3] b3[3]   (row-major, in x out)
+ * No reference counterpart (Elemental has no learned component). */
+int ElGBMLPParamCount(void);
+/* Inference for B samples X (B x 16, row-major, device): probs (B x 3) and /
+ * or argmax (B ints) on the device; either may be NULL. */
+int ElGBMLPForward(ElGBContext ctx, const float* params, const float* X, int B,
+                   float* probs, int* argmax);
+/* Mean softmax cross-entropy gradient over B labelled samples (labels in
+ * {0, 1, 2}) into grad (ElGBMLPParamCount() floats, device); *loss (host,
+ * optional) receives the mean loss and then the call synchronizes. */
+int ElGBMLPGradient(ElGBContext ctx, const float* params, const float* X,
+                    const int* labels, int B, float* grad, float* loss);
+/* One Adam step (step >= 1, bias-corrected; weight_decay * params is added
+ * to the gradient) on params with first / second moments m, v (device,
+ * ElGBMLPParamCount() floats each). */
+int ElGBMLPAdamStep(ElGBContext ctx, float* params, const float* grad, float* m,
+                    float* v, float lr, float beta1, float beta2, float eps,
+                    float weight_decay, int step);
+
 /* Batched uneven-size solves (added form): `count` independent systems
  * A_i X_i = B_i, packed column-major on the device (A_i n_i x n_i, then the
  * next; B_i and X_i n_i x nrhs, nrhs <= 8), solved by ONE persistent launch
