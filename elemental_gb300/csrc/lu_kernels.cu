@@ -137,6 +137,66 @@ __device__ __forceinline__ bool wait_epoch(const int* flag, int epoch, DevStatus
   return ok;
 }
 
+// Copies the CTA's rows [rb, rb + nr) of the panel's w columns into the
+// shared slab (column c at slab + c R) by cp.async: every element's copy is
+// in flight at once instead of a load round trip per few elements.  The
+// caller's barrier publishes the slab to the other threads.
+template <typename T>
+__device__ __forceinline__ void panel_load_slab(T* slab, const T* A, long lda, int rb, int nr,
+                                                int R, int w) {
+  for (int c = 0; c < w; ++c)
+    for (int r = threadIdx.x; r < nr; r += blockDim.x)
+      asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(
+                       (unsigned)__cvta_generic_to_shared(slab + c * R + r)),
+                   "l"(A + (long)(rb + r) + (long)c * lda), "n"((int)sizeof(T))
+                   : "memory");
+  asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
+// Column j of lu::Panel for this CTA's rows r0.. of the slab (column-major,
+// ld R): the multipliers l = a_rj / alpha and the rank-1 update of columns
+// j+1 .. w-1 with the pivot row urow; row pl (the pivot's old position)
+// takes old row j's values from s_d.  Returns this CTA's candidate for
+// column j+1 in (bv, br).  Columns go in groups of four (four loads in
+// flight per row).  (Holding urow in registers with a fully unrolled
+// 32-column body measured slower: it issues all 32 columns' predicated
+// instructions for every j.)
+template <typename T, int W>
+__device__ __forceinline__ void panel_update_rows(T* slab, int R, int nr, int r0, int j, int w,
+                                                  int pl, const T* s_d, const T* urow,
+                                                  bool singular, T inv, int rb, T& bv,
+                                                  int& br) {
+  for (int r = r0 + threadIdx.x; r < nr; r += blockDim.x) {
+    const bool pr = r == pl;
+    T l = pr ? s_d[j] : slab[j * R + r];
+    if (!singular) l *= inv;
+    slab[j * R + r] = l;
+    const T* src = pr ? s_d : slab + r;  // old row j's values for row pl
+    const int sst = pr ? 1 : R;
+    int c = j + 1;
+    for (; c + 3 < w; c += 4) {  // four loads in flight, then four fmas / stores
+      T v0 = src[c * sst], v1 = src[(c + 1) * sst], v2 = src[(c + 2) * sst],
+        v3 = src[(c + 3) * sst];
+      v0 = fma(-l, urow[c], v0);
+      v1 = fma(-l, urow[c + 1], v1);
+      v2 = fma(-l, urow[c + 2], v2);
+      v3 = fma(-l, urow[c + 3], v3);
+      slab[c * R + r] = v0;
+      slab[(c + 1) * R + r] = v1;
+      slab[(c + 2) * R + r] = v2;
+      slab[(c + 3) * R + r] = v3;
+    }
+    for (; c < w; ++c) slab[c * R + r] = fma(-l, urow[c], src[c * sst]);
+    if (j + 1 < w) {
+      const T v = absv(slab[(j + 1) * R + r]);
+      if (argmax_better(v, rb + r, bv, br)) {
+        bv = v;
+        br = rb + r;
+      }
+    }
+  }
+}
+
 template <typename T, int W>
 __global__ void __launch_bounds__(kPanelThreads)
 getf2_panel_kernel(PanelParams<T> p) {
@@ -157,9 +217,7 @@ getf2_panel_kernel(PanelParams<T> p) {
   const int re = min(rb + R, p.mp);
   const int nr = max(re - rb, 0);
 
-  for (int c = 0; c < w; ++c)
-    for (int r = tid; r < nr; r += blockDim.x)
-      slab[c * R + r] = p.A[(long)(rb + r) + (long)c * p.lda];
+  panel_load_slab(slab, p.A, p.lda, rb, nr, R, w);
   if (tid == 0) s_abort = 0;
   __syncthreads();
 
@@ -244,21 +302,7 @@ getf2_panel_kernel(PanelParams<T> p) {
     // the pivot row's position: old row j's multipliers of the earlier
     // columns move with it (columns j.. come from the update below)
     if (pl >= 0 && tid < j) slab[tid * R + pl] = s_d[tid];
-    for (int r = r0 + tid; r < nr; r += blockDim.x) {
-      const bool pr = r == pl;
-      T l = pr ? s_d[j] : slab[j * R + r];
-      if (!singular) l *= inv;
-      slab[j * R + r] = l;
-      for (int c = j + 1; c < w; ++c)
-        slab[c * R + r] = fma(-l, urow[c], pr ? s_d[c] : slab[c * R + r]);
-      if (j + 1 < w) {
-        const T v = absv(slab[(j + 1) * R + r]);
-        if (argmax_better(v, rb + r, bv, br)) {
-          bv = v;
-          br = rb + r;
-        }
-      }
-    }
+    panel_update_rows<T, W>(slab, R, nr, r0, j, w, pl, s_d, urow, singular, inv, rb, bv, br);
     block_argmax_nolead(bv, br, s_rv, s_rr);
   }
   __syncthreads();
@@ -499,9 +543,7 @@ getf2_panel_cluster_kernel(PanelParams<T> p) {
   const int re = min(rb + R, p.mp);
   const int nr = max(re - rb, 0);
 
-  for (int c = 0; c < w; ++c)
-    for (int r = tid; r < nr; r += blockDim.x)
-      slab[c * R + r] = p.A[(long)(rb + r) + (long)c * p.lda];
+  panel_load_slab(slab, p.A, p.lda, rb, nr, R, w);
   __syncthreads();
 
   T bv = T(-1);
@@ -577,21 +619,7 @@ getf2_panel_cluster_kernel(PanelParams<T> p) {
     const int r0 = max(j + 1 - rb, 0);
     const int pl = (piv != j && piv >= rb && piv < re) ? piv - rb : -1;
     if (pl >= 0 && tid < j) slab[tid * R + pl] = s_d[tid];
-    for (int r = r0 + tid; r < nr; r += blockDim.x) {
-      const bool pr = r == pl;
-      T l = pr ? s_d[j] : slab[j * R + r];
-      if (!singular) l *= inv;
-      slab[j * R + r] = l;
-      for (int c = j + 1; c < w; ++c)
-        slab[c * R + r] = fma(-l, urow[c], pr ? s_d[c] : slab[c * R + r]);
-      if (j + 1 < w) {
-        const T v = absv(slab[(j + 1) * R + r]);
-        if (argmax_better(v, rb + r, bv, br)) {
-          bv = v;
-          br = rb + r;
-        }
-      }
-    }
+    panel_update_rows<T, W>(slab, R, nr, r0, j, w, pl, s_d, urow, singular, inv, rb, bv, br);
     block_argmax_nolead(bv, br, s_rv, s_rr);
   }
   __syncthreads();
