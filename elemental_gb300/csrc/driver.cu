@@ -811,11 +811,18 @@ int ElGBCreate(ElGBContext* out, int device) {
   auto* c = new (std::nothrow) ElGBContextImpl();
   if (!c) return elgb::kElAllocError;
   c->device = device;
+  int least_prio = 0, greatest_prio = 0;
   if (cudaSetDevice(device) != cudaSuccess ||
       cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device) !=
           cudaSuccess ||
       cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&c->side_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      // the look-ahead panel's stream at the highest priority: its small,
+      // latency-bound kernels (leaf panels, the panel's own interchanges,
+      // TRSMs) are the critical path and must not queue behind the trailing
+      // update's thousands of tensor-core CTAs on the other stream
+      cudaDeviceGetStreamPriorityRange(&least_prio, &greatest_prio) != cudaSuccess ||
+      cudaStreamCreateWithPriority(&c->side_stream, cudaStreamNonBlocking, greatest_prio) !=
+          cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
       cudaMalloc(&c->status, sizeof(elgb::DevStatus)) != cudaSuccess ||

@@ -157,8 +157,8 @@ __device__ __forceinline__ void panel_load_slab(T* slab, const T* A, long lda, i
 // ld R): the multipliers l = a_rj / alpha and the rank-1 update of columns
 // j+1 .. w-1 with the pivot row urow; row pl (the pivot's old position)
 // takes old row j's values from s_d.  Returns this CTA's candidate for
-// column j+1 in (bv, br).  Columns go in groups of four (four loads in
-// flight per row).  (Holding urow in registers with a fully unrolled
+// column j+1 in (bv, br).  Columns go in groups of eight, then four (that
+// many loads in flight per row).  (Holding urow in registers with a fully unrolled
 // 32-column body measured slower: it issues all 32 columns' predicated
 // instructions for every j.)
 template <typename T, int W>
@@ -174,7 +174,16 @@ __device__ __forceinline__ void panel_update_rows(T* slab, int R, int nr, int r0
     const T* src = pr ? s_d : slab + r;  // old row j's values for row pl
     const int sst = pr ? 1 : R;
     int c = j + 1;
-    for (; c + 3 < w; c += 4) {  // four loads in flight, then four fmas / stores
+    for (; c + 7 < w; c += 8) {  // eight loads in flight, then eight fmas / stores
+      T v[8];
+#pragma unroll
+      for (int e = 0; e < 8; ++e) v[e] = src[(c + e) * sst];
+#pragma unroll
+      for (int e = 0; e < 8; ++e) v[e] = fma(-l, urow[c + e], v[e]);
+#pragma unroll
+      for (int e = 0; e < 8; ++e) slab[(c + e) * R + r] = v[e];
+    }
+    for (; c + 3 < w; c += 4) {
       T v0 = src[c * sst], v1 = src[(c + 1) * sst], v2 = src[(c + 2) * sst],
         v3 = src[(c + 3) * sst];
       v0 = fma(-l, urow[c], v0);
