@@ -102,7 +102,13 @@ struct PanelParams {
 };
 
 constexpr int kPanelW = 32;
-constexpr int kPanelThreads = 256;
+// Threads of a panel CTA: 512 for FP32 (two rows of a ~1024-row slab per
+// thread halve the local update of each pivot step), 256 for FP64 (its
+// candidate rows need the registers).
+template <typename T>
+__host__ __device__ constexpr int panel_threads() {
+  return sizeof(T) == 4 ? 512 : 256;
+}
 
 __device__ __forceinline__ void st_release_s32(int* p, int v) {
   asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
@@ -207,15 +213,15 @@ __device__ __forceinline__ void panel_update_rows(T* slab, int R, int nr, int r0
 }
 
 template <typename T, int W>
-__global__ void __launch_bounds__(kPanelThreads)
+__global__ void __launch_bounds__(panel_threads<T>())
 getf2_panel_kernel(PanelParams<T> p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* slab = reinterpret_cast<T*>(smem_raw);
   __shared__ T s_d[W];
   __shared__ T s_rv[33];
   __shared__ int s_rr[33];
-  __shared__ T s_gv[kPanelThreads];
-  __shared__ int s_gr[kPanelThreads];
+  __shared__ T s_gv[panel_threads<T>()];
+  __shared__ int s_gr[panel_threads<T>()];
   T* s_rows = slab + (size_t)p.R * W;  // [G][W] candidate rows (dynamic smem)
   __shared__ int s_abort;
 
@@ -533,7 +539,7 @@ __device__ __forceinline__ int ld_cluster_s32(uint32_t addr) {
 }
 
 template <typename T, int W>
-__global__ void __launch_bounds__(kPanelThreads)
+__global__ void __launch_bounds__(panel_threads<T>())
 getf2_panel_cluster_kernel(PanelParams<T> p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* slab = reinterpret_cast<T*>(smem_raw);
@@ -667,7 +673,7 @@ static cudaError_t launch_getf2_panel_cluster(T* A, long lda, int mp, int w, int
   if (e != cudaSuccess) return e;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(C);
-  cfg.blockDim = dim3(kPanelThreads);
+  cfg.blockDim = dim3(panel_threads<T>());
   cfg.dynamicSmemBytes = smem;
   cfg.stream = stream;
   cudaLaunchAttribute attr[1];
@@ -726,7 +732,7 @@ cudaError_t launch_getf2_panel(T* A, long lda, int mp, int w, int* ipiv, int row
   int G = std::max(ceil_div(mp, 1024), ceil_div(mp, rows_cap));
   if (G > num_sms) G = num_sms;
   if (G > s.maxG) G = s.maxG;
-  if (G > kPanelThreads) G = kPanelThreads;
+  if (G > panel_threads<T>()) G = panel_threads<T>();
   if (G < 1) G = 1;
   int R = ceil_div(mp, G);
   G = ceil_div(mp, R);  // no CTA without rows
@@ -738,7 +744,7 @@ cudaError_t launch_getf2_panel(T* A, long lda, int mp, int w, int* ipiv, int row
   if (e != cudaSuccess) return e;
   PanelParams<T> prm{A, lda, mp, w, R, ipiv, row_base, info_base, epoch_base, s, st};
   void* args[] = {&prm};
-  return cudaLaunchCooperativeKernel((const void*)kern, dim3(G), dim3(kPanelThreads),
+  return cudaLaunchCooperativeKernel((const void*)kern, dim3(G), dim3(panel_threads<T>()),
                                      args, smem, stream);
 }
 
