@@ -22,7 +22,8 @@ from . import _lib
 # Enumerations (include/El/core/types.h:211-228)
 NORMAL, TRANSPOSE, ADJOINT = 0, 1, 2
 LOWER, UPPER = 0, 1
-LU_PARTIAL = 1  # python/lapack_like/factor.py pivType
+# LU pivot types (python/lapack_like/factor.py:493)
+LU_PARTIAL, LU_FULL, LU_ROOK, LU_WITHOUT_PIVOTING = 0, 1, 2, 3
 
 _TAG = {np.dtype(np.int32): "i", np.dtype(np.float32): "s", np.dtype(np.float64): "d"}
 
@@ -151,10 +152,15 @@ def PopBlocksizeStack():
 
 
 def LU(A: Matrix, pivType=LU_PARTIAL):
-    """El.LU(A) with partial pivoting: A is overwritten by the packed L\\U;
-    returns the Permutation (python/lapack_like/factor.py:525-542)."""
+    """El.LU(A, pivType) (python/lapack_like/factor.py:525-542): A is
+    overwritten by the packed L\\U.  Partial pivoting returns the
+    Permutation; LU_WITHOUT_PIVOTING (ElLU_*) returns None and raises
+    SingularMatrixException at an exact zero pivot."""
+    if pivType == LU_WITHOUT_PIVOTING:
+        _check(getattr(A.lib, f"ElLU_{A.tag}")(A.obj), "LU", SingularMatrixException)
+        return None
     if pivType != LU_PARTIAL:
-        raise ValueError("only partial pivoting is on this path")
+        raise ValueError("full and rook pivoting are not on this path")
     P = Permutation()
     _check(getattr(A.lib, f"ElLUPartialPiv_{A.tag}")(A.obj, P.obj), "LU", SingularMatrixException)
     P._dests = _swap_dests_from_explicit(P.ExplicitVector())[: min(A.Height(), A.Width())]
@@ -174,6 +180,21 @@ def Cholesky(uplo, A: Matrix):
 def SolveAfterCholesky(uplo, orient, A: Matrix, B: Matrix):
     _check(getattr(A.lib, f"ElSolveAfterCholesky_{A.tag}")(uplo, orient, A.obj, B.obj),
            "SolveAfterCholesky")
+
+
+def Inverse(A: Matrix):
+    """El.Inverse(A) (python/lapack_like/funcs.py:85-98): A := inv(A);
+    SingularMatrixException at an exact zero pivot."""
+    _check(getattr(A.lib, f"ElInverse_{A.tag}")(A.obj), "Inverse", SingularMatrixException)
+
+
+def OneCondition(A: Matrix):
+    """El.OneCondition(A) (python/lapack_like/props.py:144-158): ||A||_1
+    ||inv(A)||_1, +inf for a singular A."""
+    cond = (ctypes.c_double if A.tag == "d" else ctypes.c_float)()
+    _check(getattr(A.lib, f"ElOneCondition_{A.tag}")(A.obj, ctypes.byref(cond)),
+           "OneCondition")
+    return cond.value
 
 
 def LinearSolve(A: Matrix, B: Matrix):

@@ -90,6 +90,9 @@ def load():
         _sig(lib, f"ElGBLinearSolve_{s}", c_int, vp, c_int, vp, c_int, c_int, vp, c_int, c_int)
         _sig(lib, f"ElGBHPDSolve_{s}", c_int, vp, c_int, c_int, vp, c_int, c_int, vp, c_int,
              c_int)
+        _sig(lib, f"ElGBLUNoPiv_{s}", c_int, vp, c_int, c_int, vp, c_int, c_int)
+        _sig(lib, f"ElGBInverse_{s}", c_int, vp, c_int, vp, c_int, c_int)
+        _sig(lib, f"ElGBOneCondition_{s}", c_int, vp, c_int, vp, c_int, c_int, P(c_double))
     _sig(lib, "ElGBLUPartialPivMixed_s", c_int, vp, c_int, c_int, vp, c_int, vp, c_int, c_int)
     _sig(lib, "ElGBGemmSubTC", c_int, vp, c_int, c_int, c_int, c_int, vp, c_int, vp, c_int, vp,
          c_int)
@@ -137,6 +140,10 @@ def load():
     _sig(lib, "ElPopBlocksizeStack", c_int)
     for s in ("s", "d"):
         _sig(lib, f"ElLUPartialPiv_{s}", c_int, vp, vp)
+        _sig(lib, f"ElLU_{s}", c_int, vp)
+        _sig(lib, f"ElInverse_{s}", c_int, vp)
+        _sig(lib, f"ElOneCondition_{s}", c_int, vp,
+             P(ctypes.c_double if s == "d" else ctypes.c_float))
         _sig(lib, f"ElSolveAfterLUPartialPiv_{s}", c_int, c_int, vp, vp, vp)
         _sig(lib, f"ElCholesky_{s}", c_int, c_int, vp)
         _sig(lib, f"ElSolveAfterCholesky_{s}", c_int, c_int, c_int, vp, vp)

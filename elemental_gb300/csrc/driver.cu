@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <limits>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -220,6 +221,7 @@ struct LuState {
   T* Bc;               // companion block receiving the same row operations
   long ldbc;           // (RowEchelon's B, src/lapack_like/solve/Linear.cpp:62-71)
   int nbc;
+  bool nopiv;          // El::LU(A): no pivot search, no interchanges
   int* dlab;           // deferred left interchanges: labels per block column
   T* dtmp;             //   and the gather's scratch
   bool tournament;     // FP32 leaf panels by tournament pivoting
@@ -255,6 +257,7 @@ template <typename T>
 static cudaError_t apply_swaps(LuState<T>& s, const LuLane& L, int c0, int w, int a0, int a1,
                                int b0, int b1, bool companion) {
   Context* ctx = s.ctx;
+  if (s.nopiv) return cudaSuccess;  // every interchange is the identity
   const int pi = ctx->prof_begin(L.st);
   LANE_CHECK(launch_build_swap_pairs(s.ipiv + c0, c0, w, L.pairs, L.pair_count, L.st), 1);
   if ((a1 > a0) || (b1 > b0))
@@ -279,7 +282,7 @@ static cudaError_t panel_rec(LuState<T>& s, const LuLane& L, int c0, int w) {
     const int pi = ctx->prof_begin(L.st);
     bool done = false;
     if constexpr (sizeof(T) == 4) {
-      if (s.tournament) {
+      if (s.tournament && !s.nopiv) {
         int nl = 0;
         const cudaError_t e = launch_calu_panel(
             reinterpret_cast<float*>(s.A) + c0 + (long)c0 * s.lda, s.lda, s.m - c0, w,
@@ -292,7 +295,7 @@ static cudaError_t panel_rec(LuState<T>& s, const LuLane& L, int c0, int w) {
     if (!done) {
       LANE_CHECK(launch_getf2_panel<T>(s.A + c0 + (long)c0 * s.lda, s.lda, s.m - c0, w,
                                        s.ipiv + c0, c0, c0, s.panel_epoch, s.ps, ctx->status,
-                                       s.panel_ctas, L.st), 1);
+                                       s.panel_ctas, L.st, s.nopiv), 1);
       s.panel_epoch += w;
     }
     ctx->prof_end(pi, L.st, ELGB_PROF_PANEL, (double)(s.m - c0) * w * w,
@@ -407,6 +410,7 @@ static cudaError_t getrf_run(LuState<T>& s, int nb) {
       if (e != cudaSuccess) return e;
     }
   }
+  if (s.nopiv) return cudaSuccess;
   // every block column of L takes the later panels' interchanges at once
   const int pi = ctx->prof_begin(s.main.st);
   LANE_CHECK(launch_defer_labels(s.ipiv, s.m, minDim, nb, s.dlab, s.main.st), 1);
@@ -455,7 +459,7 @@ static bool use_lookahead(int m, int n, int nb) { return std::min(m, n) >= 4 * n
 
 template <typename T>
 cudaError_t getrf(Context* ctx, int m, int n, T* A, long lda, int* ipiv, int nb, int tc_kind,
-                  bool tournament) {
+                  bool tournament, bool nopiv) {
   if (nb <= 0) nb = g_blocksize;
   cudaError_t e = ctx->begin_call();
   if (e != cudaSuccess) return e;
@@ -492,6 +496,7 @@ cudaError_t getrf(Context* ctx, int m, int n, T* A, long lda, int* ipiv, int nb,
   }
   if (ctx->opt_panel_ctas > 0) s.panel_ctas = std::min(ctx->opt_panel_ctas, ctx->num_sms);
   s.tournament = tournament && sizeof(T) == 4;
+  s.nopiv = nopiv;
   s.A = A;
   s.lda = lda;
   s.m = m;
@@ -776,8 +781,136 @@ cudaError_t backward_error(Context* ctx, int n, int q, const double* A, long lda
   return cudaSuccess;
 }
 
-template cudaError_t getrf<double>(Context*, int, int, double*, long, int*, int, int, bool);
-template cudaError_t getrf<float>(Context*, int, int, float*, long, int*, int, int, bool);
+// ---------------------------------------------------------------------------
+// El::Inverse and El::OneCondition
+// ---------------------------------------------------------------------------
+// max_j sum_i |A(i, j)|: one warp per column; the non-negative FP64 maxima
+// order like their bit patterns, so an integer atomicMax combines them.
+template <typename T>
+__global__ void col_abs_sum_max_kernel(const T* __restrict__ A, long lda, int m, int n,
+                                       unsigned long long* out) {
+  const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+  double best = 0.0;
+  for (int j = blockIdx.x * wpb + (threadIdx.x >> 5); j < n; j += gridDim.x * wpb) {
+    double sum = 0.0;
+    for (int i = lane; i < m; i += 32) sum += fabs((double)A[i + (long)j * lda]);
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    best = fmax(best, sum);
+  }
+  if (lane == 0) atomicMax(out, (unsigned long long)__double_as_longlong(best));
+}
+
+template <typename T>
+__global__ void set_identity_kernel(T* X, long ldx, int n) {
+  const int j = blockIdx.y;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    X[i + (long)j * ldx] = i == j ? T(1) : T(0);
+}
+
+// One-norm of an m x n device matrix (synchronizes); tmp: one device word.
+template <typename T>
+static cudaError_t one_norm(Context* ctx, int m, int n, const T* A, long lda,
+                            unsigned long long* tmp, double* out) {
+  cudaError_t e = cudaMemsetAsync(tmp, 0, sizeof(unsigned long long), ctx->stream);
+  if (e != cudaSuccess) return e;
+  const int blocks = std::max(1, std::min(ceil_div(n, 8), 4 * ctx->num_sms));
+  col_abs_sum_max_kernel<T><<<blocks, 256, 0, ctx->stream>>>(A, lda, m, n, tmp);
+  ctx->launches += 1;
+  unsigned long long h = 0;
+  e = cudaMemcpyAsync(&h, tmp, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  double v;
+  std::memcpy(&v, &h, sizeof(v));
+  *out = v;
+  return e;
+}
+
+// Reads the device status word (synchronizes).
+static cudaError_t read_status(Context* ctx, int* info, int* err) {
+  cudaError_t e = cudaMemcpyAsync(ctx->h_status, ctx->status, sizeof(DevStatus),
+                                  cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  *info = ctx->h_status->info;
+  *err = ctx->h_status->err;
+  return e;
+}
+
+// inv(A) = inv(U) inv(L) P (funcs/Inverse/General/LUPartialPiv.hpp:21-62),
+// formed as the solve of P A X = I by getrs on the factors: the same
+// operator, column by column.  ipiv: n ints; X: n x n scratch.  With a zero
+// pivot the status word keeps getrf's info and A holds the partial factors
+// (the reference throws SingularMatrixException from El::LU).
+template <typename T>
+static cudaError_t getri_impl(Context* ctx, int n, T* A, long lda, int nb, int* ipiv, T* X) {
+  cudaError_t e = getrf<T>(ctx, n, n, A, lda, ipiv, nb);
+  if (e != cudaSuccess) return e;
+  int info = 0, err = 0;
+  e = read_status(ctx, &info, &err);
+  if (e != cudaSuccess || info || err) return e;
+  set_identity_kernel<T><<<dim3(ceil_div(n, 256), n), 256, 0, ctx->stream>>>(X, n, n);
+  ctx->launches += 1;
+  e = getrs<T>(ctx, 0, n, A, lda, ipiv, n, X, n, nullptr);
+  if (e != cudaSuccess) return e;
+  return cudaMemcpy2DAsync(A, lda * sizeof(T), X, (size_t)n * sizeof(T), (size_t)n * sizeof(T),
+                           n, cudaMemcpyDeviceToDevice, ctx->stream);
+}
+
+template <typename T>
+cudaError_t getri(Context* ctx, int n, T* A, long lda, int nb) {
+  if (n == 0) return ctx->begin_call();
+  cudaError_t e = ctx->ensure2(align256((size_t)n * sizeof(int)) +
+                               align256((size_t)n * n * sizeof(T)));
+  if (e != cudaSuccess) return e;
+  char* p = static_cast<char*>(ctx->arena2);
+  int* ipiv = reinterpret_cast<int*>(p);
+  T* X = reinterpret_cast<T*>(p + align256((size_t)n * sizeof(int)));
+  return getri_impl<T>(ctx, n, A, lda, nb, ipiv, X);
+}
+
+template <typename T>
+cudaError_t one_condition(Context* ctx, int n, const T* A, long lda, int nb, double* cond) {
+  cudaError_t e = ctx->begin_call();
+  if (e != cudaSuccess) return e;
+  if (n == 0) {
+    *cond = 0.0;
+    return cudaSuccess;
+  }
+  const size_t sm = align256((size_t)n * n * sizeof(T));
+  e = ctx->ensure2(2 * sm + align256((size_t)n * sizeof(int)) + 256);
+  if (e != cudaSuccess) return e;
+  char* p = static_cast<char*>(ctx->arena2);
+  T* B = reinterpret_cast<T*>(p);
+  T* X = reinterpret_cast<T*>(p + sm);
+  int* ipiv = reinterpret_cast<int*>(p + 2 * sm);
+  auto* tmp = reinterpret_cast<unsigned long long*>(p + 2 * sm + align256((size_t)n * sizeof(int)));
+  // Matrix<Field> B( A ); oneNorm = OneNorm( B ); Inverse( B ) (One.cpp:16-19)
+  e = cudaMemcpy2DAsync(B, (size_t)n * sizeof(T), A, lda * sizeof(T), (size_t)n * sizeof(T), n,
+                        cudaMemcpyDeviceToDevice, ctx->stream);
+  double n1 = 0.0, n1inv = 0.0;
+  if (e == cudaSuccess) e = one_norm<T>(ctx, n, n, B, n, tmp, &n1);
+  if (e == cudaSuccess) e = getri_impl<T>(ctx, n, B, n, nb, ipiv, X);
+  if (e != cudaSuccess) return e;
+  int info = 0, err = 0;
+  e = read_status(ctx, &info, &err);
+  if (e != cudaSuccess) return e;
+  if (err) return cudaErrorLaunchTimeout;
+  if (info) {  // SingularMatrixException -> +inf (One.cpp:20-21), not an error
+    *cond = std::numeric_limits<double>::infinity();
+    return cudaMemsetAsync(ctx->status, 0, sizeof(DevStatus), ctx->stream);
+  }
+  e = one_norm<T>(ctx, n, n, B, n, tmp, &n1inv);
+  *cond = n1 * n1inv;
+  return e;
+}
+
+template cudaError_t getri<double>(Context*, int, double*, long, int);
+template cudaError_t getri<float>(Context*, int, float*, long, int);
+template cudaError_t one_condition<double>(Context*, int, const double*, long, int, double*);
+template cudaError_t one_condition<float>(Context*, int, const float*, long, int, double*);
+
+template cudaError_t getrf<double>(Context*, int, int, double*, long, int*, int, int, bool,
+                                   bool);
+template cudaError_t getrf<float>(Context*, int, int, float*, long, int*, int, int, bool, bool);
 template cudaError_t getrs<double>(Context*, int, int, const double*, long, const int*, int,
                                    double*, long, const int*);
 template cudaError_t getrs<float>(Context*, int, int, const float*, long, const int*, int,
@@ -986,6 +1119,27 @@ long long ElGBLaunchCount(ElGBContext ctx) { return ctx ? ctx->launches : -1; }
                        ldb >= std::max(n, 1) && (uplo == 0 || uplo == 1)))                 \
       return r;                                                                            \
     return elgb::to_el_error(elgb::hpd_solve<T>(ctx, uplo, n, A, lda, nrhs, B, ldb, nb));  \
+  }                                                                                        \
+  int ElGBLUNoPiv_##S(ElGBContext ctx, int m, int n, T* A, int lda, int nb) {              \
+    if (int r = arg_ok(ctx && m >= 0 && n >= 0 && lda >= std::max(m, 1) &&                 \
+                       (m * n == 0 || A)))                                                 \
+      return r;                                                                            \
+    const int mn = std::min(m, n);                                                         \
+    cudaError_t e = ctx->ensure2(sizeof(int) * (size_t)std::max(mn, 1));                   \
+    if (e != cudaSuccess) return elgb::to_el_error(e);                                     \
+    return elgb::to_el_error(elgb::getrf<T>(ctx, m, n, A, lda,                             \
+                                            static_cast<int*>(ctx->arena2), nb, -1, false, \
+                                            true));                                        \
+  }                                                                                        \
+  int ElGBInverse_##S(ElGBContext ctx, int n, T* A, int lda, int nb) {                     \
+    if (int r = arg_ok(ctx && n >= 0 && lda >= std::max(n, 1) && (n == 0 || A))) return r; \
+    return elgb::to_el_error(elgb::getri<T>(ctx, n, A, lda, nb));                          \
+  }                                                                                        \
+  int ElGBOneCondition_##S(ElGBContext ctx, int n, const T* A, int lda, int nb,            \
+                           double* cond) {                                                 \
+    if (int r = arg_ok(ctx && n >= 0 && lda >= std::max(n, 1) && cond && (n == 0 || A)))   \
+      return r;                                                                            \
+    return elgb::to_el_error(elgb::one_condition<T>(ctx, n, A, lda, nb, cond));            \
   }
 
 ELGB_LU(d, double)

@@ -74,7 +74,15 @@ void set_blocksize(int nb);
 
 template <typename T>
 cudaError_t getrf(Context* ctx, int m, int n, T* A, long lda, int* ipiv, int nb,
-                  int tc_kind = -1, bool tournament = false);
+                  int tc_kind = -1, bool tournament = false, bool nopiv = false);
+// El::Inverse (funcs/Inverse/General/LUPartialPiv.hpp): A := inv(A) in place
+// through getrf and getrs on the identity; info (status) at a zero pivot.
+template <typename T>
+cudaError_t getri(Context* ctx, int n, T* A, long lda, int nb);
+// El::OneCondition (props/Condition/One.cpp:12-24): ||A||_1 ||inv(A)||_1 on
+// a device copy of A (A itself untouched); +inf when A is singular.
+template <typename T>
+cudaError_t one_condition(Context* ctx, int n, const T* A, long lda, int nb, double* cond);
 template <typename T>
 cudaError_t getrs(Context* ctx, int orient, int n, const T* A, long lda, const int* ipiv,
                   int nrhs, T* B, long ldb, const int* perm);

@@ -319,6 +319,15 @@ struct Dispatch<double> {
                  int ldb, int nb) {
     return ElGBHPDSolve_d(c, u, n, A, lda, q, B, ldb, nb);
   }
+  static int lunopiv(ElGBContext c, int m, int n, double* A, int lda, int nb) {
+    return ElGBLUNoPiv_d(c, m, n, A, lda, nb);
+  }
+  static int inv(ElGBContext c, int n, double* A, int lda, int nb) {
+    return ElGBInverse_d(c, n, A, lda, nb);
+  }
+  static int cond1(ElGBContext c, int n, const double* A, int lda, int nb, double* k) {
+    return ElGBOneCondition_d(c, n, A, lda, nb, k);
+  }
 };
 template <>
 struct Dispatch<float> {
@@ -343,6 +352,15 @@ struct Dispatch<float> {
   static int hpd(ElGBContext c, int u, int n, const float* A, int lda, int q, float* B,
                  int ldb, int nb) {
     return ElGBHPDSolve_s(c, u, n, A, lda, q, B, ldb, nb);
+  }
+  static int lunopiv(ElGBContext c, int m, int n, float* A, int lda, int nb) {
+    return ElGBLUNoPiv_s(c, m, n, A, lda, nb);
+  }
+  static int inv(ElGBContext c, int n, float* A, int lda, int nb) {
+    return ElGBInverse_s(c, n, A, lda, nb);
+  }
+  static int cond1(ElGBContext c, int n, const float* A, int lda, int nb, double* k) {
+    return ElGBOneCondition_s(c, n, A, lda, nb, k);
   }
 };
 
@@ -381,6 +399,50 @@ void LU(Matrix<F>& A, Permutation& P) {
     throw SingularMatrixException();
   }
   P.SetSwapSequence(m, piv.data(), minDim);
+}
+
+// El::LU(A) without pivoting (src/lapack_like/factor/LU.cpp:21-44).
+template <typename F>
+void LU(Matrix<F>& A) {
+  std::lock_guard<std::mutex> lk(St().mu);
+  const Int m = A.Height(), n = A.Width();
+  if (std::min(m, n) == 0) return;
+  ElGBContext ctx = Ctx();
+  F* dA = reinterpret_cast<F*>(Dev(Al(sizeof(F) * (size_t)m * n)));
+  Upload(ctx, dA, A);
+  CheckRc(Dispatch<F>::lunopiv(ctx, m, n, dA, m, Blocksize()));
+  CheckStatus(ctx, false);  // lu::Unb throws at an exact zero pivot (LU/Local.hpp:50-51)
+  Download(A, dA);
+}
+
+// El::Inverse (src/lapack_like/funcs/Inverse/General.cpp:15-20).
+template <typename F>
+void Inverse(Matrix<F>& A) {
+  if (A.Height() != A.Width()) throw std::logic_error("Cannot invert non-square matrices");
+  std::lock_guard<std::mutex> lk(St().mu);
+  const Int n = A.Height();
+  if (n == 0) return;
+  ElGBContext ctx = Ctx();
+  F* dA = reinterpret_cast<F*>(Dev(Al(sizeof(F) * (size_t)n * n)));
+  Upload(ctx, dA, A);
+  CheckRc(Dispatch<F>::inv(ctx, n, dA, n, Blocksize()));
+  CheckStatus(ctx, false);
+  Download(A, dA);
+}
+
+// El::OneCondition (src/lapack_like/props/Condition/One.cpp:12-24).
+template <typename F>
+F OneCondition(const Matrix<F>& A) {
+  if (A.Height() != A.Width()) throw std::logic_error("OneCondition needs a square matrix");
+  std::lock_guard<std::mutex> lk(St().mu);
+  const Int n = A.Height();
+  if (n == 0) return F(0);
+  ElGBContext ctx = Ctx();
+  F* dA = reinterpret_cast<F*>(Dev(Al(sizeof(F) * (size_t)n * n)));
+  Upload(ctx, dA, A);
+  double k = 0.0;
+  CheckRc(Dispatch<F>::cond1(ctx, n, dA, n, Blocksize(), &k));
+  return static_cast<F>(k);
 }
 
 namespace lu {
@@ -510,6 +572,9 @@ void LinearSolveMixed(const Matrix<double>& A, Matrix<double>& B, const ElGBRefi
 
 #define EL_GB_PROTO(F)                                                                  \
   template void LU<F>(Matrix<F>&, Permutation&);                                        \
+  template void LU<F>(Matrix<F>&);                                                      \
+  template void Inverse<F>(Matrix<F>&);                                                 \
+  template F OneCondition<F>(const Matrix<F>&);                                         \
   template void lu::SolveAfter<F>(Orientation, const Matrix<F>&, const Permutation&,    \
                                   Matrix<F>&);                                          \
   template void Cholesky<F>(UpperOrLower, Matrix<F>&);                                  \
@@ -658,6 +723,18 @@ static El::UpperOrLower Ul(ElUpperOrLower u) { return u == EL_UPPER ? El::UPPER 
 ElError ElLUPartialPiv_s(ElMatrix_s A, ElPermutation P) { EL_GB_TRY(El::LU(*M<float>(A), *PP(P))) }
 ElError ElLUPartialPiv_d(ElMatrix_d A, ElPermutation P) {
   EL_GB_TRY(El::LU(*M<double>(A), *PP(P)))
+}
+ElError ElLU_s(ElMatrix_s A) { EL_GB_TRY(El::LU(*M<float>(A))) }
+ElError ElLU_d(ElMatrix_d A) { EL_GB_TRY(El::LU(*M<double>(A))) }
+ElError ElInverse_s(ElMatrix_s A) { EL_GB_TRY(El::Inverse(*M<float>(A))) }
+ElError ElInverse_d(ElMatrix_d A) { EL_GB_TRY(El::Inverse(*M<double>(A))) }
+ElError ElOneCondition_s(ElConstMatrix_s A, float* cond) {
+  if (!cond) return EL_ARG_ERROR;
+  EL_GB_TRY(*cond = El::OneCondition(*CM<float>(A)))
+}
+ElError ElOneCondition_d(ElConstMatrix_d A, double* cond) {
+  if (!cond) return EL_ARG_ERROR;
+  EL_GB_TRY(*cond = El::OneCondition(*CM<double>(A)))
 }
 ElError ElSolveAfterLUPartialPiv_s(ElOrientation o, ElConstMatrix_s A, ElConstPermutation P,
                                    ElMatrix_s B) {

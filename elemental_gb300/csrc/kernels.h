@@ -52,12 +52,13 @@ extern int g_panel_regs;
 // ipiv[c] receives the absolute pivot row (row_base + panel row).  A zero
 // pivot records info = info_base + c + 1 (first one wins) in st.
 // epoch_base: columns published so far in this factorization (the slot
-// epochs must keep growing across launches).
+// epochs must keep growing across launches).  nopiv: no pivot search, the
+// pivot of column c is row c (El::LU(A), ipiv[c] = row_base + c).
 template <typename T>
 cudaError_t launch_getf2_panel(T* A, long lda, int mp, int w, int* ipiv,
                                int row_base, int info_base, int epoch_base,
                                const PanelScratch<T>& s, DevStatus* st,
-                               int num_sms, cudaStream_t stream);
+                               int num_sms, cudaStream_t stream, bool nopiv = false);
 
 // Converts the swap sequence ipiv[0..nb) (absolute destinations for rows
 // k..k+nb) into an explicit list of (dst, src) row moves.  pairs must hold

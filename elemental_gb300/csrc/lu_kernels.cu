@@ -99,6 +99,7 @@ struct PanelParams {
   int epoch_base;  // column j of this launch publishes epoch_base + j + 1
   PanelScratch<T> s;
   DevStatus* st;
+  int nopiv;       // 1: El::LU without pivoting -- the pivot of column j is row j
 };
 
 constexpr int kPanelW = 32;
@@ -248,6 +249,10 @@ getf2_panel_kernel(PanelParams<T> p) {
   block_argmax(bv, br, s_rv, s_rr);
 
   for (int j = 0; j < w; ++j) {
+    if (p.nopiv) {  // the only candidate is row j (lu::Unb, LU/Local.hpp:42-61)
+      br = (j >= rb && j < re) ? j : -1;
+      bv = br >= 0 ? T(1) : T(-1);
+    }
     const int epoch = p.epoch_base + j + 1;
     const int par = epoch & 1;
     PanelSlot<T>* my = p.s.slots + (long)par * maxG + b;
@@ -696,11 +701,11 @@ static cudaError_t launch_getf2_panel_cluster(T* A, long lda, int mp, int w, int
 template <typename T>
 cudaError_t launch_getf2_panel(T* A, long lda, int mp, int w, int* ipiv, int row_base,
                                int info_base, int epoch_base, const PanelScratch<T>& s,
-                               DevStatus* st, int num_sms, cudaStream_t stream) {
+                               DevStatus* st, int num_sms, cudaStream_t stream, bool nopiv) {
   if (w <= 0 || mp <= 0) return cudaSuccess;
   if (w > kPanelW || mp < w) return cudaErrorInvalidValue;
   if constexpr (sizeof(T) == 4) {
-    if (g_panel_regs) {
+    if (g_panel_regs && !nopiv) {
       // ~1024 rows per CTA (512 threads x 2 rows in registers)
       const int Rr = kRegThreads * kRegRows;
       int G = ceil_div(mp, Rr);
@@ -716,7 +721,7 @@ cudaError_t launch_getf2_panel(T* A, long lda, int mp, int w, int* ipiv, int row
       }
     }
   }
-  if (g_panel_cluster > 1) {
+  if (g_panel_cluster > 1 && !nopiv) {
     const int C = cluster_ctas<T>(mp, g_panel_cluster);
     if (C > 0) {
       const cudaError_t e =
@@ -742,7 +747,8 @@ cudaError_t launch_getf2_panel(T* A, long lda, int mp, int w, int* ipiv, int row
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        kMaxSmem);
   if (e != cudaSuccess) return e;
-  PanelParams<T> prm{A, lda, mp, w, R, ipiv, row_base, info_base, epoch_base, s, st};
+  PanelParams<T> prm{A, lda, mp, w, R, ipiv, row_base, info_base, epoch_base, s, st,
+                     nopiv ? 1 : 0};
   void* args[] = {&prm};
   return cudaLaunchCooperativeKernel((const void*)kern, dim3(G), dim3(panel_threads<T>()),
                                      args, smem, stream);
@@ -750,10 +756,10 @@ cudaError_t launch_getf2_panel(T* A, long lda, int mp, int w, int* ipiv, int row
 
 template cudaError_t launch_getf2_panel<double>(double*, long, int, int, int*, int, int, int,
                                                 const PanelScratch<double>&, DevStatus*,
-                                                int, cudaStream_t);
+                                                int, cudaStream_t, bool);
 template cudaError_t launch_getf2_panel<float>(float*, long, int, int, int*, int, int, int,
                                                const PanelScratch<float>&, DevStatus*,
-                                               int, cudaStream_t);
+                                               int, cudaStream_t, bool);
 
 // ---------------------------------------------------------------------------
 // K2: row interchanges (PB.PermuteRows, src/lapack_like/factor/LU.cpp:130-131)

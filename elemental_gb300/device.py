@@ -192,6 +192,32 @@ class Context:
                        precision=PRECISION_NAMES[inf.precision],
                        backward_error=inf.backward_error)
 
+    def lu_nopiv(self, A, nb=0):
+        """El::LU(A) without pivoting, in place (ElGBLUNoPiv_*)."""
+        m, n = A.shape
+        self._bind()
+        self._rc(getattr(self.lib, f"ElGBLUNoPiv_{_DT[A.dtype]}")(self.h, m, n, _ptr(A), _ld(A),
+                                                                  nb), "LUNoPiv")
+        return A
+
+    def inverse(self, A, nb=0):
+        """El::Inverse(A): A := inv(A) in place (ElGBInverse_*)."""
+        n = A.shape[0]
+        self._bind()
+        self._rc(getattr(self.lib, f"ElGBInverse_{_DT[A.dtype]}")(self.h, n, _ptr(A), _ld(A), nb),
+                 "Inverse")
+        return A
+
+    def one_condition(self, A, nb=0):
+        """El::OneCondition(A) = ||A||_1 ||inv(A)||_1 (+inf when singular);
+        A is not modified (ElGBOneCondition_*)."""
+        n = A.shape[0]
+        out = ctypes.c_double()
+        self._bind()
+        self._rc(getattr(self.lib, f"ElGBOneCondition_{_DT[A.dtype]}")(
+            self.h, n, _ptr(A), _ld(A), nb, ctypes.byref(out)), "OneCondition")
+        return out.value
+
     def lu_solve_after(self, A, piv, B, orientation=0):
         n = A.shape[0]
         self._bind()

@@ -110,6 +110,17 @@ ElError ElSolveAfterLUPartialPiv_d(ElOrientation orientation,
                                    ElConstMatrix_d A, ElConstPermutation P,
                                    ElMatrix_d B);
 
+/* LU without pivoting (include/El/lapack_like/factor.h:467-468) */
+ElError ElLU_s(ElMatrix_s A);
+ElError ElLU_d(ElMatrix_d A);
+
+/* Inverse (include/El/lapack_like/funcs.h:99-100) and the 1-norm condition
+ * number (include/El/lapack_like/props.h:81-82) */
+ElError ElInverse_s(ElMatrix_s A);
+ElError ElInverse_d(ElMatrix_d A);
+ElError ElOneCondition_s(ElConstMatrix_s A, float* cond);
+ElError ElOneCondition_d(ElConstMatrix_d A, double* cond);
+
 /* Cholesky (include/El/lapack_like/factor.h:24-41) */
 ElError ElCholesky_s(ElUpperOrLower uplo, ElMatrix_s A);
 ElError ElCholesky_d(ElUpperOrLower uplo, ElMatrix_d A);

@@ -6,6 +6,9 @@
  *   El::Matrix<T>            include/El/core/Matrix/decl.hpp:17-241
  *   El::Permutation          include/El/core/Permutation.hpp:14-126
  *   El::LU(A, P)             include/El/lapack_like/factor.hpp:376
+ *   El::LU(A) (no pivoting)  include/El/lapack_like/factor.hpp:367
+ *   El::Inverse(A)           include/El/lapack_like/funcs.hpp:68
+ *   El::OneCondition(A)      include/El/lapack_like/props.hpp:37
  *   El::lu::SolveAfter       include/El/lapack_like/factor.hpp:434
  *   El::Cholesky(uplo, A)    include/El/lapack_like/factor.hpp:22
  *   El::cholesky::SolveAfter include/El/lapack_like/factor.hpp:63
@@ -120,6 +123,19 @@ void PopBlocksizeStack();
 
 template <typename F>
 void LU(Matrix<F>& A, Permutation& P);
+
+// LU without pivoting; throws SingularMatrixException at an exact zero pivot.
+template <typename F>
+void LU(Matrix<F>& A);
+
+// A := inv(A) (LU with partial pivoting); SingularMatrixException at an exact
+// zero pivot, LogicError for a non-square A.
+template <typename F>
+void Inverse(Matrix<F>& A);
+
+// ||A||_1 ||inv(A)||_1; +infinity for a singular A.
+template <typename F>
+F OneCondition(const Matrix<F>& A);
 
 namespace lu {
 template <typename F>

@@ -308,6 +308,29 @@ int ElGBSolveAfterCholesky_s(ElGBContext ctx, int uplo, int n,
                              const float* A, int lda, int nrhs, float* B,
                              int ldb);
 
+/* El::LU(A) without pivoting (reference src/lapack_like/factor/LU.cpp:21-44,
+ * lu::Unb LU/Local.hpp:42-61): packed unit-L \ U in place; a zero pivot
+ * sets info (the reference throws SingularMatrixException).  Replaces
+ * ElLU_d / ElLU_s (include/El/lapack_like/factor.h:467-468). */
+int ElGBLUNoPiv_d(ElGBContext ctx, int m, int n, double* A, int lda, int nb);
+int ElGBLUNoPiv_s(ElGBContext ctx, int m, int n, float* A, int lda, int nb);
+
+/* El::Inverse(A) (reference src/lapack_like/funcs/Inverse/General.cpp:15-20 ->
+ * General/LUPartialPiv.hpp:21-74): A := inv(A) in place via LU with partial
+ * pivoting; a zero pivot sets info (SingularMatrixException).  Replaces
+ * ElInverse_d / ElInverse_s (include/El/lapack_like/funcs.h:99-100). */
+int ElGBInverse_d(ElGBContext ctx, int n, double* A, int lda, int nb);
+int ElGBInverse_s(ElGBContext ctx, int n, float* A, int lda, int nb);
+
+/* El::OneCondition(A) (reference src/lapack_like/props/Condition/One.cpp:12-24):
+ * ||A||_1 ||inv(A)||_1 on a copy (A untouched), +inf when A is singular
+ * (not an error).  Synchronizes.  Replaces ElOneCondition_d / _s
+ * (include/El/lapack_like/props.h:81-82). */
+int ElGBOneCondition_d(ElGBContext ctx, int n, const double* A, int lda, int nb,
+                       double* cond);
+int ElGBOneCondition_s(ElGBContext ctx, int n, const float* A, int lda, int nb,
+                       double* cond);
+
 /* El::LinearSolve(A, B) (reference src/lapack_like/solve/Linear.cpp:212-218):
  * A is left untouched (the reference copies it); B is overwritten by X.
  * Gaussian elimination on [A | B] as RowEchelon (Linear.cpp:30-77), then

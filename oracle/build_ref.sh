@@ -1,7 +1,8 @@
 #!/usr/bin/env bash
 # Builds the reference's OWN sequential factor-and-solve path (Elemental
-# El::LU / lu::SolveAfter / El::Cholesky / cholesky::SolveAfter /
-# El::LinearSolve / El::HPDSolve) from its sources, in place, into
+# El::LU with and without pivoting / lu::SolveAfter / El::Cholesky /
+# cholesky::SolveAfter / El::LinearSolve / El::HPDSolve / El::Inverse /
+# El::OneCondition) from its sources, in place, into
 # oracle/_ref/elref.  Test infrastructure only: the product never links it.
 #
 # Nothing is copied out of the reference tree.  The recipe:
@@ -11,7 +12,9 @@
 #   2. the single-rank stub <mpi.h> in oracle/stub/;
 #   3. g++ on the reference's own translation units under src/core,
 #      src/blas_like, src/lapack_like/{perm,props}, src/matrices, plus
-#      LU.cpp, Cholesky.cpp, Linear.cpp, HPD.cpp;
+#      LU.cpp, Cholesky.cpp, Linear.cpp, HPD.cpp and the general and
+#      triangular Inverse (funcs/Inverse/{General,Triangular}.cpp, which
+#      OneCondition in props calls);
 #   4. the BLAS names Elemental calls (bare, e.g. `dgemm`; no-suffix mangling
 #      include/El/core/imports/blas.hpp:29-41) renamed in the objects to the
 #      symbols of SciPy's bundled OpenBLAS (`scipy_dgemm_`), which is linked;
@@ -56,7 +59,9 @@ TUS=$(cd "$REF" && { find src/core src/blas_like src/lapack_like/perm \
       echo src/lapack_like/factor/LU.cpp;
       echo src/lapack_like/factor/Cholesky.cpp;
       echo src/lapack_like/solve/Linear.cpp;
-      echo src/lapack_like/solve/HPD.cpp; } | sort)
+      echo src/lapack_like/solve/HPD.cpp;
+      echo src/lapack_like/funcs/Inverse/General.cpp;
+      echo src/lapack_like/funcs/Inverse/Triangular.cpp; } | sort)
 CXXFLAGS="-std=c++14 -O2 -fPIC -w -I$OUT/include -I$HERE/stub -I$REF/include
  -I$REF/external/suite_sparse/include -I$REF/external/pmrrr/include"
 export REF OUT CXXFLAGS

@@ -8,7 +8,10 @@ Python access to the CPU checker for the dense factor-and-solve path:
   (built here by :func:`build`, loaded by :func:`lib`);
 * ``_ref/elref`` — the reference's own code compiled from its sources by
   ``build_ref.sh`` (only where the reference tree is present);
-* numpy restatements of the added forms' semantics (refinement loop of
+* numpy restatements of El::LU without pivoting, El::Inverse and
+  El::OneCondition (block-level, the same steps as the reference; pinned to
+  the reference's outputs within rounding by tests/test_oracle_golden.py)
+  and of the added forms' semantics (refinement loop of
   include/El/lapack_like/solve/Refined.hpp:44-119 and the MLP).
 
 Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg may
@@ -199,6 +202,86 @@ def hpd_solve(A, B, uplo: str = "L", nb: int = 128, dtype=np.float64):
 # ---------------------------------------------------------------------------
 # the reference itself (only where oracle/_ref/elref was built)
 # ---------------------------------------------------------------------------
+def lu_nopiv(A, nb: int = 128, dtype=np.float64):
+    """El::LU(A) without pivoting (src/lapack_like/factor/LU.cpp:21-44): per
+    nb-block, lu::Unb on the diagonal block (LU/Local.hpp:42-61: scale by
+    1/alpha and a rank-1 update per column; an exact zero pivot raises
+    OracleError(3), the reference's SingularMatrixException), then
+    Trsm(RIGHT, UPPER, NORMAL, NON_UNIT) on A21, Trsm(LEFT, LOWER, NORMAL,
+    UNIT) on A12 and Gemm(-1) on A22."""
+    from scipy.linalg import solve_triangular
+
+    W = np.array(A, dtype=dtype, order="F")
+    m, n = W.shape
+    mn = min(m, n)
+    for k in range(0, mn, nb):
+        b = min(nb, mn - k)
+        A11 = W[k:k + b, k:k + b]
+        for j in range(b):
+            alpha = A11[j, j]
+            if alpha == 0:
+                raise OracleError(3)
+            A11[j + 1:, j] *= dtype(1) / alpha
+            A11[j + 1:, j + 1:] -= np.outer(A11[j + 1:, j], A11[j, j + 1:])
+        if k + b < m:
+            W[k + b:, k:k + b] = solve_triangular(np.triu(A11).T, W[k + b:, k:k + b].T,
+                                                  lower=True).T
+        if k + b < n:
+            W[k:k + b, k + b:] = solve_triangular(A11, W[k:k + b, k + b:], lower=True,
+                                                  unit_diagonal=True)
+        if k + b < m and k + b < n:
+            W[k + b:, k + b:] -= W[k + b:, k:k + b] @ W[k:k + b, k + b:]
+    return W
+
+
+def inverse(A, nb: int = 128, dtype=np.float64):
+    """El::Inverse(A) (src/lapack_like/funcs/Inverse/General/LUPartialPiv.hpp:
+    21-74): El::LU(A, P) (the C restatement above), TriangularInverse(UPPER,
+    NON_UNIT) on U, then from the last nb-block backwards: copy out L11 and
+    L21, zero the strictly lower part of the block column A1, A1 -= A2 L21,
+    A1 := A1 inv(L11) (Trsm RIGHT, LOWER, NORMAL, UNIT); finally
+    inv(A) := inv(A) P, the swap sequence replayed backwards on the columns
+    (InversePermuteCols).  A zero pivot raises OracleError(3)."""
+    from scipy.linalg import solve_triangular
+
+    W, piv = lu(A, nb, dtype)
+    n = W.shape[0]
+    if W.shape[1] != n:
+        raise OracleError(2)
+    eye = np.eye(n, dtype=dtype)
+    W = np.asfortranarray(np.triu(solve_triangular(np.triu(W), eye, lower=False))
+                          + np.tril(W, -1))
+    for k in range(((n - 1) // nb) * nb if n else -1, -1, -nb):
+        b = min(nb, n - k)
+        L11 = np.tril(W[k:k + b, k:k + b], -1) + np.eye(b, dtype=dtype)
+        L21 = W[k + b:, k:k + b].copy()
+        W[k:k + b, k:k + b] = np.triu(W[k:k + b, k:k + b])
+        W[k + b:, k:k + b] = 0
+        if k + b < n:
+            W[:, k:k + b] -= W[:, k + b:] @ L21
+        W[:, k:k + b] = solve_triangular(L11.T, W[:, k:k + b].T, lower=False,
+                                         unit_diagonal=True).T
+    for i in range(len(piv) - 1, -1, -1):
+        p = int(piv[i])
+        if p != i:
+            W[:, [i, p]] = W[:, [p, i]]
+    return W
+
+
+def one_condition(A, nb: int = 128, dtype=np.float64):
+    """El::OneCondition(A) (src/lapack_like/props/Condition/One.cpp:12-24):
+    OneNorm(A) * OneNorm(inv(A)), +inf when the inverse hits a zero pivot."""
+    A = np.asarray(A, dtype=dtype)
+    n1 = float(np.abs(A).sum(axis=0).max()) if A.size else 0.0
+    try:
+        X = inverse(A, nb, dtype)
+    except OracleError as e:
+        if e.status == 3:
+            return float("inf")
+        raise
+    return n1 * float(np.abs(X).sum(axis=0).max()) if X.size else 0.0
+
+
 def have_reference() -> bool:
     return os.path.exists(REF_EXE)
 

@@ -15,6 +15,9 @@
 //   elref <d|s> cholsolve <nb> <L|U> A B C X
 //   elref <d|s> linsolve  <nb> A B X
 //   elref <d|s> hpdsolve  <nb> <L|U> A B X
+//   elref <d|s> lunopiv   <nb> A LU         (El::LU without pivoting)
+//   elref <d|s> inverse   <nb> A Ainv       (El::Inverse)
+//   elref <d|s> onecond   <nb> A cond       (El::OneCondition, a 1 x 1 matrix)
 //   elref <d|s> lutime    <nb> A reps       (prints seconds per El::LU)
 // Exit status: 0 ok, 3 SingularMatrixException, 4 NonHPDMatrixException,
 // 2 usage / IO error.
@@ -106,6 +109,22 @@ int Run(int argc, char** argv) {
     if (!ReadMatrix(argv[5], A) || !ReadMatrix(argv[6], B)) return 2;
     El::HPDSolve(Uplo(argv[4]), El::NORMAL, A, B);
     return WriteMatrix(argv[7], B) ? 0 : 2;
+  }
+  if (op == "lunopiv" && argc == 6) {
+    if (!ReadMatrix(argv[4], A)) return 2;
+    El::LU(A);
+    return WriteMatrix(argv[5], A) ? 0 : 2;
+  }
+  if (op == "inverse" && argc == 6) {
+    if (!ReadMatrix(argv[4], A)) return 2;
+    El::Inverse(A);
+    return WriteMatrix(argv[5], A) ? 0 : 2;
+  }
+  if (op == "onecond" && argc == 6) {
+    if (!ReadMatrix(argv[4], A)) return 2;
+    El::Matrix<T> c(1, 1);
+    c(0, 0) = El::OneCondition(A);
+    return WriteMatrix(argv[5], c) ? 0 : 2;
   }
   if (op == "lutime" && argc == 6) {
     El::Matrix<T> A0;

@@ -1,10 +1,11 @@
 """Generates the golden fixtures in this folder by running the REFERENCE's own
-sequential path (Elemental's El::LU, lu::SolveAfter, El::Cholesky,
-cholesky::SolveAfter, El::LinearSolve, El::HPDSolve), compiled from its
+sequential path (Elemental's El::LU with and without pivoting,
+lu::SolveAfter, El::Cholesky, cholesky::SolveAfter, El::LinearSolve,
+El::HPDSolve, El::Inverse, El::OneCondition), compiled from its
 sources into oracle/_ref/elref by oracle/build_ref.sh.
 
 Run (where the reference tree is present):
-    oracle/build_ref.sh && python tests/golden/gen_golden.py
+    oracle/build_ref.sh && python tests/golden/gen_golden.py [name-prefix ...]
 
 Each fixture is an .npz with the inputs (or, for the large config-1 case, the
 seed plus a SHA-256 of the regenerated input), the blocksize, the
@@ -33,6 +34,9 @@ def sha(a):
 
 
 def save(name, **kw):
+    # optional arguments: only fixtures whose names start with one of them
+    if len(sys.argv) > 1 and not any(name.startswith(p) for p in sys.argv[1:]):
+        return
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **kw)
     print("wrote", name)
 
@@ -94,6 +98,45 @@ def main():
     B = mats.gaussian(120, 5, s + 501)
     st, out = O.ref_run("linsolve", nb=32, inputs=[A, B], out_dtypes=[F64])
     save("linsolve_120_nb32", op="linsolve", nb=32, status=st, A=A, B=B, X=out[0])
+
+    # El::LU without pivoting (src/lapack_like/factor/LU.cpp:21-44): square,
+    # wide and tall, diagonally dominant (stable without pivoting), and an
+    # exact zero pivot (lu::Unb throws SingularMatrixException)
+    D = mats.gaussian(100, 100, s + 600) + 100.0 * np.eye(100)
+    for name, M in (("lunopiv_100_nb32", D),
+                    ("lunopiv_90x130_nb32", mats.gaussian(90, 130, s + 601)
+                     + np.hstack([90.0 * np.eye(90), np.zeros((90, 40))])),
+                    ("lunopiv_130x90_nb32", mats.gaussian(130, 90, s + 602)
+                     + np.vstack([90.0 * np.eye(90), np.zeros((40, 90))]))):
+        st, out = O.ref_run("lunopiv", nb=32, inputs=[M], out_dtypes=[F64])
+        save(name, op="lunopiv", nb=32, status=st, A=M, LU=out[0])
+    Zp = D.copy()
+    Zp[40, 40] = 0.0
+    Zp[40, :] = 0.0
+    st, _ = O.ref_run("lunopiv", nb=32, inputs=[Zp], out_dtypes=[F64])
+    save("lunopiv_singular_100_nb32", op="lunopiv", nb=32, status=st, A=Zp)
+
+    # El::Inverse (funcs/Inverse/General/LUPartialPiv.hpp: LU, TriangularInverse,
+    # the backward sweep against L, InversePermuteCols) and El::OneCondition
+    # (props/Condition/One.cpp: ||A||_1 ||inv(A)||_1, +inf when singular)
+    for name, M, nb in (("inverse_100_nb32", mats.gaussian(100, 100, s + 610), 32),
+                        ("inverse_129_nb96", mats.gaussian(129, 129, s + 611), 96),
+                        ("inverse_haar_k1e6_80_nb16", mats.conditioned(80, 1e6, s + 612), 16)):
+        st, out = O.ref_run("inverse", nb=nb, inputs=[M], out_dtypes=[F64])
+        save(name, op="inverse", nb=nb, status=st, A=M, Ainv=out[0])
+    M = mats.gaussian(64, 64, s + 613)
+    st, out = O.ref_run("inverse", nb=32, dtype=np.float32, inputs=[M], out_dtypes=[np.float32])
+    save("inverse_s_64_nb32", op="inverse", nb=32, status=st, dtype="float32",
+         A=M.astype(np.float32), Ainv=out[0])
+    Zi = mats.gaussian(50, 50, s + 614)
+    Zi[:, 7] = 0.0
+    st, _ = O.ref_run("inverse", nb=16, inputs=[Zi], out_dtypes=[F64])
+    save("inverse_singular_50_nb16", op="inverse", nb=16, status=st, A=Zi)
+    for name, M in (("onecond_haar_k1e4_80", mats.conditioned(80, 1e4, s + 620)),
+                    ("onecond_gauss_120", mats.gaussian(120, 120, s + 621)),
+                    ("onecond_singular_50", Zi)):
+        st, out = O.ref_run("onecond", nb=32, inputs=[M], out_dtypes=[F64])
+        save(name, op="onecond", nb=32, status=st, A=M, cond=out[0].ravel()[0])
 
     # Config 1: n = 1024, 1 RHS, iid N(0,1), nb = 128 (the default blocksize)
     n = 1024

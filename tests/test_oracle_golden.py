@@ -1,7 +1,9 @@
-"""The CPU oracle (oracle/el_oracle.c) against golden fixtures produced by the
-reference itself (tests/golden/gen_golden.py).  Pivots must match exactly;
-values match bit-for-bit on the BLAS the fixtures were made with and to
-rounding on any other BLAS build."""
+"""The CPU oracle (oracle/el_oracle.c, and the numpy restatements of LU
+without pivoting, Inverse and OneCondition in oracle/oracle.py) against
+golden fixtures produced by the reference itself (tests/golden/gen_golden.py).
+Pivots must match exactly; values of the C restatement match bit-for-bit on
+the BLAS the fixtures were made with and to rounding on any other BLAS build;
+the numpy restatements match to rounding."""
 import glob
 import hashlib
 import os
@@ -68,6 +70,26 @@ def test_oracle_matches_reference_fixture(path):
         close(O.hpd_solve(g["A"], g["B"], str(g["uplo"]), nb=nb), g["X"])
     elif op == "linsolve":
         close(O.linear_solve(g["A"], g["B"], nb=nb), g["X"])
+    elif op in ("lunopiv", "inverse"):
+        dt = np.float32 if str(g.get("dtype", "float64")) == "float32" else np.float64
+        fn = O.lu_nopiv if op == "lunopiv" else O.inverse
+        if st != 0:  # SingularMatrixException in the reference
+            with pytest.raises(O.OracleError) as e:
+                fn(g["A"], nb=nb, dtype=dt)
+            assert e.value.status == st
+            return
+        X = fn(g["A"], nb=nb, dtype=dt)
+        ref = g["LU"] if op == "lunopiv" else g["Ainv"]
+        # a block-level numpy restatement: equal to rounding, relative to
+        # the result's size (the inverse of a kappa = 1e6 matrix included)
+        tol = (1e-5 if dt == np.float32 else 1e-13) * np.abs(ref).max()
+        assert np.abs(X - ref).max() <= tol, np.abs(X - ref).max()
+    elif op == "onecond":
+        c, ref = O.one_condition(g["A"], nb=nb), float(g["cond"])
+        if np.isinf(ref):
+            assert np.isinf(c)
+        else:
+            assert abs(c - ref) <= 1e-12 * ref, (c, ref)
     else:
         pytest.fail(op)
 
