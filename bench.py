@@ -14,6 +14,11 @@ lu::SolveAfter over OpenBLAS, all host threads) on a bounded sample.
   e2e    the same solve through the Elemental-style C ABI on pinned host
          buffers (ElLinearSolveMixed_d): H2D of A and B, D2H of X per step
 
+Other workloads (`--workload`): `batched` (4096 uneven LU / Cholesky systems
+in one persistent launch), `selector` (10,000 conditioned systems through the
+learned precision selector), `inverse` (El::Inverse and El::OneCondition of
+one n = 8192 FP64 matrix).
+
 `--impl reference` times the CPU reference arm alone.  Under torchrun each
 rank solves its own system (replicas; the factorization does not shard).
 """
@@ -45,7 +50,8 @@ def parse():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--n", type=int, default=32768)
+    p.add_argument("--n", type=int, default=None,
+                   help="matrix size (default 32768 for lu-ir, 8192 for inverse)")
     p.add_argument("--nrhs", type=int, default=16)
     p.add_argument("--precision", default="fp32",
                    choices=["fp32", "tf32", "bf16", "fp8", "fp64"])
@@ -56,10 +62,12 @@ def parse():
     p.add_argument("--cpu-baseline", default="on", choices=["on", "off"])
     p.add_argument("--cpu-n", type=int, default=8192)
     p.add_argument("--seed", type=int, default=20261204 + 1)
-    p.add_argument("--workload", default="lu-ir", choices=["lu-ir", "batched", "selector"],
+    p.add_argument("--workload", default="lu-ir",
+                   choices=["lu-ir", "batched", "selector", "inverse"],
                    help="lu-ir: one large mixed-precision solve (default); batched: 4096 "
                         "uneven LU/Cholesky systems in one launch; selector: 10,000 "
-                        "conditioned systems through the learned precision selector")
+                        "conditioned systems through the learned precision selector; "
+                        "inverse: El::Inverse and El::OneCondition of one FP64 matrix")
     p.add_argument("--count", type=int, default=0, help="systems (batched / selector)")
     p.add_argument("--train-count", type=int, default=3000, help="selector training systems")
     return p.parse_args()
@@ -702,8 +710,131 @@ def selector_arm(args, rank, world, local_rank):
     return 0
 
 
+# ---------------------------------------------------------------------------
+# El::Inverse / El::OneCondition of one FP64 matrix
+# ---------------------------------------------------------------------------
+def inverse_arm(args, rank, world, local_rank):
+    import numpy as np
+
+    import elemental_gb300 as El
+    from elemental_gb300 import device as D
+
+    import torch
+
+    dist, barrier, tmax_of = _dist_setup(world, local_rank)
+    ctx = D.context(local_rank)
+    n = args.n
+    g = torch.Generator(device="cuda")
+    g.manual_seed(args.seed + 7919 * rank)
+    A0 = D.colmajor(n, n)
+    A0.copy_(torch.randn(n, n, generator=g, device="cuda", dtype=torch.float64).t())
+    A = D.colmajor(n, n)
+    flops = 2.0 * n ** 3  # LAPACK's count for an inverse (getrf + getri)
+
+    def step():
+        A.copy_(A0)
+        ctx.inverse(A)
+
+    for _ in range(max(args.warmup, 0)):
+        step()
+    barrier()
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    l0 = ctx.launches()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    e1.synchronize()
+    barrier()
+    launches = ctx.launches() - l0
+    clk = clocks.stop()
+    t = tmax_of(e0.elapsed_time(e1) / 1e3)
+    info = ctx.status()
+    X = A.cpu().numpy()
+    Ah = A0.cpu().numpy()
+    resid = float(np.linalg.norm(Ah @ X - np.eye(n)) /
+                  (np.linalg.norm(Ah) * np.linalg.norm(X)))
+    # OneCondition: wall clock (it synchronizes to read the norms)
+    ctx.one_condition(A0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    cond = ctx.one_condition(A0)
+    t_cond = time.perf_counter() - t0
+    # end to end through Elemental's C ABI on pinned host memory
+    e2e = None
+    if args.e2e == "on":
+        Hp = torch.empty((n, n), dtype=torch.float64, pin_memory=True)
+        H0 = torch.empty((n, n), dtype=torch.float64, pin_memory=True)
+        H0.copy_(A0.t())
+        Hp.copy_(H0)
+        M = El.Matrix(Hp.numpy().T)
+        El.Inverse(M)
+        te = 0.0
+        for _ in range(args.steps):
+            Hp.copy_(H0)
+            t0 = time.perf_counter()
+            El.Inverse(M)
+            te += time.perf_counter() - t0
+        e2e = {"value": args.steps * world / tmax_of(te), "unit": "inverses/s",
+               "h2d_bytes_per_step": 8 * n * n, "d2h_bytes_per_step": 8 * n * n,
+               "api": "ElInverse_d (El::Matrix handle on pinned host memory)",
+               "max_abs_diff_vs_device_run": float(np.abs(M.array - X).max())}
+        del M, Hp, H0
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return 0
+    cpu = None
+    if args.cpu_baseline == "on":
+        from oracle import oracle as O
+
+        ns = min(2048, n)
+        threads = os.cpu_count() or 1
+        O.set_threads(threads)
+        As = np.random.default_rng(args.seed).standard_normal((ns, ns))
+        O.inverse(As, nb=128)
+        t0 = time.perf_counter()
+        O.inverse(As, nb=128)
+        tc = time.perf_counter() - t0
+        cpu = {"value": (ns / n) ** 3 / tc, "unit": "inverses/s", "cores": threads,
+               "kind": "port",
+               "sample": f"El::Inverse restatement (El::LU + TriangularInverse + the backward "
+                         f"sweep, OpenBLAS) at n={ns}, {threads} threads: {tc:.3f} s, scaled "
+                         f"to n={n} by n^3"}
+    value = args.steps * world / t
+    fp64_peak = ctx.fp64_peak_tflops()
+    line = {
+        "metric": METRIC, "value": value, "unit": "inverses/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: seeded iid N(0,1) FP64 (device Philox generator)",
+        "config": {"workload": f"El::Inverse of one n={n} FP64 matrix (getrf + getrs on the "
+                               f"identity), N(0,1); El::OneCondition of the same matrix",
+                   "n": n, "l2": "inputs larger than L2" if 8 * n * n > 129e6 else "in L2",
+                   "parallelism": f"replicas x{world}"},
+        "tflops_eq": flops * value / world / 1e12,
+        "residual_AX_minus_I": resid, "status": info,
+        "one_condition": {"value": cond, "seconds": t_cond},
+        "roofline": {"bound": "fp64 FMA pipe (tcgen05 has no FP64 kind)",
+                     "achieved": flops * value / world / 1e12, "peak": fp64_peak,
+                     "unit": "TFLOP/s", "frac": flops * value / world / 1e12 / fp64_peak,
+                     "peak_source": "FP64 FMA throughput probe (ElGBProbeFP64Peak) on this GPU",
+                     "traffic": None},
+        "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": launches, "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
 def main():
     args = parse()
+    if args.n is None:
+        args.n = 8192 if args.workload == "inverse" else 32768
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
@@ -713,6 +844,8 @@ def main():
         return batched_arm(args, rank, world, local_rank)
     if args.workload == "selector":
         return selector_arm(args, rank, world, local_rank)
+    if args.workload == "inverse":
+        return inverse_arm(args, rank, world, local_rank)
     return gpu_arm(args, rank, world, local_rank)
 
 

@@ -554,6 +554,46 @@ static cudaError_t trsv_any(Context* ctx, bool lower_of_A, bool trans, bool unit
   return cudaSuccess;
 }
 
+// op(A) X = W for many right-hand sides, A's lower (unit) or upper
+// (non-unit) triangle: 128-row blocks, each a triangular block solve
+// (trsm_block_kernel) followed by one GEMM update of the rows still to be
+// solved -- level-3 work, where the 16-column TRSV passes of trsv_any would
+// re-read A once per 16 columns with ~100 launches each.  The GEMMs run on
+// the CUDA cores (FP64 DFMA / FP32 FFMA), as the reference's dtrsm does.
+template <typename T>
+static cudaError_t trsm_many(Context* ctx, bool lower, bool unit, int n, const T* A, long lda,
+                             T* W, long ldw, int nrhs) {
+  LuLane L;
+  L.st = ctx->stream;
+  if (lower) {
+    for (int i0 = 0; i0 < n; i0 += 128) {
+      const int ib = std::min(128, n - i0);
+      ELGB_CHECK(launch_trsm_block<T>(A + i0 + (long)i0 * lda, lda, W + i0, ldw, ib, nrhs, true,
+                                      unit, false, false, ctx->stream),
+                 1);
+      const int rest = n - i0 - ib;
+      if (rest > 0) {
+        cudaError_t e = gemm_sub(ctx, L, rest, nrhs, ib, A + (i0 + ib) + (long)i0 * lda, lda,
+                                 W + i0, ldw, W + i0 + ib, ldw);
+        if (e != cudaSuccess) return e;
+      }
+    }
+  } else {
+    for (int i0 = ((n - 1) / 128) * 128; i0 >= 0; i0 -= 128) {
+      const int ib = std::min(128, n - i0);
+      ELGB_CHECK(launch_trsm_block<T>(A + i0 + (long)i0 * lda, lda, W + i0, ldw, ib, nrhs, false,
+                                      unit, false, false, ctx->stream),
+                 1);
+      if (i0 > 0) {
+        cudaError_t e = gemm_sub(ctx, L, i0, nrhs, ib, A + (long)i0 * lda, lda, W + i0, ldw, W,
+                                 ldw);
+        if (e != cudaSuccess) return e;
+      }
+    }
+  }
+  return cudaSuccess;
+}
+
 // lu::SolveAfter (src/lapack_like/factor/LU/SolveAfter.hpp:66-92).
 template <typename T>
 cudaError_t getrs(Context* ctx, int orient, int n, const T* A, long lda, const int* ipiv,
@@ -574,10 +614,17 @@ cudaError_t getrs(Context* ctx, int orient, int n, const T* A, long lda, const i
   }
   if (orient == 0) {
     ELGB_CHECK(launch_permute_rows<T>(B, ldb, W, n, n, nrhs, perm, false, ctx->stream), 1);
-    e = trsv_any<T>(ctx, true, false, true, n, A, lda, W, n, nrhs);
-    if (e != cudaSuccess) return e;
-    e = trsv_any<T>(ctx, false, false, false, n, A, lda, W, n, nrhs);
-    if (e != cudaSuccess) return e;
+    if (nrhs > 64) {  // many right-hand sides (e.g. El::Inverse's identity)
+      e = trsm_many<T>(ctx, true, true, n, A, lda, W, n, nrhs);
+      if (e != cudaSuccess) return e;
+      e = trsm_many<T>(ctx, false, false, n, A, lda, W, n, nrhs);
+      if (e != cudaSuccess) return e;
+    } else {
+      e = trsv_any<T>(ctx, true, false, true, n, A, lda, W, n, nrhs);
+      if (e != cudaSuccess) return e;
+      e = trsv_any<T>(ctx, false, false, false, n, A, lda, W, n, nrhs);
+      if (e != cudaSuccess) return e;
+    }
     e = cudaMemcpy2DAsync(B, ldb * sizeof(T), W, (size_t)n * sizeof(T), (size_t)n * sizeof(T),
                           nrhs, cudaMemcpyDeviceToDevice, ctx->stream);
     if (e != cudaSuccess) return e;
