@@ -22,6 +22,9 @@ from . import _lib
 # Enumerations (include/El/core/types.h:211-228)
 NORMAL, TRANSPOSE, ADJOINT = 0, 1, 2
 LOWER, UPPER = 0, 1
+# Matrix file formats (python/core/environment.py, include/El/core/types.h:237-251)
+(AUTO, ASCII, ASCII_MATLAB, BINARY, BINARY_FLAT, BMP, JPG, JPEG, MATRIX_MARKET, PNG, PPM, XBM,
+ XPM) = range(13)
 # LU pivot types (python/lapack_like/factor.py:493)
 LU_PARTIAL, LU_FULL, LU_ROOK, LU_WITHOUT_PIVOTING = 0, 1, 2, 3
 
@@ -180,6 +183,45 @@ def Cholesky(uplo, A: Matrix):
 def SolveAfterCholesky(uplo, orient, A: Matrix, B: Matrix):
     _check(getattr(A.lib, f"ElSolveAfterCholesky_{A.tag}")(uplo, orient, A.obj, B.obj),
            "SolveAfterCholesky")
+
+
+def Read(A: Matrix, filename, fileFormat=AUTO, sequential=False):
+    """El.Read(A, filename, fileFormat) (python/io.py:377-): BINARY (.bin) or
+    BINARY_FLAT (.dat, into A's current shape); A is resized to the file's
+    matrix and its numpy array replaced by the data read.  `sequential`
+    concerns distributed matrices only and is ignored."""
+    lib, t = A.lib, A.tag
+    # A's C++ matrix views the numpy array (it cannot be resized), so the
+    # file is read into an owned matrix first
+    tmp = ctypes.c_void_p()
+    _check(getattr(lib, f"ElMatrixCreate_{t}")(ctypes.byref(tmp)), "Create")
+    try:
+        _check(getattr(lib, f"ElMatrixResize_{t}")(tmp, A.Height(), A.Width()), "Resize")
+        _check(getattr(lib, f"ElRead_{t}")(tmp, str(filename).encode(), int(fileFormat)), "Read")
+        h, w, ld, buf = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_void_p()
+        getattr(lib, f"ElMatrixHeight_{t}")(tmp, ctypes.byref(h))
+        getattr(lib, f"ElMatrixWidth_{t}")(tmp, ctypes.byref(w))
+        getattr(lib, f"ElMatrixLDim_{t}")(tmp, ctypes.byref(ld))
+        getattr(lib, f"ElMatrixBuffer_{t}")(tmp, ctypes.byref(buf))
+        dt = A.array.dtype
+        arr = np.empty((h.value, w.value), dtype=dt, order="F")
+        if arr.size:
+            ptr = ctypes.cast(buf, ctypes.POINTER(np.ctypeslib.as_ctypes_type(dt)))
+            raw = np.ctypeslib.as_array(ptr, shape=(w.value * ld.value,))
+            arr[:] = raw.reshape(w.value, ld.value)[:, : h.value].T
+    finally:
+        getattr(lib, f"ElMatrixDestroy_{t}")(tmp)
+    A.array = arr
+    _check(getattr(A.lib, f"ElMatrixAttach_{A.tag}")(
+        A.obj, h.value, w.value, arr.ctypes.data_as(ctypes.c_void_p), max(h.value, 1)),
+        "Attach")
+
+
+def Write(A: Matrix, basename="matrix", fileFormat=BINARY, title=""):
+    """El.Write(A, basename, fileFormat, title) (python/io.py:424-): writes
+    basename.bin (BINARY) or basename.dat (BINARY_FLAT)."""
+    _check(getattr(A.lib, f"ElWrite_{A.tag}")(A.obj, str(basename).encode(), int(fileFormat),
+                                              str(title).encode()), "Write")
 
 
 def Inverse(A: Matrix):

@@ -124,6 +124,8 @@ def load():
         _sig(lib, f"ElMatrixLockedAttach_{s}", c_int, vp, c_int, c_int, vp, c_int)
         _sig(lib, f"ElMatrixResize_{s}", c_int, vp, c_int, c_int)
         _sig(lib, f"ElMatrixHeight_{s}", c_int, vp, P(c_int))
+        _sig(lib, f"ElRead_{s}", c_int, vp, ctypes.c_char_p, c_int)
+        _sig(lib, f"ElWrite_{s}", c_int, vp, ctypes.c_char_p, c_int, ctypes.c_char_p)
         _sig(lib, f"ElMatrixWidth_{s}", c_int, vp, P(c_int))
         _sig(lib, f"ElMatrixLDim_{s}", c_int, vp, P(c_int))
         _sig(lib, f"ElMatrixBuffer_{s}", c_int, vp, P(vp))

@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <fstream>
 #include <mutex>
 #include <new>
 #include <stdexcept>
@@ -570,6 +571,85 @@ void LinearSolveMixed(const Matrix<double>& A, Matrix<double>& B, const ElGBRefi
   Download(B, dX);
 }
 
+// ---- matrix files: src/io/File.cpp:28-70 (extensions, DetectFormat),
+// io/Write/Binary.hpp:17-37, io/Read/Binary.hpp:17-44, io/*/BinaryFlat.hpp ----
+namespace {
+const char* kExtensions[FileFormat_MAX] = {"",   "txt",  "m",  "bin", "dat", "bmp", "jpg",
+                                           "jpeg", "mm", "png", "ppm", "xbm", "xpm"};
+
+FileFormat DetectFormat(const std::string& filename) {
+  const std::string ext = filename.substr(filename.find_last_of('.') + 1);
+  for (int f = 1; f < FileFormat_MAX; ++f)
+    if (ext == kExtensions[f]) return static_cast<FileFormat>(f);
+  throw std::runtime_error("Did not detect file format");
+}
+
+long FileBytes(std::ifstream& f) {
+  const auto pos = f.tellg();
+  f.seekg(0, std::ios::end);
+  const long bytes = static_cast<long>(f.tellg());
+  f.seekg(pos);
+  return bytes;
+}
+}  // namespace
+
+template <typename T>
+void Write(const Matrix<T>& A, const std::string& basename, FileFormat format,
+           const std::string& title) {
+  (void)title;  // the binary formats carry no title
+  if (format != BINARY && format != BINARY_FLAT)
+    throw std::logic_error("Format unsupported for writing a Matrix on this path");
+  const std::string filename = basename + "." + kExtensions[format];
+  std::ofstream f(filename, std::ios::binary);
+  if (!f.is_open()) throw std::runtime_error("Could not open " + filename);
+  if (format == BINARY) {
+    const Int hw[2] = {A.Height(), A.Width()};
+    f.write(reinterpret_cast<const char*>(hw), sizeof(hw));
+  }
+  for (Int j = 0; j < A.Width(); ++j)
+    f.write(reinterpret_cast<const char*>(A.LockedBuffer(0, j)),
+            static_cast<std::streamsize>(sizeof(T)) * A.Height());
+  if (!f) throw std::runtime_error("Could not write " + filename);
+}
+
+template <typename T>
+void Read(Matrix<T>& A, const std::string& filename, FileFormat format) {
+  if (format == AUTO) format = DetectFormat(filename);
+  if (format != BINARY && format != BINARY_FLAT)
+    throw std::logic_error("Format unsupported for reading a Matrix");
+  std::ifstream f(filename, std::ios::binary);
+  if (!f.is_open()) throw std::runtime_error("Could not open " + filename);
+  Int height = A.Height(), width = A.Width();  // BINARY_FLAT keeps A's shape
+  long meta = 0;
+  if (format == BINARY) {
+    Int hw[2] = {0, 0};
+    f.read(reinterpret_cast<char*>(hw), sizeof(hw));
+    if (!f) throw std::runtime_error("Could not read the size of " + filename);
+    height = hw[0];
+    width = hw[1];
+    meta = static_cast<long>(sizeof(hw));
+  }
+  if (height < 0 || width < 0) throw std::runtime_error("Invalid matrix size in " + filename);
+  const long expect = meta + static_cast<long>(sizeof(T)) * height * width;
+  if (FileBytes(f) != expect)
+    throw std::runtime_error("Expected file to be " + std::to_string(expect) + " bytes");
+  A.Resize(height, width);
+  for (Int j = 0; j < width; ++j)
+    f.read(reinterpret_cast<char*>(A.Buffer(0, j)),
+           static_cast<std::streamsize>(sizeof(T)) * height);
+  if (!f) throw std::runtime_error("Could not read " + filename);
+}
+
+template void Read<Int>(Matrix<Int>&, const std::string&, FileFormat);
+template void Read<float>(Matrix<float>&, const std::string&, FileFormat);
+template void Read<double>(Matrix<double>&, const std::string&, FileFormat);
+template void Write<Int>(const Matrix<Int>&, const std::string&, FileFormat,
+                         const std::string&);
+template void Write<float>(const Matrix<float>&, const std::string&, FileFormat,
+                           const std::string&);
+template void Write<double>(const Matrix<double>&, const std::string&, FileFormat,
+                            const std::string&);
+
 #define EL_GB_PROTO(F)                                                                  \
   template void LU<F>(Matrix<F>&, Permutation&);                                        \
   template void LU<F>(Matrix<F>&);                                                      \
@@ -724,6 +804,20 @@ ElError ElLUPartialPiv_s(ElMatrix_s A, ElPermutation P) { EL_GB_TRY(El::LU(*M<fl
 ElError ElLUPartialPiv_d(ElMatrix_d A, ElPermutation P) {
   EL_GB_TRY(El::LU(*M<double>(A), *PP(P)))
 }
+#define EL_GB_IO(S, T)                                                                    \
+  ElError ElRead_##S(ElMatrix_##S A, const char* filename, ElFileFormat format) {          \
+    if (!A || !filename) return EL_ARG_ERROR;                                              \
+    EL_GB_TRY(El::Read(*M<T>(A), filename, static_cast<El::FileFormat>(format)))          \
+  }                                                                                        \
+  ElError ElWrite_##S(ElConstMatrix_##S A, const char* basename, ElFileFormat format,      \
+                      const char* title) {                                                 \
+    if (!A || !basename) return EL_ARG_ERROR;                                              \
+    EL_GB_TRY(El::Write(*CM<T>(A), basename, static_cast<El::FileFormat>(format),          \
+                        title ? title : ""))                                               \
+  }
+EL_GB_IO(i, El::Int)
+EL_GB_IO(s, float)
+EL_GB_IO(d, double)
 ElError ElLU_s(ElMatrix_s A) { EL_GB_TRY(El::LU(*M<float>(A))) }
 ElError ElLU_d(ElMatrix_d A) { EL_GB_TRY(El::LU(*M<double>(A))) }
 ElError ElInverse_s(ElMatrix_s A) { EL_GB_TRY(El::Inverse(*M<float>(A))) }

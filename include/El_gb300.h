@@ -38,6 +38,11 @@ const char* ElErrorString(ElError error);
 /* include/El/core/types.h:211-228 */
 typedef enum { EL_NORMAL, EL_TRANSPOSE, EL_ADJOINT } ElOrientation;
 typedef enum { EL_LOWER, EL_UPPER } ElUpperOrLower;
+/* include/El/core/types.h:237-251 (BINARY and BINARY_FLAT are supported) */
+typedef enum {
+  EL_AUTO, EL_ASCII, EL_ASCII_MATLAB, EL_BINARY, EL_BINARY_FLAT, EL_BMP, EL_JPG, EL_JPEG,
+  EL_MATRIX_MARKET, EL_PNG, EL_PPM, EL_XBM, EL_XPM, EL_FileFormat_MAX
+} ElFileFormat;
 
 /* include/El/core/Matrix.h:20-31 */
 typedef struct ElMatrix_iDummy* ElMatrix_i;
@@ -120,6 +125,17 @@ ElError ElInverse_s(ElMatrix_s A);
 ElError ElInverse_d(ElMatrix_d A);
 ElError ElOneCondition_s(ElConstMatrix_s A, float* cond);
 ElError ElOneCondition_d(ElConstMatrix_d A, double* cond);
+
+/* Matrix files (include/El/io.h:145-151, 216-224) */
+ElError ElRead_i(ElMatrix_i A, const char* filename, ElFileFormat format);
+ElError ElRead_s(ElMatrix_s A, const char* filename, ElFileFormat format);
+ElError ElRead_d(ElMatrix_d A, const char* filename, ElFileFormat format);
+ElError ElWrite_i(ElConstMatrix_i A, const char* basename, ElFileFormat format,
+                  const char* title);
+ElError ElWrite_s(ElConstMatrix_s A, const char* basename, ElFileFormat format,
+                  const char* title);
+ElError ElWrite_d(ElConstMatrix_d A, const char* basename, ElFileFormat format,
+                  const char* title);
 
 /* Cholesky (include/El/lapack_like/factor.h:24-41) */
 ElError ElCholesky_s(ElUpperOrLower uplo, ElMatrix_s A);

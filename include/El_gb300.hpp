@@ -9,6 +9,7 @@
  *   El::LU(A) (no pivoting)  include/El/lapack_like/factor.hpp:367
  *   El::Inverse(A)           include/El/lapack_like/funcs.hpp:68
  *   El::OneCondition(A)      include/El/lapack_like/props.hpp:37
+ *   El::Read / El::Write     include/El/io.hpp:117,141 (BINARY, BINARY_FLAT)
  *   El::lu::SolveAfter       include/El/lapack_like/factor.hpp:434
  *   El::Cholesky(uplo, A)    include/El/lapack_like/factor.hpp:22
  *   El::cholesky::SolveAfter include/El/lapack_like/factor.hpp:63
@@ -24,6 +25,7 @@
 #define EL_GB300_HPP
 
 #include <stdexcept>
+#include <string>
 #include <vector>
 
 namespace El {
@@ -32,6 +34,13 @@ typedef int Int;
 
 enum UpperOrLower { LOWER, UPPER };
 enum Orientation { NORMAL, TRANSPOSE, ADJOINT };
+// Matrix file formats, in the reference's order (include/El/core/types.hpp,
+// ElFileFormat include/El/core/types.h:237-251); BINARY and BINARY_FLAT are
+// on this path.
+enum FileFormat {
+  AUTO, ASCII, ASCII_MATLAB, BINARY, BINARY_FLAT, BMP, JPG, JPEG, MATRIX_MARKET, PNG, PPM,
+  XBM, XPM, FileFormat_MAX
+};
 
 // Exception types of the reference (include/El/core/environment/decl.hpp:209-231).
 class SingularMatrixException : public std::runtime_error {
@@ -136,6 +145,16 @@ void Inverse(Matrix<F>& A);
 // ||A||_1 ||inv(A)||_1; +infinity for a singular A.
 template <typename F>
 F OneCondition(const Matrix<F>& A);
+
+// Matrix files.  BINARY (basename.bin): Int height, Int width, then the
+// entries column by column; BINARY_FLAT (basename.dat): the entries only,
+// read into A's current shape.  AUTO picks the format from the extension.
+// Other formats throw std::logic_error; I/O failures std::runtime_error.
+template <typename T>
+void Read(Matrix<T>& A, const std::string& filename, FileFormat format = AUTO);
+template <typename T>
+void Write(const Matrix<T>& A, const std::string& basename = "matrix",
+           FileFormat format = BINARY, const std::string& title = "");
 
 namespace lu {
 template <typename F>

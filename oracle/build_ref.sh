@@ -14,7 +14,8 @@
 #      src/blas_like, src/lapack_like/{perm,props}, src/matrices, plus
 #      LU.cpp, Cholesky.cpp, Linear.cpp, HPD.cpp and the general and
 #      triangular Inverse (funcs/Inverse/{General,Triangular}.cpp, which
-#      OneCondition in props calls);
+#      OneCondition in props calls) and the matrix file reader / writer
+#      (io/{File,Read,Write}.cpp);
 #   4. the BLAS names Elemental calls (bare, e.g. `dgemm`; no-suffix mangling
 #      include/El/core/imports/blas.hpp:29-41) renamed in the objects to the
 #      symbols of SciPy's bundled OpenBLAS (`scipy_dgemm_`), which is linked;
@@ -61,7 +62,8 @@ TUS=$(cd "$REF" && { find src/core src/blas_like src/lapack_like/perm \
       echo src/lapack_like/solve/Linear.cpp;
       echo src/lapack_like/solve/HPD.cpp;
       echo src/lapack_like/funcs/Inverse/General.cpp;
-      echo src/lapack_like/funcs/Inverse/Triangular.cpp; } | sort)
+      echo src/lapack_like/funcs/Inverse/Triangular.cpp;
+      echo src/io/File.cpp; echo src/io/Read.cpp; echo src/io/Write.cpp; } | sort)
 CXXFLAGS="-std=c++14 -O2 -fPIC -w -I$OUT/include -I$HERE/stub -I$REF/include
  -I$REF/external/suite_sparse/include -I$REF/external/pmrrr/include"
 export REF OUT CXXFLAGS

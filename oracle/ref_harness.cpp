@@ -18,6 +18,8 @@
 //   elref <d|s> lunopiv   <nb> A LU         (El::LU without pivoting)
 //   elref <d|s> inverse   <nb> A Ainv       (El::Inverse)
 //   elref <d|s> onecond   <nb> A cond       (El::OneCondition, a 1 x 1 matrix)
+//   elref <d|s> write     <nb> <bin|dat> basename A   (El::Write, BINARY / BINARY_FLAT)
+//   elref <d|s> read      <nb> file A                 (El::Read, format from the extension)
 //   elref <d|s> lutime    <nb> A reps       (prints seconds per El::LU)
 // Exit status: 0 ok, 3 SingularMatrixException, 4 NonHPDMatrixException,
 // 2 usage / IO error.
@@ -125,6 +127,15 @@ int Run(int argc, char** argv) {
     El::Matrix<T> c(1, 1);
     c(0, 0) = El::OneCondition(A);
     return WriteMatrix(argv[5], c) ? 0 : 2;
+  }
+  if (op == "write" && argc == 7) {
+    if (!ReadMatrix(argv[6], A)) return 2;
+    El::Write(A, argv[5], argv[4][0] == 'd' ? El::BINARY_FLAT : El::BINARY);
+    return 0;
+  }
+  if (op == "read" && argc == 6) {
+    El::Read(A, argv[4]);
+    return WriteMatrix(argv[5], A) ? 0 : 2;
   }
   if (op == "lutime" && argc == 6) {
     El::Matrix<T> A0;

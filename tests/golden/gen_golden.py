@@ -1,7 +1,7 @@
 """Generates the golden fixtures in this folder by running the REFERENCE's own
 sequential path (Elemental's El::LU with and without pivoting,
 lu::SolveAfter, El::Cholesky, cholesky::SolveAfter, El::LinearSolve,
-El::HPDSolve, El::Inverse, El::OneCondition), compiled from its
+El::HPDSolve, El::Inverse, El::OneCondition, El::Write), compiled from its
 sources into oracle/_ref/elref by oracle/build_ref.sh.
 
 Run (where the reference tree is present):
@@ -137,6 +137,20 @@ def main():
                     ("onecond_singular_50", Zi)):
         st, out = O.ref_run("onecond", nb=32, inputs=[M], out_dtypes=[F64])
         save(name, op="onecond", nb=32, status=st, A=M, cond=out[0].ravel()[0])
+
+    # El::Write (src/io/Write/Binary.hpp, BinaryFlat.hpp): the reference's
+    # file bytes for BINARY and BINARY_FLAT, FP64 and FP32
+    import tempfile
+    for fmt, ext in (("bin", "bin"), ("dat", "dat")):
+        for dt, sfx in ((F64, "d"), (np.float32, "s")):
+            M = mats.gaussian(7, 5, s + 700).astype(dt)
+            with tempfile.TemporaryDirectory() as d:
+                base = os.path.join(d, "m")
+                st, _ = O.ref_run("write", fmt, base, nb=32, dtype=dt, inputs=[M], out_dtypes=[])
+                with open(base + "." + ext, "rb") as f:
+                    raw = np.frombuffer(f.read(), dtype=np.uint8)
+            save(f"io_write_{fmt}_{sfx}_7x5", op="write", fmt=fmt, status=st, A=M, raw=raw,
+                 dtype=np.dtype(dt).name)
 
     # Config 1: n = 1024, 1 RHS, iid N(0,1), nb = 128 (the default blocksize)
     n = 1024

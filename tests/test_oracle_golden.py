@@ -35,7 +35,7 @@ def test_oracle_matches_reference_fixture(path):
     g = np.load(path)
     op = str(g["op"])
     st = int(g["status"])
-    nb = int(g["nb"])
+    nb = int(g["nb"]) if "nb" in g else 128
     if op == "lu":
         dt = np.float32 if str(g["dtype"]) == "float32" else np.float64
         if st != 0:
@@ -84,6 +84,19 @@ def test_oracle_matches_reference_fixture(path):
         # the result's size (the inverse of a kappa = 1e6 matrix included)
         tol = (1e-5 if dt == np.float32 else 1e-13) * np.abs(ref).max()
         assert np.abs(X - ref).max() <= tol, np.abs(X - ref).max()
+    elif op == "write":  # the oracle's reader of Elemental's binary layout
+        raw = bytes(g["raw"])
+        A = g["A"]
+        if str(g["fmt"]) == "bin":
+            import tempfile
+
+            with tempfile.TemporaryDirectory() as d:
+                path = os.path.join(d, "m.bin")
+                with open(path, "wb") as f:
+                    f.write(raw)
+                assert np.array_equal(O.read_el_binary(path, A.dtype), A)
+        else:
+            assert np.array_equal(np.frombuffer(raw, A.dtype).reshape(A.shape[::-1]).T, A)
     elif op == "onecond":
         c, ref = O.one_condition(g["A"], nb=nb), float(g["cond"])
         if np.isinf(ref):
