@@ -155,15 +155,23 @@ def PopBlocksizeStack():
 
 
 def LU(A: Matrix, pivType=LU_PARTIAL):
-    """El.LU(A, pivType) (python/lapack_like/factor.py:525-542): A is
+    """El.LU(A, pivType) (python/lapack_like/factor.py:525-552): A is
     overwritten by the packed L\\U.  Partial pivoting returns the
-    Permutation; LU_WITHOUT_PIVOTING (ElLU_*) returns None and raises
-    SingularMatrixException at an exact zero pivot."""
+    Permutation, LU_FULL the pair (P, Q); LU_WITHOUT_PIVOTING (ElLU_*)
+    returns None and raises SingularMatrixException at an exact zero pivot."""
     if pivType == LU_WITHOUT_PIVOTING:
         _check(getattr(A.lib, f"ElLU_{A.tag}")(A.obj), "LU", SingularMatrixException)
         return None
+    if pivType == LU_FULL:  # returns (P, Q) (python/lapack_like/factor.py:543-552)
+        P, Q = Permutation(), Permutation()
+        _check(getattr(A.lib, f"ElLUFullPiv_{A.tag}")(A.obj, P.obj, Q.obj), "LU",
+               SingularMatrixException)
+        k = min(A.Height(), A.Width())
+        P._dests = _swap_dests_from_explicit(P.ExplicitVector())[:k]
+        Q._dests = _swap_dests_from_explicit(Q.ExplicitVector())[:k]
+        return P, Q
     if pivType != LU_PARTIAL:
-        raise ValueError("full and rook pivoting are not on this path")
+        raise ValueError("rook pivoting is not on this path")
     P = Permutation()
     _check(getattr(A.lib, f"ElLUPartialPiv_{A.tag}")(A.obj, P.obj), "LU", SingularMatrixException)
     P._dests = _swap_dests_from_explicit(P.ExplicitVector())[: min(A.Height(), A.Width())]
@@ -173,6 +181,11 @@ def LU(A: Matrix, pivType=LU_PARTIAL):
 def SolveAfterLUPartialPiv(orient, A: Matrix, P: Permutation, B: Matrix):
     _check(getattr(A.lib, f"ElSolveAfterLUPartialPiv_{A.tag}")(orient, A.obj, P.obj, B.obj),
            "SolveAfterLUPartialPiv")
+
+
+def SolveAfterLUFullPiv(orient, A: Matrix, P: Permutation, Q: Permutation, B: Matrix):
+    _check(getattr(A.lib, f"ElSolveAfterLUFullPiv_{A.tag}")(orient, A.obj, P.obj, Q.obj,
+                                                            B.obj), "SolveAfterLUFullPiv")
 
 
 def Cholesky(uplo, A: Matrix):

@@ -91,6 +91,9 @@ def load():
         _sig(lib, f"ElGBHPDSolve_{s}", c_int, vp, c_int, c_int, vp, c_int, c_int, vp, c_int,
              c_int)
         _sig(lib, f"ElGBLUNoPiv_{s}", c_int, vp, c_int, c_int, vp, c_int, c_int)
+        _sig(lib, f"ElGBLUFullPiv_{s}", c_int, vp, c_int, c_int, vp, c_int, vp, vp)
+        _sig(lib, f"ElGBSolveAfterLUFullPiv_{s}", c_int, vp, c_int, c_int, vp, c_int, vp, vp,
+             c_int, vp, c_int)
         _sig(lib, f"ElGBInverse_{s}", c_int, vp, c_int, vp, c_int, c_int)
         _sig(lib, f"ElGBOneCondition_{s}", c_int, vp, c_int, vp, c_int, c_int, P(c_double))
     _sig(lib, "ElGBLUPartialPivMixed_s", c_int, vp, c_int, c_int, vp, c_int, vp, c_int, c_int)
@@ -143,6 +146,8 @@ def load():
     for s in ("s", "d"):
         _sig(lib, f"ElLUPartialPiv_{s}", c_int, vp, vp)
         _sig(lib, f"ElLU_{s}", c_int, vp)
+        _sig(lib, f"ElLUFullPiv_{s}", c_int, vp, vp, vp)
+        _sig(lib, f"ElSolveAfterLUFullPiv_{s}", c_int, c_int, vp, vp, vp, vp)
         _sig(lib, f"ElInverse_{s}", c_int, vp)
         _sig(lib, f"ElOneCondition_{s}", c_int, vp,
              P(ctypes.c_double if s == "d" else ctypes.c_float))

@@ -950,6 +950,61 @@ cudaError_t one_condition(Context* ctx, int n, const T* A, long lda, int nb, dou
   return e;
 }
 
+// El::LU(A, P, Q) with full pivoting (src/lapack_like/factor/LU/Full.hpp).
+template <typename T>
+cudaError_t getrf_full(Context* ctx, int m, int n, T* A, long lda, int* p, int* q) {
+  cudaError_t e = ctx->begin_call();
+  if (e != cudaSuccess || std::min(m, n) == 0) return e;
+  const int grid = fullpiv_grid(ctx->num_sms);
+  e = ctx->ensure(align256(sizeof(FullPivState<T>)) +
+                  align256((size_t)grid * sizeof(FullPivCand<T>)));
+  if (e != cudaSuccess) return e;
+  Carver cv(ctx);
+  auto* fs = cv.take<FullPivState<T>>(1);
+  auto* part = cv.take<FullPivCand<T>>(grid);
+  if (!fs || !part) return cudaErrorMemoryAllocation;
+  return launch_lu_full<T>(A, lda, m, n, p, q, fs, part, grid, ctx->status, ctx->stream,
+                           &ctx->launches);
+}
+
+// lu::SolveAfter(orientation, A, P, Q, B) (LU/SolveAfter.hpp:120-145):
+// NORMAL = P, L, U as getrs, then Q.InversePermuteRows(B); TRANSPOSE /
+// ADJOINT = Q.PermuteRows(B), then getrs's U^T, L^T and P^-1.
+template <typename T>
+cudaError_t getrs_full(Context* ctx, int orient, int n, const T* A, long lda, const int* p,
+                       const int* q, int nrhs, T* B, long ldb) {
+  if (n == 0 || nrhs == 0) return ctx->begin_call();
+  auto permute_q = [&](bool inverse) -> cudaError_t {
+    cudaError_t e = ctx->ensure(align256((size_t)n * sizeof(int)) +
+                                align256((size_t)n * nrhs * sizeof(T)));
+    if (e != cudaSuccess) return e;
+    Carver cv(ctx);
+    int* perm = cv.take<int>(n);
+    T* W = cv.take<T>((size_t)n * nrhs);
+    if (!perm || !W) return cudaErrorMemoryAllocation;
+    ELGB_CHECK(launch_explicit_perm(q, n, n, perm, ctx->stream), 1);
+    ELGB_CHECK(launch_permute_rows<T>(B, ldb, W, n, n, nrhs, perm, inverse, ctx->stream), 1);
+    return cudaMemcpy2DAsync(B, ldb * sizeof(T), W, (size_t)n * sizeof(T), (size_t)n * sizeof(T),
+                             nrhs, cudaMemcpyDeviceToDevice, ctx->stream);
+  };
+  cudaError_t e;
+  if (orient == 0) {
+    e = getrs<T>(ctx, 0, n, A, lda, p, nrhs, B, ldb, nullptr);
+    if (e == cudaSuccess) e = permute_q(true);
+  } else {
+    e = ctx->begin_call();
+    if (e == cudaSuccess) e = permute_q(false);
+    if (e == cudaSuccess) e = getrs<T>(ctx, orient, n, A, lda, p, nrhs, B, ldb, nullptr);
+  }
+  return e;
+}
+
+template cudaError_t getrf_full<double>(Context*, int, int, double*, long, int*, int*);
+template cudaError_t getrf_full<float>(Context*, int, int, float*, long, int*, int*);
+template cudaError_t getrs_full<double>(Context*, int, int, const double*, long, const int*,
+                                        const int*, int, double*, long);
+template cudaError_t getrs_full<float>(Context*, int, int, const float*, long, const int*,
+                                       const int*, int, float*, long);
 template cudaError_t getri<double>(Context*, int, double*, long, int);
 template cudaError_t getri<float>(Context*, int, float*, long, int);
 template cudaError_t one_condition<double>(Context*, int, const double*, long, int, double*);
@@ -1177,6 +1232,22 @@ long long ElGBLaunchCount(ElGBContext ctx) { return ctx ? ctx->launches : -1; }
     return elgb::to_el_error(elgb::getrf<T>(ctx, m, n, A, lda,                             \
                                             static_cast<int*>(ctx->arena2), nb, -1, false, \
                                             true));                                        \
+  }                                                                                        \
+  int ElGBLUFullPiv_##S(ElGBContext ctx, int m, int n, T* A, int lda, int* rowDests,       \
+                        int* colDests) {                                                   \
+    if (int r = arg_ok(ctx && m >= 0 && n >= 0 && lda >= std::max(m, 1) &&                 \
+                       (m * n == 0 || (A && rowDests && colDests))))                       \
+      return r;                                                                            \
+    return elgb::to_el_error(elgb::getrf_full<T>(ctx, m, n, A, lda, rowDests, colDests));  \
+  }                                                                                        \
+  int ElGBSolveAfterLUFullPiv_##S(ElGBContext ctx, int orientation, int n, const T* A,     \
+                                  int lda, const int* rowDests, const int* colDests,       \
+                                  int nrhs, T* B, int ldb) {                               \
+    if (int r = arg_ok(ctx && n >= 0 && nrhs >= 0 && lda >= std::max(n, 1) &&              \
+                       ldb >= std::max(n, 1) && orientation >= 0 && orientation <= 2))      \
+      return r;                                                                            \
+    return elgb::to_el_error(elgb::getrs_full<T>(ctx, orientation, n, A, lda, rowDests,    \
+                                                 colDests, nrhs, B, ldb));                 \
   }                                                                                        \
   int ElGBInverse_##S(ElGBContext ctx, int n, T* A, int lda, int nb) {                     \
     if (int r = arg_ok(ctx && n >= 0 && lda >= std::max(n, 1) && (n == 0 || A))) return r; \

@@ -75,6 +75,12 @@ void set_blocksize(int nb);
 template <typename T>
 cudaError_t getrf(Context* ctx, int m, int n, T* A, long lda, int* ipiv, int nb,
                   int tc_kind = -1, bool tournament = false, bool nopiv = false);
+// El::LU(A, P, Q) with full pivoting and its lu::SolveAfter.
+template <typename T>
+cudaError_t getrf_full(Context* ctx, int m, int n, T* A, long lda, int* p, int* q);
+template <typename T>
+cudaError_t getrs_full(Context* ctx, int orient, int n, const T* A, long lda, const int* p,
+                       const int* q, int nrhs, T* B, long ldb);
 // El::Inverse (funcs/Inverse/General/LUPartialPiv.hpp): A := inv(A) in place
 // through getrf and getrs on the identity; info (status) at a zero pivot.
 template <typename T>

@@ -329,6 +329,13 @@ struct Dispatch<double> {
   static int cond1(ElGBContext c, int n, const double* A, int lda, int nb, double* k) {
     return ElGBOneCondition_d(c, n, A, lda, nb, k);
   }
+  static int lufull(ElGBContext c, int m, int n, double* A, int lda, int* p, int* q) {
+    return ElGBLUFullPiv_d(c, m, n, A, lda, p, q);
+  }
+  static int lufulls(ElGBContext c, int o, int n, const double* A, int lda, const int* p,
+                     const int* q, int nr, double* B, int ldb) {
+    return ElGBSolveAfterLUFullPiv_d(c, o, n, A, lda, p, q, nr, B, ldb);
+  }
 };
 template <>
 struct Dispatch<float> {
@@ -362,6 +369,13 @@ struct Dispatch<float> {
   }
   static int cond1(ElGBContext c, int n, const float* A, int lda, int nb, double* k) {
     return ElGBOneCondition_s(c, n, A, lda, nb, k);
+  }
+  static int lufull(ElGBContext c, int m, int n, float* A, int lda, int* p, int* q) {
+    return ElGBLUFullPiv_s(c, m, n, A, lda, p, q);
+  }
+  static int lufulls(ElGBContext c, int o, int n, const float* A, int lda, const int* p,
+                     const int* q, int nr, float* B, int ldb) {
+    return ElGBSolveAfterLUFullPiv_s(c, o, n, A, lda, p, q, nr, B, ldb);
   }
 };
 
@@ -400,6 +414,42 @@ void LU(Matrix<F>& A, Permutation& P) {
     throw SingularMatrixException();
   }
   P.SetSwapSequence(m, piv.data(), minDim);
+}
+
+// El::LU(A, P, Q) with full pivoting (src/lapack_like/factor/LU.cpp:145-152).
+template <typename F>
+void LU(Matrix<F>& A, Permutation& P, Permutation& Q) {
+  std::lock_guard<std::mutex> lk(St().mu);
+  const Int m = A.Height(), n = A.Width(), minDim = std::min(m, n);
+  P.MakeIdentity(m);
+  Q.MakeIdentity(n);
+  P.ReserveSwaps(minDim);
+  Q.ReserveSwaps(minDim);
+  if (minDim == 0) {
+    P.SetSwapSequence(m, nullptr, 0);
+    Q.SetSwapSequence(n, nullptr, 0);
+    return;
+  }
+  ElGBContext ctx = Ctx();
+  const size_t sa = Al(sizeof(F) * (size_t)m * n), sp = Al(sizeof(int) * minDim);
+  char* base = Dev(sa + 2 * sp);
+  F* dA = reinterpret_cast<F*>(base);
+  int* dP = reinterpret_cast<int*>(base + sa);
+  int* dQ = reinterpret_cast<int*>(base + sa + sp);
+  Upload(ctx, dA, A);
+  CheckRc(Dispatch<F>::lufull(ctx, m, n, dA, m, dP, dQ));
+  int info = 0, err = 0;
+  if (ElGBStatus(ctx, &info, &err) != 0) throw std::runtime_error("CUDA failure");
+  Download(A, dA);
+  std::vector<Int> p(minDim), q(minDim);
+  Check(cudaMemcpy(p.data(), dP, sizeof(int) * minDim, cudaMemcpyDeviceToHost), "pivots");
+  Check(cudaMemcpy(q.data(), dQ, sizeof(int) * minDim, cudaMemcpyDeviceToHost), "pivots");
+  if (err) throw std::runtime_error("device-side wait timed out");
+  // the reference records step k's swaps before it finds the zero pivot
+  const Int ns = info ? std::min<Int>(info, minDim) : minDim;
+  P.SetSwapSequence(m, p.data(), ns);
+  Q.SetSwapSequence(n, q.data(), ns);
+  if (info) throw SingularMatrixException();
 }
 
 // El::LU(A) without pivoting (src/lapack_like/factor/LU.cpp:21-44).
@@ -467,6 +517,37 @@ void SolveAfter(Orientation orientation, const Matrix<F>& A, const Permutation& 
   Upload(ctx, dA, A);
   Upload(ctx, dB, B);
   CheckRc(Dispatch<F>::lus(ctx, orientation == NORMAL ? 0 : 1, n, dA, n, dP, q, dB, n));
+  CheckStatus(ctx, false);
+  Download(B, dB);
+}
+
+// lu::SolveAfter(orientation, A, P, Q, B) (LU/SolveAfter.hpp:120-145).
+template <typename F>
+void SolveAfter(Orientation orientation, const Matrix<F>& A, const Permutation& P,
+                const Permutation& Q, Matrix<F>& B) {
+  if (A.Height() != A.Width()) throw std::logic_error("A must be square");
+  if (A.Height() != B.Height()) throw std::logic_error("A and B must be the same height");
+  std::lock_guard<std::mutex> lk(St().mu);
+  const Int n = A.Height(), q = B.Width();
+  if (n == 0 || q == 0) return;
+  ElGBContext ctx = Ctx();
+  const size_t sa = Al(sizeof(F) * (size_t)n * n), sb = Al(sizeof(F) * (size_t)n * q),
+               sp = Al(sizeof(int) * n);
+  char* base = Dev(sa + sb + 2 * sp);
+  F* dA = reinterpret_cast<F*>(base);
+  F* dB = reinterpret_cast<F*>(base + sa);
+  int* dP = reinterpret_cast<int*>(base + sa + sb);
+  int* dQ = reinterpret_cast<int*>(base + sa + sb + sp);
+  std::vector<int> pv(n), qv(n);
+  for (Int i = 0; i < n; ++i) {
+    pv[i] = i < P.NumSwaps() ? P.SwapDestBuffer()[i] : i;
+    qv[i] = i < Q.NumSwaps() ? Q.SwapDestBuffer()[i] : i;
+  }
+  Check(cudaMemcpy(dP, pv.data(), sizeof(int) * n, cudaMemcpyHostToDevice), "pivots");
+  Check(cudaMemcpy(dQ, qv.data(), sizeof(int) * n, cudaMemcpyHostToDevice), "pivots");
+  Upload(ctx, dA, A);
+  Upload(ctx, dB, B);
+  CheckRc(Dispatch<F>::lufulls(ctx, orientation == NORMAL ? 0 : 1, n, dA, n, dP, dQ, q, dB, n));
   CheckStatus(ctx, false);
   Download(B, dB);
 }
@@ -653,6 +734,9 @@ template void Write<double>(const Matrix<double>&, const std::string&, FileForma
 #define EL_GB_PROTO(F)                                                                  \
   template void LU<F>(Matrix<F>&, Permutation&);                                        \
   template void LU<F>(Matrix<F>&);                                                      \
+  template void LU<F>(Matrix<F>&, Permutation&, Permutation&);                          \
+  template void lu::SolveAfter<F>(Orientation, const Matrix<F>&, const Permutation&,    \
+                                  const Permutation&, Matrix<F>&);                      \
   template void Inverse<F>(Matrix<F>&);                                                 \
   template F OneCondition<F>(const Matrix<F>&);                                         \
   template void lu::SolveAfter<F>(Orientation, const Matrix<F>&, const Permutation&,    \
@@ -818,6 +902,22 @@ ElError ElLUPartialPiv_d(ElMatrix_d A, ElPermutation P) {
 EL_GB_IO(i, El::Int)
 EL_GB_IO(s, float)
 EL_GB_IO(d, double)
+ElError ElLUFullPiv_s(ElMatrix_s A, ElPermutation P, ElPermutation Q) {
+  EL_GB_TRY(El::LU(*M<float>(A), *PP(P), *PP(Q)))
+}
+ElError ElLUFullPiv_d(ElMatrix_d A, ElPermutation P, ElPermutation Q) {
+  EL_GB_TRY(El::LU(*M<double>(A), *PP(P), *PP(Q)))
+}
+ElError ElSolveAfterLUFullPiv_s(ElOrientation o, ElConstMatrix_s A, ElConstPermutation P,
+                                ElConstPermutation Q, ElMatrix_s B) {
+  EL_GB_TRY(El::lu::SolveAfter(static_cast<El::Orientation>(o), *CM<float>(A), *CP(P), *CP(Q),
+                               *M<float>(B)))
+}
+ElError ElSolveAfterLUFullPiv_d(ElOrientation o, ElConstMatrix_d A, ElConstPermutation P,
+                                ElConstPermutation Q, ElMatrix_d B) {
+  EL_GB_TRY(El::lu::SolveAfter(static_cast<El::Orientation>(o), *CM<double>(A), *CP(P),
+                               *CP(Q), *M<double>(B)))
+}
 ElError ElLU_s(ElMatrix_s A) { EL_GB_TRY(El::LU(*M<float>(A))) }
 ElError ElLU_d(ElMatrix_d A) { EL_GB_TRY(El::LU(*M<double>(A))) }
 ElError ElInverse_s(ElMatrix_s A) { EL_GB_TRY(El::Inverse(*M<float>(A))) }

@@ -60,6 +60,27 @@ cudaError_t launch_getf2_panel(T* A, long lda, int mp, int w, int* ipiv,
                                const PanelScratch<T>& s, DevStatus* st,
                                int num_sms, cudaStream_t stream, bool nopiv = false);
 
+// El::LU(A, P, Q) with full pivoting (src/lapack_like/factor/LU/Full.hpp):
+// unblocked, two kernels per step.  fs / part: device scratch (one state,
+// `grid` candidates); p / q receive the row / column swap destinations; an
+// exact zero pivot records info = step + 1.  *nlaunch += kernels enqueued.
+template <typename T>
+struct FullPivState {
+  int i, j;        // the next pivot (absolute row and column)
+  T alpha;         // its value
+  unsigned count;  // CTAs done with the current update
+};
+template <typename T>
+struct FullPivCand {
+  T v, s;  // |value| and value
+  int i, j;
+};
+int fullpiv_grid(int num_sms);
+template <typename T>
+cudaError_t launch_lu_full(T* A, long lda, int m, int n, int* p, int* q, FullPivState<T>* fs,
+                           FullPivCand<T>* part, int grid, DevStatus* st, cudaStream_t stream,
+                           long long* nlaunch);
+
 // Converts the swap sequence ipiv[0..nb) (absolute destinations for rows
 // k..k+nb) into an explicit list of (dst, src) row moves.  pairs must hold
 // 4*nb ints ([dst..., src...] as 2*nb each); count receives the number of

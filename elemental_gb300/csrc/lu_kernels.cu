@@ -762,6 +762,228 @@ template cudaError_t launch_getf2_panel<float>(float*, long, int, int, int*, int
                                                int, cudaStream_t, bool);
 
 // ---------------------------------------------------------------------------
+// El::LU(A, P, Q) with full pivoting (src/lapack_like/factor/LU/Full.hpp:15-59)
+// ---------------------------------------------------------------------------
+// Unblocked, as the reference: per step k the pivot is the entry of largest
+// magnitude of the trailing block -- on equal magnitudes the first in
+// column-major order (MaxAbsLoc's strict '>' scan from 0 at the block's
+// corner, src/blas_like/level1/MaxAbsLoc.cpp:131-163) -- then RowSwap and
+// ColSwap over the whole matrix, a21 *= 1/alpha and the rank-1 update.
+// Two kernels per step: fullpiv_swap (swaps + scaling) and fullpiv_update
+// (rank-1 update of the trailing block fused with the next step's pivot
+// search; the last CTA to finish reduces the per-CTA candidates, so no CTA
+// ever waits on another).
+template <typename T>
+__device__ __forceinline__ bool fp_better(T v, int i, int j, T bv, int bi, int bj) {
+  if (v != bv) return v > bv;  // NaN never wins (as MaxAbsLoc's '>')
+  return j < bj || (j == bj && i < bi);
+}
+
+template <typename T>
+__global__ void fullpiv_swap_kernel(T* __restrict__ A, long lda, int m, int n, int k,
+                                    FullPivState<T>* __restrict__ fs, int* __restrict__ p,
+                                    int* __restrict__ q, DevStatus* st) {
+  const int ip = fs->i, jp = fs->j;
+  const T alpha = fs->alpha;  // the pivot's value, recorded by the search
+  const bool singular = alpha == T(0);
+  const T inv = singular ? T(1) : T(1) / alpha;
+  const long tid = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long nth = (long)gridDim.x * blockDim.x;
+  if (tid == 0) {
+    p[k] = ip;
+    q[k] = jp;
+    if (singular) atomicCAS(&st->info, 0, k + 1);
+    // the four entries both swaps move: row swap, then column swap
+    const T kk = A[k + (long)k * lda], kj = A[k + (long)jp * lda];
+    const T ik = A[ip + (long)k * lda], ij = A[ip + (long)jp * lda];
+    A[k + (long)k * lda] = ij;
+    A[k + (long)jp * lda] = ik;
+    A[ip + (long)jp * lda] = kk;
+    A[ip + (long)k * lda] = ip > k ? kj * inv : kj;  // below the diagonal: scaled
+  }
+  // row swap on every other column
+  if (ip != k)
+    for (long c = tid; c < n; c += nth) {
+      if (c == k || c == jp) continue;
+      T* a = A + k + c * lda;
+      T* b = A + ip + c * lda;
+      const T t = *a;
+      *a = *b;
+      *b = t;
+    }
+  // column swap on every other row; rows below k take the scaling
+  for (long r = tid; r < m; r += nth) {
+    if (r == k || r == ip) continue;
+    T* a = A + r + (long)k * lda;
+    T* b = A + r + (long)jp * lda;
+    const T t = *a;
+    *a = r > k ? *b * inv : *b;
+    if (jp != k) *b = t;
+  }
+}
+
+constexpr int kFpThreads = 256, kFpCols = 16;
+
+// Rank-1 update of the trailing block A[k+1:m, k+1:n] (skipped for the
+// initial search, k = -1) and the next pivot: one row per thread, kFpCols
+// columns per CTA tile, tiles grid-strided.
+template <typename T>
+__global__ void __launch_bounds__(kFpThreads)
+fullpiv_update_kernel(T* __restrict__ A, long lda, int m, int n, int k,
+                      FullPivState<T>* __restrict__ fs, FullPivCand<T>* __restrict__ part) {
+  __shared__ T s_v[kFpThreads / 32];
+  __shared__ T s_s[kFpThreads / 32];
+  __shared__ int s_i[kFpThreads / 32], s_j[kFpThreads / 32];
+  __shared__ bool s_last;
+  const int r0 = k + 1;
+  const int rows = m - r0, cols = n - r0;
+  const int rt = (rows + kFpThreads - 1) / kFpThreads, ct = (cols + kFpCols - 1) / kFpCols;
+  const long tiles = (long)rt * ct;
+  T bv = T(-1), bs = T(0);
+  int bi = 0x7fffffff, bj = 0x7fffffff;
+  for (long t = blockIdx.x; t < tiles; t += gridDim.x) {
+    const int ti = (int)(t % rt), tj = (int)(t / rt);
+    const int i = r0 + ti * kFpThreads + threadIdx.x;
+    if (i >= m) continue;
+    const T l = k >= 0 ? A[i + (long)k * lda] : T(0);
+    const int j1 = min(r0 + (tj + 1) * kFpCols, n);
+    for (int j = r0 + tj * kFpCols; j < j1; ++j) {
+      T* a = A + i + (long)j * lda;
+      T v = *a;
+      if (k >= 0) {
+        v = fma(l, -A[k + (long)j * lda], v);  // Geru(-1, a21, a12, A22)
+        *a = v;
+      }
+      const T av = v < T(0) ? -v : v;
+      if (fp_better(av, i, j, bv, bi, bj)) {
+        bv = av;
+        bs = v;
+        bi = i;
+        bj = j;
+      }
+    }
+  }
+  // the CTA's candidate
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int o = 16; o > 0; o >>= 1) {
+    const T ov = __shfl_xor_sync(0xffffffffu, bv, o);
+    const T os = __shfl_xor_sync(0xffffffffu, bs, o);
+    const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+    const int oj = __shfl_xor_sync(0xffffffffu, bj, o);
+    if (fp_better(ov, oi, oj, bv, bi, bj)) {
+      bv = ov;
+      bs = os;
+      bi = oi;
+      bj = oj;
+    }
+  }
+  if (lane == 0) {
+    s_v[warp] = bv;
+    s_s[warp] = bs;
+    s_i[warp] = bi;
+    s_j[warp] = bj;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < kFpThreads / 32; ++w)
+      if (fp_better(s_v[w], s_i[w], s_j[w], s_v[0], s_i[0], s_j[0])) {
+        s_v[0] = s_v[w];
+        s_s[0] = s_s[w];
+        s_i[0] = s_i[w];
+        s_j[0] = s_j[w];
+      }
+    part[blockIdx.x] = FullPivCand<T>{s_v[0], s_s[0], s_i[0], s_j[0]};
+    __threadfence();
+    s_last = atomicAdd(&fs->count, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  // the last CTA: every candidate is published (fence before each count)
+  __threadfence();
+  bv = T(-1);
+  bs = T(0);
+  bi = bj = 0x7fffffff;
+  for (int b = threadIdx.x; b < gridDim.x; b += kFpThreads) {
+    const volatile FullPivCand<T>* c = part + b;  // written by other CTAs
+    const T cv = c->v, cs = c->s;
+    const int ci = c->i, cj = c->j;
+    if (fp_better(cv, ci, cj, bv, bi, bj)) {
+      bv = cv;
+      bs = cs;
+      bi = ci;
+      bj = cj;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const T ov = __shfl_xor_sync(0xffffffffu, bv, o);
+    const T os = __shfl_xor_sync(0xffffffffu, bs, o);
+    const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+    const int oj = __shfl_xor_sync(0xffffffffu, bj, o);
+    if (fp_better(ov, oi, oj, bv, bi, bj)) {
+      bv = ov;
+      bs = os;
+      bi = oi;
+      bj = oj;
+    }
+  }
+  if (lane == 0) {
+    s_v[warp] = bv;
+    s_s[warp] = bs;
+    s_i[warp] = bi;
+    s_j[warp] = bj;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < kFpThreads / 32; ++w)
+      if (fp_better(s_v[w], s_i[w], s_j[w], s_v[0], s_i[0], s_j[0])) {
+        s_v[0] = s_v[w];
+        s_s[0] = s_s[w];
+        s_i[0] = s_i[w];
+        s_j[0] = s_j[w];
+      }
+    // all candidates zero (or the block empty): the block's corner, as
+    // MaxAbsLoc's scan starting from 0 at (0, 0)
+    const bool none = !(s_v[0] > T(0));
+    fs->i = none ? r0 : s_i[0];
+    fs->j = none ? r0 : s_j[0];
+    fs->alpha = none ? T(0) : s_s[0];
+    fs->count = 0;
+  }
+}
+
+int fullpiv_grid(int num_sms) { return 4 * num_sms; }
+
+template <typename T>
+cudaError_t launch_lu_full(T* A, long lda, int m, int n, int* p, int* q, FullPivState<T>* fs,
+                           FullPivCand<T>* part, int grid, DevStatus* st, cudaStream_t stream,
+                           long long* nlaunch) {
+  const int mn = std::min(m, n);
+  if (mn == 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(fs, 0, sizeof(FullPivState<T>), stream);
+  if (e != cudaSuccess) return e;
+  fullpiv_update_kernel<T><<<grid, kFpThreads, 0, stream>>>(A, lda, m, n, -1, fs, part);
+  *nlaunch += 1;
+  const int sgrid = std::max(1, std::min(ceil_div(std::max(m, n), 256), 64));
+  for (int k = 0; k < mn; ++k) {
+    fullpiv_swap_kernel<T><<<sgrid, 256, 0, stream>>>(A, lda, m, n, k, fs, p, q, st);
+    *nlaunch += 1;
+    if (k + 1 < m && k + 1 < n) {
+      fullpiv_update_kernel<T><<<grid, kFpThreads, 0, stream>>>(A, lda, m, n, k, fs, part);
+      *nlaunch += 1;
+    }
+    if ((k & 255) == 0 && (e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  return cudaGetLastError();
+}
+
+template cudaError_t launch_lu_full<double>(double*, long, int, int, int*, int*,
+                                            FullPivState<double>*, FullPivCand<double>*, int,
+                                            DevStatus*, cudaStream_t, long long*);
+template cudaError_t launch_lu_full<float>(float*, long, int, int, int*, int*,
+                                           FullPivState<float>*, FullPivCand<float>*, int,
+                                           DevStatus*, cudaStream_t, long long*);
+
+// ---------------------------------------------------------------------------
 // K2: row interchanges (PB.PermuteRows, src/lapack_like/factor/LU.cpp:130-131)
 // ---------------------------------------------------------------------------
 // The nb swaps (k+i <-> ipiv[i]) are replayed once, on row labels only, by

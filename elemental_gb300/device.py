@@ -200,6 +200,26 @@ class Context:
                                                                   nb), "LUNoPiv")
         return A
 
+    def lu_full(self, A, p=None, q=None):
+        """El::LU(A, P, Q) with full pivoting, in place; returns the int32
+        row and column swap destinations (ElGBLUFullPiv_*)."""
+        m, n = A.shape
+        k = min(m, n)
+        p = torch.empty(k, dtype=torch.int32, device=A.device) if p is None else p
+        q = torch.empty(k, dtype=torch.int32, device=A.device) if q is None else q
+        self._bind()
+        self._rc(getattr(self.lib, f"ElGBLUFullPiv_{_DT[A.dtype]}")(
+            self.h, m, n, _ptr(A), _ld(A), _ptr(p), _ptr(q)), "LUFullPiv")
+        return p, q
+
+    def lu_full_solve_after(self, A, p, q, B, orientation=0):
+        n = A.shape[0]
+        self._bind()
+        self._rc(getattr(self.lib, f"ElGBSolveAfterLUFullPiv_{_DT[A.dtype]}")(
+            self.h, orientation, n, _ptr(A), _ld(A), _ptr(p), _ptr(q), B.shape[1], _ptr(B),
+            _ld(B)), "SolveAfterLUFullPiv")
+        return B
+
     def inverse(self, A, nb=0):
         """El::Inverse(A): A := inv(A) in place (ElGBInverse_*)."""
         n = A.shape[0]

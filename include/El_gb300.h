@@ -115,6 +115,14 @@ ElError ElSolveAfterLUPartialPiv_d(ElOrientation orientation,
                                    ElConstMatrix_d A, ElConstPermutation P,
                                    ElMatrix_d B);
 
+/* LU with full pivoting and its solve (include/El/lapack_like/factor.h:538-563) */
+ElError ElLUFullPiv_s(ElMatrix_s A, ElPermutation P, ElPermutation Q);
+ElError ElLUFullPiv_d(ElMatrix_d A, ElPermutation P, ElPermutation Q);
+ElError ElSolveAfterLUFullPiv_s(ElOrientation orientation, ElConstMatrix_s A,
+                                ElConstPermutation P, ElConstPermutation Q, ElMatrix_s B);
+ElError ElSolveAfterLUFullPiv_d(ElOrientation orientation, ElConstMatrix_d A,
+                                ElConstPermutation P, ElConstPermutation Q, ElMatrix_d B);
+
 /* LU without pivoting (include/El/lapack_like/factor.h:467-468) */
 ElError ElLU_s(ElMatrix_s A);
 ElError ElLU_d(ElMatrix_d A);

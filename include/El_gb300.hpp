@@ -7,6 +7,7 @@
  *   El::Permutation          include/El/core/Permutation.hpp:14-126
  *   El::LU(A, P)             include/El/lapack_like/factor.hpp:376
  *   El::LU(A) (no pivoting)  include/El/lapack_like/factor.hpp:367
+ *   El::LU(A, P, Q) (full)   include/El/lapack_like/factor.hpp:384-387
  *   El::Inverse(A)           include/El/lapack_like/funcs.hpp:68
  *   El::OneCondition(A)      include/El/lapack_like/props.hpp:37
  *   El::Read / El::Write     include/El/io.hpp:117,141 (BINARY, BINARY_FLAT)
@@ -133,6 +134,11 @@ void PopBlocksizeStack();
 template <typename F>
 void LU(Matrix<F>& A, Permutation& P);
 
+// LU with full pivoting (P rows, Q columns); SingularMatrixException at an
+// exact zero pivot (the swaps of that step are recorded).
+template <typename F>
+void LU(Matrix<F>& A, Permutation& P, Permutation& Q);
+
 // LU without pivoting; throws SingularMatrixException at an exact zero pivot.
 template <typename F>
 void LU(Matrix<F>& A);
@@ -160,6 +166,9 @@ namespace lu {
 template <typename F>
 void SolveAfter(Orientation orientation, const Matrix<F>& A, const Permutation& P,
                 Matrix<F>& B);
+template <typename F>
+void SolveAfter(Orientation orientation, const Matrix<F>& A, const Permutation& P,
+                const Permutation& Q, Matrix<F>& B);
 }  // namespace lu
 
 template <typename F>

@@ -315,6 +315,26 @@ int ElGBSolveAfterCholesky_s(ElGBContext ctx, int uplo, int n,
 int ElGBLUNoPiv_d(ElGBContext ctx, int m, int n, double* A, int lda, int nb);
 int ElGBLUNoPiv_s(ElGBContext ctx, int m, int n, float* A, int lda, int nb);
 
+/* El::LU(A, P, Q) with full pivoting (reference src/lapack_like/factor/LU.cpp:
+ * 145-152 -> LU/Full.hpp:15-59): unblocked; per step the largest-magnitude
+ * entry of the trailing block (first in column-major order on ties), row
+ * and column swap, scaling, rank-1 update.  rowDests / colDests (min(m,n)
+ * ints, device) receive the row and column swap destinations; a zero pivot
+ * sets info.  Replaces ElLUFullPiv_d / _s (include/El/lapack_like/
+ * factor.h:538-541); lu::SolveAfter(orientation, A, P, Q, B)
+ * (LU/SolveAfter.hpp:120-145) replaces ElSolveAfterLUFullPiv_d / _s
+ * (factor.h:557-563). */
+int ElGBLUFullPiv_d(ElGBContext ctx, int m, int n, double* A, int lda, int* rowDests,
+                    int* colDests);
+int ElGBLUFullPiv_s(ElGBContext ctx, int m, int n, float* A, int lda, int* rowDests,
+                    int* colDests);
+int ElGBSolveAfterLUFullPiv_d(ElGBContext ctx, int orientation, int n, const double* A,
+                              int lda, const int* rowDests, const int* colDests, int nrhs,
+                              double* B, int ldb);
+int ElGBSolveAfterLUFullPiv_s(ElGBContext ctx, int orientation, int n, const float* A,
+                              int lda, const int* rowDests, const int* colDests, int nrhs,
+                              float* B, int ldb);
+
 /* El::Inverse(A) (reference src/lapack_like/funcs/Inverse/General.cpp:15-20 ->
  * General/LUPartialPiv.hpp:21-74): A := inv(A) in place via LU with partial
  * pivoting; a zero pivot sets info (SingularMatrixException).  Replaces

@@ -234,6 +234,63 @@ def lu_nopiv(A, nb: int = 128, dtype=np.float64):
     return W
 
 
+def lu_full(A, dtype=np.float64):
+    """El::LU(A, P, Q) with full pivoting (src/lapack_like/factor/LU/Full.hpp:
+    15-59): per step k, MaxAbsLoc of the trailing block (the first maximum
+    in column-major order, strict '>' from 0 at (k, k) --
+    src/blas_like/level1/MaxAbsLoc.cpp:131-163), RowSwap and ColSwap over the
+    whole matrix, a21 *= 1/alpha, Geru(-1, a21, a12, A22) through the same
+    BLAS routine (?ger of the SciPy OpenBLAS).  Returns (packed LU, row swap
+    destinations, column swap destinations); an exact zero pivot raises
+    OracleError(3)."""
+    from scipy.linalg import blas
+
+    W = np.array(A, dtype=dtype, order="F")
+    m, n = W.shape
+    mn = min(m, n)
+    p = np.zeros(mn, dtype=np.int32)
+    q = np.zeros(mn, dtype=np.int32)
+    ger = blas.dger if W.dtype == np.float64 else blas.sger
+    for k in range(mn):
+        B = np.abs(W[k:, k:])
+        flat = int(np.argmax(B.ravel(order="F")))  # first maximum, column-major
+        i, j = flat % B.shape[0], flat // B.shape[0]
+        if B[i, j] == 0:
+            i = j = 0
+        ip, jp = k + i, k + j
+        p[k], q[k] = ip, jp
+        if ip != k:
+            W[[k, ip], :] = W[[ip, k], :]
+        if jp != k:
+            W[:, [k, jp]] = W[:, [jp, k]]
+        alpha = W[k, k]
+        if alpha == 0:
+            raise OracleError(3)
+        W[k + 1:, k] *= dtype(1) / alpha
+        if k + 1 < m and k + 1 < n:
+            W[k + 1:, k + 1:] = ger(-1.0, W[k + 1:, k], W[k, k + 1:], a=W[k + 1:, k + 1:])
+    return W, p, q
+
+
+def lu_full_solve_after(LU, p, q, B, orientation: int = 0):
+    """lu::SolveAfter(orientation, A, P, Q, B) (LU/SolveAfter.hpp:120-145):
+    NORMAL: P.PermuteRows(B), unit-lower then upper solve,
+    Q.InversePermuteRows(B); TRANSPOSE: Q.PermuteRows(B), U^T then L^T
+    solve, P.InversePermuteRows(B)."""
+    from scipy.linalg import solve_triangular
+
+    X = np.array(B, dtype=LU.dtype, order="F")
+    if orientation == 0:
+        X = permute_rows(p, X)
+        X = solve_triangular(LU, X, lower=True, unit_diagonal=True)
+        X = solve_triangular(LU, X, lower=False)
+        return permute_rows(q, np.asfortranarray(X), inverse=True)
+    X = permute_rows(q, X)
+    X = solve_triangular(LU, X, lower=False, trans="T")
+    X = solve_triangular(LU, X, lower=True, unit_diagonal=True, trans="T")
+    return permute_rows(p, np.asfortranarray(X), inverse=True)
+
+
 def inverse(A, nb: int = 128, dtype=np.float64):
     """El::Inverse(A) (src/lapack_like/funcs/Inverse/General/LUPartialPiv.hpp:
     21-74): El::LU(A, P) (the C restatement above), TriangularInverse(UPPER,

@@ -16,6 +16,8 @@
 //   elref <d|s> linsolve  <nb> A B X
 //   elref <d|s> hpdsolve  <nb> <L|U> A B X
 //   elref <d|s> lunopiv   <nb> A LU         (El::LU without pivoting)
+//   elref <d|s> lufull    <nb> A LU p q     (El::LU with full pivoting)
+//   elref <d|s> lufullsolve <nb> <N|T> A B LU p q X  (+ lu::SolveAfter with P, Q)
 //   elref <d|s> inverse   <nb> A Ainv       (El::Inverse)
 //   elref <d|s> onecond   <nb> A cond       (El::OneCondition, a 1 x 1 matrix)
 //   elref <d|s> write     <nb> <bin|dat> basename A   (El::Write, BINARY / BINARY_FLAT)
@@ -116,6 +118,21 @@ int Run(int argc, char** argv) {
     if (!ReadMatrix(argv[4], A)) return 2;
     El::LU(A);
     return WriteMatrix(argv[5], A) ? 0 : 2;
+  }
+  if (op == "lufull" && argc == 8) {
+    if (!ReadMatrix(argv[4], A)) return 2;
+    El::Permutation Q;
+    El::LU(A, P, Q);
+    return (WriteMatrix(argv[5], A) && WritePivots(argv[6], P) && WritePivots(argv[7], Q))
+               ? 0 : 2;
+  }
+  if (op == "lufullsolve" && argc == 11) {
+    if (!ReadMatrix(argv[5], A) || !ReadMatrix(argv[6], B)) return 2;
+    El::Permutation Q;
+    El::LU(A, P, Q);
+    El::lu::SolveAfter(Orient(argv[4]), A, P, Q, B);
+    return (WriteMatrix(argv[7], A) && WritePivots(argv[8], P) && WritePivots(argv[9], Q) &&
+            WriteMatrix(argv[10], B)) ? 0 : 2;
   }
   if (op == "inverse" && argc == 6) {
     if (!ReadMatrix(argv[4], A)) return 2;

@@ -116,6 +116,31 @@ def main():
     st, _ = O.ref_run("lunopiv", nb=32, inputs=[Zp], out_dtypes=[F64])
     save("lunopiv_singular_100_nb32", op="lunopiv", nb=32, status=st, A=Zp)
 
+    # El::LU(A, P, Q) with full pivoting (LU.cpp:145-152 -> LU/Full.hpp:15-59:
+    # MaxAbsLoc over the trailing block, row and column swap, scale, rank-1
+    # update) and lu::SolveAfter(orientation, A, P, Q, B) (LU/SolveAfter.hpp)
+    for name, M in (("lufull_60", mats.gaussian(60, 60, s + 630)),
+                    ("lufull_70x45", mats.gaussian(70, 45, s + 631)),
+                    ("lufull_45x70", mats.gaussian(45, 70, s + 632))):
+        st, out = O.ref_run("lufull", nb=32, inputs=[M], out_dtypes=[F64, I32, I32])
+        save(name, op="lufull", nb=32, status=st, A=M, LU=out[0], p=out[1].ravel(),
+             q=out[2].ravel())
+    st, _ = O.ref_run("lufull", nb=32, inputs=[np.zeros((30, 30))], out_dtypes=[F64, I32, I32])
+    save("lufull_zero_30", op="lufull", nb=32, status=st, A=np.zeros((30, 30)))
+    M = mats.gaussian(16, 16, s + 635)
+    M.ravel()[::7] = np.round(M.ravel()[::7])
+    M[3, 5] = M[7, 2] = 4.0  # an exact tie for the first pivot: first in column order wins
+    st, out = O.ref_run("lufull", nb=32, inputs=[M], out_dtypes=[F64, I32, I32])
+    save("lufull_tie_16", op="lufull", nb=32, status=st, A=M, LU=out[0], p=out[1].ravel(),
+         q=out[2].ravel())
+    for o in ("N", "T"):
+        A = mats.gaussian(64, 64, s + 640)
+        B = mats.gaussian(64, 3, s + 641)
+        st, out = O.ref_run("lufullsolve", o, nb=32, inputs=[A, B],
+                            out_dtypes=[F64, I32, I32, F64])
+        save(f"lufullsolve_{o}_64", op="lufullsolve", orient=o, nb=32, status=st, A=A, B=B,
+             LU=out[0], p=out[1].ravel(), q=out[2].ravel(), X=out[3])
+
     # El::Inverse (funcs/Inverse/General/LUPartialPiv.hpp: LU, TriangularInverse,
     # the backward sweep against L, InversePermuteCols) and El::OneCondition
     # (props/Condition/One.cpp: ||A||_1 ||inv(A)||_1, +inf when singular)

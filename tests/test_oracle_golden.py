@@ -97,6 +97,18 @@ def test_oracle_matches_reference_fixture(path):
                 assert np.array_equal(O.read_el_binary(path, A.dtype), A)
         else:
             assert np.array_equal(np.frombuffer(raw, A.dtype).reshape(A.shape[::-1]).T, A)
+    elif op in ("lufull", "lufullsolve"):
+        if st != 0:
+            with pytest.raises(O.OracleError) as e:
+                O.lu_full(g["A"])
+            assert e.value.status == st
+            return
+        LU, p, q = O.lu_full(g["A"])
+        assert np.array_equal(p, g["p"]) and np.array_equal(q, g["q"])
+        close(LU, g["LU"])
+        if op == "lufullsolve":
+            X = O.lu_full_solve_after(LU, p, q, g["B"], 0 if str(g["orient"]) == "N" else 1)
+            close(X, g["X"])
     elif op == "onecond":
         c, ref = O.one_condition(g["A"], nb=nb), float(g["cond"])
         if np.isinf(ref):
