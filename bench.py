@@ -568,7 +568,7 @@ def batched_arm(args, rank, world, local_rank):
         if dist is not None:
             dist.destroy_process_group()
         return 0
-    cpu = None
+    cpu = cpu_full = None
     if args.cpu_baseline == "on":
         from oracle import oracle as O
         threads = os.cpu_count() or 1
@@ -787,7 +787,7 @@ def inverse_arm(args, rank, world, local_rank):
         if dist is not None:
             dist.destroy_process_group()
         return 0
-    cpu = None
+    cpu = cpu_full = None
     if args.cpu_baseline == "on":
         from oracle import oracle as O
 
@@ -799,11 +799,40 @@ def inverse_arm(args, rank, world, local_rank):
         t0 = time.perf_counter()
         O.inverse(As, nb=128)
         tc = time.perf_counter() - t0
+        nf = 512
+        Fs = np.random.default_rng(args.seed + 1).standard_normal((nf, nf))
+        t0 = time.perf_counter()
+        O.lu_full(Fs)
+        tf = time.perf_counter() - t0
+        cpu_full = {"n": nf, "seconds": tf, "scaled_seconds_at_gpu_n": tf * (min(n, 4096) / nf) ** 3,
+                    "kind": "port", "cores": threads}
         cpu = {"value": (ns / n) ** 3 / tc, "unit": "inverses/s", "cores": threads,
                "kind": "port",
                "sample": f"El::Inverse restatement (El::LU + TriangularInverse + the backward "
                          f"sweep, OpenBLAS) at n={ns}, {threads} threads: {tc:.3f} s, scaled "
                          f"to n={n} by n^3"}
+    # El::LU(A, P, Q) with full pivoting (unblocked, as the reference) of an
+    # n_full x n_full matrix, and the oracle's restatement on a CPU sample
+    n_full = min(n, 4096)
+    F0 = D.colmajor(n_full, n_full)
+    F0.copy_(A0[:n_full, :n_full])
+    F = D.colmajor(n_full, n_full)
+    F.copy_(F0)
+    ctx.lu_full(F)
+    F.copy_(F0)
+    torch.cuda.synchronize()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    ctx.lu_full(F)
+    f1.record(stream)
+    f1.synchronize()
+    t_full = f0.elapsed_time(f1) / 1e3
+    lu_full = {"n": n_full, "seconds": t_full,
+               "gflops_eq": 2.0 / 3.0 * n_full ** 3 / t_full / 1e9,
+               "bound": "one pass over the trailing block per step (read + write)",
+               "achieved_gbs": 16.0 * n_full ** 3 / 3.0 / t_full / 1e9,
+               "status": ctx.status()}
+    del F, F0
     value = args.steps * world / t
     fp64_peak = ctx.fp64_peak_tflops()
     line = {
@@ -812,12 +841,15 @@ def inverse_arm(args, rank, world, local_rank):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic: seeded iid N(0,1) FP64 (device Philox generator)",
         "config": {"workload": f"El::Inverse of one n={n} FP64 matrix (getrf + getrs on the "
-                               f"identity), N(0,1); El::OneCondition of the same matrix",
+                               f"identity), N(0,1); El::OneCondition of the same matrix; "
+                               f"El::LU with full pivoting of its leading "
+                               f"{min(n, 4096)} x {min(n, 4096)} block",
                    "n": n, "l2": "inputs larger than L2" if 8 * n * n > 129e6 else "in L2",
                    "parallelism": f"replicas x{world}"},
         "tflops_eq": flops * value / world / 1e12,
         "residual_AX_minus_I": resid, "status": info,
         "one_condition": {"value": cond, "seconds": t_cond},
+        "lu_full_pivoting": dict(lu_full, cpu_sample=cpu_full if cpu else None),
         "roofline": {"bound": "fp64 FMA pipe (tcgen05 has no FP64 kind)",
                      "achieved": flops * value / world / 1e12, "peak": fp64_peak,
                      "unit": "TFLOP/s", "frac": flops * value / world / 1e12 / fp64_peak,
