@@ -188,9 +188,22 @@ def SolveAfterLUFullPiv(orient, A: Matrix, P: Permutation, Q: Permutation, B: Ma
                                                             B.obj), "SolveAfterLUFullPiv")
 
 
-def Cholesky(uplo, A: Matrix):
+def Cholesky(uplo, A: Matrix, piv=False):
+    """El.Cholesky(uplo, A, piv) (python/lapack_like/factor.py:34-60); with
+    piv=True, diagonal pivoting (ElCholeskyPiv_*) and the Permutation is
+    returned."""
+    if piv:
+        P = Permutation()
+        _check(getattr(A.lib, f"ElCholeskyPiv_{A.tag}")(uplo, A.obj, P.obj), "Cholesky")
+        P._dests = _swap_dests_from_explicit(P.ExplicitVector())[: A.Height()]
+        return P
     _check(getattr(A.lib, f"ElCholesky_{A.tag}")(uplo, A.obj), "Cholesky",
            SingularMatrixException)
+
+
+def SolveAfterCholeskyPiv(uplo, orient, A: Matrix, P: Permutation, B: Matrix):
+    _check(getattr(A.lib, f"ElSolveAfterCholeskyPiv_{A.tag}")(uplo, orient, A.obj, P.obj,
+                                                              B.obj), "SolveAfterCholeskyPiv")
 
 
 def SolveAfterCholesky(uplo, orient, A: Matrix, B: Matrix):

@@ -92,6 +92,9 @@ def load():
              c_int)
         _sig(lib, f"ElGBLUNoPiv_{s}", c_int, vp, c_int, c_int, vp, c_int, c_int)
         _sig(lib, f"ElGBLUFullPiv_{s}", c_int, vp, c_int, c_int, vp, c_int, vp, vp)
+        _sig(lib, f"ElGBCholeskyPiv_{s}", c_int, vp, c_int, c_int, vp, c_int, vp)
+        _sig(lib, f"ElGBSolveAfterCholeskyPiv_{s}", c_int, vp, c_int, c_int, vp, c_int, vp,
+             c_int, vp, c_int)
         _sig(lib, f"ElGBSolveAfterLUFullPiv_{s}", c_int, vp, c_int, c_int, vp, c_int, vp, vp,
              c_int, vp, c_int)
         _sig(lib, f"ElGBInverse_{s}", c_int, vp, c_int, vp, c_int, c_int)
@@ -147,6 +150,8 @@ def load():
         _sig(lib, f"ElLUPartialPiv_{s}", c_int, vp, vp)
         _sig(lib, f"ElLU_{s}", c_int, vp)
         _sig(lib, f"ElLUFullPiv_{s}", c_int, vp, vp, vp)
+        _sig(lib, f"ElCholeskyPiv_{s}", c_int, c_int, vp, vp)
+        _sig(lib, f"ElSolveAfterCholeskyPiv_{s}", c_int, c_int, c_int, vp, vp, vp)
         _sig(lib, f"ElSolveAfterLUFullPiv_{s}", c_int, c_int, vp, vp, vp, vp)
         _sig(lib, f"ElInverse_{s}", c_int, vp)
         _sig(lib, f"ElOneCondition_{s}", c_int, vp,

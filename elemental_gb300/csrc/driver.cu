@@ -999,6 +999,56 @@ cudaError_t getrs_full(Context* ctx, int orient, int n, const T* A, long lda, co
   return e;
 }
 
+// El::Cholesky(uplo, A, P) with diagonal pivoting (Cholesky.cpp:44-52).
+template <typename T>
+cudaError_t potrf_piv(Context* ctx, int uplo, int n, T* A, long lda, int* piv) {
+  cudaError_t e = ctx->begin_call();
+  if (e != cudaSuccess || n == 0) return e;
+  const int grid = fullpiv_grid(ctx->num_sms);
+  e = ctx->ensure(align256(sizeof(FullPivState<T>)) +
+                  align256((size_t)grid * sizeof(FullPivCand<T>)));
+  if (e != cudaSuccess) return e;
+  Carver cv(ctx);
+  auto* fs = cv.take<FullPivState<T>>(1);
+  auto* part = cv.take<FullPivCand<T>>(grid);
+  if (!fs || !part) return cudaErrorMemoryAllocation;
+  return launch_cholesky_piv<T>(A, lda, n, uplo == 1, piv, fs, part, grid, ctx->stream,
+                                &ctx->launches);
+}
+
+// cholesky::SolveAfter(uplo, orientation, A, P, B) on real data
+// (Cholesky/SolveAfter.hpp:46-76): P.PermuteRows(B), the Cholesky solve,
+// P.InversePermuteRows(B).
+template <typename T>
+cudaError_t potrs_piv(Context* ctx, int uplo, int n, const T* A, long lda, const int* piv,
+                      int nrhs, T* B, long ldb) {
+  if (n == 0 || nrhs == 0) return ctx->begin_call();
+  auto permute = [&](bool inverse) -> cudaError_t {
+    cudaError_t e = ctx->ensure(align256((size_t)n * sizeof(int)) +
+                                align256((size_t)n * nrhs * sizeof(T)));
+    if (e != cudaSuccess) return e;
+    Carver cv(ctx);
+    int* perm = cv.take<int>(n);
+    T* W = cv.take<T>((size_t)n * nrhs);
+    if (!perm || !W) return cudaErrorMemoryAllocation;
+    ELGB_CHECK(launch_explicit_perm(piv, n, n, perm, ctx->stream), 1);
+    ELGB_CHECK(launch_permute_rows<T>(B, ldb, W, n, n, nrhs, perm, inverse, ctx->stream), 1);
+    return cudaMemcpy2DAsync(B, ldb * sizeof(T), W, (size_t)n * sizeof(T), (size_t)n * sizeof(T),
+                             nrhs, cudaMemcpyDeviceToDevice, ctx->stream);
+  };
+  cudaError_t e = ctx->begin_call();
+  if (e == cudaSuccess) e = permute(false);
+  if (e == cudaSuccess) e = potrs<T>(ctx, uplo, n, A, lda, nrhs, B, ldb);
+  if (e == cudaSuccess) e = permute(true);
+  return e;
+}
+
+template cudaError_t potrf_piv<double>(Context*, int, int, double*, long, int*);
+template cudaError_t potrf_piv<float>(Context*, int, int, float*, long, int*);
+template cudaError_t potrs_piv<double>(Context*, int, int, const double*, long, const int*,
+                                       int, double*, long);
+template cudaError_t potrs_piv<float>(Context*, int, int, const float*, long, const int*, int,
+                                      float*, long);
 template cudaError_t getrf_full<double>(Context*, int, int, double*, long, int*, int*);
 template cudaError_t getrf_full<float>(Context*, int, int, float*, long, int*, int*);
 template cudaError_t getrs_full<double>(Context*, int, int, const double*, long, const int*,
@@ -1248,6 +1298,19 @@ long long ElGBLaunchCount(ElGBContext ctx) { return ctx ? ctx->launches : -1; }
       return r;                                                                            \
     return elgb::to_el_error(elgb::getrs_full<T>(ctx, orientation, n, A, lda, rowDests,    \
                                                  colDests, nrhs, B, ldb));                 \
+  }                                                                                        \
+  int ElGBCholeskyPiv_##S(ElGBContext ctx, int uplo, int n, T* A, int lda, int* piv) {     \
+    if (int r = arg_ok(ctx && n >= 0 && lda >= std::max(n, 1) && (uplo == 0 || uplo == 1) && \
+                       (n == 0 || (A && piv))))                                            \
+      return r;                                                                            \
+    return elgb::to_el_error(elgb::potrf_piv<T>(ctx, uplo, n, A, lda, piv));               \
+  }                                                                                        \
+  int ElGBSolveAfterCholeskyPiv_##S(ElGBContext ctx, int uplo, int n, const T* A, int lda,  \
+                                    const int* piv, int nrhs, T* B, int ldb) {             \
+    if (int r = arg_ok(ctx && n >= 0 && nrhs >= 0 && lda >= std::max(n, 1) &&              \
+                       ldb >= std::max(n, 1) && (uplo == 0 || uplo == 1)))                 \
+      return r;                                                                            \
+    return elgb::to_el_error(elgb::potrs_piv<T>(ctx, uplo, n, A, lda, piv, nrhs, B, ldb)); \
   }                                                                                        \
   int ElGBInverse_##S(ElGBContext ctx, int n, T* A, int lda, int nb) {                     \
     if (int r = arg_ok(ctx && n >= 0 && lda >= std::max(n, 1) && (n == 0 || A))) return r; \

@@ -81,6 +81,12 @@ cudaError_t getrf_full(Context* ctx, int m, int n, T* A, long lda, int* p, int* 
 template <typename T>
 cudaError_t getrs_full(Context* ctx, int orient, int n, const T* A, long lda, const int* p,
                        const int* q, int nrhs, T* B, long ldb);
+// El::Cholesky(uplo, A, P) with diagonal pivoting and its SolveAfter.
+template <typename T>
+cudaError_t potrf_piv(Context* ctx, int uplo, int n, T* A, long lda, int* piv);
+template <typename T>
+cudaError_t potrs_piv(Context* ctx, int uplo, int n, const T* A, long lda, const int* piv,
+                      int nrhs, T* B, long ldb);
 // El::Inverse (funcs/Inverse/General/LUPartialPiv.hpp): A := inv(A) in place
 // through getrf and getrs on the identity; info (status) at a zero pivot.
 template <typename T>

@@ -332,6 +332,13 @@ struct Dispatch<double> {
   static int lufull(ElGBContext c, int m, int n, double* A, int lda, int* p, int* q) {
     return ElGBLUFullPiv_d(c, m, n, A, lda, p, q);
   }
+  static int cholpiv(ElGBContext c, int u, int n, double* A, int lda, int* p) {
+    return ElGBCholeskyPiv_d(c, u, n, A, lda, p);
+  }
+  static int cholpivs(ElGBContext c, int u, int n, const double* A, int lda, const int* p,
+                      int nr, double* B, int ldb) {
+    return ElGBSolveAfterCholeskyPiv_d(c, u, n, A, lda, p, nr, B, ldb);
+  }
   static int lufulls(ElGBContext c, int o, int n, const double* A, int lda, const int* p,
                      const int* q, int nr, double* B, int ldb) {
     return ElGBSolveAfterLUFullPiv_d(c, o, n, A, lda, p, q, nr, B, ldb);
@@ -372,6 +379,13 @@ struct Dispatch<float> {
   }
   static int lufull(ElGBContext c, int m, int n, float* A, int lda, int* p, int* q) {
     return ElGBLUFullPiv_s(c, m, n, A, lda, p, q);
+  }
+  static int cholpiv(ElGBContext c, int u, int n, float* A, int lda, int* p) {
+    return ElGBCholeskyPiv_s(c, u, n, A, lda, p);
+  }
+  static int cholpivs(ElGBContext c, int u, int n, const float* A, int lda, const int* p,
+                      int nr, float* B, int ldb) {
+    return ElGBSolveAfterCholeskyPiv_s(c, u, n, A, lda, p, nr, B, ldb);
   }
   static int lufulls(ElGBContext c, int o, int n, const float* A, int lda, const int* p,
                      const int* q, int nr, float* B, int ldb) {
@@ -553,6 +567,33 @@ void SolveAfter(Orientation orientation, const Matrix<F>& A, const Permutation& 
 }
 }  // namespace lu
 
+// El::Cholesky(uplo, A, P) with diagonal pivoting (src/lapack_like/factor/
+// Cholesky.cpp:44-52).
+template <typename F>
+void Cholesky(UpperOrLower uplo, Matrix<F>& A, Permutation& P) {
+  if (A.Height() != A.Width()) throw std::logic_error("A must be square");
+  std::lock_guard<std::mutex> lk(St().mu);
+  const Int n = A.Height();
+  P.MakeIdentity(n);
+  P.ReserveSwaps(n);
+  if (n == 0) {
+    P.SetSwapSequence(n, nullptr, 0);
+    return;
+  }
+  ElGBContext ctx = Ctx();
+  const size_t sa = Al(sizeof(F) * (size_t)n * n);
+  char* base = Dev(sa + Al(sizeof(int) * n));
+  F* dA = reinterpret_cast<F*>(base);
+  int* dP = reinterpret_cast<int*>(base + sa);
+  Upload(ctx, dA, A);
+  CheckRc(Dispatch<F>::cholpiv(ctx, uplo == UPPER ? 1 : 0, n, dA, n, dP));
+  CheckStatus(ctx, true);
+  Download(A, dA);
+  std::vector<Int> p(n);
+  Check(cudaMemcpy(p.data(), dP, sizeof(int) * n, cudaMemcpyDeviceToHost), "pivots");
+  P.SetSwapSequence(n, p.data(), n);
+}
+
 template <typename F>
 void Cholesky(UpperOrLower uplo, Matrix<F>& A) {
   if (A.Height() != A.Width()) throw std::logic_error("A must be square");
@@ -587,6 +628,35 @@ void SolveAfter(UpperOrLower uplo, Orientation orientation, const Matrix<F>& A, 
   Upload(ctx, dA, A);
   Upload(ctx, dB, B);
   CheckRc(Dispatch<F>::chols(ctx, uplo == UPPER ? 1 : 0, n, dA, n, q, dB, n));
+  CheckStatus(ctx, true);
+  Download(B, dB);
+}
+}  // namespace cholesky
+
+namespace cholesky {
+// cholesky::SolveAfter(uplo, orientation, A, P, B) (Cholesky/SolveAfter.hpp:46-76);
+// on real data the orientation changes nothing.
+template <typename F>
+void SolveAfter(UpperOrLower uplo, Orientation orientation, const Matrix<F>& A,
+                const Permutation& P, Matrix<F>& B) {
+  (void)orientation;
+  if (A.Height() != A.Width()) throw std::logic_error("A must be square");
+  if (A.Height() != B.Height()) throw std::logic_error("A and B must be the same height");
+  std::lock_guard<std::mutex> lk(St().mu);
+  const Int n = A.Height(), q = B.Width();
+  if (n == 0 || q == 0) return;
+  ElGBContext ctx = Ctx();
+  const size_t sa = Al(sizeof(F) * (size_t)n * n), sb = Al(sizeof(F) * (size_t)n * q);
+  char* base = Dev(sa + sb + Al(sizeof(int) * n));
+  F* dA = reinterpret_cast<F*>(base);
+  F* dB = reinterpret_cast<F*>(base + sa);
+  int* dP = reinterpret_cast<int*>(base + sa + sb);
+  std::vector<int> pv(n);
+  for (Int i = 0; i < n; ++i) pv[i] = i < P.NumSwaps() ? P.SwapDestBuffer()[i] : i;
+  Check(cudaMemcpy(dP, pv.data(), sizeof(int) * n, cudaMemcpyHostToDevice), "pivots");
+  Upload(ctx, dA, A);
+  Upload(ctx, dB, B);
+  CheckRc(Dispatch<F>::cholpivs(ctx, uplo == UPPER ? 1 : 0, n, dA, n, dP, q, dB, n));
   CheckStatus(ctx, true);
   Download(B, dB);
 }
@@ -735,6 +805,9 @@ template void Write<double>(const Matrix<double>&, const std::string&, FileForma
   template void LU<F>(Matrix<F>&, Permutation&);                                        \
   template void LU<F>(Matrix<F>&);                                                      \
   template void LU<F>(Matrix<F>&, Permutation&, Permutation&);                          \
+  template void Cholesky<F>(UpperOrLower, Matrix<F>&, Permutation&);                    \
+  template void cholesky::SolveAfter<F>(UpperOrLower, Orientation, const Matrix<F>&,    \
+                                        const Permutation&, Matrix<F>&);                \
   template void lu::SolveAfter<F>(Orientation, const Matrix<F>&, const Permutation&,    \
                                   const Permutation&, Matrix<F>&);                      \
   template void Inverse<F>(Matrix<F>&);                                                 \
@@ -917,6 +990,20 @@ ElError ElSolveAfterLUFullPiv_d(ElOrientation o, ElConstMatrix_d A, ElConstPermu
                                 ElConstPermutation Q, ElMatrix_d B) {
   EL_GB_TRY(El::lu::SolveAfter(static_cast<El::Orientation>(o), *CM<double>(A), *CP(P),
                                *CP(Q), *M<double>(B)))
+}
+ElError ElCholeskyPiv_s(ElUpperOrLower u, ElMatrix_s A, ElPermutation P) {
+  EL_GB_TRY(El::Cholesky(Ul(u), *M<float>(A), *PP(P)))
+}
+ElError ElCholeskyPiv_d(ElUpperOrLower u, ElMatrix_d A, ElPermutation P) {
+  EL_GB_TRY(El::Cholesky(Ul(u), *M<double>(A), *PP(P)))
+}
+ElError ElSolveAfterCholeskyPiv_s(ElUpperOrLower u, ElOrientation o, ElConstMatrix_s A,
+                                  ElConstPermutation P, ElMatrix_s B) {
+  EL_GB_TRY(El::cholesky::SolveAfter(Ul(u), Or(o), *CM<float>(A), *CP(P), *M<float>(B)))
+}
+ElError ElSolveAfterCholeskyPiv_d(ElUpperOrLower u, ElOrientation o, ElConstMatrix_d A,
+                                  ElConstPermutation P, ElMatrix_d B) {
+  EL_GB_TRY(El::cholesky::SolveAfter(Ul(u), Or(o), *CM<double>(A), *CP(P), *M<double>(B)))
 }
 ElError ElLU_s(ElMatrix_s A) { EL_GB_TRY(El::LU(*M<float>(A))) }
 ElError ElLU_d(ElMatrix_d A) { EL_GB_TRY(El::LU(*M<double>(A))) }

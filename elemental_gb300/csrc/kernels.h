@@ -76,6 +76,14 @@ struct FullPivCand {
   int i, j;
 };
 int fullpiv_grid(int num_sms);
+// El::Cholesky(uplo, A, P) with diagonal pivoting: unblocked, two kernels per
+// step; piv (n ints) receives the swap destinations.  Same scratch as
+// launch_lu_full.  No error is raised for a non-positive pivot (the
+// reference takes its square root).
+template <typename T>
+cudaError_t launch_cholesky_piv(T* A, long lda, int n, bool upper, int* piv,
+                                FullPivState<T>* fs, FullPivCand<T>* part, int grid,
+                                cudaStream_t stream, long long* nlaunch);
 template <typename T>
 cudaError_t launch_lu_full(T* A, long lda, int m, int n, int* p, int* q, FullPivState<T>* fs,
                            FullPivCand<T>* part, int grid, DevStatus* st, cudaStream_t stream,

@@ -951,6 +951,197 @@ fullpiv_update_kernel(T* __restrict__ A, long lda, int m, int n, int k,
   }
 }
 
+// ---------------------------------------------------------------------------
+// El::Cholesky(uplo, A, P) with diagonal pivoting (src/lapack_like/factor/
+// Cholesky.cpp:44-52, Cholesky/Pivoted{Lower,Upper}Variant3.hpp)
+// ---------------------------------------------------------------------------
+// Right-looking and unblocked here (the reference's lazy panels compute the
+// same updated diagonals): per step the updated diagonal's largest magnitude
+// (the first on ties, VectorMaxAbsLoc) is the pivot, SymmetricSwap(LOWER)
+// moves it to (k, k) (src/blas_like/level1/Swap.cpp:243-301), the column is
+// scaled by 1/sqrt(pivot) and the trailing lower triangle takes the rank-1
+// update fused with the next pivot search.  The upper variant runs the same
+// steps on the transpose (element (i, j) of the lower view is A(j, i)).
+template <typename T>
+__device__ __forceinline__ T* pc_at(T* A, long lda, bool upper, int i, int j) {
+  return upper ? A + j + (long)i * lda : A + i + (long)j * lda;
+}
+
+template <typename T>
+__global__ void pchol_swap_kernel(T* __restrict__ A, long lda, int n, int k, int upper,
+                                  const FullPivState<T>* __restrict__ fs, int* __restrict__ piv) {
+  const int frm = fs->i;
+  const T delta = sqrt(fs->alpha);  // NaN for a negative pivot, as the reference's Sqrt
+  const T inv = T(1) / delta;
+  const bool up = upper != 0;
+  const long tid = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long nth = (long)gridDim.x * blockDim.x;
+  if (tid == 0) {
+    piv[k] = frm;
+    if (frm != k) {
+      *pc_at(A, lda, up, frm, frm) = *pc_at(A, lda, up, k, k);  // diagonal swap
+      T* c = pc_at(A, lda, up, frm, k);                          // the corner stays,
+      *c = *c * inv;                                             // below the diagonal: scaled
+    }
+    *pc_at(A, lda, up, k, k) = delta;
+  }
+  if (frm != k)
+    for (long j = tid; j < k; j += nth) {  // left: rows k and frm
+      T* a = pc_at(A, lda, up, k, (int)j);
+      T* b = pc_at(A, lda, up, frm, (int)j);
+      const T t = *a;
+      *a = *b;
+      *b = t;
+    }
+  for (long i = k + 1 + tid; i < frm; i += nth) {  // inner: column k <-> row frm
+    T* a = pc_at(A, lda, up, (int)i, k);
+    T* b = pc_at(A, lda, up, frm, (int)i);
+    const T t = *a;
+    *a = *b * inv;
+    *b = t;
+  }
+  for (long i = (long)max(frm, k) + 1 + tid; i < n; i += nth) {  // bottom: columns k, frm
+    T* a = pc_at(A, lda, up, (int)i, k);
+    T* b = pc_at(A, lda, up, (int)i, frm);
+    const T t = *a;
+    *a = *b * inv;
+    if (frm != k) *b = t;
+  }
+}
+
+// Rank-1 update of the trailing lower triangle (skipped for the initial
+// search, k = -1) and the next pivot among its diagonal entries.
+template <typename T>
+__global__ void __launch_bounds__(kFpThreads)
+pchol_update_kernel(T* __restrict__ A, long lda, int n, int k, int upper,
+                    FullPivState<T>* __restrict__ fs, FullPivCand<T>* __restrict__ part) {
+  __shared__ T s_v[kFpThreads / 32];
+  __shared__ T s_s[kFpThreads / 32];
+  __shared__ int s_i[kFpThreads / 32];
+  __shared__ bool s_last;
+  const bool up = upper != 0;
+  const int r0 = k + 1, rows = n - r0;
+  const int rt = (rows + kFpThreads - 1) / kFpThreads, ct = (rows + kFpCols - 1) / kFpCols;
+  const long tiles = (long)rt * ct;
+  T bv = T(-1), bs = T(0);
+  int bi = 0x7fffffff;
+  for (long t = blockIdx.x; t < tiles; t += gridDim.x) {
+    const int ti = (int)(t % rt), tj = (int)(t / rt);
+    const int j0 = r0 + tj * kFpCols, j1 = min(j0 + kFpCols, n);
+    if (r0 + (ti + 1) * kFpThreads - 1 < j0) continue;  // entirely above the diagonal
+    const int i = r0 + ti * kFpThreads + threadIdx.x;
+    if (i >= n || i < j0) continue;
+    const T l = k >= 0 ? *pc_at(A, lda, up, i, k) : T(0);
+    const int jl = min(j1, i + 1);  // the lower triangle: j <= i
+    for (int j = j0; j < jl; ++j) {
+      T* a = pc_at(A, lda, up, i, j);
+      T v = *a;
+      if (k >= 0) {
+        v = fma(l, -*pc_at(A, lda, up, j, k), v);  // Her(LOWER, -1, a21, A22)
+        *a = v;
+      }
+      if (j == i) {
+        const T av = v < T(0) ? -v : v;
+        if (fp_better(av, i, i, bv, bi, bi)) {
+          bv = av;
+          bs = v;
+          bi = i;
+        }
+      }
+    }
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  auto reduce_warp = [&]() {
+    for (int o = 16; o > 0; o >>= 1) {
+      const T ov = __shfl_xor_sync(0xffffffffu, bv, o);
+      const T os = __shfl_xor_sync(0xffffffffu, bs, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (fp_better(ov, oi, oi, bv, bi, bi)) {
+        bv = ov;
+        bs = os;
+        bi = oi;
+      }
+    }
+  };
+  auto reduce_cta = [&]() {
+    if (lane == 0) {
+      s_v[warp] = bv;
+      s_s[warp] = bs;
+      s_i[warp] = bi;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+      for (int w = 1; w < kFpThreads / 32; ++w)
+        if (fp_better(s_v[w], s_i[w], s_i[w], s_v[0], s_i[0], s_i[0])) {
+          s_v[0] = s_v[w];
+          s_s[0] = s_s[w];
+          s_i[0] = s_i[w];
+        }
+  };
+  reduce_warp();
+  reduce_cta();
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = FullPivCand<T>{s_v[0], s_s[0], s_i[0], s_i[0]};
+    __threadfence();
+    s_last = atomicAdd(&fs->count, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  bv = T(-1);
+  bs = T(0);
+  bi = 0x7fffffff;
+  for (int b = threadIdx.x; b < gridDim.x; b += kFpThreads) {
+    const volatile FullPivCand<T>* c = part + b;
+    const T cv = c->v, cs = c->s;
+    const int ci = c->i;
+    if (fp_better(cv, ci, ci, bv, bi, bi)) {
+      bv = cv;
+      bs = cs;
+      bi = ci;
+    }
+  }
+  reduce_warp();
+  __syncthreads();
+  reduce_cta();
+  if (threadIdx.x == 0) {
+    const bool none = !(s_v[0] > T(0));  // VectorMaxAbsLoc: index 0 at value 0
+    fs->i = fs->j = none ? r0 : s_i[0];
+    fs->alpha = none ? T(0) : s_s[0];
+    fs->count = 0;
+  }
+}
+
+template <typename T>
+cudaError_t launch_cholesky_piv(T* A, long lda, int n, bool upper, int* piv,
+                                FullPivState<T>* fs, FullPivCand<T>* part, int grid,
+                                cudaStream_t stream, long long* nlaunch) {
+  if (n == 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(fs, 0, sizeof(FullPivState<T>), stream);
+  if (e != cudaSuccess) return e;
+  const int up = upper ? 1 : 0;
+  pchol_update_kernel<T><<<grid, kFpThreads, 0, stream>>>(A, lda, n, -1, up, fs, part);
+  *nlaunch += 1;
+  const int sgrid = std::max(1, std::min(ceil_div(n, 256), 64));
+  for (int k = 0; k < n; ++k) {
+    pchol_swap_kernel<T><<<sgrid, 256, 0, stream>>>(A, lda, n, k, up, fs, piv);
+    *nlaunch += 1;
+    if (k + 1 < n) {
+      pchol_update_kernel<T><<<grid, kFpThreads, 0, stream>>>(A, lda, n, k, up, fs, part);
+      *nlaunch += 1;
+    }
+    if ((k & 255) == 0 && (e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  return cudaGetLastError();
+}
+
+template cudaError_t launch_cholesky_piv<double>(double*, long, int, bool, int*,
+                                                 FullPivState<double>*, FullPivCand<double>*,
+                                                 int, cudaStream_t, long long*);
+template cudaError_t launch_cholesky_piv<float>(float*, long, int, bool, int*,
+                                                FullPivState<float>*, FullPivCand<float>*, int,
+                                                cudaStream_t, long long*);
+
 int fullpiv_grid(int num_sms) { return 4 * num_sms; }
 
 template <typename T>

@@ -220,6 +220,23 @@ class Context:
             _ld(B)), "SolveAfterLUFullPiv")
         return B
 
+    def cholesky_piv(self, A, uplo=0, piv=None):
+        """El::Cholesky(uplo, A, P) with diagonal pivoting, in place; returns
+        the int32 swap destinations (ElGBCholeskyPiv_*)."""
+        n = A.shape[0]
+        piv = torch.empty(n, dtype=torch.int32, device=A.device) if piv is None else piv
+        self._bind()
+        self._rc(getattr(self.lib, f"ElGBCholeskyPiv_{_DT[A.dtype]}")(
+            self.h, uplo, n, _ptr(A), _ld(A), _ptr(piv)), "CholeskyPiv")
+        return piv
+
+    def cholesky_piv_solve_after(self, A, piv, B, uplo=0):
+        self._bind()
+        self._rc(getattr(self.lib, f"ElGBSolveAfterCholeskyPiv_{_DT[A.dtype]}")(
+            self.h, uplo, A.shape[0], _ptr(A), _ld(A), _ptr(piv), B.shape[1], _ptr(B), _ld(B)),
+            "SolveAfterCholeskyPiv")
+        return B
+
     def inverse(self, A, nb=0):
         """El::Inverse(A): A := inv(A) in place (ElGBInverse_*)."""
         n = A.shape[0]

@@ -115,6 +115,14 @@ ElError ElSolveAfterLUPartialPiv_d(ElOrientation orientation,
                                    ElConstMatrix_d A, ElConstPermutation P,
                                    ElMatrix_d B);
 
+/* Cholesky with diagonal pivoting and its solve (include/El/lapack_like/factor.h:80-105) */
+ElError ElCholeskyPiv_s(ElUpperOrLower uplo, ElMatrix_s A, ElPermutation P);
+ElError ElCholeskyPiv_d(ElUpperOrLower uplo, ElMatrix_d A, ElPermutation P);
+ElError ElSolveAfterCholeskyPiv_s(ElUpperOrLower uplo, ElOrientation orientation,
+                                  ElConstMatrix_s A, ElConstPermutation P, ElMatrix_s B);
+ElError ElSolveAfterCholeskyPiv_d(ElUpperOrLower uplo, ElOrientation orientation,
+                                  ElConstMatrix_d A, ElConstPermutation P, ElMatrix_d B);
+
 /* LU with full pivoting and its solve (include/El/lapack_like/factor.h:538-563) */
 ElError ElLUFullPiv_s(ElMatrix_s A, ElPermutation P, ElPermutation Q);
 ElError ElLUFullPiv_d(ElMatrix_d A, ElPermutation P, ElPermutation Q);

@@ -13,7 +13,8 @@
  *   El::Read / El::Write     include/El/io.hpp:117,141 (BINARY, BINARY_FLAT)
  *   El::lu::SolveAfter       include/El/lapack_like/factor.hpp:434
  *   El::Cholesky(uplo, A)    include/El/lapack_like/factor.hpp:22
- *   El::cholesky::SolveAfter include/El/lapack_like/factor.hpp:63
+ *   El::cholesky::SolveAfter include/El/lapack_like/factor.hpp:63 (and :76-81 with P)
+ *   El::Cholesky(uplo, A, P) include/El/lapack_like/factor.hpp:37
  *   El::LinearSolve(A, B)    include/El/lapack_like/solve.hpp:20
  *   El::HPDSolve             include/El/lapack_like/solve.hpp:190
  *   El::Blocksize / SetBlocksize / PushBlocksizeStack / PopBlocksizeStack
@@ -174,10 +175,17 @@ void SolveAfter(Orientation orientation, const Matrix<F>& A, const Permutation& 
 template <typename F>
 void Cholesky(UpperOrLower uplo, Matrix<F>& A);
 
+// Cholesky with diagonal pivoting, P A P^T = L L^T (or U^T U).
+template <typename F>
+void Cholesky(UpperOrLower uplo, Matrix<F>& A, Permutation& P);
+
 namespace cholesky {
 template <typename F>
 void SolveAfter(UpperOrLower uplo, Orientation orientation, const Matrix<F>& A,
                 Matrix<F>& B);
+template <typename F>
+void SolveAfter(UpperOrLower uplo, Orientation orientation, const Matrix<F>& A,
+                const Permutation& P, Matrix<F>& B);
 }  // namespace cholesky
 
 template <typename F>

@@ -335,6 +335,23 @@ int ElGBSolveAfterLUFullPiv_s(ElGBContext ctx, int orientation, int n, const flo
                               int lda, const int* rowDests, const int* colDests, int nrhs,
                               float* B, int ldb);
 
+/* El::Cholesky(uplo, A, P) with diagonal pivoting, P A P^T = L L^T = U^T U
+ * (reference src/lapack_like/factor/Cholesky.cpp:44-52 ->
+ * Cholesky/Pivoted{Lower,Upper}Variant3.hpp): per step the largest updated
+ * diagonal entry (the first on ties), a symmetric swap in the uplo
+ * triangle, scaling by 1/sqrt(pivot), the rank-1 update.  piv (n ints,
+ * device) receives the swap destinations; no error for a non-positive pivot
+ * (the reference takes its square root).  Replaces ElCholeskyPiv_d / _s
+ * (include/El/lapack_like/factor.h:80-83); the solve
+ * (Cholesky/SolveAfter.hpp:46-76) replaces ElSolveAfterCholeskyPiv_d / _s
+ * (factor.h:100-105). */
+int ElGBCholeskyPiv_d(ElGBContext ctx, int uplo, int n, double* A, int lda, int* piv);
+int ElGBCholeskyPiv_s(ElGBContext ctx, int uplo, int n, float* A, int lda, int* piv);
+int ElGBSolveAfterCholeskyPiv_d(ElGBContext ctx, int uplo, int n, const double* A, int lda,
+                                const int* piv, int nrhs, double* B, int ldb);
+int ElGBSolveAfterCholeskyPiv_s(ElGBContext ctx, int uplo, int n, const float* A, int lda,
+                                const int* piv, int nrhs, float* B, int ldb);
+
 /* El::Inverse(A) (reference src/lapack_like/funcs/Inverse/General.cpp:15-20 ->
  * General/LUPartialPiv.hpp:21-74): A := inv(A) in place via LU with partial
  * pivoting; a zero pivot sets info (SingularMatrixException).  Replaces

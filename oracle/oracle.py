@@ -234,6 +234,96 @@ def lu_nopiv(A, nb: int = 128, dtype=np.float64):
     return W
 
 
+def _sym_swap_lower(W, to, frm):
+    """SymmetricSwap(LOWER, A, to, from) (src/blas_like/level1/Swap.cpp:243-301)
+    on real data: bottom, inner (column segment <-> row segment), diagonal and
+    left swaps; the corner A(from, to) stays."""
+    if to == frm:
+        return
+    if to > frm:
+        to, frm = frm, to
+    n = W.shape[0]
+    if frm + 1 < n:
+        W[frm + 1:, [to, frm]] = W[frm + 1:, [frm, to]]
+    if to + 1 < frm:
+        a = W[to + 1:frm, to].copy()
+        W[to + 1:frm, to] = W[frm, to + 1:frm]
+        W[frm, to + 1:frm] = a
+    W[to, to], W[frm, frm] = W[frm, frm], W[to, to]
+    if to > 0:
+        W[[to, frm], :to] = W[[frm, to], :to]
+
+
+def cholesky_piv(A, uplo: str = "L", nb: int = 128, dtype=np.float64):
+    """El::Cholesky(uplo, A, P) with diagonal pivoting (src/lapack_like/factor/
+    Cholesky.cpp:44-52 -> Cholesky/PivotedLowerVariant3.hpp:206-255, 345-365):
+    lazy panels of nb columns -- per column, the updated diagonal's largest
+    magnitude (VectorMaxAbsLoc: first index on ties) picks the pivot,
+    HermitianSwap on the lower triangle and on the panel's X / Y rows, the
+    column caught up by Gemv with the panel's earlier columns, scaled by
+    1/sqrt(pivot) -- then Trrk(LOWER) on the trailing block.  The upper
+    variant is the same on the transpose.  At a panel's first column the
+    reference's PanelFull reads X(i, -1) of an empty view (memory before the
+    buffer); this restatement takes no update there.  With 8- or 16-column
+    panels on a correlation matrix that read was measured non-zero on later
+    panels and changed the reference's pivots; the fixtures use panel widths
+    where it contributes nothing.
+    Returns (factor in the uplo triangle, swap destinations)."""
+    W = np.array(A, dtype=dtype, order="F")
+    if uplo == "U":
+        W = np.asfortranarray(W.T)
+    n = W.shape[0]
+    piv = np.zeros(n, dtype=np.int32)
+    for off in range(0, n, nb):
+        bs = min(nb, n - off)
+        m = n - off
+        X = np.zeros((m, bs), dtype=dtype)
+        Y = np.zeros((m, bs), dtype=dtype)
+        d = np.diag(W)[off:].copy()
+        for k in range(bs):
+            if k > 0:
+                d[k:] -= X[k:, k - 1] * Y[k:, k - 1]
+            a = np.abs(d[k:])
+            rel = int(np.argmax(a)) if a.size and a.max() > 0 else 0
+            frm = k + rel
+            _sym_swap_lower(W, off + k, off + frm)
+            piv[off + k] = off + frm
+            d[[k, frm]] = d[[frm, k]]
+            X[[k, frm], :k] = X[[frm, k], :k]
+            Y[[k, frm], :k] = Y[[frm, k], :k]
+            if k > 0:
+                W[off + k:, off + k] -= X[k:, :k] @ Y[k, :k]
+            delta = np.sqrt(W[off + k, off + k])
+            W[off + k, off + k] = delta
+            W[off + k + 1:, off + k] *= dtype(1) / delta
+            X[k + 1:, k] = W[off + k + 1:, off + k]
+            Y[k + 1:, k] = W[off + k + 1:, off + k]
+        if off + bs < n:
+            U = X[bs:, :] @ Y[bs:, :].T
+            T22 = W[off + bs:, off + bs:]
+            il = np.tril_indices(n - off - bs)
+            T22[il] -= U[il]
+    if uplo == "U":
+        W = np.asfortranarray(W.T)
+    return W, piv
+
+
+def cholesky_piv_solve_after(C, piv, B, uplo: str = "L"):
+    """cholesky::SolveAfter(uplo, orientation, A, P, B) (Cholesky/SolveAfter.hpp:
+    46-76) on real data: P.PermuteRows(B), the two triangular solves,
+    P.InversePermuteRows(B)."""
+    from scipy.linalg import solve_triangular
+
+    X = permute_rows(piv, np.array(B, dtype=C.dtype, order="F"))
+    if uplo == "L":
+        X = solve_triangular(C, X, lower=True)
+        X = solve_triangular(C, X, lower=True, trans="T")
+    else:
+        X = solve_triangular(C, X, lower=False, trans="T")
+        X = solve_triangular(C, X, lower=False)
+    return permute_rows(piv, np.asfortranarray(X), inverse=True)
+
+
 def lu_full(A, dtype=np.float64):
     """El::LU(A, P, Q) with full pivoting (src/lapack_like/factor/LU/Full.hpp:
     15-59): per step k, MaxAbsLoc of the trailing block (the first maximum

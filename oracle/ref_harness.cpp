@@ -12,6 +12,8 @@
 //   elref <d|s> lu        <nb> A LU piv
 //   elref <d|s> lusolve   <nb> <N|T> A B LU piv X
 //   elref <d|s> chol      <nb> <L|U> A C
+//   elref <d|s> cholpiv   <nb> <L|U> A C piv            (El::Cholesky(uplo, A, P))
+//   elref <d|s> cholpivsolve <nb> <L|U> A B C piv X    (+ cholesky::SolveAfter with P)
 //   elref <d|s> cholsolve <nb> <L|U> A B C X
 //   elref <d|s> linsolve  <nb> A B X
 //   elref <d|s> hpdsolve  <nb> <L|U> A B X
@@ -97,6 +99,18 @@ int Run(int argc, char** argv) {
     if (!ReadMatrix(argv[5], A)) return 2;
     El::Cholesky(Uplo(argv[4]), A);
     return WriteMatrix(argv[6], A) ? 0 : 2;
+  }
+  if (op == "cholpiv" && argc == 8) {
+    if (!ReadMatrix(argv[5], A)) return 2;
+    El::Cholesky(Uplo(argv[4]), A, P);
+    return (WriteMatrix(argv[6], A) && WritePivots(argv[7], P)) ? 0 : 2;
+  }
+  if (op == "cholpivsolve" && argc == 10) {
+    if (!ReadMatrix(argv[5], A) || !ReadMatrix(argv[6], B)) return 2;
+    El::Cholesky(Uplo(argv[4]), A, P);
+    El::cholesky::SolveAfter(Uplo(argv[4]), El::NORMAL, A, P, B);
+    return (WriteMatrix(argv[7], A) && WritePivots(argv[8], P) && WriteMatrix(argv[9], B))
+               ? 0 : 2;
   }
   if (op == "cholsolve" && argc == 9) {
     if (!ReadMatrix(argv[5], A) || !ReadMatrix(argv[6], B)) return 2;

@@ -93,6 +93,31 @@ def main():
     st, _ = O.ref_run("chol", "L", nb=16, inputs=[G], out_dtypes=[F64])
     save("chol_nonhpd_60_nb16", op="chol", uplo="L", nb=16, status=st, A=G)
 
+    # El::Cholesky(uplo, A, P) with diagonal pivoting (Cholesky.cpp:44-52 ->
+    # Cholesky/Pivoted{Lower,Upper}Variant3.hpp: lazy panels of Blocksize()
+    # columns, the largest updated diagonal entry first -- the first on ties)
+    # and cholesky::SolveAfter(uplo, orientation, A, P, B) (SolveAfter.hpp:46-76)
+    Sp = mats.spd(90, s + 650)
+    Cr = mats.spd(70, s + 651)
+    dg = np.sqrt(np.diag(Cr))
+    Cr = Cr / dg[:, None] / dg[None, :]
+    np.fill_diagonal(Cr, 1.0)  # a correlation matrix: every diagonal entry ties
+    # (the reference's PivotedLowerPanel reads X(i, -1) of an empty view at
+    # each panel's first column -- memory before the buffer; with 8 or 16
+    # column panels on this correlation matrix that read is non-zero on later
+    # panels and changes the pivots, so the fixtures use panel widths where it
+    # is not)
+    for u in ("L", "U"):
+        for name, M, nb in ((f"cholpiv_{u}_spd90_nb32", Sp, 32),
+                            (f"cholpiv_{u}_corr70_nb32", Cr, 32)):
+            st, out = O.ref_run("cholpiv", u, nb=nb, inputs=[M], out_dtypes=[F64, I32])
+            save(name, op="cholpiv", uplo=u, nb=nb, status=st, A=M, C=out[0], piv=out[1].ravel())
+        B = mats.gaussian(90, 3, s + 652)
+        st, out = O.ref_run("cholpivsolve", u, nb=32, inputs=[Sp, B],
+                            out_dtypes=[F64, I32, F64])
+        save(f"cholpivsolve_{u}_spd90_nb32", op="cholpivsolve", uplo=u, nb=32, status=st, A=Sp,
+             B=B, C=out[0], piv=out[1].ravel(), X=out[2])
+
     # El::LinearSolve
     A = mats.gaussian(120, 120, s + 500)
     B = mats.gaussian(120, 5, s + 501)

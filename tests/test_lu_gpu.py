@@ -139,8 +139,9 @@ def test_cholesky_matches_oracle(ctx, uplo, n, nb):
     assert np.array_equal(np.tril(C, -1) if uplo else np.triu(C, 1), other)
 
 
-@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLD, "chol*.npz")) +
-                                        glob.glob(os.path.join(GOLD, "hpdsolve*.npz"))),
+@pytest.mark.parametrize("path", sorted(p for p in glob.glob(os.path.join(GOLD, "chol*.npz"))
+                                        if not os.path.basename(p).startswith("cholpiv")) +
+                         glob.glob(os.path.join(GOLD, "hpdsolve*.npz")),
                          ids=lambda p: os.path.basename(p)[:-4])
 def test_cholesky_fixtures(ctx, path):
     g = np.load(path)

@@ -109,6 +109,14 @@ def test_oracle_matches_reference_fixture(path):
         if op == "lufullsolve":
             X = O.lu_full_solve_after(LU, p, q, g["B"], 0 if str(g["orient"]) == "N" else 1)
             close(X, g["X"])
+    elif op in ("cholpiv", "cholpivsolve"):
+        u = str(g["uplo"])
+        C, piv = O.cholesky_piv(g["A"], u, nb=nb)
+        assert np.array_equal(piv, g["piv"])
+        tri = np.tril if u == "L" else np.triu
+        close(tri(C), tri(g["C"]))
+        if op == "cholpivsolve":
+            close(O.cholesky_piv_solve_after(C, piv, g["B"], u), g["X"])
     elif op == "onecond":
         c, ref = O.one_condition(g["A"], nb=nb), float(g["cond"])
         if np.isinf(ref):
