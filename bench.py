@@ -568,7 +568,7 @@ def batched_arm(args, rank, world, local_rank):
         if dist is not None:
             dist.destroy_process_group()
         return 0
-    cpu = cpu_full = None
+    cpu = cpu_full = cpu_chp = None
     if args.cpu_baseline == "on":
         from oracle import oracle as O
         threads = os.cpu_count() or 1
@@ -787,7 +787,7 @@ def inverse_arm(args, rank, world, local_rank):
         if dist is not None:
             dist.destroy_process_group()
         return 0
-    cpu = cpu_full = None
+    cpu = cpu_full = cpu_chp = None
     if args.cpu_baseline == "on":
         from oracle import oracle as O
 
@@ -806,6 +806,14 @@ def inverse_arm(args, rank, world, local_rank):
         tf = time.perf_counter() - t0
         cpu_full = {"n": nf, "seconds": tf, "scaled_seconds_at_gpu_n": tf * (min(n, 4096) / nf) ** 3,
                     "kind": "port", "cores": threads}
+        Gs = np.random.default_rng(args.seed + 2).standard_normal((nf, nf))
+        Ss = Gs.T @ Gs / nf + np.eye(nf)
+        t0 = time.perf_counter()
+        O.cholesky_piv(Ss, "L", nb=128)
+        tcp = time.perf_counter() - t0
+        cpu_chp = {"n": nf, "seconds": tcp,
+                   "scaled_seconds_at_gpu_n": tcp * (min(n, 4096) / nf) ** 3,
+                   "kind": "port", "cores": threads}
         cpu = {"value": (ns / n) ** 3 / tc, "unit": "inverses/s", "cores": threads,
                "kind": "port",
                "sample": f"El::Inverse restatement (El::LU + TriangularInverse + the backward "
@@ -833,6 +841,26 @@ def inverse_arm(args, rank, world, local_rank):
                "achieved_gbs": 16.0 * n_full ** 3 / 3.0 / t_full / 1e9,
                "status": ctx.status()}
     del F, F0
+    # El::Cholesky(LOWER, A, P) with diagonal pivoting of an SPD matrix
+    # G^T G / n + I (G the same leading block; input synthesis, not timed)
+    G = A0[:n_full, :n_full]
+    S0 = D.colmajor(n_full, n_full)
+    S0.copy_((G.t() @ G) / n_full + torch.eye(n_full, dtype=torch.float64, device="cuda"))
+    S = D.colmajor(n_full, n_full)
+    S.copy_(S0)
+    ctx.cholesky_piv(S)
+    S.copy_(S0)
+    torch.cuda.synchronize()
+    f0.record(stream)
+    ctx.cholesky_piv(S)
+    f1.record(stream)
+    f1.synchronize()
+    t_chp = f0.elapsed_time(f1) / 1e3
+    chol_piv = {"n": n_full, "seconds": t_chp,
+                "gflops_eq": 1.0 / 3.0 * n_full ** 3 / t_chp / 1e9,
+                "bound": "one pass over the trailing lower triangle per step",
+                "status": ctx.status()}
+    del S, S0, G
     value = args.steps * world / t
     fp64_peak = ctx.fp64_peak_tflops()
     line = {
@@ -843,13 +871,15 @@ def inverse_arm(args, rank, world, local_rank):
         "config": {"workload": f"El::Inverse of one n={n} FP64 matrix (getrf + getrs on the "
                                f"identity), N(0,1); El::OneCondition of the same matrix; "
                                f"El::LU with full pivoting of its leading "
-                               f"{min(n, 4096)} x {min(n, 4096)} block",
+                               f"{min(n, 4096)} x {min(n, 4096)} block; El::Cholesky with "
+                               f"diagonal pivoting of G^T G / n + I of that block",
                    "n": n, "l2": "inputs larger than L2" if 8 * n * n > 129e6 else "in L2",
                    "parallelism": f"replicas x{world}"},
         "tflops_eq": flops * value / world / 1e12,
         "residual_AX_minus_I": resid, "status": info,
         "one_condition": {"value": cond, "seconds": t_cond},
         "lu_full_pivoting": dict(lu_full, cpu_sample=cpu_full if cpu else None),
+        "cholesky_diagonal_pivoting": dict(chol_piv, cpu_sample=cpu_chp if cpu else None),
         "roofline": {"bound": "fp64 FMA pipe (tcgen05 has no FP64 kind)",
                      "achieved": flops * value / world / 1e12, "peak": fp64_peak,
                      "unit": "TFLOP/s", "frac": flops * value / world / 1e12 / fp64_peak,
