@@ -704,7 +704,20 @@ __device__ __noinline__ int cta_lu(T* W, int n, int ld, int nb, int ib, int* piv
             const T l = panel[r + j * mp] * inv;
             panel[r + j * mp] = l;
             const T lr = rnd(l, lowp);
-            for (int c = j + 1; c < jb; ++c)
+            // columns in groups of eight: the loads issued together, then the
+            // fmas and stores (same arithmetic, one latency per group)
+            int c = j + 1;
+            for (; c + 7 < jb; c += 8) {
+              T u[8], v[8];
+#pragma unroll
+              for (int e = 0; e < 8; ++e) {
+                u[e] = panel[j + (c + e) * mp];
+                v[e] = panel[r + (c + e) * mp];
+              }
+#pragma unroll
+              for (int e = 0; e < 8; ++e) panel[r + (c + e) * mp] = fma(-lr, rnd(u[e], lowp), v[e]);
+            }
+            for (; c < jb; ++c)
               panel[r + c * mp] = fma(-lr, rnd(panel[j + c * mp], lowp), panel[r + c * mp]);
           }
         }
