@@ -1163,23 +1163,26 @@ __device__ void cta_gemv_rows(const double* __restrict__ A, int n, const double*
     // U columns' loads issued together: RG * U independent coalesced loads
     // in flight per thread (one CTA per SM is latency-bound otherwise)
     for (int j0 = 0; j0 < n; j0 += U) {
-      double a[U][RG];
+      // the block's A and x values all loaded before any fma (x loads placed
+      // after the fmas would each wait a full round trip)
+      double a[U][RG], x[U][QM];
 #pragma unroll
       for (int u = 0; u < U; ++u) {
-        const long col = (long)min(j0 + u, n - 1) * n;
+        const int jj = min(j0 + u, n - 1);
+        const long col = (long)jj * n;
 #pragma unroll
         for (int g = 0; g < RG; ++g) a[u][g] = A[rr[g] + col];
+#pragma unroll
+        for (int c = 0; c < QM; ++c) x[u][c] = c < q ? X[jj + (long)c * n] : 0.0;
       }
 #pragma unroll
       for (int u = 0; u < U; ++u) {
-        if (j0 + u >= n) break;
-        double x[QM];
+        if (j0 + u < n) {
 #pragma unroll
-        for (int c = 0; c < QM; ++c) x[c] = c < q ? X[j0 + u + (long)c * n] : 0.0;
+          for (int g = 0; g < RG; ++g)
 #pragma unroll
-        for (int g = 0; g < RG; ++g)
-#pragma unroll
-          for (int c = 0; c < QM; ++c) acc[g][c] = fma(a[u][g], x[c], acc[g][c]);
+            for (int c = 0; c < QM; ++c) acc[g][c] = fma(a[u][g], x[u][c], acc[g][c]);
+        }
       }
     }
 #pragma unroll
@@ -1208,11 +1211,11 @@ __device__ __noinline__ void cta_gemv(const double* A, int n, const double* X, i
     else if (n <= 4 * kBT) cta_gemv_rows<4, 2, 4>(A, n, X, q, B, Y);
     else cta_gemv_rows<8, 2, 4>(A, n, X, q, B, Y);
   } else if (q <= 4) {
-    if (n <= kBT) cta_gemv_rows<1, 4, 16>(A, n, X, q, B, Y);
+    if (n <= kBT) cta_gemv_rows<1, 4, 8>(A, n, X, q, B, Y);
     else if (n <= 2 * kBT) cta_gemv_rows<2, 4, 8>(A, n, X, q, B, Y);
     else cta_gemv_rows<4, 4, 4>(A, n, X, q, B, Y);
   } else {
-    if (n <= kBT) cta_gemv_rows<1, kBQ, 8>(A, n, X, q, B, Y);
+    if (n <= kBT) cta_gemv_rows<1, kBQ, 4>(A, n, X, q, B, Y);
     else if (n <= 2 * kBT) cta_gemv_rows<2, kBQ, 4>(A, n, X, q, B, Y);
     else cta_gemv_rows<4, kBQ, 2>(A, n, X, q, B, Y);
   }
