@@ -978,12 +978,26 @@ __device__ __forceinline__ void cta_solve_rows_g(const S* W, int ld, T* x, int n
         rr[g] = r_lo + (i < rows ? i : rows - 1);  // clamped: loads stay in bounds
         acc[g] = T(0);
       }
-#pragma unroll 4
-      for (int jj = 0; jj < jb; ++jj) {
-        const T xv = xb[jj];
-        const S* wc = W + (long)(j0 + jj) * ld;
+      // U columns' W and x values loaded together, then the fmas in the
+      // same order (loads left between the fmas would each wait a round trip)
+      constexpr int U = RG >= 4 ? 4 : 16 / RG;
+      for (int jj0 = 0; jj0 < jb; jj0 += U) {
+        S wv[U][RG];
+        T xv[U];
 #pragma unroll
-        for (int g = 0; g < RG; ++g) acc[g] = fma(-(T)wc[rr[g]], xv, acc[g]);
+        for (int u = 0; u < U; ++u) {
+          const int jc = min(jj0 + u, jb - 1);
+          const S* wc = W + (long)(j0 + jc) * ld;
+#pragma unroll
+          for (int g = 0; g < RG; ++g) wv[u][g] = wc[rr[g]];
+          xv[u] = xb[jc];
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+          if (jj0 + u < jb) {
+#pragma unroll
+            for (int g = 0; g < RG; ++g) acc[g] = fma(-(T)wv[u][g], xv[u], acc[g]);
+          }
       }
 #pragma unroll
       for (int g = 0; g < RG; ++g) {
