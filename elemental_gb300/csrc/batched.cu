@@ -380,15 +380,15 @@ __device__ void cta_trsm_u12(const T* L, int mp, T* W0, int ld, int jb, int n2, 
 
 // ---- tensor-core trailing update ----------------------------------------------
 // C[m x nc] -= P[m x jb] * Q[jb x nc] on the 5th-generation tensor cores,
-// inside one CTA: P is the panel's A21 in shared memory (ld ldp), Q = U12 and
-// C = A22 in the CTA's global workspace (ld ldq / ldc).  For each 128 x 64
-// C tile the CTA writes the operands into 128-byte-swizzled K-major tiles
-// (the layout TMA's SWIZZLE_128B produces: 8-row groups of 1024 bytes, the
-// 16-byte chunk c of row r stored at chunk c ^ (r & 7)), thread 0 issues
-// tcgen05.mma into a 128 x 64 FP32 accumulator in TMEM and commits to an
-// mbarrier, and all 8 warps read the accumulator back (tcgen05.ld, warp w
-// owns TMEM lanes 32 (w % 4).. and column half w / 4) and subtract it from
-// C, whose loads were issued before the wait.
+// inside one CTA: P is A21 and Q = U12, C = A22, all in the CTA's global
+// workspace (ld ldp / ldq / ldc).  For each 128 x 128 C tile the CTA writes
+// the operands into 128-byte-swizzled K-major tiles (the layout TMA's
+// SWIZZLE_128B produces: 8-row groups of 1024 bytes, the 16-byte chunk c of
+// row r stored at chunk c ^ (r & 7)), thread 0 issues tcgen05.mma into one of
+// two 128 x 128 FP32 accumulators in TMEM and commits to an mbarrier, and all
+// 8 warps read the accumulator back (tcgen05.ld, warp w owns TMEM lanes
+// 32 (w % 4).. and column half w / 4) and subtract it from C, staged in
+// shared memory by cp.async one tile ahead (pipeline in cta_gemm_update_tc).
 //   FP32 factors: TF32 split, C -= Ahi Bhi + Ahi Blo + Alo Bhi (~FP32);
 //   BF16 factors: one kind::f16 pass on BF16 operands (FP32 accumulation).
 // K = jb <= 32 (TF32) or <= 64 (BF16): one 128-byte K row per operand row.
@@ -1766,7 +1766,7 @@ batched_solve_kernel(BatchParams p) {
   __shared__ KryShared ks;
   const int q = p.q;
   // tensor-core update state: operand tiles after the panel budget (1024-
-  // byte aligned), the commit barrier, a 64-column TMEM accumulator
+  // byte aligned), the commit barrier, two 128-column TMEM accumulators
   unsigned char* tc_tiles = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + kSmemPanel + 1023) & ~uintptr_t(1023));
   if (threadIdx.x == 0) {
