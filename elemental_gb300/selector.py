@@ -13,7 +13,7 @@ argmax (written on the device by ElGBMLPForward) is handed to the batched
 plan as its run-time precision array: features -> MLP -> solve run as three
 device launches with no host round trip.  Whatever the choice, refinement
 that stalls falls back BF16 -> FP32 -> FP64, so the FP64 LU is both the
-fallback and, through its FP64 residual, the judge of every result's error.
+fallback and, through its FP64 residual, the arbiter of every result's error.
 
 Training data are outcomes the solver itself generates: every training
 system is solved once per low precision with the fallback switched off, and
