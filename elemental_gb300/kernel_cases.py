@@ -7,6 +7,7 @@ can skip the first launch of the kernel it targets).
     python -m elemental_gb300.kernel_cases refine --n 8192 --nrhs 16
     python -m elemental_gb300.kernel_cases lu64 --n 4096
     python -m elemental_gb300.kernel_cases batched --n 1024 --count 152 --precision fp32
+    python -m elemental_gb300.kernel_cases lufull --n 2048
 
 Each prints one JSON line with the event-timed duration of the measured
 call and its algorithmic work.  Inputs are seeded N(0, 1), generated on the
@@ -121,8 +122,24 @@ def case_batched(ctx, a):
     return out
 
 
+def case_lufull(ctx, a):
+    """El::LU(A, P, Q) with full pivoting (src/lapack_like/factor/LU/Full.hpp):
+    two kernels per step (swap / update + next pivot search)."""
+    g = torch.Generator(device="cuda").manual_seed(a.seed)
+    A0 = D.colmajor(a.n, a.n)
+    A0.copy_(torch.randn(a.n, a.n, device="cuda", generator=g, dtype=torch.float64).t())
+    A = D.colmajor(a.n, a.n)
+    A.copy_(A0)
+    ctx.lu_full(A)
+    A.copy_(A0)
+    ms = _timed(lambda: ctx.lu_full(A))
+    return dict(case="lufull", n=a.n, ms=ms, gflops=2.0 / 3.0 * a.n ** 3 / (ms * 1e-3) / 1e9,
+                trailing_traffic_gbs=16.0 * a.n ** 3 / 3.0 / (ms * 1e-3) / 1e9,
+                status=ctx.status())
+
+
 CASES = {"tc_gemm": case_tc_gemm, "lu": case_lu, "lu64": case_lu64, "refine": case_refine,
-         "batched": case_batched}
+         "batched": case_batched, "lufull": case_lufull}
 
 
 def main(argv=None):
