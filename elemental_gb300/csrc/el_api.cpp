@@ -260,15 +260,18 @@ char* Dev(size_t bytes) {
 
 size_t Al(size_t b) { return (b + 255) & ~size_t(255); }
 
+// A synchronous copy from pageable memory may return once the data is staged,
+// before its DMA into device memory ends, and the factor-and-solve work runs
+// on the context's non-blocking stream, which is not ordered after the legacy
+// default stream: the legacy stream is drained before any launch reads the
+// upload (this also covers the small pivot copies issued just before it).
 template <typename T>
-void Upload(ElGBContext ctx, T* d, const Matrix<T>& A) {
+void Upload(ElGBContext, T* d, const Matrix<T>& A) {
   if (A.Height() == 0 || A.Width() == 0) return;
-  void* stream = nullptr;
-  (void)stream;
   Check(cudaMemcpy2D(d, sizeof(T) * A.Height(), A.LockedBuffer(), sizeof(T) * A.LDim(),
                      sizeof(T) * A.Height(), A.Width(), cudaMemcpyHostToDevice),
         "upload");
-  (void)ctx;
+  Check(cudaStreamSynchronize(cudaStreamLegacy), "upload");
 }
 
 template <typename T>
