@@ -2099,6 +2099,9 @@ cudaError_t batched_plan(Context* ctx, int count, const int* h_n, const int* h_k
     e = cudaMemcpy(P->d_desc, desc.data(), sizeof(SysDesc) * count, cudaMemcpyHostToDevice);
   if (e == cudaSuccess)
     e = cudaMemcpy(P->d_order, order.data(), sizeof(int) * count, cudaMemcpyHostToDevice);
+  // the memset and the pageable copies above ran on the legacy stream, which
+  // the stream the plan later launches on need not wait for: drain it now
+  if (e == cudaSuccess) e = cudaStreamSynchronize(cudaStreamLegacy);
   if (e != cudaSuccess) {
     batched_destroy(P);
     return e;

@@ -1111,12 +1111,15 @@ int ElGBCreate(ElGBContext* out, int device) {
       cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
       cudaMalloc(&c->status, sizeof(elgb::DevStatus)) != cudaSuccess ||
-      cudaMallocHost(&c->h_status, sizeof(elgb::DevStatus)) != cudaSuccess) {
+      cudaMallocHost(&c->h_status, sizeof(elgb::DevStatus)) != cudaSuccess ||
+      // zeroed on the legacy stream, which the context's non-blocking
+      // streams do not wait for: drained before the first launch
+      cudaMemset(c->status, 0, sizeof(elgb::DevStatus)) != cudaSuccess ||
+      cudaStreamSynchronize(cudaStreamLegacy) != cudaSuccess) {
     delete c;
     return elgb::kElRuntimeError;
   }
   c->stream = c->own_stream;
-  cudaMemset(c->status, 0, sizeof(elgb::DevStatus));
   *out = c;
   return 0;
 }
