@@ -72,14 +72,11 @@ cudaError_t Context::ensure(size_t bytes) {
   if (arena) cudaFree(arena);
   arena = nullptr;
   arena_bytes = 0;
-  size_t want = std::max(bytes, arena_bytes * 2);
-  e = cudaMalloc(&arena, want);
-  if (e != cudaSuccess) {
-    e = cudaMalloc(&arena, bytes);
-    if (e != cudaSuccess) return e;
-    want = bytes;
-  }
-  arena_bytes = want;
+  // sized exactly: the largest users (an n = 32768 FP32 copy, the refinement
+  // vectors) hold gigabytes, and slack would come out of the caller's HBM
+  e = cudaMalloc(&arena, bytes);
+  if (e != cudaSuccess) return e;
+  arena_bytes = bytes;
   return cudaSuccess;
 }
 
