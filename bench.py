@@ -365,6 +365,13 @@ def gpu_arm(args, rank, world, local_rank):
         "achieved_gbs": prof["bytes"] / (prof["ms"] * 1e-3) / 1e9 if prof["ms"] > 0 else None,
         "share_of_step_time": prof["ms"] * 1e-3 / tmax if tmax > 0 else None,
     }
+    # the operand kind's own ceiling on the same tensor pipe: TF32 issues at
+    # half the bf16 rate, TF32x3 issues three TF32 products per update, E4M3
+    # at twice the bf16 rate
+    per_bf16 = {"fp32": 6.0, "tf32": 2.0, "bf16": 1.0, "fp8": 0.5}.get(args.precision)
+    if per_bf16 and peak and tf_achieved:
+        roofline["operand_ceiling_tflops"] = peak / per_bf16
+        roofline["frac_of_operand_ceiling"] = tf_achieved * per_bf16 / peak
     breakdown = {k: {"launches": v["launches"], "ms_per_step": v["ms"] / args.steps}
                  for k, v in prof["by_kernel"].items()}
     cpu = None
