@@ -17,7 +17,8 @@ lu::SolveAfter over OpenBLAS, all host threads) on a bounded sample.
 Other workloads (`--workload`): `batched` (4096 uneven LU / Cholesky systems
 in one persistent launch), `selector` (10,000 conditioned systems through the
 learned precision selector), `inverse` (El::Inverse and El::OneCondition of
-one n = 8192 FP64 matrix).
+one n = 8192 FP64 matrix), `cholesky` (plain FP64 El::HPDSolve = potrf + potrs
+of one SPD n = 16384 system G^T G / n + I with 16 RHS).
 
 `--impl reference` times the CPU reference arm alone.  Under torchrun each
 rank solves its own system (replicas; the factorization does not shard).
@@ -51,7 +52,8 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--n", type=int, default=None,
-                   help="matrix size (default 32768 for lu-ir, 8192 for inverse)")
+                   help="matrix size (default 32768 for lu-ir, 8192 for inverse, 16384 for "
+                        "cholesky)")
     p.add_argument("--nrhs", type=int, default=16)
     p.add_argument("--precision", default="fp32",
                    choices=["fp32", "tf32", "bf16", "fp8", "fp64"])
@@ -63,11 +65,12 @@ def parse():
     p.add_argument("--cpu-n", type=int, default=8192)
     p.add_argument("--seed", type=int, default=20261204 + 1)
     p.add_argument("--workload", default="lu-ir",
-                   choices=["lu-ir", "batched", "selector", "inverse"],
+                   choices=["lu-ir", "batched", "selector", "inverse", "cholesky"],
                    help="lu-ir: one large mixed-precision solve (default); batched: 4096 "
                         "uneven LU/Cholesky systems in one launch; selector: 10,000 "
                         "conditioned systems through the learned precision selector; "
-                        "inverse: El::Inverse and El::OneCondition of one FP64 matrix")
+                        "inverse: El::Inverse and El::OneCondition of one FP64 matrix; "
+                        "cholesky: plain FP64 El::HPDSolve of one SPD system")
     p.add_argument("--count", type=int, default=0, help="systems (batched / selector)")
     p.add_argument("--train-count", type=int, default=3000, help="selector training systems")
     return p.parse_args()
@@ -900,10 +903,146 @@ def inverse_arm(args, rank, world, local_rank):
     return 0
 
 
+# ---------------------------------------------------------------------------
+# plain FP64 El::HPDSolve (potrf + potrs) of one SPD system
+# ---------------------------------------------------------------------------
+def cholesky_arm(args, rank, world, local_rank):
+    """El::HPDSolve(LOWER, NORMAL, A, B) (src/lapack_like/solve/HPD.cpp:47-55):
+    a copy of A, El::Cholesky (LowerVariant3Blocked) and cholesky::SolveAfter
+    on A = G^T G / n + I, G iid N(0,1), B n x nrhs iid N(0,1).  One step = one
+    HPDSolve; the FP64 FMA pipe bounds it (tcgen05 has no FP64 kind)."""
+    import numpy as np
+
+    import elemental_gb300 as El
+    from elemental_gb300 import device as D
+
+    import torch
+
+    dist, barrier, tmax_of = _dist_setup(world, local_rank)
+    ctx = D.context(local_rank)
+    n, q = args.n, args.nrhs
+    g = torch.Generator(device="cuda")
+    g.manual_seed(args.seed + 7919 * rank)
+    # input synthesis, not timed: G^T G in FP32 (exactly symmetric after the
+    # averaging below), then FP64 + I, so that every eigenvalue is >= ~1
+    G = torch.randn(n, n, generator=g, device="cuda", dtype=torch.float32)
+    S = (G.t() @ G).double().div_(n)
+    del G
+    S = S.add_(S.t().clone()).mul_(0.5)
+    S.diagonal().add_(1.0)
+    A0 = D.colmajor(n, n)
+    A0.copy_(S)
+    del S
+    B0 = D.colmajor(n, q)
+    B0.copy_(torch.randn(q, n, generator=g, device="cuda", dtype=torch.float64).t())
+    X = D.colmajor(n, q)
+    flops = 1.0 / 3.0 * n ** 3 + 2.0 * n * n * q
+
+    def step():
+        X.copy_(B0)
+        ctx.hpd_solve(A0, X, uplo=0, nb=args.nb)
+
+    for _ in range(max(args.warmup, 0)):
+        step()
+    barrier()
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    l0 = ctx.launches()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    e1.synchronize()
+    barrier()
+    launches = ctx.launches() - l0
+    clk = clocks.stop()
+    t = tmax_of(e0.elapsed_time(e1) / 1e3)
+    info = ctx.status()
+    berr = ctx.backward_error(A0, X, B0)
+    # end to end through Elemental's C ABI on pinned host memory
+    e2e = None
+    if args.e2e == "on":
+        Ah = torch.empty((n, n), dtype=torch.float64, pin_memory=True)
+        Ah.copy_(A0.t())
+        Bh0 = torch.empty((q, n), dtype=torch.float64, pin_memory=True)
+        Bh0.copy_(B0.t())
+        Bh = torch.empty((q, n), dtype=torch.float64, pin_memory=True)
+        Am = El.Matrix(Ah.numpy().T)
+        Bh.copy_(Bh0)
+        Bm = El.Matrix(Bh.numpy().T)
+        El.HPDSolve(Am, Bm)
+        te = 0.0
+        for _ in range(args.steps):
+            Bh.copy_(Bh0)
+            t0 = time.perf_counter()
+            El.HPDSolve(Am, Bm)
+            te += time.perf_counter() - t0
+        Xd = X.cpu().numpy()
+        e2e = {"value": args.steps * world / tmax_of(te), "unit": "solves/s",
+               "h2d_bytes_per_step": 8 * n * n + 8 * n * q, "d2h_bytes_per_step": 8 * n * q,
+               "api": "ElHPDSolve_d (El::Matrix handles on pinned host memory)",
+               "max_abs_diff_vs_device_run": float(np.abs(Bm.array - Xd).max())}
+        del Am, Bm, Ah, Bh, Bh0
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return 0
+    cpu = None
+    if args.cpu_baseline == "on":
+        from oracle import oracle as O
+
+        ns = min(4096, n)
+        threads = os.cpu_count() or 1
+        O.set_threads(threads)
+        rng = np.random.default_rng(args.seed)
+        Gs = rng.standard_normal((ns, ns))
+        Ss = Gs.T @ Gs / ns + np.eye(ns)
+        Bs = rng.standard_normal((ns, q))
+        O.hpd_solve(Ss, Bs, "L", nb=128)
+        t0 = time.perf_counter()
+        Xs = O.hpd_solve(Ss, Bs, "L", nb=128)
+        tc = time.perf_counter() - t0
+        fs = 1.0 / 3.0 * ns ** 3 + 2.0 * ns * ns * q
+        cpu = {"value": fs / flops / tc, "unit": "solves/s", "cores": threads, "kind": "port",
+               "sample": f"El::HPDSolve restatement (El::Cholesky LowerVariant3Blocked + "
+                         f"cholesky::SolveAfter, OpenBLAS) at n={ns}, {q} RHS, {threads} "
+                         f"threads: {tc:.3f} s, scaled to n={n} by the flop count",
+               "backward_error_sample": float(O.backward_error(Ss, Xs, Bs))}
+    value = args.steps * world / t
+    fp64_peak = ctx.fp64_peak_tflops()
+    achieved = flops * value / world / 1e12
+    line = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: SPD G^T G / n + I, G and B seeded iid N(0,1) (device Philox "
+                "generator)",
+        "config": {"workload": f"plain FP64 El::HPDSolve (copy + potrf + potrs, lower) of one "
+                               f"n={n} SPD system, {q} RHS",
+                   "n": n, "nrhs": q,
+                   "l2": "inputs larger than L2" if 8 * n * n > 129e6 else "in L2",
+                   "parallelism": f"replicas x{world}"},
+        "tflops_eq": achieved, "backward_error": berr,
+        "backward_error_bound_n_eps64": n * EPS64, "status": info,
+        "roofline": {"bound": "fp64 FMA pipe (tcgen05 has no FP64 kind)",
+                     "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                     "frac": achieved / fp64_peak if fp64_peak else None,
+                     "peak_source": "FP64 FMA throughput probe (ElGBProbeFP64Peak) on this GPU",
+                     "traffic": None},
+        "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": launches, "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
 def main():
     args = parse()
     if args.n is None:
-        args.n = 8192 if args.workload == "inverse" else 32768
+        args.n = {"inverse": 8192, "cholesky": 16384}.get(args.workload, 32768)
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
@@ -915,6 +1054,8 @@ def main():
         return selector_arm(args, rank, world, local_rank)
     if args.workload == "inverse":
         return inverse_arm(args, rank, world, local_rank)
+    if args.workload == "cholesky":
+        return cholesky_arm(args, rank, world, local_rank)
     return gpu_arm(args, rank, world, local_rank)
 
 
