@@ -71,6 +71,9 @@ def parse():
                         "conditioned systems through the learned precision selector; "
                         "inverse: El::Inverse and El::OneCondition of one FP64 matrix; "
                         "cholesky: plain FP64 El::HPDSolve of one SPD system")
+    p.add_argument("--kappa", type=float, default=0.0,
+                   help="lu-ir: A = U diag(sigma) V^T with U, V Haar and cond_2(A) = kappa "
+                        "(0, the default: A iid N(0,1))")
     p.add_argument("--count", type=int, default=0, help="systems (batched / selector)")
     p.add_argument("--train-count", type=int, default=3000, help="selector training systems")
     return p.parse_args()
@@ -205,6 +208,32 @@ def reference_arm(args, rank):
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
+def haar_conditioned(n, kappa, g, device="cuda"):
+    """A = U diag(sigma) V^T with sigma_i = kappa^(-i/(n-1)), so ||A||_2 = 1
+    and cond_2(A) = kappa: U, V the sign-fixed Q factors of Gaussian QRs (the
+    construction of src/matrices/random/misc/Haar.cpp:14-21), run in FP32 and
+    widened exactly to FP64 (orthogonal to ~1e-6, so cond_2(A) = kappa to
+    ~1e-5 relative); the product is formed in FP64 so that singular values far
+    below FP32's unit roundoff survive.  Returns a row-major n x n FP64 tensor
+    (input synthesis, not timed)."""
+    import torch
+
+    i = torch.arange(n, dtype=torch.float64, device=device)
+    sig = torch.pow(torch.full_like(i, float(kappa)), -i / max(n - 1, 1))
+    Q = []
+    for _ in range(2):
+        G = torch.randn(n, n, generator=g, device=device, dtype=torch.float32)
+        Qf, R = torch.linalg.qr(G)
+        del G
+        Qf.mul_(torch.sign(torch.diagonal(R))[None, :])
+        del R
+        Q.append(Qf.double())
+        del Qf
+    U, V = Q
+    U.mul_(sig[None, :])
+    return U @ V.t()
+
+
 def gpu_arm(args, rank, world, local_rank):
     import numpy as np
     import torch
@@ -229,7 +258,10 @@ def gpu_arm(args, rank, world, local_rank):
     g = torch.Generator(device="cuda")
     g.manual_seed(args.seed + 7919 * rank)
     A = D.colmajor(n, n)
-    A.copy_(torch.randn(n, n, generator=g, device="cuda", dtype=torch.float64).t())
+    if args.kappa > 0:
+        A.copy_(haar_conditioned(n, args.kappa, g))
+    else:
+        A.copy_(torch.randn(n, n, generator=g, device="cuda", dtype=torch.float64).t())
     B = D.colmajor(n, q)
     B.copy_(torch.randn(q, n, generator=g, device="cuda", dtype=torch.float64).t())
     X = D.colmajor(n, q)
@@ -399,11 +431,17 @@ def gpu_arm(args, rank, world, local_rank):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": {"fp32": "f64+tf32x3", "tf32": "f64+tf32", "bf16": "f64+bf16", "fp8": "f64+e4m3",
                   "fp64": "f64"}[args.precision],
-        "data": "synthetic: seeded iid N(0,1) FP64 (device Philox generator)",
+        "data": ("synthetic: seeded iid N(0,1) FP64 (device Philox generator)"
+                 if args.kappa <= 0 else
+                 f"synthetic: seeded A = U diag(sigma) V^T, U, V Haar, cond_2(A) = "
+                 f"{args.kappa:g}; B iid N(0,1) (device Philox generator)"),
         "config": {"workload": f"mixed-precision {args.method.upper()} ({prec_desc}, FP64 "
-                               f"residual) of A X = B, n={n}, {q} RHS, A,B iid N(0,1), to "
-                               f"backward error <= n*eps64",
+                               f"residual) of A X = B, n={n}, {q} RHS, "
+                               + ("A,B iid N(0,1)" if args.kappa <= 0 else
+                                  f"A Haar-conditioned kappa={args.kappa:g}")
+                               + ", to backward error <= n*eps64",
                    "n": n, "nrhs": q, "precision": args.precision, "method": args.method,
+                   "kappa": args.kappa if args.kappa > 0 else None,
                    "nb": args.nb or 512, "l2": "inputs larger than L2 (A is 8 GiB)",
                    "parallelism": f"replicas x{world}"},
         "tflops_eq": value * flops_per_solve(n, q) / 1e12,

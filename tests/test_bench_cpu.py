@@ -39,3 +39,35 @@ def test_workload_sizes_resolve():
         assert a.n is None and a.workload == "inverse"
     finally:
         sys.argv = old
+
+
+def test_cholesky_workload_and_kappa_option_parse():
+    sys.path.insert(0, ROOT)
+    import bench
+
+    old = sys.argv
+    try:
+        sys.argv = ["bench.py", "--workload", "cholesky"]
+        a = bench.parse()
+        assert a.workload == "cholesky" and a.kappa == 0.0
+        sys.argv = ["bench.py", "--kappa", "1e8"]
+        assert bench.parse().kappa == 1e8
+    finally:
+        sys.argv = old
+
+
+def test_haar_conditioned_has_the_requested_condition_number():
+    """The Haar-conditioned headline input: ||A||_2 = 1, cond_2(A) = kappa."""
+    import numpy as np
+    import torch
+
+    sys.path.insert(0, ROOT)
+    import bench
+
+    for n, kappa in ((40, 1e2), (120, 1e8)):
+        g = torch.Generator(device="cpu")
+        g.manual_seed(n)
+        s = np.linalg.svd(bench.haar_conditioned(n, kappa, g, device="cpu").numpy(),
+                          compute_uv=False)
+        assert abs(s[0] - 1.0) <= 1e-5
+        assert abs(s[0] / s[-1] / kappa - 1.0) <= 1e-4
