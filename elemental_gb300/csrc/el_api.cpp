@@ -102,18 +102,24 @@ template class Matrix<float>;
 template class Matrix<double>;
 
 // ---------------------------------------------------------------------------
-// Permutation (swap sequence with implicit origins 0, 1, 2, ...;
-// src/lapack_like/perm/Permutation.cpp:166-250, 544-631, 731-745)
+// Permutation: a swap sequence, origins implicit (0, 1, 2, ...) until a swap
+// names another origin (src/lapack_like/perm/Permutation.cpp:166-303,
+// 436-450, 544-631, 731-745).  It never becomes an arbitrary permutation:
+// past the reserved count the sequence grows.
 // ---------------------------------------------------------------------------
 void Permutation::Empty() {
   size_ = 0;
   numSwaps_ = 0;
+  implicit_ = true;
   dests_.clear();
+  origins_.clear();
 }
 
 void Permutation::MakeIdentity(Int size) {
   size_ = size;
   numSwaps_ = 0;
+  implicit_ = true;
+  origins_.clear();
 }
 
 void Permutation::ReserveSwaps(Int maxSwaps) {
@@ -123,17 +129,48 @@ void Permutation::ReserveSwaps(Int maxSwaps) {
 void Permutation::Swap(Int origin, Int dest) {
   if (origin < 0 || origin >= size_ || dest < 0 || dest >= size_)
     throw std::logic_error("Permutation::Swap: index out of range");
-  if (origin != numSwaps_)
-    throw std::logic_error("Permutation::Swap: only implicit-origin swap sequences");
   if ((Int)dests_.size() <= numSwaps_) dests_.resize(numSwaps_ + 1);
+  if (implicit_ && origin != numSwaps_) {
+    implicit_ = false;
+    origins_.resize(numSwaps_);
+    for (Int k = 0; k < numSwaps_; ++k) origins_[k] = k;
+  }
+  if (!implicit_) {
+    if ((Int)origins_.size() <= numSwaps_) origins_.resize(numSwaps_ + 1);
+    origins_[numSwaps_] = origin;
+  }
   dests_[numSwaps_++] = dest;
+}
+
+void Permutation::SwapSequence(const Permutation& P, Int offset) {
+  const Int count = P.numSwaps_;  // P may be *this
+  for (Int k = 0; k < count; ++k) Swap(P.Origin(k) + offset, P.dests_[k] + offset);
+}
+
+void Permutation::SwapSequence(const Matrix<Int>& swapOrigins, const Matrix<Int>& swapDests,
+                               Int offset) {
+  if (swapOrigins.Height() != swapDests.Height())
+    throw std::logic_error("Permutation::SwapSequence: origins and destinations differ in size");
+  for (Int k = 0; k < swapDests.Height(); ++k)
+    Swap(swapOrigins.Get(k, 0) + offset, swapDests.Get(k, 0) + offset);
+}
+
+void Permutation::ImplicitSwapSequence(const Matrix<Int>& swapDests, Int offset) {
+  const Int before = numSwaps_;
+  for (Int k = 0; k < swapDests.Height(); ++k) Swap(before + k, swapDests.Get(k, 0) + offset);
 }
 
 bool Permutation::Parity() const {
   bool p = false;
   for (Int j = 0; j < numSwaps_; ++j)
-    if (dests_[j] != j) p = !p;
+    if (dests_[j] != Origin(j)) p = !p;
   return p;
+}
+
+const Matrix<Int> Permutation::SwapOrigins() const {
+  Matrix<Int> o(numSwaps_, 1);
+  for (Int j = 0; j < numSwaps_; ++j) o(j, 0) = Origin(j);
+  return o;
 }
 
 const Matrix<Int> Permutation::SwapDestinations() const {
@@ -153,13 +190,14 @@ static void RowSwapHost(Matrix<T>& A, Int to, Int from) {
 template <typename T>
 void Permutation::PermuteRows(Matrix<T>& A, Int offset) const {
   if (A.Height() == 0 || A.Width() == 0) return;
-  for (Int j = 0; j < numSwaps_; ++j) RowSwapHost(A, j + offset, dests_[j] + offset);
+  for (Int j = 0; j < numSwaps_; ++j) RowSwapHost(A, Origin(j) + offset, dests_[j] + offset);
 }
 
 template <typename T>
 void Permutation::InversePermuteRows(Matrix<T>& A, Int offset) const {
   if (A.Height() == 0 || A.Width() == 0) return;
-  for (Int j = numSwaps_ - 1; j >= 0; --j) RowSwapHost(A, j + offset, dests_[j] + offset);
+  for (Int j = numSwaps_ - 1; j >= 0; --j)
+    RowSwapHost(A, Origin(j) + offset, dests_[j] + offset);
 }
 
 void Permutation::ExplicitVector(Matrix<Int>& p) const {
@@ -168,9 +206,33 @@ void Permutation::ExplicitVector(Matrix<Int>& p) const {
   PermuteRows(p);
 }
 
+std::vector<Int> Permutation::ImplicitSwapDests(Int n) const {
+  if (size_ > n) throw std::logic_error("Permutation is larger than the row count");
+  std::vector<Int> d(n);
+  if (implicit_) {
+    for (Int i = 0; i < n; ++i) d[i] = i < numSwaps_ ? dests_[i] : i;
+    return d;
+  }
+  // row k of P A is row p[k] of A: swap row k with the row now holding p[k]
+  Matrix<Int> p;
+  ExplicitVector(p);
+  std::vector<Int> lab(n), pos(n);
+  for (Int i = 0; i < n; ++i) lab[i] = pos[i] = i;
+  for (Int k = 0; k < n; ++k) {
+    const Int j = pos[k < size_ ? p.Get(k, 0) : k];
+    d[k] = j;
+    std::swap(lab[k], lab[j]);
+    pos[lab[k]] = k;
+    pos[lab[j]] = j;
+  }
+  return d;
+}
+
 void Permutation::SetSwapSequence(Int size, const Int* dests, Int numSwaps) {
   size_ = size;
   numSwaps_ = numSwaps;
+  implicit_ = true;
+  origins_.clear();
   dests_.assign(dests, dests + numSwaps);
 }
 
@@ -259,6 +321,16 @@ char* Dev(size_t bytes) {
 }
 
 size_t Al(size_t b) { return (b + 255) & ~size_t(255); }
+
+// The swap destinations (origins implicit 0, 1, ..., n - 1) that replay P
+// on n rows, as the device's swap kernels take them; every destination is
+// checked to lie in [0, n) before it can reach the device.
+std::vector<int> DevicePivots(const Permutation& P, Int n) {
+  const std::vector<Int> d = P.ImplicitSwapDests(n);
+  for (Int i = 0; i < n; ++i)
+    if (d[i] < 0 || d[i] >= n) throw std::logic_error("Permutation swap out of range");
+  return std::vector<int>(d.begin(), d.end());
+}
 
 // A synchronous copy from pageable memory may return once the data is staged,
 // before its DMA into device memory ends, and the factor-and-solve work runs
@@ -528,8 +600,7 @@ void SolveAfter(Orientation orientation, const Matrix<F>& A, const Permutation& 
   F* dA = reinterpret_cast<F*>(base);
   F* dB = reinterpret_cast<F*>(base + sa);
   int* dP = reinterpret_cast<int*>(base + sa + sb);
-  std::vector<int> piv(n);
-  for (Int i = 0; i < n; ++i) piv[i] = i < P.NumSwaps() ? P.SwapDestBuffer()[i] : i;
+  const std::vector<int> piv = DevicePivots(P, n);
   Check(cudaMemcpy(dP, piv.data(), sizeof(int) * n, cudaMemcpyHostToDevice), "pivots");
   Upload(ctx, dA, A);
   Upload(ctx, dB, B);
@@ -555,11 +626,7 @@ void SolveAfter(Orientation orientation, const Matrix<F>& A, const Permutation& 
   F* dB = reinterpret_cast<F*>(base + sa);
   int* dP = reinterpret_cast<int*>(base + sa + sb);
   int* dQ = reinterpret_cast<int*>(base + sa + sb + sp);
-  std::vector<int> pv(n), qv(n);
-  for (Int i = 0; i < n; ++i) {
-    pv[i] = i < P.NumSwaps() ? P.SwapDestBuffer()[i] : i;
-    qv[i] = i < Q.NumSwaps() ? Q.SwapDestBuffer()[i] : i;
-  }
+  const std::vector<int> pv = DevicePivots(P, n), qv = DevicePivots(Q, n);
   Check(cudaMemcpy(dP, pv.data(), sizeof(int) * n, cudaMemcpyHostToDevice), "pivots");
   Check(cudaMemcpy(dQ, qv.data(), sizeof(int) * n, cudaMemcpyHostToDevice), "pivots");
   Upload(ctx, dA, A);
@@ -654,8 +721,7 @@ void SolveAfter(UpperOrLower uplo, Orientation orientation, const Matrix<F>& A,
   F* dA = reinterpret_cast<F*>(base);
   F* dB = reinterpret_cast<F*>(base + sa);
   int* dP = reinterpret_cast<int*>(base + sa + sb);
-  std::vector<int> pv(n);
-  for (Int i = 0; i < n; ++i) pv[i] = i < P.NumSwaps() ? P.SwapDestBuffer()[i] : i;
+  const std::vector<int> pv = DevicePivots(P, n);
   Check(cudaMemcpy(dP, pv.data(), sizeof(int) * n, cudaMemcpyHostToDevice), "pivots");
   Upload(ctx, dA, A);
   Upload(ctx, dB, B);
@@ -928,6 +994,9 @@ ElError ElPermutationReserveSwaps(ElPermutation P, ElInt maxSwaps) {
 }
 ElError ElPermutationSwap(ElPermutation P, ElInt origin, ElInt dest) {
   EL_GB_TRY(PP(P)->Swap(origin, dest))
+}
+ElError ElPermutationSwapSequence(ElPermutation P, ElConstPermutation PAppend, ElInt offset) {
+  EL_GB_TRY(PP(P)->SwapSequence(*CP(PAppend), offset))
 }
 ElError ElPermutationHeight(ElConstPermutation P, ElInt* h) { EL_GB_TRY(*h = CP(P)->Height()) }
 ElError ElPermutationWidth(ElConstPermutation P, ElInt* w) { EL_GB_TRY(*w = CP(P)->Width()) }

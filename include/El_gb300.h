@@ -87,6 +87,9 @@ ElError ElPermutationEmpty(ElPermutation P);
 ElError ElPermutationMakeIdentity(ElPermutation P, ElInt size);
 ElError ElPermutationReserveSwaps(ElPermutation P, ElInt maxSwaps);
 ElError ElPermutationSwap(ElPermutation P, ElInt origin, ElInt dest);
+/* include/El/core/Permutation.h:82-83: appends PAppend's swaps, shifted by offset */
+ElError ElPermutationSwapSequence(ElPermutation P, ElConstPermutation PAppend,
+                                  ElInt offset);
 ElError ElPermutationHeight(ElConstPermutation P, ElInt* height);
 ElError ElPermutationWidth(ElConstPermutation P, ElInt* width);
 ElError ElPermutationParity(ElConstPermutation P, bool* parity);

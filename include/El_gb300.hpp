@@ -100,14 +100,23 @@ class Permutation {
   void Empty();
   void MakeIdentity(Int size);
   void ReserveSwaps(Int maxSwaps);
+  // Appends the swap (origin, dest).  While every origin equals the number of
+  // swaps before it the origins stay implicit (0, 1, 2, ...); the first other
+  // origin makes them explicit (src/lapack_like/perm/Permutation.cpp:205-250).
   void Swap(Int origin, Int dest);
+  void SwapSequence(const Permutation& P, Int offset = 0);
+  void SwapSequence(const Matrix<Int>& swapOrigins, const Matrix<Int>& swapDests,
+                    Int offset = 0);
+  void ImplicitSwapSequence(const Matrix<Int>& swapDests, Int offset = 0);
 
   Int Height() const { return size_; }
   Int Width() const { return size_; }
   bool Parity() const;
   bool IsSwapSequence() const { return true; }
-  bool IsImplicitSwapSequence() const { return true; }
+  bool IsImplicitSwapSequence() const { return implicit_; }
 
+  // The origins of the recorded swaps (0, 1, ... when implicit).
+  const Matrix<Int> SwapOrigins() const;
   const Matrix<Int> SwapDestinations() const;
   template <typename T>
   void PermuteRows(Matrix<T>& A, Int offset = 0) const;
@@ -115,16 +124,24 @@ class Permutation {
   void InversePermuteRows(Matrix<T>& A, Int offset = 0) const;
   void ExplicitVector(Matrix<Int>& p) const;
 
-  // Number of swaps recorded and direct access to their destinations.
+  // Number of swaps recorded and direct access to their destinations (whose
+  // origins are 0, 1, ... only when IsImplicitSwapSequence()).
   Int NumSwaps() const { return numSwaps_; }
   const Int* SwapDestBuffer() const { return dests_.data(); }
   // Replaces the swap sequence by `numSwaps` destinations (origins 0..).
   void SetSwapSequence(Int size, const Int* dests, Int numSwaps);
+  // The destinations of an implicit-origin sequence of n swaps that permutes
+  // n rows exactly as this one does (n >= Height()).
+  std::vector<Int> ImplicitSwapDests(Int n) const;
 
  private:
+  Int Origin(Int k) const { return implicit_ ? k : origins_[k]; }
+
   Int size_ = 0;
   Int numSwaps_ = 0;
+  bool implicit_ = true;
   std::vector<Int> dests_;
+  std::vector<Int> origins_;  // used once the origins are explicit
 };
 
 Int Blocksize();

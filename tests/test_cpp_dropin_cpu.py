@@ -1,8 +1,9 @@
 """The C++ drop-in on the CPU: a program that includes include/El_gb300.hpp
 in place of Elemental's El.hpp compiles with g++, links libelgb300.so and runs
 the path's host-side pieces with the reference's semantics -- El::Matrix
-(owned, copied, attached views), El::Permutation swap sequences
-(src/lapack_like/perm/Permutation.cpp:205-250, 544-631, 731-745), the
+(owned, copied, attached views), El::Permutation swap sequences with implicit
+and explicit origins (src/lapack_like/perm/Permutation.cpp:205-303, 436-450,
+544-631, 731-745) and their implicit-origin form for the device, the
 blocksize stack (src/blas_like/blocksizes.cpp:37-60) and El::Write / El::Read
 (src/io/Write/Binary.hpp:17-37, src/io/Read/Binary.hpp:17-44).  No GPU
 call."""
@@ -72,6 +73,74 @@ int main(int argc, char** argv) {
     Read(R, base + ".xyz");
     return 11;
   } catch (const std::runtime_error&) {
+  }
+  // explicit origins from the first swap whose origin is not the swap count
+  Permutation E;
+  E.MakeIdentity(4);
+  E.Swap(2, 0);
+  E.Swap(3, 1);
+  E.Swap(1, 1);
+  if (E.IsImplicitSwapSequence()) return 12;
+  const Matrix<Int> eo = E.SwapOrigins();
+  if (eo.Height() != 3 || eo.Get(0, 0) != 2 || eo.Get(1, 0) != 3 || eo.Get(2, 0) != 1)
+    return 13;
+  if (E.Parity()) return 14;  // two non-trivial swaps
+  Matrix<Int> e;
+  E.ExplicitVector(e);  // [0 1 2 3] -> [2 1 0 3] -> [2 3 0 1]
+  if (e.Get(0, 0) != 2 || e.Get(1, 0) != 3 || e.Get(2, 0) != 0 || e.Get(3, 0) != 1) return 15;
+  // the implicit-origin sequence handed to the device replays the same rows
+  const std::vector<Int> di = E.ImplicitSwapDests(4);
+  Permutation I;
+  I.SetSwapSequence(4, di.data(), 4);
+  Matrix<Int> ie;
+  I.ExplicitVector(ie);
+  for (Int k = 0; k < 4; ++k)
+    if (ie.Get(k, 0) != e.Get(k, 0)) return 16;
+  Matrix<double> M(4, 1);
+  for (Int i = 0; i < 4; ++i) M.Set(i, 0, i);
+  E.PermuteRows(M);
+  for (Int i = 0; i < 4; ++i)
+    if (M.Get(i, 0) != e.Get(i, 0)) return 17;
+  E.InversePermuteRows(M);
+  for (Int i = 0; i < 4; ++i)
+    if (M.Get(i, 0) != i) return 18;
+  // appending another sequence with an offset, and appending to itself
+  Permutation F;
+  F.MakeIdentity(6);
+  F.SwapSequence(E, 2);
+  if (F.NumSwaps() != 3 || F.SwapOrigins().Get(0, 0) != 4 || F.SwapDestinations().Get(0, 0) != 2)
+    return 19;
+  F.SwapSequence(F);
+  if (F.NumSwaps() != 6) return 20;
+  Permutation G;
+  G.MakeIdentity(3);
+  Matrix<Int> gd(2, 1);
+  gd.Set(0, 0, 2);
+  gd.Set(1, 0, 1);
+  G.ImplicitSwapSequence(gd);
+  if (!G.IsImplicitSwapSequence() || G.NumSwaps() != 2) return 21;
+  // random explicit-origin sequences: the implicit form permutes identically
+  unsigned long long seed = 12345;
+  auto next = [&seed](Int m) {
+    seed = seed * 6364136223846793005ULL + 1442695040888963407ULL;
+    return (Int)((seed >> 33) % (unsigned long long)m);
+  };
+  for (int trial = 0; trial < 200; ++trial) {
+    const Int n = 1 + next(12);
+    Permutation R2;
+    R2.MakeIdentity(n);
+    const Int swaps = next(2 * n + 1);
+    for (Int k = 0; k < swaps; ++k) R2.Swap(next(n), next(n));
+    Matrix<Int> r, ri;
+    R2.ExplicitVector(r);
+    const std::vector<Int> d2 = R2.ImplicitSwapDests(n);
+    Permutation I2;
+    I2.SetSwapSequence(n, d2.data(), n);
+    I2.ExplicitVector(ri);
+    for (Int k = 0; k < n; ++k) {
+      if (ri.Get(k, 0) != r.Get(k, 0)) return 22;
+      if (!R2.IsImplicitSwapSequence() && d2[k] < k) return 23;  // rewritten: dest >= k
+    }
   }
   std::puts("dropin ok");
   return 0;
