@@ -976,6 +976,14 @@ const char* ElErrorString(ElError error) {
   }                                                                                      \
   ElError ElMatrixSet_##S(ElMatrix_##S A, ElInt i, ElInt j, T val) {                     \
     EL_GB_TRY(M<T>(A)->Set(i, j, val))                                                   \
+  }                                                                                      \
+  ElError ElView_##S(ElMatrix_##S A, ElMatrix_##S B, ElRange_i I, ElRange_i J) {         \
+    EL_GB_TRY(El::View(*M<T>(A), *M<T>(B), El::IR(I.beg, I.end), El::IR(J.beg, J.end)))  \
+  }                                                                                      \
+  ElError ElLockedView_##S(ElMatrix_##S A, ElConstMatrix_##S B, ElRange_i I,             \
+                           ElRange_i J) {                                                \
+    EL_GB_TRY(El::LockedView(*M<T>(A), *CM<T>(B), El::IR(I.beg, I.end),                  \
+                             El::IR(J.beg, J.end)))                                      \
   }
 EL_GB_MATRIX_IMPL(i, ElInt)
 EL_GB_MATRIX_IMPL(s, float)

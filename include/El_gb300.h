@@ -80,6 +80,18 @@ EL_GB_MATRIX_DECLS(s, float)
 EL_GB_MATRIX_DECLS(d, double)
 #undef EL_GB_MATRIX_DECLS
 
+/* include/El/core/types.h:36 */
+typedef struct { ElInt beg, end; } ElRange_i;
+
+/* include/El/core/View.h:20-25, 42-47: A becomes a view of B's rows iRange and
+ * columns jRange (end == -100, El::END, stands for the full extent) */
+ElError ElView_i(ElMatrix_i A, ElMatrix_i B, ElRange_i iRange, ElRange_i jRange);
+ElError ElView_s(ElMatrix_s A, ElMatrix_s B, ElRange_i iRange, ElRange_i jRange);
+ElError ElView_d(ElMatrix_d A, ElMatrix_d B, ElRange_i iRange, ElRange_i jRange);
+ElError ElLockedView_i(ElMatrix_i A, ElConstMatrix_i B, ElRange_i iRange, ElRange_i jRange);
+ElError ElLockedView_s(ElMatrix_s A, ElConstMatrix_s B, ElRange_i iRange, ElRange_i jRange);
+ElError ElLockedView_d(ElMatrix_d A, ElConstMatrix_d B, ElRange_i iRange, ElRange_i jRange);
+
 /* Permutation (include/El/core/Permutation.h:55-199) */
 ElError ElPermutationCreate(ElPermutation* P);
 ElError ElPermutationDestroy(ElConstPermutation P);

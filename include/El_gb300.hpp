@@ -4,6 +4,7 @@
  *
  * Same names, signatures, layouts and exceptions as the reference:
  *   El::Matrix<T>            include/El/core/Matrix/decl.hpp:17-241
+ *   El::IR / ALL / View      include/El/core/types.hpp:15-68, View/decl.hpp:89-124
  *   El::Permutation          include/El/core/Permutation.hpp:14-126
  *   El::LU(A, P)             include/El/lapack_like/factor.hpp:376
  *   El::LU(A) (no pivoting)  include/El/lapack_like/factor.hpp:367
@@ -28,6 +29,7 @@
 
 #include <stdexcept>
 #include <string>
+#include <utility>
 #include <vector>
 
 namespace El {
@@ -43,6 +45,35 @@ enum FileFormat {
   AUTO, ASCII, ASCII_MATLAB, BINARY, BINARY_FLAT, BMP, JPG, JPEG, MATRIX_MARKET, PNG, PPM,
   XBM, XPM, FileFormat_MAX
 };
+
+// Index ranges [beg, end) (include/El/core/types.hpp:15-68): IR(i) is the one
+// index i, END stands for the extent of the dimension it is applied to.
+template <typename T>
+struct Range {
+  T beg, end;
+  Range() : beg(0), end(0) {}
+  Range(T begArg, T endArg) : beg(begArg), end(endArg) {}
+};
+
+static const Int END = -100;
+
+template <>
+struct Range<Int> {
+  Int beg, end;
+  Range() : beg(0), end(0) {}
+  Range(Int index) : beg(index), end(index + 1) {}
+  Range(Int begArg, Int endArg) : beg(begArg), end(endArg) {}
+  Range<Int> operator+(Int shift) const {
+    if (end == END) throw std::logic_error("Unsupported shift");
+    return Range<Int>(beg + shift, end + shift);
+  }
+  Range<Int> operator-(Int shift) const {
+    if (end == END) throw std::logic_error("Unsupported shift");
+    return Range<Int>(beg - shift, end - shift);
+  }
+};
+typedef Range<Int> IR;
+static const IR ALL(0, END);
 
 // Exception types of the reference (include/El/core/environment/decl.hpp:209-231).
 class SingularMatrixException : public std::runtime_error {
@@ -63,7 +94,47 @@ class Matrix {
   Matrix(Int height, Int width) { Resize(height, width); }
   Matrix(Int height, Int width, Int ldim) { Resize(height, width, ldim); }
   Matrix(const Matrix<T>& A) { *this = A; }
+  // A moved matrix keeps its kind: a view stays a view of the same buffer
+  // (include/El/core/Matrix/impl.hpp:77-81).
+  Matrix(Matrix<T>&& A) noexcept
+      : height_(A.height_), width_(A.width_), ldim_(A.ldim_), buf_(A.buf_), cbuf_(A.cbuf_),
+        viewing_(A.viewing_), locked_(A.locked_), mem_(std::move(A.mem_)) {
+    A.Forget();
+  }
   Matrix<T>& operator=(const Matrix<T>& A);
+  // Moving into or out of a view copies the entries (impl.hpp:243-260).
+  Matrix<T>& operator=(Matrix<T>&& A) {
+    if (this == &A) return *this;
+    if (viewing_ || A.viewing_) return *this = static_cast<const Matrix<T>&>(A);
+    mem_.swap(A.mem_);
+    height_ = A.height_;
+    width_ = A.width_;
+    ldim_ = A.ldim_;
+    buf_ = A.buf_;
+    cbuf_ = A.cbuf_;
+    locked_ = false;
+    A.Forget();
+    A.mem_.clear();
+    return *this;
+  }
+
+  // A view of rows I and columns J (decl.hpp:79-80); of a locked matrix, or
+  // through a const matrix, a locked view.
+  Matrix<T> operator()(Range<Int> I, Range<Int> J) {
+    Matrix<T> V;
+    Sub(I, J);
+    if (locked_)
+      V.LockedAttach(I.end - I.beg, J.end - J.beg, LockedBuffer(I.beg, J.beg), ldim_);
+    else
+      V.Attach(I.end - I.beg, J.end - J.beg, Buffer(I.beg, J.beg), ldim_);
+    return V;
+  }
+  const Matrix<T> operator()(Range<Int> I, Range<Int> J) const {
+    Matrix<T> V;
+    Sub(I, J);
+    V.LockedAttach(I.end - I.beg, J.end - J.beg, LockedBuffer(I.beg, J.beg), ldim_);
+    return V;
+  }
 
   void Empty();
   void Resize(Int height, Int width);
@@ -87,13 +158,66 @@ class Matrix {
   T& operator()(Int i, Int j) { return Buffer()[i + (long)j * ldim_]; }
   const T& operator()(Int i, Int j) const { return cbuf_[i + (long)j * ldim_]; }
 
+  // Resolves END and checks that rows I, columns J lie inside the matrix.
+  void Sub(Range<Int>& I, Range<Int>& J) const {
+    if (I.end == END) I.end = height_;
+    if (J.end == END) J.end = width_;
+    if (I.beg < 0 || J.beg < 0 || I.end < I.beg || J.end < J.beg || I.end > height_ ||
+        J.end > width_)
+      throw std::logic_error("Trying to view outside of a Matrix");
+  }
+
  private:
+  void Forget() {
+    height_ = width_ = 0;
+    ldim_ = 1;
+    buf_ = nullptr;
+    cbuf_ = nullptr;
+    viewing_ = locked_ = false;
+  }
+
   Int height_ = 0, width_ = 0, ldim_ = 1;
   T* buf_ = nullptr;
   const T* cbuf_ = nullptr;
   bool viewing_ = false, locked_ = false;
   std::vector<T> mem_;
 };
+
+// Views of a contiguous submatrix (include/El/core/View/decl.hpp:89-124,
+// impl.hpp:274-387): A becomes a view of B's rows I and columns J.
+template <typename T>
+void View(Matrix<T>& A, Matrix<T>& B, Range<Int> I, Range<Int> J) {
+  B.Sub(I, J);
+  if (B.Locked())
+    A.LockedAttach(I.end - I.beg, J.end - J.beg, B.LockedBuffer(I.beg, J.beg), B.LDim());
+  else
+    A.Attach(I.end - I.beg, J.end - J.beg, B.Buffer(I.beg, J.beg), B.LDim());
+}
+template <typename T>
+void LockedView(Matrix<T>& A, const Matrix<T>& B, Range<Int> I, Range<Int> J) {
+  B.Sub(I, J);
+  A.LockedAttach(I.end - I.beg, J.end - J.beg, B.LockedBuffer(I.beg, J.beg), B.LDim());
+}
+template <typename T>
+void View(Matrix<T>& A, Matrix<T>& B, Int i, Int j, Int height, Int width) {
+  View(A, B, IR(i, i + height), IR(j, j + width));
+}
+template <typename T>
+void LockedView(Matrix<T>& A, const Matrix<T>& B, Int i, Int j, Int height, Int width) {
+  LockedView(A, B, IR(i, i + height), IR(j, j + width));
+}
+template <typename T>
+Matrix<T> View(Matrix<T>& B, Range<Int> I, Range<Int> J) {
+  Matrix<T> A;
+  View(A, B, I, J);
+  return A;
+}
+template <typename T>
+Matrix<T> LockedView(const Matrix<T>& B, Range<Int> I, Range<Int> J) {
+  Matrix<T> A;
+  LockedView(A, B, I, J);
+  return A;
+}
 
 class Permutation {
  public:

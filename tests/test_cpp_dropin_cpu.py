@@ -1,7 +1,8 @@
 """The C++ drop-in on the CPU: a program that includes include/El_gb300.hpp
 in place of Elemental's El.hpp compiles with g++, links libelgb300.so and runs
 the path's host-side pieces with the reference's semantics -- El::Matrix
-(owned, copied, attached views), El::Permutation swap sequences with implicit
+(owned, copied, moved, attached, and views A(IR, IR) / El::View with END,
+include/El/core/View/impl.hpp:274-387, also through ElView_d), El::Permutation swap sequences with implicit
 and explicit origins (src/lapack_like/perm/Permutation.cpp:205-303, 436-450,
 544-631, 731-745) and their implicit-origin form for the device, the
 blocksize stack (src/blas_like/blocksizes.cpp:37-60) and El::Write / El::Read
@@ -19,6 +20,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 PROGRAM = r"""
 #include "El_gb300.hpp"
+#include "El_gb300.h"
 #include <cstdio>
 #include <string>
 
@@ -142,6 +144,59 @@ int main(int argc, char** argv) {
       if (!R2.IsImplicitSwapSequence() && d2[k] < k) return 23;  // rewritten: dest >= k
     }
   }
+  // views: A(IR, IR) shares A's buffer; END resolves to the extent
+  Matrix<double> W(5, 4);
+  for (Int j = 0; j < 4; ++j)
+    for (Int i = 0; i < 5; ++i) W.Set(i, j, 100.0 * i + j);
+  auto S = W(IR(1, 4), IR(2, END));
+  if (!S.Viewing() || S.Height() != 3 || S.Width() != 2 || S.LDim() != 5) return 24;
+  if (S.Get(0, 0) != 102.0 || S.Get(2, 1) != 303.0) return 25;
+  S.Set(1, 1, -1.0);
+  if (W.Get(2, 3) != -1.0) return 26;
+  const Matrix<double>& Wc = W;
+  auto L = Wc(ALL, IR(1));
+  if (!L.Locked() || L.Height() != 5 || L.Width() != 1 || L.Get(4, 0) != 401.0) return 27;
+  try {
+    L.Buffer();
+    return 28;
+  } catch (const std::logic_error&) {
+  }
+  try {
+    W(IR(0, 6), ALL);
+    return 29;
+  } catch (const std::logic_error&) {
+  }
+  Matrix<double> X2;
+  View(X2, W, 1, 1, 2, 2);
+  if (X2.Get(1, 1) != 202.0) return 30;
+  // a permutation applied through a view moves the parent's rows
+  Permutation Q2;
+  Q2.MakeIdentity(3);
+  Q2.Swap(0, 2);
+  Q2.PermuteRows(S);
+  if (W.Get(1, 2) != 302.0 || W.Get(3, 2) != 102.0 || W.Get(1, 1) != 101.0) return 31;
+  // moving keeps an owned matrix's data; copying a view gives an owned copy
+  Matrix<double> Mv(std::move(C));
+  if (Mv.Get(2, 1) != 12.0 || C.Height() != 0) return 32;
+  Matrix<double> Cp(S);
+  if (Cp.Viewing() || Cp.Get(1, 1) != -1.0) return 33;
+  // the same through the C interface
+  ElMatrix_d cA, cV;
+  ElMatrixCreate_d(&cA);
+  ElMatrixCreate_d(&cV);
+  ElMatrixResize_d(cA, 4, 3);
+  ElMatrixSet_d(cA, 2, 1, 5.0);
+  ElRange_i ri = {1, 3}, rj = {0, -100};
+  if (ElView_d(cV, cA, ri, rj) != EL_SUCCESS) return 34;
+  double v = 0;
+  ElInt h = 0;
+  ElMatrixGet_d(cV, 1, 1, &v);
+  ElMatrixHeight_d(cV, &h);
+  if (v != 5.0 || h != 2) return 35;
+  ElRange_i bad = {0, 9};
+  if (ElView_d(cV, cA, bad, rj) != EL_LOGIC_ERROR) return 36;
+  ElMatrixDestroy_d(cV);
+  ElMatrixDestroy_d(cA);
   std::puts("dropin ok");
   return 0;
 }
