@@ -77,6 +77,32 @@ class Matrix:
     def ToNumPy(self):
         return self.array
 
+    def __getitem__(self, idx):
+        """A[I, J] with integers or unit-step slices: a view sharing this
+        matrix's memory (El::View through ElView_*), as the reference's
+        Matrix.__getitem__ (python/core/Matrix.py:456-482).  Factoring or
+        permuting the view changes the parent in place."""
+        i, j = idx
+
+        def bounds(s, n):
+            if isinstance(s, (int, np.integer)):
+                return int(s), int(s) + 1
+            if not isinstance(s, slice) or s.step not in (None, 1):
+                raise IndexError("views take integers or unit-step slices")
+            b, e, _ = s.indices(n)
+            return b, max(b, e)
+
+        (i0, i1), (j0, j1) = bounds(i, self.Height()), bounds(j, self.Width())
+        V = Matrix.__new__(Matrix)
+        V.array = self.array[i0:i1, j0:j1]
+        V.tag, V.lib, V._parent = self.tag, self.lib, self
+        h = ctypes.c_void_p()
+        _check(getattr(self.lib, f"ElMatrixCreate_{self.tag}")(ctypes.byref(h)), "Create")
+        V.obj = h
+        _check(getattr(self.lib, f"ElView_{self.tag}")(h, self.obj, _lib.Range(i0, i1),
+                                                      _lib.Range(j0, j1)), "View")
+        return V
+
     def __del__(self):
         try:
             getattr(self.lib, f"ElMatrixDestroy_{self.tag}")(self.obj)

@@ -50,6 +50,13 @@ class BatchOptions(ctypes.Structure):
                 ("selector_params", c_void_p), ("simt_update", c_int)]
 
 
+class Range(ctypes.Structure):
+    """ElRange_i (reference include/El/core/types.h:36): rows / columns
+    [beg, end); end = -100 (El::END) is the full extent."""
+
+    _fields_ = [("beg", ctypes.c_int), ("end", ctypes.c_int)]
+
+
 def _sig(lib, name, res, *args):
     f = getattr(lib, name)
     f.restype = res
@@ -135,6 +142,8 @@ def load():
         _sig(lib, f"ElMatrixWidth_{s}", c_int, vp, P(c_int))
         _sig(lib, f"ElMatrixLDim_{s}", c_int, vp, P(c_int))
         _sig(lib, f"ElMatrixBuffer_{s}", c_int, vp, P(vp))
+        _sig(lib, f"ElView_{s}", c_int, vp, vp, Range, Range)
+        _sig(lib, f"ElLockedView_{s}", c_int, vp, vp, Range, Range)
     _sig(lib, "ElPermutationCreate", c_int, P(vp))
     _sig(lib, "ElPermutationDestroy", c_int, vp)
     _sig(lib, "ElPermutationHeight", c_int, vp, P(c_int))

@@ -89,3 +89,32 @@ def test_device_api_fails_loudly_without_gpu():
     lib = _lib.load()
     h = ctypes.c_void_p()
     assert lib.ElGBCreate(ctypes.byref(h), 0) != 0
+
+
+def test_python_matrix_views_share_memory():
+    """El.Matrix slicing gives views through ElView_d (the reference's
+    Matrix.__getitem__, python/core/Matrix.py:456-482); a permutation applied
+    through a view moves the parent's rows."""
+    lib = _lib.load()
+    a = np.asfortranarray(np.arange(20, dtype=np.float64).reshape(5, 4))
+    A = El.Matrix(a)
+    V = A[1:4, 2:]
+    h, w, ld = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    assert lib.ElMatrixHeight_d(V.obj, ctypes.byref(h)) == 0 and h.value == 3
+    assert lib.ElMatrixWidth_d(V.obj, ctypes.byref(w)) == 0 and w.value == 2
+    assert lib.ElMatrixLDim_d(V.obj, ctypes.byref(ld)) == 0 and ld.value == 5
+    buf = ctypes.c_void_p()
+    assert lib.ElMatrixBuffer_d(V.obj, ctypes.byref(buf)) == 0
+    assert buf.value == a.ctypes.data + (1 + 2 * 5) * 8
+    assert np.array_equal(V.array, a[1:4, 2:])
+    P = El.Permutation()
+    assert lib.ElPermutationMakeIdentity(P.obj, 3) == 0
+    assert lib.ElPermutationSwap(P.obj, 0, 2) == 0
+    before = a.copy()
+    P.PermuteRows(V)
+    assert np.array_equal(a[1, 2:], before[3, 2:]) and np.array_equal(a[3, 2:], before[1, 2:])
+    assert np.array_equal(a[:, :2], before[:, :2])
+    col = A[:, 1]
+    assert col.array.shape == (5, 1) and col.array[4, 0] == a[4, 1]
+    with pytest.raises(IndexError):
+        A[::2, :]
