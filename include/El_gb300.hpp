@@ -18,6 +18,7 @@
  *   El::Cholesky(uplo, A, P) include/El/lapack_like/factor.hpp:37
  *   El::LinearSolve(A, B)    include/El/lapack_like/solve.hpp:20
  *   El::HPDSolve             include/El/lapack_like/solve.hpp:190
+ *   El::hpd_solve::Overwrite include/El/lapack_like/solve.hpp:213-228
  *   El::Blocksize / SetBlocksize / PushBlocksizeStack / PopBlocksizeStack
  *                            src/blas_like/blocksizes.cpp:37-60
  * Matrices live in host memory (as El::Matrix does); each call moves them to
@@ -334,6 +335,16 @@ void LinearSolve(const Matrix<F>& A, Matrix<F>& B);
 
 template <typename F>
 void HPDSolve(UpperOrLower uplo, Orientation orientation, const Matrix<F>& A, Matrix<F>& B);
+
+namespace hpd_solve {
+// HPDSolve without the copy of A: A is overwritten by its Cholesky factor
+// (include/El/lapack_like/solve.hpp:213-228, src/lapack_like/solve/HPD.cpp:15-25).
+template <typename F>
+void Overwrite(UpperOrLower uplo, Orientation orientation, Matrix<F>& A, Matrix<F>& B) {
+  Cholesky(uplo, A);
+  cholesky::SolveAfter(uplo, orientation, A, B);
+}
+}  // namespace hpd_solve
 
 }  // namespace El
 

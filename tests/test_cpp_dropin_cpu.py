@@ -197,6 +197,12 @@ int main(int argc, char** argv) {
   if (ElView_d(cV, cA, bad, rj) != EL_LOGIC_ERROR) return 36;
   ElMatrixDestroy_d(cV);
   ElMatrixDestroy_d(cA);
+  // the header's inline solver entry points instantiate for the path's types
+  void (*hpd_d)(UpperOrLower, Orientation, Matrix<double>&, Matrix<double>&) =
+      &hpd_solve::Overwrite<double>;
+  void (*hpd_s)(UpperOrLower, Orientation, Matrix<float>&, Matrix<float>&) =
+      &hpd_solve::Overwrite<float>;
+  if (!hpd_d || !hpd_s) return 37;
   std::puts("dropin ok");
   return 0;
 }
