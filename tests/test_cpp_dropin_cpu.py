@@ -227,3 +227,60 @@ def test_cpp_program_builds_against_the_dropin_header_and_runs(tmp_path):
     # the file is the reference's BINARY layout: Int height, Int width, entries
     raw = (tmp_path / "m.bin").read_bytes()
     assert len(raw) == 2 * 4 + 6 * 8
+
+
+C_PROGRAM = r"""
+#include "El_gb300.h"
+#include <stdio.h>
+
+int main(void) {
+  ElMatrix_d A, V;
+  ElPermutation P;
+  ElRange_i rows = {1, 3}, cols = {0, -100};
+  double v = 0.0;
+  ElInt h = 0, nb = 0;
+  if (ElMatrixCreate_d(&A) != EL_SUCCESS || ElMatrixCreate_d(&V) != EL_SUCCESS) return 1;
+  if (ElMatrixResize_d(A, 4, 2) != EL_SUCCESS) return 2;
+  ElMatrixSet_d(A, 2, 1, 3.5);
+  if (ElView_d(V, A, rows, cols) != EL_SUCCESS) return 3;
+  ElMatrixGet_d(V, 1, 1, &v);
+  ElMatrixHeight_d(V, &h);
+  if (v != 3.5 || h != 2) return 4;
+  if (ElPermutationCreate(&P) != EL_SUCCESS) return 5;
+  ElPermutationMakeIdentity(P, 2);
+  ElPermutationSwap(P, 0, 1);
+  if (ElPermutationPermuteRows_d(P, V, 0) != EL_SUCCESS) return 6;
+  ElMatrixGet_d(A, 1, 1, &v);
+  if (v != 3.5) return 7;
+  if (ElPermutationSwap(P, 0, 9) != EL_LOGIC_ERROR) return 8;
+  ElBlocksize(&nb);
+  if (nb != 128) return 9;
+  ElPermutationDestroy(P);
+  ElMatrixDestroy_d(V);
+  ElMatrixDestroy_d(A);
+  puts("c ok");
+  return 0;
+}
+"""
+
+
+@pytest.mark.parametrize("std", ["c99", "c11"])
+def test_c_program_builds_against_the_c_interface_and_runs(tmp_path, std):
+    """include/El_gb300.h is plain C (a C caller of Elemental's interface):
+    it compiles warning-free as C99 (the reference's C headers need C99 too:
+    stdbool.h, long long) and C11, and the host-side entry points behave as
+    the reference's."""
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("gcc not available")
+    assert os.path.exists(LIB), "libelgb300.so not built"
+    src = tmp_path / "cabi.c"
+    src.write_text(C_PROGRAM)
+    exe = tmp_path / "cabi"
+    r = subprocess.run([gcc, f"-std={std}", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I",
+                        os.path.join(ROOT, "include"), str(src), "-L", LIBDIR, "-lelgb300",
+                        "-Wl,-rpath," + LIBDIR, "-o", str(exe)],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    run = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert run.returncode == 0 and run.stdout.strip() == "c ok", (run.returncode, run.stdout)
