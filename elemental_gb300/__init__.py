@@ -111,18 +111,59 @@ class Matrix:
 
 
 class Permutation:
-    """El::Permutation (swap sequence with implicit origins)."""
+    """El::Permutation, a swap sequence (python/core/Permutation.py:56-187)."""
 
     def __init__(self):
         self.lib = _lib.load()
         h = ctypes.c_void_p()
         _check(self.lib.ElPermutationCreate(ctypes.byref(h)), "PermutationCreate")
         self.obj = h
+        self._dests = np.zeros(0, dtype=np.int32)
+
+    def Empty(self):
+        _check(self.lib.ElPermutationEmpty(self.obj), "Empty")
+        self._dests = np.zeros(0, dtype=np.int32)
+
+    def MakeIdentity(self, size):
+        _check(self.lib.ElPermutationMakeIdentity(self.obj, int(size)), "MakeIdentity")
+        self._dests = np.zeros(0, dtype=np.int32)
+
+    def ReserveSwaps(self, maxSwaps):
+        _check(self.lib.ElPermutationReserveSwaps(self.obj, int(maxSwaps)), "ReserveSwaps")
+
+    def Swap(self, origin, dest):
+        _check(self.lib.ElPermutationSwap(self.obj, int(origin), int(dest)), "Swap")
+        self._dests = np.append(self._dests, np.int32(dest))
+
+    def SwapSequence(self, PAppend, offset=0):
+        appended = PAppend._dests + int(offset)
+        _check(self.lib.ElPermutationSwapSequence(self.obj, PAppend.obj, int(offset)),
+               "SwapSequence")
+        self._dests = np.concatenate([self._dests, appended]).astype(np.int32)
 
     def Height(self):
         v = ctypes.c_int()
         _check(self.lib.ElPermutationHeight(self.obj, ctypes.byref(v)), "Height")
         return v.value
+
+    def Width(self):
+        v = ctypes.c_int()
+        _check(self.lib.ElPermutationWidth(self.obj, ctypes.byref(v)), "Width")
+        return v.value
+
+    def _flag(self, name):
+        v = ctypes.c_bool()
+        _check(getattr(self.lib, name)(self.obj, ctypes.byref(v)), name)
+        return bool(v.value)
+
+    def Parity(self):
+        return self._flag("ElPermutationParity")
+
+    def IsSwapSequence(self):
+        return self._flag("ElPermutationIsSwapSequence")
+
+    def IsImplicitSwapSequence(self):
+        return self._flag("ElPermutationIsImplicitSwapSequence")
 
     def ExplicitVector(self):
         n = self.Height()
@@ -131,8 +172,8 @@ class Permutation:
         return p.array.ravel().copy()
 
     def SwapDestinations(self):
-        """The swap destinations, recovered from the explicit vector's
-        replay is ambiguous, so they are kept from the factorization."""
+        """The destinations of the recorded swaps, in order (as
+        Permutation::SwapDestinations, src/lapack_like/perm/Permutation.cpp:444-450)."""
         return self._dests.copy()
 
     def PermuteRows(self, A: Matrix, offset=0):

@@ -147,6 +147,15 @@ def load():
     _sig(lib, "ElPermutationCreate", c_int, P(vp))
     _sig(lib, "ElPermutationDestroy", c_int, vp)
     _sig(lib, "ElPermutationHeight", c_int, vp, P(c_int))
+    _sig(lib, "ElPermutationWidth", c_int, vp, P(c_int))
+    _sig(lib, "ElPermutationEmpty", c_int, vp)
+    _sig(lib, "ElPermutationMakeIdentity", c_int, vp, c_int)
+    _sig(lib, "ElPermutationReserveSwaps", c_int, vp, c_int)
+    _sig(lib, "ElPermutationSwap", c_int, vp, c_int, c_int)
+    _sig(lib, "ElPermutationSwapSequence", c_int, vp, vp, c_int)
+    _sig(lib, "ElPermutationParity", c_int, vp, P(ctypes.c_bool))
+    _sig(lib, "ElPermutationIsSwapSequence", c_int, vp, P(ctypes.c_bool))
+    _sig(lib, "ElPermutationIsImplicitSwapSequence", c_int, vp, P(ctypes.c_bool))
     _sig(lib, "ElPermutationExplicitVector", c_int, vp, vp)
     _sig(lib, "ElPermutationPermuteRows_d", c_int, vp, vp, c_int)
     _sig(lib, "ElPermutationPermuteRows_s", c_int, vp, vp, c_int)

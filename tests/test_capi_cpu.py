@@ -118,3 +118,33 @@ def test_python_matrix_views_share_memory():
     assert col.array.shape == (5, 1) and col.array[4, 0] == a[4, 1]
     with pytest.raises(IndexError):
         A[::2, :]
+
+
+def test_python_permutation_swap_sequence_api():
+    """El.Permutation's swap-sequence methods (python/core/Permutation.py:56-187)
+    over the C interface: implicit origins until a swap names another origin,
+    parity, appending with an offset."""
+    P = El.Permutation()
+    P.MakeIdentity(4)
+    P.ReserveSwaps(4)
+    P.Swap(0, 2)
+    P.Swap(1, 1)
+    assert P.IsSwapSequence() and P.IsImplicitSwapSequence() and P.Parity()
+    P.Swap(3, 0)  # origin 3 is not the swap count 2: explicit origins
+    assert not P.IsImplicitSwapSequence() and not P.Parity()
+    assert list(P.SwapDestinations()) == [2, 1, 0]
+    lab = list(range(4))
+    for o, d in ((0, 2), (1, 1), (3, 0)):
+        lab[o], lab[d] = lab[d], lab[o]
+    assert list(P.ExplicitVector()) == lab
+    Q = El.Permutation()
+    Q.MakeIdentity(6)
+    Q.SwapSequence(P, 2)
+    assert list(Q.SwapDestinations()) == [4, 3, 2] and Q.Height() == Q.Width() == 6
+    B = El.Matrix(np.arange(6, dtype=np.float64).reshape(6, 1))
+    Q.PermuteRows(B)
+    assert list(B.array[:, 0]) == [0.0, 1.0] + [2.0 + v for v in lab]
+    with pytest.raises(El.ElError):
+        P.Swap(0, 9)
+    P.Empty()
+    assert P.Height() == 0 and len(P.SwapDestinations()) == 0
