@@ -74,6 +74,8 @@ def parse():
     p.add_argument("--kappa", type=float, default=0.0,
                    help="lu-ir: A = U diag(sigma) V^T with U, V Haar and cond_2(A) = kappa "
                         "(0, the default: A iid N(0,1))")
+    p.add_argument("--tol", type=float, default=0.0,
+                   help="lu-ir: target normwise backward error (0, the default: n*eps64)")
     p.add_argument("--count", type=int, default=0, help="systems (batched / selector)")
     p.add_argument("--train-count", type=int, default=3000, help="selector training systems")
     return p.parse_args()
@@ -234,6 +236,25 @@ def haar_conditioned(n, kappa, g, device="cuda"):
     return U @ V.t()
 
 
+def host_backward_error(AT, X, B, block=1024):
+    """Normwise backward error max_j ||b_j - A x_j||_2 / (||A||_F ||x_j||_2 +
+    ||b_j||_2) recomputed on the host in FP64 (numpy over OpenBLAS), from
+    AT = A^T as a row-major (n, n) array (the pinned host copy of the
+    column-major A), X and B (n, q).  Row blocks keep the temporaries small."""
+    import numpy as np
+
+    n = AT.shape[0]
+    R = np.array(B, dtype=np.float64, copy=True)
+    nA2 = 0.0
+    for j0 in range(0, n, block):
+        blk = AT[j0:j0 + block]          # rows j0.. of A^T = columns j0.. of A
+        R -= blk.T @ X[j0:j0 + block]
+        nA2 += float(np.einsum("ij,ij->", blk, blk))
+    num = np.linalg.norm(R, axis=0)
+    den = np.sqrt(nA2) * np.linalg.norm(X, axis=0) + np.linalg.norm(B, axis=0)
+    return float(np.max(num / den))
+
+
 def gpu_arm(args, rank, world, local_rank):
     import numpy as np
     import torch
@@ -267,9 +288,9 @@ def gpu_arm(args, rank, world, local_rank):
     X = D.colmajor(n, q)
     torch.cuda.synchronize()
 
-    def solve():
+    def solve(tol=args.tol):
         return ctx.refined_solve(A, B, X, precision=args.precision, method=args.method,
-                                 nb=args.nb)
+                                 nb=args.nb, tol=tol)
 
     info = None
     for _ in range(max(args.warmup, 0)):
@@ -319,16 +340,20 @@ def gpu_arm(args, rank, world, local_rank):
         Bh.copy_(B0)
         Bm = El.Matrix(Bh.numpy().T)
         assert Bm.array.ctypes.data == Bh.data_ptr()
-        El.LinearSolveMixed(Am, Bm, precision=args.precision, method=args.method, nb=args.nb)
+        El.LinearSolveMixed(Am, Bm, precision=args.precision, method=args.method, nb=args.nb,
+                            tol=args.tol)
         tot = 0.0
         einfo = None
+        phases = {"upload_ms": 0.0, "compute_ms": 0.0, "download_ms": 0.0}
         for _ in range(args.steps):
             Bh.copy_(B0)
             barrier()
             t0 = time.perf_counter()
             einfo = El.LinearSolveMixed(Am, Bm, precision=args.precision, method=args.method,
-                                        nb=args.nb)
+                                        nb=args.nb, tol=args.tol)
             tot += time.perf_counter() - t0
+            for k, v in El.LastHostCallTimes().items():
+                phases[k] += v / args.steps
         te = tot
         if dist is not None:
             tt = torch.tensor([te], device="cuda")
@@ -336,12 +361,23 @@ def gpu_arm(args, rank, world, local_rank):
             te = float(tt.item())
         Xh = torch.from_numpy(Bm.array.T.copy())
         err = float((Xh.cuda() - X.t()).abs().max())
+        # the solution returned through the public API, re-checked on the
+        # host in FP64 against the host copies of A and B (not timed)
+        th = time.perf_counter()
+        host_berr = host_backward_error(Ah.numpy(), Bm.array, B0.numpy().T)
+        th = time.perf_counter() - th
         e2e = {"value": args.steps * world / te, "unit": "solves/s",
                "h2d_bytes_per_step": 8 * n * n + 8 * n * q, "d2h_bytes_per_step": 8 * n * q,
                "api": "ElLinearSolveMixed_d (El::Matrix handles on pinned host memory)",
                "max_abs_diff_vs_device_run": err,
                "iterations": einfo["iterations"] if einfo else None,
-               "backward_error": einfo["backward_error"] if einfo else None}
+               "backward_error": einfo["backward_error"] if einfo else None,
+               "backward_error_host_fp64": host_berr,
+               "host_check": f"||B - A X|| / (||A||_F ||X|| + ||B||) per column, numpy FP64 "
+                             f"on the host ({th:.1f} s, not timed)",
+               "phases_ms_per_step": phases,
+               "h2d_gbs": (8 * n * n + 8 * n * q) / (phases["upload_ms"] * 1e-3) / 1e9
+               if phases["upload_ms"] > 0 else None}
         del Ah, B0, Bh, Am, Bm
 
     # plain FP64 GPU LU on the same system (one step; warm-up on a small case)
@@ -365,6 +401,19 @@ def gpu_arm(args, rank, world, local_rank):
                 "backward_error": finfo["backward_error"],
                 "fp64_fma_peak_tflops_probe": ctx.fp64_peak_tflops(),
                 "speedup_mixed_vs_fp64": tf / (tmax / args.steps)}
+        # the mixed solve run on to the FP64 LU's own backward error on this
+        # system (one solve, events on the same stream)
+        lvl = finfo["backward_error"]
+        f0.record(stream)
+        _, linfo = ctx.refined_solve(A, B, X, precision=args.precision, method=args.method,
+                                     nb=args.nb, tol=lvl, fallback=False)
+        f1.record(stream)
+        f1.synchronize()
+        tl = f0.elapsed_time(f1) / 1e3
+        fp64["mixed_to_fp64_level"] = {
+            "tol": lvl, "ms": tl * 1e3, "iterations": linfo["iterations"],
+            "backward_error": linfo["backward_error"], "fell_back": linfo["fell_back"],
+            "speedup_vs_fp64": tf / tl}
 
     if rank != 0:
         if dist is not None:
@@ -442,6 +491,7 @@ def gpu_arm(args, rank, world, local_rank):
                                + ", to backward error <= n*eps64",
                    "n": n, "nrhs": q, "precision": args.precision, "method": args.method,
                    "kappa": args.kappa if args.kappa > 0 else None,
+                   "tol": args.tol if args.tol > 0 else n * EPS64,
                    "nb": args.nb or 512, "l2": "inputs larger than L2 (A is 8 GiB)",
                    "parallelism": f"replicas x{world}"},
         "tflops_eq": value * flops_per_solve(n, q) / 1e12,

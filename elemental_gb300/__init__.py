@@ -356,3 +356,12 @@ def LinearSolveMixed(A: Matrix, B: Matrix, precision="fp32", method="lu-ir", tol
     return dict(iterations=inf.iterations, converged=bool(inf.converged),
                 fell_back=bool(inf.fell_back), precision=PRECISION_NAMES[inf.precision],
                 backward_error=inf.backward_error)
+
+
+def LastHostCallTimes():
+    """Host-side phases of the last completed host-matrix call (ms): upload,
+    device work (with its synchronisation), download."""
+    lib = _lib.load()
+    v = [ctypes.c_double() for _ in range(3)]
+    _check(lib.ElGBLastHostCallTimes(*[ctypes.byref(x) for x in v]), "LastHostCallTimes")
+    return {"upload_ms": v[0].value, "compute_ms": v[1].value, "download_ms": v[2].value}

@@ -180,6 +180,8 @@ def load():
         _sig(lib, f"ElLinearSolve_{s}", c_int, vp, vp)
         _sig(lib, f"ElHPDSolve_{s}", c_int, c_int, c_int, vp, vp)
     _sig(lib, "ElLinearSolveMixed_d", c_int, vp, vp, P(RefineCtrl), P(RefineInfo))
+    _sig(lib, "ElGBLastHostCallTimes", c_int, P(ctypes.c_double), P(ctypes.c_double),
+         P(ctypes.c_double))
     _lib = lib
     return lib
 

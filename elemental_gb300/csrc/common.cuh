@@ -109,5 +109,8 @@ __device__ __forceinline__ void warp_argmax(T& v, int& r) {
 }
 
 __host__ __device__ constexpr int ceil_div(int a, int b) { return (a + b - 1) / b; }
+// grid.y of a launch with one column per y index: at most 65535, so the
+// kernels loop over the columns j = blockIdx.y, blockIdx.y + gridDim.y, ...
+__host__ __device__ constexpr int grid_y(int ncols) { return ncols < 65535 ? ncols : 65535; }
 
 }  // namespace elgb

@@ -846,9 +846,9 @@ __global__ void col_abs_sum_max_kernel(const T* __restrict__ A, long lda, int m,
 
 template <typename T>
 __global__ void set_identity_kernel(T* X, long ldx, int n) {
-  const int j = blockIdx.y;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    X[i + (long)j * ldx] = i == j ? T(1) : T(0);
+  for (int j = blockIdx.y; j < n; j += gridDim.y)
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+      X[i + (long)j * ldx] = i == j ? T(1) : T(0);
 }
 
 // One-norm of an m x n device matrix (synchronizes); tmp: one device word.
@@ -891,7 +891,7 @@ static cudaError_t getri_impl(Context* ctx, int n, T* A, long lda, int nb, int* 
   int info = 0, err = 0;
   e = read_status(ctx, &info, &err);
   if (e != cudaSuccess || info || err) return e;
-  set_identity_kernel<T><<<dim3(ceil_div(n, 256), n), 256, 0, ctx->stream>>>(X, n, n);
+  set_identity_kernel<T><<<dim3(ceil_div(n, 256), grid_y(n)), 256, 0, ctx->stream>>>(X, n, n);
   ctx->launches += 1;
   e = getrs<T>(ctx, 0, n, A, lda, ipiv, n, X, n, nullptr);
   if (e != cudaSuccess) return e;

@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <fstream>
 #include <mutex>
 #include <new>
@@ -26,9 +27,13 @@ namespace El {
 template <typename T>
 Matrix<T>& Matrix<T>::operator=(const Matrix<T>& A) {
   if (this == &A) return *this;
+  // a locked matrix has no writable buffer: the reference's Copy reaches it
+  // through Buffer(), which raises the same LogicError
+  if (locked_) throw std::logic_error("Cannot return non-const buffer of locked Matrix");
   Resize(A.Height(), A.Width());
+  T* dst = Buffer();
   for (Int j = 0; j < width_; ++j)
-    for (Int i = 0; i < height_; ++i) buf_[i + (long)j * ldim_] = A.Get(i, j);
+    for (Int i = 0; i < height_; ++i) dst[i + (long)j * ldim_] = A.Get(i, j);
   return *this;
 }
 
@@ -43,9 +48,19 @@ void Matrix<T>::Empty() {
   mem_.shrink_to_fit();
 }
 
+// The reference's Resize_ (include/El/core/Matrix/impl.hpp:698-716): the
+// leading dimension and the entries stay unless the new shape needs more
+// rows than the leading dimension or more columns than before; a view may
+// only shrink (impl.hpp:101-115).
 template <typename T>
 void Matrix<T>::Resize(Int height, Int width) {
-  Resize(height, width, std::max(height, 1));
+  if (height < 0 || width < 0) throw std::logic_error("Matrix::Resize: invalid dimensions");
+  if (viewing_ && (height > height_ || width > width_))
+    throw std::logic_error("Cannot increase the size of a view");
+  const bool realloc = !viewing_ && (height > ldim_ || width > width_);
+  height_ = height;
+  width_ = width;
+  if (realloc) Reallocate(std::max(height, 1));
 }
 
 template <typename T>
@@ -54,11 +69,21 @@ void Matrix<T>::Resize(Int height, Int width, Int ldim) {
     throw std::logic_error("Matrix::Resize: invalid dimensions");
   if (viewing_ && (height > height_ || width > width_ || ldim != ldim_))
     throw std::logic_error("Cannot increase the size of a view");
+  const bool realloc = !viewing_ && (height > ldim_ || width > width_ || ldim != ldim_);
   height_ = height;
   width_ = width;
-  if (viewing_) return;
+  if (realloc) Reallocate(ldim);
+}
+
+// Storage for ldim x width entries: as the reference's Memory::Require
+// (include/El/core/Memory/impl.hpp:69-100), a buffer that is already large
+// enough is kept as it is; a larger one replaces it (zero-filled here) and
+// the old entries are not carried over.
+template <typename T>
+void Matrix<T>::Reallocate(Int ldim) {
   ldim_ = ldim;
-  mem_.assign((size_t)ldim * std::max(width, 0), T(0));
+  const size_t need = (size_t)ldim * std::max(width_, 0);
+  if (need > mem_.size()) mem_.assign(need, T(0));
   buf_ = mem_.data();
   cbuf_ = buf_;
 }
@@ -272,12 +297,18 @@ void PopBlocksizeStack() {
 // ---------------------------------------------------------------------------
 namespace {
 
+using Clock = std::chrono::steady_clock;
+
 struct Staging {
   std::mutex mu;
   ElGBContext ctx = nullptr;
   int device = -1;
   void* buf = nullptr;
   size_t bytes = 0;
+  cudaStream_t copy[2] = {nullptr, nullptr};  // host <-> device copy streams
+  // host-side phases of the current / last call (ElGBLastHostCallTimes)
+  double up_ms = 0, down_ms = 0;
+  double last[3] = {0, 0, 0};
 };
 
 Staging& St() {
@@ -290,6 +321,26 @@ void Check(cudaError_t e, const char* what) {
     throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+double MsSince(Clock::time_point t0) {
+  return std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
+}
+
+// Serialises the host-matrix entry points (they share the staging buffer)
+// and records the call's host-side phases: upload, download, and the rest
+// (the device work and its synchronisation).
+struct CallGuard {
+  std::lock_guard<std::mutex> lk;
+  Clock::time_point t0;
+  CallGuard() : lk(St().mu), t0(Clock::now()) { St().up_ms = St().down_ms = 0; }
+  ~CallGuard() {
+    Staging& s = St();
+    const double tot = MsSince(t0);
+    s.last[0] = s.up_ms;
+    s.last[1] = std::max(tot - s.up_ms - s.down_ms, 0.0);
+    s.last[2] = s.down_ms;
+  }
+};
+
 ElGBContext Ctx() {
   Staging& s = St();
   int dev = 0;
@@ -300,10 +351,15 @@ ElGBContext Ctx() {
     if (s.buf) cudaFree(s.buf);
     s.buf = nullptr;
     s.bytes = 0;
+    for (auto& c : s.copy) {
+      if (c) cudaStreamDestroy(c);
+      c = nullptr;
+    }
   }
   if (!s.ctx) {
     if (ElGBCreate(&s.ctx, dev) != 0) throw std::runtime_error("no usable CUDA device");
     s.device = dev;
+    for (auto& c : s.copy) Check(cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking), "stream");
   }
   return s.ctx;
 }
@@ -332,26 +388,46 @@ std::vector<int> DevicePivots(const Permutation& P, Int n) {
   return std::vector<int>(d.begin(), d.end());
 }
 
-// A synchronous copy from pageable memory may return once the data is staged,
-// before its DMA into device memory ends, and the factor-and-solve work runs
-// on the context's non-blocking stream, which is not ordered after the legacy
-// default stream: the legacy stream is drained before any launch reads the
-// upload (this also covers the small pivot copies issued just before it).
+// Host -> device copy of a column-major matrix: blocks of columns of about
+// 64 MiB, alternating between two copy streams so that both copy engines of
+// the direction can run, one call per block (a contiguous matrix takes plain
+// 1-D copies), then a wait for both streams.  The legacy default stream is
+// drained as well: a synchronous copy from pageable memory (the small pivot
+// copies some callers issue just before) may return once its data is staged,
+// before its DMA ends, and the factor-and-solve work runs on the context's
+// non-blocking stream, which is not ordered after the legacy stream.
 template <typename T>
 void Upload(ElGBContext, T* d, const Matrix<T>& A) {
   if (A.Height() == 0 || A.Width() == 0) return;
-  Check(cudaMemcpy2D(d, sizeof(T) * A.Height(), A.LockedBuffer(), sizeof(T) * A.LDim(),
-                     sizeof(T) * A.Height(), A.Width(), cudaMemcpyHostToDevice),
-        "upload");
+  Staging& s = St();
+  const Clock::time_point t0 = Clock::now();
+  const Int h = A.Height(), w = A.Width(), ld = A.LDim();
+  const size_t colb = sizeof(T) * (size_t)h;
+  const Int cols = std::max<Int>(1, (Int)(((size_t)64 << 20) / colb));
+  int k = 0;
+  for (Int j = 0; j < w; j += cols, ++k) {
+    const Int nc = std::min(cols, w - j);
+    cudaStream_t st = s.copy[k & 1];
+    if (ld == h || nc == 1)
+      Check(cudaMemcpyAsync(d + (size_t)j * h, A.LockedBuffer(0, j), colb * nc,
+                            cudaMemcpyHostToDevice, st), "upload");
+    else
+      Check(cudaMemcpy2DAsync(d + (size_t)j * h, colb, A.LockedBuffer(0, j), sizeof(T) * ld,
+                              colb, nc, cudaMemcpyHostToDevice, st), "upload");
+  }
+  for (cudaStream_t st : s.copy) Check(cudaStreamSynchronize(st), "upload");
   Check(cudaStreamSynchronize(cudaStreamLegacy), "upload");
+  s.up_ms += MsSince(t0);
 }
 
 template <typename T>
 void Download(Matrix<T>& A, const T* d) {
   if (A.Height() == 0 || A.Width() == 0) return;
+  const Clock::time_point t0 = Clock::now();
   Check(cudaMemcpy2D(A.Buffer(), sizeof(T) * A.LDim(), d, sizeof(T) * A.Height(),
                      sizeof(T) * A.Height(), A.Width(), cudaMemcpyDeviceToHost),
         "download");
+  St().down_ms += MsSince(t0);
 }
 
 void CheckStatus(ElGBContext ctx, bool cholesky) {
@@ -476,7 +552,7 @@ struct Dispatch<float> {
 // ---------------------------------------------------------------------------
 template <typename F>
 void LU(Matrix<F>& A, Permutation& P) {
-  std::lock_guard<std::mutex> lk(St().mu);
+  CallGuard guard;
   const Int m = A.Height(), n = A.Width(), minDim = std::min(m, n);
   P.MakeIdentity(m);
   P.ReserveSwaps(minDim);
@@ -508,7 +584,7 @@ void LU(Matrix<F>& A, Permutation& P) {
 // El::LU(A, P, Q) with full pivoting (src/lapack_like/factor/LU.cpp:145-152).
 template <typename F>
 void LU(Matrix<F>& A, Permutation& P, Permutation& Q) {
-  std::lock_guard<std::mutex> lk(St().mu);
+  CallGuard guard;
   const Int m = A.Height(), n = A.Width(), minDim = std::min(m, n);
   P.MakeIdentity(m);
   Q.MakeIdentity(n);
@@ -544,7 +620,7 @@ void LU(Matrix<F>& A, Permutation& P, Permutation& Q) {
 // El::LU(A) without pivoting (src/lapack_like/factor/LU.cpp:21-44).
 template <typename F>
 void LU(Matrix<F>& A) {
-  std::lock_guard<std::mutex> lk(St().mu);
+  CallGuard guard;
   const Int m = A.Height(), n = A.Width();
   if (std::min(m, n) == 0) return;
   ElGBContext ctx = Ctx();
@@ -559,7 +635,7 @@ void LU(Matrix<F>& A) {
 template <typename F>
 void Inverse(Matrix<F>& A) {
   if (A.Height() != A.Width()) throw std::logic_error("Cannot invert non-square matrices");
-  std::lock_guard<std::mutex> lk(St().mu);
+  CallGuard guard;
   const Int n = A.Height();
   if (n == 0) return;
   ElGBContext ctx = Ctx();
@@ -574,7 +650,7 @@ void Inverse(Matrix<F>& A) {
 template <typename F>
 F OneCondition(const Matrix<F>& A) {
   if (A.Height() != A.Width()) throw std::logic_error("OneCondition needs a square matrix");
-  std::lock_guard<std::mutex> lk(St().mu);
+  CallGuard guard;
   const Int n = A.Height();
   if (n == 0) return F(0);
   ElGBContext ctx = Ctx();
@@ -591,7 +667,7 @@ void SolveAfter(Orientation orientation, const Matrix<F>& A, const Permutation& 
                 Matrix<F>& B) {
   if (A.Height() != A.Width()) throw std::logic_error("A must be square");
   if (A.Height() != B.Height()) throw std::logic_error("A and B must be the same height");
-  std::lock_guard<std::mutex> lk(St().mu);
+  CallGuard guard;
   const Int n = A.Height(), q = B.Width();
   if (n == 0 || q == 0) return;
   ElGBContext ctx = Ctx();
@@ -615,7 +691,7 @@ void SolveAfter(Orientation orientation, const Matrix<F>& A, const Permutation& 
                 const Permutation& Q, Matrix<F>& B) {
   if (A.Height() != A.Width()) throw std::logic_error("A must be square");
   if (A.Height() != B.Height()) throw std::logic_error("A and B must be the same height");
-  std::lock_guard<std::mutex> lk(St().mu);
+  CallGuard guard;
   const Int n = A.Height(), q = B.Width();
   if (n == 0 || q == 0) return;
   ElGBContext ctx = Ctx();
@@ -642,7 +718,7 @@ void SolveAfter(Orientation orientation, const Matrix<F>& A, const Permutation& 
 template <typename F>
 void Cholesky(UpperOrLower uplo, Matrix<F>& A, Permutation& P) {
   if (A.Height() != A.Width()) throw std::logic_error("A must be square");
-  std::lock_guard<std::mutex> lk(St().mu);
+  CallGuard guard;
   const Int n = A.Height();
   P.MakeIdentity(n);
   P.ReserveSwaps(n);
@@ -667,7 +743,7 @@ void Cholesky(UpperOrLower uplo, Matrix<F>& A, Permutation& P) {
 template <typename F>
 void Cholesky(UpperOrLower uplo, Matrix<F>& A) {
   if (A.Height() != A.Width()) throw std::logic_error("A must be square");
-  std::lock_guard<std::mutex> lk(St().mu);
+  CallGuard guard;
   const Int n = A.Height();
   if (n == 0) return;
   ElGBContext ctx = Ctx();
@@ -687,7 +763,7 @@ void SolveAfter(UpperOrLower uplo, Orientation orientation, const Matrix<F>& A, 
   (void)orientation;  // real scalars: Conjugate(B) is the identity
   if (A.Height() != A.Width()) throw std::logic_error("A must be square");
   if (A.Height() != B.Height()) throw std::logic_error("A and B must be the same height");
-  std::lock_guard<std::mutex> lk(St().mu);
+  CallGuard guard;
   const Int n = A.Height(), q = B.Width();
   if (n == 0 || q == 0) return;
   ElGBContext ctx = Ctx();
@@ -712,7 +788,7 @@ void SolveAfter(UpperOrLower uplo, Orientation orientation, const Matrix<F>& A,
   (void)orientation;
   if (A.Height() != A.Width()) throw std::logic_error("A must be square");
   if (A.Height() != B.Height()) throw std::logic_error("A and B must be the same height");
-  std::lock_guard<std::mutex> lk(St().mu);
+  CallGuard guard;
   const Int n = A.Height(), q = B.Width();
   if (n == 0 || q == 0) return;
   ElGBContext ctx = Ctx();
@@ -735,7 +811,7 @@ template <typename F>
 void LinearSolve(const Matrix<F>& A, Matrix<F>& B) {
   if (A.Height() != A.Width()) throw std::logic_error("A must be square");
   if (A.Height() != B.Height()) throw std::logic_error("A and B must be the same height");
-  std::lock_guard<std::mutex> lk(St().mu);
+  CallGuard guard;
   const Int n = A.Height(), q = B.Width();
   if (n == 0) return;
   ElGBContext ctx = Ctx();
@@ -755,7 +831,7 @@ void HPDSolve(UpperOrLower uplo, Orientation orientation, const Matrix<F>& A, Ma
   (void)orientation;
   if (A.Height() != A.Width()) throw std::logic_error("A must be square");
   if (A.Height() != B.Height()) throw std::logic_error("A and B must be the same height");
-  std::lock_guard<std::mutex> lk(St().mu);
+  CallGuard guard;
   const Int n = A.Height(), q = B.Width();
   if (n == 0) return;
   ElGBContext ctx = Ctx();
@@ -770,12 +846,17 @@ void HPDSolve(UpperOrLower uplo, Orientation orientation, const Matrix<F>& A, Ma
   Download(B, dB);
 }
 
+void LastHostCallTimes(double* t) {
+  std::lock_guard<std::mutex> lk(St().mu);
+  for (int i = 0; i < 3; ++i) t[i] = St().last[i];
+}
+
 // Mixed-precision El::LinearSolve on host matrices (added form).
 void LinearSolveMixed(const Matrix<double>& A, Matrix<double>& B, const ElGBRefineCtrl* ctrl,
                       ElGBRefineInfo* info) {
   if (A.Height() != A.Width()) throw std::logic_error("A must be square");
   if (A.Height() != B.Height()) throw std::logic_error("A and B must be the same height");
-  std::lock_guard<std::mutex> lk(St().mu);
+  CallGuard guard;
   const Int n = A.Height(), q = B.Width();
   if (n == 0 || q == 0) return;
   ElGBContext ctx = Ctx();
@@ -1126,6 +1207,14 @@ ElError ElLinearSolve_d(ElConstMatrix_d A, ElMatrix_d B) {
 ElError ElLinearSolveMixed_d(ElConstMatrix_d A, ElMatrix_d B, const ElGBRefineCtrl* ctrl,
                              ElGBRefineInfo* info) {
   EL_GB_TRY(El::LinearSolveMixed(*CM<double>(A), *M<double>(B), ctrl, info))
+}
+ElError ElGBLastHostCallTimes(double* upload_ms, double* compute_ms, double* download_ms) {
+  double t[3];
+  El::LastHostCallTimes(t);
+  if (upload_ms) *upload_ms = t[0];
+  if (compute_ms) *compute_ms = t[1];
+  if (download_ms) *download_ms = t[2];
+  return EL_SUCCESS;
 }
 ElError ElHPDSolve_s(ElUpperOrLower u, ElOrientation o, ElConstMatrix_s A, ElMatrix_s B) {
   EL_GB_TRY(El::HPDSolve(Ul(u), Or(o), *CM<float>(A), *M<float>(B)))

@@ -39,8 +39,8 @@ constexpr int kRowChunk = 2048;  // rows per partial sum in the reductions
 __global__ void cvt_f64_f32_kernel(const double* __restrict__ src, long lds, int m, int n,
                                    float* __restrict__ dst, long ldd) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y;
-  if (i < m && j < n) dst[i + (long)j * ldd] = (float)src[i + (long)j * lds];
+  if (i >= m) return;
+  for (int j = blockIdx.y; j < n; j += gridDim.y) dst[i + (long)j * ldd] = (float)src[i + (long)j * lds];
 }
 
 // Per-column max |R(:, c)| over row chunks (partial), then finish.
@@ -339,7 +339,8 @@ cudaError_t refined_solve(Context* ctx, int n, const double* A, long lda, int nr
       w.dpart = (double*)take((size_t)Q * nch * kMaxBasis * sizeof(double));
     }
     // 1. low-precision factorization of an FP32 copy of A
-    cvt_f64_f32_kernel<<<dim3((n + 255) / 256, n), 256, 0, ctx->stream>>>(A, lda, n, n, w.Af, n);
+    cvt_f64_f32_kernel<<<dim3((n + 255) / 256, grid_y(n)), 256, 0, ctx->stream>>>(A, lda, n, n,
+                                                                             w.Af, n);
     ctx->launches += 1;
     IR_CHECK(cudaGetLastError());
     IR_CHECK(getrf<float>(ctx, n, n, w.Af, n, w.ipiv, c.nb, tc_kind, c.pivoting == 1));

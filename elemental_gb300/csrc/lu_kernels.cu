@@ -1459,20 +1459,21 @@ __global__ void permute_rows_kernel(const T* __restrict__ X, long ldx, T* __rest
                                     long ldy, int n, int ncols,
                                     const int* __restrict__ perm, int inverse) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int c = blockIdx.y;
-  if (i >= n || c >= ncols) return;
+  if (i >= n) return;
   const int pi = perm[i];
-  if (!inverse)
-    Y[i + (long)c * ldy] = X[pi + (long)c * ldx];
-  else
-    Y[pi + (long)c * ldy] = X[i + (long)c * ldx];
+  for (int c = blockIdx.y; c < ncols; c += gridDim.y) {
+    if (!inverse)
+      Y[i + (long)c * ldy] = X[pi + (long)c * ldx];
+    else
+      Y[pi + (long)c * ldy] = X[i + (long)c * ldx];
+  }
 }
 
 template <typename T>
 cudaError_t launch_permute_rows(const T* X, long ldx, T* Y, long ldy, int n, int ncols,
                                 const int* perm, bool inverse, cudaStream_t stream) {
   if (n <= 0 || ncols <= 0) return cudaSuccess;
-  dim3 grid(ceil_div(n, 256), ncols);
+  dim3 grid(ceil_div(n, 256), grid_y(ncols));
   permute_rows_kernel<T><<<grid, 256, 0, stream>>>(X, ldx, Y, ldy, n, ncols, perm,
                                                    inverse ? 1 : 0);
   return cudaGetLastError();

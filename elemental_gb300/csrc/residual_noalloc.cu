@@ -1,10 +1,10 @@
 // FP64 residual R = B - A X for callers that cannot allocate device memory.
 //
-// Some callers of this library may not call cudaMalloc at all: code running
-// while a CUDA stream is being captured into a graph that must not contain
-// allocation nodes, real-time or embedded hosts whose device memory is
-// budgeted up front, and frameworks that own every byte of device memory
-// through their own allocator.  ElGBResidual_d needs scratch for its
+// Some callers of this library may not call cudaMalloc at all: real-time or
+// embedded hosts whose device memory is budgeted up front, frameworks that
+// own every byte of device memory through their own allocator, and code on a
+// latency-critical path that must not let cudaMalloc / cudaFree synchronize
+// the device.  ElGBResidual_d needs scratch for its
 // partial sums and takes it from a context arena that grows with cudaMalloc;
 // this entry point instead keeps that scratch in a fixed file-scope device
 // array, so it allocates nothing, ever.

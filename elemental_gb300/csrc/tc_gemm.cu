@@ -242,9 +242,9 @@ __global__ void pack_b_kernel(const float* __restrict__ B, long ldb, int K, int 
                               void* __restrict__ out, void* __restrict__ lo,
                               const float* __restrict__ amax) {
   const float scale = KIND == kTcFP8 ? fp8_scale(amax[1]) : 1.f;
-  const int j = blockIdx.y;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < Kp; k += gridDim.x * blockDim.x)
-    store_op<KIND>(out, lo, (size_t)j * Kp + k, k < K ? B[k + (long)j * ldb] : 0.f, scale);
+  for (int j = blockIdx.y; j < n; j += gridDim.y)
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < Kp; k += gridDim.x * blockDim.x)
+      store_op<KIND>(out, lo, (size_t)j * Kp + k, k < K ? B[k + (long)j * ldb] : 0.f, scale);
 }
 
 // amax[0] = max |A| (m x K), amax[1] = max |B| (K x n), both column-major;
@@ -339,17 +339,17 @@ cudaError_t launch_tc_gemm_sub(int kind, int m, int n, int K, const float* A, lo
     if (e0 != cudaSuccess) return e0;
     absmax_kernel<<<1024, 256, 0, stream>>>(A, lda, m, K, B, ldb, n, amax);
     pack_a_kernel<kTcFP8><<<pg, dim3(32, 8), 0, stream>>>(A, lda, m, K, Kp, Abuf, nullptr, amax);
-    pack_b_kernel<kTcFP8><<<dim3((Kp + 255) / 256, n), 256, 0, stream>>>(B, ldb, K, n, Kp,
+    pack_b_kernel<kTcFP8><<<dim3((Kp + 255) / 256, grid_y(n)), 256, 0, stream>>>(B, ldb, K, n, Kp,
                                                                         Bbuf, nullptr, amax);
     nl = 3;
   } else if (kind == kTcBF16) {
     pack_a_kernel<kTcBF16><<<pg, dim3(32, 8), 0, stream>>>(A, lda, m, K, Kp, Abuf, nullptr,
                                                            amax);
-    pack_b_kernel<kTcBF16><<<dim3((Kp + 255) / 256, n), 256, 0, stream>>>(B, ldb, K, n, Kp,
+    pack_b_kernel<kTcBF16><<<dim3((Kp + 255) / 256, grid_y(n)), 256, 0, stream>>>(B, ldb, K, n, Kp,
                                                                          Bbuf, nullptr, amax);
   } else {
     pack_a_kernel<kTcTF32><<<pg, dim3(32, 8), 0, stream>>>(A, lda, m, K, Kp, Abuf, Alo, amax);
-    pack_b_kernel<kTcTF32><<<dim3((Kp + 255) / 256, n), 256, 0, stream>>>(B, ldb, K, n, Kp,
+    pack_b_kernel<kTcTF32><<<dim3((Kp + 255) / 256, grid_y(n)), 256, 0, stream>>>(B, ldb, K, n, Kp,
                                                                          Bbuf, Blo, amax);
   }
   cudaError_t e = cudaGetLastError();

@@ -192,6 +192,13 @@ ElError ElHPDSolve_d(ElUpperOrLower uplo, ElOrientation orientation,
 ElError ElLinearSolveMixed_d(ElConstMatrix_d A, ElMatrix_d B,
                              const ElGBRefineCtrl* ctrl, ElGBRefineInfo* info);
 
+/* Added, no counterpart in the reference: the host-side phases of the last
+ * completed call of this interface that takes host matrices (milliseconds):
+ * the host -> device uploads, the device work with its synchronisation, and
+ * the device -> host downloads.  Any pointer may be NULL. */
+ElError ElGBLastHostCallTimes(double* upload_ms, double* compute_ms,
+                              double* download_ms);
+
 #ifdef __cplusplus
 }
 #endif

@@ -169,6 +169,7 @@ class Matrix {
   }
 
  private:
+  void Reallocate(Int ldim);
   void Forget() {
     height_ = width_ = 0;
     ldim_ = 1;
@@ -357,6 +358,11 @@ namespace El {
 // an FP64 residual, FP64 LU fallback).  ctrl may be null.
 void LinearSolveMixed(const Matrix<double>& A, Matrix<double>& B,
                       const ElGBRefineCtrl* ctrl = nullptr, ElGBRefineInfo* info = nullptr);
+
+// Added (no counterpart in the reference): the host-side phases of the last
+// completed host-matrix call in milliseconds: t[0] uploads, t[1] the device
+// work with its synchronisation, t[2] downloads.
+void LastHostCallTimes(double* t);
 
 }  // namespace El
 

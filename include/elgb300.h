@@ -391,8 +391,9 @@ int ElGBResidual_d(ElGBContext ctx, int n, int nrhs, const double* A,
                    int ldb, double* R, int ldr);
 
 /* The residual of ElGBResidual_d for callers that cannot allocate device
- * memory (stream capture without allocation nodes, budgeted or externally
- * owned device memory).  No counterpart in the reference.  It calls no
+ * memory: device memory budgeted up front or owned by another allocator, or
+ * code that must not let cudaMalloc / cudaFree synchronize the device.  No
+ * counterpart in the reference.  It calls no
  * cudaMalloc / cudaFree and needs no context: its scratch is a fixed 8 MiB
  * device array that the library holds on every GPU it is loaded on, so it
  * accepts only n * min(nrhs, 16) * ceil(n / 4096) <= 1048576 (e.g. n <= 16384

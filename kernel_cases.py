@@ -2,12 +2,12 @@
 profiler captures (one warm-up call, then one measured call, so a profiler
 can skip the first launch of the kernel it targets).
 
-    python -m elemental_gb300.kernel_cases tc_gemm --m 16384 --n 16384 --k 512 --kind 2
-    python -m elemental_gb300.kernel_cases lu --n 8192 --kind 2
-    python -m elemental_gb300.kernel_cases refine --n 8192 --nrhs 16
-    python -m elemental_gb300.kernel_cases lu64 --n 4096
-    python -m elemental_gb300.kernel_cases batched --n 1024 --count 152 --precision fp32
-    python -m elemental_gb300.kernel_cases lufull --n 2048
+    python kernel_cases.py tc_gemm --m 16384 --n 16384 --k 512 --kind 2
+    python kernel_cases.py lu --n 8192 --kind 2
+    python kernel_cases.py refine --n 8192 --nrhs 16
+    python kernel_cases.py lu64 --n 4096
+    python kernel_cases.py batched --n 1024 --count 152 --precision fp32
+    python kernel_cases.py lufull --n 2048
 
 Each prints one JSON line with the event-timed duration of the measured
 call and its algorithmic work.  Inputs are seeded N(0, 1), generated on the
@@ -18,7 +18,7 @@ import json
 
 import torch
 
-from . import device as D
+from elemental_gb300 import device as D
 
 KIND_NAMES = {-1: "simt-fp32", 0: "bf16", 1: "tf32", 2: "tf32x3"}
 

@@ -203,6 +203,49 @@ int main(int argc, char** argv) {
   void (*hpd_s)(UpperOrLower, Orientation, Matrix<float>&, Matrix<float>&) =
       &hpd_solve::Overwrite<float>;
   if (!hpd_d || !hpd_s) return 37;
+  // copying into a proper sub-view writes the parent's entries in place
+  // (the view keeps its leading dimension, include/El/core/Matrix/impl.hpp:698-716)
+  Matrix<double> Pm(4, 4);
+  for (Int j = 0; j < 4; ++j)
+    for (Int i = 0; i < 4; ++i) Pm.Set(i, j, 10.0 * i + j);
+  Matrix<double> Sm(2, 2);
+  Sm.Set(0, 0, -1.0);
+  Sm.Set(1, 0, -2.0);
+  Sm.Set(0, 1, -3.0);
+  Sm.Set(1, 1, -4.0);
+  auto Vw = Pm(IR(1, 3), IR(2, 4));
+  Vw = Sm;
+  if (!Vw.Viewing() || Vw.LDim() != 4) return 38;
+  if (Pm.Get(1, 2) != -1.0 || Pm.Get(2, 2) != -2.0 || Pm.Get(1, 3) != -3.0 ||
+      Pm.Get(2, 3) != -4.0 || Pm.Get(0, 2) != 2.0 || Pm.Get(3, 3) != 33.0)
+    return 39;
+  // moving into a view copies the entries too
+  Matrix<double> Sm2(Sm);
+  Sm2.Set(0, 0, 99.0);
+  Vw = std::move(Sm2);
+  if (Pm.Get(1, 2) != 99.0) return 40;
+  // a view may shrink but not grow
+  auto Vw2 = Pm(IR(0, 2), ALL);
+  Vw2.Resize(2, 4);
+  Vw2.Resize(1, 3);
+  if (Vw2.LDim() != 4 || Vw2.Height() != 1 || Vw2.Width() != 3) return 41;
+  try {
+    Vw2.Resize(3, 3);
+    return 42;
+  } catch (const std::logic_error&) {
+  }
+  // copying into a locked view raises the reference's LogicError
+  Matrix<double> Lk;
+  LockedView(Lk, Pm, 0, 0, 2, 2);
+  try {
+    Lk = Sm;
+    return 43;
+  } catch (const std::logic_error&) {
+  }
+  if (Pm.Get(0, 0) != 0.0 || Pm.Get(1, 1) != 11.0) return 44;
+  // shrinking an owned matrix keeps its buffer, leading dimension and entries
+  Pm.Resize(2, 3);
+  if (Pm.LDim() != 4 || Pm.Get(1, 2) != 99.0 || Pm.Get(0, 1) != 1.0) return 45;
   std::puts("dropin ok");
   return 0;
 }
