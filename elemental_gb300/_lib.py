@@ -113,6 +113,8 @@ def load():
          P(RefineCtrl), P(RefineInfo))
     _sig(lib, "ElGBResidual_d", c_int, vp, c_int, c_int, vp, c_int, vp, c_int, vp, c_int, vp,
          c_int)
+    _sig(lib, "ElGBResidualDF_d", c_int, vp, c_int, c_int, vp, c_int, vp, c_int, vp, c_int, vp,
+         c_int)
     _sig(lib, "ElGBMLPParamCount", c_int)
     _sig(lib, "ElGBMLPForward", c_int, vp, vp, vp, c_int, vp, vp)
     _sig(lib, "ElGBMLPGradient", c_int, vp, vp, vp, vp, c_int, vp, P(ctypes.c_float))

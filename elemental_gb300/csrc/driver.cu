@@ -1216,6 +1216,9 @@ int ElGBSetOption(ElGBContext ctx, int option, int value) {
     case ELGB_OPT_PANEL_REGS:
       elgb::g_panel_regs = value ? 1 : 0;
       return 0;
+    case ELGB_OPT_RESIDUAL_DF:
+      ctx->opt_residual_df = value ? 1 : 0;
+      return 0;
     default:
       return elgb::kElArgError;
   }

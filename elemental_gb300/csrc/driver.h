@@ -36,6 +36,7 @@ struct Context {
   int opt_lookahead = 1;          // ElGBSetOption(ELGB_OPT_LOOKAHEAD)
   int opt_panel_ctas = 0;         // ElGBSetOption(ELGB_OPT_PANEL_CTAS), 0 = automatic
   int opt_tournament = 0;         // ElGBSetOption(ELGB_OPT_TOURNAMENT)
+  int opt_residual_df = 1;        // ElGBSetOption(ELGB_OPT_RESIDUAL_DF)
   void* arena2 = nullptr;  // second arena for drivers that call the ones above
   size_t arena2_bytes = 0;
 

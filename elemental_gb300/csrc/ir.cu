@@ -196,6 +196,16 @@ struct Ws {
   int* flags;        // block-row done flags of the one-launch triangular solves
   unsigned* ticket;
   int epoch;
+  // double-float residual (residual_df.cu): FP32 words of A, the scaled
+  // split X, per-column unscaling, partial sums, ||A||_F^2 and max |a|
+  float* Ahi;
+  float* Alo;
+  float2* Xs;
+  double* xinv;
+  double* dfpart;
+  double* spart;
+  double* astat;
+  bool df;           // residuals in double-float arithmetic
 };
 
 size_t al(size_t b) { return (b + 255) & ~size_t(255); }
@@ -265,6 +275,26 @@ static void backward_errors(const std::vector<double>& nr, const std::vector<dou
   }
 }
 
+// R = B - A X (B == nullptr: R = A X) for q <= 16 columns: double-float on
+// the FP32 pipe, or FP64.
+static cudaError_t ir_residual(Context* ctx, const Ws& w, int n, int q, const double* A,
+                               long lda, const double* X, long ldx, const double* B, long ldb,
+                               double* R, long ldr) {
+  const int pr = ctx->prof_begin(ctx->stream);
+  cudaError_t e;
+  if (w.df) {
+    e = launch_residual_df(n, q, w.Ahi, w.Alo, w.astat + 1, X, ldx, B, ldb, R, ldr, w.Xs,
+                           w.xinv, w.dfpart, ctx->stream);
+    ctx->launches += 3;
+  } else {
+    e = launch_residual_f64(n, q, A, lda, X, ldx, B, ldb, R, ldr, w.rpart, ctx->stream);
+    ctx->launches += 2;
+  }
+  ctx->prof_end(pr, ctx->stream, ELGB_PROF_RESIDUAL, 2.0 * n * (double)n * q,
+                8.0 * n * (double)n);
+  return e;
+}
+
 cudaError_t refined_solve(Context* ctx, int n, const double* A, long lda, int nrhs,
                           const double* B, long ldb, double* X, long ldx,
                           const ElGBRefineCtrl& cin, ElGBRefineInfo* info) {
@@ -299,6 +329,12 @@ cudaError_t refined_solve(Context* ctx, int n, const double* A, long lda, int nr
   const int nblk = trsv_blocks(n);
   need += 2 * al((size_t)nblk * 4096 * sizeof(float)) + al((size_t)nblk * sizeof(int)) +
           al(sizeof(unsigned));
+  const bool df = ctx->opt_residual_df != 0;
+  const size_t xs_count = ((size_t)(n + 63) / 64 * 64 + 1) * 16;
+  need += al(2 * df_split_parts(n) * sizeof(double)) + al(2 * sizeof(double));
+  if (df)
+    need += 2 * al((size_t)n * n * sizeof(float)) + al(xs_count * sizeof(float2)) +
+            al(16 * sizeof(double)) + al(df_residual_partial_doubles(n) * sizeof(double));
   if (gm)
     need += al((size_t)Q * kb * n * sizeof(double)) + al((size_t)Q * c.restart * n * sizeof(double)) +
             al((size_t)n * Q * sizeof(double)) + al((size_t)Q * kb * sizeof(double)) +
@@ -330,6 +366,15 @@ cudaError_t refined_solve(Context* ctx, int n, const double* A, long lda, int nr
     w.flags = (int*)take((size_t)nblk * sizeof(int));
     w.ticket = (unsigned*)take(sizeof(unsigned));
     w.epoch = 0;
+    w.spart = (double*)take(2 * df_split_parts(n) * sizeof(double));
+    w.astat = (double*)take(2 * sizeof(double));
+    if (df) {
+      w.Ahi = (float*)take((size_t)n * n * sizeof(float));
+      w.Alo = (float*)take((size_t)n * n * sizeof(float));
+      w.Xs = (float2*)take(xs_count * sizeof(float2));
+      w.xinv = (double*)take(16 * sizeof(double));
+      w.dfpart = (double*)take(df_residual_partial_doubles(n) * sizeof(double));
+    }
     IR_CHECK(cudaMemsetAsync(w.flags, 0, (size_t)nblk * sizeof(int), ctx->stream));
     if (gm) {
       w.V = (double*)take((size_t)Q * kb * n * sizeof(double));
@@ -338,11 +383,17 @@ cudaError_t refined_solve(Context* ctx, int n, const double* A, long lda, int nr
       w.H = (double*)take((size_t)Q * kb * sizeof(double));
       w.dpart = (double*)take((size_t)Q * nch * kMaxBasis * sizeof(double));
     }
-    // 1. low-precision factorization of an FP32 copy of A
-    cvt_f64_f32_kernel<<<dim3((n + 255) / 256, grid_y(n)), 256, 0, ctx->stream>>>(A, lda, n, n,
-                                                                             w.Af, n);
-    ctx->launches += 1;
-    IR_CHECK(cudaGetLastError());
+    // 1. low-precision factorization of an FP32 copy of A; the same pass over
+    // A makes its FP32 words for the double-float residual and its norms
+    if (df) {
+      IR_CHECK(launch_split_a(A, lda, n, w.Af, w.Ahi, w.Alo, w.spart, w.astat, ctx->stream));
+      ctx->launches += 2;
+    } else {
+      cvt_f64_f32_kernel<<<dim3((n + 255) / 256, grid_y(n)), 256, 0, ctx->stream>>>(A, lda, n,
+                                                                               n, w.Af, n);
+      ctx->launches += 1;
+      IR_CHECK(cudaGetLastError());
+    }
     IR_CHECK(getrf<float>(ctx, n, n, w.Af, n, w.ipiv, c.nb, tc_kind, c.pivoting == 1));
     IR_CHECK(cudaMemcpyAsync(ctx->h_status, ctx->status, sizeof(DevStatus),
                              cudaMemcpyDeviceToHost, ctx->stream));
@@ -354,14 +405,22 @@ cudaError_t refined_solve(Context* ctx, int n, const double* A, long lda, int nr
       IR_CHECK(launch_trtri_diag<float>(w.Af, n, n, true, true, w.Dl, ctx->stream));
       IR_CHECK(launch_trtri_diag<float>(w.Af, n, n, false, false, w.Du, ctx->stream));
       ctx->launches += 3;
-      // ||A||_F
-      IR_CHECK(launch_col_sumsq<double>(A, lda, n, n, w.colout, w.part, ctx->stream));
-      ctx->launches += 2;
-      double nA2 = 0;
-      IR_CHECK(cudaMemcpyAsync(&nA2, w.colout + n, sizeof(double), cudaMemcpyDeviceToHost,
-                               ctx->stream));
+      // ||A||_F (and max |a|, from the split pass)
+      double stat[2] = {0.0, 0.0};
+      if (!df) {
+        IR_CHECK(launch_col_sumsq<double>(A, lda, n, n, w.colout, w.part, ctx->stream));
+        ctx->launches += 2;
+        IR_CHECK(cudaMemcpyAsync(&stat[0], w.colout + n, sizeof(double), cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+      } else {
+        IR_CHECK(cudaMemcpyAsync(stat, w.astat, 2 * sizeof(double), cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+      }
       IR_CHECK(cudaStreamSynchronize(ctx->stream));
-      const double nA = std::sqrt(nA2);
+      const double nA = std::sqrt(stat[0]);
+      // double-float words need max |a| well inside FP32's exponent range
+      // (the scaled products then stay O(1)); otherwise FP64 residuals
+      w.df = df && stat[1] > 0x1p-100 && stat[1] < 0x1p100;
       bool all_ok = true;
       int max_it = 0;
       double worst = 0.0;
@@ -376,12 +435,7 @@ cudaError_t refined_solve(Context* ctx, int n, const double* A, long lda, int nr
         int it = 0;
         bool conv = false;
         while (true) {
-          const int pr = ctx->prof_begin(ctx->stream);
-          IR_CHECK(launch_residual_f64(n, q, A, lda, Xc, ldx, Bc, ldb, w.R, n, w.rpart,
-                                       ctx->stream));
-          ctx->prof_end(pr, ctx->stream, ELGB_PROF_RESIDUAL, 2.0 * n * (double)n * q,
-                        8.0 * n * (double)n);
-          ctx->launches += 2;
+          IR_CHECK(ir_residual(ctx, w, n, q, A, lda, Xc, ldx, Bc, ldb, w.R, n));
           IR_CHECK(colnorm2(ctx, w.R, n, n, q, w.sums, w.part, nr));
           IR_CHECK(colnorm2(ctx, Xc, ldx, n, q, w.sums + 17, w.part, nx));
           backward_errors(nr, nx, nb, nA, q, be);
@@ -440,12 +494,8 @@ cudaError_t refined_solve(Context* ctx, int n, const double* A, long lda, int nr
             IR_CHECK(lowprec_solve(ctx, n, q, w, w.V + (long)j * n, vcs, w.Z + (long)j * n, zcs,
                                    false, false));
             // W = A Z(:, j)
-            const int pg = ctx->prof_begin(ctx->stream);
-            IR_CHECK(launch_residual_f64(n, q, A, lda, w.Z + (long)j * n, zcs, nullptr, 0, w.W,
-                                         n, w.rpart, ctx->stream));
-            ctx->prof_end(pg, ctx->stream, ELGB_PROF_RESIDUAL, 2.0 * n * (double)n * q,
-                          8.0 * n * (double)n);
-            ctx->launches += 2;
+            IR_CHECK(ir_residual(ctx, w, n, q, A, lda, w.Z + (long)j * n, zcs, nullptr, 0, w.W,
+                                 n));
             // classical Gram-Schmidt, twice
             for (int pass = 0; pass < 2; ++pass) {
               multi_dot_partial_kernel<<<dim3(nch, q), 256, 0, ctx->stream>>>(w.V, vcs, n, j + 1,
@@ -569,7 +619,74 @@ cudaError_t refined_solve(Context* ctx, int n, const double* A, long lda, int nr
   return cudaSuccess;
 }
 
+// R = B - A X in double-float arithmetic for any nrhs (blocks of 16): the
+// split of A into FP32 words, then the residual kernels.
+cudaError_t residual_df(Context* ctx, int n, int nrhs, const double* A, long lda,
+                        const double* X, long ldx, const double* B, long ldb, double* R,
+                        long ldr) {
+  IR_CHECK(cudaSetDevice(ctx->device));
+  IR_CHECK(ctx->begin_call());
+  if (n == 0 || nrhs == 0) return cudaSuccess;
+  const size_t xs_count = ((size_t)(n + 63) / 64 * 64 + 1) * 16;
+  // partial sums of either kernel set (FP64: one per 4096-column chunk)
+  const size_t npart = std::max(df_residual_partial_doubles(n),
+                                (size_t)((n + 4095) / 4096) * n * 16);
+  IR_CHECK(ctx->ensure(2 * al((size_t)n * n * sizeof(float)) +
+                       al(2 * df_split_parts(n) * sizeof(double)) + al(2 * sizeof(double)) +
+                       al(xs_count * sizeof(float2)) + al(16 * sizeof(double)) +
+                       al(npart * sizeof(double))));
+  char* p = static_cast<char*>(ctx->arena);
+  auto take = [&](size_t b) {
+    char* r = p;
+    p += al(b);
+    return r;
+  };
+  float* Ahi = (float*)take((size_t)n * n * sizeof(float));
+  float* Alo = (float*)take((size_t)n * n * sizeof(float));
+  double* spart = (double*)take(2 * df_split_parts(n) * sizeof(double));
+  double* astat = (double*)take(2 * sizeof(double));
+  float2* Xs = (float2*)take(xs_count * sizeof(float2));
+  double* inv = (double*)take(16 * sizeof(double));
+  double* part = (double*)take(npart * sizeof(double));
+  IR_CHECK(launch_split_a(A, lda, n, nullptr, Ahi, Alo, spart, astat, ctx->stream));
+  ctx->launches += 2;
+  // A's entries must sit well inside FP32's exponent range for the split;
+  // otherwise the FP64 kernels (their partial sums fit in the same scratch)
+  double amax = 0.0;
+  IR_CHECK(cudaMemcpyAsync(&amax, astat + 1, sizeof(double), cudaMemcpyDeviceToHost,
+                           ctx->stream));
+  IR_CHECK(cudaStreamSynchronize(ctx->stream));
+  if (!(amax > 0x1p-100 && amax < 0x1p100)) {
+    for (int c = 0; c < nrhs; c += 16) {
+      const int q = std::min(16, nrhs - c);
+      IR_CHECK(launch_residual_f64(n, q, A, lda, X + (long)c * ldx, ldx,
+                                   B ? B + (long)c * ldb : nullptr, ldb, R + (long)c * ldr, ldr,
+                                   part, ctx->stream));
+      ctx->launches += 2;
+    }
+    return cudaSuccess;
+  }
+  for (int c = 0; c < nrhs; c += 16) {
+    const int q = std::min(16, nrhs - c);
+    IR_CHECK(launch_residual_df(n, q, Ahi, Alo, astat + 1, X + (long)c * ldx, ldx,
+                                B ? B + (long)c * ldb : nullptr, ldb, R + (long)c * ldr, ldr,
+                                Xs, inv, part, ctx->stream));
+    ctx->launches += 3;
+  }
+  return cudaSuccess;
+}
+
 }  // namespace elgb
+
+extern "C" int ElGBResidualDF_d(ElGBContext ctx, int n, int nrhs, const double* A, int lda,
+                                const double* X, int ldx, const double* B, int ldb, double* R,
+                                int ldr) {
+  if (!ctx || n < 0 || nrhs < 0 || lda < std::max(n, 1) || ldx < std::max(n, 1) ||
+      ldb < std::max(n, 1) || ldr < std::max(n, 1))
+    return elgb::kElArgError;
+  auto* cx = static_cast<elgb::Context*>(ctx);
+  return elgb::to_el_error(elgb::residual_df(cx, n, nrhs, A, lda, X, ldx, B, ldb, R, ldr));
+}
 
 extern "C" int ElGBRefinedSolve_d(ElGBContext ctx, int n, const double* A, int lda, int nrhs,
                                   const double* B, int ldb, double* X, int ldx,

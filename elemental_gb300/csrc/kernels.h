@@ -173,6 +173,22 @@ cudaError_t launch_residual_f64(int n, int q, const double* A, long lda,
                                 long ldb, double* R, long ldr, double* partial,
                                 cudaStream_t stream);
 
+// The refinement's residual to FP64 accuracy on the FP32 pipe (double-float
+// arithmetic, residual_df.cu).  launch_split_a makes, from the FP64 A (n x n),
+// the FP32 copy Af, the FP32 words Ahi + Alo of A (all ld n) and out[0] =
+// ||A||_F^2, out[1] = max |a_ij|; part holds 2 * df_split_parts(n) doubles.
+// launch_residual_df computes R = B - A X (B == nullptr: R = A X), q <= 16,
+// from Ahi, Alo and amaxA (= &out[1]); Xs holds (round_up(n, 64) + 1) * 16
+// float2, inv 16 doubles, partial df_residual_partial_doubles(n) doubles.
+size_t df_split_parts(int n);
+size_t df_residual_partial_doubles(int n);
+cudaError_t launch_split_a(const double* A, long lda, int n, float* Af, float* Ahi, float* Alo,
+                           double* part, double* out, cudaStream_t stream);
+cudaError_t launch_residual_df(int n, int q, const float* Ahi, const float* Alo,
+                               const double* amaxA, const double* X, long ldx, const double* B,
+                               long ldb, double* R, long ldr, float2* Xs, double* inv,
+                               double* partial, cudaStream_t stream);
+
 // Sum of squares of each column (out[j]) and of all entries (out[ncols]) of
 // an m x ncols matrix, deterministic.  partial holds 64 * (ncols + 1) doubles
 // followed by one zero-initialised unsigned counter (left zero on return).

@@ -160,49 +160,31 @@ __device__ __forceinline__ void panel_load_slab(T* slab, const T* A, long lda, i
   asm volatile("cp.async.wait_all;" ::: "memory");
 }
 
-// Column j of lu::Panel for this CTA's rows r0.. of the slab (column-major,
-// ld R): the multipliers l = a_rj / alpha and the rank-1 update of columns
-// j+1 .. w-1 with the pivot row urow; row pl (the pivot's old position)
-// takes old row j's values from s_d.  Returns this CTA's candidate for
-// column j+1 in (bv, br).  Columns go in groups of eight, then four (that
-// many loads in flight per row).  (Holding urow in registers with a fully unrolled
-// 32-column body measured slower: it issues all 32 columns' predicated
-// instructions for every j.)
-template <typename T, int W>
-__device__ __forceinline__ void panel_update_rows(T* slab, int R, int nr, int r0, int j, int w,
-                                                  int pl, const T* s_d, const T* urow,
-                                                  bool singular, T inv, int rb, T& bv,
-                                                  int& br) {
+// Step j of lu::Panel in two halves, so that the exchange of column j+1's
+// pivot runs while most of step j's rank-1 update is still to do:
+//   front: the multipliers of column j (scaled by the pivot's reciprocal,
+//          Panel.hpp:53-55), the pivot row's old position pl in full (it
+//          takes old row j from s_d), column j+1 of the other rows, and this
+//          CTA's candidate for column j+1;
+//   back:  columns j+2 .. w-1 of the other rows.
+// Until the back half has run, pending_value() gives a row's entries as the
+// whole step leaves them: every entry sees the same fma with the same
+// operands as in one pass, so results are bit-identical.
+template <typename T>
+__device__ __forceinline__ void panel_step_front(T* slab, int R, int nr, int r0, int j, int w,
+                                                 int pl, const T* s_d, const T* urow,
+                                                 bool singular, T inv, int rb, T& bv,
+                                                 int& br) {
   for (int r = r0 + threadIdx.x; r < nr; r += blockDim.x) {
     const bool pr = r == pl;
     T l = pr ? s_d[j] : slab[j * R + r];
     if (!singular) l *= inv;
     slab[j * R + r] = l;
-    const T* src = pr ? s_d : slab + r;  // old row j's values for row pl
-    const int sst = pr ? 1 : R;
-    int c = j + 1;
-    for (; c + 7 < w; c += 8) {  // eight loads in flight, then eight fmas / stores
-      T v[8];
-#pragma unroll
-      for (int e = 0; e < 8; ++e) v[e] = src[(c + e) * sst];
-#pragma unroll
-      for (int e = 0; e < 8; ++e) v[e] = fma(-l, urow[c + e], v[e]);
-#pragma unroll
-      for (int e = 0; e < 8; ++e) slab[(c + e) * R + r] = v[e];
+    if (pr) {
+      for (int c = j + 1; c < w; ++c) slab[c * R + r] = fma(-l, urow[c], s_d[c]);
+    } else if (j + 1 < w) {
+      slab[(j + 1) * R + r] = fma(-l, urow[j + 1], slab[(j + 1) * R + r]);
     }
-    for (; c + 3 < w; c += 4) {
-      T v0 = src[c * sst], v1 = src[(c + 1) * sst], v2 = src[(c + 2) * sst],
-        v3 = src[(c + 3) * sst];
-      v0 = fma(-l, urow[c], v0);
-      v1 = fma(-l, urow[c + 1], v1);
-      v2 = fma(-l, urow[c + 2], v2);
-      v3 = fma(-l, urow[c + 3], v3);
-      slab[c * R + r] = v0;
-      slab[(c + 1) * R + r] = v1;
-      slab[(c + 2) * R + r] = v2;
-      slab[(c + 3) * R + r] = v3;
-    }
-    for (; c < w; ++c) slab[c * R + r] = fma(-l, urow[c], src[c * sst]);
     if (j + 1 < w) {
       const T v = absv(slab[(j + 1) * R + r]);
       if (argmax_better(v, rb + r, bv, br)) {
@@ -211,6 +193,50 @@ __device__ __forceinline__ void panel_update_rows(T* slab, int R, int nr, int r0
       }
     }
   }
+}
+
+template <typename T>
+__device__ __forceinline__ void panel_step_back(T* slab, int R, int nr, int r0, int j, int w,
+                                                int pl, const T* urow) {
+  if (j + 2 >= w) return;
+  for (int r = r0 + threadIdx.x; r < nr; r += blockDim.x) {
+    if (r == pl) continue;
+    const T l = slab[j * R + r];
+    T* row = slab + r;
+    int c = j + 2;
+    for (; c + 7 < w; c += 8) {  // eight loads in flight, then eight fmas / stores
+      T v[8];
+#pragma unroll
+      for (int e = 0; e < 8; ++e) v[e] = row[(c + e) * R];
+#pragma unroll
+      for (int e = 0; e < 8; ++e) v[e] = fma(-l, urow[c + e], v[e]);
+#pragma unroll
+      for (int e = 0; e < 8; ++e) row[(c + e) * R] = v[e];
+    }
+    for (; c + 3 < w; c += 4) {
+      T v0 = row[c * R], v1 = row[(c + 1) * R], v2 = row[(c + 2) * R], v3 = row[(c + 3) * R];
+      v0 = fma(-l, urow[c], v0);
+      v1 = fma(-l, urow[c + 1], v1);
+      v2 = fma(-l, urow[c + 2], v2);
+      v3 = fma(-l, urow[c + 3], v3);
+      row[c * R] = v0;
+      row[(c + 1) * R] = v1;
+      row[(c + 2) * R] = v2;
+      row[(c + 3) * R] = v3;
+    }
+    for (; c < w; ++c) row[c * R] = fma(-l, urow[c], row[c * R]);
+  }
+}
+
+// Entry (r, c) of the slab (local row r) as step pj leaves it, before
+// panel_step_back(pj) has run (pj < 0: no step pending).  Only rows the step
+// updates (global row > pj) are asked for.
+template <typename T>
+__device__ __forceinline__ T pending_value(const T* slab, int R, int r, int c, int pj, int plp,
+                                           const T* urowp) {
+  T v = slab[c * R + r];
+  if (pj >= 0 && c >= pj + 2 && r != plp) v = fma(-slab[pj * R + r], urowp[c], v);
+  return v;
 }
 
 template <typename T, int W>
@@ -248,6 +274,9 @@ getf2_panel_kernel(PanelParams<T> p) {
   }
   block_argmax(bv, br, s_rv, s_rr);
 
+  // the step whose back half is still to run (pj < 0: none)
+  int pj = -1, plp = -1, r0p = 0;
+  const T* urowp = nullptr;
   for (int j = 0; j < w; ++j) {
     if (p.nopiv) {  // the only candidate is row j (lu::Unb, LU/Local.hpp:42-61)
       br = (j >= rb && j < re) ? j : -1;
@@ -257,15 +286,20 @@ getf2_panel_kernel(PanelParams<T> p) {
     const int par = epoch & 1;
     PanelSlot<T>* my = p.s.slots + (long)par * maxG + b;
     // 1. publish (the release store orders the CTA's slot writes, which
-    // the barrier makes visible to the publishing thread)
-    if (br >= 0 && tid < w) my->cand[tid] = slab[tid * R + (br - rb)];
-    if (j >= rb && j < re && tid < w) my->diag[tid] = slab[tid * R + (j - rb)];
+    // the barrier makes visible to the publishing thread); the rows carry
+    // the pending step's update
+    if (br >= 0 && tid < w) my->cand[tid] = pending_value(slab, R, br - rb, tid, pj, plp, urowp);
+    if (j >= rb && j < re && tid < w)
+      my->diag[tid] = pending_value(slab, R, j - rb, tid, pj, plp, urowp);
     if (tid == 0) {
       my->val = bv;
       my->row = br;
     }
     __syncthreads();
     if (tid == 0) st_release_s32(&my->epoch, epoch);
+    // the rest of the previous step's update while the other CTAs publish
+    if (pj >= 0) panel_step_back<T>(slab, R, nr, r0p, pj, w, plp, urowp);
+    __syncthreads();  // urowp (s_rows / s_d) is read before the exchange refills them
     // 2. the barrier: every slot carries this epoch.  The thread that polled
     // slot g copies g's candidate row (and, for the owner of row j, row j)
     // right away, so the winner's row is already on chip after the barrier.
@@ -322,8 +356,12 @@ getf2_panel_kernel(PanelParams<T> p) {
     // the pivot row's position: old row j's multipliers of the earlier
     // columns move with it (columns j.. come from the update below)
     if (pl >= 0 && tid < j) slab[tid * R + pl] = s_d[tid];
-    panel_update_rows<T, W>(slab, R, nr, r0, j, w, pl, s_d, urow, singular, inv, rb, bv, br);
+    panel_step_front<T>(slab, R, nr, r0, j, w, pl, s_d, urow, singular, inv, rb, bv, br);
     block_argmax_nolead(bv, br, s_rv, s_rr);
+    pj = j;
+    plp = pl;
+    r0p = r0;
+    urowp = urow;
   }
   __syncthreads();
   for (int c = 0; c < w; ++c)
@@ -520,6 +558,12 @@ __device__ __forceinline__ void cluster_barrier() {
   asm volatile("barrier.cluster.arrive.release.aligned;\n"
                "barrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
+__device__ __forceinline__ void cluster_arrive() {
+  asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void cluster_wait() {
+  asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
 
 __device__ __forceinline__ uint32_t cluster_map(const void* local, unsigned rank) {
   uint32_t a = static_cast<uint32_t>(__cvta_generic_to_shared(local)), r;
@@ -578,16 +622,23 @@ getf2_panel_cluster_kernel(PanelParams<T> p) {
   block_argmax(bv, br, s_rv, s_rr);
   cluster_barrier();  // every CTA of the cluster is running
 
+  int pj = -1, plp = -1, r0p = 0;  // the step whose back half is still to run
+  const T* urowp = nullptr;
   for (int j = 0; j < w; ++j) {
     ClusterSlot<T>* my = &slots[j & 1];
-    // 1. publish in this CTA's shared memory
-    if (br >= 0 && tid < w) my->cand[tid] = slab[tid * R + (br - rb)];
-    if (j >= rb && j < re && tid < w) my->diag[tid] = slab[tid * R + (j - rb)];
+    // 1. publish in this CTA's shared memory (rows with the pending update)
+    if (br >= 0 && tid < w) my->cand[tid] = pending_value(slab, R, br - rb, tid, pj, plp, urowp);
+    if (j >= rb && j < re && tid < w)
+      my->diag[tid] = pending_value(slab, R, j - rb, tid, pj, plp, urowp);
     if (tid == 0) {
       my->val = bv;
       my->row = br;
     }
-    cluster_barrier();
+    cluster_arrive();
+    // the rest of the previous step's update while the cluster gathers
+    if (pj >= 0) panel_step_back<T>(slab, R, nr, r0p, pj, w, plp, urowp);
+    __syncthreads();  // urowp (s_rows / s_d) is read before the exchange refills them
+    cluster_wait();
     // 2. thread g < C reads CTA g's slot
     if (tid < G) {
       const uint32_t base = cluster_map(my, (unsigned)tid);
@@ -632,15 +683,19 @@ getf2_panel_cluster_kernel(PanelParams<T> p) {
     const bool singular = (alpha == T(0));
     if (singular && b == 0 && tid == 0) atomicCAS(&p.st->info, 0, p.info_base + j + 1);
     const T inv = singular ? T(1) : T(1) / alpha;
-    // 4. swap, update, next candidate (as getf2_panel_kernel)
+    // 4. swap, the front of the update, next candidate (as getf2_panel_kernel)
     if (piv != j && tid < w && j >= rb && j < re) slab[tid * R + (j - rb)] = urow[tid];
     bv = T(-1);
     br = -1;
     const int r0 = max(j + 1 - rb, 0);
     const int pl = (piv != j && piv >= rb && piv < re) ? piv - rb : -1;
     if (pl >= 0 && tid < j) slab[tid * R + pl] = s_d[tid];
-    panel_update_rows<T, W>(slab, R, nr, r0, j, w, pl, s_d, urow, singular, inv, rb, bv, br);
+    panel_step_front<T>(slab, R, nr, r0, j, w, pl, s_d, urow, singular, inv, rb, bv, br);
     block_argmax_nolead(bv, br, s_rv, s_rr);
+    pj = j;
+    plp = pl;
+    r0p = r0;
+    urowp = urow;
   }
   __syncthreads();
   for (int c = 0; c < w; ++c)
@@ -1177,95 +1232,171 @@ template cudaError_t launch_lu_full<float>(float*, long, int, int, int*, int*,
 // ---------------------------------------------------------------------------
 // K2: row interchanges (PB.PermuteRows, src/lapack_like/factor/LU.cpp:130-131)
 // ---------------------------------------------------------------------------
-// The nb swaps (k+i <-> ipiv[i]) are replayed once, on row labels only, by
-// one thread with an open-addressing hash table in shared memory for the rows
-// below the block; the result is the list of rows whose contents change and
-// the row each one receives.  Applying that list touches every affected
-// element once (read all, then write all) instead of replaying nb dependent
-// swaps.
+// The nb swaps (k+i <-> ipiv[i], applied in order) become the list of rows
+// whose contents change and the original row each one receives; applying
+// that list touches every affected element once (read all, then write all)
+// instead of replaying nb dependent swaps.  The list is built in parallel:
+//   * E(t), the original row sitting at row k+t just before swap t, is
+//     E(t') for the last earlier swap t' whose target was row k+t, else k+t
+//     itself (resolved for all t at once by pointer jumping, the links
+//     point to earlier swaps only);
+//   * row k+i ends with what swap i brings in: E(i) if ipiv[i] = k+i, else
+//     E(t) of the last earlier swap t with the same target, else the
+//     untouched original row ipiv[i];
+//   * a row below the block ends with E(t) of the last swap t targeting it.
+// Targets are found through an open-addressing hash table in shared memory,
+// each slot with the chain of swaps that target its row.
 __device__ __forceinline__ int swap_hash(int row, int mask) {
   return (int)(((unsigned)row * 2654435761u) >> 7) & mask;
 }
 
-__global__ void build_swap_pairs_kernel(const int* __restrict__ ipiv, int k, int nb, int tbits,
-                                        int* __restrict__ pairs, int* __restrict__ count) {
-  extern __shared__ int sh[];
-  const int tsize = 1 << tbits, mask = tsize - 1;
-  int* top = sh;                  // top[i]: original row now at row k+i
-  int* piv = sh + nb;             // the pivots, staged
-  int* order = sh + 2 * nb;       // table slots in insertion order
-  int* keys = sh + 3 * nb;        // rows >= k+nb that were touched (-1 = empty)
-  int* vals = keys + tsize;       // original row now at keys[slot]
-  __shared__ int s_nk;
-  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
-    top[i] = k + i;
-    piv[i] = ipiv[i];
+// Slot of `key` (inserted beforehand), or -1 when absent.
+__device__ __forceinline__ int swap_find(const int* keys, int key, int mask) {
+  int h = swap_hash(key, mask);
+  while (true) {
+    const int v = keys[h];
+    if (v == key) return h;
+    if (v == -1) return -1;
+    h = (h + 1) & mask;
   }
-  for (int i = threadIdx.x; i < tsize; i += blockDim.x) keys[i] = -1;
+}
+
+__global__ void __launch_bounds__(1024)
+build_swap_pairs_kernel(const int* __restrict__ ipiv, int k, int nb, int tbits,
+                        int* __restrict__ pairs, int* __restrict__ count) {
+  extern __shared__ int sh[];
+  __shared__ int s_wsum[32];
+  const int tsize = 1 << tbits, mask = tsize - 1;
+  const int tid = threadIdx.x, bd = blockDim.x;
+  int* p = sh;             // targets
+  int* nxt = p + nb;       // next swap of the same target's chain (-1 ends)
+  int* prv = nxt + nb;     // last earlier swap with the same target (-1)
+  int* lst = prv + nb;     // 1: no later swap has the same target
+  int* E0 = lst + nb;      // pointer jumping: resolved E(t) or -1 ...
+  int* E1 = E0 + nb;
+  int* P0 = E1 + nb;       // ... and the swap whose E is still needed
+  int* P1 = P0 + nb;
+  int* keys = P1 + nb;     // hash: target row (-1 empty)
+  int* head = keys + tsize;  // first swap of the slot's chain (-1)
+  for (int t = tid; t < nb; t += bd) p[t] = ipiv[t];
+  for (int h = tid; h < tsize; h += bd) {
+    keys[h] = -1;
+    head[h] = -1;
+  }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    int nk = 0;
-    for (int i = 0; i < nb; ++i) {
-      const int p = piv[i];
-      if (p < k + nb) {
-        const int t = top[i];
-        top[i] = top[p - k];
-        top[p - k] = t;
-      } else {
-        int h = swap_hash(p, mask);
-        while (keys[h] != -1 && keys[h] != p) h = (h + 1) & mask;
-        if (keys[h] == p) {
-          const int t = vals[h];
-          vals[h] = top[i];
-          top[i] = t;
+  for (int t = tid; t < nb; t += bd) {
+    const int key = p[t];
+    int h = swap_hash(key, mask);
+    while (true) {
+      const int old = atomicCAS(&keys[h], -1, key);
+      if (old == -1 || old == key) break;
+      h = (h + 1) & mask;
+    }
+    nxt[t] = atomicExch(&head[h], t);
+  }
+  __syncthreads();
+  for (int t = tid; t < nb; t += bd) {
+    int pv = -1, mx = -1;
+    for (int q = head[swap_find(keys, p[t], mask)]; q >= 0; q = nxt[q]) {
+      mx = max(mx, q);
+      if (q < t) pv = max(pv, q);
+    }
+    prv[t] = pv;
+    lst[t] = mx == t;
+    int lk = -1;  // last earlier swap that targeted row k+t
+    const int h = swap_find(keys, k + t, mask);
+    if (h >= 0)
+      for (int q = head[h]; q >= 0; q = nxt[q])
+        if (q < t) lk = max(lk, q);
+    E0[t] = lk < 0 ? k + t : -1;
+    P0[t] = lk;
+  }
+  __syncthreads();
+  int* Ec = E0;
+  int* Pc = P0;
+  int* En = E1;
+  int* Pn = P1;
+  for (int span = 1; span < 2 * nb; span *= 2) {
+    for (int t = tid; t < nb; t += bd) {
+      int e = Ec[t], q = Pc[t];
+      if (e < 0) {
+        if (Ec[q] >= 0) {
+          e = Ec[q];
+          q = -1;
         } else {
-          keys[h] = p;
-          vals[h] = top[i];
-          top[i] = p;
-          order[nk++] = h;
+          q = Pc[q];
         }
       }
+      En[t] = e;
+      Pn[t] = q;
     }
-    s_nk = nk;
+    __syncthreads();
+    int* x = Ec;
+    Ec = En;
+    En = x;
+    x = Pc;
+    Pc = Pn;
+    Pn = x;
+  }
+  // the changed rows: count per thread, block-wide scan, then write
+  auto fin_in = [&](int t) {
+    return p[t] == k + t ? Ec[t] : (prv[t] >= 0 ? Ec[prv[t]] : p[t]);
+  };
+  auto out_row = [&](int t) { return lst[t] && p[t] >= k + nb && Ec[t] != p[t]; };
+  int mine = 0;
+  for (int t = tid; t < nb; t += bd) mine += (fin_in(t) != k + t) + out_row(t);
+  const int lane = tid & 31, warp = tid >> 5;
+  int incl = mine;
+  for (int o = 1; o < 32; o *= 2) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  if (lane == 31) s_wsum[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = (bd + 31) >> 5;
+    int v = lane < nw ? s_wsum[lane] : 0;
+    for (int o = 1; o < 32; o *= 2) {
+      const int u = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v += u;
+    }
+    if (lane < nw) s_wsum[lane] = v;  // inclusive per warp
   }
   __syncthreads();
-  // emit (dst, src) for changed rows; lane-parallel with a block-wide scan
-  // kept simple: thread 0 compacts (at most 2 nb entries)
-  if (threadIdx.x == 0) {
-    int* dst = pairs;
-    int* src = pairs + 2 * nb;
-    int c = 0;
-    for (int i = 0; i < nb; ++i)
-      if (top[i] != k + i) {
-        dst[c] = k + i;
-        src[c] = top[i];
-        ++c;
-      }
-    for (int t = 0; t < s_nk; ++t) {
-      const int h = order[t];
-      if (vals[h] != keys[h]) {
-        dst[c] = keys[h];
-        src[c] = vals[h];
-        ++c;
-      }
+  int off = incl - mine + (warp > 0 ? s_wsum[warp - 1] : 0);
+  int* dst = pairs;
+  int* src = pairs + 2 * nb;
+  for (int t = tid; t < nb; t += bd) {
+    const int f = fin_in(t);
+    if (f != k + t) {
+      dst[off] = k + t;
+      src[off] = f;
+      ++off;
     }
-    *count = c;
+    if (out_row(t)) {
+      dst[off] = p[t];
+      src[off] = Ec[t];
+      ++off;
+    }
   }
+  if (tid == bd - 1) *count = off;
 }
 
 cudaError_t launch_build_swap_pairs(const int* ipiv, int k, int nb, int* pairs, int* count,
                                     cudaStream_t stream) {
   if (nb <= 0) return cudaMemsetAsync(count, 0, sizeof(int), stream);
   int tbits = 5;
-  while ((1 << tbits) < 4 * nb) ++tbits;
-  const size_t smem = (3 * (size_t)nb + 2 * ((size_t)1 << tbits)) * sizeof(int);
+  while ((1 << tbits) < 2 * nb) ++tbits;
+  const size_t smem = (8 * (size_t)nb + 2 * ((size_t)1 << tbits)) * sizeof(int);
+  if (smem > 200 * 1024) return cudaErrorInvalidValue;
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(build_swap_pairs_kernel,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
   }
-  build_swap_pairs_kernel<<<1, 128, smem, stream>>>(ipiv, k, nb, tbits, pairs, count);
+  const int threads = std::min(1024, (nb + 31) / 32 * 32);
+  build_swap_pairs_kernel<<<1, threads, smem, stream>>>(ipiv, k, nb, tbits, pairs, count);
   return cudaGetLastError();
 }
 

@@ -112,7 +112,7 @@ class Context:
         """ElGBSetOption: "lookahead" (0/1), "panel_ctas" (0 = auto) or
         "tournament" (0/1: tournament pivoting in lu_mixed's leaf panels)."""
         code = {"lookahead": 1, "panel_ctas": 2, "tournament": 3, "panel_cluster": 4,
-                "panel_regs": 5}[option]
+                "panel_regs": 5, "residual_df": 6}[option]
         self._rc(self.lib.ElGBSetOption(self.h, code, int(value)), "SetOption")
 
     def launches(self):
@@ -302,6 +302,18 @@ class Context:
         self._bind()
         self._rc(self.lib.ElGBResidual_d(self.h, n, q, _ptr(A), _ld(A), _ptr(X), _ld(X),
                                          _ptr(B), _ld(B), _ptr(R), _ld(R)), "Residual")
+        return R
+
+    def residual_df(self, A, X, B=None, R=None):
+        """R = B - A X (B None: R = A X) to FP64 accuracy in double-float
+        arithmetic on the FP32 pipe (ElGBResidualDF_d)."""
+        n, q = X.shape
+        if R is None:
+            R = colmajor(n, q, torch.float64, A.device)
+        self._bind()
+        bp, bl = (_ptr(B), _ld(B)) if B is not None else (None, n)
+        self._rc(self.lib.ElGBResidualDF_d(self.h, n, q, _ptr(A), _ld(A), _ptr(X), _ld(X),
+                                           bp, bl, _ptr(R), _ld(R)), "ResidualDF")
         return R
 
     def backward_error(self, A, X, B):

@@ -58,15 +58,20 @@ int ElGBSetBlocksize(int nb);
  *                       through distributed shared memory and the cluster
  *                       barrier; 1: always the cooperative kernel.
  *                       Process-wide (every context).
- *   ELGB_OPT_PANEL_REGS 1 (default): FP32 panels keep their rows in
- *                       registers (512 threads x 2 rows per CTA); 0: in
- *                       shared memory.  Process-wide. */
+ *   ELGB_OPT_PANEL_REGS 1: FP32 panels keep their rows in registers (512
+ *                       threads x 2 rows per CTA); 0 (default): in shared
+ *                       memory.  Process-wide.
+ *   ELGB_OPT_RESIDUAL_DF 1 (default): ElGBRefinedSolve_d computes its
+ *                       residuals and GMRES products in double-float
+ *                       arithmetic on the FP32 pipe (FP64-level accuracy);
+ *                       0: in FP64 arithmetic. */
 enum {
   ELGB_OPT_LOOKAHEAD = 1,
   ELGB_OPT_PANEL_CTAS = 2,
   ELGB_OPT_TOURNAMENT = 3,
   ELGB_OPT_PANEL_CLUSTER = 4,
-  ELGB_OPT_PANEL_REGS = 5
+  ELGB_OPT_PANEL_REGS = 5,
+  ELGB_OPT_RESIDUAL_DF = 6
 };
 int ElGBSetOption(ElGBContext ctx, int option, int value);
 
@@ -389,6 +394,16 @@ int ElGBHPDSolve_s(ElGBContext ctx, int uplo, int n, const float* A, int lda,
 int ElGBResidual_d(ElGBContext ctx, int n, int nrhs, const double* A,
                    int lda, const double* X, int ldx, const double* B,
                    int ldb, double* R, int ldr);
+
+/* R = B - A X (n x nrhs, any nrhs) to FP64 accuracy in double-float
+ * arithmetic on the FP32 pipe: the residual ElGBRefinedSolve_d computes by
+ * default (ELGB_OPT_RESIDUAL_DF).  Each call splits A into two FP32 words
+ * (8 n^2 bytes of context scratch), then 2 n^2 nrhs double-float products.
+ * Deterministic order.  The residual of the refinement loop of reference
+ * include/El/lapack_like/solve/Refined.hpp:70-73. */
+int ElGBResidualDF_d(ElGBContext ctx, int n, int nrhs, const double* A,
+                     int lda, const double* X, int ldx, const double* B,
+                     int ldb, double* R, int ldr);
 
 /* The residual of ElGBResidual_d for callers that cannot allocate device
  * memory: device memory budgeted up front or owned by another allocator, or

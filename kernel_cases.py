@@ -8,6 +8,8 @@ can skip the first launch of the kernel it targets).
     python kernel_cases.py lu64 --n 4096
     python kernel_cases.py batched --n 1024 --count 152 --precision fp32
     python kernel_cases.py lufull --n 2048
+    python kernel_cases.py residual --n 32768 --nrhs 16
+    python kernel_cases.py lu_breakdown --n 32768 --nb 512
 
 Each prints one JSON line with the event-timed duration of the measured
 call and its algorithmic work.  Inputs are seeded N(0, 1), generated on the
@@ -98,7 +100,7 @@ def case_refine(ctx, a):
 def case_batched(ctx, a):
     """`count` N(0, 1) LU systems of order n, one persistent batched launch
     (warm-up replay, then the measured replay)."""
-    from .batched import BatchedSolver
+    from elemental_gb300.batched import BatchedSolver
     g = torch.Generator(device="cuda").manual_seed(a.seed)
     A = torch.randn(a.count * a.n * a.n, device="cuda", generator=g, dtype=torch.float64)
     B = torch.randn(a.count * a.n * a.nrhs, device="cuda", generator=g, dtype=torch.float64)
@@ -138,8 +140,46 @@ def case_lufull(ctx, a):
                 status=ctx.status())
 
 
+def case_residual(ctx, a):
+    """The refinement's residual R = B - A X (n x nrhs): double-float on the
+    FP32 pipe (ElGBResidualDF_d, including its split of A) and FP64
+    (ElGBResidual_d), each timed once after a warm-up call."""
+    g = torch.Generator(device="cuda").manual_seed(a.seed)
+    A = D.colmajor(a.n, a.n)
+    X = D.colmajor(a.n, a.nrhs)
+    B = D.colmajor(a.n, a.nrhs)
+    A.copy_(torch.randn(a.n, a.n, device="cuda", generator=g, dtype=torch.float64))
+    X.copy_(torch.randn(a.n, a.nrhs, device="cuda", generator=g, dtype=torch.float64))
+    B.copy_(torch.randn(a.n, a.nrhs, device="cuda", generator=g, dtype=torch.float64))
+    ctx.residual_df(A, X, B)
+    ms_df = _timed(lambda: ctx.residual_df(A, X, B))
+    ctx.residual(A, X, B)
+    ms_64 = _timed(lambda: ctx.residual(A, X, B))
+    fl = 2.0 * a.n * a.n * a.nrhs
+    return dict(case="residual", n=a.n, nrhs=a.nrhs, ms_df_with_split=ms_df, ms_fp64=ms_64,
+                tflops_eq_df=fl / (ms_df * 1e-3) / 1e12, tflops_fp64=fl / (ms_64 * 1e-3) / 1e12)
+
+
+def case_lu_breakdown(ctx, a):
+    """El::LU on an FP32 matrix (tensor-core updates) with the per-kernel
+    event timing of the library's profiler: panel, swaps, TRSM, GEMMs."""
+    g = torch.Generator(device="cuda").manual_seed(a.seed)
+    A0 = torch.randn(a.n, a.n, device="cuda", generator=g).t()
+    A = A0.clone()
+    ctx.lu_mixed(A, gemm_kind=a.kind, nb=a.nb)
+    A.copy_(A0)
+    ctx.profile_start()
+    ms = _timed(lambda: ctx.lu_mixed(A, gemm_kind=a.kind, nb=a.nb))
+    prof = ctx.profile_stop()
+    return dict(case="lu_breakdown", n=a.n, kind=KIND_NAMES[a.kind], ms=ms,
+                tflops=2.0 / 3.0 * a.n ** 3 / (ms * 1e-3) / 1e12,
+                kernel_ms={k: round(v["ms"], 3) for k, v in prof["by_kernel"].items()},
+                kernel_launches={k: v["launches"] for k, v in prof["by_kernel"].items()})
+
+
 CASES = {"tc_gemm": case_tc_gemm, "lu": case_lu, "lu64": case_lu64, "refine": case_refine,
-         "batched": case_batched, "lufull": case_lufull}
+         "batched": case_batched, "lufull": case_lufull, "residual": case_residual,
+         "lu_breakdown": case_lu_breakdown}
 
 
 def main(argv=None):
