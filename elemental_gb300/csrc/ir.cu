@@ -329,7 +329,9 @@ cudaError_t refined_solve(Context* ctx, int n, const double* A, long lda, int nr
   const int nblk = trsv_blocks(n);
   need += 2 * al((size_t)nblk * 4096 * sizeof(float)) + al((size_t)nblk * sizeof(int)) +
           al(sizeof(unsigned));
-  const bool df = ctx->opt_residual_df != 0;
+  // double-float residuals where the FP64 pipe bounds the residual (below
+  // n = 2048 it costs little either way)
+  const bool df = ctx->opt_residual_df != 0 && n >= 2048;
   const size_t xs_count = ((size_t)(n + 63) / 64 * 64 + 1) * 16;
   need += al(2 * df_split_parts(n) * sizeof(double)) + al(2 * sizeof(double));
   if (df)

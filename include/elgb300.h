@@ -62,9 +62,10 @@ int ElGBSetBlocksize(int nb);
  *                       threads x 2 rows per CTA); 0 (default): in shared
  *                       memory.  Process-wide.
  *   ELGB_OPT_RESIDUAL_DF 1 (default): ElGBRefinedSolve_d computes its
- *                       residuals and GMRES products in double-float
- *                       arithmetic on the FP32 pipe (FP64-level accuracy);
- *                       0: in FP64 arithmetic. */
+ *                       residuals and GMRES products for n >= 2048 in
+ *                       double-float arithmetic on the FP32 pipe
+ *                       (FP64-level accuracy, see ElGBResidualDF_d);
+ *                       0: always in FP64 arithmetic. */
 enum {
   ELGB_OPT_LOOKAHEAD = 1,
   ELGB_OPT_PANEL_CTAS = 2,
@@ -399,7 +400,9 @@ int ElGBResidual_d(ElGBContext ctx, int n, int nrhs, const double* A,
  * arithmetic on the FP32 pipe: the residual ElGBRefinedSolve_d computes by
  * default (ELGB_OPT_RESIDUAL_DF).  Each call splits A into two FP32 words
  * (8 n^2 bytes of context scratch), then 2 n^2 nrhs double-float products.
- * Deterministic order.  The residual of the refinement loop of reference
+ * Each entry is within 16 ulps of sum_j |a_ij x_j| + |b_i| of the exact
+ * residual for n >= 1024 (32 below); A's entries must lie in FP32's
+ * exponent range (outside it the FP64 kernels run).  Deterministic order.  The residual of the refinement loop of reference
  * include/El/lapack_like/solve/Refined.hpp:70-73. */
 int ElGBResidualDF_d(ElGBContext ctx, int n, int nrhs, const double* A,
                      int lda, const double* X, int ldx, const double* B,
