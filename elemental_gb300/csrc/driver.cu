@@ -60,6 +60,7 @@ Context::~Context() {
   if (side_stream) cudaStreamDestroy(side_stream);
   if (arena) cudaFree(arena);
   if (arena2) cudaFree(arena2);
+  if (trace_buf) cudaFree(trace_buf);
   if (status) cudaFree(status);
   if (h_status) cudaFreeHost(h_status);
   if (own_stream) cudaStreamDestroy(own_stream);
@@ -222,6 +223,8 @@ struct LuState {
   int* dlab;           // deferred left interchanges: labels per block column
   T* dtmp;             //   and the gather's scratch
   bool tournament;     // FP32 leaf panels by tournament pivoting
+  unsigned long long* trace;  // leaf-panel timestamps (4 per column), or null
+  int trace_cols;
 };
 
 // Blocked TRSM, left / lower / unit: B := L11^{-1} B with L11 nb x nb (any
@@ -290,8 +293,10 @@ static cudaError_t panel_rec(LuState<T>& s, const LuLane& L, int c0, int w) {
       }
     }
     if (!done) {
+      PanelScratch<T> ps = s.ps;
+      ps.trace = (s.trace && c0 + w <= s.trace_cols) ? s.trace + 4 * (long)c0 : nullptr;
       LANE_CHECK(launch_getf2_panel<T>(s.A + c0 + (long)c0 * s.lda, s.lda, s.m - c0, w,
-                                       s.ipiv + c0, c0, c0, s.panel_epoch, s.ps, ctx->status,
+                                       s.ipiv + c0, c0, c0, s.panel_epoch, ps, ctx->status,
                                        s.panel_ctas, L.st, s.nopiv), 1);
       s.panel_epoch += w;
     }
@@ -494,6 +499,8 @@ cudaError_t getrf(Context* ctx, int m, int n, T* A, long lda, int* ipiv, int nb,
   if (ctx->opt_panel_ctas > 0) s.panel_ctas = std::min(ctx->opt_panel_ctas, ctx->num_sms);
   s.tournament = tournament && sizeof(T) == 4;
   s.nopiv = nopiv;
+  s.trace = ctx->trace_buf;
+  s.trace_cols = ctx->trace_cols;
   s.A = A;
   s.lda = lda;
   s.m = m;
@@ -1219,9 +1226,36 @@ int ElGBSetOption(ElGBContext ctx, int option, int value) {
     case ELGB_OPT_RESIDUAL_DF:
       ctx->opt_residual_df = value ? 1 : 0;
       return 0;
+    case ELGB_OPT_PANEL_TRACE: {
+      if (value < 0) return elgb::kElArgError;
+      cudaSetDevice(ctx->device);
+      if (ctx->trace_buf) cudaFree(ctx->trace_buf);
+      ctx->trace_buf = nullptr;
+      ctx->trace_cols = 0;
+      if (value > 0) {
+        const size_t bytes = 4 * (size_t)value * sizeof(unsigned long long);
+        if (cudaMalloc(&ctx->trace_buf, bytes) != cudaSuccess) return elgb::kElAllocError;
+        if (cudaMemset(ctx->trace_buf, 0, bytes) != cudaSuccess) return elgb::kElRuntimeError;
+        ctx->trace_cols = value;
+      }
+      return 0;
+    }
     default:
       return elgb::kElArgError;
   }
+}
+
+int ElGBPanelTrace(ElGBContext ctx, unsigned long long* out, int ncols) {
+  if (!ctx || !out || ncols < 0 || ncols > ctx->trace_cols) return elgb::kElArgError;
+  if (ncols == 0) return 0;
+  cudaSetDevice(ctx->device);
+  if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return elgb::kElRuntimeError;
+  if (ctx->side_stream && cudaStreamSynchronize(ctx->side_stream) != cudaSuccess)
+    return elgb::kElRuntimeError;
+  return cudaMemcpy(out, ctx->trace_buf, 4 * (size_t)ncols * sizeof(unsigned long long),
+                    cudaMemcpyDeviceToHost) == cudaSuccess
+             ? 0
+             : elgb::kElRuntimeError;
 }
 
 int ElGBBlocksize(void) { return elgb::get_blocksize(); }

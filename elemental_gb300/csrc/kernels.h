@@ -29,6 +29,12 @@ struct PanelScratch {
   PanelSlot<T>* slots;
   int maxG;
   int* cand;  // tournament pivoting: maxG x 33 candidate lists
+  // panel trace (ElGBSetOption(ELGB_OPT_PANEL_TRACE)): when set, CTA 0 of a
+  // leaf panel stamps %globaltimer four times per column at trace[4 j ..]
+  // (before its candidate is published, after the previous step's deferred
+  // update, once the exchange is complete, after the step's front half and
+  // argmax); null: no trace
+  unsigned long long* trace = nullptr;
 };
 
 // Tournament-pivoted leaf panel of the FP32 (preconditioner) LU, w <= 32

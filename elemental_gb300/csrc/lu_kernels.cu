@@ -285,6 +285,8 @@ getf2_panel_kernel(PanelParams<T> p) {
     const int epoch = p.epoch_base + j + 1;
     const int par = epoch & 1;
     PanelSlot<T>* my = p.s.slots + (long)par * maxG + b;
+    unsigned long long* tr = (p.s.trace && b == 0 && tid == 0) ? p.s.trace + 4 * (long)j : nullptr;
+    if (tr) tr[0] = globaltimer_ns();
     // 1. publish (the release store orders the CTA's slot writes, which
     // the barrier makes visible to the publishing thread); the rows carry
     // the pending step's update
@@ -300,6 +302,7 @@ getf2_panel_kernel(PanelParams<T> p) {
     // the rest of the previous step's update while the other CTAs publish
     if (pj >= 0) panel_step_back<T>(slab, R, nr, r0p, pj, w, plp, urowp);
     __syncthreads();  // urowp (s_rows / s_d) is read before the exchange refills them
+    if (tr) tr[1] = globaltimer_ns();
     // 2. the barrier: every slot carries this epoch.  The thread that polled
     // slot g copies g's candidate row (and, for the owner of row j, row j)
     // right away, so the winner's row is already on chip after the barrier.
@@ -326,6 +329,7 @@ getf2_panel_kernel(PanelParams<T> p) {
     }
     __syncthreads();
     if (s_abort) return;
+    if (tr) tr[2] = globaltimer_ns();
     // 3. reduce (every warp, identical result)
     int piv;
     {
@@ -358,6 +362,7 @@ getf2_panel_kernel(PanelParams<T> p) {
     if (pl >= 0 && tid < j) slab[tid * R + pl] = s_d[tid];
     panel_step_front<T>(slab, R, nr, r0, j, w, pl, s_d, urow, singular, inv, rb, bv, br);
     block_argmax_nolead(bv, br, s_rv, s_rr);
+    if (tr) tr[3] = globaltimer_ns();
     pj = j;
     plp = pl;
     r0p = r0;
@@ -626,6 +631,8 @@ getf2_panel_cluster_kernel(PanelParams<T> p) {
   const T* urowp = nullptr;
   for (int j = 0; j < w; ++j) {
     ClusterSlot<T>* my = &slots[j & 1];
+    unsigned long long* tr = (p.s.trace && b == 0 && tid == 0) ? p.s.trace + 4 * (long)j : nullptr;
+    if (tr) tr[0] = globaltimer_ns();
     // 1. publish in this CTA's shared memory (rows with the pending update)
     if (br >= 0 && tid < w) my->cand[tid] = pending_value(slab, R, br - rb, tid, pj, plp, urowp);
     if (j >= rb && j < re && tid < w)
@@ -638,6 +645,7 @@ getf2_panel_cluster_kernel(PanelParams<T> p) {
     // the rest of the previous step's update while the cluster gathers
     if (pj >= 0) panel_step_back<T>(slab, R, nr, r0p, pj, w, plp, urowp);
     __syncthreads();  // urowp (s_rows / s_d) is read before the exchange refills them
+    if (tr) tr[1] = globaltimer_ns();
     cluster_wait();
     // 2. thread g < C reads CTA g's slot
     if (tid < G) {
@@ -665,6 +673,7 @@ getf2_panel_cluster_kernel(PanelParams<T> p) {
         for (int c = 0; c < W; ++c) s_d[c] = dr[c];
     }
     __syncthreads();
+    if (tr) tr[2] = globaltimer_ns();
     // 3. reduce (every warp, identical result)
     int piv;
     {
@@ -692,6 +701,7 @@ getf2_panel_cluster_kernel(PanelParams<T> p) {
     if (pl >= 0 && tid < j) slab[tid * R + pl] = s_d[tid];
     panel_step_front<T>(slab, R, nr, r0, j, w, pl, s_d, urow, singular, inv, rb, bv, br);
     block_argmax_nolead(bv, br, s_rv, s_rr);
+    if (tr) tr[3] = globaltimer_ns();
     pj = j;
     plp = pl;
     r0p = r0;
@@ -722,7 +732,8 @@ static int cluster_ctas(int mp, int max_cluster) {
 template <typename T>
 static cudaError_t launch_getf2_panel_cluster(T* A, long lda, int mp, int w, int* ipiv,
                                               int row_base, int info_base, DevStatus* st,
-                                              int C, cudaStream_t stream) {
+                                              int C, unsigned long long* trace,
+                                              cudaStream_t stream) {
   const int R = ceil_div(mp, C);
   const size_t smem = ((size_t)R + C) * kPanelW * sizeof(T);
   auto kern = getf2_panel_cluster_kernel<T, kPanelW>;
@@ -749,7 +760,9 @@ static cudaError_t launch_getf2_panel_cluster(T* A, long lda, int mp, int w, int
     cudaGetLastError();
     return cudaErrorNotSupported;
   }
-  PanelParams<T> prm{A, lda, mp, w, R, ipiv, row_base, info_base, 0, PanelScratch<T>{}, st};
+  PanelScratch<T> ps{};
+  ps.trace = trace;
+  PanelParams<T> prm{A, lda, mp, w, R, ipiv, row_base, info_base, 0, ps, st};
   return cudaLaunchKernelEx(&cfg, kern, prm);
 }
 
@@ -780,7 +793,8 @@ cudaError_t launch_getf2_panel(T* A, long lda, int mp, int w, int* ipiv, int row
     const int C = cluster_ctas<T>(mp, g_panel_cluster);
     if (C > 0) {
       const cudaError_t e =
-          launch_getf2_panel_cluster<T>(A, lda, mp, w, ipiv, row_base, info_base, st, C, stream);
+          launch_getf2_panel_cluster<T>(A, lda, mp, w, ipiv, row_base, info_base, st, C, s.trace,
+                                        stream);
       if (e != cudaErrorNotSupported) return e;
     }
   }

@@ -112,8 +112,18 @@ class Context:
         """ElGBSetOption: "lookahead" (0/1), "panel_ctas" (0 = auto) or
         "tournament" (0/1: tournament pivoting in lu_mixed's leaf panels)."""
         code = {"lookahead": 1, "panel_ctas": 2, "tournament": 3, "panel_cluster": 4,
-                "panel_regs": 5, "residual_df": 6}[option]
+                "panel_regs": 5, "residual_df": 6, "panel_trace": 7}[option]
         self._rc(self.lib.ElGBSetOption(self.h, code, int(value)), "SetOption")
+
+    def panel_trace(self, ncols):
+        """Per-column leaf-panel timestamps of the last factorization (see
+        ELGB_OPT_PANEL_TRACE): int64 array (ncols, 4), ns."""
+        import numpy as np
+
+        out = np.zeros((ncols, 4), dtype=np.uint64)
+        self._rc(self.lib.ElGBPanelTrace(self.h, out.ctypes.data_as(ctypes.c_void_p), ncols),
+                 "PanelTrace")
+        return out.astype(np.int64)
 
     def launches(self):
         return int(self.lib.ElGBLaunchCount(self.h))

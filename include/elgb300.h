@@ -65,16 +65,32 @@ int ElGBSetBlocksize(int nb);
  *                       residuals and GMRES products for n >= 2048 in
  *                       double-float arithmetic on the FP32 pipe
  *                       (FP64-level accuracy, see ElGBResidualDF_d);
- *                       0: always in FP64 arithmetic. */
+ *                       0: always in FP64 arithmetic.
+ *   ELGB_OPT_PANEL_TRACE value > 0: the context keeps a device buffer of
+ *                       4 timestamps per column (%globaltimer, ns) for the
+ *                       first `value` columns of each LU it factors; CTA 0
+ *                       of each leaf panel stamps, per pivot step: before
+ *                       publishing its candidate, after the previous step's
+ *                       deferred rank-1 update, once the pivot exchange is
+ *                       complete, after the step's multipliers, next column
+ *                       and argmax.  Read with ElGBPanelTrace.  0 (default):
+ *                       off. */
 enum {
   ELGB_OPT_LOOKAHEAD = 1,
   ELGB_OPT_PANEL_CTAS = 2,
   ELGB_OPT_TOURNAMENT = 3,
   ELGB_OPT_PANEL_CLUSTER = 4,
   ELGB_OPT_PANEL_REGS = 5,
-  ELGB_OPT_RESIDUAL_DF = 6
+  ELGB_OPT_RESIDUAL_DF = 6,
+  ELGB_OPT_PANEL_TRACE = 7
 };
 int ElGBSetOption(ElGBContext ctx, int option, int value);
+
+/* Copies the first ncols columns' panel timestamps (4 * ncols values, see
+ * ELGB_OPT_PANEL_TRACE) to host memory `out`; synchronizes the context.
+ * Columns that no leaf panel traced (e.g. factored by the batched kernel)
+ * hold zeros. */
+int ElGBPanelTrace(ElGBContext ctx, unsigned long long* out, int ncols);
 
 /* Number of kernel launches this context has issued so far. */
 long long ElGBLaunchCount(ElGBContext ctx);

@@ -10,6 +10,7 @@ can skip the first launch of the kernel it targets).
     python kernel_cases.py lufull --n 2048
     python kernel_cases.py residual --n 32768 --nrhs 16
     python kernel_cases.py lu_breakdown --n 32768 --nb 512
+    python kernel_cases.py panel_trace --n 32768 --nb 512
 
 Each prints one JSON line with the event-timed duration of the measured
 call and its algorithmic work.  Inputs are seeded N(0, 1), generated on the
@@ -177,9 +178,53 @@ def case_lu_breakdown(ctx, a):
                 kernel_launches={k: v["launches"] for k, v in prof["by_kernel"].items()})
 
 
+def case_panel_trace(ctx, a):
+    """El::LU on an FP32 matrix (tensor-core updates) with the leaf-panel
+    trace on: per pivot step, the time from publishing the candidate to the
+    end of the previous step's deferred update (publish + deferred update),
+    from there to the complete exchange (exchange wait), and the step's
+    front half (swap, multipliers, next column, argmax); medians over the
+    columns of the leaves of each height band."""
+    import numpy as np
+
+    g = torch.Generator(device="cuda").manual_seed(a.seed)
+    A0 = torch.randn(a.n, a.n, device="cuda", generator=g).t()
+    A = A0.clone()
+    ctx.set_option("panel_trace", a.n)
+    try:
+        ctx.lu_mixed(A, gemm_kind=a.kind, nb=a.nb)
+        A.copy_(A0)
+        ms = _timed(lambda: ctx.lu_mixed(A, gemm_kind=a.kind, nb=a.nb))
+        tr = ctx.panel_trace(a.n)
+    finally:
+        ctx.set_option("panel_trace", 0)
+    ok = np.all(tr > 0, axis=1)
+    cols = np.arange(a.n)
+    d_pub = (tr[:, 1] - tr[:, 0]) / 1e3
+    d_x = (tr[:, 2] - tr[:, 1]) / 1e3
+    d_front = (tr[:, 3] - tr[:, 2]) / 1e3
+    step = np.full(a.n, np.nan)
+    same_leaf = (cols[1:] // 32) == (cols[:-1] // 32)
+    step[:-1][same_leaf] = (tr[1:, 0] - tr[:-1, 0])[same_leaf] / 1e3
+    bands = {}
+    for lo, hi in [(0, 8192), (8192, 16384), (16384, 24576), (24576, a.n)]:
+        sel = ok & (a.n - cols > lo) & (a.n - cols <= hi)
+        if not sel.any():
+            continue
+        bands[f"rows {lo + 1}-{hi}"] = {
+            "columns": int(sel.sum()),
+            "us_publish_and_deferred_update": round(float(np.median(d_pub[sel])), 3),
+            "us_exchange_wait": round(float(np.median(d_x[sel])), 3),
+            "us_front_half": round(float(np.median(d_front[sel])), 3),
+            "us_per_step": round(float(np.nanmedian(step[sel])), 3)}
+    tot_steps = float(np.nansum(step[ok])) / 1e3
+    return dict(case="panel_trace", n=a.n, kind=KIND_NAMES[a.kind], ms=ms, traced=int(ok.sum()),
+                leaf_step_ms_total=tot_steps, bands=bands)
+
+
 CASES = {"tc_gemm": case_tc_gemm, "lu": case_lu, "lu64": case_lu64, "refine": case_refine,
          "batched": case_batched, "lufull": case_lufull, "residual": case_residual,
-         "lu_breakdown": case_lu_breakdown}
+         "lu_breakdown": case_lu_breakdown, "panel_trace": case_panel_trace}
 
 
 def main(argv=None):

@@ -66,12 +66,11 @@ def test_df_residual_is_correctly_rounded_to_a_few_ulps(ctx, n, q):
     # of the row's scale (measured at most 6 ulps by a bit-faithful CPU
     # emulation of the same arithmetic at n <= 4096)
     assert err.max() <= (16 if n >= 1024 else 32) * EPS, err.max()
-    # normwise it is at the FP64 kernel's level
-    R64 = ctx.residual(dev(A), dev(X), dev(B)).cpu().numpy()
+    # normwise, in the units of the backward error ||r|| / (||A|| ||x|| +
+    # ||b||), it is well below one FP64 rounding error
     den = np.linalg.norm(A) * np.linalg.norm(X) + np.linalg.norm(B)
     nw = np.linalg.norm(Rg[rows] - Rex) / den
-    nw64 = np.linalg.norm(R64[rows] - Rex) / den
-    assert nw <= max(4 * nw64, 4 * EPS / np.sqrt(n)), (nw, nw64)
+    assert nw <= 2 * EPS, nw
 
 
 def test_df_product_without_b_and_extreme_scaling(ctx):
