@@ -76,6 +76,10 @@ def parse():
                         "(0, the default: A iid N(0,1))")
     p.add_argument("--tol", type=float, default=0.0,
                    help="lu-ir: target normwise backward error (0, the default: n*eps64)")
+    p.add_argument("--max-iters", type=int, default=0,
+                   help="lu-ir: refinement steps (GMRES-IR: inner iterations) before the FP64 "
+                        "fallback (0: the library's default)")
+    p.add_argument("--restart", type=int, default=0, help="lu-ir, GMRES-IR: restart length")
     p.add_argument("--count", type=int, default=0, help="systems (batched / selector)")
     p.add_argument("--train-count", type=int, default=3000, help="selector training systems")
     return p.parse_args()
@@ -290,7 +294,8 @@ def gpu_arm(args, rank, world, local_rank):
 
     def solve(tol=args.tol):
         return ctx.refined_solve(A, B, X, precision=args.precision, method=args.method,
-                                 nb=args.nb, tol=tol)
+                                 nb=args.nb, tol=tol, max_iters=args.max_iters,
+                                 restart=args.restart)
 
     info = None
     for _ in range(max(args.warmup, 0)):
@@ -505,6 +510,7 @@ def gpu_arm(args, rank, world, local_rank):
                    "n": n, "nrhs": q, "precision": args.precision, "method": args.method,
                    "kappa": args.kappa if args.kappa > 0 else None,
                    "tol": args.tol if args.tol > 0 else n * EPS64,
+                   "max_iters": args.max_iters or None, "restart": args.restart or None,
                    "nb": args.nb or 512, "l2": "inputs larger than L2 (A is 8 GiB)",
                    "parallelism": f"replicas x{world}"},
         "tflops_eq": value * flops_per_solve(n, q) / 1e12,
