@@ -476,6 +476,8 @@ def gpu_arm(args, rank, world, local_rank):
         roofline["frac_of_operand_ceiling"] = tf_achieved * per_bf16 / peak
     breakdown = {k: {"launches": v["launches"], "ms_per_step": v["ms"] / args.steps}
                  for k, v in prof["by_kernel"].items()}
+    for k, v in prof.get("by_kernel_lookahead_stream", {}).items():
+        breakdown[k]["lookahead_stream_ms_per_step"] = v["ms"] / args.steps
     cpu = None
     if args.cpu_baseline == "on":
         ns = min(args.cpu_n, n)

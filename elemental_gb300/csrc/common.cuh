@@ -108,6 +108,25 @@ __device__ __forceinline__ void warp_argmax(T& v, int& r) {
   }
 }
 
+// FP32: two warp reductions instead of five shuffle rounds.  Non-negative
+// floats order as their bit patterns, so the largest |value| is a max over
+// (bits + 1), with empty slots (-1) and NaN mapped to 0, which never wins;
+// the row is then the lowest among the lanes holding that value.  Without
+// NaN the result equals argmax_better's order; every lane gets it.
+__device__ __forceinline__ void warp_argmax(float& v, int& r) {
+  const unsigned key = v >= 0.f ? (__float_as_uint(v) & 0x7fffffffu) + 1u : 0u;
+  const unsigned kmax = __reduce_max_sync(0xffffffffu, key);
+  const unsigned rmin =
+      __reduce_min_sync(0xffffffffu, key == kmax ? (unsigned)r : 0xffffffffu);
+  if (kmax == 0u) {
+    v = -1.f;
+    r = -1;
+  } else {
+    v = __uint_as_float(kmax - 1u);
+    r = (int)rmin;
+  }
+}
+
 __host__ __device__ constexpr int ceil_div(int a, int b) { return (a + b - 1) / b; }
 // grid.y of a launch with one column per y index: at most 65535, so the
 // kernels loop over the columns j = blockIdx.y, blockIdx.y + gridDim.y, ...

@@ -51,6 +51,7 @@ void Context::prof_end(int idx, cudaStream_t st, int tag, double flops, double b
   prof[idx].tag = tag;
   prof[idx].flops = flops;
   prof[idx].bytes = bytes;
+  prof[idx].side = st == side_stream && side_stream != nullptr;
 }
 
 Context::~Context() {
@@ -194,7 +195,8 @@ static cudaError_t gemm_sub(Context* ctx, const LuLane& L, int m, int n, int k, 
       const double esz = kind == kTcBF16 ? 2.0 : kind == kTcFP8 ? 1.0 : 4.0;
       const double copies = kind == kTcTF32x3 ? 2.0 : 1.0;
       ctx->prof.push_back({a, b, 2.0 * m * n * (double)k,
-                           8.0 * m * n + copies * esz * (double)k * (m + n), ELGB_PROF_TC_GEMM});
+                           8.0 * m * n + copies * esz * (double)k * (m + n), ELGB_PROF_TC_GEMM,
+                           L.st == ctx->side_stream && ctx->side_stream != nullptr});
     }
     return e;
   }
@@ -1176,11 +1178,14 @@ int ElGBProfileStop(ElGBContext ctx, long long* launches, double* ms, double* fl
     if (!r.b || r.tag < 0 || r.tag >= 16) continue;
     float x = 0;
     if (cudaEventElapsedTime(&x, r.a, r.b) != cudaSuccess) return elgb::kElRuntimeError;
-    auto& ps = ctx->prof_sum[r.tag];
-    ps.launches += 1;
-    ps.ms += x;
-    ps.flops += r.flops;
-    ps.bytes += r.bytes;
+    for (int t : {r.tag, r.side && r.tag < 8 ? r.tag + 8 : -1}) {
+      if (t < 0) continue;
+      auto& ps = ctx->prof_sum[t];
+      ps.launches += 1;
+      ps.ms += x;
+      ps.flops += r.flops;
+      ps.bytes += r.bytes;
+    }
   }
   const auto& g = ctx->prof_sum[ELGB_PROF_TC_GEMM];
   const double t = g.ms, f = g.flops, b = g.bytes;

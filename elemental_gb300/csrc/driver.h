@@ -50,7 +50,8 @@ struct Context {
   struct ProfRec {
     cudaEvent_t a, b;
     double flops, bytes;
-    int tag;  // ELGB_PROF_*
+    int tag;            // ELGB_PROF_*
+    bool side = false;  // recorded on the look-ahead panel stream
   };
   struct ProfSum {
     long long launches = 0;

@@ -144,6 +144,13 @@ class Context:
                                              ctypes.byref(fl), ctypes.byref(by)), "ProfileTag")
             tags[name] = dict(launches=n.value, ms=ms.value)
         out["by_kernel"] = tags
+        side = {}
+        for name, tag in PROFILE_TAGS.items():
+            self._rc(self.lib.ElGBProfileTag(self.h, tag + 8, ctypes.byref(n), ctypes.byref(ms),
+                                             ctypes.byref(fl), ctypes.byref(by)), "ProfileTag")
+            if n.value:
+                side[name] = dict(launches=n.value, ms=ms.value)
+        out["by_kernel_lookahead_stream"] = side
         return out
 
     # -- the path -----------------------------------------------------------

@@ -112,7 +112,10 @@ enum {
   ELGB_PROF_TRSM = 3,      /* diagonal-block triangular solves (factorization) */
   ELGB_PROF_GEMM_SIMT = 4, /* CUDA-core GEMM (FP64 path, small FP32 updates) */
   ELGB_PROF_RESIDUAL = 5,  /* FP64 residual b - A x                          */
-  ELGB_PROF_SOLVE = 6      /* low-precision triangular solves of refinement  */
+  ELGB_PROF_SOLVE = 6,     /* low-precision triangular solves of refinement  */
+  ELGB_PROF_SIDE = 8       /* + tag: that kernel's launches on the look-ahead
+                              panel stream only (the factorization's critical
+                              chain); the plain tags count both streams     */
 };
 int ElGBProfileTag(ElGBContext ctx, int tag, long long* launches, double* ms,
                    double* flops, double* bytes);

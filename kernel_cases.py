@@ -175,6 +175,8 @@ def case_lu_breakdown(ctx, a):
     return dict(case="lu_breakdown", n=a.n, kind=KIND_NAMES[a.kind], ms=ms,
                 tflops=2.0 / 3.0 * a.n ** 3 / (ms * 1e-3) / 1e12,
                 kernel_ms={k: round(v["ms"], 3) for k, v in prof["by_kernel"].items()},
+                kernel_ms_lookahead_stream={k: round(v["ms"], 3)
+                                            for k, v in prof["by_kernel_lookahead_stream"].items()},
                 kernel_launches={k: v["launches"] for k, v in prof["by_kernel"].items()})
 
 
