@@ -94,3 +94,26 @@ def test_network_gains_over_fp64_and_the_kappa_rule(ctx, trained):
     # solve; the gain grows with n, ~1.5x at n in [64, 2048])
     assert tm < 0.95 * t64, (tm, t64)
     assert tm < tr, (tm, tr)
+
+
+def test_network_against_the_fitted_kappa_rule(ctx, trained):
+    """The stronger baseline: kappa thresholds fitted to the same training
+    outcomes.  The network matches it (the condition estimate is the feature
+    that decides); the test holds it to within a few percent of that rule's
+    label accuracy and solver work, never worse by more."""
+    sel, F, y, te, Ft, yt = (trained[k] for k in ("sel", "F", "y", "te", "Ft", "yt"))
+    lk_tr = F[:, S.LOG10_KAPPA_FEATURE].cpu().numpy()
+    lk = Ft[:, S.LOG10_KAPPA_FEATURE].cpu().numpy()
+    thr, _ = S.fit_kappa_rule(lk_tr, y)
+    acc_mlp = float((sel.predict(Ft) == yt).mean())
+    acc_fit = float((S.kappa_rule(lk, *thr) == yt).mean())
+    assert acc_mlp >= acc_fit - 0.05, (acc_mlp, acc_fit)
+    res_m, _, bs = S.solve_selected(te, sel.params, ctx=ctx, tol=TOL)
+    bs.close()
+    res_f, _, bs = S.solve_selected(te, S.rule_network(*thr), ctx=ctx, tol=TOL)
+    bs.close()
+    for res in (res_m, res_f):
+        assert all(r["converged"] and r["backward_error"] <= TOL for r in res)
+    tm, tf = _device_s(res_m), _device_s(res_f)
+    print(f"device s: MLP {tm:.3f}  fitted kappa rule {tf:.3f}  (acc {acc_mlp:.2f} / {acc_fit:.2f})")
+    assert tm <= 1.05 * tf, (tm, tf)
