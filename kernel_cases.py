@@ -167,12 +167,14 @@ def case_lu_breakdown(ctx, a):
     g = torch.Generator(device="cuda").manual_seed(a.seed)
     A0 = torch.randn(a.n, a.n, device="cuda", generator=g).t()
     A = A0.clone()
+    ctx.set_option("lookahead", a.lookahead)
     ctx.lu_mixed(A, gemm_kind=a.kind, nb=a.nb)
     A.copy_(A0)
     ctx.profile_start()
     ms = _timed(lambda: ctx.lu_mixed(A, gemm_kind=a.kind, nb=a.nb))
     prof = ctx.profile_stop()
-    return dict(case="lu_breakdown", n=a.n, kind=KIND_NAMES[a.kind], ms=ms,
+    ctx.set_option("lookahead", 1)
+    return dict(case="lu_breakdown", n=a.n, kind=KIND_NAMES[a.kind], lookahead=a.lookahead, ms=ms,
                 tflops=2.0 / 3.0 * a.n ** 3 / (ms * 1e-3) / 1e12,
                 kernel_ms={k: round(v["ms"], 3) for k, v in prof["by_kernel"].items()},
                 kernel_ms_lookahead_stream={k: round(v["ms"], 3)
@@ -243,6 +245,7 @@ def main(argv=None):
     p.add_argument("--simt", action="store_true", help="batched: SIMT trailing updates")
     p.add_argument("--precision", default="fp32", choices=["fp64", "fp32", "bf16"])
     p.add_argument("--seed", type=int, default=20261204)
+    p.add_argument("--lookahead", type=int, default=1, help="lu_breakdown: 0 = one stream")
     a = p.parse_args(argv)
     ctx = D.context(0)
     out = CASES[a.case](ctx, a)
