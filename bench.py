@@ -290,6 +290,16 @@ def gpu_arm(args, rank, world, local_rank):
     B = D.colmajor(n, q)
     B.copy_(torch.randn(q, n, generator=g, device="cuda", dtype=torch.float64).t())
     X = D.colmajor(n, q)
+    # the host copies of the system for the end-to-end arm, made first, as a
+    # caller's data exists before any solve (pinned buffers allocated after
+    # the device arm's solves measured up to 8x slower host -> device
+    # copies on these boxes)
+    if args.e2e == "on":
+        Ah = torch.empty((n, n), dtype=torch.float64, pin_memory=True)
+        Ah.copy_(A.t())  # row-major (n, n) of A^T = column-major A
+        B0 = torch.empty((q, n), dtype=torch.float64, pin_memory=True)
+        B0.copy_(B.t())
+        Bh = torch.empty((q, n), dtype=torch.float64, pin_memory=True)
     torch.cuda.synchronize()
 
     def solve(tol=args.tol):
@@ -335,11 +345,6 @@ def gpu_arm(args, rank, world, local_rank):
     # up to 1.8x slower while the host side ramps back up)
     e2e = None
     if args.e2e == "on":
-        Ah = torch.empty((n, n), dtype=torch.float64, pin_memory=True)
-        Ah.copy_(A.t())  # row-major (n, n) of A^T = column-major A
-        B0 = torch.empty((q, n), dtype=torch.float64, pin_memory=True)
-        B0.copy_(B.t())
-        Bh = torch.empty((q, n), dtype=torch.float64, pin_memory=True)
         Am = El.Matrix(Ah.numpy().T)
         assert Am.array.ctypes.data == Ah.data_ptr()
         Bh.copy_(B0)
