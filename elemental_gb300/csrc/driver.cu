@@ -156,6 +156,10 @@ struct LuLane {
   int* pairs = nullptr;  // 4 * cap ints
   int* pair_count = nullptr;
   GemmCfg gemm;
+  // SMs the lane's tensor-core updates may hold (TcGridMode): while the
+  // look-ahead panel runs, the trailing update leaves a GPC free for it and
+  // the panel's own updates stay small
+  int grid_mode = kGridFull;
 };
 
 #define LANE_CHECK(expr, nk)                   \
@@ -189,7 +193,7 @@ static cudaError_t gemm_sub(Context* ctx, const LuLane& L, int m, int n, int k, 
       b = ctx->next_event();
     }
     cudaError_t e = launch_tc_gemm_sub(kind, m, n, k, A, lda, B, ldb, C, ldc, g.ws,
-                                       ctx->status, L.st, &nl, a, b);
+                                       ctx->status, L.st, &nl, a, b, L.grid_mode);
     ctx->launches += nl;
     if (a && b) {
       const double esz = kind == kTcBF16 ? 2.0 : kind == kTcFP8 ? 1.0 : 4.0;
@@ -402,9 +406,11 @@ static cudaError_t getrf_run(LuState<T>& s, int nb) {
       e = apply_swaps(s, s.main, k, jb, kn + jb2, s.n, 0, 0, true);
       if (e != cudaSuccess) return e;
     }
+    // beside the look-ahead panel the trailing update keeps off one GPC
+    if (split) s.main.grid_mode = kGridSpareGpc;
     e = update_cols(s, s.main, k, jb, kn + jb2, s.n);
-    if (e != cudaSuccess) return e;
-    e = update_companion(s, s.main, k, jb);
+    if (e == cudaSuccess) e = update_companion(s, s.main, k, jb);
+    s.main.grid_mode = kGridFull;
     if (e != cudaSuccess) return e;
     if (jb2 > 0) {
       if (la)
@@ -492,6 +498,7 @@ cudaError_t getrf(Context* ctx, int m, int n, T* A, long lda, int* ipiv, int nb,
   }
   if (la) {
     s.side.st = ctx->side_stream;
+    s.side.grid_mode = kGridSmall;
     s.side.gemm.tc_kind = tc ? inner_kind : -1;
     if (tc) {
       s.side.gemm.ws = cv.take<char>(tcs);

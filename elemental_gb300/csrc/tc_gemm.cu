@@ -5,23 +5,15 @@
 // updates, written for sm_103a with tcgen05 + TMEM + TMA in inline PTX.
 //
 // Operands are first packed (pack_a / pack_b) into K-major tiles of the
-// operand precision: BF16 (tcgen05.mma kind::f16) or TF32 (kind::tf32, FP32
-// storage rounded to TF32).  One CTA computes a 128 x 256 tile of C:
-//   warp 0 / lane 0  TMA producer: 128-byte-swizzled A and B k-blocks into a
-//                    2-stage shared-memory ring (mbarrier full/empty);
-//   warp 1 / lane 0  MMA issuer: 4 tcgen05.mma (K = 128 bytes) per k-block
-//                    into a 128 x 256 FP32 accumulator in TMEM, commits free
-//                    the stage and finally signal the epilogue;
-//   warps 0-7        epilogue: tcgen05.ld 32 lanes x 32 columns, C -= acc
-//                    with coalesced loads/stores (lane = row of the column-
-//                    major C), the C loads issued before the accumulator is
-//                    ready.
-// ~97 KB of shared memory and 256 TMEM columns per CTA, so two CTAs share an
-// SM and one's epilogue (HBM-bound) overlaps the other's MMA.  Every wait is
-// bounded (globaltimer); a timeout records an error and the CTA still frees
-// its TMEM.
+// operand precision: BF16 (tcgen05.mma kind::f16), TF32 (kind::tf32, FP32
+// storage rounded to TF32, optionally split hi + lo for three products) or
+// E4M3 (kind::f8f6f4, scaled per call).  tc_gemm_persistent_kernel then walks
+// the 128 x 256 C tiles with one CTA per SM of a bounded grid; its layout is
+// described above the kernel.
 #include <cuda.h>
 #include <cuda_bf16.h>
+
+#include <algorithm>
 #include <cuda_fp8.h>
 #include <cudaTypedefs.h>
 
@@ -38,11 +30,8 @@ using namespace tc;
 constexpr int kBM = 128;
 constexpr int kBN = 256;
 constexpr int kBKBytes = 128;  // one 128-byte swizzle row of K per stage
-constexpr int kStages = 2;
 constexpr int kStageA = kBM * kBKBytes;  // 16 KB
 constexpr int kStageB = kBN * kBKBytes;  // 32 KB
-constexpr int kTmemCols = 256;
-constexpr int kGemmThreads = 256;
 
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar,
                                             int x, int y) {
@@ -70,123 +59,212 @@ __host__ __device__ __forceinline__ float fp8_scale(float amax) {
   return ldexpf(1.f, ilogbf(448.f / amax));
 }
 
-// passes = 1: C -= A B.  passes = 3 (TF32 split, ~FP32 accuracy):
-// C -= Ahi Bhi + Ahi Blo + Alo Bhi, one accumulator, the three products
-// streamed through the same pipeline one after the other.
-template <int KIND>
-__global__ void __launch_bounds__(kGemmThreads, 2)
-tc_gemm_sub_kernel(const __grid_constant__ CUtensorMap tmA,
-                   const __grid_constant__ CUtensorMap tmB,
-                   const __grid_constant__ CUtensorMap tmAlo,
-                   const __grid_constant__ CUtensorMap tmBlo, float* __restrict__ C, long ldc,
-                   int m, int n, int num_kb, int passes, const float* __restrict__ amax,
-                   DevStatus* st) {
+// ---------------------------------------------------------------------------
+// Persistent form: one CTA per SM (of a bounded grid) walks the 128 x 256
+// tiles in m-fastest order.  Each stage of the shared-memory ring holds a
+// k-block of every operand copy at once -- for TF32x3 the hi and lo tiles of
+// A and of B (96 KB), from which the three products are issued, instead of
+// streaming the operands three times -- and two 256-column TMEM
+// accumulators let the epilogue of tile t overlap the MMAs of tile t + 1.
+//   warp 0 / lane 0  TMA producer over (tile, k-block), 2-stage ring (4 for
+//                    the single-product kinds);
+//   warp 1 / lane 0  MMA issuer; commits free a stage, and a finished
+//                    accumulator is signalled on tfull[b];
+//   warps 2..5       epilogue (warp w reads TMEM lanes 32 (w % 4) ..), C -=
+//                    acc, then one arrive per warp on tempty[b].
+// 197 KB of shared memory: one CTA per SM, so the grid bounds the SMs the
+// kernel holds (the look-ahead panel of the factorization keeps the rest).
+// Every wait is bounded; a timeout records an error and the CTA still frees
+// its TMEM.
+constexpr int kPThreads = 192;
+constexpr int kPRing = 192 * 1024;
+constexpr int kPTmemCols = 512;
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+template <int KIND, bool SPLIT>
+__global__ void __launch_bounds__(kPThreads, 1)
+tc_gemm_persistent_kernel(const __grid_constant__ CUtensorMap tmA,
+                          const __grid_constant__ CUtensorMap tmB,
+                          const __grid_constant__ CUtensorMap tmAlo,
+                          const __grid_constant__ CUtensorMap tmBlo, float* __restrict__ C,
+                          long ldc, int m, int n, int num_kb, const float* __restrict__ amax,
+                          DevStatus* st) {
+  constexpr int kStageBytes = (SPLIT ? 2 : 1) * (kStageA + kStageB);
+  constexpr int kS = kPRing / kStageBytes;  // 2 (split) or 4 stages
   extern __shared__ __align__(1024) unsigned char smem_raw[];
-  // 1024-byte alignment for the swizzled tiles
   unsigned char* base = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  unsigned char* sA = base;
-  unsigned char* sB = base + kStages * kStageA;
-  __shared__ __align__(8) uint64_t full_bar[kStages];
-  __shared__ __align__(8) uint64_t empty_bar[kStages];
-  __shared__ __align__(8) uint64_t accum_bar;
+  __shared__ __align__(8) uint64_t full_bar[kS];
+  __shared__ __align__(8) uint64_t empty_bar[kS];
+  __shared__ __align__(8) uint64_t tfull[2];
+  __shared__ __align__(8) uint64_t tempty[2];
+  __shared__ __align__(8) uint64_t drain_bar;
   __shared__ uint32_t s_tmem;
-  __shared__ int s_abort;
+  __shared__ volatile int s_abort;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * kBN;
+  const int tiles_m = (m + kBM - 1) / kBM, tiles_n = (n + kBN - 1) / kBN;
+  const int ntiles = tiles_m * tiles_n;
+  // stage s: A hi | B hi | A lo | B lo
+  auto sA = [&](int s) { return base + (size_t)s * kStageBytes; };
+  auto sB = [&](int s) { return base + (size_t)s * kStageBytes + kStageA; };
+  auto sAl = [&](int s) { return base + (size_t)s * kStageBytes + kStageA + kStageB; };
+  auto sBl = [&](int s) { return base + (size_t)s * kStageBytes + 2 * kStageA + kStageB; };
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < kStages; ++s) {
+    for (int s = 0; s < kS; ++s) {
       mbar_init(&full_bar[s], 1);
       mbar_init(&empty_bar[s], 1);
     }
-    mbar_init(&accum_bar, 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&tfull[b], 1);
+      mbar_init(&tempty[b], 4);
+    }
+    mbar_init(&drain_bar, 1);
     s_abort = 0;
     fence_mbar_init();
   }
-  if (warp == 1) tmem_alloc(&s_tmem, kTmemCols);
+  if (warp == 1) tmem_alloc(&s_tmem, kPTmemCols);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = s_tmem;
 
-  const int total_kb = num_kb * passes;
+  uint32_t it_issued = 0;  // producer: k-blocks whose loads were issued
   if (warp == 0 && lane == 0) {
     // TMA producer
-    for (int kb = 0; kb < total_kb; ++kb) {
-      const int s = kb % kStages;
-      if (kb >= kStages) {
-        if (!mbar_wait(&empty_bar[s], ((kb / kStages) & 1) ^ 1, st, 10)) {
+    uint32_t it = 0;
+    for (int t = blockIdx.x; t < ntiles && !s_abort; t += gridDim.x) {
+      const int m0 = (t % tiles_m) * kBM, n0 = (t / tiles_m) * kBN;
+      for (int kb = 0; kb < num_kb; ++kb, ++it) {
+        const int s = it % kS;
+        if (it >= (uint32_t)kS && !mbar_wait(&empty_bar[s], ((it / kS) & 1) ^ 1, st, 20)) {
           s_abort = 1;
           break;
         }
+        mbar_arrive_expect_tx(&full_bar[s], kStageBytes);
+        const int xk = kb * (kBKBytes / (KIND == kTcBF16 ? 2 : KIND == kTcFP8 ? 1 : 4));
+        tma_load_2d(sA(s), &tmA, &full_bar[s], xk, m0);
+        tma_load_2d(sB(s), &tmB, &full_bar[s], xk, n0);
+        if (SPLIT) {
+          tma_load_2d(sAl(s), &tmAlo, &full_bar[s], xk, m0);
+          tma_load_2d(sBl(s), &tmBlo, &full_bar[s], xk, n0);
+        }
+        it_issued = it + 1;
       }
-      const int pass = kb / num_kb;
-      mbar_arrive_expect_tx(&full_bar[s], kStageA + kStageB);
-      const int xk = (kb - pass * num_kb) * (kBKBytes / (KIND == kTcBF16 ? 2 : KIND == kTcFP8 ? 1 : 4));
-      tma_load_2d(sA + s * kStageA, pass == 2 ? &tmAlo : &tmA, &full_bar[s], xk, m0);
-      tma_load_2d(sB + s * kStageB, pass == 1 ? &tmBlo : &tmB, &full_bar[s], xk, n0);
     }
   } else if (warp == 1 && lane == 0) {
     // MMA issuer
     constexpr uint32_t idesc = idesc_m128n256<KIND>();
-    bool ok = true;
-    for (int kb = 0; kb < total_kb && ok; ++kb) {
-      const int s = kb % kStages;
-      if (!mbar_wait(&full_bar[s], (kb / kStages) & 1, st, 11)) {
+    uint32_t it = 0, lt = 0;
+    for (int t = blockIdx.x; t < ntiles && !s_abort; t += gridDim.x, ++lt) {
+      const int b = lt & 1;
+      const uint32_t u = lt >> 1;
+      if (lt >= 2 && !mbar_wait(&tempty[b], (u - 1) & 1, st, 21)) {
         s_abort = 1;
-        ok = false;
         break;
       }
       tc_fence_after();
-      const uint64_t adesc = sdesc_sw128(smem_u32(sA + s * kStageA));
-      const uint64_t bdesc = sdesc_sw128(smem_u32(sB + s * kStageB));
+      const uint32_t d = tmem + (uint32_t)(b * kBN);
+      bool ok = true;
+      for (int kb = 0; kb < num_kb; ++kb, ++it) {
+        const int s = it % kS;
+        if (!mbar_wait(&full_bar[s], (it / kS) & 1, st, 22)) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const uint64_t ah = sdesc_sw128(smem_u32(sA(s))), bh = sdesc_sw128(smem_u32(sB(s)));
+        const uint64_t al = sdesc_sw128(smem_u32(sAl(s))), bl = sdesc_sw128(smem_u32(sBl(s)));
 #pragma unroll
-      for (int kk = 0; kk < 4; ++kk)  // 4 x 32 bytes of K per 128-byte row
-        umma<KIND>(tmem, adesc + 2 * kk, bdesc + 2 * kk, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
-      umma_commit(&empty_bar[s]);
+        for (int kk = 0; kk < 4; ++kk) {  // 4 x 32 bytes of K per 128-byte row
+          umma<KIND>(d, ah + 2 * kk, bh + 2 * kk, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
+          if (SPLIT) {
+            umma<KIND>(d, ah + 2 * kk, bl + 2 * kk, idesc, 1u);
+            umma<KIND>(d, al + 2 * kk, bh + 2 * kk, idesc, 1u);
+          }
+        }
+        umma_commit(&empty_bar[s]);
+      }
+      if (!ok) {
+        s_abort = 1;
+        break;
+      }
+      umma_commit(&tfull[b]);
     }
-    umma_commit(&accum_bar);
-  }
-  __syncwarp();
-
-  // Epilogue: all 8 warps.  Warp w reads TMEM lanes 32*(w%4).. (rows) and
-  // the column half w/4.
-  const int wl = warp & 3, half = warp >> 2;
-  const int row = m0 + 32 * wl + lane;
-  const bool row_ok = row < m;
-  float* crow = C + row;
-  // FP8: the products carry the operands' scales (exact powers of two)
-  const float unscale = KIND == kTcFP8 ? 1.f / (fp8_scale(amax[0]) * fp8_scale(amax[1])) : 1.f;
-  bool ready = false;
-  for (int cc = 0; cc < 4; ++cc) {
-    const int cbase = half * 128 + cc * 32;
-    float cv[32];
+  } else if (warp >= 2) {
+    // epilogue: warp w reads TMEM lanes 32 * (w % 4) .. (rows of the tile)
+    const int q = warp & 3;
+    const float unscale =
+        KIND == kTcFP8 ? 1.f / (fp8_scale(amax[0]) * fp8_scale(amax[1])) : 1.f;
+    uint32_t lt = 0;
+    for (int t = blockIdx.x; t < ntiles && !s_abort; t += gridDim.x, ++lt) {
+      const int b = lt & 1;
+      const uint32_t u = lt >> 1;
+      const int m0 = (t % tiles_m) * kBM, n0 = (t / tiles_m) * kBN;
+      const int row = m0 + 32 * q + lane;
+      const bool row_ok = row < m;
+      float* crow = C + row;
+      float cv[32];
 #pragma unroll
-    for (int j = 0; j < 32; ++j) {
-      const int col = n0 + cbase + j;
-      cv[j] = (row_ok && col < n) ? crow[(long)col * ldc] : 0.f;
-    }
-    if (!ready) {
-      // warp-uniform decision: tcgen05.ld below is a whole-warp instruction
-      ready = __all_sync(0xffffffffu, mbar_wait(&accum_bar, 0, st, 12));
+      for (int j = 0; j < 32; ++j) {
+        const int col = n0 + j;
+        cv[j] = (row_ok && col < n) ? crow[(long)col * ldc] : 0.f;
+      }
+      // warp-uniform: tcgen05.ld below is a whole-warp instruction
+      const bool ready = __all_sync(0xffffffffu, mbar_wait(&tfull[b], u & 1, st, 23));
       tc_fence_after();
-      if (!ready) break;
-    }
-    uint32_t acc[32];
-    tmem_ld32(tmem + ((uint32_t)(32 * wl) << 16) + (uint32_t)cbase, acc);
+      if (!ready) {
+        s_abort = 1;
+        break;
+      }
+      for (int cc = 0; cc < kBN / 32; ++cc) {
+        uint32_t acc[32];
+        tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * kBN + cc * 32), acc);
+        float nx[32];
+        if (cc + 1 < kBN / 32) {
 #pragma unroll
-    for (int j = 0; j < 32; ++j) {
-      const int col = n0 + cbase + j;
-      if (row_ok && col < n) crow[(long)col * ldc] = cv[j] - __uint_as_float(acc[j]) * unscale;
+          for (int j = 0; j < 32; ++j) {
+            const int col = n0 + (cc + 1) * 32 + j;
+            nx[j] = (row_ok && col < n) ? crow[(long)col * ldc] : 0.f;
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const int col = n0 + cc * 32 + j;
+          if (row_ok && col < n) crow[(long)col * ldc] = cv[j] - __uint_as_float(acc[j]) * unscale;
+        }
+        if (cc + 1 < kBN / 32) {
+#pragma unroll
+          for (int j = 0; j < 32; ++j) cv[j] = nx[j];
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&tempty[b]);
+    }
+  }
+  __syncthreads();
+  if (s_abort) {
+    // a wait gave up: let this CTA's own asynchronous work land (bounded)
+    // before its shared memory and TMEM go away
+    if (warp == 0 && lane == 0) {
+      const uint32_t first = it_issued > (uint32_t)kS ? it_issued - kS : 0;
+      for (uint32_t i = first; i < it_issued; ++i)
+        mbar_wait(&full_bar[i % kS], (i / kS) & 1, st, 24);
+    } else if (warp == 1 && lane == 0) {
+      umma_commit(&drain_bar);
+      mbar_wait(&drain_bar, 0, st, 25);
     }
   }
   tc_fence_before();
   __syncthreads();
   if (warp == 1) {
     tc_fence_after();
-    tmem_dealloc(tmem, kTmemCols);
+    tmem_dealloc(tmem, kPTmemCols);
   }
 }
 
@@ -315,10 +393,54 @@ size_t tc_gemm_workspace_bytes(int kind, int m, int n, int K) {
   return copies * (rup1k((size_t)m * Kp * esz) + rup1k((size_t)n * Kp * esz)) + 1024;
 }
 
+// SMs of the current device (cached per device).
+static int num_sms() {
+  static int cache[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return 148;
+  if (!cache[dev]) {
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    cache[dev] = v > 0 ? v : 148;
+  }
+  return cache[dev];
+}
+
+// How many 16-CTA clusters of the persistent kernel fit the device at once
+// (one per GPC that has 16 free SMs); 0 if clusters of 16 are unavailable.
+template <typename K>
+static int clusters16(K kern, size_t smem) {
+  static int cache[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 0 && dev < 64 && cache[dev]) return cache[dev] > 0 ? cache[dev] : 0;
+  int r = -1;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+      cudaSuccess) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(16);
+    cfg.blockDim = dim3(kPThreads);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 16;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int nc = 0;
+    if (cudaOccupancyMaxActiveClusters(&nc, (void*)kern, &cfg) == cudaSuccess && nc > 0) r = nc;
+  }
+  cudaGetLastError();
+  if (dev >= 0 && dev < 64) cache[dev] = r;
+  return r > 0 ? r : 0;
+}
+
 cudaError_t launch_tc_gemm_sub(int kind, int m, int n, int K, const float* A, long lda,
                                const float* B, long ldb, float* C, long ldc, void* ws,
                                DevStatus* st, cudaStream_t stream, int* nlaunch,
-                               cudaEvent_t ev0, cudaEvent_t ev1) {
+                               cudaEvent_t ev0, cudaEvent_t ev1, int grid_mode) {
   if (nlaunch) *nlaunch = 0;
   if (m <= 0 || n <= 0 || K <= 0) return cudaSuccess;
   const bool split = kind == kTcTF32x3;
@@ -367,18 +489,44 @@ cudaError_t launch_tc_gemm_sub(int kind, int m, int n, int K, const float* A, lo
     tmAlo = tmA;
     tmBlo = tmB;
   }
-  const size_t smem = kStages * (kStageA + kStageB) + 1024;
-  dim3 grid((m + kBM - 1) / kBM, (n + kBN - 1) / kBN);
   const int num_kb = Kp / kbe;
-  const int passes = split ? 3 : 1;
-  if (ev0) cudaEventRecord(ev0, stream);
-  auto kern = kind == kTcBF16  ? tc_gemm_sub_kernel<kTcBF16>
-              : kind == kTcFP8 ? tc_gemm_sub_kernel<kTcFP8>
-                               : tc_gemm_sub_kernel<kTcTF32>;
+  const int tiles = ((m + kBM - 1) / kBM) * ((n + kBN - 1) / kBN);
+  const int sms = num_sms();
+  auto kern = kind == kTcBF16  ? tc_gemm_persistent_kernel<kTcBF16, false>
+              : kind == kTcFP8 ? tc_gemm_persistent_kernel<kTcFP8, false>
+              : split          ? tc_gemm_persistent_kernel<kTcTF32, true>
+                               : tc_gemm_persistent_kernel<kTcTF32, false>;
+  const size_t smem = kPRing + 1024;
   e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  kern<<<grid, kGemmThreads, smem, stream>>>(tmA, tmB, tmAlo, tmBlo, C, ldc, m, n, num_kb,
-                                             passes, amax, st);
+  cudaLaunchConfig_t cfg = {};
+  cfg.blockDim = dim3(kPThreads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  int grid = std::min(tiles, sms);
+  if (grid_mode == kGridSmall) grid = std::min(tiles, kSmallGrid);
+  if (grid_mode == kGridSpareGpc) {
+    // 16-CTA clusters (one per GPC: a GPC has fewer than 32 SMs) on all GPCs
+    // but one, which stays free for the kernels of the other stream
+    const int gpcs = clusters16(kern, smem);
+    if (gpcs >= 2) {
+      grid = std::min(16 * (gpcs - 1), (tiles + 15) / 16 * 16);
+      attr[0].id = cudaLaunchAttributeClusterDimension;
+      attr[0].val.clusterDim.x = 16;
+      attr[0].val.clusterDim.y = 1;
+      attr[0].val.clusterDim.z = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+    } else {
+      grid = std::min(tiles, std::max(1, sms - 2 * kSmallGrid));
+    }
+  }
+  cfg.gridDim = dim3(grid);
+  if (ev0) cudaEventRecord(ev0, stream);
+  e = cudaLaunchKernelEx(&cfg, kern, tmA, tmB, tmAlo, tmBlo, C, ldc, m, n, num_kb,
+                         (const float*)amax, st);
+  if (e != cudaSuccess) return e;
   if (ev1) cudaEventRecord(ev1, stream);
   if (nlaunch) *nlaunch = nl + 1;
   return cudaGetLastError();

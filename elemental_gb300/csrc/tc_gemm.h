@@ -26,9 +26,19 @@ size_t tc_gemm_workspace_bytes(int kind, int m, int n, int K);
 // tcgen05 kernel.  *nlaunch receives the number of kernels enqueued.
 // If ev0/ev1 are given they are recorded immediately before and after the
 // tensor-core kernel itself (not the packing), for live per-kernel timing.
+// grid_mode: how many SMs the persistent kernel may hold (one CTA per SM).
+enum TcGridMode : int {
+  kGridFull = 0,      // every SM (up to one CTA per tile)
+  kGridSpareGpc = 1,  // all GPCs but one (16-CTA clusters), for an update that
+                      // runs beside the look-ahead panel stream
+  kGridSmall = 2,     // at most kSmallGrid CTAs, for the look-ahead stream's own
+                      // small updates while the trailing update holds the rest
+};
+constexpr int kSmallGrid = 16;
 cudaError_t launch_tc_gemm_sub(int kind, int m, int n, int K, const float* A, long lda,
                                const float* B, long ldb, float* C, long ldc, void* ws,
                                DevStatus* st, cudaStream_t stream, int* nlaunch,
-                               cudaEvent_t ev0 = nullptr, cudaEvent_t ev1 = nullptr);
+                               cudaEvent_t ev0 = nullptr, cudaEvent_t ev1 = nullptr,
+                               int grid_mode = kGridFull);
 
 }  // namespace elgb
