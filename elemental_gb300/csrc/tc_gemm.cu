@@ -247,6 +247,7 @@ tc_gemm_persistent_kernel(const __grid_constant__ CUtensorMap tmA,
       if (lane == 0) mbar_arrive(&tempty[b]);
     }
   }
+  __syncwarp();  // lanes 1..31 of the producer and MMA warps wait for lane 0
   __syncthreads();
   if (s_abort) {
     // a wait gave up: let this CTA's own asynchronous work land (bounded)
@@ -259,6 +260,7 @@ tc_gemm_persistent_kernel(const __grid_constant__ CUtensorMap tmA,
       umma_commit(&drain_bar);
       mbar_wait(&drain_bar, 0, st, 25);
     }
+    __syncwarp();
   }
   tc_fence_before();
   __syncthreads();
@@ -407,14 +409,17 @@ static int num_sms() {
   return cache[dev];
 }
 
-// How many 16-CTA clusters of the persistent kernel fit the device at once
-// (one per GPC that has 16 free SMs); 0 if clusters of 16 are unavailable.
+// How many 16-CTA clusters of the persistent kernel `kern` fit the device at
+// once (one per GPC with 16 SMs to spare); 0 if clusters of 16 are
+// unavailable.  Cached per device and kernel variant (0..3); the non-portable
+// cluster size is allowed on the kernel at the first query.
 template <typename K>
-static int clusters16(K kern, size_t smem) {
-  static int cache[64] = {0};
+static int clusters16(K kern, int variant, size_t smem) {
+  static int cache[64][4] = {};
   int dev = 0;
   cudaGetDevice(&dev);
-  if (dev >= 0 && dev < 64 && cache[dev]) return cache[dev] > 0 ? cache[dev] : 0;
+  const bool cached = dev >= 0 && dev < 64 && variant >= 0 && variant < 4;
+  if (cached && cache[dev][variant]) return cache[dev][variant] > 0 ? cache[dev][variant] : 0;
   int r = -1;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
       cudaSuccess) {
@@ -433,7 +438,7 @@ static int clusters16(K kern, size_t smem) {
     if (cudaOccupancyMaxActiveClusters(&nc, (void*)kern, &cfg) == cudaSuccess && nc > 0) r = nc;
   }
   cudaGetLastError();
-  if (dev >= 0 && dev < 64) cache[dev] = r;
+  if (cached) cache[dev][variant] = r;
   return r > 0 ? r : 0;
 }
 
@@ -496,6 +501,7 @@ cudaError_t launch_tc_gemm_sub(int kind, int m, int n, int K, const float* A, lo
               : kind == kTcFP8 ? tc_gemm_persistent_kernel<kTcFP8, false>
               : split          ? tc_gemm_persistent_kernel<kTcTF32, true>
                                : tc_gemm_persistent_kernel<kTcTF32, false>;
+  const int variant = kind == kTcBF16 ? 0 : kind == kTcFP8 ? 1 : split ? 2 : 3;
   const size_t smem = kPRing + 1024;
   e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
@@ -509,7 +515,7 @@ cudaError_t launch_tc_gemm_sub(int kind, int m, int n, int K, const float* A, lo
   if (grid_mode == kGridSpareGpc) {
     // 16-CTA clusters (one per GPC: a GPC has fewer than 32 SMs) on all GPCs
     // but one, which stays free for the kernels of the other stream
-    const int gpcs = clusters16(kern, smem);
+    const int gpcs = clusters16(kern, variant, smem);
     if (gpcs >= 2) {
       grid = std::min(16 * (gpcs - 1), (tiles + 15) / 16 * 16);
       attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -519,7 +525,7 @@ cudaError_t launch_tc_gemm_sub(int kind, int m, int n, int K, const float* A, lo
       cfg.attrs = attr;
       cfg.numAttrs = 1;
     } else {
-      grid = std::min(tiles, std::max(1, sms - 2 * kSmallGrid));
+      grid = std::min(tiles, std::max(1, sms - kSmallGrid - 8));
     }
   }
   cfg.gridDim = dim3(grid);

@@ -34,7 +34,7 @@ enum TcGridMode : int {
   kGridSmall = 2,     // at most kSmallGrid CTAs, for the look-ahead stream's own
                       // small updates while the trailing update holds the rest
 };
-constexpr int kSmallGrid = 16;
+constexpr int kSmallGrid = 32;
 cudaError_t launch_tc_gemm_sub(int kind, int m, int n, int K, const float* A, long lda,
                                const float* B, long ldb, float* C, long ldc, void* ws,
                                DevStatus* st, cudaStream_t stream, int* nlaunch,
