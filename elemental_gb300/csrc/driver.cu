@@ -231,6 +231,7 @@ struct LuState {
   bool tournament;     // FP32 leaf panels by tournament pivoting
   unsigned long long* trace;  // leaf-panel timestamps (4 per column), or null
   int trace_cols;
+  int trail_grid;      // TcGridMode of the trailing update beside the look-ahead panel
 };
 
 // Blocked TRSM, left / lower / unit: B := L11^{-1} B with L11 nb x nb (any
@@ -406,8 +407,8 @@ static cudaError_t getrf_run(LuState<T>& s, int nb) {
       e = apply_swaps(s, s.main, k, jb, kn + jb2, s.n, 0, 0, true);
       if (e != cudaSuccess) return e;
     }
-    // beside the look-ahead panel the trailing update keeps off one GPC
-    if (split) s.main.grid_mode = kGridSpareGpc;
+    // beside the look-ahead panel the trailing update leaves SMs to it
+    if (split) s.main.grid_mode = s.trail_grid;
     e = update_cols(s, s.main, k, jb, kn + jb2, s.n);
     if (e == cudaSuccess) e = update_companion(s, s.main, k, jb);
     s.main.grid_mode = kGridFull;
@@ -496,9 +497,15 @@ cudaError_t getrf(Context* ctx, int m, int n, T* A, long lda, int* ipiv, int nb,
     s.main.gemm.ws = cv.take<char>(tcb);
     if (!s.main.gemm.ws) return cudaErrorMemoryAllocation;
   }
+  // ELGB_OPT_TRAIL_GRID: 0 every SM (persistent), 1 all GPCs but one
+  // (default), 2 the same with the look-ahead stream's updates also one CTA
+  // per tile, 3 one CTA per tile for both streams
+  s.trail_grid = ctx->opt_trail_grid == 0   ? kGridFull
+                 : ctx->opt_trail_grid == 3 ? kGridTiles
+                                            : kGridSpareGpc;
   if (la) {
     s.side.st = ctx->side_stream;
-    s.side.grid_mode = kGridSmall;
+    s.side.grid_mode = ctx->opt_trail_grid >= 2 ? kGridTiles : kGridSmall;
     s.side.gemm.tc_kind = tc ? inner_kind : -1;
     if (tc) {
       s.side.gemm.ws = cv.take<char>(tcs);
@@ -1237,6 +1244,10 @@ int ElGBSetOption(ElGBContext ctx, int option, int value) {
       return 0;
     case ELGB_OPT_RESIDUAL_DF:
       ctx->opt_residual_df = value ? 1 : 0;
+      return 0;
+    case ELGB_OPT_TRAIL_GRID:
+      if (value < 0 || value > 3) return elgb::kElArgError;
+      ctx->opt_trail_grid = value;
       return 0;
     case ELGB_OPT_PANEL_TRACE: {
       if (value < 0) return elgb::kElArgError;

@@ -512,6 +512,7 @@ cudaError_t launch_tc_gemm_sub(int kind, int m, int n, int K, const float* A, lo
   cudaLaunchAttribute attr[1];
   int grid = std::min(tiles, sms);
   if (grid_mode == kGridSmall) grid = std::min(tiles, kSmallGrid);
+  if (grid_mode == kGridTiles) grid = tiles;
   if (grid_mode == kGridSpareGpc) {
     // 16-CTA clusters (one per GPC: a GPC has fewer than 32 SMs) on all GPCs
     // but one, which stays free for the kernels of the other stream

@@ -33,6 +33,7 @@ enum TcGridMode : int {
                       // runs beside the look-ahead panel stream
   kGridSmall = 2,     // at most kSmallGrid CTAs, for the look-ahead stream's own
                       // small updates while the trailing update holds the rest
+  kGridTiles = 3,     // one CTA per tile: SMs are released tile by tile
 };
 constexpr int kSmallGrid = 32;
 cudaError_t launch_tc_gemm_sub(int kind, int m, int n, int K, const float* A, long lda,

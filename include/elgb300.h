@@ -74,7 +74,14 @@ int ElGBSetBlocksize(int nb);
  *                       deferred rank-1 update, once the pivot exchange is
  *                       complete, after the step's multipliers, next column
  *                       and argmax.  Read with ElGBPanelTrace.  0 (default):
- *                       off. */
+ *                       off.
+ *   ELGB_OPT_TRAIL_GRID how the FP32 LU's tensor-core updates share the SMs
+ *                       while the look-ahead panel runs: 1 (default) the
+ *                       trailing update holds all GPCs but one (16-CTA
+ *                       clusters, persistent) and the panel's own updates
+ *                       at most 32 CTAs; 0 the trailing update holds every
+ *                       SM; 2 as 1 with the panel's updates one CTA per
+ *                       tile; 3 one CTA per tile for both. */
 enum {
   ELGB_OPT_LOOKAHEAD = 1,
   ELGB_OPT_PANEL_CTAS = 2,
@@ -82,7 +89,8 @@ enum {
   ELGB_OPT_PANEL_CLUSTER = 4,
   ELGB_OPT_PANEL_REGS = 5,
   ELGB_OPT_RESIDUAL_DF = 6,
-  ELGB_OPT_PANEL_TRACE = 7
+  ELGB_OPT_PANEL_TRACE = 7,
+  ELGB_OPT_TRAIL_GRID = 8
 };
 int ElGBSetOption(ElGBContext ctx, int option, int value);
 
