@@ -472,6 +472,19 @@ def gpu_arm(args, rank, world, local_rank):
         "achieved_gbs": prof["bytes"] / (prof["ms"] * 1e-3) / 1e9 if prof["ms"] > 0 else None,
         "share_of_step_time": prof["ms"] * 1e-3 / tmax if tmax > 0 else None,
     }
+    # the trailing update alone (the launches on the main stream), which
+    # holds all GPCs but one while the look-ahead panel runs beside it
+    side = prof.get("by_kernel_lookahead_stream", {}).get("tc_gemm")
+    tc_all = prof["by_kernel"].get("tc_gemm")
+    if side and tc_all and tc_all["ms"] > side["ms"]:
+        roofline["trailing_update_only"] = {
+            "launches": tc_all["launches"] - side["launches"],
+            "achieved": (prof["flops"] - prof.get("flops_lookahead_tc", 0.0))
+            / ((tc_all["ms"] - side["ms"]) * 1e-3) / 1e12
+            if prof.get("flops_lookahead_tc") is not None else None,
+            "note": "beside the look-ahead panel the update holds all GPCs but one "
+                    "(16-CTA clusters, ELGB_OPT_TRAIL_GRID); the look-ahead stream's own "
+                    "small updates are the rest of the launches"}
     # the operand kind's own ceiling on the same tensor pipe: TF32 issues at
     # half the bf16 rate, TF32x3 issues three TF32 products per update, E4M3
     # at twice the bf16 rate

@@ -497,9 +497,10 @@ cudaError_t getrf(Context* ctx, int m, int n, T* A, long lda, int* ipiv, int nb,
     s.main.gemm.ws = cv.take<char>(tcb);
     if (!s.main.gemm.ws) return cudaErrorMemoryAllocation;
   }
-  // ELGB_OPT_TRAIL_GRID: 0 every SM (persistent), 1 all GPCs but one
-  // (default), 2 the same with the look-ahead stream's updates also one CTA
-  // per tile, 3 one CTA per tile for both streams
+  // ELGB_OPT_TRAIL_GRID: 0 every SM (persistent), 1 all GPCs but one, 2
+  // (default) the same with the look-ahead stream's updates one CTA per tile,
+  // 3 one CTA per tile for both streams.  Measured at n = 32768 (LU ms):
+  // 379, 329, 325, 361.
   s.trail_grid = ctx->opt_trail_grid == 0   ? kGridFull
                  : ctx->opt_trail_grid == 3 ? kGridTiles
                                             : kGridSpareGpc;

@@ -150,6 +150,8 @@ class Context:
                                              ctypes.byref(fl), ctypes.byref(by)), "ProfileTag")
             if n.value:
                 side[name] = dict(launches=n.value, ms=ms.value)
+                if name == "tc_gemm":
+                    out["flops_lookahead_tc"] = fl.value
         out["by_kernel_lookahead_stream"] = side
         return out
 

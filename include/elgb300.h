@@ -76,12 +76,13 @@ int ElGBSetBlocksize(int nb);
  *                       and argmax.  Read with ElGBPanelTrace.  0 (default):
  *                       off.
  *   ELGB_OPT_TRAIL_GRID how the FP32 LU's tensor-core updates share the SMs
- *                       while the look-ahead panel runs: 1 (default) the
+ *                       while the look-ahead panel runs: 2 (default) the
  *                       trailing update holds all GPCs but one (16-CTA
  *                       clusters, persistent) and the panel's own updates
- *                       at most 32 CTAs; 0 the trailing update holds every
- *                       SM; 2 as 1 with the panel's updates one CTA per
- *                       tile; 3 one CTA per tile for both. */
+ *                       run one CTA per tile; 1 as 2 with the panel's
+ *                       updates on at most 32 persistent CTAs; 0 the
+ *                       trailing update holds every SM; 3 one CTA per tile
+ *                       for both. */
 enum {
   ELGB_OPT_LOOKAHEAD = 1,
   ELGB_OPT_PANEL_CTAS = 2,

@@ -175,7 +175,7 @@ def case_lu_breakdown(ctx, a):
     ms = _timed(lambda: ctx.lu_mixed(A, gemm_kind=a.kind, nb=a.nb))
     prof = ctx.profile_stop()
     ctx.set_option("lookahead", 1)
-    ctx.set_option("trail_grid", 1)
+    ctx.set_option("trail_grid", 2)
     return dict(case="lu_breakdown", n=a.n, kind=KIND_NAMES[a.kind], lookahead=a.lookahead,
                 trail_grid=a.trail_grid, ms=ms,
                 tflops=2.0 / 3.0 * a.n ** 3 / (ms * 1e-3) / 1e12,
@@ -249,7 +249,7 @@ def main(argv=None):
     p.add_argument("--precision", default="fp32", choices=["fp64", "fp32", "bf16"])
     p.add_argument("--seed", type=int, default=20261204)
     p.add_argument("--lookahead", type=int, default=1, help="lu_breakdown: 0 = one stream")
-    p.add_argument("--trail-grid", type=int, default=1, help="lu_breakdown: ELGB_OPT_TRAIL_GRID")
+    p.add_argument("--trail-grid", type=int, default=2, help="lu_breakdown: ELGB_OPT_TRAIL_GRID")
     a = p.parse_args(argv)
     ctx = D.context(0)
     out = CASES[a.case](ctx, a)
