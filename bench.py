@@ -240,6 +240,20 @@ def haar_conditioned(n, kappa, g, device="cuda"):
     return U @ V.t()
 
 
+def host_tensor(shape):
+    """FP64 host buffer for the end-to-end arms: the library's host memory
+    (ElGBHostAlloc: anonymous pages registered with the CUDA driver), viewed
+    as a torch tensor.  Host -> device copies from it kept ~200 GB/s after
+    GPU compute on GB300, where cudaHostAlloc memory (torch's pin_memory)
+    fell to 40-100 GB/s."""
+    import numpy as np
+    import torch
+
+    import elemental_gb300 as El
+
+    return torch.from_numpy(El.host_empty(shape, np.float64, order="C"))
+
+
 def host_backward_error(AT, X, B, block=1024):
     """Normwise backward error max_j ||b_j - A x_j||_2 / (||A||_F ||x_j||_2 +
     ||b_j||_2) recomputed on the host in FP64 (numpy over OpenBLAS), from
@@ -291,15 +305,14 @@ def gpu_arm(args, rank, world, local_rank):
     B.copy_(torch.randn(q, n, generator=g, device="cuda", dtype=torch.float64).t())
     X = D.colmajor(n, q)
     # the host copies of the system for the end-to-end arm, made first, as a
-    # caller's data exists before any solve (pinned buffers allocated after
-    # the device arm's solves measured up to 8x slower host -> device
-    # copies on these boxes)
+    # caller's data exists before any solve; in the library's host memory
+    # (host_tensor)
     if args.e2e == "on":
-        Ah = torch.empty((n, n), dtype=torch.float64, pin_memory=True)
+        Ah = host_tensor((n, n))
         Ah.copy_(A.t())  # row-major (n, n) of A^T = column-major A
-        B0 = torch.empty((q, n), dtype=torch.float64, pin_memory=True)
+        B0 = host_tensor((q, n))
         B0.copy_(B.t())
-        Bh = torch.empty((q, n), dtype=torch.float64, pin_memory=True)
+        Bh = host_tensor((q, n))
     torch.cuda.synchronize()
 
     def solve(tol=args.tol):
@@ -339,10 +352,8 @@ def gpu_arm(args, rank, world, local_rank):
     berr = max(i["backward_error"] for i in infos)
     iters = max(i["iterations"] for i in infos)
 
-    # end to end through the Elemental-style C ABI on pinned host buffers,
-    # right after the device arm (after the ~20 s FP64 comparison, during
-    # which the host thread only waits, the first host-staged calls measured
-    # up to 1.8x slower while the host side ramps back up)
+    # end to end through the Elemental-style C ABI on registered host
+    # buffers, right after the device arm (before the ~20 s FP64 comparison)
     e2e = None
     if args.e2e == "on":
         Am = El.Matrix(Ah.numpy().T)
@@ -390,7 +401,7 @@ def gpu_arm(args, rank, world, local_rank):
         th = time.perf_counter() - th
         e2e = {"value": args.steps * world / te, "unit": "solves/s",
                "h2d_bytes_per_step": 8 * n * n + 8 * n * q, "d2h_bytes_per_step": 8 * n * q,
-               "api": "ElLinearSolveMixed_d (El::Matrix handles on pinned host memory)",
+               "api": "ElLinearSolveMixed_d (El::Matrix handles on ElGBHostAlloc host memory, pinned by registration)",
                "max_abs_diff_vs_device_run": err,
                "iterations": einfo["iterations"] if einfo else None,
                "backward_error": einfo["backward_error"] if einfo else None,
@@ -448,23 +459,24 @@ def gpu_arm(args, rank, world, local_rank):
     peak = peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops"))
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "tc_gemm_traffic.json")
-    if os.path.exists(tpath) and prof["launches"]:
+    if os.path.exists(tpath) and prof["launches"] and args.precision == "fp32":
         with open(tpath) as f:
             tj = json.load(f)
-        # DRAM bytes per GEMM flop from one ncu capture of the same LU at a
-        # smaller n (all tc_gemm launches of one step), applied to the
-        # average launch of this run
-        traffic = tj["dram_bytes_per_flop"] * prof["flops"] / prof["launches"]
+        # DRAM bytes over algorithmic bytes from one ncu capture of the
+        # largest trailing update of the n = 32768 factorization, applied to
+        # the average launch of this run
+        traffic = tj["dram_over_algorithmic"] * prof["bytes"] / prof["launches"]
     roofline = {
-        "kernel": "tc_gemm_sub_kernel (tcgen05 trailing update, "
+        "kernel": "tc_gemm_persistent_kernel (tcgen05 trailing update, "
                   f"{ {'fp32': 'TF32x3', 'tf32': 'TF32', 'bf16': 'BF16', 'fp8': 'E4M3', 'fp64': 'n/a'}[args.precision] } operands)",
         "bound": "tensor", "achieved": tf_achieved, "peak": peak, "unit": "TFLOP/s",
         "frac": (tf_achieved / peak) if tf_achieved else None,
         "peak_source": f"{peak_kind} bf16 dense (sustained): the kernel is timed inside a long step",
         "traffic": traffic,
-        "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum over every "
-                           "tc_gemm_sub_kernel launch of an n=8192 step, per GEMM flop, scaled "
-                           "to this run's average launch (profiles/tc_gemm_traffic.json)")
+        "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
+                           "tc_gemm_persistent_kernel launch (32768 x 32256 x 512, TF32x3) "
+                           "over its algorithmic bytes, times this run's average algorithmic "
+                           "bytes per launch (profiles/tc_gemm_traffic.json)")
         if traffic is not None else None,
         "launches": prof["launches"], "kernel_ms_total": prof["ms"],
         "algorithmic_flops_per_launch": prof["flops"] / max(prof["launches"], 1),
@@ -654,9 +666,9 @@ def batched_arm(args, rank, world, local_rank):
     berr = max(r["backward_error"] for r in res)
     ok = all(r["converged"] for r in res)
     # e2e: host (pinned) packed inputs -> device, one replay, solutions -> host
-    Ah = torch.empty(A.numel(), dtype=torch.float64, pin_memory=True)
-    Bh = torch.empty(B.numel(), dtype=torch.float64, pin_memory=True)
-    Xh = torch.empty(B.numel(), dtype=torch.float64, pin_memory=True)
+    Ah = host_tensor((A.numel(),))
+    Bh = host_tensor((B.numel(),))
+    Xh = host_tensor((B.numel(),))
     Ah.copy_(A)
     Bh.copy_(B)
     barrier()
@@ -903,8 +915,8 @@ def inverse_arm(args, rank, world, local_rank):
     # end to end through Elemental's C ABI on pinned host memory
     e2e = None
     if args.e2e == "on":
-        Hp = torch.empty((n, n), dtype=torch.float64, pin_memory=True)
-        H0 = torch.empty((n, n), dtype=torch.float64, pin_memory=True)
+        Hp = host_tensor((n, n))
+        H0 = host_tensor((n, n))
         H0.copy_(A0.t())
         Hp.copy_(H0)
         M = El.Matrix(Hp.numpy().T)
@@ -917,7 +929,7 @@ def inverse_arm(args, rank, world, local_rank):
             te += time.perf_counter() - t0
         e2e = {"value": args.steps * world / tmax_of(te), "unit": "inverses/s",
                "h2d_bytes_per_step": 8 * n * n, "d2h_bytes_per_step": 8 * n * n,
-               "api": "ElInverse_d (El::Matrix handle on pinned host memory)",
+               "api": "ElInverse_d (El::Matrix handle on ElGBHostAlloc host memory, pinned by registration)",
                "max_abs_diff_vs_device_run": float(np.abs(M.array - X).max())}
         del M, Hp, H0
     if rank != 0:
@@ -1091,11 +1103,11 @@ def cholesky_arm(args, rank, world, local_rank):
     # end to end through Elemental's C ABI on pinned host memory
     e2e = None
     if args.e2e == "on":
-        Ah = torch.empty((n, n), dtype=torch.float64, pin_memory=True)
+        Ah = host_tensor((n, n))
         Ah.copy_(A0.t())
-        Bh0 = torch.empty((q, n), dtype=torch.float64, pin_memory=True)
+        Bh0 = host_tensor((q, n))
         Bh0.copy_(B0.t())
-        Bh = torch.empty((q, n), dtype=torch.float64, pin_memory=True)
+        Bh = host_tensor((q, n))
         Am = El.Matrix(Ah.numpy().T)
         Bh.copy_(Bh0)
         Bm = El.Matrix(Bh.numpy().T)
@@ -1109,7 +1121,7 @@ def cholesky_arm(args, rank, world, local_rank):
         Xd = X.cpu().numpy()
         e2e = {"value": args.steps * world / tmax_of(te), "unit": "solves/s",
                "h2d_bytes_per_step": 8 * n * n + 8 * n * q, "d2h_bytes_per_step": 8 * n * q,
-               "api": "ElHPDSolve_d (El::Matrix handles on pinned host memory)",
+               "api": "ElHPDSolve_d (El::Matrix handles on ElGBHostAlloc host memory, pinned by registration)",
                "max_abs_diff_vs_device_run": float(np.abs(Bm.array - Xd).max())}
         del Am, Bm, Ah, Bh, Bh0
     if rank != 0:

@@ -358,6 +358,38 @@ def LinearSolveMixed(A: Matrix, B: Matrix, precision="fp32", method="lu-ir", tol
                 backward_error=inf.backward_error)
 
 
+class _HostBlock:
+    """Owner of one ElGBHostAlloc block; frees it when the last array using
+    it goes away."""
+
+    def __init__(self, nbytes):
+        lib = _lib.load()
+        p = ctypes.c_void_p()
+        _check(lib.ElGBHostAlloc(nbytes, ctypes.byref(p)), "HostAlloc")
+        self.ptr = p.value
+        self.nbytes = nbytes
+
+    def __del__(self):
+        if getattr(self, "ptr", None):
+            _lib.load().ElGBHostFree(self.ptr)
+            self.ptr = None
+
+
+def host_empty(shape, dtype=np.float64, order="F"):
+    """numpy array in ElGBHostAlloc memory (registered with the CUDA driver),
+    for matrices that move to and from the GPU: attach El.Matrix to it (order
+    "F", the column-major layout of El::Matrix)."""
+    shape = tuple(int(d) for d in np.atleast_1d(shape))
+    dt = np.dtype(dtype)
+    nbytes = int(np.prod(shape)) * dt.itemsize
+    if nbytes == 0:
+        return np.empty(shape, dtype=dt, order=order)
+    blk = _HostBlock(nbytes)
+    buf = (ctypes.c_char * nbytes).from_address(blk.ptr)
+    buf._owner = blk  # the block lives as long as a view of the buffer
+    return np.ndarray(shape, dtype=dt, buffer=buf, order=order)
+
+
 def LastHostCallTimes():
     """Host-side phases of the last completed host-matrix call (ms): upload,
     device work (with its synchronisation), download."""

@@ -185,6 +185,8 @@ def load():
     _sig(lib, "ElLinearSolveMixed_d", c_int, vp, vp, P(RefineCtrl), P(RefineInfo))
     _sig(lib, "ElGBLastHostCallTimes", c_int, P(ctypes.c_double), P(ctypes.c_double),
          P(ctypes.c_double))
+    _sig(lib, "ElGBHostAlloc", c_int, ctypes.c_size_t, P(vp))
+    _sig(lib, "ElGBHostFree", c_int, vp)
     _lib = lib
     return lib
 

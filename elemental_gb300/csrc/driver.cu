@@ -1250,6 +1250,10 @@ int ElGBSetOption(ElGBContext ctx, int option, int value) {
       if (value < 0 || value > 3) return elgb::kElArgError;
       ctx->opt_trail_grid = value;
       return 0;
+    case ELGB_OPT_PANEL_ROWS:
+      if (value < 64 || value > 1536) return elgb::kElArgError;
+      elgb::g_panel_rows = value;
+      return 0;
     case ELGB_OPT_PANEL_TRACE: {
       if (value < 0) return elgb::kElArgError;
       cudaSetDevice(ctx->device);

@@ -5,6 +5,7 @@
 // exceptions to ElError exactly as the reference's EL_TRY does
 // (include/El/core/CReflect.hpp:12-26).
 #include <cuda_runtime.h>
+#include <sys/mman.h>
 
 #include <algorithm>
 #include <chrono>
@@ -13,6 +14,7 @@
 #include <new>
 #include <stdexcept>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/El_gb300.h"
@@ -1208,6 +1210,53 @@ ElError ElLinearSolveMixed_d(ElConstMatrix_d A, ElMatrix_d B, const ElGBRefineCt
                              ElGBRefineInfo* info) {
   EL_GB_TRY(El::LinearSolveMixed(*CM<double>(A), *M<double>(B), ctrl, info))
 }
+// Host buffers: anonymous mappings registered with the driver, by length.
+static std::mutex g_host_mu;
+static std::unordered_map<void*, size_t>& HostMaps() {
+  static std::unordered_map<void*, size_t> m;
+  return m;
+}
+
+ElError ElGBHostAlloc(size_t bytes, void** ptr) {
+  if (!ptr) return EL_ARG_ERROR;
+  *ptr = nullptr;
+  if (bytes == 0) return EL_SUCCESS;
+  const size_t align = size_t(2) << 20;
+  const size_t len = (bytes + align - 1) / align * align;
+  void* p = mmap(nullptr, len, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS, -1, 0);
+  if (p == MAP_FAILED) return EL_ALLOC_ERROR;
+#ifdef MADV_HUGEPAGE
+  madvise(p, len, MADV_HUGEPAGE);  // advice only: without it the pages stay small
+#endif
+  if (cudaHostRegister(p, len, cudaHostRegisterDefault) != cudaSuccess) {
+    cudaGetLastError();
+    munmap(p, len);
+    return EL_RUNTIME_ERROR;
+  }
+  {
+    std::lock_guard<std::mutex> lk(g_host_mu);
+    HostMaps()[p] = len;
+  }
+  *ptr = p;
+  return EL_SUCCESS;
+}
+
+ElError ElGBHostFree(void* ptr) {
+  if (!ptr) return EL_SUCCESS;
+  size_t len = 0;
+  {
+    std::lock_guard<std::mutex> lk(g_host_mu);
+    auto it = HostMaps().find(ptr);
+    if (it == HostMaps().end()) return EL_LOGIC_ERROR;
+    len = it->second;
+    HostMaps().erase(it);
+  }
+  cudaHostUnregister(ptr);
+  cudaGetLastError();
+  munmap(ptr, len);
+  return EL_SUCCESS;
+}
+
 ElError ElGBLastHostCallTimes(double* upload_ms, double* compute_ms, double* download_ms) {
   double t[3];
   El::LastHostCallTimes(t);

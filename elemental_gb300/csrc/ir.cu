@@ -193,9 +193,9 @@ struct Ws {
   double* dpart;
   float* Dl;         // inverted 64 x 64 diagonal blocks of L (unit lower)
   float* Du;         // ... and of U
-  int* flags;        // block-row done flags of the one-launch triangular solves
+  unsigned long long* tags;  // words the one-launch triangular solves publish
   unsigned* ticket;
-  int epoch;
+  unsigned epoch;
   // double-float residual (residual_df.cu): FP32 words of A, the scaled
   // split X, per-column unscaling, partial sums, ||A||_F^2 and max |a|
   float* Ahi;
@@ -251,10 +251,10 @@ static cudaError_t lowprec_solve(Context* ctx, int n, int q, Ws& w, const double
   IR_CHECK(cudaGetLastError());
   // (P^T L U)^{-1}: L then U, each one launch
   const int pi = ctx->prof_begin(ctx->stream);
-  IR_CHECK(launch_trsv_persistent<float>(w.Af, n, w.Dl, w.Rf, n, n, q, true, w.ticket, w.flags,
+  IR_CHECK(launch_trsv_persistent<float>(w.Af, n, w.Dl, w.Rf, n, n, q, true, w.ticket, w.tags,
                                          ++w.epoch, ctx->status, ctx->num_sms, ctx->stream));
   IR_CHECK(launch_trsv_persistent<float>(w.Af, n, w.Du, w.Rf, n, n, q, false, w.ticket,
-                                         w.flags, ++w.epoch, ctx->status, ctx->num_sms,
+                                         w.tags, ++w.epoch, ctx->status, ctx->num_sms,
                                          ctx->stream));
   ctx->launches += 2;
   ctx->prof_end(pi, ctx->stream, ELGB_PROF_SOLVE, 2.0 * n * (double)n * q,
@@ -327,8 +327,8 @@ cudaError_t refined_solve(Context* ctx, int n, const double* A, long lda, int nr
                 al((size_t)rch * n * 16 * sizeof(double)) + al(4 * (Q + 1) * sizeof(double)) +
                 al((size_t)(n + 1) * sizeof(double));
   const int nblk = trsv_blocks(n);
-  need += 2 * al((size_t)nblk * 4096 * sizeof(float)) + al((size_t)nblk * sizeof(int)) +
-          al(sizeof(unsigned));
+  need += 2 * al((size_t)nblk * 4096 * sizeof(float)) +
+          al(trsv_tag_words(n) * sizeof(unsigned long long)) + al(sizeof(unsigned));
   // double-float residuals where the FP64 pipe bounds the residual (below
   // n = 2048 it costs little either way)
   const bool df = ctx->opt_residual_df != 0 && n >= 2048;
@@ -365,7 +365,7 @@ cudaError_t refined_solve(Context* ctx, int n, const double* A, long lda, int nr
     w.colout = (double*)take((size_t)(n + 1) * sizeof(double));
     w.Dl = (float*)take((size_t)nblk * 4096 * sizeof(float));
     w.Du = (float*)take((size_t)nblk * 4096 * sizeof(float));
-    w.flags = (int*)take((size_t)nblk * sizeof(int));
+    w.tags = (unsigned long long*)take(trsv_tag_words(n) * sizeof(unsigned long long));
     w.ticket = (unsigned*)take(sizeof(unsigned));
     w.epoch = 0;
     w.spart = (double*)take(2 * df_split_parts(n) * sizeof(double));
@@ -377,7 +377,8 @@ cudaError_t refined_solve(Context* ctx, int n, const double* A, long lda, int nr
       w.xinv = (double*)take(16 * sizeof(double));
       w.dfpart = (double*)take(df_residual_partial_doubles(n) * sizeof(double));
     }
-    IR_CHECK(cudaMemsetAsync(w.flags, 0, (size_t)nblk * sizeof(int), ctx->stream));
+    IR_CHECK(cudaMemsetAsync(w.tags, 0, trsv_tag_words(n) * sizeof(unsigned long long),
+                             ctx->stream));
     if (gm) {
       w.V = (double*)take((size_t)Q * kb * n * sizeof(double));
       w.Z = (double*)take((size_t)Q * c.restart * n * sizeof(double));
@@ -387,6 +388,7 @@ cudaError_t refined_solve(Context* ctx, int n, const double* A, long lda, int nr
     }
     // 1. low-precision factorization of an FP32 copy of A; the same pass over
     // A makes its FP32 words for the double-float residual and its norms
+    const int pc = ctx->prof_begin(ctx->stream);
     if (df) {
       IR_CHECK(launch_split_a(A, lda, n, w.Af, w.Ahi, w.Alo, w.spart, w.astat, ctx->stream));
       ctx->launches += 2;
@@ -396,6 +398,9 @@ cudaError_t refined_solve(Context* ctx, int n, const double* A, long lda, int nr
       ctx->launches += 1;
       IR_CHECK(cudaGetLastError());
     }
+    // bytes: A read, the FP32 copy (and the two words) written
+    ctx->prof_end(pc, ctx->stream, ELGB_PROF_CONVERT, 0.0,
+                  (df ? 20.0 : 12.0) * n * (double)n);
     IR_CHECK(getrf<float>(ctx, n, n, w.Af, n, w.ipiv, c.nb, tc_kind, c.pivoting == 1));
     IR_CHECK(cudaMemcpyAsync(ctx->h_status, ctx->status, sizeof(DevStatus),
                              cudaMemcpyDeviceToHost, ctx->stream));

@@ -49,6 +49,8 @@ cudaError_t launch_calu_panel(float* A, long lda, int mp, int w, int* ipiv, int 
 // Largest thread-block cluster the panel kernel may use (1: the cooperative
 // kernel only); process-wide, ElGBSetOption(ELGB_OPT_PANEL_CLUSTER).
 extern int g_panel_cluster;
+// Rows per CTA the leaf-panel kernels aim for (ElGBSetOption(ELGB_OPT_PANEL_ROWS)).
+extern int g_panel_rows;
 // FP32 panels with the rows in registers (1, default) or in shared memory.
 extern int g_panel_regs;
 

@@ -14,6 +14,7 @@ namespace elgb {
 // Largest thread-block cluster the panel may use (1: the cooperative kernel
 // only); set by ElGBSetOption(ELGB_OPT_PANEL_CLUSTER).
 int g_panel_cluster = 16;
+int g_panel_rows = 1024;
 // FP32 panels with the rows in registers (ElGBSetOption(ELGB_OPT_PANEL_REGS)).
 int g_panel_regs = 0;
 
@@ -714,17 +715,17 @@ getf2_panel_cluster_kernel(PanelParams<T> p) {
   cluster_barrier();  // no CTA leaves while another may still read its slots
 }
 
-// Cluster size for a panel of mp rows: the power of two giving ~1024 rows
-// per CTA (at least 2 CTAs, at most max_cluster), or 0 when one cluster
-// cannot hold the panel in shared memory or the panel is too small for one
-// (the caller then uses the cooperative kernel).
+// Cluster size for a panel of mp rows: the power of two giving about
+// g_panel_rows rows per CTA (at least 2 CTAs, at most max_cluster), or 0
+// when one cluster cannot hold the panel in shared memory or the panel is
+// too small for one (the caller then uses the cooperative kernel).
 template <typename T>
 static int cluster_ctas(int mp, int max_cluster) {
   constexpr int kMaxSmem = 200 * 1024;
   const int rows_cap = (int)(kMaxSmem / (kPanelW * sizeof(T))) - 32;
   if (mp < 128) return 0;
   int C = 2;
-  while (C < max_cluster && (mp + C - 1) / C > 1024) C *= 2;
+  while (C < max_cluster && (mp + C - 1) / C > g_panel_rows) C *= 2;
   if (C > max_cluster || (mp + C - 1) / C > rows_cap) return 0;
   return C;
 }
@@ -799,11 +800,11 @@ cudaError_t launch_getf2_panel(T* A, long lda, int mp, int w, int* ipiv, int row
     }
   }
   constexpr int kMaxSmem = 200 * 1024;
-  // About 1024 rows per CTA: fewer CTAs make the per-column exchange cheap
-  // (every CTA copies every candidate row), more only where shared memory
-  // forces it.
+  // About g_panel_rows rows per CTA: fewer CTAs make the per-column
+  // exchange cheap (every CTA copies every candidate row), more make the
+  // local update short; shared memory sets the fewest.
   const int rows_cap = (int)(kMaxSmem / (kPanelW * sizeof(T))) - 64;
-  int G = std::max(ceil_div(mp, 1024), ceil_div(mp, rows_cap));
+  int G = std::max(ceil_div(mp, g_panel_rows), ceil_div(mp, rows_cap));
   if (G > num_sms) G = num_sms;
   if (G > s.maxG) G = s.maxG;
   if (G > panel_threads<T>()) G = panel_threads<T>();

@@ -15,14 +15,16 @@
 //     the cross terms ah xl + al xh (al xl ~ 2^-48 is dropped);
 //   * the running sum S takes p with TwoSum, whose exact error goes to the
 //     low word L with e and the cross terms; (S, L) is renormalised by
-//     TwoSum every 4 columns and flushed into an FP64 accumulator every 32
-//     columns.  L's own FP32 rounding is the leading error, about
-//     2^-48 sqrt(32 * 4 / n) of sum_j |a_ij x_j| per row.
+//     TwoSum every 4 columns, which leaves |L| <= ulp(S) / 2, and S alone
+//     is flushed into an FP64 accumulator every 32 columns (one conversion
+//     and one FP64 add per right-hand side; L carries on and is added at
+//     the end of the chunk).  L's own FP32 rounding is the leading error,
+//     about 2^-48 sqrt(32 * 4 / n) of sum_j |a_ij x_j| per row.
 // Every multiply and add of the transformations is an explicit _rn
 // intrinsic, so no contraction into an FMA can break them.  A bit-faithful
 // CPU emulation against correctly rounded residuals (N(0,1) A, x near the
 // solution): at most 6 ulps of sum_j |a_ij x_j| + |b_i| per row at
-// n = 1024 .. 4096 and fewer beyond (13 at n = 100).
+// n = 1024 .. 4096 and fewer beyond (18 at n = 100).
 //
 // The sum over columns is split into chunks (one CTA per 128 rows x chunk);
 // the chunks' FP64 partial sums are added in a fixed order by the finish
@@ -65,34 +67,80 @@ __device__ __forceinline__ int exp2_of(double v) {
   return (v == 0.0 || !isfinite(v)) ? 0 : ilogb(v);
 }
 
+// (fl32(v), fl32(v - fl32(v))) for |v| in [2^-74, 2^127) by integer operations
+// on v's bits, bit-identical to the two cvt.rn.f32.f64 conversions (GB300
+// converts FP64 on its FP64 pipe, which would bind the split).  With
+// v = (-1)^s m 2^(E-1075), m the 53-bit significand: the high word keeps
+// m's top 24 bits rounded to nearest even (a carry out of them moves into
+// the exponent), and v - fl32(v) = (-1)^s d 2^(E-1075) exactly, with d the
+// signed remainder (|d| <= 2^28), so its FP32 rounding is that of the
+// integer d times a power of two.  Returns false outside the range (zero,
+// subnormal, huge, inf, NaN): the caller converts in FP64 there.
+__device__ __forceinline__ bool split_bits(double v, float& hi, float& lo) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const int E = (int)((b >> 52) & 0x7ff);
+  if (E < 949 || E > 1149) return false;
+  const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+  const unsigned q = (unsigned)(m >> 29);
+  const unsigned rem = (unsigned)m & 0x1FFFFFFFu;
+  const unsigned inc = (rem > 0x10000000u || (rem == 0x10000000u && (q & 1u))) ? 1u : 0u;
+  const unsigned sgn = (unsigned)(b >> 63);
+  hi = __uint_as_float((sgn << 31) | (((unsigned)(E - 896) << 23) + (q + inc - 0x800000u)));
+  const int d = (int)rem - (int)(inc << 29);
+  lo = __fmul_rn(__int2float_rn(sgn ? -d : d), __uint_as_float((unsigned)(E - 948) << 23));
+  return true;
+}
+
 }  // namespace
 
 // a -> Af = fl32(a) (the copy the factorization overwrites; skipped when Af
-// is null), ah = fl32(a),
-// al = fl32(a - ah); per CTA the sum of squares and max |a| of its part of
-// A (one CTA per column range, fixed-order reductions).
+// is null), ah = fl32(a), al = fl32(a - ah); per CTA the sum of squares and
+// max |a| of the entries it visited (fixed-order reductions).  The work is
+// cut into chunks of 1024 rows of one column, taken in column-major order
+// by a grid-stride loop, so the CTAs running at once stream one contiguous
+// stretch of A and of the outputs (CTAs walking whole columns of their own
+// start 2 MB apart at n = 32768, all on the same memory partition).  Four
+// rows per thread are in flight at once; the only FP64 arithmetic per entry
+// is the sum of squares.
 __global__ void __launch_bounds__(256)
 split_a_kernel(const double* __restrict__ A, long lda, int n, float* __restrict__ Af,
                float* __restrict__ Ahi, float* __restrict__ Alo, double* __restrict__ part) {
   __shared__ double s_sq[256], s_mx[256];
-  const int cols = ceil_div(n, gridDim.x);
-  const int j0 = blockIdx.x * cols, j1 = min(j0 + cols, n);
-  double sq = 0.0, mx = 0.0;
-  for (int j = j0; j < j1; ++j) {
-    const double* a = A + (long)j * lda;
-    const long o = (long)j * n;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-      const double v = a[i];
-      const float h = (float)v;
-      if (Af) Af[o + i] = h;
-      Ahi[o + i] = h;
-      Alo[o + i] = (float)(v - (double)h);
-      sq = fma(v, v, sq);
-      mx = fmax(mx, fabs(v));
+  double sq = 0.0;
+  unsigned long long mxb = 0ull;  // bits of max |a| (non-negative doubles order as integers)
+  auto one = [&](double v, long o) {
+    float h, l;
+    if (!split_bits(v, h, l)) {
+      h = (float)v;
+      l = (float)(v - (double)h);
+    }
+    if (Af) Af[o] = h;
+    Ahi[o] = h;
+    Alo[o] = l;
+    sq = fma(v, v, sq);
+    const unsigned long long ab = (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
+    if (ab <= 0x7FF0000000000000ull && ab > mxb) mxb = ab;  // NaN never counts
+  };
+  const int rch = ceil_div(n, 1024);
+  const long nchunks = (long)rch * n;
+  for (long c = blockIdx.x; c < nchunks; c += gridDim.x) {
+    const int j = (int)(c / rch);
+    const int i0 = (int)(c - (long)j * rch) * 1024;
+    const double* a = A + (long)j * lda + i0;
+    const long o = (long)j * n + i0;
+    const int i = threadIdx.x;
+    if (i0 + 1024 <= n) {
+      double v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) v[u] = __ldcs(a + i + 256 * u);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) one(v[u], o + i + 256 * u);
+    } else {
+      for (int r = i; i0 + r < n; r += 256) one(a[r], o + r);
     }
   }
   s_sq[threadIdx.x] = sq;
-  s_mx[threadIdx.x] = mx;
+  s_mx[threadIdx.x] = __longlong_as_double((long long)mxb);
   __syncthreads();
   for (int s = 128; s > 0; s >>= 1) {
     if (threadIdx.x < s) {
@@ -107,17 +155,30 @@ split_a_kernel(const double* __restrict__ A, long lda, int n, float* __restrict_
   }
 }
 
-// out[0] = ||A||_F^2, out[1] = max |a| (fixed order over the CTAs).
-__global__ void split_a_finish_kernel(const double* __restrict__ part, int nblk,
-                                      double* __restrict__ out) {
-  if (threadIdx.x != 0) return;
+// out[0] = ||A||_F^2, out[1] = max |a|: thread t adds the partials t, t + 256,
+// ... in order, then a fixed tree (reproducible run to run).
+__global__ void __launch_bounds__(256)
+split_a_finish_kernel(const double* __restrict__ part, int nblk, double* __restrict__ out) {
+  __shared__ double s_sq[256], s_mx[256];
   double sq = 0.0, mx = 0.0;
-  for (int b = 0; b < nblk; ++b) {
+  for (int b = threadIdx.x; b < nblk; b += 256) {
     sq += part[2 * b];
     mx = fmax(mx, part[2 * b + 1]);
   }
-  out[0] = sq;
-  out[1] = mx;
+  s_sq[threadIdx.x] = sq;
+  s_mx[threadIdx.x] = mx;
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      s_sq[threadIdx.x] += s_sq[threadIdx.x + s];
+      s_mx[threadIdx.x] = fmax(s_mx[threadIdx.x], s_mx[threadIdx.x + s]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out[0] = s_sq[0];
+    out[1] = s_mx[0];
+  }
 }
 
 // Column c of X (c < q; zero columns up to Q): scale s_c = 2^-(k_A + k_x)
@@ -149,7 +210,8 @@ split_x_kernel(const double* __restrict__ X, long ldx, int n, int q, int Q,
 }
 
 // partial[(chunk Q + c) n + i] = sum over this chunk's columns j of
-// a_ij (s_c x_jc), in double-float words flushed to FP64 every 32 columns.
+// a_ij (s_c x_jc), in double-float words whose high word is flushed to FP64
+// every 32 columns.
 template <int Q>
 __global__ void __launch_bounds__(kDfRows)
 df_residual_partial_kernel(int n, const float* __restrict__ Ahi, const float* __restrict__ Alo,
@@ -179,8 +241,12 @@ df_residual_partial_kernel(int n, const float* __restrict__ Ahi, const float* __
   };
 
   double acc[Q];
+  float L[Q];
 #pragma unroll
-  for (int c = 0; c < Q; ++c) acc[c] = 0.0;
+  for (int c = 0; c < Q; ++c) {
+    acc[c] = 0.0;
+    L[c] = 0.f;
+  }
   if (j0 < j1) stage_copy(0, j0);
   int buf = 0;
   for (int js = j0; js < j1; js += kDfStage, buf ^= 1) {
@@ -192,9 +258,9 @@ df_residual_partial_kernel(int n, const float* __restrict__ Ahi, const float* __
       asm volatile("cp.async.wait_group 0;" ::: "memory");
     }
     __syncthreads();
-    float S[Q], L[Q];
+    float S[Q];
 #pragma unroll
-    for (int c = 0; c < Q; ++c) S[c] = L[c] = 0.f;
+    for (int c = 0; c < Q; ++c) S[c] = 0.f;
     const float* ph = Ahi + ia + (long)js * n;
     const float* pl = Alo + ia + (long)js * n;
     const float2* xs = sx[buf];
@@ -221,8 +287,7 @@ df_residual_partial_kernel(int n, const float* __restrict__ Ahi, const float* __
 #pragma unroll
         for (int c = 0; c < Q; ++c) {
           acc[c] += (double)S[c];
-          acc[c] += (double)L[c];
-          S[c] = L[c] = 0.f;
+          S[c] = 0.f;
         }
       }
     }
@@ -236,12 +301,11 @@ df_residual_partial_kernel(int n, const float* __restrict__ Ahi, const float* __
       }
     }
 #pragma unroll
-    for (int c = 0; c < Q; ++c) {
-      acc[c] += (double)S[c];
-      acc[c] += (double)L[c];
-    }
+    for (int c = 0; c < Q; ++c) acc[c] += (double)S[c];
     __syncthreads();  // every thread is done with sx[buf] before it is refilled
   }
+#pragma unroll
+  for (int c = 0; c < Q; ++c) acc[c] += (double)L[c];
   if (row)
 #pragma unroll
     for (int c = 0; c < Q; ++c) partial[((long)chunk * Q + c) * n + i] = acc[c];
@@ -270,7 +334,7 @@ cudaError_t launch_split_a(const double* A, long lda, int n, float* Af, float* A
   if (n <= 0) return cudaSuccess;
   const int nblk = (int)df_split_parts(n);
   split_a_kernel<<<nblk, 256, 0, stream>>>(A, lda, n, Af, Ahi, Alo, part);
-  split_a_finish_kernel<<<1, 32, 0, stream>>>(part, nblk, out);
+  split_a_finish_kernel<<<1, 256, 0, stream>>>(part, nblk, out);
   return cudaGetLastError();
 }
 

@@ -61,7 +61,8 @@ __host__ __device__ __forceinline__ float fp8_scale(float amax) {
 
 // ---------------------------------------------------------------------------
 // Persistent form: one CTA per SM (of a bounded grid) walks the 128 x 256
-// tiles in m-fastest order.  Each stage of the shared-memory ring holds a
+// tiles in groups of `group_n` tile columns, n fastest within a group (see
+// tile_origin).  Each stage of the shared-memory ring holds a
 // k-block of every operand copy at once -- for TF32x3 the hi and lo tiles of
 // A and of B (96 KB), from which the three products are issued, instead of
 // streaming the operands three times -- and two 256-column TMEM
@@ -84,14 +85,28 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
+// Origin (m0, n0) of tile t.  The tile columns are taken `group_n` at a time
+// and, within a group, the tiles run n fastest: the CTAs of one wave share a
+// few rows of A tiles and the group's B tiles, which stay in L2 from wave to
+// wave, so A streams from DRAM once per group instead of once per tile
+// column (m fastest re-read all of A for every column of tiles).
+__device__ __forceinline__ void tile_origin(int t, int tiles_m, int tiles_n, int group_n,
+                                            int& m0, int& n0) {
+  const int per_group = group_n * tiles_m;
+  const int g = t / per_group, idx = t - g * per_group;
+  const int gn = min(group_n, tiles_n - g * group_n);
+  m0 = (idx / gn) * kBM;
+  n0 = (g * group_n + idx % gn) * kBN;
+}
+
 template <int KIND, bool SPLIT>
 __global__ void __launch_bounds__(kPThreads, 1)
 tc_gemm_persistent_kernel(const __grid_constant__ CUtensorMap tmA,
                           const __grid_constant__ CUtensorMap tmB,
                           const __grid_constant__ CUtensorMap tmAlo,
                           const __grid_constant__ CUtensorMap tmBlo, float* __restrict__ C,
-                          long ldc, int m, int n, int num_kb, const float* __restrict__ amax,
-                          DevStatus* st) {
+                          long ldc, int m, int n, int num_kb, int group_n,
+                          const float* __restrict__ amax, DevStatus* st) {
   constexpr int kStageBytes = (SPLIT ? 2 : 1) * (kStageA + kStageB);
   constexpr int kS = kPRing / kStageBytes;  // 2 (split) or 4 stages
   extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -138,7 +153,8 @@ tc_gemm_persistent_kernel(const __grid_constant__ CUtensorMap tmA,
     // TMA producer
     uint32_t it = 0;
     for (int t = blockIdx.x; t < ntiles && !s_abort; t += gridDim.x) {
-      const int m0 = (t % tiles_m) * kBM, n0 = (t / tiles_m) * kBN;
+      int m0, n0;
+      tile_origin(t, tiles_m, tiles_n, group_n, m0, n0);
       for (int kb = 0; kb < num_kb; ++kb, ++it) {
         const int s = it % kS;
         if (it >= (uint32_t)kS && !mbar_wait(&empty_bar[s], ((it / kS) & 1) ^ 1, st, 20)) {
@@ -204,7 +220,8 @@ tc_gemm_persistent_kernel(const __grid_constant__ CUtensorMap tmA,
     for (int t = blockIdx.x; t < ntiles && !s_abort; t += gridDim.x, ++lt) {
       const int b = lt & 1;
       const uint32_t u = lt >> 1;
-      const int m0 = (t % tiles_m) * kBM, n0 = (t / tiles_m) * kBN;
+      int m0, n0;
+      tile_origin(t, tiles_m, tiles_n, group_n, m0, n0);
       const int row = m0 + 32 * q + lane;
       const bool row_ok = row < m;
       float* crow = C + row;
@@ -530,8 +547,13 @@ cudaError_t launch_tc_gemm_sub(int kind, int m, int n, int K, const float* A, lo
     }
   }
   cfg.gridDim = dim3(grid);
+  // tile columns per group: the group's B tiles (every operand copy) take
+  // ~16 MB of the 129 MB L2, beside a wave's C tiles (~40 MB read and written)
+  const int tiles_n = (n + kBN - 1) / kBN;
+  const size_t btile = (size_t)kBN * Kp * esz * (split ? 2 : 1);
+  const int group_n = (int)std::max<size_t>(1, std::min<size_t>(tiles_n, (16u << 20) / btile));
   if (ev0) cudaEventRecord(ev0, stream);
-  e = cudaLaunchKernelEx(&cfg, kern, tmA, tmB, tmAlo, tmBlo, C, ldc, m, n, num_kb,
+  e = cudaLaunchKernelEx(&cfg, kern, tmA, tmB, tmAlo, tmBlo, C, ldc, m, n, num_kb, group_n,
                          (const float*)amax, st);
   if (e != cudaSuccess) return e;
   if (ev1) cudaEventRecord(ev1, stream);

@@ -19,13 +19,19 @@ template <typename T>
 cudaError_t launch_trtri_diag(const T* A, long lda, int n, bool lower, bool unit, T* Dinv,
                               cudaStream_t stream);
 
+// 64-bit words the solve publishes its block rows in (two 64 x 16 tiles
+// per block row).
+size_t trsv_tag_words(int n);
+
 // op(A) X = B in place (B n x q, q <= 16) with op(A) the lower or upper
-// triangle of A and Dinv its inverted diagonal blocks.  flags holds
-// trsv_blocks(n) ints that never held `epoch` before this call (start them
-// at zero and use a new epoch per call); ticket is one unsigned.
+// triangle of A and Dinv its inverted diagonal blocks.  tags holds
+// trsv_tag_words(n) words whose high halves never held `epoch` before this
+// call (start them at zero and use a new epoch per call); ticket is one
+// unsigned.
 template <typename T>
 cudaError_t launch_trsv_persistent(const T* A, long lda, const T* Dinv, T* X, long ldx, int n,
-                                   int q, bool lower, unsigned* ticket, int* flags, int epoch,
-                                   DevStatus* st, int num_sms, cudaStream_t stream);
+                                   int q, bool lower, unsigned* ticket, unsigned long long* tags,
+                                   unsigned epoch, DevStatus* st, int num_sms,
+                                   cudaStream_t stream);
 
 }  // namespace elgb

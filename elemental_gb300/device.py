@@ -21,7 +21,7 @@ PRECISIONS = {"fp64": 0, "fp32": 1, "tf32": 2, "bf16": 3, "fp8": 4}
 PRECISION_NAMES = {v: k for k, v in PRECISIONS.items()}
 METHODS = {"lu-ir": 0, "gmres-ir": 1}
 PROFILE_TAGS = {"tc_gemm": 0, "panel": 1, "swap": 2, "trsm": 3, "gemm_simt": 4,
-                "residual": 5, "lowprec_solve": 6}
+                "residual": 5, "lowprec_solve": 6, "convert": 7}
 
 
 class ElGBError(RuntimeError):
@@ -112,7 +112,8 @@ class Context:
         """ElGBSetOption: "lookahead" (0/1), "panel_ctas" (0 = auto) or
         "tournament" (0/1: tournament pivoting in lu_mixed's leaf panels)."""
         code = {"lookahead": 1, "panel_ctas": 2, "tournament": 3, "panel_cluster": 4,
-                "panel_regs": 5, "residual_df": 6, "panel_trace": 7, "trail_grid": 8}[option]
+                "panel_regs": 5, "residual_df": 6, "panel_trace": 7, "trail_grid": 8,
+                "panel_rows": 9}[option]
         self._rc(self.lib.ElGBSetOption(self.h, code, int(value)), "SetOption")
 
     def panel_trace(self, ncols):

@@ -82,7 +82,12 @@ int ElGBSetBlocksize(int nb);
  *                       run one CTA per tile; 1 as 2 with the panel's
  *                       updates on at most 32 persistent CTAs; 0 the
  *                       trailing update holds every SM; 3 one CTA per tile
- *                       for both. */
+ *                       for both.
+ *   ELGB_OPT_PANEL_ROWS  rows of a leaf panel per CTA that the panel kernels
+ *                       aim for (64 .. 1536, default 1024): more CTAs make
+ *                       each pivot step's local update shorter and its
+ *                       exchange longer.  Process-wide, like
+ *                       ELGB_OPT_PANEL_CLUSTER. */
 enum {
   ELGB_OPT_LOOKAHEAD = 1,
   ELGB_OPT_PANEL_CTAS = 2,
@@ -91,7 +96,8 @@ enum {
   ELGB_OPT_PANEL_REGS = 5,
   ELGB_OPT_RESIDUAL_DF = 6,
   ELGB_OPT_PANEL_TRACE = 7,
-  ELGB_OPT_TRAIL_GRID = 8
+  ELGB_OPT_TRAIL_GRID = 8,
+  ELGB_OPT_PANEL_ROWS = 9
 };
 int ElGBSetOption(ElGBContext ctx, int option, int value);
 
@@ -122,6 +128,8 @@ enum {
   ELGB_PROF_GEMM_SIMT = 4, /* CUDA-core GEMM (FP64 path, small FP32 updates) */
   ELGB_PROF_RESIDUAL = 5,  /* FP64 residual b - A x                          */
   ELGB_PROF_SOLVE = 6,     /* low-precision triangular solves of refinement  */
+  ELGB_PROF_CONVERT = 7,   /* FP64 -> FP32 copy of A (with the double-float
+                              words and the norms of A, when those are made) */
   ELGB_PROF_SIDE = 8       /* + tag: that kernel's launches on the look-ahead
                               panel stream only (the factorization's critical
                               chain); the plain tags count both streams     */

@@ -198,6 +198,10 @@ def case_panel_trace(ctx, a):
     A0 = torch.randn(a.n, a.n, device="cuda", generator=g).t()
     A = A0.clone()
     ctx.set_option("panel_trace", a.n)
+    ctx.set_option("lookahead", a.lookahead)
+    ctx.set_option("trail_grid", a.trail_grid)
+    ctx.set_option("panel_cluster", a.panel_cluster)
+    ctx.set_option("panel_rows", a.panel_rows)
     try:
         ctx.lu_mixed(A, gemm_kind=a.kind, nb=a.nb)
         A.copy_(A0)
@@ -205,6 +209,10 @@ def case_panel_trace(ctx, a):
         tr = ctx.panel_trace(a.n)
     finally:
         ctx.set_option("panel_trace", 0)
+        ctx.set_option("lookahead", 1)
+        ctx.set_option("trail_grid", 2)
+        ctx.set_option("panel_cluster", 16)
+        ctx.set_option("panel_rows", 1024)
     ok = np.all(tr > 0, axis=1)
     cols = np.arange(a.n)
     d_pub = (tr[:, 1] - tr[:, 0]) / 1e3
@@ -225,7 +233,9 @@ def case_panel_trace(ctx, a):
             "us_front_half": round(float(np.median(d_front[sel])), 3),
             "us_per_step": round(float(np.nanmedian(step[sel])), 3)}
     tot_steps = float(np.nansum(step[ok])) / 1e3
-    return dict(case="panel_trace", n=a.n, kind=KIND_NAMES[a.kind], ms=ms, traced=int(ok.sum()),
+    return dict(case="panel_trace", n=a.n, kind=KIND_NAMES[a.kind], lookahead=a.lookahead,
+                trail_grid=a.trail_grid, panel_cluster=a.panel_cluster,
+                panel_rows=a.panel_rows, ms=ms, traced=int(ok.sum()),
                 leaf_step_ms_total=tot_steps, bands=bands)
 
 
@@ -248,8 +258,14 @@ def main(argv=None):
     p.add_argument("--simt", action="store_true", help="batched: SIMT trailing updates")
     p.add_argument("--precision", default="fp32", choices=["fp64", "fp32", "bf16"])
     p.add_argument("--seed", type=int, default=20261204)
-    p.add_argument("--lookahead", type=int, default=1, help="lu_breakdown: 0 = one stream")
-    p.add_argument("--trail-grid", type=int, default=2, help="lu_breakdown: ELGB_OPT_TRAIL_GRID")
+    p.add_argument("--lookahead", type=int, default=1,
+                   help="lu_breakdown, panel_trace: 0 = one stream")
+    p.add_argument("--trail-grid", type=int, default=2,
+                   help="lu_breakdown, panel_trace: ELGB_OPT_TRAIL_GRID")
+    p.add_argument("--panel-cluster", type=int, default=16,
+                   help="panel_trace: ELGB_OPT_PANEL_CLUSTER (1 = cooperative leaf panels only)")
+    p.add_argument("--panel-rows", type=int, default=1024,
+                   help="panel_trace: ELGB_OPT_PANEL_ROWS")
     a = p.parse_args(argv)
     ctx = D.context(0)
     out = CASES[a.case](ctx, a)

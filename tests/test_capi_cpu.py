@@ -91,6 +91,24 @@ def test_device_api_fails_loudly_without_gpu():
     assert lib.ElGBCreate(ctypes.byref(h), 0) != 0
 
 
+def test_host_alloc_argument_handling():
+    """ElGBHostAlloc / ElGBHostFree: zero bytes, NULL and foreign pointers
+    (host logic only); without a GPU the driver refuses the registration
+    and the call fails cleanly."""
+    import torch
+
+    lib = _lib.load()
+    p = ctypes.c_void_p(1234)
+    assert lib.ElGBHostAlloc(0, ctypes.byref(p)) == 0 and not p.value
+    assert lib.ElGBHostFree(None) == 0
+    buf = ctypes.create_string_buffer(64)
+    assert lib.ElGBHostFree(ctypes.cast(buf, ctypes.c_void_p)) == 4  # EL_LOGIC_ERROR
+    assert lib.ElGBHostAlloc(1 << 20, None) == 3  # EL_ARG_ERROR
+    if not torch.cuda.is_available():
+        assert lib.ElGBHostAlloc(1 << 20, ctypes.byref(p)) == 5  # EL_RUNTIME_ERROR
+        assert not p.value
+
+
 def test_python_matrix_views_share_memory():
     """El.Matrix slicing gives views through ElView_d (the reference's
     Matrix.__getitem__, python/core/Matrix.py:456-482); a permutation applied

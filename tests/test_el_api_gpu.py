@@ -61,3 +61,32 @@ def test_cholesky_hpd_linear_solve_through_el_c_abi():
     G = El.Matrix(mats.gaussian(30, 30, 9))
     with pytest.raises(El.SingularMatrixException):
         El.Cholesky(El.LOWER, G)
+
+
+def test_linear_solve_mixed_on_library_host_memory():
+    """El.host_empty (ElGBHostAlloc: registered anonymous pages) holds the
+    matrices of a host-matrix call; results equal those on ordinary host
+    memory, and the memory round-trips through device copies."""
+    import torch
+
+    n, q = 2048, 3
+    A0 = mats.gaussian(n, n, 21)
+    B0 = mats.gaussian(n, q, 22)
+    Ah = El.host_empty((n, n))
+    Ah[...] = A0
+    Bh = El.host_empty((n, q))
+    Bh[...] = B0
+    assert Ah.flags.f_contiguous and Bh.flags.f_contiguous
+    A = El.Matrix(Ah)
+    B = El.Matrix(Bh)
+    assert A.array.ctypes.data == Ah.ctypes.data
+    El.LinearSolveMixed(A, B)
+    B2 = El.Matrix(B0.copy(order="F"))
+    El.LinearSolveMixed(El.Matrix(A0.copy(order="F")), B2)
+    assert np.array_equal(Bh, B2.array)
+    assert O.backward_error(A0, Bh, B0) <= n * EPS
+    t = torch.from_numpy(Ah)
+    d = t.cuda(non_blocking=True)
+    back = El.host_empty((n, n))
+    torch.from_numpy(back).copy_(d)
+    assert np.array_equal(back, A0)

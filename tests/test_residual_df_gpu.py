@@ -90,6 +90,23 @@ def test_df_product_without_b_and_extreme_scaling(ctx):
     assert np.all(np.abs(R[rows] - Rex) <= 16 * EPS * scale)
 
 
+def test_df_split_of_entries_across_exponents(ctx):
+    """Entries from 2^-90 to 2^40 (with exact zeros): the split of A takes
+    its integer path for |a| in [2^-74, 2^127) and FP64 conversions for the
+    rest; both must give the words of cvt.rn.f32.f64."""
+    n = 1536
+    rng = np.random.default_rng(8)
+    A = rng.standard_normal((n, n)) * np.exp2(rng.integers(-90, 41, (n, n)))
+    A[rng.random((n, n)) < 0.01] = 0.0
+    X = rng.standard_normal((n, 3))
+    B = A @ X
+    R = ctx.residual_df(dev(A), dev(X), dev(B)).cpu().numpy()
+    rows = np.arange(0, n, 61)
+    Rex = exact_residual_rows(A, X, B, rows)
+    scale = np.abs(A[rows]) @ np.abs(X) + np.abs(B[rows])
+    assert np.all(np.abs(R[rows] - Rex) <= 16 * EPS * scale)
+
+
 def test_df_residual_falls_back_for_entries_outside_fp32_range(ctx):
     n = 512
     rng = np.random.default_rng(6)
