@@ -14,6 +14,7 @@ Device-resident work (torch CUDA tensors, no host copies) goes through
 from __future__ import annotations
 
 import ctypes
+import sys
 
 import numpy as np
 
@@ -370,9 +371,11 @@ class _HostBlock:
         self.nbytes = nbytes
 
     def __del__(self):
-        if getattr(self, "ptr", None):
+        # not during interpreter shutdown: the CUDA runtime may already be
+        # torn down, and the process's pages go back to the system anyway
+        if getattr(self, "ptr", None) and not sys.is_finalizing():
             _lib.load().ElGBHostFree(self.ptr)
-            self.ptr = None
+        self.ptr = None
 
 
 def host_empty(shape, dtype=np.float64, order="F"):

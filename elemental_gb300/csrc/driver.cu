@@ -1241,7 +1241,8 @@ int ElGBSetOption(ElGBContext ctx, int option, int value) {
       elgb::g_panel_cluster = value;
       return 0;
     case ELGB_OPT_PANEL_REGS:
-      elgb::g_panel_regs = value ? 1 : 0;
+      if (value < 0 || value > 2) return elgb::kElArgError;
+      elgb::g_panel_regs = value;
       return 0;
     case ELGB_OPT_RESIDUAL_DF:
       ctx->opt_residual_df = value ? 1 : 0;

@@ -15,8 +15,9 @@ namespace elgb {
 // only); set by ElGBSetOption(ELGB_OPT_PANEL_CLUSTER).
 int g_panel_cluster = 16;
 int g_panel_rows = 1024;
-// FP32 panels with the rows in registers (ElGBSetOption(ELGB_OPT_PANEL_REGS)).
-int g_panel_regs = 0;
+// FP32 panels with the rows in registers (ElGBSetOption(ELGB_OPT_PANEL_REGS)):
+// 1 cooperative, 2 on a cluster where one fits (the default).
+int g_panel_regs = 2;
 
 template <typename T>
 __device__ __forceinline__ T absv(T x) { return x < T(0) ? -x : x; }
@@ -715,6 +716,194 @@ getf2_panel_cluster_kernel(PanelParams<T> p) {
   cluster_barrier();  // no CTA leaves while another may still read its slots
 }
 
+// The cluster panel with the rows in registers (FP32).  512 threads; thread
+// t holds local rows t and t + 512 of its CTA's R <= 1024 rows, all W
+// values of each in registers, and the column loop is unrolled so every
+// register index is fixed.  Per column: publish (candidate row and row j
+// from registers into the CTA's own slot), the cluster barrier, thread
+// g < C reads CTA g's slot, every warp picks the pivot, then the whole
+// rank-1 update of the thread's two rows and the next column's candidate.
+// No shared-memory traffic per entry, so a step is the exchange plus a few
+// dozen register FMAs.  Same slots, exchange, pivot choice and arithmetic
+// (l = a_j * (1 / pivot), a_c = fma(-l, u_c, a_c)) as the kernels above:
+// same pivots, same factors.
+constexpr int kRcThreads = 512;
+
+// The register kernel's slot: 16-byte aligned rows, read with vector
+// distributed-shared-memory loads.
+struct __align__(16) RcSlot {
+  float cand[kPanelW];
+  float diag[kPanelW];
+  float val;
+  int row;
+};
+
+__device__ __forceinline__ float4 ld_cluster_v4(uint32_t addr) {
+  float4 v;
+  asm volatile("ld.shared::cluster.v4.f32 {%0, %1, %2, %3}, [%4];"
+               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+               : "r"(addr));
+  return v;
+}
+__device__ __forceinline__ void ld_cluster_head(uint32_t addr, float& v, int& r) {
+  asm volatile("ld.shared::cluster.v2.b32 {%0, %1}, [%2];" : "=f"(v), "=r"(r) : "r"(addr));
+}
+
+template <int W>
+__global__ void __launch_bounds__(kRcThreads, 1)
+getf2_panel_cluster_reg_kernel(PanelParams<float> p) {
+  static_assert(W == kPanelW, "one slot layout");
+  __shared__ RcSlot slots[2];
+  __shared__ __align__(16) float s_d[W];
+  __shared__ __align__(16) float s_rows[16][W];
+  __shared__ float s_gv[32];
+  __shared__ int s_gr[32];
+  __shared__ float s_rv[33];
+  __shared__ int s_rr[33];
+
+  const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x;
+  const int lane = tid & 31;
+  const int R = p.R, w = p.w;
+  const int rb = b * R;
+  const int re = min(rb + R, p.mp);
+  const int nr = max(re - rb, 0);
+
+  float a[2][W];
+  int grow[2];  // global panel row of each register row, -1 past the CTA's rows
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const int r = tid + i * kRcThreads;
+    grow[i] = r < nr ? rb + r : -1;
+#pragma unroll
+    for (int c = 0; c < W; ++c)
+      a[i][c] = (grow[i] >= 0 && c < w) ? p.A[(long)grow[i] + (long)c * p.lda] : 0.f;
+  }
+
+  float bv = -1.f;
+  int br = -1;
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+    if (grow[i] >= 0) {
+      const float v = fabsf(a[i][0]);
+      if (argmax_better(v, grow[i], bv, br)) {
+        bv = v;
+        br = grow[i];
+      }
+    }
+  block_argmax(bv, br, s_rv, s_rr);
+  cluster_barrier();  // every CTA of the cluster is running
+
+#pragma unroll
+  for (int j = 0; j < W; ++j) {
+    if (j < w) {
+      RcSlot* my = &slots[j & 1];
+      unsigned long long* tr =
+          (p.s.trace && b == 0 && tid == 0) ? p.s.trace + 4 * (long)j : nullptr;
+      if (tr) tr[0] = globaltimer_ns();
+      // 1. publish from the registers of the rows' owners
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        if (grow[i] >= 0 && grow[i] == br)
+#pragma unroll
+          for (int c = 0; c < W; ++c) my->cand[c] = a[i][c];
+        if (grow[i] == j)
+#pragma unroll
+          for (int c = 0; c < W; ++c) my->diag[c] = a[i][c];
+      }
+      if (tid == 0) {
+        my->val = bv;
+        my->row = br;
+      }
+      cluster_arrive();
+      if (tr) tr[1] = globaltimer_ns();
+      cluster_wait();
+      // 2. thread g < C reads CTA g's slot: head and candidate row in one
+      // round trip, row j (its owner's slot only) in a second
+      if (tid < G) {
+        const uint32_t base = cluster_map(my, (unsigned)tid);
+        float gv;
+        int gr;
+        ld_cluster_head(base + (uint32_t)offsetof(RcSlot, val), gv, gr);
+        float4 cr[W / 4];
+#pragma unroll
+        for (int c = 0; c < W / 4; ++c)
+          cr[c] = ld_cluster_v4(base + (uint32_t)offsetof(RcSlot, cand) + 16u * c);
+        s_gv[tid] = gv;
+        s_gr[tid] = gr;
+#pragma unroll
+        for (int c = 0; c < W / 4; ++c) reinterpret_cast<float4*>(s_rows[tid])[c] = cr[c];
+        if (tid == j / R) {
+#pragma unroll
+          for (int c = 0; c < W / 4; ++c)
+            cr[c] = ld_cluster_v4(base + (uint32_t)offsetof(RcSlot, diag) + 16u * c);
+#pragma unroll
+          for (int c = 0; c < W / 4; ++c) reinterpret_cast<float4*>(s_d)[c] = cr[c];
+        }
+      }
+      __syncthreads();
+      if (tr) tr[2] = globaltimer_ns();
+      // 3. the pivot (every warp, identical result)
+      int piv;
+      {
+        float v = -1.f;
+        int r = -1;
+        if (lane < G && argmax_better(s_gv[lane], s_gr[lane], v, r)) {
+          v = s_gv[lane];
+          r = s_gr[lane];
+        }
+        warp_argmax(v, r);
+        piv = (r < 0) ? j : r;
+      }
+      const float* urow = (piv == j) ? s_d : s_rows[piv / R];
+      if (b == 0 && tid == 0) p.ipiv[j] = p.row_base + piv;
+      const float alpha = urow[j];
+      const bool singular = (alpha == 0.f);
+      if (singular && b == 0 && tid == 0) atomicCAS(&p.st->info, 0, p.info_base + j + 1);
+      const float inv = singular ? 1.f : 1.f / alpha;
+      // 4. interchange, multipliers, rank-1 update, next candidate
+      bv = -1.f;
+      br = -1;
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        const int row = grow[i];
+        if (row < 0) continue;
+        if (piv != j && row == j) {  // row j takes the pivot row; not updated
+#pragma unroll
+          for (int c = 0; c < W; ++c) a[i][c] = urow[c];
+          continue;
+        }
+        if (piv != j && row == piv)  // the pivot row's position takes old row j
+#pragma unroll
+          for (int c = 0; c < W; ++c) a[i][c] = s_d[c];
+        if (row <= j) continue;
+        float l = a[i][j];
+        if (!singular) l *= inv;
+        a[i][j] = l;
+#pragma unroll
+        for (int c = j + 1; c < W; ++c) a[i][c] = fmaf(-l, urow[c], a[i][c]);
+        if (j + 1 < w) {
+          const float v = fabsf(a[i][j + 1 < W ? j + 1 : j]);
+          if (argmax_better(v, row, bv, br)) {
+            bv = v;
+            br = row;
+          }
+        }
+      }
+      // the leading barrier of block_argmax also orders every read of s_d /
+      // s_rows above before the next column's gather refills them
+      block_argmax(bv, br, s_rv, s_rr);
+      if (tr) tr[3] = globaltimer_ns();
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+    if (grow[i] >= 0)
+#pragma unroll
+      for (int c = 0; c < W; ++c)
+        if (c < w) p.A[(long)grow[i] + (long)c * p.lda] = a[i][c];
+  cluster_barrier();  // no CTA leaves while another may still read its slots
+}
+
 // Cluster size for a panel of mp rows: the power of two giving about
 // g_panel_rows rows per CTA (at least 2 CTAs, at most max_cluster), or 0
 // when one cluster cannot hold the panel in shared memory or the panel is
@@ -767,6 +956,43 @@ static cudaError_t launch_getf2_panel_cluster(T* A, long lda, int mp, int w, int
   return cudaLaunchKernelEx(&cfg, kern, prm);
 }
 
+// The register cluster kernel for an FP32 panel of mp rows on C CTAs
+// (ceil(mp / C) <= 1024); cudaErrorNotSupported when the cluster cannot be
+// placed.
+static cudaError_t launch_getf2_panel_cluster_reg(float* A, long lda, int mp, int w, int* ipiv,
+                                                  int row_base, int info_base, DevStatus* st,
+                                                  int C, unsigned long long* trace,
+                                                  cudaStream_t stream) {
+  const int R = ceil_div(mp, C);
+  if (R > 2 * kRcThreads) return cudaErrorNotSupported;
+  auto kern = getf2_panel_cluster_reg_kernel<kPanelW>;
+  cudaError_t e = cudaSuccess;
+  if (C > 8) e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(C);
+  cfg.blockDim = dim3(kRcThreads);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = C;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int nclusters = 0;
+  e = cudaOccupancyMaxActiveClusters(&nclusters, (void*)kern, &cfg);
+  if (e != cudaSuccess || nclusters < 1) {
+    cudaGetLastError();
+    return cudaErrorNotSupported;
+  }
+  PanelScratch<float> ps{};
+  ps.trace = trace;
+  PanelParams<float> prm{A, lda, mp, w, R, ipiv, row_base, info_base, 0, ps, st};
+  return cudaLaunchKernelEx(&cfg, kern, prm);
+}
+
 template <typename T>
 cudaError_t launch_getf2_panel(T* A, long lda, int mp, int w, int* ipiv, int row_base,
                                int info_base, int epoch_base, const PanelScratch<T>& s,
@@ -774,7 +1000,17 @@ cudaError_t launch_getf2_panel(T* A, long lda, int mp, int w, int* ipiv, int row
   if (w <= 0 || mp <= 0) return cudaSuccess;
   if (w > kPanelW || mp < w) return cudaErrorInvalidValue;
   if constexpr (sizeof(T) == 4) {
-    if (g_panel_regs && !nopiv) {
+    if (g_panel_regs == 2 && g_panel_cluster > 1 && !nopiv) {
+      // rows in registers on a cluster where one fits (<= 1024 rows per CTA)
+      const int C = cluster_ctas<T>(mp, g_panel_cluster);
+      if (C > 0 && ceil_div(mp, C) <= 2 * kRcThreads) {
+        const cudaError_t e = launch_getf2_panel_cluster_reg(
+            reinterpret_cast<float*>(A), lda, mp, w, ipiv, row_base, info_base, st, C, s.trace,
+            stream);
+        if (e != cudaErrorNotSupported) return e;
+      }
+    }
+    if (g_panel_regs == 1 && !nopiv) {
       // ~1024 rows per CTA (512 threads x 2 rows in registers)
       const int Rr = kRegThreads * kRegRows;
       int G = ceil_div(mp, Rr);

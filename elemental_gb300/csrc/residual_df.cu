@@ -68,23 +68,24 @@ __device__ __forceinline__ int exp2_of(double v) {
 }
 
 // (fl32(v), fl32(v - fl32(v))) for |v| in [2^-74, 2^127) by integer operations
-// on v's bits, bit-identical to the two cvt.rn.f32.f64 conversions (GB300
-// converts FP64 on its FP64 pipe, which would bind the split).  With
-// v = (-1)^s m 2^(E-1075), m the 53-bit significand: the high word keeps
-// m's top 24 bits rounded to nearest even (a carry out of them moves into
-// the exponent), and v - fl32(v) = (-1)^s d 2^(E-1075) exactly, with d the
-// signed remainder (|d| <= 2^28), so its FP32 rounding is that of the
-// integer d times a power of two.  Returns false outside the range (zero,
-// subnormal, huge, inf, NaN): the caller converts in FP64 there.
+// on v's two 32-bit halves, bit-identical to the two cvt.rn.f32.f64
+// conversions.  GB300 runs FP64 conversions -- and 64-bit integer shifts --
+// on its FP64 pipe, which bound the split at a third of HBM speed; on
+// 32-bit halves it streams at HBM speed.  With v = (-1)^s m 2^(E-1075), m the
+// 53-bit significand: the high word keeps m's top 24 bits rounded to
+// nearest even (a carry out of them moves into the exponent), and
+// v - fl32(v) = (-1)^s d 2^(E-1075) exactly, with d the signed remainder
+// (|d| <= 2^28), so its FP32 rounding is that of the integer d times a power
+// of two.  Returns false outside the range (zero, subnormal, huge, inf, NaN):
+// the caller converts in FP64 there.
 __device__ __forceinline__ bool split_bits(double v, float& hi, float& lo) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
-  const int E = (int)((b >> 52) & 0x7ff);
+  const unsigned bh = (unsigned)__double2hiint(v), bl = (unsigned)__double2loint(v);
+  const int E = (int)((bh >> 20) & 0x7ffu);
   if (E < 949 || E > 1149) return false;
-  const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-  const unsigned q = (unsigned)(m >> 29);
-  const unsigned rem = (unsigned)m & 0x1FFFFFFFu;
+  const unsigned q = (((bh & 0xFFFFFu) | 0x100000u) << 3) | (bl >> 29);  // top 24 bits of m
+  const unsigned rem = bl & 0x1FFFFFFFu;
   const unsigned inc = (rem > 0x10000000u || (rem == 0x10000000u && (q & 1u))) ? 1u : 0u;
-  const unsigned sgn = (unsigned)(b >> 63);
+  const unsigned sgn = bh >> 31;
   hi = __uint_as_float((sgn << 31) | (((unsigned)(E - 896) << 23) + (q + inc - 0x800000u)));
   const int d = (int)rem - (int)(inc << 29);
   lo = __fmul_rn(__int2float_rn(sgn ? -d : d), __uint_as_float((unsigned)(E - 948) << 23));
@@ -98,10 +99,8 @@ __device__ __forceinline__ bool split_bits(double v, float& hi, float& lo) {
 // max |a| of the entries it visited (fixed-order reductions).  The work is
 // cut into chunks of 1024 rows of one column, taken in column-major order
 // by a grid-stride loop, so the CTAs running at once stream one contiguous
-// stretch of A and of the outputs (CTAs walking whole columns of their own
-// start 2 MB apart at n = 32768, all on the same memory partition).  Four
-// rows per thread are in flight at once; the only FP64 arithmetic per entry
-// is the sum of squares.
+// stretch of A and of the outputs.  Four rows per thread are in flight at
+// once; the only FP64-pipe work per entry is the sum of squares.
 __global__ void __launch_bounds__(256)
 split_a_kernel(const double* __restrict__ A, long lda, int n, float* __restrict__ Af,
                float* __restrict__ Ahi, float* __restrict__ Alo, double* __restrict__ part) {

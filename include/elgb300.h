@@ -58,9 +58,12 @@ int ElGBSetBlocksize(int nb);
  *                       through distributed shared memory and the cluster
  *                       barrier; 1: always the cooperative kernel.
  *                       Process-wide (every context).
- *   ELGB_OPT_PANEL_REGS 1: FP32 panels keep their rows in registers (512
- *                       threads x 2 rows per CTA); 0 (default): in shared
- *                       memory.  Process-wide.
+ *   ELGB_OPT_PANEL_REGS FP32 leaf panels keep their rows in registers
+ *                       (512 threads x 2 rows per CTA): 2 (default) on a
+ *                       thread-block cluster where one holds the panel
+ *                       (<= 1024 rows per CTA, i.e. up to 16384 rows), in
+ *                       shared memory otherwise; 1 on a cooperative grid;
+ *                       0 always in shared memory.  Process-wide.
  *   ELGB_OPT_RESIDUAL_DF 1 (default): ElGBRefinedSolve_d computes its
  *                       residuals and GMRES products for n >= 2048 in
  *                       double-float arithmetic on the FP32 pipe

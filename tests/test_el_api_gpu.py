@@ -90,3 +90,16 @@ def test_linear_solve_mixed_on_library_host_memory():
     back = El.host_empty((n, n))
     torch.from_numpy(back).copy_(d)
     assert np.array_equal(back, A0)
+
+
+def test_host_memory_blocks_are_reusable():
+    """Blocks of ElGBHostAlloc memory allocated, written, used for device
+    copies and freed in turn (the mapping of a freed block may come back)."""
+    import torch
+
+    for k in range(4):
+        a = El.host_empty((1024, 1024 + 7 * k))
+        a[...] = k + 0.5
+        d = torch.from_numpy(a).cuda()
+        assert float(d.sum()) == (k + 0.5) * a.size
+        del a, d

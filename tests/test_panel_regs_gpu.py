@@ -1,0 +1,80 @@
+"""Leaf-panel kernels with the rows in registers (ELGB_OPT_PANEL_REGS = 2:
+one thread-block cluster, 512 threads x 2 rows per CTA) against the
+shared-memory cluster kernel: the same lu::Panel steps
+(src/lapack_like/factor/LU/Panel.hpp:15-59) in the same arithmetic order,
+so pivots and factors must agree bit for bit, including ties and singular
+columns; and P A = L U to FP32 accuracy."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _lu(ctx, A0, regs, nb=0, kind=2):
+    A = A0.clone()  # keeps the column-major strides
+    assert A.stride(0) == 1
+    ctx.set_option("panel_regs", regs)
+    try:
+        piv = ctx.lu_mixed(A, gemm_kind=kind, nb=nb)
+        ctx.check()
+    finally:
+        ctx.set_option("panel_regs", 2)
+    return A, piv
+
+
+def _matrix(m, n, seed):
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    return torch.randn(n, m, device="cuda", generator=g).t()  # column-major m x n
+
+
+@pytest.mark.parametrize("m,n", [(300, 300), (1000, 700), (2100, 2100), (5000, 1200),
+                                 (8192, 8192), (16384, 640)])
+def test_register_cluster_panels_match_shared_memory_panels(ctx, m, n):
+    A0 = _matrix(m, n, m + n)
+    A1, p1 = _lu(ctx, A0, 0)
+    A2, p2 = _lu(ctx, A0, 2)
+    assert torch.equal(p1, p2)
+    assert torch.equal(A1, A2)
+
+
+def test_register_cluster_panels_ties_and_zero_columns(ctx):
+    """Exact ties (integer entries) pick the lowest row; a zero column is
+    reported at its 1-based index and the factorization goes on."""
+    m = n = 1536
+    g = np.random.default_rng(3)
+    A = g.integers(-3, 4, (m, n)).astype(np.float32)
+    A[:, 77] = 0.0
+    A0 = torch.from_numpy(A.T.copy()).cuda().t()
+    outs = []
+    for regs in (0, 2):
+        Ac = A0.clone()
+        ctx.set_option("panel_regs", regs)
+        try:
+            piv = ctx.lu_mixed(Ac, gemm_kind=2)
+            info, err = ctx.status()
+        finally:
+            ctx.set_option("panel_regs", 2)
+        outs.append((Ac, piv, info, err))
+    assert outs[0][2] == outs[1][2] == 78 and outs[1][3] == 0
+    assert torch.equal(outs[0][1], outs[1][1])
+    assert torch.equal(outs[0][0], outs[1][0])
+
+
+def test_register_cluster_panels_backward_error(ctx):
+    """P A = L U to FP32 accuracy (exact-FP32 SIMT updates), checked in FP64
+    on the host, with the first pivots equal to the oracle's FP32 El::LU
+    (later ones may differ at near-ties that rounding breaks the other way)."""
+    n = 2048
+    A0 = _matrix(n, n, 11)
+    A, piv = _lu(ctx, A0, 2, nb=256, kind=-1)
+    Ah = A0.double().cpu().numpy()
+    LU = A.double().cpu().numpy()
+    L = np.tril(LU, -1) + np.eye(n)
+    U = np.triu(LU)
+    PA = O.permute_rows(piv.cpu().numpy(), Ah)
+    assert np.linalg.norm(PA - L @ U) / np.linalg.norm(Ah) <= 4e-5
+    _, pivr = O.lu(Ah.astype(np.float32), nb=256, dtype=np.float32)
+    assert np.array_equal(piv.cpu().numpy()[:8], pivr[:8])
