@@ -79,7 +79,8 @@ __device__ __forceinline__ int exp2_of(double v) {
 // of two.  Returns false outside the range (zero, subnormal, huge, inf, NaN):
 // the caller converts in FP64 there.
 __device__ __forceinline__ bool split_bits(double v, float& hi, float& lo) {
-  const unsigned bh = (unsigned)__double2hiint(v), bl = (unsigned)__double2loint(v);
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const unsigned bh = (unsigned)(b >> 32), bl = (unsigned)b;
   const int E = (int)((bh >> 20) & 0x7ffu);
   if (E < 949 || E > 1149) return false;
   const unsigned q = (((bh & 0xFFFFFu) | 0x100000u) << 3) | (bl >> 29);  // top 24 bits of m
@@ -107,19 +108,6 @@ split_a_kernel(const double* __restrict__ A, long lda, int n, float* __restrict_
   __shared__ double s_sq[256], s_mx[256];
   double sq = 0.0;
   unsigned long long mxb = 0ull;  // bits of max |a| (non-negative doubles order as integers)
-  auto one = [&](double v, long o) {
-    float h, l;
-    if (!split_bits(v, h, l)) {
-      h = (float)v;
-      l = (float)(v - (double)h);
-    }
-    if (Af) Af[o] = h;
-    Ahi[o] = h;
-    Alo[o] = l;
-    sq = fma(v, v, sq);
-    const unsigned long long ab = (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
-    if (ab <= 0x7FF0000000000000ull && ab > mxb) mxb = ab;  // NaN never counts
-  };
   const int rch = ceil_div(n, 1024);
   const long nchunks = (long)rch * n;
   for (long c = blockIdx.x; c < nchunks; c += gridDim.x) {
@@ -127,15 +115,30 @@ split_a_kernel(const double* __restrict__ A, long lda, int n, float* __restrict_
     const int i0 = (int)(c - (long)j * rch) * 1024;
     const double* a = A + (long)j * lda + i0;
     const long o = (long)j * n + i0;
-    const int i = threadIdx.x;
-    if (i0 + 1024 <= n) {
-      double v[4];
+    const int nr = min(1024, n - i0);
+    double v[4];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) v[u] = __ldcs(a + i + 256 * u);
+    for (int u = 0; u < 4; ++u) {
+      const int r = threadIdx.x + 256 * u;
+      v[u] = r < nr ? __ldcs(a + r) : 0.0;
+    }
 #pragma unroll
-      for (int u = 0; u < 4; ++u) one(v[u], o + i + 256 * u);
-    } else {
-      for (int r = i; i0 + r < n; r += 256) one(a[r], o + r);
+    for (int u = 0; u < 4; ++u) {
+      const int r = threadIdx.x + 256 * u;
+      if (r < nr) {
+        float h, l;
+        if (!split_bits(v[u], h, l)) {
+          h = (float)v[u];
+          l = (float)(v[u] - (double)h);
+        }
+        if (Af) Af[o + r] = h;
+        Ahi[o + r] = h;
+        Alo[o + r] = l;
+        sq = fma(v[u], v[u], sq);
+        const unsigned long long ab =
+            (unsigned long long)__double_as_longlong(v[u]) & 0x7FFFFFFFFFFFFFFFull;
+        if (ab <= 0x7FF0000000000000ull && ab > mxb) mxb = ab;  // NaN never counts
+      }
     }
   }
   s_sq[threadIdx.x] = sq;

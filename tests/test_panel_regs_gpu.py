@@ -1,6 +1,7 @@
 """Leaf-panel kernels with the rows in registers (ELGB_OPT_PANEL_REGS = 2:
-one thread-block cluster, 512 threads x 2 rows per CTA) against the
-shared-memory cluster kernel: the same lu::Panel steps
+one thread-block cluster, 512 threads x 2 rows per CTA, panels of up to
+16384 rows; taller ones keep the shared-memory kernels) against the
+shared-memory kernels: the same lu::Panel steps
 (src/lapack_like/factor/LU/Panel.hpp:15-59) in the same arithmetic order,
 so pivots and factors must agree bit for bit, including ties and singular
 columns; and P A = L U to FP32 accuracy."""
@@ -31,7 +32,7 @@ def _matrix(m, n, seed):
 
 
 @pytest.mark.parametrize("m,n", [(300, 300), (1000, 700), (2100, 2100), (5000, 1200),
-                                 (8192, 8192), (16384, 640)])
+                                 (8192, 8192), (16384, 640), (20000, 600), (32768, 544)])
 def test_register_cluster_panels_match_shared_memory_panels(ctx, m, n):
     A0 = _matrix(m, n, m + n)
     A1, p1 = _lu(ctx, A0, 0)
