@@ -561,14 +561,20 @@ struct ClusterSlot {
   T diag[kPanelW];
 };
 
+// The .aligned cluster barriers must be executed by every thread of a warp
+// together; the callers reach them right after thread-divergent stores, so
+// each first reconverges its warp explicitly.
 __device__ __forceinline__ void cluster_barrier() {
+  __syncwarp();
   asm volatile("barrier.cluster.arrive.release.aligned;\n"
                "barrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
 __device__ __forceinline__ void cluster_arrive() {
+  __syncwarp();
   asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
 }
 __device__ __forceinline__ void cluster_wait() {
+  __syncwarp();
   asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
 
@@ -1910,21 +1916,43 @@ trsm_block_kernel(const T* __restrict__ A, long lda, T* __restrict__ Bm, long ld
       }
     }
     __syncthreads();
-    for (int c = warp; c < cw; c += blockDim.x >> 5) {
-      T x[NT];
+    // warp w solves columns w, w + 8, w + 16, w + 24 of the chunk together:
+    // each column's operations and their order are those of a column solved
+    // alone, but the four dependency chains (shuffle, FMA) interleave
+    {
+      constexpr int kW = kTrsmThreads / 32;
+      constexpr int CPW = kTrsmCols / kW;
+      static_assert(CPW * kW == kTrsmCols, "columns per warp");
+      T x[CPW][NT];
+      bool on[CPW];
 #pragma unroll
-      for (int t = 0; t < NT; ++t) x[t] = sB[lane + 32 * t + c * LDS];
+      for (int q = 0; q < CPW; ++q) {
+        const int c = warp + kW * q;
+        on[q] = c < cw;
+#pragma unroll
+        for (int t = 0; t < NT; ++t) x[q][t] = on[q] ? sB[lane + 32 * t + c * LDS] : T(0);
+      }
       if (lower) {
 #pragma unroll
         for (int t = 0; t < NT; ++t) {
           for (int jj = 0; jj < 32; ++jj) {
             const int j = 32 * t + jj;
-            if (!unit && lane == jj) x[t] = x[t] / sA[j + j * NB];
-            const T xj = __shfl_sync(0xffffffffu, x[t], jj);
+            if (!unit && lane == jj) {
+              const T d = sA[j + j * NB];
+#pragma unroll
+              for (int q = 0; q < CPW; ++q) x[q][t] = x[q][t] / d;
+            }
+            T xj[CPW];
+#pragma unroll
+            for (int q = 0; q < CPW; ++q) xj[q] = __shfl_sync(0xffffffffu, x[q][t], jj);
 #pragma unroll
             for (int tt = t; tt < NT; ++tt) {
               const int i = lane + 32 * tt;
-              if (i > j) x[tt] = fma(-sA[i + j * NB], xj, x[tt]);
+              if (i > j) {
+                const T a = sA[i + j * NB];
+#pragma unroll
+                for (int q = 0; q < CPW; ++q) x[q][tt] = fma(-a, xj[q], x[q][tt]);
+              }
             }
           }
         }
@@ -1933,18 +1961,31 @@ trsm_block_kernel(const T* __restrict__ A, long lda, T* __restrict__ Bm, long ld
         for (int t = NT - 1; t >= 0; --t) {
           for (int jj = 31; jj >= 0; --jj) {
             const int j = 32 * t + jj;
-            if (!unit && lane == jj) x[t] = x[t] / sA[j + j * NB];
-            const T xj = __shfl_sync(0xffffffffu, x[t], jj);
+            if (!unit && lane == jj) {
+              const T d = sA[j + j * NB];
+#pragma unroll
+              for (int q = 0; q < CPW; ++q) x[q][t] = x[q][t] / d;
+            }
+            T xj[CPW];
+#pragma unroll
+            for (int q = 0; q < CPW; ++q) xj[q] = __shfl_sync(0xffffffffu, x[q][t], jj);
 #pragma unroll
             for (int tt = 0; tt <= t; ++tt) {
               const int i = lane + 32 * tt;
-              if (i < j) x[tt] = fma(-sA[i + j * NB], xj, x[tt]);
+              if (i < j) {
+                const T a = sA[i + j * NB];
+#pragma unroll
+                for (int q = 0; q < CPW; ++q) x[q][tt] = fma(-a, xj[q], x[q][tt]);
+              }
             }
           }
         }
       }
 #pragma unroll
-      for (int t = 0; t < NT; ++t) sB[lane + 32 * t + c * LDS] = x[t];
+      for (int q = 0; q < CPW; ++q)
+        if (on[q])
+#pragma unroll
+          for (int t = 0; t < NT; ++t) sB[lane + 32 * t + (warp + kW * q) * LDS] = x[q][t];
     }
     __syncthreads();
     if (!trans_b) {
