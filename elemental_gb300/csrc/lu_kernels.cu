@@ -8,6 +8,7 @@
 #include <algorithm>
 
 #include "kernels.h"
+#include "tcgen05.cuh"
 
 namespace elgb {
 
@@ -73,7 +74,7 @@ __device__ __forceinline__ void block_argmax_nolead(T& v, int& r, T* s_v, int* s
 // ---------------------------------------------------------------------------
 // One cooperative launch factors a w-column panel (w <= W = 32).  CTA b owns
 // panel rows [b*R, b*R + R) and keeps them in shared memory for the whole
-// panel (column-major slab, slab[c * R + r]).  Per column j:
+// panel (column-major slab, slab[c * S + r], S = slab_stride(R)).  Per column j:
 //   1. each CTA writes its slot: its best candidate (|a|, row) for column j
 //      with that row, and (the owner of row j only) row j itself, then
 //      publishes the slot with a release store of the column's epoch;
@@ -146,20 +147,80 @@ __device__ __forceinline__ bool wait_epoch(const int* flag, int epoch, DevStatus
   return ok;
 }
 
-// Copies the CTA's rows [rb, rb + nr) of the panel's w columns into the
-// shared slab (column c at slab + c R) by cp.async: every element's copy is
-// in flight at once instead of a load round trip per few elements.  The
-// caller's barrier publishes the slab to the other threads.
+// Shared-memory slab of a CTA's panel rows: column c of local row r at
+// slab[c * S + r], S = slab_stride(R) (R rounded up so that every column
+// can start on the 16-byte phase of its rows in global memory), and slab =
+// the 16-byte aligned shared base + mis, mis being the CTA's first row's
+// offset from a 16-byte boundary in elements.  The slab takes
+// slab_elems(R) elements from that base.
 template <typename T>
-__device__ __forceinline__ void panel_load_slab(T* slab, const T* A, long lda, int rb, int nr,
-                                                int R, int w) {
-  for (int c = 0; c < w; ++c)
-    for (int r = threadIdx.x; r < nr; r += blockDim.x)
-      asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(
-                       (unsigned)__cvta_generic_to_shared(slab + c * R + r)),
-                   "l"(A + (long)(rb + r) + (long)c * lda), "n"((int)sizeof(T))
-                   : "memory");
-  asm volatile("cp.async.wait_all;" ::: "memory");
+__host__ __device__ constexpr int slab_stride(int R) {
+  return (R + 2 * (16 / (int)sizeof(T)) - 2) / (16 / (int)sizeof(T)) * (16 / (int)sizeof(T));
+}
+template <typename T>
+__host__ __device__ constexpr size_t slab_elems(int R) {
+  return (size_t)slab_stride<T>(R) * kPanelW + 16 / sizeof(T);
+}
+
+// Stages the CTA's rows [rb, rb + nr) of the panel's w columns in the slab
+// with the TMA engine: per column one bulk copy (cp.async.bulk) of the
+// 16-byte aligned middle of its rows, completing on an mbarrier, and the
+// at most 2 x (16 / sizeof(T) - 1) rows at either end by plain loads.  When
+// a column's stride is not a multiple of 16 bytes, every entry goes by
+// cp.async instead.  Returns the slab (shared base + mis).  A bounded wait:
+// a timeout records an error and the kernel carries on (it must still meet
+// every barrier of the other CTAs); the host then reports the failure.
+template <typename T>
+__device__ __forceinline__ T* panel_load_slab(unsigned char* smem, const T* A, long lda, int rb,
+                                              int nr, int R, int w, uint64_t* mbar,
+                                              DevStatus* st) {
+  constexpr int E = 16 / (int)sizeof(T);
+  const int S = slab_stride<T>(R);
+  const T* src0 = A + rb;
+  const int mis = (int)(((uintptr_t)src0 & 15u) / sizeof(T));
+  T* slab = reinterpret_cast<T*>(smem) + mis;
+  if (((size_t)lda * sizeof(T)) % 16 != 0) {
+    for (int c = 0; c < w; ++c)
+      for (int r = threadIdx.x; r < nr; r += blockDim.x)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(
+                         (unsigned)__cvta_generic_to_shared(slab + c * S + r)),
+                     "l"(src0 + (long)r + (long)c * lda), "n"((int)sizeof(T))
+                     : "memory");
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    return slab;
+  }
+  const int h = (E - mis) % E;                      // rows before the first aligned one
+  const int mid = nr > h ? (nr - h) / E * E : 0;    // rows in whole 16-byte units
+  const uint32_t bytes = (uint32_t)(mid * sizeof(T));
+  if (mid > 0) {
+    if (threadIdx.x == 0) {
+      tc::mbar_init(mbar, 1);
+      tc::fence_mbar_init();
+      tc::mbar_arrive_expect_tx(mbar, bytes * (uint32_t)w);
+    }
+    __syncthreads();
+    if (threadIdx.x < w) {
+      const int c = threadIdx.x;
+      asm volatile(
+          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, "
+          "[%3];" ::"r"((unsigned)__cvta_generic_to_shared(slab + c * S + h)),
+          "l"(src0 + h + (long)c * lda), "r"(bytes), "r"(tc::smem_u32(mbar))
+          : "memory");
+    }
+  }
+  // the ends of each column
+  const int tail0 = h + mid, ntail = nr - tail0;
+  for (int idx = threadIdx.x; idx < w * E * 2; idx += blockDim.x) {
+    const int c = idx / (2 * E), k = idx % (2 * E);
+    const int r = k < E ? k : tail0 + (k - E);
+    const bool in = k < E ? (r < min(h, nr)) : (k - E < ntail);
+    if (in) slab[c * S + r] = src0[(long)r + (long)c * lda];
+  }
+  if (mid > 0 && !tc::mbar_wait(mbar, 0, st, 40)) {
+    // the copies may still land: wait for them once more before going on
+    tc::mbar_wait(mbar, 0, st, 41);
+  }
+  return slab;
 }
 
 // Step j of lu::Panel in two halves, so that the exchange of column j+1's
@@ -173,22 +234,22 @@ __device__ __forceinline__ void panel_load_slab(T* slab, const T* A, long lda, i
 // whole step leaves them: every entry sees the same fma with the same
 // operands as in one pass, so results are bit-identical.
 template <typename T>
-__device__ __forceinline__ void panel_step_front(T* slab, int R, int nr, int r0, int j, int w,
+__device__ __forceinline__ void panel_step_front(T* slab, int S, int nr, int r0, int j, int w,
                                                  int pl, const T* s_d, const T* urow,
                                                  bool singular, T inv, int rb, T& bv,
                                                  int& br) {
   for (int r = r0 + threadIdx.x; r < nr; r += blockDim.x) {
     const bool pr = r == pl;
-    T l = pr ? s_d[j] : slab[j * R + r];
+    T l = pr ? s_d[j] : slab[j * S + r];
     if (!singular) l *= inv;
-    slab[j * R + r] = l;
+    slab[j * S + r] = l;
     if (pr) {
-      for (int c = j + 1; c < w; ++c) slab[c * R + r] = fma(-l, urow[c], s_d[c]);
+      for (int c = j + 1; c < w; ++c) slab[c * S + r] = fma(-l, urow[c], s_d[c]);
     } else if (j + 1 < w) {
-      slab[(j + 1) * R + r] = fma(-l, urow[j + 1], slab[(j + 1) * R + r]);
+      slab[(j + 1) * S + r] = fma(-l, urow[j + 1], slab[(j + 1) * S + r]);
     }
     if (j + 1 < w) {
-      const T v = absv(slab[(j + 1) * R + r]);
+      const T v = absv(slab[(j + 1) * S + r]);
       if (argmax_better(v, rb + r, bv, br)) {
         bv = v;
         br = rb + r;
@@ -198,35 +259,35 @@ __device__ __forceinline__ void panel_step_front(T* slab, int R, int nr, int r0,
 }
 
 template <typename T>
-__device__ __forceinline__ void panel_step_back(T* slab, int R, int nr, int r0, int j, int w,
+__device__ __forceinline__ void panel_step_back(T* slab, int S, int nr, int r0, int j, int w,
                                                 int pl, const T* urow) {
   if (j + 2 >= w) return;
   for (int r = r0 + threadIdx.x; r < nr; r += blockDim.x) {
     if (r == pl) continue;
-    const T l = slab[j * R + r];
+    const T l = slab[j * S + r];
     T* row = slab + r;
     int c = j + 2;
     for (; c + 7 < w; c += 8) {  // eight loads in flight, then eight fmas / stores
       T v[8];
 #pragma unroll
-      for (int e = 0; e < 8; ++e) v[e] = row[(c + e) * R];
+      for (int e = 0; e < 8; ++e) v[e] = row[(c + e) * S];
 #pragma unroll
       for (int e = 0; e < 8; ++e) v[e] = fma(-l, urow[c + e], v[e]);
 #pragma unroll
-      for (int e = 0; e < 8; ++e) row[(c + e) * R] = v[e];
+      for (int e = 0; e < 8; ++e) row[(c + e) * S] = v[e];
     }
     for (; c + 3 < w; c += 4) {
-      T v0 = row[c * R], v1 = row[(c + 1) * R], v2 = row[(c + 2) * R], v3 = row[(c + 3) * R];
+      T v0 = row[c * S], v1 = row[(c + 1) * S], v2 = row[(c + 2) * S], v3 = row[(c + 3) * S];
       v0 = fma(-l, urow[c], v0);
       v1 = fma(-l, urow[c + 1], v1);
       v2 = fma(-l, urow[c + 2], v2);
       v3 = fma(-l, urow[c + 3], v3);
-      row[c * R] = v0;
-      row[(c + 1) * R] = v1;
-      row[(c + 2) * R] = v2;
-      row[(c + 3) * R] = v3;
+      row[c * S] = v0;
+      row[(c + 1) * S] = v1;
+      row[(c + 2) * S] = v2;
+      row[(c + 3) * S] = v3;
     }
-    for (; c < w; ++c) row[c * R] = fma(-l, urow[c], row[c * R]);
+    for (; c < w; ++c) row[c * S] = fma(-l, urow[c], row[c * S]);
   }
 }
 
@@ -234,10 +295,10 @@ __device__ __forceinline__ void panel_step_back(T* slab, int R, int nr, int r0, 
 // panel_step_back(pj) has run (pj < 0: no step pending).  Only rows the step
 // updates (global row > pj) are asked for.
 template <typename T>
-__device__ __forceinline__ T pending_value(const T* slab, int R, int r, int c, int pj, int plp,
+__device__ __forceinline__ T pending_value(const T* slab, int S, int r, int c, int pj, int plp,
                                            const T* urowp) {
-  T v = slab[c * R + r];
-  if (pj >= 0 && c >= pj + 2 && r != plp) v = fma(-slab[pj * R + r], urowp[c], v);
+  T v = slab[c * S + r];
+  if (pj >= 0 && c >= pj + 2 && r != plp) v = fma(-slab[pj * S + r], urowp[c], v);
   return v;
 }
 
@@ -245,23 +306,24 @@ template <typename T, int W>
 __global__ void __launch_bounds__(panel_threads<T>())
 getf2_panel_kernel(PanelParams<T> p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* slab = reinterpret_cast<T*>(smem_raw);
+  __shared__ __align__(8) uint64_t s_mbar;
   __shared__ T s_d[W];
   __shared__ T s_rv[33];
   __shared__ int s_rr[33];
   __shared__ T s_gv[panel_threads<T>()];
   __shared__ int s_gr[panel_threads<T>()];
-  T* s_rows = slab + (size_t)p.R * W;  // [G][W] candidate rows (dynamic smem)
+  T* s_rows = reinterpret_cast<T*>(smem_raw) + slab_elems<T>(p.R);  // [G][W] candidate rows
   __shared__ int s_abort;
 
   const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x;
   const int lane = tid & 31;
   const int R = p.R, w = p.w, maxG = p.s.maxG;
+  const int S = slab_stride<T>(R);
   const int rb = b * R;
   const int re = min(rb + R, p.mp);
   const int nr = max(re - rb, 0);
 
-  panel_load_slab(slab, p.A, p.lda, rb, nr, R, w);
+  T* slab = panel_load_slab(smem_raw, p.A, p.lda, rb, nr, R, w, &s_mbar, p.st);
   if (tid == 0) s_abort = 0;
   __syncthreads();
 
@@ -292,9 +354,9 @@ getf2_panel_kernel(PanelParams<T> p) {
     // 1. publish (the release store orders the CTA's slot writes, which
     // the barrier makes visible to the publishing thread); the rows carry
     // the pending step's update
-    if (br >= 0 && tid < w) my->cand[tid] = pending_value(slab, R, br - rb, tid, pj, plp, urowp);
+    if (br >= 0 && tid < w) my->cand[tid] = pending_value(slab, S, br - rb, tid, pj, plp, urowp);
     if (j >= rb && j < re && tid < w)
-      my->diag[tid] = pending_value(slab, R, j - rb, tid, pj, plp, urowp);
+      my->diag[tid] = pending_value(slab, S, j - rb, tid, pj, plp, urowp);
     if (tid == 0) {
       my->val = bv;
       my->row = br;
@@ -302,7 +364,7 @@ getf2_panel_kernel(PanelParams<T> p) {
     __syncthreads();
     if (tid == 0) st_release_s32(&my->epoch, epoch);
     // the rest of the previous step's update while the other CTAs publish
-    if (pj >= 0) panel_step_back<T>(slab, R, nr, r0p, pj, w, plp, urowp);
+    if (pj >= 0) panel_step_back<T>(slab, S, nr, r0p, pj, w, plp, urowp);
     __syncthreads();  // urowp (s_rows / s_d) is read before the exchange refills them
     if (tr) tr[1] = globaltimer_ns();
     // 2. the barrier: every slot carries this epoch.  The thread that polled
@@ -354,15 +416,15 @@ getf2_panel_kernel(PanelParams<T> p) {
     const T inv = singular ? T(1) : T(1) / alpha;
     // 4. row j takes the pivot row (row j is not updated below); the pivot
     // row's position takes old row j, updated from s_d
-    if (piv != j && tid < w && j >= rb && j < re) slab[tid * R + (j - rb)] = urow[tid];
+    if (piv != j && tid < w && j >= rb && j < re) slab[tid * S + (j - rb)] = urow[tid];
     bv = T(-1);
     br = -1;
     const int r0 = max(j + 1 - rb, 0);
     const int pl = (piv != j && piv >= rb && piv < re) ? piv - rb : -1;
     // the pivot row's position: old row j's multipliers of the earlier
     // columns move with it (columns j.. come from the update below)
-    if (pl >= 0 && tid < j) slab[tid * R + pl] = s_d[tid];
-    panel_step_front<T>(slab, R, nr, r0, j, w, pl, s_d, urow, singular, inv, rb, bv, br);
+    if (pl >= 0 && tid < j) slab[tid * S + pl] = s_d[tid];
+    panel_step_front<T>(slab, S, nr, r0, j, w, pl, s_d, urow, singular, inv, rb, bv, br);
     block_argmax_nolead(bv, br, s_rv, s_rr);
     if (tr) tr[3] = globaltimer_ns();
     pj = j;
@@ -373,7 +435,7 @@ getf2_panel_kernel(PanelParams<T> p) {
   __syncthreads();
   for (int c = 0; c < w; ++c)
     for (int r = tid; r < nr; r += blockDim.x)
-      p.A[(long)(rb + r) + (long)c * p.lda] = slab[c * R + r];
+      p.A[(long)(rb + r) + (long)c * p.lda] = slab[c * S + r];
 }
 
 // ---------------------------------------------------------------------------
@@ -604,23 +666,24 @@ template <typename T, int W>
 __global__ void __launch_bounds__(panel_threads<T>())
 getf2_panel_cluster_kernel(PanelParams<T> p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* slab = reinterpret_cast<T*>(smem_raw);
+  __shared__ __align__(8) uint64_t s_mbar;
   __shared__ ClusterSlot<T> slots[2];
   __shared__ T s_d[W];
   __shared__ T s_rv[33];
   __shared__ int s_rr[33];
   __shared__ T s_gv[32];
   __shared__ int s_gr[32];
-  T* s_rows = slab + (size_t)p.R * W;  // [C][W] candidate rows
+  T* s_rows = reinterpret_cast<T*>(smem_raw) + slab_elems<T>(p.R);  // [C][W] candidate rows
 
   const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x;
   const int lane = tid & 31;
   const int R = p.R, w = p.w;
+  const int S = slab_stride<T>(R);
   const int rb = b * R;
   const int re = min(rb + R, p.mp);
   const int nr = max(re - rb, 0);
 
-  panel_load_slab(slab, p.A, p.lda, rb, nr, R, w);
+  T* slab = panel_load_slab(smem_raw, p.A, p.lda, rb, nr, R, w, &s_mbar, p.st);
   __syncthreads();
 
   T bv = T(-1);
@@ -642,16 +705,16 @@ getf2_panel_cluster_kernel(PanelParams<T> p) {
     unsigned long long* tr = (p.s.trace && b == 0 && tid == 0) ? p.s.trace + 4 * (long)j : nullptr;
     if (tr) tr[0] = globaltimer_ns();
     // 1. publish in this CTA's shared memory (rows with the pending update)
-    if (br >= 0 && tid < w) my->cand[tid] = pending_value(slab, R, br - rb, tid, pj, plp, urowp);
+    if (br >= 0 && tid < w) my->cand[tid] = pending_value(slab, S, br - rb, tid, pj, plp, urowp);
     if (j >= rb && j < re && tid < w)
-      my->diag[tid] = pending_value(slab, R, j - rb, tid, pj, plp, urowp);
+      my->diag[tid] = pending_value(slab, S, j - rb, tid, pj, plp, urowp);
     if (tid == 0) {
       my->val = bv;
       my->row = br;
     }
     cluster_arrive();
     // the rest of the previous step's update while the cluster gathers
-    if (pj >= 0) panel_step_back<T>(slab, R, nr, r0p, pj, w, plp, urowp);
+    if (pj >= 0) panel_step_back<T>(slab, S, nr, r0p, pj, w, plp, urowp);
     __syncthreads();  // urowp (s_rows / s_d) is read before the exchange refills them
     if (tr) tr[1] = globaltimer_ns();
     cluster_wait();
@@ -701,13 +764,13 @@ getf2_panel_cluster_kernel(PanelParams<T> p) {
     if (singular && b == 0 && tid == 0) atomicCAS(&p.st->info, 0, p.info_base + j + 1);
     const T inv = singular ? T(1) : T(1) / alpha;
     // 4. swap, the front of the update, next candidate (as getf2_panel_kernel)
-    if (piv != j && tid < w && j >= rb && j < re) slab[tid * R + (j - rb)] = urow[tid];
+    if (piv != j && tid < w && j >= rb && j < re) slab[tid * S + (j - rb)] = urow[tid];
     bv = T(-1);
     br = -1;
     const int r0 = max(j + 1 - rb, 0);
     const int pl = (piv != j && piv >= rb && piv < re) ? piv - rb : -1;
-    if (pl >= 0 && tid < j) slab[tid * R + pl] = s_d[tid];
-    panel_step_front<T>(slab, R, nr, r0, j, w, pl, s_d, urow, singular, inv, rb, bv, br);
+    if (pl >= 0 && tid < j) slab[tid * S + pl] = s_d[tid];
+    panel_step_front<T>(slab, S, nr, r0, j, w, pl, s_d, urow, singular, inv, rb, bv, br);
     block_argmax_nolead(bv, br, s_rv, s_rr);
     if (tr) tr[3] = globaltimer_ns();
     pj = j;
@@ -718,7 +781,7 @@ getf2_panel_cluster_kernel(PanelParams<T> p) {
   __syncthreads();
   for (int c = 0; c < w; ++c)
     for (int r = tid; r < nr; r += blockDim.x)
-      p.A[(long)(rb + r) + (long)c * p.lda] = slab[c * R + r];
+      p.A[(long)(rb + r) + (long)c * p.lda] = slab[c * S + r];
   cluster_barrier();  // no CTA leaves while another may still read its slots
 }
 
@@ -917,7 +980,8 @@ getf2_panel_cluster_reg_kernel(PanelParams<float> p) {
 template <typename T>
 static int cluster_ctas(int mp, int max_cluster) {
   constexpr int kMaxSmem = 200 * 1024;
-  const int rows_cap = (int)(kMaxSmem / (kPanelW * sizeof(T))) - 32;
+  // the slab's row padding (slab_elems) comes out of the cap
+  const int rows_cap = (int)(kMaxSmem / (kPanelW * sizeof(T))) - 32 - 16;
   if (mp < 128) return 0;
   int C = 2;
   while (C < max_cluster && (mp + C - 1) / C > g_panel_rows) C *= 2;
@@ -931,7 +995,7 @@ static cudaError_t launch_getf2_panel_cluster(T* A, long lda, int mp, int w, int
                                               int C, unsigned long long* trace,
                                               cudaStream_t stream) {
   const int R = ceil_div(mp, C);
-  const size_t smem = ((size_t)R + C) * kPanelW * sizeof(T);
+  const size_t smem = (slab_elems<T>(R) + (size_t)C * kPanelW) * sizeof(T);
   auto kern = getf2_panel_cluster_kernel<T, kPanelW>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);
@@ -1045,7 +1109,7 @@ cudaError_t launch_getf2_panel(T* A, long lda, int mp, int w, int* ipiv, int row
   // About g_panel_rows rows per CTA: fewer CTAs make the per-column
   // exchange cheap (every CTA copies every candidate row), more make the
   // local update short; shared memory sets the fewest.
-  const int rows_cap = (int)(kMaxSmem / (kPanelW * sizeof(T))) - 64;
+  const int rows_cap = (int)(kMaxSmem / (kPanelW * sizeof(T))) - 64 - 16;
   int G = std::max(ceil_div(mp, g_panel_rows), ceil_div(mp, rows_cap));
   if (G > num_sms) G = num_sms;
   if (G > s.maxG) G = s.maxG;
@@ -1053,7 +1117,7 @@ cudaError_t launch_getf2_panel(T* A, long lda, int mp, int w, int* ipiv, int row
   if (G < 1) G = 1;
   int R = ceil_div(mp, G);
   G = ceil_div(mp, R);  // no CTA without rows
-  size_t smem = ((size_t)R + G) * kPanelW * sizeof(T);  // slab + candidate rows
+  size_t smem = (slab_elems<T>(R) + (size_t)G * kPanelW) * sizeof(T);  // slab + candidate rows
   if (smem > (size_t)kMaxSmem) return cudaErrorInvalidValue;
   auto kern = getf2_panel_kernel<T, kPanelW>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
