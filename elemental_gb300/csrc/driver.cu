@@ -278,16 +278,20 @@ static cudaError_t apply_swaps(LuState<T>& s, const LuLane& L, int c0, int w, in
   return cudaSuccess;
 }
 
-// Recursive panel factorization of columns [c0, c0 + w), rows [c0, m):
-// left half, its swaps / TRSM / GEMM onto the right half, right half, then
-// the right half's swaps back onto the left half.  Leaves of <= 32 columns
-// go to the cooperative getf2 kernel.
+// Recursive panel factorization of columns [c0, c0 + w), rows [c0, m), of
+// the block panel [b0, b1): left half, TRSM / GEMM onto the right half,
+// right half.  Leaves of <= 32 columns go to the getf2 kernels, and each
+// leaf's row interchanges go at once onto every other column of the block
+// (by the leaf kernel itself where it can, else one swap launch): the same
+// row moves, in the same order per column, as swapping each half's
+// interchanges onto its sibling after it -- no operation reads those
+// columns in between -- with one launch per leaf instead of two per node.
 template <typename T>
-static cudaError_t panel_rec(LuState<T>& s, const LuLane& L, int c0, int w) {
+static cudaError_t panel_rec(LuState<T>& s, const LuLane& L, int c0, int w, int b0, int b1) {
   Context* ctx = s.ctx;
   if (w <= 32) {
     const int pi = ctx->prof_begin(L.st);
-    bool done = false;
+    bool done = false, swapped = false;
     if constexpr (sizeof(T) == 4) {
       if (s.tournament && !s.nopiv) {
         int nl = 0;
@@ -304,19 +308,22 @@ static cudaError_t panel_rec(LuState<T>& s, const LuLane& L, int c0, int w) {
       ps.trace = (s.trace && c0 + w <= s.trace_cols) ? s.trace + 4 * (long)c0 : nullptr;
       LANE_CHECK(launch_getf2_panel<T>(s.A + c0 + (long)c0 * s.lda, s.lda, s.m - c0, w,
                                        s.ipiv + c0, c0, c0, s.panel_epoch, ps, ctx->status,
-                                       s.panel_ctas, L.st, s.nopiv), 1);
+                                       s.panel_ctas, L.st, s.nopiv, b0 - c0, b1 - c0,
+                                       &swapped), 1);
       s.panel_epoch += w;
     }
     ctx->prof_end(pi, L.st, ELGB_PROF_PANEL, (double)(s.m - c0) * w * w,
                   2.0 * sizeof(T) * (s.m - c0) * (double)w);
+    if (!swapped && (b0 < c0 || c0 + w < b1)) {
+      cudaError_t e = apply_swaps(s, L, c0, w, b0, c0, c0 + w, b1, false);
+      if (e != cudaSuccess) return e;
+    }
     return cudaSuccess;
   }
   int w1 = (w / 2 + 31) / 32 * 32;
   if (w1 >= w) w1 = w - 32;
   const int w2 = w - w1;
-  cudaError_t e = panel_rec(s, L, c0, w1);
-  if (e != cudaSuccess) return e;
-  e = apply_swaps(s, L, c0, w1, c0 + w1, c0 + w, 0, 0, false);
+  cudaError_t e = panel_rec(s, L, c0, w1, b0, b1);
   if (e != cudaSuccess) return e;
   T* A11 = s.A + c0 + (long)c0 * s.lda;
   T* A12 = s.A + c0 + (long)(c0 + w1) * s.lda;
@@ -326,9 +333,7 @@ static cudaError_t panel_rec(LuState<T>& s, const LuLane& L, int c0, int w) {
   if (e != cudaSuccess) return e;
   e = gemm_sub(ctx, L, s.m - c0 - w1, w2, w1, A21, s.lda, A12, s.lda, A22, s.lda);
   if (e != cudaSuccess) return e;
-  e = panel_rec(s, L, c0 + w1, w2);
-  if (e != cudaSuccess) return e;
-  return apply_swaps(s, L, c0 + w1, w2, c0, c0 + w1, 0, 0, false);
+  return panel_rec(s, L, c0 + w1, w2, b0, b1);
 }
 
 // Trailing update of block k (columns [c_begin, c_end) of the right part):
@@ -378,7 +383,7 @@ static cudaError_t getrf_run(LuState<T>& s, int nb) {
   const bool la = s.side.st != nullptr;
   cudaError_t e = cudaSuccess;
   if (minDim == 0) return e;
-  e = panel_rec(s, s.main, 0, std::min(nb, minDim));
+  e = panel_rec(s, s.main, 0, std::min(nb, minDim), 0, std::min(nb, minDim));
   if (e != cudaSuccess) return e;
   for (int k = 0; k < minDim; k += nb) {
     const int jb = std::min(nb, minDim - k);
@@ -398,7 +403,7 @@ static cudaError_t getrf_run(LuState<T>& s, int nb) {
       if (la) {
         e = cudaEventRecord(ctx->ev_fork, s.main.st);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(s.side.st, ctx->ev_fork, 0);
-        if (e == cudaSuccess) e = panel_rec(s, s.side, kn, jb2);
+        if (e == cudaSuccess) e = panel_rec(s, s.side, kn, jb2, kn, kn + jb2);
         if (e == cudaSuccess) e = cudaEventRecord(ctx->ev_join, s.side.st);
         if (e != cudaSuccess) return e;
       }
@@ -417,7 +422,7 @@ static cudaError_t getrf_run(LuState<T>& s, int nb) {
       if (la)
         e = cudaStreamWaitEvent(s.main.st, ctx->ev_join, 0);
       else
-        e = panel_rec(s, s.main, kn, jb2);
+        e = panel_rec(s, s.main, kn, jb2, kn, kn + jb2);
       if (e != cudaSuccess) return e;
     }
   }

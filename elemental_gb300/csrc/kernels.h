@@ -62,11 +62,16 @@ extern int g_panel_regs;
 // epoch_base: columns published so far in this factorization (the slot
 // epochs must keep growing across launches).  nopiv: no pivot search, the
 // pivot of column c is row c (El::LU(A), ipiv[c] = row_base + c).
+// swap_lo <= 0 <= w <= swap_hi: the leaf's row interchanges are also due on
+// the columns [swap_lo, 0) and [w, swap_hi) of A (relative to the leaf's
+// first column); a kernel that applies them itself sets *swaps_done, and the
+// caller applies them otherwise.
 template <typename T>
 cudaError_t launch_getf2_panel(T* A, long lda, int mp, int w, int* ipiv,
                                int row_base, int info_base, int epoch_base,
                                const PanelScratch<T>& s, DevStatus* st,
-                               int num_sms, cudaStream_t stream, bool nopiv = false);
+                               int num_sms, cudaStream_t stream, bool nopiv = false,
+                               int swap_lo = 0, int swap_hi = 0, bool* swaps_done = nullptr);
 
 // El::LU(A, P, Q) with full pivoting (src/lapack_like/factor/LU/Full.hpp):
 // unblocked, two kernels per step.  fs / part: device scratch (one state,

@@ -103,6 +103,9 @@ struct PanelParams {
   PanelScratch<T> s;
   DevStatus* st;
   int nopiv;       // 1: El::LU without pivoting -- the pivot of column j is row j
+  // the leaf's interchanges also applied to columns [swap_lo, 0) and
+  // [w, swap_hi) (relative to A) by the kernels that do so (0, 0: none)
+  int swap_lo, swap_hi;
 };
 
 constexpr int kPanelW = 32;
@@ -829,6 +832,9 @@ getf2_panel_cluster_reg_kernel(PanelParams<float> p) {
   __shared__ int s_gr[32];
   __shared__ float s_rv[33];
   __shared__ int s_rr[33];
+  __shared__ int s_piv[W];                     // the pivot of each column (panel row)
+  __shared__ int s_dst[2 * W], s_src[2 * W];   // the interchanges' net row moves
+  __shared__ int s_nmove;
 
   const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x;
   const int lane = tid & 31;
@@ -925,6 +931,7 @@ getf2_panel_cluster_reg_kernel(PanelParams<float> p) {
       }
       const float* urow = (piv == j) ? s_d : s_rows[piv / R];
       if (b == 0 && tid == 0) p.ipiv[j] = p.row_base + piv;
+      if (tid == 0) s_piv[j] = piv;
       const float alpha = urow[j];
       const bool singular = (alpha == 0.f);
       if (singular && b == 0 && tid == 0) atomicCAS(&p.st->info, 0, p.info_base + j + 1);
@@ -970,6 +977,56 @@ getf2_panel_cluster_reg_kernel(PanelParams<float> p) {
 #pragma unroll
       for (int c = 0; c < W; ++c)
         if (c < w) p.A[(long)grow[i] + (long)c * p.lda] = a[i][c];
+  // The leaf's interchanges (rows j and s_piv[j], j = 0 .. w-1, in order) on
+  // the other columns of its block: their net row moves (at most 2w rows),
+  // then one warp per column reads every moved row before writing any.
+  const int nleft = -p.swap_lo, nright = max(p.swap_hi - w, 0);
+  if (nleft + nright > 0) {
+    if (tid == 0) {
+      int* key = s_dst;  // row
+      int* val = s_src;  // the row whose value ends up there
+      int nk = w;
+      for (int r = 0; r < w; ++r) key[r] = val[r] = r;
+      for (int j = 0; j < w; ++j) {
+        const int pv = s_piv[j];
+        if (pv == j) continue;
+        int ip = -1;
+        if (pv < w) {
+          ip = pv;
+        } else {
+          for (int k = w; k < nk; ++k)
+            if (key[k] == pv) ip = k;
+          if (ip < 0) {
+            ip = nk++;
+            key[ip] = val[ip] = pv;
+          }
+        }
+        const int t = val[j];
+        val[j] = val[ip];
+        val[ip] = t;
+      }
+      int m = 0;  // keep the rows that move, in place
+      for (int k = 0; k < nk; ++k)
+        if (key[k] != val[k]) {
+          key[m] = key[k];
+          val[m] = val[k];
+          ++m;
+        }
+      s_nmove = m;
+    }
+    __syncthreads();
+    const int nmove = s_nmove;
+    const int nw = kRcThreads / 32, warp = tid >> 5;
+    for (int q = b * nw + warp; q < nleft + nright; q += G * nw) {
+      const int c = q < nleft ? p.swap_lo + q : w + (q - nleft);
+      float* col = p.A + (long)c * p.lda;
+      const float v0 = lane < nmove ? col[s_src[lane]] : 0.f;
+      const float v1 = lane + 32 < nmove ? col[s_src[lane + 32]] : 0.f;
+      __syncwarp();
+      if (lane < nmove) col[s_dst[lane]] = v0;
+      if (lane + 32 < nmove) col[s_dst[lane + 32]] = v1;
+    }
+  }
   cluster_barrier();  // no CTA leaves while another may still read its slots
 }
 
@@ -1032,7 +1089,7 @@ static cudaError_t launch_getf2_panel_cluster(T* A, long lda, int mp, int w, int
 static cudaError_t launch_getf2_panel_cluster_reg(float* A, long lda, int mp, int w, int* ipiv,
                                                   int row_base, int info_base, DevStatus* st,
                                                   int C, unsigned long long* trace,
-                                                  cudaStream_t stream) {
+                                                  cudaStream_t stream, int swap_lo, int swap_hi) {
   const int R = ceil_div(mp, C);
   if (R > 2 * kRcThreads) return cudaErrorNotSupported;
   auto kern = getf2_panel_cluster_reg_kernel<kPanelW>;
@@ -1059,14 +1116,17 @@ static cudaError_t launch_getf2_panel_cluster_reg(float* A, long lda, int mp, in
   }
   PanelScratch<float> ps{};
   ps.trace = trace;
-  PanelParams<float> prm{A, lda, mp, w, R, ipiv, row_base, info_base, 0, ps, st};
+  PanelParams<float> prm{A, lda, mp, w, R, ipiv, row_base, info_base, 0, ps, st, 0,
+                         swap_lo, swap_hi};
   return cudaLaunchKernelEx(&cfg, kern, prm);
 }
 
 template <typename T>
 cudaError_t launch_getf2_panel(T* A, long lda, int mp, int w, int* ipiv, int row_base,
                                int info_base, int epoch_base, const PanelScratch<T>& s,
-                               DevStatus* st, int num_sms, cudaStream_t stream, bool nopiv) {
+                               DevStatus* st, int num_sms, cudaStream_t stream, bool nopiv,
+                               int swap_lo, int swap_hi, bool* swaps_done) {
+  if (swaps_done) *swaps_done = false;
   if (w <= 0 || mp <= 0) return cudaSuccess;
   if (w > kPanelW || mp < w) return cudaErrorInvalidValue;
   if constexpr (sizeof(T) == 4) {
@@ -1074,9 +1134,11 @@ cudaError_t launch_getf2_panel(T* A, long lda, int mp, int w, int* ipiv, int row
       // rows in registers on a cluster where one fits (<= 1024 rows per CTA)
       const int C = cluster_ctas<T>(mp, g_panel_cluster);
       if (C > 0 && ceil_div(mp, C) <= 2 * kRcThreads) {
+        const bool fuse = swaps_done != nullptr && (swap_lo < 0 || swap_hi > w);
         const cudaError_t e = launch_getf2_panel_cluster_reg(
             reinterpret_cast<float*>(A), lda, mp, w, ipiv, row_base, info_base, st, C, s.trace,
-            stream);
+            stream, fuse ? swap_lo : 0, fuse ? swap_hi : 0);
+        if (e == cudaSuccess && fuse) *swaps_done = true;
         if (e != cudaErrorNotSupported) return e;
       }
     }
@@ -1132,10 +1194,10 @@ cudaError_t launch_getf2_panel(T* A, long lda, int mp, int w, int* ipiv, int row
 
 template cudaError_t launch_getf2_panel<double>(double*, long, int, int, int*, int, int, int,
                                                 const PanelScratch<double>&, DevStatus*,
-                                                int, cudaStream_t, bool);
+                                                int, cudaStream_t, bool, int, int, bool*);
 template cudaError_t launch_getf2_panel<float>(float*, long, int, int, int*, int, int, int,
                                                const PanelScratch<float>&, DevStatus*,
-                                               int, cudaStream_t, bool);
+                                               int, cudaStream_t, bool, int, int, bool*);
 
 // ---------------------------------------------------------------------------
 // El::LU(A, P, Q) with full pivoting (src/lapack_like/factor/LU/Full.hpp:15-59)
