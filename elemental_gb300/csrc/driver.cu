@@ -232,6 +232,9 @@ struct LuState {
   unsigned long long* trace;  // leaf-panel timestamps (4 per column), or null
   int trace_cols;
   int trail_grid;      // TcGridMode of the trailing update beside the look-ahead panel
+  bool trail_split;    // the trailing update's columns past the look-ahead panel's
+                       // expected end wait for it and take every SM
+  double trail_split_scale;  // margin on that expected end
 };
 
 // Blocked TRSM, left / lower / unit: B := L11^{-1} B with L11 nb x nb (any
@@ -412,10 +415,23 @@ static cudaError_t getrf_run(LuState<T>& s, int nb) {
       e = apply_swaps(s, s.main, k, jb, kn + jb2, s.n, 0, 0, true);
       if (e != cudaSuccess) return e;
     }
-    // beside the look-ahead panel the trailing update leaves SMs to it
+    // beside the look-ahead panel the trailing update leaves SMs to it; with
+    // trail_split, only the columns it is expected to take while the panel
+    // runs, and the rest after the panel on every SM
+    int c_mid = s.n;
+    if (split && s.trail_split && s.n > kn + jb2) {
+      // the panel of jb2 columns on m - kn rows: ~2 us per pivot step up to
+      // 16384 rows (registers), ~4.4 us above, plus ~1 ms of recursion
+      // kernels; the update at ~180 TF/s beside it (TF32x3 on all GPCs but
+      // one), rounded up to whole 256-column tiles
+      const double side_s =
+          (jb2 * ((s.m - kn) <= 16384 ? 2.1e-6 : 4.4e-6) + 1.0e-3) * s.trail_split_scale;
+      const double cols = side_s * 180e12 / (2.0 * (double)(s.m - kn) * jb);
+      const long c = (long)kn + jb2 + ((long)std::ceil(cols / 256.0)) * 256;
+      if (c < s.n) c_mid = (int)c;
+    }
     if (split) s.main.grid_mode = s.trail_grid;
-    e = update_cols(s, s.main, k, jb, kn + jb2, s.n);
-    if (e == cudaSuccess) e = update_companion(s, s.main, k, jb);
+    e = update_cols(s, s.main, k, jb, kn + jb2, c_mid);
     s.main.grid_mode = kGridFull;
     if (e != cudaSuccess) return e;
     if (jb2 > 0) {
@@ -425,6 +441,12 @@ static cudaError_t getrf_run(LuState<T>& s, int nb) {
         e = panel_rec(s, s.main, kn, jb2, kn, kn + jb2);
       if (e != cudaSuccess) return e;
     }
+    if (c_mid < s.n) {
+      e = update_cols(s, s.main, k, jb, c_mid, s.n);
+      if (e != cudaSuccess) return e;
+    }
+    e = update_companion(s, s.main, k, jb);
+    if (e != cudaSuccess) return e;
   }
   if (s.nopiv) return cudaSuccess;
   // every block column of L takes the later panels' interchanges at once
@@ -509,6 +531,8 @@ cudaError_t getrf(Context* ctx, int m, int n, T* A, long lda, int* ipiv, int nb,
   s.trail_grid = ctx->opt_trail_grid == 0   ? kGridFull
                  : ctx->opt_trail_grid == 3 ? kGridTiles
                                             : kGridSpareGpc;
+  s.trail_split = tc && ctx->opt_trail_split && s.trail_grid == kGridSpareGpc;
+  s.trail_split_scale = ctx->opt_trail_split > 1 ? ctx->opt_trail_split / 100.0 : 1.1;
   if (la) {
     s.side.st = ctx->side_stream;
     s.side.grid_mode = ctx->opt_trail_grid >= 2 ? kGridTiles : kGridSmall;
@@ -1255,6 +1279,10 @@ int ElGBSetOption(ElGBContext ctx, int option, int value) {
     case ELGB_OPT_TRAIL_GRID:
       if (value < 0 || value > 3) return elgb::kElArgError;
       ctx->opt_trail_grid = value;
+      return 0;
+    case ELGB_OPT_TRAIL_SPLIT:
+      if (value < 0 || value > 1000) return elgb::kElArgError;
+      ctx->opt_trail_split = value;
       return 0;
     case ELGB_OPT_PANEL_ROWS:
       if (value < 64 || value > 1536) return elgb::kElArgError;

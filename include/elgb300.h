@@ -86,6 +86,14 @@ int ElGBSetBlocksize(int nb);
  *                       updates on at most 32 persistent CTAs; 0 the
  *                       trailing update holds every SM; 3 one CTA per tile
  *                       for both.
+ *   ELGB_OPT_TRAIL_SPLIT 1 (default): in the tensor-core LU, the trailing
+ *                       update takes the SMs it shares with the look-ahead
+ *                       panel only for the columns it is expected to finish
+ *                       while the panel runs, then waits for the panel and
+ *                       updates the remaining columns on every SM; 0: the
+ *                       whole update beside the panel; 2 .. 1000: as 1 with
+ *                       the panel's expected time scaled by value / 100
+ *                       (1 means 110).
  *   ELGB_OPT_PANEL_ROWS  rows of a leaf panel per CTA that the panel kernels
  *                       aim for (64 .. 1536, default 1024): more CTAs make
  *                       each pivot step's local update shorter and its
@@ -100,7 +108,8 @@ enum {
   ELGB_OPT_RESIDUAL_DF = 6,
   ELGB_OPT_PANEL_TRACE = 7,
   ELGB_OPT_TRAIL_GRID = 8,
-  ELGB_OPT_PANEL_ROWS = 9
+  ELGB_OPT_PANEL_ROWS = 9,
+  ELGB_OPT_TRAIL_SPLIT = 10
 };
 int ElGBSetOption(ElGBContext ctx, int option, int value);
 
