@@ -283,16 +283,31 @@ static cudaError_t apply_swaps(LuState<T>& s, const LuLane& L, int c0, int w, in
 
 // Recursive panel factorization of columns [c0, c0 + w), rows [c0, m), of
 // the block panel [b0, b1): left half, TRSM / GEMM onto the right half,
-// right half.  Leaves of <= 32 columns go to the getf2 kernels, and each
+// right half.  Leaves of <= 32 columns (16 on panels taller than 16384
+// rows, see leaf_width) go to the getf2 kernels, and each
 // leaf's row interchanges go at once onto every other column of the block
 // (by the leaf kernel itself where it can, else one swap launch): the same
 // row moves, in the same order per column, as swapping each half's
 // interchanges onto its sibling after it -- no operation reads those
 // columns in between -- with one launch per leaf instead of two per node.
+// Leaf width of the block starting at column b0: 16 where the FP32 panel is
+// taller than 16384 rows (up to 32768), so that its rows still fit in the
+// registers of one 16-CTA cluster (16 columns, 4 rows a thread); else 32.
+template <typename T>
+static int leaf_width(const LuState<T>& s, int b0) {
+  if constexpr (sizeof(T) == 4) {
+    if (g_panel_regs == 2 && g_panel_cluster == 16 && !s.nopiv && !s.tournament &&
+        s.m - b0 > 16384 && s.m - b0 <= 32768)
+      return 16;
+  }
+  return 32;
+}
+
 template <typename T>
 static cudaError_t panel_rec(LuState<T>& s, const LuLane& L, int c0, int w, int b0, int b1) {
   Context* ctx = s.ctx;
-  if (w <= 32) {
+  const int lw = leaf_width(s, b0);
+  if (w <= lw) {
     const int pi = ctx->prof_begin(L.st);
     bool done = false, swapped = false;
     if constexpr (sizeof(T) == 4) {
@@ -323,8 +338,8 @@ static cudaError_t panel_rec(LuState<T>& s, const LuLane& L, int c0, int w, int 
     }
     return cudaSuccess;
   }
-  int w1 = (w / 2 + 31) / 32 * 32;
-  if (w1 >= w) w1 = w - 32;
+  int w1 = (w / 2 + lw - 1) / lw * lw;
+  if (w1 >= w) w1 = w - lw;
   const int w2 = w - w1;
   cudaError_t e = panel_rec(s, L, c0, w1, b0, b1);
   if (e != cudaSuccess) return e;

@@ -789,9 +789,10 @@ getf2_panel_cluster_kernel(PanelParams<T> p) {
 }
 
 // The cluster panel with the rows in registers (FP32).  512 threads; thread
-// t holds local rows t and t + 512 of its CTA's R <= 1024 rows, all W
-// values of each in registers, and the column loop is unrolled so every
-// register index is fixed.  Per column: publish (candidate row and row j
+// t holds local rows t, t + 512, ... (RPT of them) of its CTA's R <= 512 RPT
+// rows, all W values of each in registers (W x RPT <= 64: 32 columns and 2
+// rows, or 16 columns and 4 rows for panels of up to 32768 rows on 16 CTAs),
+// and the column loop is unrolled so every register index is fixed.  Per column: publish (candidate row and row j
 // from registers into the CTA's own slot), the cluster barrier, thread
 // g < C reads CTA g's slot, every warp picks the pivot, then the whole
 // rank-1 update of the thread's two rows and the next column's candidate.
@@ -821,10 +822,10 @@ __device__ __forceinline__ void ld_cluster_head(uint32_t addr, float& v, int& r)
   asm volatile("ld.shared::cluster.v2.b32 {%0, %1}, [%2];" : "=f"(v), "=r"(r) : "r"(addr));
 }
 
-template <int W>
+template <int W, int RPT>
 __global__ void __launch_bounds__(kRcThreads, 1)
 getf2_panel_cluster_reg_kernel(PanelParams<float> p) {
-  static_assert(W == kPanelW, "one slot layout");
+  static_assert(W <= kPanelW && W % 4 == 0 && W * RPT <= 64, "slot layout, registers");
   __shared__ RcSlot slots[2];
   __shared__ __align__(16) float s_d[W];
   __shared__ __align__(16) float s_rows[16][W];
@@ -843,10 +844,10 @@ getf2_panel_cluster_reg_kernel(PanelParams<float> p) {
   const int re = min(rb + R, p.mp);
   const int nr = max(re - rb, 0);
 
-  float a[2][W];
-  int grow[2];  // global panel row of each register row, -1 past the CTA's rows
+  float a[RPT][W];
+  int grow[RPT];  // global panel row of each register row, -1 past the CTA's rows
 #pragma unroll
-  for (int i = 0; i < 2; ++i) {
+  for (int i = 0; i < RPT; ++i) {
     const int r = tid + i * kRcThreads;
     grow[i] = r < nr ? rb + r : -1;
 #pragma unroll
@@ -857,7 +858,7 @@ getf2_panel_cluster_reg_kernel(PanelParams<float> p) {
   float bv = -1.f;
   int br = -1;
 #pragma unroll
-  for (int i = 0; i < 2; ++i)
+  for (int i = 0; i < RPT; ++i)
     if (grow[i] >= 0) {
       const float v = fabsf(a[i][0]);
       if (argmax_better(v, grow[i], bv, br)) {
@@ -877,7 +878,7 @@ getf2_panel_cluster_reg_kernel(PanelParams<float> p) {
       if (tr) tr[0] = globaltimer_ns();
       // 1. publish from the registers of the rows' owners
 #pragma unroll
-      for (int i = 0; i < 2; ++i) {
+      for (int i = 0; i < RPT; ++i) {
         if (grow[i] >= 0 && grow[i] == br)
 #pragma unroll
           for (int c = 0; c < W; ++c) my->cand[c] = a[i][c];
@@ -940,7 +941,7 @@ getf2_panel_cluster_reg_kernel(PanelParams<float> p) {
       bv = -1.f;
       br = -1;
 #pragma unroll
-      for (int i = 0; i < 2; ++i) {
+      for (int i = 0; i < RPT; ++i) {
         const int row = grow[i];
         if (row < 0) continue;
         if (piv != j && row == j) {  // row j takes the pivot row; not updated
@@ -972,7 +973,7 @@ getf2_panel_cluster_reg_kernel(PanelParams<float> p) {
     }
   }
 #pragma unroll
-  for (int i = 0; i < 2; ++i)
+  for (int i = 0; i < RPT; ++i)
     if (grow[i] >= 0)
 #pragma unroll
       for (int c = 0; c < W; ++c)
@@ -1091,8 +1092,10 @@ static cudaError_t launch_getf2_panel_cluster_reg(float* A, long lda, int mp, in
                                                   int C, unsigned long long* trace,
                                                   cudaStream_t stream, int swap_lo, int swap_hi) {
   const int R = ceil_div(mp, C);
-  if (R > 2 * kRcThreads) return cudaErrorNotSupported;
-  auto kern = getf2_panel_cluster_reg_kernel<kPanelW>;
+  const bool narrow = w <= 16 && R > 2 * kRcThreads;  // 16 columns, 4 rows a thread
+  if (R > (narrow ? 4 : 2) * kRcThreads) return cudaErrorNotSupported;
+  auto kern = narrow ? getf2_panel_cluster_reg_kernel<16, 4>
+                     : getf2_panel_cluster_reg_kernel<kPanelW, 2>;
   cudaError_t e = cudaSuccess;
   if (C > 8) e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   if (e != cudaSuccess) return e;
@@ -1131,9 +1134,13 @@ cudaError_t launch_getf2_panel(T* A, long lda, int mp, int w, int* ipiv, int row
   if (w > kPanelW || mp < w) return cudaErrorInvalidValue;
   if constexpr (sizeof(T) == 4) {
     if (g_panel_regs == 2 && g_panel_cluster > 1 && !nopiv) {
-      // rows in registers on a cluster where one fits (<= 1024 rows per CTA)
-      const int C = cluster_ctas<T>(mp, g_panel_cluster);
-      if (C > 0 && ceil_div(mp, C) <= 2 * kRcThreads) {
+      // rows in registers on a cluster where one fits (<= 1024 rows per CTA;
+      // narrow leaves of taller panels: 16 CTAs of up to 2048 rows)
+      int C = cluster_ctas<T>(mp, g_panel_cluster);
+      if (w <= 16 && g_panel_cluster == 16 && mp > 16 * 2 * kRcThreads &&
+          mp <= 16 * 4 * kRcThreads)
+        C = 16;
+      if (C > 0 && ceil_div(mp, C) <= (w <= 16 ? 4 : 2) * kRcThreads) {
         const bool fuse = swaps_done != nullptr && (swap_lo < 0 || swap_hi > w);
         const cudaError_t e = launch_getf2_panel_cluster_reg(
             reinterpret_cast<float*>(A), lda, mp, w, ipiv, row_base, info_base, st, C, s.trace,
