@@ -240,6 +240,20 @@ def haar_conditioned(n, kappa, g, device="cuda"):
     return U @ V.t()
 
 
+def host_thp_gib():
+    """Transparent huge pages backing this process's anonymous memory (GiB),
+    or None where the kernel does not report them: the host buffers' page
+    size, beside their measured upload rate."""
+    try:
+        with open("/proc/self/smaps_rollup") as f:
+            for line in f:
+                if line.startswith("AnonHugePages:"):
+                    return int(line.split()[1]) / (1 << 20)
+    except OSError:
+        pass
+    return None
+
+
 def host_tensor(shape):
     """FP64 host buffer for the end-to-end arms: the library's host memory
     (ElGBHostAlloc: anonymous pages registered with the CUDA driver), viewed
@@ -410,6 +424,7 @@ def gpu_arm(args, rank, world, local_rank):
                              f"on the host ({th:.1f} s, not timed)",
                "phases_ms_per_step": phases,
                "h2d_gbs_torch_same_buffer": torch_h2d,
+               "host_thp_gib": host_thp_gib(),
                "h2d_gbs": (8 * n * n + 8 * n * q) / (phases["upload_ms"] * 1e-3) / 1e9
                if phases["upload_ms"] > 0 else None}
         del Ah, B0, Bh, Am, Bm
