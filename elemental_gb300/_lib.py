@@ -88,6 +88,7 @@ def load():
     _sig(lib, "ElGBProfileStop", c_int, vp, P(c_ll), P(c_double), P(c_double), P(c_double))
     _sig(lib, "ElGBProfileTag", c_int, vp, c_int, P(c_ll), P(c_double), P(c_double),
          P(c_double))
+    _sig(lib, "ElGBProfileRecords", c_int, vp, c_int, P(c_int), vp, vp, vp, vp)
     for s in ("d", "s"):
         _sig(lib, f"ElGBLUPartialPiv_{s}", c_int, vp, c_int, c_int, vp, c_int, vp, c_int)
         _sig(lib, f"ElGBSolveAfterLUPartialPiv_{s}", c_int, vp, c_int, c_int, vp, c_int, vp,

@@ -1266,6 +1266,32 @@ int ElGBProfileTag(ElGBContext ctx, int tag, long long* launches, double* ms, do
   return 0;
 }
 
+int ElGBProfileRecords(ElGBContext ctx, int cap, int* count, float* start_ms, float* dur_ms,
+                       int* tag, int* side) {
+  if (!ctx || !count || cap < 0 || (cap > 0 && (!start_ms || !dur_ms || !tag || !side)))
+    return elgb::kElArgError;
+  if (ctx->prof_on) return elgb::kElLogicError;
+  int n = 0;
+  cudaEvent_t base = nullptr;
+  for (auto& r : ctx->prof) {
+    if (!r.a || !r.b || r.tag < 0 || r.tag >= 16) continue;
+    if (!base) base = r.a;
+    if (n < cap) {
+      float t0 = 0, d = 0;
+      if (cudaEventElapsedTime(&t0, base, r.a) != cudaSuccess ||
+          cudaEventElapsedTime(&d, r.a, r.b) != cudaSuccess)
+        return elgb::kElRuntimeError;
+      start_ms[n] = t0;
+      dur_ms[n] = d;
+      tag[n] = r.tag;
+      side[n] = r.side ? 1 : 0;
+    }
+    ++n;
+  }
+  *count = n;
+  return 0;
+}
+
 int ElGBSetOption(ElGBContext ctx, int option, int value) {
   if (!ctx) return elgb::kElArgError;
   switch (option) {

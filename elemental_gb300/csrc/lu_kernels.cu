@@ -980,52 +980,91 @@ getf2_panel_cluster_reg_kernel(PanelParams<float> p) {
         if (c < w) p.A[(long)grow[i] + (long)c * p.lda] = a[i][c];
   // The leaf's interchanges (rows j and s_piv[j], j = 0 .. w-1, in order) on
   // the other columns of its block: their net row moves (at most 2w rows),
-  // then one warp per column reads every moved row before writing any.
+  // then each warp takes a few columns at a time and reads every moved row
+  // of them before writing any.
   const int nleft = -p.swap_lo, nright = max(p.swap_hi - w, 0);
   if (nleft + nright > 0) {
-    if (tid == 0) {
-      int* key = s_dst;  // row
-      int* val = s_src;  // the row whose value ends up there
-      int nk = w;
-      for (int r = 0; r < w; ++r) key[r] = val[r] = r;
-      for (int j = 0; j < w; ++j) {
-        const int pv = s_piv[j];
-        if (pv == j) continue;
-        int ip = -1;
-        if (pv < w) {
-          ip = pv;
-        } else {
-          for (int k = w; k < nk; ++k)
-            if (key[k] == pv) ip = k;
-          if (ip < 0) {
-            ip = nk++;
-            key[ip] = val[ip] = pv;
+    if (tid < 32) {
+      // warp 0: slots 0 .. w-1 are rows 0 .. w-1; each distinct pivot row
+      // >= w gets the next slot in the order of its first use
+      const int pv = lane < w ? s_piv[lane] : lane;
+      const bool ext = lane < w && pv >= w;
+      const unsigned grp = __match_any_sync(0xffffffffu, ext ? pv : -1 - lane);
+      const int leader = __ffs(grp) - 1;
+      const unsigned firsts = __ballot_sync(0xffffffffu, ext && leader == lane);
+      const int slot = ext ? w + __popc(firsts & ((1u << leader) - 1u)) : pv;
+      const int nslot = w + __popc(firsts);
+      if (ext && leader == lane) s_dst[slot] = pv;  // the row of each extra slot
+      __syncwarp();
+      const int key0 = lane < w ? lane : (lane < nslot ? s_dst[lane] : -1);
+      const int key1 = lane + 32 < nslot ? s_dst[lane + 32] : -1;
+      __syncwarp();
+      // the swaps in order on the slots' contents (slot q: lane q & 31,
+      // register q >> 5)
+      int v0 = key0, v1 = key1;
+#pragma unroll
+      for (int j = 0; j < W; ++j) {
+        if (j < w) {
+          const int sj = __shfl_sync(0xffffffffu, slot, j);
+          const int x = __shfl_sync(0xffffffffu, v0, j);
+          const int y = __shfl_sync(0xffffffffu, sj < 32 ? v0 : v1, sj & 31);
+          if (lane == j) v0 = y;
+          if (sj < 32) {
+            if (lane == sj) v0 = x;
+          } else if (lane == sj - 32) {
+            v1 = x;
           }
         }
-        const int t = val[j];
-        val[j] = val[ip];
-        val[ip] = t;
       }
-      int m = 0;  // keep the rows that move, in place
-      for (int k = 0; k < nk; ++k)
-        if (key[k] != val[k]) {
-          key[m] = key[k];
-          val[m] = val[k];
-          ++m;
-        }
-      s_nmove = m;
+      const bool mv0 = lane < nslot && key0 != v0;
+      const bool mv1 = lane + 32 < nslot && key1 != v1;
+      const unsigned m0 = __ballot_sync(0xffffffffu, mv0);
+      const unsigned m1 = __ballot_sync(0xffffffffu, mv1);
+      const unsigned lt = (1u << lane) - 1u;
+      if (mv0) {
+        const int o = __popc(m0 & lt);
+        s_dst[o] = key0;
+        s_src[o] = v0;
+      }
+      if (mv1) {
+        const int o = __popc(m0) + __popc(m1 & lt);
+        s_dst[o] = key1;
+        s_src[o] = v1;
+      }
+      if (lane == 0) s_nmove = __popc(m0) + __popc(m1);
     }
     __syncthreads();
     const int nmove = s_nmove;
     const int nw = kRcThreads / 32, warp = tid >> 5;
-    for (int q = b * nw + warp; q < nleft + nright; q += G * nw) {
-      const int c = q < nleft ? p.swap_lo + q : w + (q - nleft);
-      float* col = p.A + (long)c * p.lda;
-      const float v0 = lane < nmove ? col[s_src[lane]] : 0.f;
-      const float v1 = lane + 32 < nmove ? col[s_src[lane + 32]] : 0.f;
+    const int d0 = lane < nmove ? s_dst[lane] : 0, s0 = lane < nmove ? s_src[lane] : 0;
+    const int d1 = lane + 32 < nmove ? s_dst[lane + 32] : 0;
+    const int s1 = lane + 32 < nmove ? s_src[lane + 32] : 0;
+    constexpr int kCB = 4;  // columns a warp moves together
+    const int ncol = nleft + nright, stride = G * nw;
+    for (int q0 = b * nw + warp; q0 < ncol; q0 += kCB * stride) {
+      float x0[kCB], x1[kCB];
+#pragma unroll
+      for (int u = 0; u < kCB; ++u) {
+        const int q = q0 + u * stride;
+        x0[u] = x1[u] = 0.f;
+        if (q < ncol) {
+          const int c = q < nleft ? p.swap_lo + q : w + (q - nleft);
+          const float* col = p.A + (long)c * p.lda;
+          if (lane < nmove) x0[u] = col[s0];
+          if (lane + 32 < nmove) x1[u] = col[s1];
+        }
+      }
       __syncwarp();
-      if (lane < nmove) col[s_dst[lane]] = v0;
-      if (lane + 32 < nmove) col[s_dst[lane + 32]] = v1;
+#pragma unroll
+      for (int u = 0; u < kCB; ++u) {
+        const int q = q0 + u * stride;
+        if (q < ncol) {
+          const int c = q < nleft ? p.swap_lo + q : w + (q - nleft);
+          float* col = p.A + (long)c * p.lda;
+          if (lane < nmove) col[d0] = x0[u];
+          if (lane + 32 < nmove) col[d1] = x1[u];
+        }
+      }
     }
   }
   cluster_barrier();  // no CTA leaves while another may still read its slots
@@ -1111,12 +1150,20 @@ static cudaError_t launch_getf2_panel_cluster_reg(float* A, long lda, int mp, in
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  int nclusters = 0;
-  e = cudaOccupancyMaxActiveClusters(&nclusters, (void*)kern, &cfg);
-  if (e != cudaSuccess || nclusters < 1) {
-    cudaGetLastError();
-    return cudaErrorNotSupported;
+  // whether a cluster of C fits, asked once per device, variant and C
+  static signed char fits[64][2][17] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  signed char* f = (dev >= 0 && dev < 64 && C <= 16) ? &fits[dev][narrow ? 1 : 0][C] : nullptr;
+  bool ok = f && *f > 0;
+  if (!f || *f == 0) {
+    int nclusters = 0;
+    e = cudaOccupancyMaxActiveClusters(&nclusters, (void*)kern, &cfg);
+    if (e != cudaSuccess) cudaGetLastError();
+    ok = e == cudaSuccess && nclusters >= 1;
+    if (f) *f = ok ? 1 : -1;
   }
+  if (!ok) return cudaErrorNotSupported;
   PanelScratch<float> ps{};
   ps.trace = trace;
   PanelParams<float> prm{A, lda, mp, w, R, ipiv, row_base, info_base, 0, ps, st, 0,
@@ -1779,7 +1826,9 @@ cudaError_t launch_build_swap_pairs(const int* ipiv, int k, int nb, int* pairs, 
   while ((1 << tbits) < 2 * nb) ++tbits;
   const size_t smem = (8 * (size_t)nb + 2 * ((size_t)1 << tbits)) * sizeof(int);
   if (smem > 200 * 1024) return cudaErrorInvalidValue;
-  if (smem > 48 * 1024) {
+  // the kernel's static shared memory (s_wsum) counts against the same 48 KB
+  // default: at nb = 1024 the dynamic part alone is exactly 48 KB
+  if (smem + sizeof(int) * 32 > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(build_swap_pairs_kernel,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);

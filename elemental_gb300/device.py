@@ -9,6 +9,7 @@ only device memory and streams; the arithmetic is the library's kernels.
 from __future__ import annotations
 
 import ctypes
+import numpy as np
 
 import torch
 
@@ -154,6 +155,28 @@ class Context:
                 if name == "tc_gemm":
                     out["flops_lookahead_tc"] = fl.value
         out["by_kernel_lookahead_stream"] = side
+        return out
+
+    def profile_records(self):
+        """After profile_stop: every event-bracketed launch group in issue
+        order as a structured array (start_ms, dur_ms, tag, side), the start
+        relative to the first group."""
+        cnt = ctypes.c_int()
+        self._rc(self.lib.ElGBProfileRecords(self.h, 0, ctypes.byref(cnt), None, None, None,
+                                             None), "ProfileRecords")
+        n = cnt.value
+        start = np.zeros(n, np.float32)
+        dur = np.zeros(n, np.float32)
+        tag = np.zeros(n, np.int32)
+        side = np.zeros(n, np.int32)
+        if n:
+            self._rc(self.lib.ElGBProfileRecords(
+                self.h, n, ctypes.byref(cnt), start.ctypes.data_as(ctypes.c_void_p),
+                dur.ctypes.data_as(ctypes.c_void_p), tag.ctypes.data_as(ctypes.c_void_p),
+                side.ctypes.data_as(ctypes.c_void_p)), "ProfileRecords")
+        out = np.zeros(n, dtype=[("start_ms", "f4"), ("dur_ms", "f4"), ("tag", "i4"),
+                                 ("side", "i4")])
+        out["start_ms"], out["dur_ms"], out["tag"], out["side"] = start, dur, tag, side
         return out
 
     # -- the path -----------------------------------------------------------

@@ -148,6 +148,13 @@ enum {
 };
 int ElGBProfileTag(ElGBContext ctx, int tag, long long* launches, double* ms,
                    double* flops, double* bytes);
+/* After ElGBProfileStop: the event-bracketed launch groups one by one, in
+ * issue order (the timeline of both streams).  Fills up to cap records:
+ * start (ms after the first group's start), duration (ms), tag (the family
+ * above) and side (1 on the look-ahead panel stream); *count receives the
+ * number of groups recorded. */
+int ElGBProfileRecords(ElGBContext ctx, int cap, int* count, float* start_ms,
+                       float* dur_ms, int* tag, int* side);
 
 /* El::LU(A, P) with partial pivoting (reference
  * src/lapack_like/factor/LU.cpp:104-138): A (m x n) is overwritten by the

@@ -161,6 +161,40 @@ def case_residual(ctx, a):
                 tflops_eq_df=fl / (ms_df * 1e-3) / 1e12, tflops_fp64=fl / (ms_64 * 1e-3) / 1e12)
 
 
+def _stream_overlap(rec, segments=8):
+    """From the profiler's launch groups: how long the main stream, the
+    look-ahead panel stream, both or neither had a launch group running, in
+    total and per eighth of the run."""
+    import numpy as np
+
+    if len(rec) == 0:
+        return {}
+    t = np.concatenate([rec["start_ms"], rec["start_ms"] + rec["dur_ms"]])
+    edges = np.unique(np.concatenate([t, np.linspace(t.min(), t.max(), segments + 1)]))
+    mid = 0.5 * (edges[1:] + edges[:-1])
+    width = np.diff(edges)
+
+    def busy(sel):
+        s = rec["start_ms"][sel]
+        e = s + rec["dur_ms"][sel]
+        order = np.argsort(s)
+        s, e = s[order], np.maximum.accumulate(e[order])
+        i = np.searchsorted(s, mid, side="right") - 1
+        return (i >= 0) & (e[np.maximum(i, 0)] > mid)
+
+    m, sd = busy(rec["side"] == 0), busy(rec["side"] == 1)
+    seg = np.minimum(((mid - t.min()) / (t.max() - t.min()) * segments).astype(int),
+                     segments - 1)
+    out = {}
+    for name, mask in (("both", m & sd), ("main_only", m & ~sd), ("side_only", ~m & sd),
+                       ("neither", ~m & ~sd)):
+        out[name + "_ms"] = round(float(width[mask].sum()), 2)
+        out[name + "_ms_by_eighth"] = [round(float(width[mask & (seg == k)].sum()), 2)
+                                       for k in range(segments)]
+    out["span_ms"] = round(float(t.max() - t.min()), 2)
+    return out
+
+
 def case_lu_breakdown(ctx, a):
     """El::LU on an FP32 matrix (tensor-core updates) with the per-kernel
     event timing of the library's profiler: panel, swaps, TRSM, GEMMs."""
@@ -174,10 +208,15 @@ def case_lu_breakdown(ctx, a):
     ctx.profile_start()
     ms = _timed(lambda: ctx.lu_mixed(A, gemm_kind=a.kind, nb=a.nb))
     prof = ctx.profile_stop()
+    rec = ctx.profile_records()
+    if a.records:
+        import numpy as np
+
+        np.save(a.records, rec)
     ctx.set_option("lookahead", 1)
     ctx.set_option("trail_grid", 2)
     return dict(case="lu_breakdown", n=a.n, kind=KIND_NAMES[a.kind], lookahead=a.lookahead,
-                trail_grid=a.trail_grid, ms=ms,
+                trail_grid=a.trail_grid, ms=ms, timeline=_stream_overlap(rec),
                 tflops=2.0 / 3.0 * a.n ** 3 / (ms * 1e-3) / 1e12,
                 kernel_ms={k: round(v["ms"], 3) for k, v in prof["by_kernel"].items()},
                 kernel_ms_lookahead_stream={k: round(v["ms"], 3)
@@ -275,6 +314,8 @@ def main(argv=None):
                    help="panel_trace: ELGB_OPT_TRAIL_SPLIT")
     p.add_argument("--panel-regs", type=int, default=2,
                    help="panel_trace: ELGB_OPT_PANEL_REGS (2 = register cluster kernel)")
+    p.add_argument("--records", default="",
+                   help="lu_breakdown: save the profiler's launch groups (.npy)")
     a = p.parse_args(argv)
     ctx = D.context(0)
     out = CASES[a.case](ctx, a)

@@ -53,7 +53,7 @@ def gpu_lu(ctx, A, nb, dtype=torch.float64):
                                     (33, 33, 32), (100, 100, 96), (129, 129, 32),
                                     (150, 100, 32), (100, 150, 32), (257, 257, 64),
                                     (300, 300, 128), (520, 520, 128), (1000, 700, 128),
-                                    (1002, 517, 64)])
+                                    (1002, 517, 64), (2100, 2100, 1024)])
 def test_lu_matches_oracle(ctx, m, n, nb):
     A = mats.gaussian(m, n, 7 * m + n)
     LU, piv, info = gpu_lu(ctx, A, nb)

@@ -31,12 +31,13 @@ def _matrix(m, n, seed):
     return torch.randn(n, m, device="cuda", generator=g).t()  # column-major m x n
 
 
-@pytest.mark.parametrize("m,n", [(300, 300), (1000, 700), (2100, 2100), (5000, 1200),
-                                 (8192, 8192), (16384, 640)])
-def test_register_cluster_panels_match_shared_memory_panels(ctx, m, n):
+@pytest.mark.parametrize("m,n,nb", [(300, 300, 0), (1000, 700, 0), (2100, 2100, 0),
+                                    (5000, 1200, 0), (8192, 8192, 0), (16384, 640, 0),
+                                    (4100, 3000, 1024), (6000, 4096, 768)])
+def test_register_cluster_panels_match_shared_memory_panels(ctx, m, n, nb):
     A0 = _matrix(m, n, m + n)
-    A1, p1 = _lu(ctx, A0, 0)
-    A2, p2 = _lu(ctx, A0, 2)
+    A1, p1 = _lu(ctx, A0, 0, nb=nb)
+    A2, p2 = _lu(ctx, A0, 2, nb=nb)
     assert torch.equal(p1, p2)
     assert torch.equal(A1, A2)
 
