@@ -895,20 +895,24 @@ getf2_panel_cluster_reg_kernel(PanelParams<float> p) {
       cluster_wait();
       // 2. thread g < C reads CTA g's slot: head and candidate row in one
       // round trip, row j (its owner's slot only) in a second
-      if (tid < G) {
-        const uint32_t base = cluster_map(my, (unsigned)tid);
-        float gv;
-        int gr;
-        ld_cluster_head(base + (uint32_t)offsetof(RcSlot, val), gv, gr);
+      // (row j comes from its owner's slot through thread 32, in warp 1, at
+      // the same time)
+      if (tid < G || tid == 32) {
+        const unsigned src = tid < G ? (unsigned)tid : (unsigned)(j / R);
+        const uint32_t base = cluster_map(my, src);
         float4 cr[W / 4];
+        if (tid < G) {
+          float gv;
+          int gr;
+          ld_cluster_head(base + (uint32_t)offsetof(RcSlot, val), gv, gr);
 #pragma unroll
-        for (int c = 0; c < W / 4; ++c)
-          cr[c] = ld_cluster_v4(base + (uint32_t)offsetof(RcSlot, cand) + 16u * c);
-        s_gv[tid] = gv;
-        s_gr[tid] = gr;
+          for (int c = 0; c < W / 4; ++c)
+            cr[c] = ld_cluster_v4(base + (uint32_t)offsetof(RcSlot, cand) + 16u * c);
+          s_gv[tid] = gv;
+          s_gr[tid] = gr;
 #pragma unroll
-        for (int c = 0; c < W / 4; ++c) reinterpret_cast<float4*>(s_rows[tid])[c] = cr[c];
-        if (tid == j / R) {
+          for (int c = 0; c < W / 4; ++c) reinterpret_cast<float4*>(s_rows[tid])[c] = cr[c];
+        } else {
 #pragma unroll
           for (int c = 0; c < W / 4; ++c)
             cr[c] = ld_cluster_v4(base + (uint32_t)offsetof(RcSlot, diag) + 16u * c);
@@ -931,7 +935,8 @@ getf2_panel_cluster_reg_kernel(PanelParams<float> p) {
         piv = (r < 0) ? j : r;
       }
       const float* urow = (piv == j) ? s_d : s_rows[piv / R];
-      if (b == 0 && tid == 0) p.ipiv[j] = p.row_base + piv;
+      // (the pivots go to global memory after the last column: a global store
+      // here would hold up the release of thread 0's next cluster arrive)
       if (tid == 0) s_piv[j] = piv;
       const float alpha = urow[j];
       const bool singular = (alpha == 0.f);
@@ -966,12 +971,15 @@ getf2_panel_cluster_reg_kernel(PanelParams<float> p) {
           }
         }
       }
-      // the leading barrier of block_argmax also orders every read of s_d /
-      // s_rows above before the next column's gather refills them
-      block_argmax(bv, br, s_rv, s_rr);
+      // every warp reduces the CTA's candidates itself (one barrier).  The
+      // next column's cluster barrier orders every read above (s_d, s_rows,
+      // s_rv) before the gather and the per-warp writes that refill them:
+      // each thread reads before it arrives, they write after the wait.
+      block_argmax_nolead(bv, br, s_rv, s_rr);
       if (tr) tr[3] = globaltimer_ns();
     }
   }
+  if (b == 0 && tid < w) p.ipiv[tid] = p.row_base + s_piv[tid];
 #pragma unroll
   for (int i = 0; i < RPT; ++i)
     if (grow[i] >= 0)
