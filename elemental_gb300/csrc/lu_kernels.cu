@@ -1882,6 +1882,48 @@ apply_swap_pairs_kernel(T* __restrict__ A, long lda, int c0a, int c1a, int c0b, 
   }
 }
 
+// The same with each lane's moved entries of a column in registers (at most
+// 32 x PER moves): every load of the column is in flight at once before the
+// stores, and shared memory holds only the pairs.  The moved rows are
+// scattered over the column (one 32-byte sector each), so the kernel is
+// bound by the number of DRAM sectors in flight, not by bytes.
+template <typename T, int PER>
+__global__ void __launch_bounds__(kSwapThreads)
+apply_swap_pairs_reg_kernel(T* __restrict__ A, long lda, int c0a, int c1a, int c0b, int c1b,
+                            const int* __restrict__ pairs, const int* __restrict__ count,
+                            int nb) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  int* s_dst = reinterpret_cast<int*>(smem_raw);
+  int* s_src = s_dst + 32 * PER;
+  const int cnt = min(*count, 32 * PER);
+  for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+    s_dst[e] = pairs[e];
+    s_src[e] = pairs[2 * nb + e];
+  }
+  __syncthreads();
+  if (cnt == 0) return;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int na = c1a - c0a, ncols = na + (c1b - c0b);
+  const int gw = blockIdx.x * (blockDim.x >> 5) + warp;
+  const int nw = gridDim.x * (blockDim.x >> 5);
+  for (int q = gw; q < ncols; q += nw) {
+    const int col = q < na ? c0a + q : c0b + (q - na);
+    T* colp = A + (long)col * lda;
+    T v[PER];
+#pragma unroll
+    for (int u = 0; u < PER; ++u) {
+      const int e = lane + 32 * u;
+      if (e < cnt) v[u] = colp[s_src[e]];
+    }
+    __syncwarp();
+#pragma unroll
+    for (int u = 0; u < PER; ++u) {
+      const int e = lane + 32 * u;
+      if (e < cnt) colp[s_dst[e]] = v[u];
+    }
+  }
+}
+
 template <typename T>
 cudaError_t launch_apply_swap_pairs(T* A, long lda, int c0a, int c1a, int c0b, int c1b,
                                     const int* pairs, const int* count, int nb,
@@ -1890,6 +1932,17 @@ cudaError_t launch_apply_swap_pairs(T* A, long lda, int c0a, int c1a, int c0b, i
   if (ncols == 0 || nb <= 0) return cudaSuccess;
   if (c1a < c0a) c1a = c0a;
   if (c1b < c0b) c1b = c0b;
+  if (2 * nb <= 32 * 32) {  // at most 2 nb moves a column
+    const int per = 2 * nb <= 32 * 8 ? 8 : 2 * nb <= 32 * 16 ? 16 : 32;
+    auto kern = per == 8    ? apply_swap_pairs_reg_kernel<T, 8>
+                : per == 16 ? apply_swap_pairs_reg_kernel<T, 16>
+                            : apply_swap_pairs_reg_kernel<T, 32>;
+    const size_t smem = 2 * 32 * (size_t)per * sizeof(int);
+    int blocks = ceil_div(ncols, kSwapThreads / 32);
+    if (blocks > 8192) blocks = 8192;
+    kern<<<blocks, kSwapThreads, smem, stream>>>(A, lda, c0a, c1a, c0b, c1b, pairs, count, nb);
+    return cudaGetLastError();
+  }
   const size_t smem = 4 * (size_t)nb * sizeof(int) +
                       (size_t)(kSwapThreads / 32) * 2 * nb * sizeof(T);
   auto kern = apply_swap_pairs_kernel<T>;
