@@ -226,7 +226,8 @@ struct LuState {
   long ldbc;           // (RowEchelon's B, src/lapack_like/solve/Linear.cpp:62-71)
   int nbc;
   bool nopiv;          // El::LU(A): no pivot search, no interchanges
-  int* dlab;           // deferred left interchanges: labels per block column
+  int* dlab;           // deferred left interchanges: labels per block column,
+  int* dwork;          //   the labels' scratch
   T* dtmp;             //   and the gather's scratch
   bool tournament;     // FP32 leaf panels by tournament pivoting
   unsigned long long* trace;  // leaf-panel timestamps (4 per column), or null
@@ -465,8 +466,10 @@ static cudaError_t getrf_run(LuState<T>& s, int nb) {
   }
   if (s.nopiv) return cudaSuccess;
   // every block column of L takes the later panels' interchanges at once
-  const int pi = ctx->prof_begin(s.main.st);
-  LANE_CHECK(launch_defer_labels(s.ipiv, s.m, minDim, nb, s.dlab, s.main.st), 1);
+  int pi = ctx->prof_begin(s.main.st);
+  LANE_CHECK(launch_defer_labels(s.ipiv, s.m, minDim, nb, s.dlab, s.dwork, s.main.st), 2);
+  ctx->prof_end(pi, s.main.st, ELGB_PROF_SWAP, 0.0, 0.0);
+  pi = ctx->prof_begin(s.main.st);
   LANE_CHECK(launch_defer_gather<T>(s.A, s.lda, s.m, minDim, nb, s.dlab, s.dtmp,
                                     defer_gather_grid(ctx->num_sms), s.main.st), 1);
   ctx->prof_end(pi, s.main.st, ELGB_PROF_SWAP, 0.0,
@@ -480,6 +483,7 @@ static size_t getrf_scratch_bytes(const Context* ctx, int nb, int m, int n) {
   const size_t nblk = (size_t)(std::min(m, n) + nb - 1) / std::max(nb, 1);
   return panel_scratch_bytes<T>(ctx->num_sms) + 2 * align256(4 * (size_t)cap * sizeof(int)) +
          2 * align256(sizeof(int)) + align256(nblk * (size_t)m * sizeof(int)) +
+         align256(defer_labels_work_ints(m, std::min(m, n), nb) * sizeof(int)) +
          align256((size_t)defer_gather_grid(ctx->num_sms) * m * sizeof(T));
 }
 
@@ -488,6 +492,7 @@ static cudaError_t setup_lu_state(Context* ctx, LuState<T>& s, Carver& cv, int n
   const int cap = std::max(nb, 32);
   const size_t nblk = (size_t)(std::min(m, n) + nb - 1) / std::max(nb, 1);
   s.dlab = cv.take<int>(nblk * (size_t)m);
+  s.dwork = cv.take<int>(defer_labels_work_ints(m, std::min(m, n), nb));
   s.dtmp = cv.take<T>((size_t)defer_gather_grid(ctx->num_sms) * m);
   if (!s.dtmp) return cudaErrorMemoryAllocation;
   s.ctx = ctx;

@@ -124,9 +124,12 @@ cudaError_t launch_apply_swap_pairs(T* A, long lda, int c0a, int c1a,
 // interchanges applied; instead of swapping those rows after each panel,
 // lab[b m + r] (r >= (b+1) nb) receives the original row whose content ends
 // at row r after the interchanges ipiv[(b+1) nb .. mn), and the gather
-// A(r, c) <- A(lab[r], c) applies them once per column (coalesced writes,
-// L2-resident reads).  tmp: gridDim x m elements of scratch.
-cudaError_t launch_defer_labels(const int* ipiv, int m, int mn, int nb, int* lab,
+// A(r, c) <- A(lab[r], c) applies them once per column (through shared
+// memory when a column fits, coalesced both ways).  tmp: gridDim x m
+// elements of scratch for columns that do not fit.  work (may be null: one
+// serial replay a block column instead): defer_labels_work_ints ints.
+size_t defer_labels_work_ints(int m, int mn, int nb);
+cudaError_t launch_defer_labels(const int* ipiv, int m, int mn, int nb, int* lab, int* work,
                                 cudaStream_t stream);
 template <typename T>
 cudaError_t launch_defer_gather(T* A, long lda, int m, int mn, int nb, const int* lab, T* tmp,

@@ -1968,6 +1968,8 @@ template cudaError_t launch_apply_swap_pairs<float>(float*, long, int, int, int,
 // One CTA per block column b: replay the interchanges of every later panel
 // on row labels (shared memory when they fit, else in place in global
 // memory), serially in one thread -- the replay is inherently ordered.
+constexpr int kDeferChunk = 2048;
+
 __global__ void defer_labels_kernel(const int* __restrict__ ipiv, int m, int mn, int nb,
                                     int* __restrict__ lab, int use_smem) {
   extern __shared__ int sl[];
@@ -1978,51 +1980,173 @@ __global__ void defer_labels_kernel(const int* __restrict__ ipiv, int m, int mn,
   int* L = use_smem ? sl : lab + (long)b * m + base;
   for (int i = threadIdx.x; i < rows; i += blockDim.x) L[i] = base + i;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    for (int t = base; t < mn; ++t) {
-      const int p = ipiv[t];  // partial pivoting: p >= t >= base
-      if (p != t) {
-        const int a = L[t - base];
-        L[t - base] = L[p - base];
-        L[p - base] = a;
+  // the swaps come through shared memory a chunk at a time, so thread 0's
+  // serial replay waits on shared memory only
+  __shared__ int s_p[kDeferChunk];
+  for (int t0 = base; t0 < mn; t0 += kDeferChunk) {
+    const int nc = min(kDeferChunk, mn - t0);
+    for (int i = threadIdx.x; i < nc; i += blockDim.x) s_p[i] = ipiv[t0 + i];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int i = 0; i < nc; ++i) {
+        const int t = t0 + i, p = s_p[i];  // partial pivoting: p >= t >= base
+        if (p != t) {
+          const int a = L[t - base];
+          L[t - base] = L[p - base];
+          L[p - base] = a;
+        }
       }
     }
+    __syncthreads();
   }
-  __syncthreads();
   if (use_smem)
     for (int i = threadIdx.x; i < rows; i += blockDim.x) lab[(long)b * m + base + i] = L[i];
 }
 
-// Columns c < (last block start): A(r, c) <- A(lab_b[r], c) for r >= base_b,
-// through the CTA's own m-element slice of tmp.
-template <typename T>
-__global__ void __launch_bounds__(256)
+// Columns c < (last block start): A(r, c) <- A(lab_b[r], c) for r >= base_b.
+// With STAGE the CTA reads rows base_b .. m of the column into shared memory
+// (coalesced) and writes them back permuted (coalesced; the random reads hit
+// shared memory); otherwise through the CTA's own m-element slice of tmp (the
+// gather from global memory is then one DRAM sector a row).
+template <typename T, bool STAGE>
+__global__ void __launch_bounds__(1024)
 defer_gather_kernel(T* __restrict__ A, long lda, int m, int mn, int nb,
                     const int* __restrict__ lab, T* __restrict__ tmp) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* s_col = reinterpret_cast<T*>(smem_raw);
   const int nblk = (mn + nb - 1) / nb;
   const int ncols = (nblk - 1) * nb;  // the last block column has no later panel
+  const int bd = blockDim.x, tid = threadIdx.x;
   T* t = tmp + (long)blockIdx.x * m;
   for (int c = blockIdx.x; c < ncols; c += gridDim.x) {
     const int b = c / nb, base = (b + 1) * nb;
     if (base >= m) continue;
     const int* lb = lab + (long)b * m;
     T* col = A + (long)c * lda;
-    for (int r = base + threadIdx.x; r < m; r += blockDim.x) t[r] = col[lb[r]];
-    __syncthreads();
-    for (int r = base + threadIdx.x; r < m; r += blockDim.x) col[r] = t[r];
+    if (STAGE) {
+#pragma unroll 4
+      for (int r = base + tid; r < m; r += bd) s_col[r - base] = col[r];
+      __syncthreads();
+#pragma unroll 4
+      for (int r = base + tid; r < m; r += bd) col[r] = s_col[lb[r] - base];
+    } else {
+      for (int r = base + tid; r < m; r += bd) t[r] = col[lb[r]];
+      __syncthreads();
+      for (int r = base + tid; r < m; r += bd) col[r] = t[r];
+    }
     __syncthreads();
   }
 }
 
 int defer_gather_grid(int num_sms) { return 2 * num_sms; }
 
-cudaError_t launch_defer_labels(const int* ipiv, int m, int mn, int nb, int* lab,
+// Parallel form of the same labels.  With Q_b the replay from step base_b to
+// the end applied to the identity, Q_b[i] = S_b[Q_{b+1}[i]], where S_b is the
+// replay of block b+1's own steps [base_b, base_b + nb) alone (the identity
+// outside at most 2 nb positions).  defer_maps_kernel makes every S_b at once
+// (one CTA a block, nb serial steps each) as (position, value) pairs;
+// defer_compose_kernel then walks the blocks from the last one back, one
+// parallel gather a block.
+__global__ void defer_maps_kernel(const int* __restrict__ ipiv, int m, int mn, int nb,
+                                  int* __restrict__ pairs, int* __restrict__ counts) {
+  extern __shared__ int sl[];  // positions base .. m
+  __shared__ int s_p[kDeferChunk];
+  __shared__ int s_cnt;
+  const int b = blockIdx.x, base = (b + 1) * nb;
+  const int rows = m - base;
+  for (int i = threadIdx.x; i < rows; i += blockDim.x) sl[i] = base + i;
+  if (threadIdx.x == 0) s_cnt = 0;
+  __syncthreads();
+  const int t_end = min(base + nb, mn);
+  for (int t0 = base; t0 < t_end; t0 += kDeferChunk) {
+    const int nc = min(kDeferChunk, t_end - t0);
+    for (int i = threadIdx.x; i < nc; i += blockDim.x) s_p[i] = ipiv[t0 + i];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int i = 0; i < nc; ++i) {
+        const int t = t0 + i, p = s_p[i];  // p >= t >= base
+        if (p != t) {
+          const int a = sl[t - base];
+          sl[t - base] = sl[p - base];
+          sl[p - base] = a;
+        }
+      }
+    }
+    __syncthreads();
+  }
+  int* pos = pairs + (long)b * 4 * nb;
+  int* val = pos + 2 * nb;
+  for (int i = threadIdx.x; i < rows; i += blockDim.x)
+    if (sl[i] != base + i) {
+      const int k = atomicAdd(&s_cnt, 1);  // at most 2 nb moved positions
+      pos[k] = base + i;
+      val[k] = sl[i];
+    }
+  __syncthreads();
+  if (threadIdx.x == 0) counts[b] = s_cnt;
+}
+
+__global__ void __launch_bounds__(1024)
+defer_compose_kernel(int m, int mn, int nb, const int* __restrict__ pairs,
+                     const int* __restrict__ counts, int* __restrict__ map, int* __restrict__ lab) {
+  extern __shared__ int cur[];  // Q_{b+1}, the identity to start with
+  const int nblk = (mn + nb - 1) / nb;
+  for (int i = threadIdx.x; i < m; i += blockDim.x) {
+    cur[i] = i;
+    map[i] = i;
+  }
+  __syncthreads();
+  for (int b = nblk - 2; b >= 0; --b) {
+    const int base = (b + 1) * nb, cnt = counts[b];
+    const int* pos = pairs + (long)b * 4 * nb;
+    const int* val = pos + 2 * nb;
+    for (int e = threadIdx.x; e < cnt; e += blockDim.x) map[pos[e]] = val[e];
+    __syncthreads();
+    int* lb = lab + (long)b * m;
+#pragma unroll 4
+    for (int i = base + threadIdx.x; i < m; i += blockDim.x) {
+      const int v = map[cur[i]];
+      cur[i] = v;
+      lb[i] = v;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < cnt; e += blockDim.x) map[pos[e]] = pos[e];
+    __syncthreads();
+  }
+}
+
+size_t defer_labels_work_ints(int m, int mn, int nb) {
+  const size_t nblk = (size_t)(std::max(mn, 1) + nb - 1) / std::max(nb, 1);
+  return nblk * 4 * (size_t)nb + nblk + (size_t)m;
+}
+
+cudaError_t launch_defer_labels(const int* ipiv, int m, int mn, int nb, int* lab, int* work,
                                 cudaStream_t stream) {
   const int nblk = (mn + nb - 1) / nb;
   if (nblk <= 1) return cudaSuccess;
   const size_t smem = (size_t)m * sizeof(int);
   const bool use_smem = smem <= 200 * 1024;
-  if (use_smem && smem > 48 * 1024) {
+  if (use_smem && work) {
+    int* pairs = work;
+    int* counts = pairs + (size_t)nblk * 4 * nb;
+    int* map = counts + nblk;
+    const size_t msm = (size_t)std::max(m - nb, 1) * sizeof(int);
+    if (msm + kDeferChunk * sizeof(int) > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(defer_maps_kernel,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)msm);
+      if (e != cudaSuccess) return e;
+    }
+    if (smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(defer_compose_kernel,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+    }
+    defer_maps_kernel<<<nblk - 1, 256, msm, stream>>>(ipiv, m, mn, nb, pairs, counts);
+    defer_compose_kernel<<<1, 1024, smem, stream>>>(m, mn, nb, pairs, counts, map, lab);
+    return cudaGetLastError();
+  }
+  // (the kernel's static pivot chunk counts against the same 48 KB default)
+  if (use_smem && smem + kDeferChunk * sizeof(int) > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(defer_labels_kernel,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -2037,7 +2161,21 @@ cudaError_t launch_defer_gather(T* A, long lda, int m, int mn, int nb, const int
                                 int grid, cudaStream_t stream) {
   const int nblk = (mn + nb - 1) / nb;
   if (nblk <= 1) return cudaSuccess;
-  defer_gather_kernel<T><<<grid, 256, 0, stream>>>(A, lda, m, mn, nb, lab, tmp);
+  // rows nb .. m of a column (block column 0's share, the largest)
+  const size_t smem = (size_t)std::max(m - nb, 0) * sizeof(T);
+  if (smem <= 200 * 1024) {
+    auto kern = defer_gather_kernel<T, true>;
+    if (smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)smem);
+      if (e != cudaSuccess) return e;
+    }
+    // one CTA an SM while a column takes over ~100 KB, else two
+    const int per_sm = smem > 100 * 1024 ? 1 : 2;
+    kern<<<grid / 2 * per_sm, 1024, smem, stream>>>(A, lda, m, mn, nb, lab, tmp);
+    return cudaGetLastError();
+  }
+  defer_gather_kernel<T, false><<<grid, 256, 0, stream>>>(A, lda, m, mn, nb, lab, tmp);
   return cudaGetLastError();
 }
 
