@@ -236,6 +236,9 @@ struct LuState {
   bool trail_split;    // the trailing update's columns past the look-ahead panel's
                        // expected end wait for it and take every SM
   double trail_split_scale;  // margin on that expected end
+  bool inv_trsm;       // U12 = A12 - N A12 with N = I - L11^{-1} (tensor cores)
+  T* ninv;             // N of block ninv_k (nb x nb, leading dimension nb)
+  int ninv_ld, ninv_k;
 };
 
 // Blocked TRSM, left / lower / unit: B := L11^{-1} B with L11 nb x nb (any
@@ -357,15 +360,35 @@ static cudaError_t panel_rec(LuState<T>& s, const LuLane& L, int c0, int w, int 
 
 // Trailing update of block k (columns [c_begin, c_end) of the right part):
 // Trsm(LEFT, LOWER, NORMAL, UNIT) on A12 then Gemm(-1) on A22.
+// U12 := L11^{-1} U12 for block k (jb x ncols at B): one tensor-core product
+// U12 - N U12 with N = I - L11^{-1} where gemm_sub takes the tensor cores for
+// it (it packs B before C is written, so B may be C), else the blocked
+// substitution.  N is strictly lower: L11 N = L11 - I, solved once per block.
+template <typename T>
+static cudaError_t trsm_block_rows(LuState<T>& s, const LuLane& L, int k, int jb, T* B, long ldb,
+                                   int ncols) {
+  Context* ctx = s.ctx;
+  T* A11 = s.A + k + (long)k * s.lda;
+  if (s.inv_trsm && L.gemm.tc_kind >= 0 && jb >= 64 && ncols >= 64) {
+    if (s.ninv_k != k) {
+      LANE_CHECK(launch_copy_strict_lower<T>(A11, s.lda, jb, s.ninv, s.ninv_ld, L.st), 1);
+      cudaError_t e = trsm_llnu<T>(ctx, L, A11, s.lda, jb, s.ninv, s.ninv_ld, jb);
+      if (e != cudaSuccess) return e;
+      s.ninv_k = k;
+    }
+    return gemm_sub(ctx, L, jb, ncols, jb, s.ninv, s.ninv_ld, B, ldb, B, ldb);
+  }
+  return trsm_llnu<T>(ctx, L, A11, s.lda, jb, B, ldb, ncols);
+}
+
 template <typename T>
 static cudaError_t update_cols(LuState<T>& s, const LuLane& L, int k, int jb, int c_begin,
                                int c_end) {
   if (c_end <= c_begin) return cudaSuccess;
   Context* ctx = s.ctx;
   const int m2 = s.m - k - jb;
-  T* A11 = s.A + k + (long)k * s.lda;
-  cudaError_t e = trsm_llnu<T>(ctx, L, A11, s.lda, jb, s.A + k + (long)c_begin * s.lda, s.lda,
-                               c_end - c_begin);
+  cudaError_t e = trsm_block_rows<T>(s, L, k, jb, s.A + k + (long)c_begin * s.lda, s.lda,
+                                     c_end - c_begin);
   if (e != cudaSuccess) return e;
   if (m2 > 0)
     e = gemm_sub(ctx, L, m2, c_end - c_begin, jb, s.A + (k + jb) + (long)k * s.lda, s.lda,
@@ -379,8 +402,7 @@ static cudaError_t update_companion(LuState<T>& s, const LuLane& L, int k, int j
   if (!s.Bc || s.nbc <= 0) return cudaSuccess;
   Context* ctx = s.ctx;
   const int m2 = s.m - k - jb;
-  T* A11 = s.A + k + (long)k * s.lda;
-  cudaError_t e = trsm_llnu<T>(ctx, L, A11, s.lda, jb, s.Bc + k, s.ldbc, s.nbc);
+  cudaError_t e = trsm_block_rows<T>(s, L, k, jb, s.Bc + k, s.ldbc, s.nbc);
   if (e != cudaSuccess || m2 <= 0) return e;
   return gemm_sub(ctx, L, m2, s.nbc, jb, s.A + (k + jb) + (long)k * s.lda, s.lda, s.Bc + k,
                   s.ldbc, s.Bc + k + jb, s.ldbc);
@@ -484,6 +506,7 @@ static size_t getrf_scratch_bytes(const Context* ctx, int nb, int m, int n) {
   return panel_scratch_bytes<T>(ctx->num_sms) + 2 * align256(4 * (size_t)cap * sizeof(int)) +
          2 * align256(sizeof(int)) + align256(nblk * (size_t)m * sizeof(int)) +
          align256(defer_labels_work_ints(m, std::min(m, n), nb) * sizeof(int)) +
+         align256((size_t)nb * nb * sizeof(T)) +
          align256((size_t)defer_gather_grid(ctx->num_sms) * m * sizeof(T));
 }
 
@@ -493,6 +516,9 @@ static cudaError_t setup_lu_state(Context* ctx, LuState<T>& s, Carver& cv, int n
   const size_t nblk = (size_t)(std::min(m, n) + nb - 1) / std::max(nb, 1);
   s.dlab = cv.take<int>(nblk * (size_t)m);
   s.dwork = cv.take<int>(defer_labels_work_ints(m, std::min(m, n), nb));
+  s.ninv = cv.take<T>((size_t)nb * nb);
+  s.ninv_ld = nb;
+  s.ninv_k = -1;
   s.dtmp = cv.take<T>((size_t)defer_gather_grid(ctx->num_sms) * m);
   if (!s.dtmp) return cudaErrorMemoryAllocation;
   s.ctx = ctx;
@@ -553,6 +579,7 @@ cudaError_t getrf(Context* ctx, int m, int n, T* A, long lda, int* ipiv, int nb,
                                             : kGridSpareGpc;
   s.trail_split = tc && ctx->opt_trail_split && s.trail_grid == kGridSpareGpc;
   s.trail_split_scale = ctx->opt_trail_split > 1 ? ctx->opt_trail_split / 100.0 : 1.1;
+  s.inv_trsm = tc && ctx->opt_inv_trsm && s.ninv;
   if (la) {
     s.side.st = ctx->side_stream;
     s.side.grid_mode = ctx->opt_trail_grid >= 2 ? kGridTiles : kGridSmall;
@@ -1329,6 +1356,9 @@ int ElGBSetOption(ElGBContext ctx, int option, int value) {
     case ELGB_OPT_TRAIL_SPLIT:
       if (value < 0 || value > 1000) return elgb::kElArgError;
       ctx->opt_trail_split = value;
+      return 0;
+    case ELGB_OPT_INV_TRSM:
+      ctx->opt_inv_trsm = value ? 1 : 0;
       return 0;
     case ELGB_OPT_PANEL_ROWS:
       if (value < 64 || value > 1536) return elgb::kElArgError;

@@ -39,6 +39,7 @@ struct Context {
   int opt_residual_df = 1;        // ElGBSetOption(ELGB_OPT_RESIDUAL_DF)
   int opt_trail_grid = 2;         // ElGBSetOption(ELGB_OPT_TRAIL_GRID)
   int opt_trail_split = 1;        // ElGBSetOption(ELGB_OPT_TRAIL_SPLIT)
+  int opt_inv_trsm = 0;           // ElGBSetOption(ELGB_OPT_INV_TRSM)
   // ElGBSetOption(ELGB_OPT_PANEL_TRACE): per-column leaf-panel timestamps of
   // the last factorization, 4 per column, for its first trace_cols columns
   unsigned long long* trace_buf = nullptr;

@@ -158,6 +158,11 @@ cudaError_t launch_trsm_block(const T* A11, long lda, T* Bm, long ldb, int nb,
                               int ncols, bool lower, bool unit, bool trans_a,
                               bool trans_b, cudaStream_t stream);
 
+// out (n x n) := the strictly lower triangle of A, zeros elsewhere.
+template <typename T>
+cudaError_t launch_copy_strict_lower(const T* A, long lda, int n, T* out, long ldo,
+                                     cudaStream_t stream);
+
 // C = alpha * op(A) * op(B) + beta * C on CUDA cores (SIMT FMA).
 // uplo: 0 full, 1 lower triangle only (i >= j), 2 upper only (i <= j).
 template <typename T>

@@ -2422,6 +2422,28 @@ template cudaError_t launch_trsm_block<double>(const double*, long, double*, lon
 template cudaError_t launch_trsm_block<float>(const float*, long, float*, long, int, int,
                                               bool, bool, bool, bool, cudaStream_t);
 
+// out (n x n, leading dimension ldo) := the strictly lower triangle of A
+// (zeros on and above the diagonal).
+template <typename T>
+__global__ void copy_strict_lower_kernel(const T* __restrict__ A, long lda, int n,
+                                         T* __restrict__ out, long ldo) {
+  const int j = blockIdx.y;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    out[i + (long)j * ldo] = i > j ? A[i + (long)j * lda] : T(0);
+}
+
+template <typename T>
+cudaError_t launch_copy_strict_lower(const T* A, long lda, int n, T* out, long ldo,
+                                     cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  copy_strict_lower_kernel<T><<<dim3(ceil_div(n, 256), n), 256, 0, stream>>>(A, lda, n, out, ldo);
+  return cudaGetLastError();
+}
+template cudaError_t launch_copy_strict_lower<double>(const double*, long, int, double*, long,
+                                                      cudaStream_t);
+template cudaError_t launch_copy_strict_lower<float>(const float*, long, int, float*, long,
+                                                     cudaStream_t);
+
 // ---------------------------------------------------------------------------
 // K5 (FP64 and FP32 SIMT): C = alpha op(A) op(B) + beta C
 // ---------------------------------------------------------------------------

@@ -98,7 +98,15 @@ int ElGBSetBlocksize(int nb);
  *                       aim for (64 .. 1536, default 1024): more CTAs make
  *                       each pivot step's local update shorter and its
  *                       exchange longer.  Process-wide, like
- *                       ELGB_OPT_PANEL_CLUSTER. */
+ *                       ELGB_OPT_PANEL_CLUSTER.
+ *   ELGB_OPT_INV_TRSM   0 (default): the tensor-core LU's trailing
+ *                       triangular solve U12 = L11^-1 A12 is a blocked
+ *                       substitution; 1: one tensor-core product,
+ *                       U12 = A12 - N A12 with N = I - L11^-1 solved once
+ *                       per block.  1 shortens the LU (236 vs 241 ms at
+ *                       n = 32768) but the product's rounding grows with
+ *                       |N|: the factors are less accurate and refinement
+ *                       took one more iteration (5 vs 4), a net loss. */
 enum {
   ELGB_OPT_LOOKAHEAD = 1,
   ELGB_OPT_PANEL_CTAS = 2,
@@ -109,7 +117,8 @@ enum {
   ELGB_OPT_PANEL_TRACE = 7,
   ELGB_OPT_TRAIL_GRID = 8,
   ELGB_OPT_PANEL_ROWS = 9,
-  ELGB_OPT_TRAIL_SPLIT = 10
+  ELGB_OPT_TRAIL_SPLIT = 10,
+  ELGB_OPT_INV_TRSM = 11
 };
 int ElGBSetOption(ElGBContext ctx, int option, int value);
 

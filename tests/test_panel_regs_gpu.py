@@ -105,3 +105,26 @@ def test_register_cluster_panels_backward_error(ctx):
     assert np.linalg.norm(PA - L @ U) / np.linalg.norm(Ah) <= 4e-5
     _, pivr = O.lu(Ah.astype(np.float32), nb=256, dtype=np.float32)
     assert np.array_equal(piv.cpu().numpy()[:8], pivr[:8])
+
+
+def test_product_form_trailing_solve_factors_to_fp32_accuracy(ctx):
+    """ELGB_OPT_INV_TRSM = 1: the trailing update's U12 = L11^-1 A12 as
+    A12 - N A12 with N = I - L11^-1 on the tensor cores.  Rounding differs
+    from the substitution, so P A = L U is checked to FP32 accuracy and the
+    first pivots against the default path."""
+    n = 3000
+    A0 = _matrix(n, n, 5)
+    Ah = A0.double().cpu().numpy()
+    A1, p1 = _lu(ctx, A0, 2)
+    ctx.set_option("inv_trsm", 1)
+    try:
+        A2, p2 = _lu(ctx, A0, 2)
+    finally:
+        ctx.set_option("inv_trsm", 0)
+    LU = A2.double().cpu().numpy()
+    L = np.tril(LU, -1) + np.eye(n)
+    U = np.triu(LU)
+    PA = O.permute_rows(p2.cpu().numpy(), Ah)
+    assert np.linalg.norm(PA - L @ U) / np.linalg.norm(Ah) <= 1e-4
+    assert np.array_equal(p1.cpu().numpy()[:512], p2.cpu().numpy()[:512])
+    assert not torch.equal(A1, A2)  # the option took the other path
