@@ -11,6 +11,7 @@ can skip the first launch of the kernel it targets).
     python kernel_cases.py residual --n 32768 --nrhs 16
     python kernel_cases.py lu_breakdown --n 32768 --nb 512
     python kernel_cases.py panel_trace --n 32768 --nb 512
+    python kernel_cases.py leaf_costs --m 8192 --n 512 --nb 512
 
 Each prints one JSON line with the event-timed duration of the measured
 call and its algorithmic work.  Inputs are seeded N(0, 1), generated on the
@@ -283,7 +284,45 @@ def case_panel_trace(ctx, a):
                 leaf_step_ms_total=tot_steps, bands=bands)
 
 
-CASES = {"tc_gemm": case_tc_gemm, "lu": case_lu, "lu64": case_lu64, "refine": case_refine,
+def case_leaf_costs(ctx, a):
+    """Fixed cost of the leaf-panel launches: per leaf, the event-timed launch
+    group minus the traced span from its first pivot step's start to its
+    last step's end (load, exchange set-up, write-back, the interchanges on
+    the block's other columns, launch), for an m x n FP32 LU with block
+    size nb and one stream (so that the leaves run in column order)."""
+    import numpy as np
+
+    m, n, nb = a.m, a.n, a.nb
+    g = torch.Generator(device="cuda").manual_seed(a.seed)
+    A0 = torch.randn(n, m, device="cuda", generator=g).t()
+    A = A0.clone()
+    ctx.set_option("panel_trace", n)
+    ctx.set_option("lookahead", 0)
+    try:
+        ctx.lu_mixed(A, gemm_kind=a.kind, nb=nb)
+        A.copy_(A0)
+        torch.cuda.synchronize()
+        ctx.profile_start()
+        ctx.lu_mixed(A, gemm_kind=a.kind, nb=nb)
+        ctx.profile_stop()
+        rec = ctx.profile_records()
+        tr = ctx.panel_trace(n)
+    finally:
+        ctx.set_option("panel_trace", 0)
+        ctx.set_option("lookahead", 1)
+    pan = rec[rec["tag"] == 1]
+    pan = pan[np.argsort(pan["start_ms"])]
+    lw = 16 if 16384 < m <= 32768 else 32  # the leaf width of the first block
+    c0s = list(range(0, n, lw))[:len(pan)]
+    dur = pan["dur_ms"] * 1e3
+    span = np.array([(tr[c + lw - 1, 3] - tr[c, 0]) / 1e3 for c in c0s])
+    return dict(case="leaf_costs", m=m, n=n, nb=nb, leaf_width=lw, leaves=len(pan),
+                us_launch_median=round(float(np.median(dur)), 1),
+                us_steps_median=round(float(np.median(span)), 1),
+                us_fixed_median=round(float(np.median(dur - span)), 1))
+
+
+CASES = {"leaf_costs": case_leaf_costs, "tc_gemm": case_tc_gemm, "lu": case_lu, "lu64": case_lu64, "refine": case_refine,
          "batched": case_batched, "lufull": case_lufull, "residual": case_residual,
          "lu_breakdown": case_lu_breakdown, "panel_trace": case_panel_trace}
 
