@@ -52,13 +52,17 @@ void Context::prof_end(int idx, cudaStream_t st, int tag, double flops, double b
   prof[idx].flops = flops;
   prof[idx].bytes = bytes;
   prof[idx].side = st == side_stream && side_stream != nullptr;
+  prof[idx].lane = stream_lane(st);
 }
 
 Context::~Context() {
   for (cudaEvent_t e : ev_pool) cudaEventDestroy(e);
   if (ev_fork) cudaEventDestroy(ev_fork);
   if (ev_join) cudaEventDestroy(ev_join);
+  if (ev_iter) cudaEventDestroy(ev_iter);
+  if (ev_swapped) cudaEventDestroy(ev_swapped);
   if (side_stream) cudaStreamDestroy(side_stream);
+  if (swap_stream) cudaStreamDestroy(swap_stream);
   if (arena) cudaFree(arena);
   if (arena2) cudaFree(arena2);
   if (trace_buf) cudaFree(trace_buf);
@@ -200,7 +204,8 @@ static cudaError_t gemm_sub(Context* ctx, const LuLane& L, int m, int n, int k, 
       const double copies = kind == kTcTF32x3 ? 2.0 : 1.0;
       ctx->prof.push_back({a, b, 2.0 * m * n * (double)k,
                            8.0 * m * n + copies * esz * (double)k * (m + n), ELGB_PROF_TC_GEMM,
-                           L.st == ctx->side_stream && ctx->side_stream != nullptr});
+                           L.st == ctx->side_stream && ctx->side_stream != nullptr,
+                           ctx->stream_lane(L.st)});
     }
     return e;
   }
@@ -222,6 +227,7 @@ struct LuState {
   int panel_ctas;      // CTAs of a panel launch (fewer when it overlaps the update)
   int panel_epoch;     // panel columns published so far (slot epochs)
   LuLane main, side;   // side.st == nullptr: no look-ahead
+  LuLane swp;          // interchanges of the trailing update's second part
   T* Bc;               // companion block receiving the same row operations
   long ldbc;           // (RowEchelon's B, src/lapack_like/solve/Linear.cpp:62-71)
   int nbc;
@@ -434,6 +440,36 @@ static cudaError_t getrf_run(LuState<T>& s, int nb) {
     // deferred to the end); with look-ahead the next panel's block column
     // goes first, so only its share of the swap sits on the critical path
     const bool split = la && jb2 > 0;
+    // beside the look-ahead panel the trailing update leaves SMs to it; with
+    // trail_split, only the columns it is expected to take while the panel
+    // runs, and the rest after the panel on every SM
+    int c_mid = s.n;
+    if (split && s.trail_split && s.n > kn + jb2) {
+      // the panel of jb2 columns on m - kn rows: ~2 us per pivot step up to
+      // 16384 rows (registers), ~4.4 us above, plus ~1 ms of recursion
+      // kernels; the update at ~180 TF/s beside it (TF32x3 on all GPCs but
+      // one), rounded up to whole 256-column tiles
+      const double side_s =
+          (jb2 * ((s.m - kn) <= 16384 ? 2.1e-6 : 4.4e-6) + 1.0e-3) * s.trail_split_scale;
+      const double cols = side_s * 180e12 / (2.0 * (double)(s.m - kn) * jb);
+      const long c = (long)kn + jb2 + ((long)std::ceil(cols / 256.0)) * 256;
+      if (c < s.n) c_mid = (int)c;
+    }
+    // the interchanges of the second part's columns [c_mid, n) on the swap
+    // stream, beside everything up to that part (nothing else touches those
+    // columns in between; the stream starts after the previous block's
+    // update of them)
+    const bool swap_apart = c_mid < s.n && s.swp.st != nullptr;
+    if (swap_apart) {
+      e = cudaEventRecord(ctx->ev_iter, s.main.st);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(s.swp.st, ctx->ev_iter, 0);
+      if (e == cudaSuccess) e = apply_swaps(s, s.swp, k, jb, c_mid, s.n, 0, 0, false);
+      if (e == cudaSuccess) e = cudaEventRecord(ctx->ev_swapped, s.swp.st);
+      if (e != cudaSuccess) return e;
+    }
+    // interchanges right of the panel (left of it, earlier L columns, are
+    // deferred to the end); with look-ahead the next panel's block column
+    // goes first, so only its share of the swap sits on the critical path
     e = split ? apply_swaps(s, s.main, k, jb, kn, kn + jb2, 0, 0, false)
               : apply_swaps(s, s.main, k, jb, 0, 0, kn, s.n, true);
     if (e != cudaSuccess) return e;
@@ -450,23 +486,8 @@ static cudaError_t getrf_run(LuState<T>& s, int nb) {
       }
     }
     if (split) {
-      e = apply_swaps(s, s.main, k, jb, kn + jb2, s.n, 0, 0, true);
+      e = apply_swaps(s, s.main, k, jb, kn + jb2, swap_apart ? c_mid : s.n, 0, 0, true);
       if (e != cudaSuccess) return e;
-    }
-    // beside the look-ahead panel the trailing update leaves SMs to it; with
-    // trail_split, only the columns it is expected to take while the panel
-    // runs, and the rest after the panel on every SM
-    int c_mid = s.n;
-    if (split && s.trail_split && s.n > kn + jb2) {
-      // the panel of jb2 columns on m - kn rows: ~2 us per pivot step up to
-      // 16384 rows (registers), ~4.4 us above, plus ~1 ms of recursion
-      // kernels; the update at ~180 TF/s beside it (TF32x3 on all GPCs but
-      // one), rounded up to whole 256-column tiles
-      const double side_s =
-          (jb2 * ((s.m - kn) <= 16384 ? 2.1e-6 : 4.4e-6) + 1.0e-3) * s.trail_split_scale;
-      const double cols = side_s * 180e12 / (2.0 * (double)(s.m - kn) * jb);
-      const long c = (long)kn + jb2 + ((long)std::ceil(cols / 256.0)) * 256;
-      if (c < s.n) c_mid = (int)c;
     }
     if (split) s.main.grid_mode = s.trail_grid;
     e = update_cols(s, s.main, k, jb, kn + jb2, c_mid);
@@ -480,7 +501,8 @@ static cudaError_t getrf_run(LuState<T>& s, int nb) {
       if (e != cudaSuccess) return e;
     }
     if (c_mid < s.n) {
-      e = update_cols(s, s.main, k, jb, c_mid, s.n);
+      if (swap_apart) e = cudaStreamWaitEvent(s.main.st, ctx->ev_swapped, 0);
+      if (e == cudaSuccess) e = update_cols(s, s.main, k, jb, c_mid, s.n);
       if (e != cudaSuccess) return e;
     }
     e = update_companion(s, s.main, k, jb);
@@ -503,8 +525,8 @@ template <typename T>
 static size_t getrf_scratch_bytes(const Context* ctx, int nb, int m, int n) {
   const int cap = std::max(nb, 32);
   const size_t nblk = (size_t)(std::min(m, n) + nb - 1) / std::max(nb, 1);
-  return panel_scratch_bytes<T>(ctx->num_sms) + 2 * align256(4 * (size_t)cap * sizeof(int)) +
-         2 * align256(sizeof(int)) + align256(nblk * (size_t)m * sizeof(int)) +
+  return panel_scratch_bytes<T>(ctx->num_sms) + 3 * align256(4 * (size_t)cap * sizeof(int)) +
+         3 * align256(sizeof(int)) + align256(nblk * (size_t)m * sizeof(int)) +
          align256(defer_labels_work_ints(m, std::min(m, n), nb) * sizeof(int)) +
          align256((size_t)nb * nb * sizeof(T)) +
          align256((size_t)defer_gather_grid(ctx->num_sms) * m * sizeof(T));
@@ -534,7 +556,9 @@ static cudaError_t setup_lu_state(Context* ctx, LuState<T>& s, Carver& cv, int n
   s.main.pair_count = cv.take<int>(1);
   s.side.pairs = cv.take<int>(4 * (size_t)cap);
   s.side.pair_count = cv.take<int>(1);
-  if (!s.side.pair_count) return cudaErrorMemoryAllocation;
+  s.swp.pairs = cv.take<int>(4 * (size_t)cap);
+  s.swp.pair_count = cv.take<int>(1);
+  if (!s.swp.pair_count) return cudaErrorMemoryAllocation;
   return cudaSuccess;
 }
 
@@ -580,6 +604,7 @@ cudaError_t getrf(Context* ctx, int m, int n, T* A, long lda, int* ipiv, int nb,
   s.trail_split = tc && ctx->opt_trail_split && s.trail_grid == kGridSpareGpc;
   s.trail_split_scale = ctx->opt_trail_split > 1 ? ctx->opt_trail_split / 100.0 : 1.1;
   s.inv_trsm = tc && ctx->opt_inv_trsm && s.ninv;
+  if (la && ctx->opt_swap_stream) s.swp.st = ctx->swap_stream;
   if (la) {
     s.side.st = ctx->side_stream;
     s.side.grid_mode = ctx->opt_trail_grid >= 2 ? kGridTiles : kGridSmall;
@@ -1205,8 +1230,14 @@ int ElGBCreate(ElGBContext* out, int device) {
       cudaDeviceGetStreamPriorityRange(&least_prio, &greatest_prio) != cudaSuccess ||
       cudaStreamCreateWithPriority(&c->side_stream, cudaStreamNonBlocking, greatest_prio) !=
           cudaSuccess ||
+      // the deferred share of a block's interchanges at the lowest priority:
+      // it only has to finish before the trailing update's second part
+      cudaStreamCreateWithPriority(&c->swap_stream, cudaStreamNonBlocking, least_prio) !=
+          cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_iter, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_swapped, cudaEventDisableTiming) != cudaSuccess ||
       cudaMalloc(&c->status, sizeof(elgb::DevStatus)) != cudaSuccess ||
       cudaMallocHost(&c->h_status, sizeof(elgb::DevStatus)) != cudaSuccess ||
       // zeroed on the legacy stream, which the context's non-blocking
@@ -1316,7 +1347,7 @@ int ElGBProfileRecords(ElGBContext ctx, int cap, int* count, float* start_ms, fl
       start_ms[n] = t0;
       dur_ms[n] = d;
       tag[n] = r.tag;
-      side[n] = r.side ? 1 : 0;
+      side[n] = r.lane;
     }
     ++n;
   }
@@ -1359,6 +1390,9 @@ int ElGBSetOption(ElGBContext ctx, int option, int value) {
       return 0;
     case ELGB_OPT_INV_TRSM:
       ctx->opt_inv_trsm = value ? 1 : 0;
+      return 0;
+    case ELGB_OPT_SWAP_STREAM:
+      ctx->opt_swap_stream = value ? 1 : 0;
       return 0;
     case ELGB_OPT_PANEL_ROWS:
       if (value < 64 || value > 1536) return elgb::kElArgError;

@@ -27,7 +27,9 @@ struct Context {
   cudaStream_t stream = nullptr;
   cudaStream_t own_stream = nullptr;
   cudaStream_t side_stream = nullptr;  // look-ahead panels run here
+  cudaStream_t swap_stream = nullptr;  // interchanges of the columns updated last
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  cudaEvent_t ev_iter = nullptr, ev_swapped = nullptr;
   void* arena = nullptr;  // growable device scratch, reused across calls
   size_t arena_bytes = 0;
   DevStatus* status = nullptr;    // device status word of the last call
@@ -40,6 +42,7 @@ struct Context {
   int opt_trail_grid = 2;         // ElGBSetOption(ELGB_OPT_TRAIL_GRID)
   int opt_trail_split = 1;        // ElGBSetOption(ELGB_OPT_TRAIL_SPLIT)
   int opt_inv_trsm = 0;           // ElGBSetOption(ELGB_OPT_INV_TRSM)
+  int opt_swap_stream = 0;        // ElGBSetOption(ELGB_OPT_SWAP_STREAM)
   // ElGBSetOption(ELGB_OPT_PANEL_TRACE): per-column leaf-panel timestamps of
   // the last factorization, 4 per column, for its first trace_cols columns
   unsigned long long* trace_buf = nullptr;
@@ -55,7 +58,11 @@ struct Context {
     double flops, bytes;
     int tag;            // ELGB_PROF_*
     bool side = false;  // recorded on the look-ahead panel stream
+    int lane = 0;       // 0 main stream, 1 look-ahead stream, 2 swap stream
   };
+  int stream_lane(cudaStream_t st) const {
+    return (side_stream && st == side_stream) ? 1 : (swap_stream && st == swap_stream) ? 2 : 0;
+  }
   struct ProfSum {
     long long launches = 0;
     double ms = 0, flops = 0, bytes = 0;

@@ -106,7 +106,14 @@ int ElGBSetBlocksize(int nb);
  *                       per block.  1 shortens the LU (236 vs 241 ms at
  *                       n = 32768) but the product's rounding grows with
  *                       |N|: the factors are less accurate and refinement
- *                       took one more iteration (5 vs 4), a net loss. */
+ *                       took one more iteration (5 vs 4), a net loss.
+ *   ELGB_OPT_SWAP_STREAM 0 (default): a block's interchanges run on the
+ *                       main stream; 1: with look-ahead and the split
+ *                       trailing update, those on the columns updated after
+ *                       the panel run on a third stream (lowest priority)
+ *                       beside the panel and the first part of the update.
+ *                       Same factors; no measured change in the LU at
+ *                       n = 32768 (225.8 vs 225.9 ms), so off. */
 enum {
   ELGB_OPT_LOOKAHEAD = 1,
   ELGB_OPT_PANEL_CTAS = 2,
@@ -118,7 +125,8 @@ enum {
   ELGB_OPT_TRAIL_GRID = 8,
   ELGB_OPT_PANEL_ROWS = 9,
   ELGB_OPT_TRAIL_SPLIT = 10,
-  ELGB_OPT_INV_TRSM = 11
+  ELGB_OPT_INV_TRSM = 11,
+  ELGB_OPT_SWAP_STREAM = 12
 };
 int ElGBSetOption(ElGBContext ctx, int option, int value);
 
@@ -158,10 +166,11 @@ enum {
 int ElGBProfileTag(ElGBContext ctx, int tag, long long* launches, double* ms,
                    double* flops, double* bytes);
 /* After ElGBProfileStop: the event-bracketed launch groups one by one, in
- * issue order (the timeline of both streams).  Fills up to cap records:
+ * issue order (the timeline of the streams).  Fills up to cap records:
  * start (ms after the first group's start), duration (ms), tag (the family
- * above) and side (1 on the look-ahead panel stream); *count receives the
- * number of groups recorded. */
+ * above) and side (the stream: 0 main, 1 look-ahead panel stream, 2 the
+ * stream of the interchanges deferred to the second part of a split
+ * trailing update); *count receives the number of groups recorded. */
 int ElGBProfileRecords(ElGBContext ctx, int cap, int* count, float* start_ms,
                        float* dur_ms, int* tag, int* side);
 

@@ -183,7 +183,7 @@ def _stream_overlap(rec, segments=8):
         i = np.searchsorted(s, mid, side="right") - 1
         return (i >= 0) & (e[np.maximum(i, 0)] > mid)
 
-    m, sd = busy(rec["side"] == 0), busy(rec["side"] == 1)
+    m, sd = busy(rec["side"] != 1), busy(rec["side"] == 1)
     seg = np.minimum(((mid - t.min()) / (t.max() - t.min()) * segments).astype(int),
                      segments - 1)
     out = {}

@@ -128,3 +128,20 @@ def test_product_form_trailing_solve_factors_to_fp32_accuracy(ctx):
     assert np.linalg.norm(PA - L @ U) / np.linalg.norm(Ah) <= 1e-4
     assert np.array_equal(p1.cpu().numpy()[:512], p2.cpu().numpy()[:512])
     assert not torch.equal(A1, A2)  # the option took the other path
+
+
+def test_interchanges_on_the_swap_stream_change_nothing(ctx):
+    """ELGB_OPT_SWAP_STREAM: the interchanges of the trailing update's second
+    part run on a third stream beside the panel; each column sees the same
+    row moves before the same update, so the factors are bit-identical."""
+    n = 8192
+    A0 = _matrix(n, n, 17)
+    outs = []
+    for v in (0, 1):
+        ctx.set_option("swap_stream", v)
+        try:
+            outs.append(_lu(ctx, A0, 2))
+        finally:
+            ctx.set_option("swap_stream", 0)
+    assert torch.equal(outs[0][1], outs[1][1])
+    assert torch.equal(outs[0][0], outs[1][0])
