@@ -341,7 +341,10 @@ def gpu_arm(args, rank, world, local_rank):
     clocks = ClockSampler(local_rank)
     clocks.start()
     l0 = ctx.launches()
-    ctx.profile_start()
+    # inside the timed region only the dominant kernel is bracketed with
+    # events (for the roofline); the per-family breakdown comes from one
+    # extra, untimed, fully bracketed solve after it
+    ctx.profile_start(tags=["tc_gemm"])
     stream = torch.cuda.current_stream()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -356,6 +359,9 @@ def gpu_arm(args, rank, world, local_rank):
     prof = ctx.profile_stop()
     launches = ctx.launches() - l0
     clk = clocks.stop()
+    ctx.profile_start()
+    solve()
+    prof_all = ctx.profile_stop()
     t = e0.elapsed_time(e1) / 1e3
     tmax = t
     if dist is not None:
@@ -519,10 +525,12 @@ def gpu_arm(args, rank, world, local_rank):
     if per_bf16 and peak and tf_achieved:
         roofline["operand_ceiling_tflops"] = peak / per_bf16
         roofline["frac_of_operand_ceiling"] = tf_achieved * per_bf16 / peak
-    breakdown = {k: {"launches": v["launches"], "ms_per_step": v["ms"] / args.steps}
-                 for k, v in prof["by_kernel"].items()}
-    for k, v in prof.get("by_kernel_lookahead_stream", {}).items():
-        breakdown[k]["lookahead_stream_ms_per_step"] = v["ms"] / args.steps
+    breakdown = {k: {"launches": v["launches"], "ms_per_step": v["ms"]}
+                 for k, v in prof_all["by_kernel"].items()}
+    for k, v in prof_all.get("by_kernel_lookahead_stream", {}).items():
+        breakdown[k]["lookahead_stream_ms_per_step"] = v["ms"]
+    breakdown["note"] = ("one extra solve after the timed region with every launch group "
+                         "bracketed by events (the brackets lengthen it by ~5 %)")
     cpu = None
     if args.cpu_baseline == "on":
         ns = min(args.cpu_n, n)

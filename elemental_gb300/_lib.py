@@ -85,6 +85,7 @@ def load():
     _sig(lib, "ElGBSetOption", c_int, vp, c_int, c_int)
     _sig(lib, "ElGBPanelTrace", c_int, vp, vp, c_int)
     _sig(lib, "ElGBProfileStart", c_int, vp)
+    _sig(lib, "ElGBProfileStartTags", c_int, vp, ctypes.c_uint)
     _sig(lib, "ElGBProfileStop", c_int, vp, P(c_ll), P(c_double), P(c_double), P(c_double))
     _sig(lib, "ElGBProfileTag", c_int, vp, c_int, P(c_ll), P(c_double), P(c_double),
          P(c_double))

@@ -33,8 +33,8 @@ cudaEvent_t Context::next_event() {
   return ev_pool[ev_used++];
 }
 
-int Context::prof_begin(cudaStream_t st) {
-  if (!prof_on) return -1;
+int Context::prof_begin(cudaStream_t st, int tag) {
+  if (!prof_wants(tag)) return -1;
   cudaEvent_t a = next_event();
   if (!a) return -1;
   cudaEventRecord(a, st);
@@ -177,7 +177,7 @@ static cudaError_t gemm_sub(Context* ctx, const LuLane& L, int m, int n, int k, 
                             long lda, const double* B, long ldb, double* C, long ldc,
                             bool trailing = false) {
   (void)trailing;
-  const int pi = ctx->prof_begin(L.st);
+  const int pi = ctx->prof_begin(L.st, ELGB_PROF_GEMM_SIMT);
   LANE_CHECK(launch_gemm_simt<double>(false, false, m, n, k, -1.0, A, lda, B, ldb, 1.0, C, ldc,
                                       0, L.st), 1);
   ctx->prof_end(pi, L.st, ELGB_PROF_GEMM_SIMT, 2.0 * m * n * (double)k, 24.0 * m * n);
@@ -192,7 +192,7 @@ static cudaError_t gemm_sub(Context* ctx, const LuLane& L, int m, int n, int k, 
   if (kind >= 0 && m >= 64 && n >= 64 && k >= 16) {
     int nl = 0;
     cudaEvent_t a = nullptr, b = nullptr;
-    if (ctx->prof_on) {
+    if (ctx->prof_wants(ELGB_PROF_TC_GEMM)) {
       a = ctx->next_event();
       b = ctx->next_event();
     }
@@ -209,7 +209,7 @@ static cudaError_t gemm_sub(Context* ctx, const LuLane& L, int m, int n, int k, 
     }
     return e;
   }
-  const int pi = ctx->prof_begin(L.st);
+  const int pi = ctx->prof_begin(L.st, ELGB_PROF_GEMM_SIMT);
   LANE_CHECK(launch_gemm_simt<float>(false, false, m, n, k, -1.f, A, lda, B, ldb, 1.f, C, ldc,
                                      0, L.st), 1);
   ctx->prof_end(pi, L.st, ELGB_PROF_GEMM_SIMT, 2.0 * m * n * (double)k, 12.0 * m * n);
@@ -255,7 +255,7 @@ static cudaError_t trsm_llnu(Context* ctx, const LuLane& L, const T* Lm, long ld
   if (ncols <= 0) return cudaSuccess;
   for (int i0 = 0; i0 < nb; i0 += 128) {
     const int ib = std::min(128, nb - i0);
-    const int pi = ctx->prof_begin(L.st);
+    const int pi = ctx->prof_begin(L.st, ELGB_PROF_TRSM);
     LANE_CHECK(launch_trsm_block<T>(Lm + i0 + (long)i0 * ldl, ldl, Bm + i0, ldb, ib, ncols,
                                     true, true, false, false, L.st), 1);
     ctx->prof_end(pi, L.st, ELGB_PROF_TRSM, (double)ib * ib * ncols,
@@ -278,7 +278,7 @@ static cudaError_t apply_swaps(LuState<T>& s, const LuLane& L, int c0, int w, in
                                int b0, int b1, bool companion) {
   Context* ctx = s.ctx;
   if (s.nopiv) return cudaSuccess;  // every interchange is the identity
-  const int pi = ctx->prof_begin(L.st);
+  const int pi = ctx->prof_begin(L.st, ELGB_PROF_SWAP);
   LANE_CHECK(launch_build_swap_pairs(s.ipiv + c0, c0, w, L.pairs, L.pair_count, L.st), 1);
   if ((a1 > a0) || (b1 > b0))
     LANE_CHECK(launch_apply_swap_pairs<T>(s.A, s.lda, a0, a1, b0, b1, L.pairs, L.pair_count, w,
@@ -318,7 +318,7 @@ static cudaError_t panel_rec(LuState<T>& s, const LuLane& L, int c0, int w, int 
   Context* ctx = s.ctx;
   const int lw = leaf_width(s, b0);
   if (w <= lw) {
-    const int pi = ctx->prof_begin(L.st);
+    const int pi = ctx->prof_begin(L.st, ELGB_PROF_PANEL);
     bool done = false, swapped = false;
     if constexpr (sizeof(T) == 4) {
       if (s.tournament && !s.nopiv) {
@@ -510,10 +510,10 @@ static cudaError_t getrf_run(LuState<T>& s, int nb) {
   }
   if (s.nopiv) return cudaSuccess;
   // every block column of L takes the later panels' interchanges at once
-  int pi = ctx->prof_begin(s.main.st);
+  int pi = ctx->prof_begin(s.main.st, ELGB_PROF_SWAP);
   LANE_CHECK(launch_defer_labels(s.ipiv, s.m, minDim, nb, s.dlab, s.dwork, s.main.st), 2);
   ctx->prof_end(pi, s.main.st, ELGB_PROF_SWAP, 0.0, 0.0);
-  pi = ctx->prof_begin(s.main.st);
+  pi = ctx->prof_begin(s.main.st, ELGB_PROF_SWAP);
   LANE_CHECK(launch_defer_gather<T>(s.A, s.lda, s.m, minDim, nb, s.dlab, s.dtmp,
                                     defer_gather_grid(ctx->num_sms), s.main.st), 1);
   ctx->prof_end(pi, s.main.st, ELGB_PROF_SWAP, 0.0,
@@ -1282,10 +1282,13 @@ int ElGBStatus(ElGBContext ctx, int* info, int* err) {
   return 0;
 }
 
-int ElGBProfileStart(ElGBContext ctx) {
+int ElGBProfileStart(ElGBContext ctx) { return ElGBProfileStartTags(ctx, ~0u); }
+
+int ElGBProfileStartTags(ElGBContext ctx, unsigned tags) {
   if (!ctx) return elgb::kElArgError;
   ctx->prof.clear();
   ctx->ev_used = 0;
+  ctx->prof_mask = tags;
   ctx->prof_on = true;
   return 0;
 }

@@ -70,9 +70,11 @@ struct Context {
   ProfSum prof_sum[16];
   // Brackets the launches issued between begin and end on `st` when
   // profiling is on; returns -1 when off.
-  int prof_begin(cudaStream_t st);
+  int prof_begin(cudaStream_t st, int tag);
   void prof_end(int idx, cudaStream_t st, int tag, double flops, double bytes);
   bool prof_on = false;
+  unsigned prof_mask = ~0u;  // families (1 << ELGB_PROF_*) bracketed while prof_on
+  bool prof_wants(int tag) const { return prof_on && ((prof_mask >> tag) & 1u); }
   std::vector<ProfRec> prof;        // records of the current window
   std::vector<cudaEvent_t> ev_pool;  // reusable events
   size_t ev_used = 0;

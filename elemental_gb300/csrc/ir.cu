@@ -250,7 +250,7 @@ static cudaError_t lowprec_solve(Context* ctx, int n, int q, Ws& w, const double
   ctx->launches += 1;
   IR_CHECK(cudaGetLastError());
   // (P^T L U)^{-1}: L then U, each one launch
-  const int pi = ctx->prof_begin(ctx->stream);
+  const int pi = ctx->prof_begin(ctx->stream, ELGB_PROF_SOLVE);
   IR_CHECK(launch_trsv_persistent<float>(w.Af, n, w.Dl, w.Rf, n, n, q, true, w.ticket, w.tags,
                                          ++w.epoch, ctx->status, ctx->num_sms, ctx->stream));
   IR_CHECK(launch_trsv_persistent<float>(w.Af, n, w.Du, w.Rf, n, n, q, false, w.ticket,
@@ -280,7 +280,7 @@ static void backward_errors(const std::vector<double>& nr, const std::vector<dou
 static cudaError_t ir_residual(Context* ctx, const Ws& w, int n, int q, const double* A,
                                long lda, const double* X, long ldx, const double* B, long ldb,
                                double* R, long ldr) {
-  const int pr = ctx->prof_begin(ctx->stream);
+  const int pr = ctx->prof_begin(ctx->stream, ELGB_PROF_RESIDUAL);
   cudaError_t e;
   if (w.df) {
     e = launch_residual_df(n, q, w.Ahi, w.Alo, w.astat + 1, X, ldx, B, ldb, R, ldr, w.Xs,
@@ -388,7 +388,7 @@ cudaError_t refined_solve(Context* ctx, int n, const double* A, long lda, int nr
     }
     // 1. low-precision factorization of an FP32 copy of A; the same pass over
     // A makes its FP32 words for the double-float residual and its norms
-    const int pc = ctx->prof_begin(ctx->stream);
+    const int pc = ctx->prof_begin(ctx->stream, ELGB_PROF_CONVERT);
     if (df) {
       IR_CHECK(launch_split_a(A, lda, n, w.Af, w.Ahi, w.Alo, w.spart, w.astat, ctx->stream));
       ctx->launches += 2;

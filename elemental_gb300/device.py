@@ -130,8 +130,16 @@ class Context:
     def launches(self):
         return int(self.lib.ElGBLaunchCount(self.h))
 
-    def profile_start(self):
-        self._rc(self.lib.ElGBProfileStart(self.h), "ProfileStart")
+    def profile_start(self, tags=None):
+        """Brackets every launch group (tags None) or only the named kernel
+        families (PROFILE_TAGS keys) with CUDA events until profile_stop."""
+        if tags is None:
+            self._rc(self.lib.ElGBProfileStart(self.h), "ProfileStart")
+        else:
+            mask = 0
+            for t in tags:
+                mask |= 1 << PROFILE_TAGS[t]
+            self._rc(self.lib.ElGBProfileStartTags(self.h, mask), "ProfileStartTags")
 
     def profile_stop(self):
         """Summed event timing of the tensor-core GEMM launches since

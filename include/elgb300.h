@@ -144,6 +144,11 @@ long long ElGBLaunchCount(ElGBContext ctx);
  * summed device time (ms) and their algorithmic flops (2 m n k) and bytes
  * (C read + write, packed operands read). */
 int ElGBProfileStart(ElGBContext ctx);
+/* The same for the kernel families whose bit (1 << ELGB_PROF_*, below) is set
+ * in tags only: fewer events in the timeline, so a timed region perturbed
+ * less (bracketing every launch group of a refined solve at n = 32768 costs
+ * ~14 ms of its ~295). */
+int ElGBProfileStartTags(ElGBContext ctx, unsigned tags);
 int ElGBProfileStop(ElGBContext ctx, long long* launches, double* ms,
                     double* flops, double* bytes);
 /* After ElGBProfileStop: the same sums for one kernel family (event-bracketed

@@ -96,7 +96,18 @@ def case_refine(ctx, a):
         info.update(ctx.refined_solve(A, B, precision="fp32", method=a.method)[1])
 
     ms = _timed(run)
-    return dict(case="refine", n=a.n, nrhs=a.nrhs, method=a.method, ms=ms, **info)
+    out = dict(case="refine", n=a.n, nrhs=a.nrhs, method=a.method, ms=ms, **info)
+    if a.records:
+        import numpy as np
+
+        ctx.profile_start()
+        out["ms_profiled"] = _timed(run)
+        ctx.profile_stop()
+        rec = ctx.profile_records()
+        np.save(a.records, rec)
+        out["tagged_ms"] = {str(t): round(float(rec["dur_ms"][rec["tag"] == t].sum()), 2)
+                            for t in sorted(set(rec["tag"].tolist()))}
+    return out
 
 
 def case_batched(ctx, a):
