@@ -1397,6 +1397,10 @@ int ElGBSetOption(ElGBContext ctx, int option, int value) {
     case ELGB_OPT_SWAP_STREAM:
       ctx->opt_swap_stream = value ? 1 : 0;
       return 0;
+    case ELGB_OPT_PANEL_PUSH:
+      if (value < 0 || value > 2) return elgb::kElArgError;
+      elgb::g_panel_push = value;
+      return 0;
     case ELGB_OPT_PANEL_ROWS:
       if (value < 64 || value > 1536) return elgb::kElArgError;
       elgb::g_panel_rows = value;

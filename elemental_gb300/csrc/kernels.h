@@ -53,6 +53,9 @@ extern int g_panel_cluster;
 extern int g_panel_rows;
 // FP32 panels with the rows in registers (1, default) or in shared memory.
 extern int g_panel_regs;
+// register leaf panels: candidates pushed into every CTA with asynchronous
+// DSMEM stores on an mbarrier (1) or read after a cluster barrier (0)
+extern int g_panel_push;
 
 // getf2 on a w-wide panel (w <= 32): El's lu::Panel
 // (src/lapack_like/factor/LU/Panel.hpp:15-59) as one cooperative launch.

@@ -19,6 +19,7 @@ int g_panel_rows = 1024;
 // FP32 panels with the rows in registers (ElGBSetOption(ELGB_OPT_PANEL_REGS)):
 // 1 cooperative, 2 on a cluster where one fits (the default).
 int g_panel_regs = 2;
+int g_panel_push = 1;
 
 template <typename T>
 __device__ __forceinline__ T absv(T x) { return x < T(0) ? -x : x; }
@@ -822,17 +823,79 @@ __device__ __forceinline__ void ld_cluster_head(uint32_t addr, float& v, int& r)
   asm volatile("ld.shared::cluster.v2.b32 {%0, %1}, [%2];" : "=f"(v), "=r"(r) : "r"(addr));
 }
 
-template <int W, int RPT>
+// Push exchange: every CTA sends its candidate (and the owner of row j that
+// row) into every CTA's receive buffer with asynchronous distributed-shared-
+// memory stores that complete on the receiver's mbarrier, so a step waits
+// for its data once (no cluster barrier, no remote read round trip).
+struct __align__(16) PushSlot {
+  float cand[kPanelW];
+  float val;
+  int row;
+  int pad[2];
+};
+
+__device__ __forceinline__ void st_async_v4(uint32_t addr, float x, float y, float z, float w,
+                                            uint32_t bar) {
+  asm volatile(
+      "st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.f32 [%0], {%1, %2, %3, %4}, "
+      "[%5];" ::"r"(addr),
+      "f"(x), "f"(y), "f"(z), "f"(w), "r"(bar)
+      : "memory");
+}
+__device__ __forceinline__ void st_async_head(uint32_t addr, float v, int r, uint32_t bar) {
+  asm volatile(
+      "st.async.shared::cluster.mbarrier::complete_tx::bytes.v2.b32 [%0], {%1, %2}, [%3];" ::"r"(
+          addr),
+      "r"(__float_as_uint(v)), "r"(r), "r"(bar)
+      : "memory");
+}
+// test_wait does not suspend the thread: the waiting warps leave the moment
+// the phase completes (a suspended try_wait was seen to wake late)
+__device__ __forceinline__ bool mbar_try_wait_cluster(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n"
+      ".reg .pred p;\n"
+      "mbarrier.test_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
+      "selp.u32 %0, 1, 0, p;\n"
+      "}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Sends W values (a row held in registers) to slot `slot_off` of every CTA's
+// buffer at `buf` (same layout in every CTA), completing on each CTA's `bar`.
+template <int W>
+__device__ __forceinline__ void push_row(const float (&v)[W], const void* buf, uint32_t slot_off,
+                                         const uint64_t* bar, int G) {
+  for (int d = 0; d < G; ++d) {
+    const uint32_t dst = cluster_map(buf, (unsigned)d) + slot_off;
+    const uint32_t rb = cluster_map(bar, (unsigned)d);
+#pragma unroll
+    for (int c = 0; c < W; c += 4) st_async_v4(dst + 4u * c, v[c], v[c + 1], v[c + 2], v[c + 3], rb);
+  }
+}
+
+template <int W, int RPT, bool PUSH>
 __global__ void __launch_bounds__(kRcThreads, 1)
 getf2_panel_cluster_reg_kernel(PanelParams<float> p) {
   static_assert(W <= kPanelW && W % 4 == 0 && W * RPT <= 64, "slot layout, registers");
   __shared__ RcSlot slots[2];
+  // PUSH: receive buffers (slot g = CTA g's candidate), row j, their mbarriers
+  __shared__ PushSlot s_in[PUSH ? 2 : 1][PUSH ? 16 : 1];
+  __shared__ __align__(16) float s_din[PUSH ? 2 : 1][W];
+  __shared__ __align__(16) float s_stage[PUSH ? 2 : 1][2][W];  // rows being sent
+  __shared__ __align__(8) uint64_t s_mbar[2];
   __shared__ __align__(16) float s_d[W];
   __shared__ __align__(16) float s_rows[16][W];
   __shared__ float s_gv[32];
   __shared__ int s_gr[32];
-  __shared__ float s_rv[33];
-  __shared__ int s_rr[33];
+  // per-step CTA argmax buffers, alternating by column: with the push
+  // exchange nothing else keeps a fast warp from the next column's writes
+  // while a slow one still reads
+  __shared__ float s_rv[2][33];
+  __shared__ int s_rr[2][33];
   __shared__ int s_piv[W];                     // the pivot of each column (panel row)
   __shared__ int s_dst[2 * W], s_src[2 * W];   // the interchanges' net row moves
   __shared__ int s_nmove;
@@ -866,75 +929,152 @@ getf2_panel_cluster_reg_kernel(PanelParams<float> p) {
         br = grow[i];
       }
     }
-  block_argmax(bv, br, s_rv, s_rr);
-  cluster_barrier();  // every CTA of the cluster is running
+  if (PUSH && tid == 0) {
+    tc::mbar_init(&s_mbar[0], 1);
+    tc::mbar_init(&s_mbar[1], 1);
+    tc::fence_mbar_init();
+  }
+  block_argmax(bv, br, s_rv[0], s_rr[0]);
+  cluster_barrier();  // every CTA of the cluster is running (and its mbarriers set)
+  bool dead = false;  // PUSH: a wait timed out (recorded); later waits are skipped
+  (void)dead;
 
 #pragma unroll
   for (int j = 0; j < W; ++j) {
     if (j < w) {
       RcSlot* my = &slots[j & 1];
+      const int bb = j & 1;
+      (void)bb;
       unsigned long long* tr =
           (p.s.trace && b == 0 && tid == 0) ? p.s.trace + 4 * (long)j : nullptr;
       if (tr) tr[0] = globaltimer_ns();
-      // 1. publish from the registers of the rows' owners
+      if constexpr (PUSH) {
+        // 1. every CTA's candidate (zeros with an empty head if it has none)
+        // and row j go straight into every CTA's buffer bb: the owner stages
+        // its row in shared memory, then lane d of its warp sends it to CTA d
+        if (tid == 0)
+          tc::mbar_arrive_expect_tx(&s_mbar[bb], (uint32_t)(G * (8 + 4 * W) + 4 * W));
 #pragma unroll
-      for (int i = 0; i < RPT; ++i) {
-        if (grow[i] >= 0 && grow[i] == br)
+        for (int i = 0; i < RPT; ++i) {
+          if (grow[i] >= 0 && grow[i] == br)
 #pragma unroll
-          for (int c = 0; c < W; ++c) my->cand[c] = a[i][c];
-        if (grow[i] == j)
+            for (int c = 0; c < W; ++c) s_stage[bb][0][c] = a[i][c];
+          if (grow[i] == j)
 #pragma unroll
-          for (int c = 0; c < W; ++c) my->diag[c] = a[i][c];
-      }
-      if (tid == 0) {
-        my->val = bv;
-        my->row = br;
-      }
-      cluster_arrive();
-      if (tr) tr[1] = globaltimer_ns();
-      cluster_wait();
-      // 2. thread g < C reads CTA g's slot: head and candidate row in one
-      // round trip, row j (its owner's slot only) in a second
-      // (row j comes from its owner's slot through thread 32, in warp 1, at
-      // the same time)
-      if (tid < G || tid == 32) {
-        const unsigned src = tid < G ? (unsigned)tid : (unsigned)(j / R);
-        const uint32_t base = cluster_map(my, src);
-        float4 cr[W / 4];
-        if (tid < G) {
-          float gv;
-          int gr;
-          ld_cluster_head(base + (uint32_t)offsetof(RcSlot, val), gv, gr);
-#pragma unroll
-          for (int c = 0; c < W / 4; ++c)
-            cr[c] = ld_cluster_v4(base + (uint32_t)offsetof(RcSlot, cand) + 16u * c);
-          s_gv[tid] = gv;
-          s_gr[tid] = gr;
-#pragma unroll
-          for (int c = 0; c < W / 4; ++c) reinterpret_cast<float4*>(s_rows[tid])[c] = cr[c];
-        } else {
-#pragma unroll
-          for (int c = 0; c < W / 4; ++c)
-            cr[c] = ld_cluster_v4(base + (uint32_t)offsetof(RcSlot, diag) + 16u * c);
-#pragma unroll
-          for (int c = 0; c < W / 4; ++c) reinterpret_cast<float4*>(s_d)[c] = cr[c];
+            for (int c = 0; c < W; ++c) s_stage[bb][1][c] = a[i][c];
         }
+        if (br < 0 && tid == 0)
+#pragma unroll
+          for (int c = 0; c < W; ++c) s_stage[bb][0][c] = 0.f;
+        __syncwarp();
+        const int warp = tid >> 5;
+        const int cand_warp = br >= 0 ? ((br - rb) & (kRcThreads - 1)) >> 5 : 0;
+        const int diag_warp = (j >= rb && j < re) ? ((j - rb) & (kRcThreads - 1)) >> 5 : -1;
+        if (lane < G && (warp == cand_warp || warp == diag_warp)) {
+          const uint32_t rbar = cluster_map(&s_mbar[bb], (unsigned)lane);
+          if (warp == cand_warp) {
+            const uint32_t dst =
+                cluster_map(&s_in[bb][0], (unsigned)lane) + (uint32_t)(b * sizeof(PushSlot));
+#pragma unroll
+            for (int c = 0; c < W; c += 4) {
+              const float4 v = *reinterpret_cast<const float4*>(&s_stage[bb][0][c]);
+              st_async_v4(dst + 4u * c, v.x, v.y, v.z, v.w, rbar);
+            }
+            st_async_head(dst + (uint32_t)offsetof(PushSlot, val), bv, br, rbar);
+          }
+          if (warp == diag_warp) {
+            const uint32_t dst = cluster_map(&s_din[bb][0], (unsigned)lane);
+#pragma unroll
+            for (int c = 0; c < W; c += 4) {
+              const float4 v = *reinterpret_cast<const float4*>(&s_stage[bb][1][c]);
+              st_async_v4(dst + 4u * c, v.x, v.y, v.z, v.w, rbar);
+            }
+          }
+        }
+        if (tr) tr[1] = globaltimer_ns();
+        // 2. this step's buffer is complete (bounded wait)
+        const uint32_t mb = tc::smem_u32(&s_mbar[bb]), par = (uint32_t)((j >> 1) & 1);
+        if (!dead && !mbar_try_wait_cluster(mb, par)) {
+          const unsigned long long t0 = globaltimer_ns();
+          while (!mbar_try_wait_cluster(mb, par)) {
+            if (globaltimer_ns() - t0 > kSpinLimitNs) {
+              atomicCAS(&p.st->err, 0, (int)kErrMbarTimeout);
+              p.st->err_where = 40;
+              dead = true;
+              break;
+            }
+          }
+        }
+        if (tr) tr[2] = globaltimer_ns();
+      } else {
+        // 1. publish from the registers of the rows' owners
+  #pragma unroll
+        for (int i = 0; i < RPT; ++i) {
+          if (grow[i] >= 0 && grow[i] == br)
+  #pragma unroll
+            for (int c = 0; c < W; ++c) my->cand[c] = a[i][c];
+          if (grow[i] == j)
+  #pragma unroll
+            for (int c = 0; c < W; ++c) my->diag[c] = a[i][c];
+        }
+        if (tid == 0) {
+          my->val = bv;
+          my->row = br;
+        }
+        cluster_arrive();
+        if (tr) tr[1] = globaltimer_ns();
+        cluster_wait();
+        // 2. thread g < C reads CTA g's slot: head and candidate row in one
+        // round trip, row j (its owner's slot only) in a second
+        // (row j comes from its owner's slot through thread 32, in warp 1, at
+        // the same time)
+        if (tid < G || tid == 32) {
+          const unsigned src = tid < G ? (unsigned)tid : (unsigned)(j / R);
+          const uint32_t base = cluster_map(my, src);
+          float4 cr[W / 4];
+          if (tid < G) {
+            float gv;
+            int gr;
+            ld_cluster_head(base + (uint32_t)offsetof(RcSlot, val), gv, gr);
+  #pragma unroll
+            for (int c = 0; c < W / 4; ++c)
+              cr[c] = ld_cluster_v4(base + (uint32_t)offsetof(RcSlot, cand) + 16u * c);
+            s_gv[tid] = gv;
+            s_gr[tid] = gr;
+  #pragma unroll
+            for (int c = 0; c < W / 4; ++c) reinterpret_cast<float4*>(s_rows[tid])[c] = cr[c];
+          } else {
+  #pragma unroll
+            for (int c = 0; c < W / 4; ++c)
+              cr[c] = ld_cluster_v4(base + (uint32_t)offsetof(RcSlot, diag) + 16u * c);
+  #pragma unroll
+            for (int c = 0; c < W / 4; ++c) reinterpret_cast<float4*>(s_d)[c] = cr[c];
+          }
+        }
+        __syncthreads();
+        if (tr) tr[2] = globaltimer_ns();
       }
-      __syncthreads();
-      if (tr) tr[2] = globaltimer_ns();
       // 3. the pivot (every warp, identical result)
       int piv;
       {
         float v = -1.f;
         int r = -1;
-        if (lane < G && argmax_better(s_gv[lane], s_gr[lane], v, r)) {
-          v = s_gv[lane];
-          r = s_gr[lane];
+        const float hv = PUSH ? (lane < G ? s_in[bb & (PUSH ? 1 : 0)][lane & 15].val : -1.f)
+                              : (lane < G ? s_gv[lane] : -1.f);
+        const int hr = PUSH ? (lane < G ? s_in[bb & (PUSH ? 1 : 0)][lane & 15].row : -1)
+                            : (lane < G ? s_gr[lane] : -1);
+        if (lane < G && argmax_better(hv, hr, v, r)) {
+          v = hv;
+          r = hr;
         }
         warp_argmax(v, r);
-        piv = (r < 0) ? j : r;
+        piv = (r < j || r >= p.mp) ? j : r;  // (r < 0: no candidate; else r >= j)
       }
-      const float* urow = (piv == j) ? s_d : s_rows[piv / R];
+      const float* drow = PUSH ? s_din[bb & (PUSH ? 1 : 0)] : s_d;
+      const float* urow = (piv == j)
+                              ? drow
+                              : (PUSH ? s_in[bb & (PUSH ? 1 : 0)][(piv / R) & 15].cand
+                                      : s_rows[piv / R]);
       // (the pivots go to global memory after the last column: a global store
       // here would hold up the release of thread 0's next cluster arrive)
       if (tid == 0) s_piv[j] = piv;
@@ -956,7 +1096,7 @@ getf2_panel_cluster_reg_kernel(PanelParams<float> p) {
         }
         if (piv != j && row == piv)  // the pivot row's position takes old row j
 #pragma unroll
-          for (int c = 0; c < W; ++c) a[i][c] = s_d[c];
+          for (int c = 0; c < W; ++c) a[i][c] = drow[c];
         if (row <= j) continue;
         float l = a[i][j];
         if (!singular) l *= inv;
@@ -971,11 +1111,13 @@ getf2_panel_cluster_reg_kernel(PanelParams<float> p) {
           }
         }
       }
-      // every warp reduces the CTA's candidates itself (one barrier).  The
-      // next column's cluster barrier orders every read above (s_d, s_rows,
-      // s_rv) before the gather and the per-warp writes that refill them:
-      // each thread reads before it arrives, they write after the wait.
-      block_argmax_nolead(bv, br, s_rv, s_rr);
+      // every warp reduces the CTA's candidates itself (one barrier).  Its
+      // buffers alternate by column; the exchange buffers of this column are
+      // refilled only after every CTA has passed this barrier (cluster
+      // barrier: each thread reads before it arrives, the gather writes
+      // after the wait; push: the next-but-one column's data is sent only
+      // after the sender has received this CTA's next column).
+      block_argmax_nolead(bv, br, s_rv[bb], s_rr[bb]);
       if (tr) tr[3] = globaltimer_ns();
     }
   }
@@ -1141,8 +1283,11 @@ static cudaError_t launch_getf2_panel_cluster_reg(float* A, long lda, int mp, in
   const int R = ceil_div(mp, C);
   const bool narrow = w <= 16 && R > 2 * kRcThreads;  // 16 columns, 4 rows a thread
   if (R > (narrow ? 4 : 2) * kRcThreads) return cudaErrorNotSupported;
-  auto kern = narrow ? getf2_panel_cluster_reg_kernel<16, 4>
-                     : getf2_panel_cluster_reg_kernel<kPanelW, 2>;
+  const bool push = C <= 16 && (g_panel_push == 1 || (g_panel_push == 2 && !narrow));
+  auto kern = narrow ? (push ? getf2_panel_cluster_reg_kernel<16, 4, true>
+                             : getf2_panel_cluster_reg_kernel<16, 4, false>)
+                     : (push ? getf2_panel_cluster_reg_kernel<kPanelW, 2, true>
+                             : getf2_panel_cluster_reg_kernel<kPanelW, 2, false>);
   cudaError_t e = cudaSuccess;
   if (C > 8) e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   if (e != cudaSuccess) return e;
@@ -1159,10 +1304,12 @@ static cudaError_t launch_getf2_panel_cluster_reg(float* A, long lda, int mp, in
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   // whether a cluster of C fits, asked once per device, variant and C
-  static signed char fits[64][2][17] = {};
+  static signed char fits[64][4][17] = {};
   int dev = 0;
   cudaGetDevice(&dev);
-  signed char* f = (dev >= 0 && dev < 64 && C <= 16) ? &fits[dev][narrow ? 1 : 0][C] : nullptr;
+  signed char* f = (dev >= 0 && dev < 64 && C <= 16)
+                       ? &fits[dev][(narrow ? 2 : 0) + (push ? 1 : 0)][C]
+                       : nullptr;
   bool ok = f && *f > 0;
   if (!f || *f == 0) {
     int nclusters = 0;

@@ -113,7 +113,15 @@ int ElGBSetBlocksize(int nb);
  *                       the panel run on a third stream (lowest priority)
  *                       beside the panel and the first part of the update.
  *                       Same factors; no measured change in the LU at
- *                       n = 32768 (225.8 vs 225.9 ms), so off. */
+ *                       n = 32768 (225.8 vs 225.9 ms), so off.
+ *   ELGB_OPT_PANEL_PUSH 1 (default): the register leaf panels exchange each
+ *                       column's candidates by pushing them into every CTA
+ *                       of the cluster (asynchronous DSMEM stores completing
+ *                       on the receiver's mbarrier); 0: each CTA publishes
+ *                       into its own slot and the others read it after a
+ *                       cluster barrier; 2: push for 32-column leaves only.
+ *                       Same pivots and factors.  Process-wide, like
+ *                       ELGB_OPT_PANEL_REGS. */
 enum {
   ELGB_OPT_LOOKAHEAD = 1,
   ELGB_OPT_PANEL_CTAS = 2,
@@ -126,7 +134,8 @@ enum {
   ELGB_OPT_PANEL_ROWS = 9,
   ELGB_OPT_TRAIL_SPLIT = 10,
   ELGB_OPT_INV_TRSM = 11,
-  ELGB_OPT_SWAP_STREAM = 12
+  ELGB_OPT_SWAP_STREAM = 12,
+  ELGB_OPT_PANEL_PUSH = 13
 };
 int ElGBSetOption(ElGBContext ctx, int option, int value);
 

@@ -145,3 +145,22 @@ def test_interchanges_on_the_swap_stream_change_nothing(ctx):
             ctx.set_option("swap_stream", 0)
     assert torch.equal(outs[0][1], outs[1][1])
     assert torch.equal(outs[0][0], outs[1][0])
+
+
+@pytest.mark.parametrize("m,n", [(300, 300), (2100, 2100), (8192, 2048), (20000, 600)])
+def test_push_exchange_matches_barrier_exchange(ctx, m, n):
+    """ELGB_OPT_PANEL_PUSH: candidates pushed into every CTA on an mbarrier
+    instead of read after a cluster barrier.  Only the exchange differs, so
+    pivots and factors are bit-identical."""
+    A0 = _matrix(m, n, 7 * m + n)
+    outs = []
+    for v in (0, 1):
+        ctx.set_option("panel_push", v)
+        try:
+            outs.append(_lu(ctx, A0, 2))
+        finally:
+            ctx.set_option("panel_push", 1)
+    assert torch.equal(outs[0][1], outs[1][1])
+    assert torch.equal(outs[0][0], outs[1][0])
+    info, err = ctx.status()
+    assert err == 0
