@@ -255,6 +255,7 @@ def case_panel_trace(ctx, a):
     ctx.set_option("panel_rows", a.panel_rows)
     ctx.set_option("panel_regs", a.panel_regs)
     ctx.set_option("trail_split", a.trail_split)
+    ctx.set_option("panel_push", a.panel_push)
     try:
         ctx.lu_mixed(A, gemm_kind=a.kind, nb=a.nb)
         A.copy_(A0)
@@ -268,6 +269,7 @@ def case_panel_trace(ctx, a):
         ctx.set_option("panel_rows", 1024)
         ctx.set_option("panel_regs", 2)
         ctx.set_option("trail_split", 1)
+        ctx.set_option("panel_push", 1)
     ok = np.all(tr > 0, axis=1)
     cols = np.arange(a.n)
     d_pub = (tr[:, 1] - tr[:, 0]) / 1e3
@@ -291,6 +293,7 @@ def case_panel_trace(ctx, a):
     return dict(case="panel_trace", n=a.n, kind=KIND_NAMES[a.kind], lookahead=a.lookahead,
                 trail_grid=a.trail_grid, panel_cluster=a.panel_cluster,
                 panel_rows=a.panel_rows, panel_regs=a.panel_regs, trail_split=a.trail_split,
+                panel_push=a.panel_push,
                 ms=ms, traced=int(ok.sum()),
                 leaf_step_ms_total=tot_steps, bands=bands)
 
@@ -362,6 +365,8 @@ def main(argv=None):
                    help="panel_trace: ELGB_OPT_PANEL_ROWS")
     p.add_argument("--trail-split", type=int, default=1,
                    help="panel_trace: ELGB_OPT_TRAIL_SPLIT")
+    p.add_argument("--panel-push", type=int, default=1,
+                   help="panel_trace: ELGB_OPT_PANEL_PUSH (0 = cluster-barrier exchange)")
     p.add_argument("--panel-regs", type=int, default=2,
                    help="panel_trace: ELGB_OPT_PANEL_REGS (2 = register cluster kernel)")
     p.add_argument("--records", default="",
