@@ -257,7 +257,7 @@ static cudaError_t trsm_llnu(Context* ctx, const LuLane& L, const T* Lm, long ld
     const int ib = std::min(128, nb - i0);
     const int pi = ctx->prof_begin(L.st, ELGB_PROF_TRSM);
     LANE_CHECK(launch_trsm_block<T>(Lm + i0 + (long)i0 * ldl, ldl, Bm + i0, ldb, ib, ncols,
-                                    true, true, false, false, L.st), 1);
+                                    true, true, false, false, L.st, ctx->status), 1);
     ctx->prof_end(pi, L.st, ELGB_PROF_TRSM, (double)ib * ib * ncols,
                   2.0 * sizeof(T) * ib * (double)ncols);
     const int rest = nb - i0 - ib;

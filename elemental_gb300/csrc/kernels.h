@@ -156,10 +156,12 @@ cudaError_t launch_permute_rows(const T* X, long ldx, T* Y, long ldy, int n,
 // lower/upper and unit/non-unit refer to op(A11); trans_a loads A11
 // transposed; trans_b means B is stored transposed (B^T is ncols x nb at
 // Bm with leading dimension ldb).
+// st (may be null): where a bounded wait reports a timeout; with it, A11's
+// triangle is staged by bulk copies when its columns are 16-byte aligned.
 template <typename T>
 cudaError_t launch_trsm_block(const T* A11, long lda, T* Bm, long ldb, int nb,
                               int ncols, bool lower, bool unit, bool trans_a,
-                              bool trans_b, cudaStream_t stream);
+                              bool trans_b, cudaStream_t stream, DevStatus* st = nullptr);
 
 // out (n x n) := the strictly lower triangle of A, zeros elsewhere.
 template <typename T>

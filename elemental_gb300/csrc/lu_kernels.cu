@@ -2412,32 +2412,55 @@ constexpr int kTrsmCols = 32;
 template <typename T, int NB>
 __global__ void __launch_bounds__(kTrsmThreads)
 trsm_block_kernel(const T* __restrict__ A, long lda, T* __restrict__ Bm, long ldb, int nb,
-                  int ncols, int lower, int unit, int trans_a, int trans_b) {
+                  int ncols, int lower, int unit, int trans_a, int trans_b, int bulk,
+                  DevStatus* st) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t s_mbar;
   T* sA = reinterpret_cast<T*>(smem_raw);  // op(A)(i, j) at sA[i + j * NB]
   T* sB = sA + NB * NB;                     // B(i, c) at sB[i + c * (NB + 1)]
   constexpr int LDS = NB + 1;
   const int tid = threadIdx.x;
-  for (int idx = tid; idx < NB * NB; idx += blockDim.x) {
-    const int i = idx % NB, j = idx / NB;
-    T v;
-    if (i < nb && j < nb)
-      v = trans_a ? A[j + (long)i * lda] : A[i + (long)j * lda];
-    else
-      v = (i == j) ? T(1) : T(0);
-    sA[idx] = v;
+  if (bulk) {
+    // (caller: A, lda and nb rows of T in 16-byte units, A11 not
+    // transposed) each of the nb columns' first nb rows in one bulk copy
+    // by the TMA engine: one round trip instead of a loop of loads
+    if (tid == 0) {
+      tc::mbar_init(&s_mbar, 1);
+      tc::fence_mbar_init();
+      tc::mbar_arrive_expect_tx(&s_mbar, (uint32_t)(nb * nb * sizeof(T)));
+    }
+    __syncthreads();
+    for (int j = tid; j < nb; j += blockDim.x)
+      asm volatile(
+          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, "
+          "[%3];" ::"r"((unsigned)__cvta_generic_to_shared(sA + j * NB)),
+          "l"(A + (long)j * lda), "r"((uint32_t)(nb * sizeof(T))), "r"(tc::smem_u32(&s_mbar))
+          : "memory");
+    for (int idx = tid; idx < NB * NB; idx += blockDim.x) {
+      const int i = idx % NB, j = idx / NB;
+      if (i >= nb || j >= nb) sA[idx] = (i == j) ? T(1) : T(0);
+    }
+    tc::mbar_wait(&s_mbar, 0, st, 42);
+  } else {
+    for (int idx = tid; idx < NB * NB; idx += blockDim.x) {
+      const int i = idx % NB, j = idx / NB;
+      T v;
+      if (i < nb && j < nb)
+        v = trans_a ? A[j + (long)i * lda] : A[i + (long)j * lda];
+      else
+        v = (i == j) ? T(1) : T(0);
+      sA[idx] = v;
+    }
   }
   const int lane = tid & 31, warp = tid >> 5;
   constexpr int NT = NB / 32;
   for (int c0 = blockIdx.x * kTrsmCols; c0 < ncols; c0 += gridDim.x * kTrsmCols) {
     const int cw = min(kTrsmCols, ncols - c0);
-    __syncthreads();
-    if (!trans_b) {
-      for (int idx = tid; idx < NB * kTrsmCols; idx += blockDim.x) {
-        const int i = idx % NB, c = idx / NB;
-        sB[i + c * LDS] = (i < nb && c < cw) ? Bm[i + (long)(c0 + c) * ldb] : T(0);
-      }
-    } else {
+    // B not transposed: each lane loads its rows of its columns straight into
+    // registers (coalesced, all in flight at once); transposed: through
+    // shared memory
+    if (trans_b) {
+      __syncthreads();
       for (int idx = tid; idx < NB * kTrsmCols; idx += blockDim.x) {
         const int c = idx % kTrsmCols, i = idx / kTrsmCols;
         sB[i + c * LDS] = (i < nb && c < cw) ? Bm[(c0 + c) + (long)i * ldb] : T(0);
@@ -2458,11 +2481,17 @@ trsm_block_kernel(const T* __restrict__ A, long lda, T* __restrict__ Bm, long ld
         const int c = warp + kW * q;
         on[q] = c < cw;
 #pragma unroll
-        for (int t = 0; t < NT; ++t) x[q][t] = on[q] ? sB[lane + 32 * t + c * LDS] : T(0);
+        for (int t = 0; t < NT; ++t) {
+          const int i = lane + 32 * t;
+          x[q][t] = !on[q] ? T(0)
+                    : trans_b ? sB[i + c * LDS]
+                              : (i < nb ? Bm[i + (long)(c0 + c) * ldb] : T(0));
+        }
       }
       if (lower) {
 #pragma unroll
         for (int t = 0; t < NT; ++t) {
+#pragma unroll 8
           for (int jj = 0; jj < 32; ++jj) {
             const int j = 32 * t + jj;
             if (!unit && lane == jj) {
@@ -2487,6 +2516,7 @@ trsm_block_kernel(const T* __restrict__ A, long lda, T* __restrict__ Bm, long ld
       } else {
 #pragma unroll
         for (int t = NT - 1; t >= 0; --t) {
+#pragma unroll 8
           for (int jj = 31; jj >= 0; --jj) {
             const int j = 32 * t + jj;
             if (!unit && lane == jj) {
@@ -2513,15 +2543,16 @@ trsm_block_kernel(const T* __restrict__ A, long lda, T* __restrict__ Bm, long ld
       for (int q = 0; q < CPW; ++q)
         if (on[q])
 #pragma unroll
-          for (int t = 0; t < NT; ++t) sB[lane + 32 * t + (warp + kW * q) * LDS] = x[q][t];
+          for (int t = 0; t < NT; ++t) {
+            const int i = lane + 32 * t;
+            if (trans_b)
+              sB[i + (warp + kW * q) * LDS] = x[q][t];
+            else if (i < nb)
+              Bm[i + (long)(c0 + warp + kW * q) * ldb] = x[q][t];
+          }
     }
-    __syncthreads();
-    if (!trans_b) {
-      for (int idx = tid; idx < NB * kTrsmCols; idx += blockDim.x) {
-        const int i = idx % NB, c = idx / NB;
-        if (i < nb && c < cw) Bm[i + (long)(c0 + c) * ldb] = sB[i + c * LDS];
-      }
-    } else {
+    if (trans_b) {
+      __syncthreads();
       for (int idx = tid; idx < NB * kTrsmCols; idx += blockDim.x) {
         const int c = idx % kTrsmCols, i = idx / kTrsmCols;
         if (i < nb && c < cw) Bm[(c0 + c) + (long)i * ldb] = sB[i + c * LDS];
@@ -2533,41 +2564,44 @@ trsm_block_kernel(const T* __restrict__ A, long lda, T* __restrict__ Bm, long ld
 template <typename T, int NB>
 static cudaError_t trsm_block_nb(const T* A11, long lda, T* Bm, long ldb, int nb, int ncols,
                                  bool lower, bool unit, bool trans_a, bool trans_b,
-                                 cudaStream_t stream) {
+                                 cudaStream_t stream, DevStatus* st) {
   const size_t smem = ((size_t)NB * NB + (size_t)(NB + 1) * kTrsmCols) * sizeof(T);
   auto kern = trsm_block_kernel<T, NB>;
-  if (smem > 48 * 1024) {
+  if (smem + 64 > 48 * 1024) {  // (with the kernel's static mbarrier)
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
   }
   int blocks = ceil_div(ncols, kTrsmCols);
   if (blocks > 1024) blocks = 1024;
+  const int bulk = !trans_a && st != nullptr && ((uintptr_t)A11 % 16) == 0 &&
+                   ((size_t)lda * sizeof(T)) % 16 == 0 && ((size_t)nb * sizeof(T)) % 16 == 0;
   kern<<<blocks, kTrsmThreads, smem, stream>>>(A11, lda, Bm, ldb, nb, ncols, lower, unit,
-                                                trans_a, trans_b);
+                                                trans_a, trans_b, bulk, st);
   return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t launch_trsm_block(const T* A11, long lda, T* Bm, long ldb, int nb, int ncols,
                               bool lower, bool unit, bool trans_a, bool trans_b,
-                              cudaStream_t stream) {
+                              cudaStream_t stream, DevStatus* st) {
   if (nb <= 0 || ncols <= 0) return cudaSuccess;
   if (nb <= 32)
     return trsm_block_nb<T, 32>(A11, lda, Bm, ldb, nb, ncols, lower, unit, trans_a, trans_b,
-                                stream);
+                                stream, st);
   if (nb <= 64)
     return trsm_block_nb<T, 64>(A11, lda, Bm, ldb, nb, ncols, lower, unit, trans_a, trans_b,
-                                stream);
+                                stream, st);
   if (nb <= 128)
     return trsm_block_nb<T, 128>(A11, lda, Bm, ldb, nb, ncols, lower, unit, trans_a,
-                                 trans_b, stream);
+                                 trans_b, stream, st);
   return cudaErrorInvalidValue;
 }
 template cudaError_t launch_trsm_block<double>(const double*, long, double*, long, int, int,
-                                               bool, bool, bool, bool, cudaStream_t);
+                                               bool, bool, bool, bool, cudaStream_t,
+                                               DevStatus*);
 template cudaError_t launch_trsm_block<float>(const float*, long, float*, long, int, int,
-                                              bool, bool, bool, bool, cudaStream_t);
+                                              bool, bool, bool, bool, cudaStream_t, DevStatus*);
 
 // out (n x n, leading dimension ldo) := the strictly lower triangle of A
 // (zeros on and above the diagonal).
