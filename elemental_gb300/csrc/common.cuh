@@ -34,6 +34,16 @@ __device__ __forceinline__ unsigned long long globaltimer_ns() {
   return t;
 }
 
+// Programmatic dependent launch: a kernel launched with programmatic stream
+// serialization may start while its predecessor on the stream still runs;
+// pdl_wait() blocks until that predecessor has completed and its memory is
+// visible (a no-op for a kernel launched normally).  pdl_launch_dependents()
+// lets such a successor start being scheduled (no effect on any other).
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_launch_dependents() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
   unsigned v;
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");

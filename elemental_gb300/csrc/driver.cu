@@ -1397,6 +1397,9 @@ int ElGBSetOption(ElGBContext ctx, int option, int value) {
     case ELGB_OPT_SWAP_STREAM:
       ctx->opt_swap_stream = value ? 1 : 0;
       return 0;
+    case ELGB_OPT_PANEL_PDL:
+      elgb::g_panel_pdl = value ? 1 : 0;
+      return 0;
     case ELGB_OPT_PANEL_PUSH:
       if (value < 0 || value > 2) return elgb::kElArgError;
       elgb::g_panel_push = value;

@@ -56,6 +56,9 @@ extern int g_panel_regs;
 // register leaf panels: candidates pushed into every CTA with asynchronous
 // DSMEM stores on an mbarrier (1) or read after a cluster barrier (0)
 extern int g_panel_push;
+// register leaf panels launched as programmatic dependents of the kernel
+// before them on their stream (1) or normally (0)
+extern int g_panel_pdl;
 
 // getf2 on a w-wide panel (w <= 32): El's lu::Panel
 // (src/lapack_like/factor/LU/Panel.hpp:15-59) as one cooperative launch.

@@ -20,6 +20,7 @@ int g_panel_rows = 1024;
 // 1 cooperative, 2 on a cluster where one fits (the default).
 int g_panel_regs = 2;
 int g_panel_push = 1;
+int g_panel_pdl = 1;
 
 template <typename T>
 __device__ __forceinline__ T absv(T x) { return x < T(0) ? -x : x; }
@@ -900,6 +901,7 @@ getf2_panel_cluster_reg_kernel(PanelParams<float> p) {
   __shared__ int s_dst[2 * W], s_src[2 * W];   // the interchanges' net row moves
   __shared__ int s_nmove;
 
+  pdl_wait();  // (launched as the side stream's programmatic dependent)
   const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x;
   const int lane = tid & 31;
   const int R = p.R, w = p.w;
@@ -1296,7 +1298,7 @@ static cudaError_t launch_getf2_panel_cluster_reg(float* A, long lda, int mp, in
   cfg.blockDim = dim3(kRcThreads);
   cfg.dynamicSmemBytes = 0;
   cfg.stream = stream;
-  cudaLaunchAttribute attr[1];
+  cudaLaunchAttribute attr[2];
   attr[0].id = cudaLaunchAttributeClusterDimension;
   attr[0].val.clusterDim.x = C;
   attr[0].val.clusterDim.y = 1;
@@ -1323,6 +1325,13 @@ static cudaError_t launch_getf2_panel_cluster_reg(float* A, long lda, int mp, in
   ps.trace = trace;
   PanelParams<float> prm{A, lda, mp, w, R, ipiv, row_base, info_base, 0, ps, st, 0,
                          swap_lo, swap_hi};
+  if (g_panel_pdl) {
+    // the leaf may be placed while the update before it on the stream
+    // finishes; it waits for that update (pdl_wait) before touching memory
+    attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[1].val.programmaticStreamSerializationAllowed = 1;
+    cfg.numAttrs = 2;
+  }
   return cudaLaunchKernelEx(&cfg, kern, prm);
 }
 
@@ -2420,6 +2429,7 @@ trsm_block_kernel(const T* __restrict__ A, long lda, T* __restrict__ Bm, long ld
   T* sB = sA + NB * NB;                     // B(i, c) at sB[i + c * (NB + 1)]
   constexpr int LDS = NB + 1;
   const int tid = threadIdx.x;
+  pdl_launch_dependents();
   if (bulk) {
     // (caller: A, lda and nb rows of T in 16-byte units, A11 not
     // transposed) each of the nb columns' first nb rows in one bulk copy
@@ -2640,6 +2650,7 @@ gemm_simt_kernel(int m, int n, int k, T alpha, const T* __restrict__ A, long lda
                  int uplo) {
   __shared__ T sA[kGBK][kGBM + 1];
   __shared__ T sB[kGBK][kGBN + 1];
+  pdl_launch_dependents();  // a leaf panel after it may be scheduled now
   const int tid = threadIdx.x;
   const int tx = tid & 15, ty = tid >> 4;
   const int row0 = blockIdx.x * kGBM, col0 = blockIdx.y * kGBN;

@@ -123,6 +123,7 @@ tc_gemm_persistent_kernel(const __grid_constant__ CUtensorMap tmA,
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int tiles_m = (m + kBM - 1) / kBM, tiles_n = (n + kBN - 1) / kBN;
   const int ntiles = tiles_m * tiles_n;
+  pdl_launch_dependents();  // a leaf panel after it may be scheduled now
   // stage s: A hi | B hi | A lo | B lo
   auto sA = [&](int s) { return base + (size_t)s * kStageBytes; };
   auto sB = [&](int s) { return base + (size_t)s * kStageBytes + kStageA; };

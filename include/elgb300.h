@@ -121,7 +121,12 @@ int ElGBSetBlocksize(int nb);
  *                       into its own slot and the others read it after a
  *                       cluster barrier; 2: push for 32-column leaves only.
  *                       Same pivots and factors.  Process-wide, like
- *                       ELGB_OPT_PANEL_REGS. */
+ *                       ELGB_OPT_PANEL_REGS.
+ *   ELGB_OPT_PANEL_PDL  1 (default): register leaf panels are launched as
+ *                       programmatic dependents of the kernel before them on
+ *                       their stream (placed while it finishes, waiting for
+ *                       it before touching memory); 0: normal launches.
+ *                       Process-wide. */
 enum {
   ELGB_OPT_LOOKAHEAD = 1,
   ELGB_OPT_PANEL_CTAS = 2,
@@ -135,7 +140,8 @@ enum {
   ELGB_OPT_TRAIL_SPLIT = 10,
   ELGB_OPT_INV_TRSM = 11,
   ELGB_OPT_SWAP_STREAM = 12,
-  ELGB_OPT_PANEL_PUSH = 13
+  ELGB_OPT_PANEL_PUSH = 13,
+  ELGB_OPT_PANEL_PDL = 14
 };
 int ElGBSetOption(ElGBContext ctx, int option, int value);
 
