@@ -189,7 +189,12 @@ static cudaError_t gemm_sub(Context* ctx, const LuLane& L, int m, int n, int k, 
                             bool trailing = false) {
   const GemmCfg& g = L.gemm;
   const int kind = (trailing && g.trail_kind >= 0) ? g.trail_kind : g.tc_kind;
-  if (kind >= 0 && m >= 64 && n >= 64 && k >= 16) {
+  // the look-ahead stream's narrow updates (its recursion's m x n x n) go to
+  // the CUDA cores below ctx->opt_side_tc_min_n columns: the tensor-core
+  // path's fixed cost (two packing launches and the persistent kernel's
+  // set-up) exceeds their work
+  const int min_n = (L.st == ctx->side_stream && ctx->side_stream) ? ctx->opt_side_tc_min_n : 64;
+  if (kind >= 0 && m >= 64 && n >= min_n && k >= 16) {
     int nl = 0;
     cudaEvent_t a = nullptr, b = nullptr;
     if (ctx->prof_wants(ELGB_PROF_TC_GEMM)) {
@@ -1396,6 +1401,10 @@ int ElGBSetOption(ElGBContext ctx, int option, int value) {
       return 0;
     case ELGB_OPT_SWAP_STREAM:
       ctx->opt_swap_stream = value ? 1 : 0;
+      return 0;
+    case ELGB_OPT_SIDE_TC_MIN_N:
+      if (value < 16 || value > 4096) return elgb::kElArgError;
+      ctx->opt_side_tc_min_n = value;
       return 0;
     case ELGB_OPT_PANEL_PDL:
       elgb::g_panel_pdl = value ? 1 : 0;

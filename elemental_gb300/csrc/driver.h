@@ -43,6 +43,7 @@ struct Context {
   int opt_trail_split = 1;        // ElGBSetOption(ELGB_OPT_TRAIL_SPLIT)
   int opt_inv_trsm = 0;           // ElGBSetOption(ELGB_OPT_INV_TRSM)
   int opt_swap_stream = 0;        // ElGBSetOption(ELGB_OPT_SWAP_STREAM)
+  int opt_side_tc_min_n = 256;    // ElGBSetOption(ELGB_OPT_SIDE_TC_MIN_N)
   // ElGBSetOption(ELGB_OPT_PANEL_TRACE): per-column leaf-panel timestamps of
   // the last factorization, 4 per column, for its first trace_cols columns
   unsigned long long* trace_buf = nullptr;

@@ -126,7 +126,13 @@ int ElGBSetBlocksize(int nb);
  *                       programmatic dependents of the kernel before them on
  *                       their stream (placed while it finishes, waiting for
  *                       it before touching memory); 0: normal launches.
- *                       Process-wide. */
+ *                       Process-wide.
+ *   ELGB_OPT_SIDE_TC_MIN_N  the fewest columns (16 .. 4096, default 256)
+ *                       for which the look-ahead stream's recursion updates
+ *                       (m x n x n) use the tensor cores; narrower ones run
+ *                       on the CUDA cores (exact FP32 FMAs).  At n = 32768
+ *                       the LU took 216.5 / 213.7 / 213.0 / 213.6 ms with
+ *                       64 / 128 / 256 / 512. */
 enum {
   ELGB_OPT_LOOKAHEAD = 1,
   ELGB_OPT_PANEL_CTAS = 2,
@@ -141,7 +147,8 @@ enum {
   ELGB_OPT_INV_TRSM = 11,
   ELGB_OPT_SWAP_STREAM = 12,
   ELGB_OPT_PANEL_PUSH = 13,
-  ELGB_OPT_PANEL_PDL = 14
+  ELGB_OPT_PANEL_PDL = 14,
+  ELGB_OPT_SIDE_TC_MIN_N = 15
 };
 int ElGBSetOption(ElGBContext ctx, int option, int value);
 
