@@ -450,12 +450,12 @@ static cudaError_t getrf_run(LuState<T>& s, int nb) {
     // runs, and the rest after the panel on every SM
     int c_mid = s.n;
     if (split && s.trail_split && s.n > kn + jb2) {
-      // the panel of jb2 columns on m - kn rows: ~2 us per pivot step up to
-      // 16384 rows (registers), ~4.4 us above, plus ~1 ms of recursion
-      // kernels; the update at ~180 TF/s beside it (TF32x3 on all GPCs but
-      // one), rounded up to whole 256-column tiles
+      // the panel of jb2 columns on m - kn rows: ~1.5 us per pivot step up
+      // to 16384 rows (registers, push exchange), ~2.6 us above, plus ~1 ms
+      // of recursion kernels; the update at ~180 TF/s beside it (TF32x3 on
+      // all GPCs but one), rounded up to whole 256-column tiles
       const double side_s =
-          (jb2 * ((s.m - kn) <= 16384 ? 2.1e-6 : 4.4e-6) + 1.0e-3) * s.trail_split_scale;
+          (jb2 * ((s.m - kn) <= 16384 ? 1.5e-6 : 2.6e-6) + 1.0e-3) * s.trail_split_scale;
       const double cols = side_s * 180e12 / (2.0 * (double)(s.m - kn) * jb);
       const long c = (long)kn + jb2 + ((long)std::ceil(cols / 256.0)) * 256;
       if (c < s.n) c_mid = (int)c;
