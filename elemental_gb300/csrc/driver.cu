@@ -318,54 +318,84 @@ static int leaf_width(const LuState<T>& s, int b0) {
   return 32;
 }
 
+// Whether gemm_sub runs this m x n x k update on the CUDA cores (the path
+// whose arithmetic the fused node update of the register leaf kernel copies).
+static bool gemm_sub_is_simt(const Context* ctx, const LuLane& L, int m, int n, int k) {
+  const int kind = L.gemm.tc_kind;
+  const int min_n = (L.st == ctx->side_stream && ctx->side_stream) ? ctx->opt_side_tc_min_n : 64;
+  return !(kind >= 0 && m >= 64 && n >= min_n && k >= 16);
+}
+
+// One leaf panel, columns [c0, c0 + w) of the block [b0, b1), its
+// interchanges onto the block's other columns; sib_w > 0: the leaf is the
+// left child of a node whose right child has sib_w columns, and *node_done
+// tells whether the leaf kernel also applied that node's TRSM and update.
+template <typename T>
+static cudaError_t panel_leaf(LuState<T>& s, const LuLane& L, int c0, int w, int b0, int b1,
+                              int sib_w, bool* node_done) {
+  Context* ctx = s.ctx;
+  if (node_done) *node_done = false;
+  const int pi = ctx->prof_begin(L.st, ELGB_PROF_PANEL);
+  bool done = false, swapped = false;
+  if constexpr (sizeof(T) == 4) {
+    if (s.tournament && !s.nopiv) {
+      int nl = 0;
+      const cudaError_t e = launch_calu_panel(
+          reinterpret_cast<float*>(s.A) + c0 + (long)c0 * s.lda, s.lda, s.m - c0, w,
+          s.ipiv + c0, c0, c0, s.ps.cand, s.ps.maxG, ctx->status, s.panel_ctas, L.st, &nl);
+      ctx->launches += nl;
+      if (e == cudaSuccess) done = true;
+      else if (e != cudaErrorNotSupported) return e;
+    }
+  }
+  if (!done) {
+    PanelScratch<T> ps = s.ps;
+    ps.trace = (s.trace && c0 + w <= s.trace_cols) ? s.trace + 4 * (long)c0 : nullptr;
+    LANE_CHECK(launch_getf2_panel<T>(s.A + c0 + (long)c0 * s.lda, s.lda, s.m - c0, w,
+                                     s.ipiv + c0, c0, c0, s.panel_epoch, ps, ctx->status,
+                                     s.panel_ctas, L.st, s.nopiv, b0 - c0, b1 - c0, &swapped,
+                                     sib_w, node_done),
+               1);
+    s.panel_epoch += w;
+  }
+  ctx->prof_end(pi, L.st, ELGB_PROF_PANEL, (double)(s.m - c0) * w * w,
+                2.0 * sizeof(T) * (s.m - c0) * (double)w);
+  if (!swapped && (b0 < c0 || c0 + w < b1)) {
+    cudaError_t e = apply_swaps(s, L, c0, w, b0, c0, c0 + w, b1, false);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
 template <typename T>
 static cudaError_t panel_rec(LuState<T>& s, const LuLane& L, int c0, int w, int b0, int b1) {
   Context* ctx = s.ctx;
   const int lw = leaf_width(s, b0);
-  if (w <= lw) {
-    const int pi = ctx->prof_begin(L.st, ELGB_PROF_PANEL);
-    bool done = false, swapped = false;
-    if constexpr (sizeof(T) == 4) {
-      if (s.tournament && !s.nopiv) {
-        int nl = 0;
-        const cudaError_t e = launch_calu_panel(
-            reinterpret_cast<float*>(s.A) + c0 + (long)c0 * s.lda, s.lda, s.m - c0, w,
-            s.ipiv + c0, c0, c0, s.ps.cand, s.ps.maxG, ctx->status, s.panel_ctas, L.st, &nl);
-        ctx->launches += nl;
-        if (e == cudaSuccess) done = true;
-        else if (e != cudaErrorNotSupported) return e;
-      }
-    }
-    if (!done) {
-      PanelScratch<T> ps = s.ps;
-      ps.trace = (s.trace && c0 + w <= s.trace_cols) ? s.trace + 4 * (long)c0 : nullptr;
-      LANE_CHECK(launch_getf2_panel<T>(s.A + c0 + (long)c0 * s.lda, s.lda, s.m - c0, w,
-                                       s.ipiv + c0, c0, c0, s.panel_epoch, ps, ctx->status,
-                                       s.panel_ctas, L.st, s.nopiv, b0 - c0, b1 - c0,
-                                       &swapped), 1);
-      s.panel_epoch += w;
-    }
-    ctx->prof_end(pi, L.st, ELGB_PROF_PANEL, (double)(s.m - c0) * w * w,
-                  2.0 * sizeof(T) * (s.m - c0) * (double)w);
-    if (!swapped && (b0 < c0 || c0 + w < b1)) {
-      cudaError_t e = apply_swaps(s, L, c0, w, b0, c0, c0 + w, b1, false);
-      if (e != cudaSuccess) return e;
-    }
-    return cudaSuccess;
-  }
+  if (w <= lw) return panel_leaf(s, L, c0, w, b0, b1, 0, nullptr);
   int w1 = (w / 2 + lw - 1) / lw * lw;
   if (w1 >= w) w1 = w - lw;
   const int w2 = w - w1;
-  cudaError_t e = panel_rec(s, L, c0, w1, b0, b1);
+  // a node of two leaves: the left leaf's kernel may apply the node's TRSM
+  // and update itself (when the update would run on the CUDA cores, whose
+  // arithmetic it copies)
+  const bool two_leaves = w1 <= lw && w2 <= lw && ctx->opt_panel_node;
+  bool node_done = false;
+  cudaError_t e =
+      two_leaves ? panel_leaf(s, L, c0, w1, b0, b1,
+                              gemm_sub_is_simt(ctx, L, s.m - c0 - w1, w2, w1) ? w2 : 0,
+                              &node_done)
+                 : panel_rec(s, L, c0, w1, b0, b1);
   if (e != cudaSuccess) return e;
-  T* A11 = s.A + c0 + (long)c0 * s.lda;
-  T* A12 = s.A + c0 + (long)(c0 + w1) * s.lda;
-  T* A21 = s.A + (c0 + w1) + (long)c0 * s.lda;
-  T* A22 = s.A + (c0 + w1) + (long)(c0 + w1) * s.lda;
-  e = trsm_llnu<T>(ctx, L, A11, s.lda, w1, A12, s.lda, w2);
-  if (e != cudaSuccess) return e;
-  e = gemm_sub(ctx, L, s.m - c0 - w1, w2, w1, A21, s.lda, A12, s.lda, A22, s.lda);
-  if (e != cudaSuccess) return e;
+  if (!node_done) {
+    T* A11 = s.A + c0 + (long)c0 * s.lda;
+    T* A12 = s.A + c0 + (long)(c0 + w1) * s.lda;
+    T* A21 = s.A + (c0 + w1) + (long)c0 * s.lda;
+    T* A22 = s.A + (c0 + w1) + (long)(c0 + w1) * s.lda;
+    e = trsm_llnu<T>(ctx, L, A11, s.lda, w1, A12, s.lda, w2);
+    if (e != cudaSuccess) return e;
+    e = gemm_sub(ctx, L, s.m - c0 - w1, w2, w1, A21, s.lda, A12, s.lda, A22, s.lda);
+    if (e != cudaSuccess) return e;
+  }
   return panel_rec(s, L, c0 + w1, w2, b0, b1);
 }
 
@@ -1401,6 +1431,9 @@ int ElGBSetOption(ElGBContext ctx, int option, int value) {
       return 0;
     case ELGB_OPT_SWAP_STREAM:
       ctx->opt_swap_stream = value ? 1 : 0;
+      return 0;
+    case ELGB_OPT_PANEL_NODE:
+      ctx->opt_panel_node = value ? 1 : 0;
       return 0;
     case ELGB_OPT_SIDE_TC_MIN_N:
       if (value < 16 || value > 4096) return elgb::kElArgError;

@@ -44,6 +44,7 @@ struct Context {
   int opt_inv_trsm = 0;           // ElGBSetOption(ELGB_OPT_INV_TRSM)
   int opt_swap_stream = 0;        // ElGBSetOption(ELGB_OPT_SWAP_STREAM)
   int opt_side_tc_min_n = 256;    // ElGBSetOption(ELGB_OPT_SIDE_TC_MIN_N)
+  int opt_panel_node = 0;         // ElGBSetOption(ELGB_OPT_PANEL_NODE)
   // ElGBSetOption(ELGB_OPT_PANEL_TRACE): per-column leaf-panel timestamps of
   // the last factorization, 4 per column, for its first trace_cols columns
   unsigned long long* trace_buf = nullptr;

@@ -71,13 +71,17 @@ extern int g_panel_pdl;
 // swap_lo <= 0 <= w <= swap_hi: the leaf's row interchanges are also due on
 // the columns [swap_lo, 0) and [w, swap_hi) of A (relative to the leaf's
 // first column); a kernel that applies them itself sets *swaps_done, and the
-// caller applies them otherwise.
+// caller applies them otherwise.  sib_w > 0: the leaf is the left child of a
+// recursion node whose right child is columns [w, w + sib_w); a kernel that
+// also applies that node's TRSM and update (the same operations in the same
+// order as launch_trsm_block and launch_gemm_simt) sets *node_done.
 template <typename T>
 cudaError_t launch_getf2_panel(T* A, long lda, int mp, int w, int* ipiv,
                                int row_base, int info_base, int epoch_base,
                                const PanelScratch<T>& s, DevStatus* st,
                                int num_sms, cudaStream_t stream, bool nopiv = false,
-                               int swap_lo = 0, int swap_hi = 0, bool* swaps_done = nullptr);
+                               int swap_lo = 0, int swap_hi = 0, bool* swaps_done = nullptr,
+                               int sib_w = 0, bool* node_done = nullptr);
 
 // El::LU(A, P, Q) with full pivoting (src/lapack_like/factor/LU/Full.hpp):
 // unblocked, two kernels per step.  fs / part: device scratch (one state,

@@ -108,6 +108,12 @@ struct PanelParams {
   // the leaf's interchanges also applied to columns [swap_lo, 0) and
   // [w, swap_hi) (relative to A) by the kernels that do so (0, 0: none)
   int swap_lo, swap_hi;
+  // > 0 (register cluster kernel): this leaf is the left child of a
+  // recursion node whose right child is columns [w, w + sib_w); the kernel
+  // also applies the node's update to them (U12 = L11^-1 A12 on rows
+  // [0, w), A22 -= L21 U12 below), with trsm_block's and gemm_simt's
+  // arithmetic in their order
+  int sib_w;
 };
 
 constexpr int kPanelW = 32;
@@ -898,6 +904,7 @@ getf2_panel_cluster_reg_kernel(PanelParams<float> p) {
   __shared__ float s_rv[2][33];
   __shared__ int s_rr[2][33];
   __shared__ int s_piv[W];                     // the pivot of each column (panel row)
+  __shared__ __align__(16) float s_u[W][W];    // sib_w: the node's U12 (w x sib_w)
   __shared__ int s_dst[2 * W], s_src[2 * W];   // the interchanges' net row moves
   __shared__ int s_nmove;
 
@@ -1219,7 +1226,79 @@ getf2_panel_cluster_reg_kernel(PanelParams<float> p) {
       }
     }
   }
-  cluster_barrier();  // no CTA leaves while another may still read its slots
+  cluster_barrier();  // no CTA leaves while another may still read its slots;
+                      // every CTA's write-back and interchanges are visible
+  if (p.sib_w > 0) {
+    // The recursion node: U12 = L11^-1 A12 by warp 0 of CTA 0 (rows 0 .. w-1
+    // are its threads' register rows 0), column by column of U12 in chunks
+    // of 8 (each entry sees trsm_block's fma(-l_rc, u_c, u_r), c = 0 .. r-1);
+    // then every CTA takes U12 and subtracts L21 U12 from its rows below w
+    // (gemm_simt's sum from 0 over c, then one fma(-1, sum, a)).
+    const int sw = p.sib_w;
+    if (b == 0 && tid < 32) {
+      const int r = tid;
+#pragma unroll
+      for (int c0 = 0; c0 < W; c0 += 8) {
+        if (c0 < sw) {
+          float u[8];
+#pragma unroll
+          for (int k = 0; k < 8; ++k)
+            u[k] = (r < w && c0 + k < sw) ? p.A[(long)r + (long)(w + c0 + k) * p.lda] : 0.f;
+#pragma unroll
+          for (int c = 0; c < W; ++c) {
+            if (c < w) {
+              if (r == c)
+#pragma unroll
+                for (int k = 0; k < 8; ++k) s_u[c][c0 + k] = u[k];
+              __syncwarp();
+              if (r > c && r < w) {
+                const float l = a[0][c];
+#pragma unroll
+                for (int k = 0; k < 8; ++k) u[k] = fmaf(-l, s_u[c][c0 + k], u[k]);
+              }
+            }
+          }
+          if (r < w)
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+              if (c0 + k < sw) p.A[(long)r + (long)(w + c0 + k) * p.lda] = u[k];
+        }
+      }
+    }
+    cluster_barrier();  // CTA 0's U12 complete
+    if (b != 0) {
+      static_assert((W * W) % 4 == 0, "U12 in 16-byte pieces");
+      const uint32_t src = cluster_map(&s_u[0][0], 0u);
+      for (int v = tid; v < W * W / 4; v += kRcThreads)
+        reinterpret_cast<float4*>(&s_u[0][0])[v] = ld_cluster_v4(src + 16u * v);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < RPT; ++i) {
+      const int row = grow[i];
+      if (row < w) continue;  // (and rows past the CTA's)
+#pragma unroll
+      for (int c0 = 0; c0 < W; c0 += 8) {
+        if (c0 < sw) {
+          float acc[8];
+#pragma unroll
+          for (int k = 0; k < 8; ++k) acc[k] = 0.f;
+#pragma unroll
+          for (int c = 0; c < W; ++c)
+            if (c < w)
+#pragma unroll
+              for (int k = 0; k < 8; ++k) acc[k] = fmaf(a[i][c], s_u[c][c0 + k], acc[k]);
+#pragma unroll
+          for (int k = 0; k < 8; ++k)
+            if (c0 + k < sw) {
+              float* pc = p.A + (long)row + (long)(w + c0 + k) * p.lda;
+              *pc = fmaf(-1.f, acc[k], *pc);
+            }
+        }
+      }
+    }
+    cluster_barrier();  // no CTA leaves while another may still read CTA 0's U12
+  }
 }
 
 // Cluster size for a panel of mp rows: the power of two giving about
@@ -1281,7 +1360,8 @@ static cudaError_t launch_getf2_panel_cluster(T* A, long lda, int mp, int w, int
 static cudaError_t launch_getf2_panel_cluster_reg(float* A, long lda, int mp, int w, int* ipiv,
                                                   int row_base, int info_base, DevStatus* st,
                                                   int C, unsigned long long* trace,
-                                                  cudaStream_t stream, int swap_lo, int swap_hi) {
+                                                  cudaStream_t stream, int swap_lo, int swap_hi,
+                                                  int sib_w) {
   const int R = ceil_div(mp, C);
   const bool narrow = w <= 16 && R > 2 * kRcThreads;  // 16 columns, 4 rows a thread
   if (R > (narrow ? 4 : 2) * kRcThreads) return cudaErrorNotSupported;
@@ -1324,7 +1404,7 @@ static cudaError_t launch_getf2_panel_cluster_reg(float* A, long lda, int mp, in
   PanelScratch<float> ps{};
   ps.trace = trace;
   PanelParams<float> prm{A, lda, mp, w, R, ipiv, row_base, info_base, 0, ps, st, 0,
-                         swap_lo, swap_hi};
+                         swap_lo, swap_hi, sib_w};
   if (g_panel_pdl) {
     // the leaf may be placed while the update before it on the stream
     // finishes; it waits for that update (pdl_wait) before touching memory
@@ -1339,8 +1419,10 @@ template <typename T>
 cudaError_t launch_getf2_panel(T* A, long lda, int mp, int w, int* ipiv, int row_base,
                                int info_base, int epoch_base, const PanelScratch<T>& s,
                                DevStatus* st, int num_sms, cudaStream_t stream, bool nopiv,
-                               int swap_lo, int swap_hi, bool* swaps_done) {
+                               int swap_lo, int swap_hi, bool* swaps_done, int sib_w,
+                               bool* node_done) {
   if (swaps_done) *swaps_done = false;
+  if (node_done) *node_done = false;
   if (w <= 0 || mp <= 0) return cudaSuccess;
   if (w > kPanelW || mp < w) return cudaErrorInvalidValue;
   if constexpr (sizeof(T) == 4) {
@@ -1353,10 +1435,15 @@ cudaError_t launch_getf2_panel(T* A, long lda, int mp, int w, int* ipiv, int row
         C = 16;
       if (C > 0 && ceil_div(mp, C) <= (w <= 16 ? 4 : 2) * kRcThreads) {
         const bool fuse = swaps_done != nullptr && (swap_lo < 0 || swap_hi > w);
+        // the node update needs the sibling's interchanges done first, here
+        const int sw = (fuse && node_done && sib_w > 0 && sib_w <= w && w + sib_w <= swap_hi)
+                           ? sib_w
+                           : 0;
         const cudaError_t e = launch_getf2_panel_cluster_reg(
             reinterpret_cast<float*>(A), lda, mp, w, ipiv, row_base, info_base, st, C, s.trace,
-            stream, fuse ? swap_lo : 0, fuse ? swap_hi : 0);
+            stream, fuse ? swap_lo : 0, fuse ? swap_hi : 0, sw);
         if (e == cudaSuccess && fuse) *swaps_done = true;
+        if (e == cudaSuccess && sw > 0) *node_done = true;
         if (e != cudaErrorNotSupported) return e;
       }
     }
@@ -1412,10 +1499,12 @@ cudaError_t launch_getf2_panel(T* A, long lda, int mp, int w, int* ipiv, int row
 
 template cudaError_t launch_getf2_panel<double>(double*, long, int, int, int*, int, int, int,
                                                 const PanelScratch<double>&, DevStatus*,
-                                                int, cudaStream_t, bool, int, int, bool*);
+                                                int, cudaStream_t, bool, int, int, bool*, int,
+                                                bool*);
 template cudaError_t launch_getf2_panel<float>(float*, long, int, int, int*, int, int, int,
                                                const PanelScratch<float>&, DevStatus*,
-                                               int, cudaStream_t, bool, int, int, bool*);
+                                               int, cudaStream_t, bool, int, int, bool*, int,
+                                               bool*);
 
 // ---------------------------------------------------------------------------
 // El::LU(A, P, Q) with full pivoting (src/lapack_like/factor/LU/Full.hpp:15-59)

@@ -114,7 +114,7 @@ class Context:
         "tournament" (0/1: tournament pivoting in lu_mixed's leaf panels)."""
         code = {"lookahead": 1, "panel_ctas": 2, "tournament": 3, "panel_cluster": 4,
                 "panel_regs": 5, "residual_df": 6, "panel_trace": 7, "trail_grid": 8,
-                "panel_rows": 9, "trail_split": 10, "inv_trsm": 11, "swap_stream": 12, "panel_push": 13, "panel_pdl": 14, "side_tc_min_n": 15}[option]
+                "panel_rows": 9, "trail_split": 10, "inv_trsm": 11, "swap_stream": 12, "panel_push": 13, "panel_pdl": 14, "side_tc_min_n": 15, "panel_node": 16}[option]
         self._rc(self.lib.ElGBSetOption(self.h, code, int(value)), "SetOption")
 
     def panel_trace(self, ncols):

@@ -132,7 +132,13 @@ int ElGBSetBlocksize(int nb);
  *                       (m x n x n) use the tensor cores; narrower ones run
  *                       on the CUDA cores (exact FP32 FMAs).  At n = 32768
  *                       the LU took 216.5 / 213.7 / 213.0 / 213.6 ms with
- *                       64 / 128 / 256 / 512. */
+ *                       64 / 128 / 256 / 512.
+ *   ELGB_OPT_PANEL_NODE 0 (default): a recursion node of two leaf panels
+ *                       runs its TRSM and update as separate launches; 1:
+ *                       the left leaf's register kernel applies them itself
+ *                       (bit-identical factors).  1 saves two launches a
+ *                       node but runs the update on the cluster's few SMs:
+ *                       LU 207.5 -> 227.5 ms at n = 32768, so off. */
 enum {
   ELGB_OPT_LOOKAHEAD = 1,
   ELGB_OPT_PANEL_CTAS = 2,
@@ -148,7 +154,8 @@ enum {
   ELGB_OPT_SWAP_STREAM = 12,
   ELGB_OPT_PANEL_PUSH = 13,
   ELGB_OPT_PANEL_PDL = 14,
-  ELGB_OPT_SIDE_TC_MIN_N = 15
+  ELGB_OPT_SIDE_TC_MIN_N = 15,
+  ELGB_OPT_PANEL_NODE = 16
 };
 int ElGBSetOption(ElGBContext ctx, int option, int value);
 

@@ -164,3 +164,25 @@ def test_push_exchange_matches_barrier_exchange(ctx, m, n):
     assert torch.equal(outs[0][0], outs[1][0])
     info, err = ctx.status()
     assert err == 0
+
+
+@pytest.mark.parametrize("m,n,nb", [(2100, 2100, 0), (8192, 1024, 0), (20000, 600, 0)])
+def test_fused_node_update_matches_separate_launches(ctx, m, n, nb):
+    """ELGB_OPT_PANEL_NODE = 1: the left leaf of a two-leaf recursion node
+    applies the node's TRSM and update itself, with launch_trsm_block's and
+    launch_gemm_simt's operations in their order, so the factors equal those
+    of the separate launches bit for bit (and, up to 16384 rows, the
+    shared-memory kernels')."""
+    A0 = _matrix(m, n, 3 * m + n)
+    A1, p1 = _lu(ctx, A0, 2, nb=nb)
+    ctx.set_option("panel_node", 1)
+    try:
+        A2, p2 = _lu(ctx, A0, 2, nb=nb)
+    finally:
+        ctx.set_option("panel_node", 0)
+    assert torch.equal(p1, p2)
+    assert torch.equal(A1, A2)
+    if m <= 16384:
+        A0s, p0s = _lu(ctx, A0, 0, nb=nb)
+        assert torch.equal(p0s, p2)
+        assert torch.equal(A0s, A2)
