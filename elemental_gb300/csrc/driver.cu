@@ -151,6 +151,13 @@ struct GemmCfg {
   int tc_kind = -1;     // panel-internal and TRSM GEMMs
   int trail_kind = -1;  // the trailing-matrix update (>= 0: overrides tc_kind)
   void* ws = nullptr;
+  // the trailing updates' own workspace: a block's three updates (its next
+  // block column, the columns beside the panel, the rest) share one L21, so
+  // its packed words are made once (what ws_trail holds: trail_a ...)
+  void* ws_trail = nullptr;
+  mutable const float* trail_a = nullptr;
+  mutable long trail_lda = 0;
+  mutable int trail_m = 0, trail_k = 0, trail_kind_packed = -1;
 };
 
 // One stream of the factorization with the scratch only it touches, so two
@@ -201,8 +208,23 @@ static cudaError_t gemm_sub(Context* ctx, const LuLane& L, int m, int n, int k, 
       a = ctx->next_event();
       b = ctx->next_event();
     }
-    cudaError_t e = launch_tc_gemm_sub(kind, m, n, k, A, lda, B, ldb, C, ldc, g.ws,
-                                       ctx->status, L.st, &nl, a, b, L.grid_mode);
+    void* ws = g.ws;
+    bool a_packed = false;
+    const bool reuse = trailing && g.ws_trail && kind != kTcFP8;
+    if (reuse) {
+      ws = g.ws_trail;
+      a_packed = g.trail_a == A && g.trail_lda == lda && g.trail_m == m && g.trail_k == k &&
+                 g.trail_kind_packed == kind;
+    }
+    cudaError_t e = launch_tc_gemm_sub(kind, m, n, k, A, lda, B, ldb, C, ldc, ws, ctx->status,
+                                       L.st, &nl, a, b, L.grid_mode, a_packed);
+    if (reuse) {
+      g.trail_a = e == cudaSuccess ? A : nullptr;
+      g.trail_lda = lda;
+      g.trail_m = m;
+      g.trail_k = k;
+      g.trail_kind_packed = kind;
+    }
     ctx->launches += nl;
     if (a && b) {
       const double esz = kind == kTcBF16 ? 2.0 : kind == kTcFP8 ? 1.0 : 4.0;
@@ -617,7 +639,7 @@ cudaError_t getrf(Context* ctx, int m, int n, T* A, long lda, int* ipiv, int nb,
                     tc_gemm_workspace_bytes(inner_kind, m, std::max(n, nb), nb))
          : 0;
   const size_t tcs = (tc && la) ? tc_gemm_workspace_bytes(inner_kind, m, nb, nb) : 0;
-  e = ctx->ensure(getrf_scratch_bytes<T>(ctx, nb, m, n) + align256(tcb) + align256(tcs));
+  e = ctx->ensure(getrf_scratch_bytes<T>(ctx, nb, m, n) + 2 * align256(tcb) + align256(tcs));
   if (e != cudaSuccess) return e;
   Carver cv(ctx);
   LuState<T> s{};
@@ -627,7 +649,8 @@ cudaError_t getrf(Context* ctx, int m, int n, T* A, long lda, int* ipiv, int nb,
     s.main.gemm.tc_kind = inner_kind;
     s.main.gemm.trail_kind = tc_kind;
     s.main.gemm.ws = cv.take<char>(tcb);
-    if (!s.main.gemm.ws) return cudaErrorMemoryAllocation;
+    s.main.gemm.ws_trail = cv.take<char>(tcb);
+    if (!s.main.gemm.ws_trail) return cudaErrorMemoryAllocation;
   }
   // ELGB_OPT_TRAIL_GRID: 0 every SM (persistent), 1 all GPCs but one, 2
   // (default) the same with the look-ahead stream's updates one CTA per tile,

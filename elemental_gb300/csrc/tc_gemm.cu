@@ -463,22 +463,25 @@ static int clusters16(K kern, int variant, size_t smem) {
 cudaError_t launch_tc_gemm_sub(int kind, int m, int n, int K, const float* A, long lda,
                                const float* B, long ldb, float* C, long ldc, void* ws,
                                DevStatus* st, cudaStream_t stream, int* nlaunch,
-                               cudaEvent_t ev0, cudaEvent_t ev1, int grid_mode) {
+                               cudaEvent_t ev0, cudaEvent_t ev1, int grid_mode, bool a_packed) {
   if (nlaunch) *nlaunch = 0;
   if (m <= 0 || n <= 0 || K <= 0) return cudaSuccess;
   const bool split = kind == kTcTF32x3;
   const int esz = op_esz(kind);
   const int kbe = kBKBytes / esz;
   const int Kp = (K + kbe - 1) / kbe * kbe;
+  // the packed A words first (their place depends on m and K only, so a
+  // caller may reuse them: a_packed), then B's
+  const size_t asz = rup1k((size_t)m * Kp * esz), bsz = rup1k((size_t)n * Kp * esz);
   char* Abuf = static_cast<char*>(ws);
-  char* Bbuf = Abuf + rup1k((size_t)m * Kp * esz);
-  char* Alo = split ? Bbuf + rup1k((size_t)n * Kp * esz) : nullptr;
-  char* Blo = split ? Alo + rup1k((size_t)m * Kp * esz) : nullptr;
+  char* Alo = split ? Abuf + asz : nullptr;
+  char* Bbuf = Abuf + (split ? 2 : 1) * asz;
+  char* Blo = split ? Bbuf + bsz : nullptr;
   // FP8 operand maxima (per call, i.e. per panel) after the packed operands
-  float* amax = reinterpret_cast<float*>(
-      Abuf + (split ? 2 : 1) * (rup1k((size_t)m * Kp * esz) + rup1k((size_t)n * Kp * esz)));
+  float* amax = reinterpret_cast<float*>(Abuf + (split ? 2 : 1) * (asz + bsz));
+  if (kind == kTcFP8) a_packed = false;  // its scale is taken over A and B per call
   dim3 pg((m + 31) / 32, (Kp + 31) / 32);
-  int nl = 2;
+  int nl = a_packed ? 1 : 2;
   if (kind == kTcFP8) {
     cudaError_t e0 = cudaMemsetAsync(amax, 0, 2 * sizeof(float), stream);
     if (e0 != cudaSuccess) return e0;
@@ -488,12 +491,14 @@ cudaError_t launch_tc_gemm_sub(int kind, int m, int n, int K, const float* A, lo
                                                                         Bbuf, nullptr, amax);
     nl = 3;
   } else if (kind == kTcBF16) {
-    pack_a_kernel<kTcBF16><<<pg, dim3(32, 8), 0, stream>>>(A, lda, m, K, Kp, Abuf, nullptr,
-                                                           amax);
+    if (!a_packed)
+      pack_a_kernel<kTcBF16><<<pg, dim3(32, 8), 0, stream>>>(A, lda, m, K, Kp, Abuf, nullptr,
+                                                             amax);
     pack_b_kernel<kTcBF16><<<dim3((Kp + 255) / 256, grid_y(n)), 256, 0, stream>>>(B, ldb, K, n, Kp,
                                                                          Bbuf, nullptr, amax);
   } else {
-    pack_a_kernel<kTcTF32><<<pg, dim3(32, 8), 0, stream>>>(A, lda, m, K, Kp, Abuf, Alo, amax);
+    if (!a_packed)
+      pack_a_kernel<kTcTF32><<<pg, dim3(32, 8), 0, stream>>>(A, lda, m, K, Kp, Abuf, Alo, amax);
     pack_b_kernel<kTcTF32><<<dim3((Kp + 255) / 256, grid_y(n)), 256, 0, stream>>>(B, ldb, K, n, Kp,
                                                                          Bbuf, Blo, amax);
   }

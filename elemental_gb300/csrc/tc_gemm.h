@@ -36,10 +36,13 @@ enum TcGridMode : int {
   kGridTiles = 3,     // one CTA per tile: SMs are released tile by tile
 };
 constexpr int kSmallGrid = 32;
+// a_packed: ws already holds A's packed words from an earlier call with the
+// same A, lda, m, K and kind, and nothing has changed them since (not for
+// FP8, whose scale covers A and B per call).
 cudaError_t launch_tc_gemm_sub(int kind, int m, int n, int K, const float* A, long lda,
                                const float* B, long ldb, float* C, long ldc, void* ws,
                                DevStatus* st, cudaStream_t stream, int* nlaunch,
                                cudaEvent_t ev0 = nullptr, cudaEvent_t ev1 = nullptr,
-                               int grid_mode = kGridFull);
+                               int grid_mode = kGridFull, bool a_packed = false);
 
 }  // namespace elgb
