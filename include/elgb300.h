@@ -525,9 +525,9 @@ int ElGBResidualDF_d(ElGBContext ctx, int n, int nrhs, const double* A,
  * with 16 right-hand sides, n <= 32768 with 4) and returns EL_ARG_ERROR (3)
  * beyond that, before touching any memory.  Runs on `stream` (a cudaStream_t,
  * NULL = legacy default stream) of the current device.  The first call on a
- * device looks up the array's device address (cudaGetSymbolAddress); make
- * that first call before any stream capture.  All calls share the array:
- * calls that overlap on the GPU race on it, calls on one stream do not. */
+ * device looks up the array's device address (cudaGetSymbolAddress).  All
+ * calls share the array: calls that overlap on the GPU race on it, calls on
+ * one stream do not. */
 int ElGBResidualNoAlloc_d(int n, int nrhs, const double* A, int lda,
                           const double* X, int ldx, const double* B, int ldb,
                           double* R, int ldr, void* stream);
