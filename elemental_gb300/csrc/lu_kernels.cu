@@ -15,7 +15,7 @@ namespace elgb {
 // Largest thread-block cluster the panel may use (1: the cooperative kernel
 // only); set by ElGBSetOption(ELGB_OPT_PANEL_CLUSTER).
 int g_panel_cluster = 16;
-int g_panel_rows = 1024;
+int g_panel_rows = 512;
 // FP32 panels with the rows in registers (ElGBSetOption(ELGB_OPT_PANEL_REGS)):
 // 1 cooperative, 2 on a cluster where one fits (the default).
 int g_panel_regs = 2;
@@ -1366,10 +1366,14 @@ static cudaError_t launch_getf2_panel_cluster_reg(float* A, long lda, int mp, in
   const bool narrow = w <= 16 && R > 2 * kRcThreads;  // 16 columns, 4 rows a thread
   if (R > (narrow ? 4 : 2) * kRcThreads) return cudaErrorNotSupported;
   const bool push = C <= 16 && (g_panel_push == 1 || (g_panel_push == 2 && !narrow));
+  // at most one row a thread: the one-row instance (half the step code, which
+  // is what the unrolled kernel waits on when fetching instructions)
+  const bool single = !narrow && R <= kRcThreads && push;
   auto kern = narrow ? (push ? getf2_panel_cluster_reg_kernel<16, 4, true>
                              : getf2_panel_cluster_reg_kernel<16, 4, false>)
-                     : (push ? getf2_panel_cluster_reg_kernel<kPanelW, 2, true>
-                             : getf2_panel_cluster_reg_kernel<kPanelW, 2, false>);
+              : single ? getf2_panel_cluster_reg_kernel<kPanelW, 1, true>
+                       : (push ? getf2_panel_cluster_reg_kernel<kPanelW, 2, true>
+                               : getf2_panel_cluster_reg_kernel<kPanelW, 2, false>);
   cudaError_t e = cudaSuccess;
   if (C > 8) e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   if (e != cudaSuccess) return e;
@@ -1386,11 +1390,11 @@ static cudaError_t launch_getf2_panel_cluster_reg(float* A, long lda, int mp, in
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   // whether a cluster of C fits, asked once per device, variant and C
-  static signed char fits[64][4][17] = {};
+  static signed char fits[64][5][17] = {};
   int dev = 0;
   cudaGetDevice(&dev);
   signed char* f = (dev >= 0 && dev < 64 && C <= 16)
-                       ? &fits[dev][(narrow ? 2 : 0) + (push ? 1 : 0)][C]
+                       ? &fits[dev][single ? 4 : (narrow ? 2 : 0) + (push ? 1 : 0)][C]
                        : nullptr;
   bool ok = f && *f > 0;
   if (!f || *f == 0) {

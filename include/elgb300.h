@@ -95,10 +95,12 @@ int ElGBSetBlocksize(int nb);
  *                       the panel's expected time scaled by value / 100
  *                       (1 means 110).
  *   ELGB_OPT_PANEL_ROWS  rows of a leaf panel per CTA that the panel kernels
- *                       aim for (64 .. 1536, default 1024): more CTAs make
+ *                       aim for (64 .. 1536, default 512): more CTAs make
  *                       each pivot step's local update shorter and its
- *                       exchange longer.  Process-wide, like
- *                       ELGB_OPT_PANEL_CLUSTER.
+ *                       exchange longer; at <= 512 rows a CTA the register
+ *                       kernel holds one row a thread (half the step code;
+ *                       LU 205.0 -> 202.2 ms at n = 32768 against 1024).
+ *                       Process-wide, like ELGB_OPT_PANEL_CLUSTER.
  *   ELGB_OPT_INV_TRSM   0 (default): the tensor-core LU's trailing
  *                       triangular solve U12 = L11^-1 A12 is a blocked
  *                       substitution; 1: one tensor-core product,

@@ -266,7 +266,7 @@ def case_panel_trace(ctx, a):
         ctx.set_option("lookahead", 1)
         ctx.set_option("trail_grid", 2)
         ctx.set_option("panel_cluster", 16)
-        ctx.set_option("panel_rows", 1024)
+        ctx.set_option("panel_rows", 512)
         ctx.set_option("panel_regs", 2)
         ctx.set_option("trail_split", 1)
         ctx.set_option("panel_push", 1)
@@ -361,7 +361,7 @@ def main(argv=None):
                    help="lu_breakdown, panel_trace: ELGB_OPT_TRAIL_GRID")
     p.add_argument("--panel-cluster", type=int, default=16,
                    help="panel_trace: ELGB_OPT_PANEL_CLUSTER (1 = cooperative leaf panels only)")
-    p.add_argument("--panel-rows", type=int, default=1024,
+    p.add_argument("--panel-rows", type=int, default=512,
                    help="panel_trace: ELGB_OPT_PANEL_ROWS")
     p.add_argument("--trail-split", type=int, default=1,
                    help="panel_trace: ELGB_OPT_TRAIL_SPLIT")
