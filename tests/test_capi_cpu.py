@@ -109,6 +109,18 @@ def test_host_alloc_argument_handling():
         assert not p.value
 
 
+def test_profile_and_option_entry_points_reject_a_null_context():
+    """The profiling and option entry points check their context before
+    touching anything (host logic only)."""
+    lib = _lib.load()
+    cnt = ctypes.c_int(-1)
+    assert lib.ElGBProfileStartTags(None, 1) == 3  # EL_ARG_ERROR
+    assert lib.ElGBProfileRecords(None, 0, ctypes.byref(cnt), None, None, None, None) == 3
+    assert cnt.value == -1
+    for opt in range(1, 18):
+        assert lib.ElGBSetOption(None, opt, 1) == 3
+
+
 def test_python_matrix_views_share_memory():
     """El.Matrix slicing gives views through ElView_d (the reference's
     Matrix.__getitem__, python/core/Matrix.py:456-482); a permutation applied
