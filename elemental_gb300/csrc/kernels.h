@@ -49,9 +49,11 @@ cudaError_t launch_calu_panel(float* A, long lda, int mp, int w, int* ipiv, int 
 // Largest thread-block cluster the panel kernel may use (1: the cooperative
 // kernel only); process-wide, ElGBSetOption(ELGB_OPT_PANEL_CLUSTER).
 extern int g_panel_cluster;
-// Rows per CTA the leaf-panel kernels aim for (ElGBSetOption(ELGB_OPT_PANEL_ROWS)).
+// Rows per CTA the leaf-panel kernels aim for (ElGBSetOption(ELGB_OPT_PANEL_ROWS),
+// default 512: the register kernel then holds one row a thread up to 8192 rows).
 extern int g_panel_rows;
-// FP32 panels with the rows in registers (1, default) or in shared memory.
+// FP32 panels with the rows in registers: 2 on one cluster (default), 1 on a
+// cooperative grid, 0 in shared memory.
 extern int g_panel_regs;
 // register leaf panels: candidates pushed into every CTA with asynchronous
 // DSMEM stores on an mbarrier (1) or read after a cluster barrier (0)

@@ -15,6 +15,7 @@ namespace elgb {
 // Largest thread-block cluster the panel may use (1: the cooperative kernel
 // only); set by ElGBSetOption(ELGB_OPT_PANEL_CLUSTER).
 int g_panel_cluster = 16;
+// Rows per CTA the leaf-panel kernels aim for (ElGBSetOption(ELGB_OPT_PANEL_ROWS)).
 int g_panel_rows = 512;
 // FP32 panels with the rows in registers (ElGBSetOption(ELGB_OPT_PANEL_REGS)):
 // 1 cooperative, 2 on a cluster where one fits (the default).
